@@ -1,0 +1,234 @@
+"""Benchmark: F+dF evaluations per second at 128^3 (the LJ droplet system:
+WhiteBearI FMT + QF mean field of the cut-and-shifted LJ, kT = 0.8, dx = 0.1),
+one JSON line on stdout.
+
+`value`  FP32-bulk evaluations/s with the density resident in HBM (FP64
+         reductions), timed with CUDA events per step; L2 flushed between steps.
+`e2e`    the same evaluation through the public C ABI from host buffers
+         (host density in, host dF out, copies inside the timed region).
+Extra keys: the FP64 rate, a per-pass breakdown with roofline fractions, the
+oracle CPU baseline. With --impl reference the FP64 CPU oracle (the port of the
+reference's path; the reference itself needs FFTW/GSL/Boost/Armadillo, absent
+on the GPU machines) is timed on all host cores.
+Multi-GPU: replicas only (each rank evaluates its own system); value is the sum.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FMT F+dF evals/s at 128^3; s to resid 1e-8: warm-start mixed vs plain FP64"
+SHAPE, DX, KT, R_DROP, W_DROP, RHO_V, RHO_L = (128, 128, 128), 0.1, 0.8, 4.0, 0.5, 0.01, 0.75
+
+
+def droplet():
+    ax = [DX * (np.arange(m) - m / 2.0) for m in SHAPE]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    r = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
+    return RHO_V + (RHO_L - RHO_V) * 0.5 * (1 - np.tanh((r - R_DROP) / W_DROP))
+
+
+def workload():
+    return {"workload": "LJ droplet F+dF evaluation, 128^3, dx=0.1, WhiteBearI + QF mean field, kT=0.8, "
+                        "rho_v=0.01, rho_l=0.75, R=4, w=0.5, grand canonical at mu(rho_v)",
+            "grid": list(SHAPE), "model": "WhiteBearI", "interaction": "QF", "precision_bulk": "fp32",
+            "reductions": "fp64 compensated", "l2": "flushed between timed steps (256 MB write)"}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs", 6800.0), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def __enter__(self):
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,"
+                                          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                                          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                    vals = [v.strip() for v in out.stdout.strip().split(",")]
+                    if len(vals) >= 6:
+                        self.samples.append(vals)
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
+        mx = max(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[2 + k].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def cpu_baseline(budget_s=15.0, steps=None):
+    from oracle import pyoracle
+    o = pyoracle.Oracle(SHAPE, DX, "WhiteBearI", hsd=None, lj=True, kT=KT)
+    o.set_mu(o.mu_times_beta(RHO_V))
+    rho = droplet()
+    o.eval(rho)  # warm-up (plans, threads)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.eval(rho)
+        n += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and n >= steps) or (steps is None and el > budget_s):
+            break
+    return n / el, n, el
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    steps = max(1, args.steps)
+    for _ in range(min(args.warmup, 1)):
+        pass
+    rate, n, el = cpu_baseline(steps=steps)
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": "evals/s", "n_gpus": args.gpus,
+            "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * el / n, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload(),
+            "cpu_baseline": {"value": rate, "unit": "evals/s", "cores": cores, "kind": "port",
+                             "sample": "%d FP64 F+dF evaluations of the 128^3 LJ droplet (OpenMP, %d threads)" % (n, cores)},
+            "e2e": {"value": rate, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import classicaldft_gb300 as cd
+
+    rho = droplet()
+    c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=None, lj=True, kT=KT, precision=cd.FP32)
+    c.set_chem_potential(c.bulk(RHO_V)["mu"])
+    c.set_density(rho)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(K, W, fn):
+        for _ in range(W):
+            fn()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        total = 0.0
+        for _ in range(K):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            total += a.elapsed_time(b)
+        torch.cuda.synchronize()
+        t = torch.tensor([total], device="cuda")
+        if dist:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return t.item() / K  # ms per step, max over ranks
+
+    with Clocks(local) as clk:
+        ms32 = timed(args.steps, max(3, args.warmup), lambda: c.eval(want_dF=False))
+    clocks = clk.summary()
+    passes = c.time_passes(reps=5)
+    c.set_precision(cd.FP64)
+    ms64 = timed(max(3, args.steps // 10), 3, lambda: c.eval(want_dF=False))
+    c.set_precision(cd.FP32)
+    # e2e through the public API: host density in, host dF out, every step
+    host_rho = rho.copy()
+    K2 = max(5, args.steps // 2)
+    for _ in range(3):
+        c.set_density(host_rho)
+        c.eval()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K2):
+        c.set_density(host_rho)
+        c.eval()
+    e2e_s = (time.perf_counter() - t0) / K2
+    n_per_eval = 14  # kernels per evaluation (9 passes + 3 reductions + 2 for the residual max)
+    peak, peak_kind = measured_peaks()
+    top = max(passes, key=lambda p: p["ms"])
+    achieved = top["bytes"] / (top["ms"] * 1e-3) / 1e9
+    N = np.prod(SHAPE)
+    Nc = SHAPE[0] * SHAPE[1] * (SHAPE[2] // 2 + 1)
+    B_dft = 4 * (N * (4 * 11 + 3) + Nc * (2 * 11 + 11))
+    line = {"metric": METRIC, "value": world * 1e3 / ms32, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload(),
+            "gpu_launches": n_per_eval * args.steps,
+            "e2e": {"value": world / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(N * 8),
+                    "d2h_bytes_per_step": int(N * 8 + 8 * 8)},
+            "roofline": {"bound": "hbm", "kernel": top["pass"], "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": None},
+            "eval_roofline": {"algorithmic_bytes_per_eval": B_dft, "achieved_gbs": B_dft / (ms32 * 1e-3) / 1e9,
+                              "frac": B_dft / (ms32 * 1e-3) / 1e9 / peak},
+            "fp64_evals_per_s": world * 1e3 / ms64, "fp64_ms_per_step": ms64,
+            "passes": [{"pass": p["pass"], "ms": round(p["ms"], 5), "GBs": round(p["bytes"] / max(p["ms"], 1e-9) / 1e6, 1)}
+                       for p in passes],
+            "clocks": clocks}
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, n, el = cpu_baseline()
+        line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": "%d FP64 F+dF evaluations of the same 128^3 system by the oracle in %.1f s" % (n, el)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

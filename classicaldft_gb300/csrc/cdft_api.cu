@@ -1,0 +1,939 @@
+// C ABI of the GB300 engine (include/cdft.h): context management, the F+dF
+// evaluation with the Species begin/end force constraints, bulk
+// thermodynamics, and the FIRE2 and DDFT drivers. The drivers keep the
+// reference's step logic on the host (scalars only) and run every N-sized
+// operation on the device, with fused FP64 compensated reductions.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+#include "../../include/cdft.h"
+#include "cdft_internal.h"
+#include "cdft_kernels.cuh"
+
+using namespace cdft;
+
+namespace {
+
+// ------------------------------------------------------- map-reduce ---
+// Each functor fills NS sums (compensated) and NM maxima for element i.
+template <int NS, int NM, class F>
+__global__ void __launch_bounds__(256) k_map_reduce(long n, F f, double* __restrict__ part) {
+  Acc acc[NS > 0 ? NS : 1];
+  double mx[NM > 0 ? NM : 1];
+  for (int v = 0; v < NS; ++v) acc[v].init();
+  for (int v = 0; v < NM; ++v) mx[v] = -INFINITY;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double s[NS > 0 ? NS : 1], m[NM > 0 ? NM : 1];
+    f(i, s, m);
+    for (int v = 0; v < NS; ++v) acc[v].add(s[v]);
+    for (int v = 0; v < NM; ++v) mx[v] = fmax(mx[v], m[v]);
+  }
+  constexpr int kNS = (NS > 0) ? NS : 1;
+  if (NS > 0) block_reduce_store<kNS>(acc, part, blockIdx.x);
+  // maxima: warp then block
+  __shared__ double red[32][NM > 0 ? NM : 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int v = 0; v < NM; ++v) {
+    for (int o = 16; o > 0; o >>= 1) mx[v] = fmax(mx[v], __shfl_down_sync(0xffffffffu, mx[v], o));
+    if (lane == 0) red[warp][v] = mx[v];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && NM > 0) {
+    double* pm = part + (long)gridDim.x * 2 * NS;
+    for (int v = 0; v < NM; ++v) {
+      double t = -INFINITY;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, red[w][v]);
+      pm[(long)blockIdx.x * NM + v] = t;
+    }
+  }
+}
+
+__global__ void k_finish_map_reduce(const double* __restrict__ part, int nblk, int ns, int nm, double* __restrict__ out) {
+  // deterministic single-block finish: sums in block order, maxima
+  if (threadIdx.x == 0) {
+    for (int v = 0; v < ns; ++v) {
+      Acc a;
+      a.init();
+      for (int b = 0; b < nblk; ++b) a.merge(part[(b * ns + v) * 2], part[(b * ns + v) * 2 + 1]);
+      out[v] = a.s + a.c;
+    }
+    const double* pm = part + (long)nblk * 2 * ns;
+    for (int v = 0; v < nm; ++v) {
+      double t = -INFINITY;
+      for (int b = 0; b < nblk; ++b) t = fmax(t, pm[b * nm + v]);
+      out[ns + v] = t;
+    }
+  }
+}
+
+struct FSumRho {
+  const double* r;
+  __device__ void operator()(long i, double* s, double*) const { s[0] = r[i]; }
+};
+struct FAbsMax {
+  const double* a;
+  __device__ void operator()(long i, double*, double* m) const { m[0] = fabs(a[i]); }
+};
+
+// FMT_Species alias maps (src/FMT_Species.cpp:29-93): rho = dmin + c y^2/(1+y^2).
+struct Alias {
+  double dmin, c;
+};
+__device__ __forceinline__ double alias_rho(const Alias& a, double y) { return a.dmin + a.c * y * y / (1 + y * y); }
+
+__global__ void k_alias_from_rho(const double* __restrict__ rho, double* __restrict__ x, long n, Alias a) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double z = (rho[i] - a.dmin) / a.c;
+    x[i] = sqrt(fabs(z / (1 - z)));
+  }
+}
+__global__ void k_rho_from_alias(const double* __restrict__ x, double* __restrict__ rho, long n, Alias a) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) rho[i] = alias_rho(a, x[i]);
+}
+__global__ void k_scale_vec(double* __restrict__ x, long n, double s) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) x[i] *= s;
+}
+__global__ void k_add_const(double* __restrict__ x, long n, double s) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) x[i] = x[i] - s;
+}
+
+// FIRE2 step, first half (fireMinimizer2::step uphill branch + SemiImplicitEuler
+// first line, src/Minimizer.cpp:198-217, 279-289): xo = x - dt/2 v (uphill),
+// vo = (0.1 v if uphill else v) - dt dF; sums |vo|^2, |dF|^2.
+struct FFirePre {
+  const double *x, *v, *dF;
+  double *xo, *vo;
+  double dt;
+  int uphill;
+  __device__ void operator()(long i, double* s, double*) const {
+    double xi = x[i], vi = v[i];
+    if (uphill) {
+      xi += vi * (-0.5 * dt);
+      vi *= 0.1;
+    }
+    const double g = dF[i];
+    vi += g * (-dt);
+    xo[i] = xi;
+    vo[i] = vi;
+    s[0] = vi * vi;
+    s[1] = g * g;
+  }
+};
+// Second half (src/Minimizer.cpp:292-297): v = (1-a) v - a c dF; x += dt v; rho = alias(x).
+__global__ void k_fire_mix(double* __restrict__ x, double* __restrict__ v, const double* __restrict__ dF, double* __restrict__ rho, long n,
+                           double dt, double alpha, double coef, Alias a) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double vi = v[i] * (1 - alpha);
+    vi += dF[i] * (-alpha * coef);
+    const double xi = x[i] + vi * dt;
+    v[i] = vi;
+    x[i] = xi;
+    rho[i] = alias_rho(a, xi);
+  }
+}
+// After an accepted evaluation (Minimizer::getDF_DX, src/Minimizer.cpp:90-115):
+// dF_alias = dF 2 c y/(1+y^2)^2; sums v.dF_alias; maxima |dF|, |dF_alias|.
+struct FFirePost {
+  const double *dF, *x, *v;
+  double* dFa;
+  double c;
+  __device__ void operator()(long i, double* s, double* m) const {
+    const double y = x[i], g = dF[i];
+    const double ga = g * (2 * c * y / ((1 + y * y) * (1 + y * y)));
+    dFa[i] = ga;
+    s[0] = v[i] * ga;
+    m[0] = fabs(g);
+    m[1] = fabs(ga);
+  }
+};
+
+// DDFT right-hand side (DDFT::calculate_excess_RHS, g_dot_x, subtract_ideal_gas;
+// src/DDFT.cpp:212-235, 320-351): R = g.dF / dV - Laplacian_h rho with
+// g.x = sum_axes D [(rho+ + rho0)(x+ - x0) - (rho0 + rho-)(x0 - x-)], D = 1/(2 dx^2).
+struct FDdftRhs {
+  const double *rho, *dF;
+  double* R;
+  int nx, ny, nz;
+  double dx, dV;
+  __device__ void operator()(long p, double*, double* m) const {
+    const int k = (int)(p % nz);
+    const long t = p / nz;
+    const int j = (int)(t % ny), i = (int)(t / ny);
+    auto at = [&](int a, int b, int c) -> long {
+      a = (a + nx) % nx; b = (b + ny) % ny; c = (c + nz) % nz;
+      return c + (long)nz * (b + (long)ny * a);
+    };
+    const long px = at(i + 1, j, k), mx = at(i - 1, j, k), py = at(i, j + 1, k), my = at(i, j - 1, k), pz = at(i, j, k + 1), mz = at(i, j, k - 1);
+    const double D = 1.0 / (2 * dx * dx);
+    const double x0 = dF[p], d0 = rho[p];
+    double g = D * ((rho[px] + d0) * (dF[px] - x0) - (d0 + rho[mx]) * (x0 - dF[mx]));
+    g += D * ((rho[py] + d0) * (dF[py] - x0) - (d0 + rho[my]) * (x0 - dF[my]));
+    g += D * ((rho[pz] + d0) * (dF[pz] - x0) - (d0 + rho[mz]) * (x0 - dF[mz]));
+    g *= 1.0 / dV;
+    m[0] = fabs(g);
+    const double L = 1.0 / (dx * dx);
+    R[p] = g + (-L * (rho[px] + rho[mx] - 2 * d0) - L * (rho[py] + rho[my] - 2 * d0) - L * (rho[pz] + rho[mz] - 2 * d0));
+  }
+};
+// DDFT::apply_diffusion_propogator k-space update (src/DDFT.cpp:239-273):
+// work = U0 rho0~ + U1 R0~ + U2 (R1~ - R0~), U0 = e^{L dt}, U1 = (e^{L dt}-1)/L,
+// U2 = (e^{L dt}-1-L dt)/(L^2 dt); at k = 0: U1 = dt, U2 = dt/2.
+template <class T>
+__global__ void k_ddft_prop(const typename Cx<T>::type* __restrict__ rk, const typename Cx<T>::type* __restrict__ R0,
+                            const typename Cx<T>::type* __restrict__ R1, typename Cx<T>::type* __restrict__ out,
+                            const double* __restrict__ fac, int nx, int ny, int nzc, double dt) {
+  const long Nc = (long)nx * ny * nzc;
+  const double* Lx = fac;
+  const double* Ly = Lx + nx;
+  const double* Lz = Ly + ny;
+  const double* fx = Lz + nzc;
+  const double* fy = fx + nx;
+  const double* fz = fy + ny;
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Nc; p += (long)gridDim.x * blockDim.x) {
+    const int iz = (int)(p % nzc);
+    const long t = p / nzc;
+    const int iy = (int)(t % ny), ix = (int)(t / ny);
+    const double Lam = Lx[ix] + Ly[iy] + Lz[iz];
+    const double e = fx[ix] * fy[iy] * fz[iz];
+    const double U0 = e;
+    const double U1 = (p == 0 ? dt : (e - 1) / Lam);
+    const double U2 = (p == 0 ? dt / 2 : (e - 1 - dt * Lam) / (Lam * Lam * dt));
+    const typename Cx<T>::type x = rk[p], a = R0[p], b = R1[p];
+    out[p] = mk<T>((T)(U0 * (double)x.x + U1 * (double)a.x + U2 * ((double)b.x - (double)a.x)),
+                   (T)(U0 * (double)x.y + U1 * (double)a.y + U2 * ((double)b.y - (double)a.y)));
+  }
+}
+struct FDdftDev {
+  const double *d1, *dn;
+  __device__ void operator()(long i, double*, double* m) const {
+    m[0] = fabs(d1[i] - dn[i]);
+    m[1] = -dn[i];  // max(-x) = -min(x)
+  }
+};
+
+unsigned grid_for(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + 255) / 256, 152 * 8)); }
+
+}  // namespace
+
+// ------------------------------------------------------------- context ---
+struct cdft_ctx {
+  cdft_params p{};
+  cdft_info info{};
+  std::string err;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::shared_ptr<FFTTable> tx, ty, tz;
+  std::unique_ptr<Evaluator<double>> e64;
+  std::unique_ptr<Evaluator<float>> e32;
+  int precision = CDFT_FP64;
+  double mu = 0, fixed_mass = -1;
+  double* rho = nullptr;
+  double* dF = nullptr;
+  double* vext = nullptr;
+  double* red_part = nullptr;  // map-reduce partials
+  double* red_out = nullptr;   // finished values
+  double* host_out = nullptr;  // pinned copy of red_out
+  // FIRE state (fireMinimizer2 members)
+  bool fire_ready = false;
+  cdft_fire_params fp{};
+  double* fx[2] = {nullptr, nullptr};
+  double* fv[2] = {nullptr, nullptr};
+  double* fg[2] = {nullptr, nullptr};
+  int cur = 0;
+  double F = 0, dt = 0, dt_max = 0, alpha = 0, vv = 1, dt_best = 0, fmax = -1, resid = 0, vdotf = 0;
+  int Npos = 0, Nneg = 0, backtracks = 0;
+  unsigned it = 0;
+  long fire_steps = 0, calls = 0;
+  // DDFT state
+  bool ddft_ready = false;
+  double ddft_dt = 0, ddft_dt_max = 1, ddft_tol = 1e-4, ddft_time = 0, ddft_rhs = 1;
+  bool ddft_have_factors = false;
+  int ddft_successes = 0;
+  double *dd0 = nullptr, *dd1 = nullptr, *ddn = nullptr, *dR = nullptr, *dfac = nullptr;
+  void *rk0 = nullptr, *R0k = nullptr, *R1k = nullptr, *work = nullptr;
+  std::vector<double> Lx, Ly, Lz;
+
+  Alias alias() const {
+    Alias a;
+    a.dmin = 1e-18;  // SMALL_VALUE (include/Density.h:24)
+    const double etamin = a.dmin * (4 * M_PI * info.hsd * info.hsd * info.hsd / 3);
+    a.c = (1.0 - etamin) / info.dV;
+    return a;
+  }
+};
+
+static int fail(cdft_ctx* c, int code, const std::string& m) {
+  if (c) c->err = m;
+  return code;
+}
+#define CUDA_OR_FAIL(c, x)                                                                  \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess) return fail(c, CDFT_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+static int ensure_evaluator(cdft_ctx* c, int precision) {
+  const int nx = c->p.nx, ny = c->p.ny, nz = c->p.nz;
+  if ((precision == CDFT_FP64 && c->e64) || (precision == CDFT_FP32 && c->e32)) return CDFT_OK;
+  std::vector<double> w[11], watt;
+  const bool fmt = c->p.model >= 0;
+  try {
+    if (fmt) fmt_weights_real(nx, ny, nz, c->p.dx, c->info.hsd, w);
+    if (c->p.lj) {
+      double a;
+      qf_kernel_real(nx, ny, nz, c->p.dx, c->p.lj_sigma, c->p.lj_eps, c->p.lj_rc, c->p.kT, watt, a);
+    }
+  } catch (std::exception& e) {
+    return fail(c, CDFT_ERR_ARG, e.what());
+  }
+  std::string err;
+  int rc;
+  if (precision == CDFT_FP64) {
+    c->e64.reset(new Evaluator<double>());
+    rc = c->e64->init(nx, ny, nz, c->p.model, c->info.hsd, c->p.es_A, c->p.es_B, fmt ? w : nullptr, c->p.lj ? &watt : nullptr, c->tx.get(),
+                      c->ty.get(), c->tz.get(), c->stream, &err);
+    if (rc) c->e64.reset();
+  } else {
+    c->e32.reset(new Evaluator<float>());
+    rc = c->e32->init(nx, ny, nz, c->p.model, c->info.hsd, c->p.es_A, c->p.es_B, fmt ? w : nullptr, c->p.lj ? &watt : nullptr, c->tx.get(),
+                      c->ty.get(), c->tz.get(), c->stream, &err);
+    if (rc) c->e32.reset();
+  }
+  if (rc) return fail(c, rc, err);
+  return CDFT_OK;
+}
+
+template <int NS, int NM, class F>
+static int map_reduce(cdft_ctx* c, long n, F f, double* host_out) {
+  const unsigned g = grid_for(n);
+  k_map_reduce<NS, NM, F><<<g, 256, 0, c->stream>>>(n, f, c->red_part);
+  k_finish_map_reduce<<<1, 32, 0, c->stream>>>(c->red_part, (int)g, NS, NM, c->red_out);
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->host_out, c->red_out, (NS + NM) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  std::memcpy(host_out, c->host_out, (NS + NM) * sizeof(double));
+  return CDFT_OK;
+}
+
+// One evaluation on the context's density: Species::beginForceCalculation,
+// DFT::calculateFreeEnergyAndDerivatives_internal_, Species::endForceCalculation.
+static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
+  const long N = c->info.N;
+  const double dV = c->info.dV;
+  int rc = ensure_evaluator(c, c->precision);
+  if (rc) return rc;
+  if (c->fixed_mass > 0) {  // src/Species.cpp:64-71
+    double s;
+    rc = map_reduce<1, 0>(c, N, FSumRho{c->rho}, &s);
+    if (rc) return rc;
+    k_scale_vec<<<grid_for(N), 256, 0, c->stream>>>(c->rho, N, c->fixed_mass / (s * dV));
+    c->mu = 0.0;
+  }
+  EvalTerms t;
+  if (c->precision == CDFT_FP64) rc = c->e64->eval(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, &t, c->stream);
+  else rc = c->e32->eval(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, &t, c->stream);
+  if (rc) return fail(c, CDFT_ERR_CUDA, std::string("evaluation launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+  if (c->fixed_mass > 0) {  // src/Species.cpp:97-109
+    c->mu = t.sum_dF_rho / c->fixed_mass;
+    k_add_const<<<grid_for(N), 256, 0, c->stream>>>(c->dF, N, c->mu * dV);
+  }
+  double mx;
+  rc = map_reduce<0, 1>(c, N, FAbsMax{c->dF}, &mx);
+  if (rc) return rc;
+  if (terms8) {
+    terms8[0] = t.Omega;
+    terms8[1] = t.F_id;
+    terms8[2] = t.F_hs;
+    terms8[3] = t.F_mf;
+    terms8[4] = t.F_ext;
+    terms8[5] = c->mu;
+    terms8[6] = mx / dV;
+    terms8[7] = t.sum_rho * dV;
+  }
+  if (t.status & 1u) return fail(c, CDFT_ERR_ETA, "Eta too large in FMT::dPHI");
+  return CDFT_OK;
+}
+
+extern "C" {
+
+int cdft_create(const cdft_params* p, cdft_ctx** out) {
+  if (!p || !out) return CDFT_ERR_ARG;
+  *out = nullptr;
+  std::unique_ptr<cdft_ctx> c(new cdft_ctx());
+  c->p = *p;
+  if (p->nx < 2 || p->ny < 2 || p->nz < 2 || !(p->dx > 0)) return fail(nullptr, CDFT_ERR_ARG, "bad lattice");
+  if (p->precision != CDFT_FP64 && p->precision != CDFT_FP32) return CDFT_ERR_ARG;
+  if (p->model < -1 || p->model > 4) return CDFT_ERR_ARG;
+  cudaGetDevice(&c->device);
+  c->stream = nullptr;
+  c->precision = p->precision;
+  c->mu = p->mu;
+  c->fixed_mass = p->fixed_mass;
+  if (p->fixed_mass > 0) c->mu = 0.0;
+  c->info.nx = p->nx; c->info.ny = p->ny; c->info.nz = p->nz;
+  c->info.N = (long)p->nx * p->ny * p->nz;
+  c->info.Nc = (long)p->nx * p->ny * (p->nz / 2 + 1);
+  c->info.dV = p->dx * p->dx * p->dx;
+  c->info.volume = c->info.N * c->info.dV;
+  c->info.hsd = p->hsd;
+  if (p->lj && p->hsd <= 0) c->info.hsd = bh_diameter_lj(p->lj_sigma, p->lj_eps, p->lj_rc, p->kT);
+  if (p->model >= 0 && !(c->info.hsd >= p->dx)) return CDFT_ERR_ARG;  // generateWeights throws for hsd < dx
+  if (p->lj) {
+    std::vector<double> w;
+    double a;
+    qf_kernel_real(2, 2, 2, p->dx, p->lj_sigma, p->lj_eps, p->lj_rc, p->kT, w, a);  // a_vdw does not depend on the box
+    c->info.a_vdw = a;
+  }
+  std::string err;
+  c->tx = make_fft_table(p->nx, &err);
+  c->ty = (p->ny == p->nx) ? c->tx : make_fft_table(p->ny, &err);
+  c->tz = (p->nz == p->nx) ? c->tx : (p->nz == p->ny ? c->ty : make_fft_table(p->nz, &err));
+  if (!c->tx || !c->ty || !c->tz) return CDFT_ERR_ARG;
+  const long N = c->info.N;
+  if (cudaMalloc(&c->rho, N * sizeof(double)) != cudaSuccess || cudaMalloc(&c->dF, N * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->red_part, (size_t)152 * 8 * 16 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->red_out, 16 * sizeof(double)) != cudaSuccess || cudaMallocHost(&c->host_out, 16 * sizeof(double)) != cudaSuccess)
+    return CDFT_ERR_CUDA;
+  cudaMemset(c->rho, 0, N * sizeof(double));
+  cudaMemset(c->dF, 0, N * sizeof(double));
+  int rc = ensure_evaluator(c.get(), c->precision);
+  if (rc) return rc;
+  *out = c.release();
+  return CDFT_OK;
+}
+
+int cdft_destroy(cdft_ctx* c) {
+  if (!c) return CDFT_OK;
+  cudaStreamSynchronize(c->stream);
+  c->e64.reset();
+  c->e32.reset();
+  cudaFree(c->rho); cudaFree(c->dF); cudaFree(c->vext); cudaFree(c->red_part); cudaFree(c->red_out); cudaFreeHost(c->host_out);
+  for (int i = 0; i < 2; ++i) { cudaFree(c->fx[i]); cudaFree(c->fv[i]); cudaFree(c->fg[i]); }
+  cudaFree(c->dd0); cudaFree(c->dd1); cudaFree(c->ddn); cudaFree(c->dR); cudaFree(c->dfac);
+  cudaFree(c->rk0); cudaFree(c->R0k); cudaFree(c->R1k); cudaFree(c->work);
+  delete c;
+  return CDFT_OK;
+}
+
+const char* cdft_last_error(const cdft_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+int cdft_set_stream(cdft_ctx* c, void* s) {
+  if (!c) return CDFT_ERR_ARG;
+  cudaStreamSynchronize(c->stream);
+  c->stream = (cudaStream_t)s;
+  return CDFT_OK;
+}
+
+int cdft_get_info(const cdft_ctx* c, cdft_info* out) {
+  if (!c || !out) return CDFT_ERR_ARG;
+  *out = c->info;
+  return CDFT_OK;
+}
+
+int cdft_set_precision(cdft_ctx* c, int precision) {
+  if (!c || (precision != CDFT_FP64 && precision != CDFT_FP32)) return CDFT_ERR_ARG;
+  int rc = ensure_evaluator(c, precision);
+  if (rc) return rc;
+  c->precision = precision;
+  return CDFT_OK;
+}
+
+int cdft_set_density(cdft_ctx* c, const double* rho, int on_device) {
+  if (!c || !rho) return CDFT_ERR_ARG;
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rho, rho, c->info.N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return CDFT_OK;
+}
+
+int cdft_get_density(const cdft_ctx* c, double* rho, int on_device) {
+  if (!c || !rho) return CDFT_ERR_ARG;
+  if (cudaMemcpyAsync(rho, c->rho, c->info.N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream) !=
+      cudaSuccess)
+    return CDFT_ERR_CUDA;
+  return cudaStreamSynchronize(c->stream) == cudaSuccess ? CDFT_OK : CDFT_ERR_CUDA;
+}
+
+int cdft_set_external_field(cdft_ctx* c, const double* v, int on_device) {
+  if (!c) return CDFT_ERR_ARG;
+  if (!v) {
+    cudaFree(c->vext);
+    c->vext = nullptr;
+    return CDFT_OK;
+  }
+  if (!c->vext) CUDA_OR_FAIL(c, cudaMalloc(&c->vext, c->info.N * sizeof(double)));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->vext, v, c->info.N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return CDFT_OK;
+}
+
+int cdft_set_chem_potential(cdft_ctx* c, double mu) {
+  if (!c) return CDFT_ERR_ARG;
+  c->mu = mu;
+  c->fixed_mass = -1;
+  return CDFT_OK;
+}
+int cdft_set_fixed_mass(cdft_ctx* c, double m) {
+  if (!c) return CDFT_ERR_ARG;
+  c->fixed_mass = m;
+  if (m > 0.0) c->mu = 0.0;
+  return CDFT_OK;
+}
+int cdft_get_chem_potential(const cdft_ctx* c, double* mu) {
+  if (!c || !mu) return CDFT_ERR_ARG;
+  *mu = c->mu;
+  return CDFT_OK;
+}
+
+int cdft_eval(cdft_ctx* c, int only_fex, double* terms, double* dF, int on_device) {
+  if (!c) return CDFT_ERR_ARG;
+  int rc = eval_internal(c, terms, only_fex);
+  if (dF && (rc == CDFT_OK || rc == CDFT_ERR_ETA)) {
+    if (cudaMemcpyAsync(dF, c->dF, c->info.N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+      return fail(c, CDFT_ERR_CUDA, "copy of dF failed");
+  }
+  return rc;
+}
+
+int cdft_time_passes(cdft_ctx* c, int reps, double* ms, double* bytes, int* npass) {
+  if (!c || reps < 1) return CDFT_ERR_ARG;
+  int rc = ensure_evaluator(c, c->precision);
+  if (rc) return rc;
+  cudaEvent_t ev[CDFT_NPASS + 1];
+  for (auto& e : ev) cudaEventCreate(&e);
+  std::vector<double> acc(CDFT_NPASS, 0.0);
+  for (int r = 0; r < reps; ++r) {
+    if (c->precision == CDFT_FP64) c->e64->launch(c->rho, c->vext, c->dF, c->info.dV, c->mu, 1, c->stream, ev);
+    else c->e32->launch(c->rho, c->vext, c->dF, c->info.dV, c->mu, 1, c->stream, ev);
+    CUDA_OR_FAIL(c, cudaEventSynchronize(ev[CDFT_NPASS]));
+    for (int i = 0; i < CDFT_NPASS; ++i) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+      acc[i] += t;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (ms)
+    for (int i = 0; i < CDFT_NPASS; ++i) ms[i] = acc[i] / reps;
+  if (bytes) {
+    if (c->precision == CDFT_FP64) c->e64->pass_bytes(bytes);
+    else c->e32->pass_bytes(bytes);
+  }
+  if (npass) *npass = CDFT_NPASS;
+  return CDFT_OK;
+}
+
+int cdft_bulk(const cdft_ctx* c, double rho, double* out3) {
+  if (!c || !out3 || !(rho > 0)) return CDFT_ERR_ARG;
+  const int m = c->p.model;
+  // DFT::mu_times_beta: compensated sum of ln rho, FMT BulkMuex, interaction Mu (src/DFT.cpp:58-71)
+  double s = 0, cc = 0;
+  auto add = [&](double v) {
+    double t = s + v;
+    if (std::fabs(s) >= std::fabs(v)) cc += (s - t) + v;
+    else cc += (v - t) + s;
+    s = t;
+  };
+  add(std::log(rho));
+  if (m >= 0) add(bulk_muex(m, c->p.es_A, c->p.es_B, c->info.hsd, rho));
+  if (c->p.lj) add(0.5 * c->info.a_vdw * rho + 0.5 * c->info.a_vdw * rho);
+  const double mu = s + cc;
+  double F = rho * std::log(rho) - rho;  // fhelmholtz_times_beta_over_volume (src/DFT.cpp:90-115)
+  if (m >= 0) F += bulk_fex(m, c->p.es_A, c->p.es_B, c->info.hsd, rho);
+  if (c->p.lj) F += 0.5 * c->info.a_vdw * rho * rho;
+  out3[0] = mu;
+  out3[1] = F - rho * mu;
+  out3[2] = F;
+  return CDFT_OK;
+}
+
+int cdft_bh_diameter(double sigma, double eps, double rc, double kT, double* out) {
+  if (!out || !(kT > 0) || !(rc > 0)) return CDFT_ERR_ARG;
+  *out = bh_diameter_lj(sigma, eps, rc, kT);
+  return CDFT_OK;
+}
+
+int cdft_get_weights(const cdft_ctx* c, double* w11, double* w_att) {
+  if (!c) return CDFT_ERR_ARG;
+  const long N = c->info.N;
+  try {
+    if (w11 && c->p.model >= 0) {
+      std::vector<double> w[11];
+      fmt_weights_real(c->p.nx, c->p.ny, c->p.nz, c->p.dx, c->info.hsd, w);
+      for (int a = 0; a < 11; ++a) std::memcpy(w11 + a * N, w[a].data(), N * sizeof(double));
+    }
+    if (w_att && c->p.lj) {
+      std::vector<double> w;
+      double a;
+      qf_kernel_real(c->p.nx, c->p.ny, c->p.nz, c->p.dx, c->p.lj_sigma, c->p.lj_eps, c->p.lj_rc, c->p.kT, w, a);
+      std::memcpy(w_att, w.data(), N * sizeof(double));
+    }
+  } catch (std::exception&) {
+    return CDFT_ERR_ARG;
+  }
+  return CDFT_OK;
+}
+
+// ------------------------------------------------------------------ FIRE ---
+int cdft_fire_default_params(cdft_fire_params* p) {
+  if (!p) return CDFT_ERR_ARG;
+  // fireMinimizer2 constructor defaults (src/Minimizer.cpp:117-147), Minimizer forceLimit_ (:18)
+  p->dt = 1e-3;
+  p->dt_max = 1e-2;
+  p->dt_min = 0.0;
+  p->alpha_start = 0.1;
+  p->f_alf = 0.99;
+  p->f_dec = 0.5;
+  p->f_inc = 1.1;
+  p->force_limit = 0.1;
+  p->n_delay = 5;
+  p->n_p_negative_max = 20;
+  p->initial_delay = 1;
+  return CDFT_OK;
+}
+
+// Minimizer::getDF_DX on the pending alias state xs, vs (device): density from
+// alias (already in c->rho), evaluate, convert dF to alias derivative into gs.
+static int fire_accept(cdft_ctx* c, int s_idx) {
+  double red[3];
+  FFirePost f{c->dF, c->fx[s_idx], c->fv[s_idx], c->fg[s_idx], c->alias().c};
+  int rc = map_reduce<1, 2>(c, c->info.N, f, red);
+  if (rc) return rc;
+  c->vdotf = red[0];
+  c->resid = red[1] / c->info.dV;
+  c->fmax = red[2] / c->info.dV;
+  return CDFT_OK;
+}
+
+int cdft_fire_init(cdft_ctx* c, const cdft_fire_params* p) {
+  if (!c) return CDFT_ERR_ARG;
+  cdft_fire_params d;
+  cdft_fire_default_params(&d);
+  c->fp = p ? *p : d;
+  const long N = c->info.N;
+  for (int i = 0; i < 2; ++i) {
+    if (!c->fx[i]) CUDA_OR_FAIL(c, cudaMalloc(&c->fx[i], N * sizeof(double)));
+    if (!c->fv[i]) CUDA_OR_FAIL(c, cudaMalloc(&c->fv[i], N * sizeof(double)));
+    if (!c->fg[i]) CUDA_OR_FAIL(c, cudaMalloc(&c->fg[i], N * sizeof(double)));
+  }
+  c->cur = 0;
+  const Alias a = c->alias();
+  // Minimizer::Minimizer: x = alias(rho); fireMinimizer2: F = getDF_DX(), v = 0
+  k_alias_from_rho<<<grid_for(N), 256, 0, c->stream>>>(c->rho, c->fx[0], N, a);
+  k_rho_from_alias<<<grid_for(N), 256, 0, c->stream>>>(c->fx[0], c->rho, N, a);
+  CUDA_OR_FAIL(c, cudaMemsetAsync(c->fv[0], 0, N * sizeof(double), c->stream));
+  double t[8];
+  int rc = eval_internal(c, t);
+  if (rc) return rc;
+  c->calls = 1;
+  c->F = t[0];
+  rc = fire_accept(c, 0);
+  if (rc) return rc;
+  c->dt = c->fp.dt;
+  c->dt_max = c->fp.dt_max;
+  c->alpha = c->fp.alpha_start;
+  c->vv = 1.0;
+  c->dt_best = 1e-3;  // dt_best_ = the constructor's dt_ before setTimeStep
+  c->Npos = c->Nneg = c->backtracks = 0;
+  c->it = 0;
+  c->fire_steps = 0;
+  c->fire_ready = true;
+  return CDFT_OK;
+}
+
+// fireMinimizer2::step (src/Minimizer.cpp:160-271).
+static int fire_one_step(cdft_ctx* c, int* backtracked) {
+  const long N = c->info.N;
+  const cdft_fire_params& fp = c->fp;
+  c->it++;
+  const double P = -c->vdotf;
+  const double fold = c->F;
+  bool uphill = false;
+  if (P > 0) {
+    c->Npos++;
+    c->Nneg = 0;
+    if (c->Npos > fp.n_delay) {
+      c->dt = std::min(c->dt * fp.f_inc, c->dt_max);
+      c->alpha = c->alpha * fp.f_alf;
+    }
+  } else {
+    c->Npos = 0;
+    c->Nneg++;
+    if (c->Nneg > fp.n_p_negative_max) return fail(c, CDFT_ERR_UPHILL, "Cannot stop going uphill in Fire2");
+    if (!(fp.initial_delay && c->it < (unsigned)fp.n_delay)) {
+      if (c->dt * fp.f_dec >= fp.dt_min) c->dt *= fp.f_dec;
+      c->alpha = fp.alpha_start;
+    }
+    uphill = true;
+    c->backtracks++;
+  }
+  const int s = c->cur, n = 1 - c->cur;
+  double red[2];
+  FFirePre pre{c->fx[s], c->fv[s], c->fg[s], c->fx[n], c->fv[n], c->dt, uphill ? 1 : 0};
+  int rc = map_reduce<2, 0>(c, N, pre, red);
+  if (rc) return rc;
+  const double nv = std::sqrt(red[0]), nf = std::sqrt(red[1]);
+  const double vnorm = nv * nv, fnorm = nf * nf;
+  k_fire_mix<<<grid_for(N), 256, 0, c->stream>>>(c->fx[n], c->fv[n], c->fg[s], c->rho, N, c->dt, c->alpha, std::sqrt(vnorm / fnorm), c->alias());
+  double t[8];
+  rc = eval_internal(c, t);
+  c->calls++;
+  if (rc == CDFT_ERR_ETA) {
+    // restore x, v (x0.5), dF; halve dt (src/Minimizer.cpp:233-245)
+    k_scale_vec<<<grid_for(N), 256, 0, c->stream>>>(c->fv[s], N, 0.5);
+    c->vdotf *= 0.5;
+    c->dt /= 2;
+    c->fmax = 1000;
+    c->backtracks++;
+    if (backtracked) *backtracked = 1;
+  } else if (rc) {
+    return rc;
+  } else {
+    c->F = t[0];
+    rc = fire_accept(c, n);
+    if (rc) return rc;
+    c->cur = n;
+    c->vv = c->vv * 0.9 + 0.1 * (std::fabs(c->F - fold) / c->dt);
+    c->dt_best = std::max(c->dt, c->dt_best);
+  }
+  if (c->backtracks >= 10) {
+    c->dt_max = std::min(c->dt_best, 0.9 * c->dt_max);
+    c->dt_best = 0;
+    c->backtracks = 0;
+  }
+  c->fire_steps++;
+  return CDFT_OK;
+}
+
+static void fire_report(const cdft_ctx* c, long steps, int bt, int stop, cdft_fire_report* r) {
+  if (!r) return;
+  r->steps = steps;
+  r->total_steps = c->fire_steps;
+  r->calls = c->calls;
+  r->F = c->F;
+  r->dt = c->dt;
+  r->dt_max = c->dt_max;
+  r->alpha = c->alpha;
+  r->vv = c->vv;
+  r->fmax = c->fmax;
+  r->resid = c->resid;
+  r->backtracks = bt;
+  r->stop = stop;
+}
+
+static int fire_loop(cdft_ctx* c, long max_steps, double resid_tol, bool use_monitor, cdft_fire_report* rep) {
+  if (!c) return CDFT_ERR_ARG;
+  if (!c->fire_ready) return fail(c, CDFT_ERR_STATE, "cdft_fire_init has not been called");
+  long k = 0;
+  int bt = 0, stop = 0;
+  while (true) {
+    int b = 0;
+    int rc = fire_one_step(c, &b);
+    bt += b;
+    if (rc) {
+      fire_report(c, k, bt, stop, rep);
+      return rc;
+    }
+    ++k;
+    if (use_monitor && std::fabs(c->vv / c->info.volume) < c->fp.force_limit) { stop = 1; break; }
+    if (!use_monitor && c->resid <= resid_tol && c->fmax < 1000) { stop = 2; break; }
+    if (max_steps > 0 && k >= max_steps) break;
+  }
+  fire_report(c, k, bt, stop, rep);
+  return CDFT_OK;
+}
+
+int cdft_fire_step(cdft_ctx* c, int nsteps, cdft_fire_report* rep) {
+  if (!c) return CDFT_ERR_ARG;
+  if (!c->fire_ready) return fail(c, CDFT_ERR_STATE, "cdft_fire_init has not been called");
+  int bt = 0;
+  for (int k = 0; k < nsteps; ++k) {
+    int b = 0;
+    int rc = fire_one_step(c, &b);
+    bt += b;
+    if (rc) {
+      fire_report(c, k, bt, 0, rep);
+      return rc;
+    }
+  }
+  fire_report(c, nsteps, bt, 0, rep);
+  return CDFT_OK;
+}
+
+int cdft_fire_run(cdft_ctx* c, long max_steps, cdft_fire_report* rep) { return fire_loop(c, max_steps, 0.0, true, rep); }
+int cdft_fire_run_to_residual(cdft_ctx* c, double resid_tol, long max_steps, cdft_fire_report* rep) {
+  return fire_loop(c, max_steps, resid_tol, false, rep);
+}
+
+// ------------------------------------------------------------------ DDFT ---
+static int ddft_r2c(cdft_ctx* c, const double* real, void* spec) {
+  if (c->precision == CDFT_FP64) c->e64->r2c(real, reinterpret_cast<double2*>(spec), c->stream);
+  else c->e32->r2c(real, reinterpret_cast<float2*>(spec), c->stream);
+  return CDFT_OK;
+}
+
+int cdft_ddft_init(cdft_ctx* c, double dt, double dt_max, double tol) {
+  if (!c) return CDFT_ERR_ARG;
+  if (c->p.model < 0 && !c->p.lj) return fail(c, CDFT_ERR_ARG, "DDFT needs an FMT model or an interaction");
+  const long N = c->info.N, Nc = c->info.Nc;
+  const size_t cs = sizeof(double2);  // large enough for either precision
+  if (!c->dd0) {
+    CUDA_OR_FAIL(c, cudaMalloc(&c->dd0, N * sizeof(double)));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->dd1, N * sizeof(double)));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->ddn, N * sizeof(double)));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->dR, N * sizeof(double)));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->rk0, Nc * cs));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->R0k, Nc * cs));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->R1k, Nc * cs));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->work, Nc * cs));
+    CUDA_OR_FAIL(c, cudaMalloc(&c->dfac, 2 * (c->p.nx + c->p.ny + c->p.nz) * sizeof(double)));
+  }
+  const int nx = c->p.nx, ny = c->p.ny, nz = c->p.nz, nzc = nz / 2 + 1;
+  const double D = 1.0 / (c->p.dx * c->p.dx);
+  c->Lx.resize(nx); c->Ly.resize(ny); c->Lz.resize(nzc);
+  for (int i = 0; i < nx; i++) c->Lx[i] = 2 * D * (std::cos((2 * M_PI * i) / nx) - 1);  // DDFT::DDFT, src/DDFT.cpp:66-92
+  for (int i = 0; i < ny; i++) c->Ly[i] = 2 * D * (std::cos((2 * M_PI * i) / ny) - 1);
+  for (int i = 0; i < nzc; i++) c->Lz[i] = 2 * D * (std::cos((2 * M_PI * i) / nz) - 1);
+  double t[8];
+  int rc = eval_internal(c, t);  // the constructor's evaluation (src/DDFT.cpp:52)
+  if (rc) return rc;
+  c->ddft_dt = dt;
+  c->ddft_dt_max = dt_max;
+  c->ddft_tol = tol;
+  c->ddft_time = 0;
+  c->ddft_successes = 0;
+  c->ddft_have_factors = false;
+  c->ddft_ready = true;
+  return CDFT_OK;
+}
+
+// DDFT::change_timestep (src/DDFT.cpp:194-215), with its early return.
+static void ddft_change_timestep(cdft_ctx* c, double ndt) {
+  if (std::fabs(c->ddft_dt - ndt) < 1e-10) return;
+  c->ddft_dt = ndt;
+  const int nx = c->p.nx, ny = c->p.ny, nzc = c->p.nz / 2 + 1;
+  std::vector<double> h;
+  h.insert(h.end(), c->Lx.begin(), c->Lx.end());
+  h.insert(h.end(), c->Ly.begin(), c->Ly.end());
+  h.insert(h.end(), c->Lz.begin(), c->Lz.end());
+  for (int i = 0; i < nx; i++) h.push_back(std::exp(c->Lx[i] * ndt));
+  for (int i = 0; i < ny; i++) h.push_back(std::exp(c->Ly[i] * ndt));
+  for (int i = 0; i < nzc; i++) h.push_back(std::exp(c->Lz[i] * ndt));
+  cudaMemcpyAsync(c->dfac, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  cudaStreamSynchronize(c->stream);
+  c->ddft_have_factors = true;
+}
+
+static int ddft_rhs(cdft_ctx* c, const double* rho, void* spec, double* rmax) {
+  double m;
+  FDdftRhs f{rho, c->dF, c->dR, c->p.nx, c->p.ny, c->p.nz, c->p.dx, c->info.dV};
+  int rc = map_reduce<0, 1>(c, c->info.N, f, &m);
+  if (rc) return rc;
+  if (rmax) *rmax = m / c->info.dV;
+  return ddft_r2c(c, c->dR, spec);
+}
+
+// DDFT::step (src/DDFT.cpp:113-182), single species, periodic boundaries.
+static int ddft_one_step(cdft_ctx* c, int* restarts) {
+  const long N = c->info.N;
+  const size_t nb = N * sizeof(double);
+  if (!c->ddft_have_factors) {
+    double tmp = c->ddft_dt;
+    c->ddft_dt = 0;
+    ddft_change_timestep(c, tmp);
+  }
+  double t[8];
+  int rc = eval_internal(c, t);
+  if (rc) return rc;
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->dd0, c->rho, nb, cudaMemcpyDeviceToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->dd1, c->rho, nb, cudaMemcpyDeviceToDevice, c->stream));
+  double rhs_max = 0;
+  rc = ddft_rhs(c, c->dd0, c->R0k, &rhs_max);
+  if (rc) return rc;
+  c->ddft_rhs = rhs_max;
+  ddft_r2c(c, c->dd0, c->rk0);
+  bool decreased = false, restart;
+  int tries = 0;
+  do {
+    if (++tries > 40) return fail(c, CDFT_ERR_TIMEOUT, "DDFT fixed point did not converge after 40 time-step reductions");
+    double deviation = 1;
+    restart = false;
+    for (int i = 0; i < 100 && deviation > c->ddft_tol && !restart; i++) {
+      CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rho, c->dd1, nb, cudaMemcpyDeviceToDevice, c->stream));
+      rc = eval_internal(c, t);
+      if (rc) return rc;
+      rc = ddft_rhs(c, c->dd1, c->R1k, nullptr);
+      if (rc) return rc;
+      const int nx = c->p.nx, ny = c->p.ny, nzc = c->p.nz / 2 + 1;
+      const unsigned g = grid_for(c->info.Nc);
+      if (c->precision == CDFT_FP64) {
+        k_ddft_prop<double><<<g, 256, 0, c->stream>>>((const double2*)c->rk0, (const double2*)c->R0k, (const double2*)c->R1k, (double2*)c->work,
+                                                       c->dfac, nx, ny, nzc, c->ddft_dt);
+        c->e64->c2r((const double2*)c->work, c->ddn, 1.0 / (double)N, c->stream);
+      } else {
+        k_ddft_prop<float><<<g, 256, 0, c->stream>>>((const float2*)c->rk0, (const float2*)c->R0k, (const float2*)c->R1k, (float2*)c->work,
+                                                      c->dfac, nx, ny, nzc, c->ddft_dt);
+        c->e32->c2r((const float2*)c->work, c->ddn, 1.0f / (float)N, c->stream);
+      }
+      double red[2];
+      rc = map_reduce<0, 2>(c, N, FDdftDev{c->dd1, c->ddn}, red);
+      if (rc) return rc;
+      const double old = deviation;
+      deviation = red[0];
+      const double mn = -red[1];
+      std::swap(c->dd1, c->ddn);
+      if (mn < 0 || (i > 0 && old < deviation)) restart = true;
+    }
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rho, c->dd0, nb, cudaMemcpyDeviceToDevice, c->stream));
+    if (restart || deviation > c->ddft_tol) {
+      ddft_change_timestep(c, c->ddft_dt / 10);
+      CUDA_OR_FAIL(c, cudaMemcpyAsync(c->dd1, c->dd0, nb, cudaMemcpyDeviceToDevice, c->stream));
+      decreased = true;
+      restart = true;
+      if (restarts) (*restarts)++;
+    }
+  } while (restart);
+  c->ddft_time += c->ddft_dt;
+  if (decreased) c->ddft_successes = 0;
+  else c->ddft_successes++;
+  if (c->ddft_successes >= 5 && c->ddft_dt < c->ddft_dt_max) {
+    ddft_change_timestep(c, std::min(2 * c->ddft_dt, c->ddft_dt_max));
+    c->ddft_successes = 0;
+  }
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rho, c->dd1, nb, cudaMemcpyDeviceToDevice, c->stream));
+  rc = eval_internal(c, t);
+  if (rc) return rc;
+  c->F = t[0];
+  return CDFT_OK;
+}
+
+int cdft_ddft_step(cdft_ctx* c, int nsteps, cdft_ddft_report* rep) {
+  if (!c) return CDFT_ERR_ARG;
+  if (!c->ddft_ready) return fail(c, CDFT_ERR_STATE, "cdft_ddft_init has not been called");
+  int restarts = 0;
+  for (int k = 0; k < nsteps; ++k) {
+    int rc = ddft_one_step(c, &restarts);
+    if (rc) return rc;
+  }
+  if (rep) {
+    double s;
+    int rc = map_reduce<1, 0>(c, c->info.N, FSumRho{c->rho}, &s);
+    if (rc) return rc;
+    rep->steps = nsteps;
+    rep->F = c->F;
+    rep->time = c->ddft_time;
+    rep->dt = c->ddft_dt;
+    rep->mass = s * c->info.dV;
+    rep->rhs_max = c->ddft_rhs;
+    rep->restarts = restarts;
+  }
+  return CDFT_OK;
+}
+
+}  // extern "C"

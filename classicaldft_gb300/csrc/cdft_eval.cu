@@ -1,0 +1,359 @@
+// Evaluation engine: FFT tables, weight spectra, and the launch sequence of
+// one F+dF evaluation (kernels in cdft_kernels.cuh).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include "cdft_internal.h"
+#include "cdft_kernels.cuh"
+
+namespace cdft {
+
+#define CK(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) {                                                                    \
+      if (err) *err = std::string(#x) + ": " + cudaGetErrorString(e_);                          \
+      return 5;                                                                                 \
+    }                                                                                           \
+  } while (0)
+
+// ------------------------------------------------------------ FFT tables ---
+FFTTable::~FFTTable() {
+  if (d64) cudaFree(d64);
+  if (d32) cudaFree(d32);
+}
+
+std::shared_ptr<FFTTable> make_fft_table(int n, std::string* err) {
+  auto t = std::make_shared<FFTTable>();
+  FFTPlan& P = t->plan;
+  std::memset(&P, 0, sizeof(P));
+  P.n = n;
+  int m = n;
+  while (m > 1) {
+    int r = 0;
+    if (m % 8 == 0 && m != 16) r = 8;  // 16 = 4 x 4 keeps both stages radix 4
+    else if (m % 4 == 0) r = 4;
+    else if (m % 2 == 0) r = 2;
+    else {
+      for (int f = 3; f <= m; f += 2)
+        if (m % f == 0) { r = f; break; }
+    }
+    if (r > kMaxRadix || P.nst >= kMaxStages) {
+      if (err) *err = "grid length " + std::to_string(n) + " has a prime factor above 31";
+      return nullptr;
+    }
+    P.radix[P.nst++] = r;
+    m /= r;
+  }
+  // table: for each stage the m*p twiddles exp(-2 pi i q t/len), then the p roots exp(-2 pi i t/p)
+  std::vector<long double> re, im;
+  auto push = [&](long num, long den) {
+    num %= den;
+    const long double a = 6.283185307179586476925286766559005768L * (long double)num / (long double)den;
+    re.push_back(cosl(a));
+    im.push_back(-sinl(a));
+  };
+  int len = n;
+  for (int st = 0; st < P.nst; ++st) {
+    const int p = P.radix[st], sub = len / p;
+    P.tw_off[st] = (int)re.size();
+    for (int q = 0; q < sub; ++q)
+      for (int tt = 0; tt < p; ++tt) push((long)q * tt, len);
+    P.root_off[st] = (int)re.size();
+    for (int tt = 0; tt < p; ++tt) push(tt, p);
+    len = sub;
+  }
+  const size_t cnt = re.size();
+  std::vector<double2> h64(cnt);
+  std::vector<float2> h32(cnt);
+  for (size_t i = 0; i < cnt; ++i) {
+    h64[i] = make_double2((double)re[i], (double)im[i]);
+    h32[i] = make_float2((float)re[i], (float)im[i]);
+  }
+  if (cudaMalloc(&t->d64, cnt * sizeof(double2)) != cudaSuccess || cudaMalloc(&t->d32, cnt * sizeof(float2)) != cudaSuccess) {
+    if (err) *err = "cudaMalloc of FFT tables failed";
+    return nullptr;
+  }
+  cudaMemcpy(t->d64, h64.data(), cnt * sizeof(double2), cudaMemcpyHostToDevice);
+  cudaMemcpy(t->d32, h32.data(), cnt * sizeof(float2), cudaMemcpyHostToDevice);
+  return t;
+}
+
+template <class T> const typename Cx<T>::type* twp(const FFTTable* t);
+template <> const double2* twp<double>(const FFTTable* t) { return reinterpret_cast<const double2*>(t->d64); }
+template <> const float2* twp<float>(const FFTTable* t) { return reinterpret_cast<const float2*>(t->d32); }
+
+// --------------------------------------------------------- small kernels ---
+__global__ void k_finish_reduce(const double* __restrict__ part, long nblk, int nv, double* __restrict__ out) {
+  // one block; thread t sums blocks t, t+256, ... in order; then a fixed tree
+  __shared__ double ss[256], sc[256];
+  for (int v = 0; v < nv; ++v) {
+    Acc a;
+    a.init();
+    for (long b = threadIdx.x; b < nblk; b += blockDim.x) a.merge(part[(b * nv + v) * 2], part[(b * nv + v) * 2 + 1]);
+    ss[threadIdx.x] = a.s;
+    sc[threadIdx.x] = a.c;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if ((int)threadIdx.x < o) {
+        Acc t;
+        t.s = ss[threadIdx.x];
+        t.c = sc[threadIdx.x];
+        t.merge(ss[threadIdx.x + o], sc[threadIdx.x + o]);
+        ss[threadIdx.x] = t.s;
+        sc[threadIdx.x] = t.c;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[v] = ss[0] + sc[0];
+    __syncthreads();
+  }
+}
+
+template <class T>
+__global__ void k_compact(const double2* __restrict__ full, T* __restrict__ out, long n, int odd, double scale) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    out[i] = (T)((odd ? full[i].y : full[i].x) * scale);
+}
+
+// ------------------------------------------------------------ Evaluator ---
+template <class T>
+Evaluator<T>::~Evaluator() {
+  cudaFree(A_); cudaFree(Cf_); cudaFree(E_); cudaFree(w_); cudaFree(watt_); cudaFree(part_); cudaFree(terms_); cudaFree(status_);
+}
+
+template <class T>
+long Evaluator<T>::grid_blocks_rows() const {
+  const long pairs = (rows_ + 1) / 2;
+  return (pairs + rb_rows_ - 1) / rb_rows_;
+}
+
+static size_t smem_bytes(int lines, int n, size_t csize, int nbuf) { return (size_t)nbuf * lines * (n + 1) * csize; }
+
+template <class T, class F>
+static void set_smem(F f, size_t bytes) {
+  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// FP64 real -> full FP64 half spectrum with the double-precision kernels.
+static void r2c_f64(const double* in, double2* out, const Dims& d, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s) {
+  const int RB = 16, TC = 16;
+  const long pairs = (d.rows + 1) / 2;
+  const size_t sm_r = smem_bytes(RB, d.nz, sizeof(double2), 2);
+  set_smem<double>(k_rows_r2c<double, double>, sm_r);
+  k_rows_r2c<double, double><<<(unsigned)((pairs + RB - 1) / RB), 256, sm_r, s>>>(in, out, d, tz->plan, twp<double>(tz), RB);
+  const size_t sm_y = smem_bytes(TC, d.ny, sizeof(double2), 2);
+  set_smem<double>(k_cols_fft<double, -1>, sm_y);
+  k_cols_fft<double, -1><<<dim3((unsigned)(((long)d.nx * d.nzc + TC - 1) / TC), 1), 256, sm_y, s>>>(out, 0, 1, d, ty->plan, twp<double>(ty), TC);
+  const size_t sm_x = smem_bytes(TC, d.nx, sizeof(double2), 2);
+  set_smem<double>(k_cols_fft<double, -1>, std::max(sm_x, sm_y));
+  k_cols_fft<double, -1><<<dim3((unsigned)(((long)d.ny * d.nzc + TC - 1) / TC), 1), 256, sm_x, s>>>(out, 0, 0, d, tx->plan, twp<double>(tx), TC);
+}
+
+template <class T>
+int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA, double esB, const std::vector<double>* w_fmt,
+                       const std::vector<double>* w_att, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s, std::string* err) {
+  nx_ = nx; ny_ = ny; nz_ = nz; nzc_ = nz / 2 + 1;
+  N_ = (long)nx * ny * nz;
+  Nc_ = (long)nx * ny * nzc_;
+  rows_ = (long)nx * ny;
+  model_ = model;
+  M_ = (model < 0) ? 0 : (model >= MODEL_ESFMT ? 11 : 5);
+  hsd_ = hsd; esA_ = esA; esB_ = esB;
+  mf_ = (w_att != nullptr);
+  tx_ = tx; ty_ = ty; tz_ = tz;
+  Dims d{nx, ny, nz, nzc_, N_, Nc_, rows_};
+  const size_t cs = sizeof(C);
+  CK(cudaMalloc(&A_, Nc_ * cs));
+  CK(cudaMalloc(&E_, Nc_ * cs));
+  if (M_ > 0) CK(cudaMalloc(&Cf_, (size_t)M_ * Nc_ * cs));
+  // launch geometry and shared memory
+  smem_rows_ = smem_bytes(rb_rows_, nz, cs, 2);
+  // fused phi kernel: NP lines per row; shrink rows per block to fit 200 KB
+  const int NP = (M_ + 1) / 2;
+  rb_phi_ = 8;
+  while (rb_phi_ > 1 && (NP > 0) && smem_bytes(NP * rb_phi_, nz, cs, 2) > 200 * 1024) rb_phi_ /= 2;
+  smem_phi_ = NP > 0 ? smem_bytes(NP * rb_phi_, nz, cs, 2) : 0;
+  smem_colx_ = smem_bytes(tc_, nx, cs, 2);
+  smem_coly_ = smem_bytes(tc_, ny, cs, 2);
+  smem_xconv_ = smem_bytes(tc_, nx, cs, 3);
+  smem_xback_ = smem_bytes(tc_, nx, cs, 3);
+  if (std::max(std::max(smem_rows_, smem_phi_), std::max(smem_xconv_, smem_coly_)) > 220 * 1024) {
+    if (err) *err = "grid too large for the shared-memory transform tiles";
+    return 4;
+  }
+  set_smem<T>(k_rows_r2c<T, double>, smem_rows_);
+  set_smem<T>(k_rows_c2r<T, double>, smem_rows_);
+  set_smem<T>(k_final_rows<T>, smem_rows_);
+  set_smem<T>(k_cols_fft<T, -1>, std::max(smem_colx_, smem_coly_));
+  set_smem<T>(k_cols_fft<T, +1>, std::max(smem_colx_, smem_coly_));
+  set_smem<T>(k_xconv<T>, smem_xconv_);
+  set_smem<T>(k_xbackconv<T>, smem_xback_);
+  set_smem<T>(k_phi_rows<T, MODEL_ROSENFELD>, smem_phi_);
+  set_smem<T>(k_phi_rows<T, MODEL_RSLT>, smem_phi_);
+  set_smem<T>(k_phi_rows<T, MODEL_ESFMT>, smem_phi_);
+  set_smem<T>(k_phi_rows<T, MODEL_WHITEBEAR_I>, smem_phi_);
+  set_smem<T>(k_phi_rows<T, MODEL_WHITEBEAR_II>, smem_phi_);
+  // partial-sum storage: phi blocks (1 value), x columns (1 value), final rows (4 values)
+  const long nphi = (rows_ + rb_phi_ - 1) / rb_phi_;
+  const long ncolx = ((long)ny * nzc_ + tc_ - 1) / tc_;
+  part_len_ = 2 * (nphi + ncolx + 4 * grid_blocks_rows());
+  CK(cudaMalloc(&part_, part_len_ * sizeof(double)));
+  CK(cudaMalloc(&terms_, 8 * sizeof(double)));
+  CK(cudaMalloc(&status_, sizeof(unsigned)));
+  CK(cudaMemsetAsync(terms_, 0, 8 * sizeof(double), s));
+  // weight spectra: FP64 r2c on the device, keep the non-zero component, fold 1/N
+  double* tmp_real = nullptr;
+  double2* tmp_spec = nullptr;
+  CK(cudaMalloc(&tmp_real, N_ * sizeof(double)));
+  CK(cudaMalloc(&tmp_spec, Nc_ * sizeof(double2)));
+  const unsigned cgrid = (unsigned)std::min<long>((Nc_ + 255) / 256, 4096);
+  if (M_ > 0) {
+    CK(cudaMalloc(&w_, (size_t)M_ * Nc_ * sizeof(T)));
+    for (int a = 0; a < M_; ++a) {
+      CK(cudaMemcpyAsync(tmp_real, w_fmt[a].data(), N_ * sizeof(double), cudaMemcpyHostToDevice, s));
+      r2c_f64(tmp_real, tmp_spec, d, tx, ty, tz, s);
+      k_compact<T><<<cgrid, 256, 0, s>>>(tmp_spec, w_ + (long)a * Nc_, Nc_, (a >= 2 && a <= 4) ? 1 : 0, 1.0 / (double)N_);
+    }
+  }
+  if (mf_) {
+    CK(cudaMalloc(&watt_, Nc_ * sizeof(T)));
+    CK(cudaMemcpyAsync(tmp_real, w_att->data(), N_ * sizeof(double), cudaMemcpyHostToDevice, s));
+    r2c_f64(tmp_real, tmp_spec, d, tx, ty, tz, s);
+    k_compact<T><<<cgrid, 256, 0, s>>>(tmp_spec, watt_, Nc_, 0, 1.0 / (double)N_);
+  }
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  cudaFree(tmp_real);
+  cudaFree(tmp_spec);
+  return 0;
+}
+
+template <class T>
+void Evaluator<T>::r2c(const double* in, C* out, cudaStream_t s) {
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_};
+  k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(in, out, d, tz_->plan, twp<T>(tz_), rb_rows_);
+  k_cols_fft<T, -1><<<dim3((unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_coly_, s>>>(out, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  k_cols_fft<T, -1><<<dim3((unsigned)(((long)ny_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_colx_, s>>>(out, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
+}
+
+template <class T>
+void Evaluator<T>::c2r(const C* in, double* out, T scale, cudaStream_t s) {
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_};
+  C* work = E_;
+  cudaMemcpyAsync(work, in, Nc_ * sizeof(C), cudaMemcpyDeviceToDevice, s);
+  k_cols_fft<T, +1><<<dim3((unsigned)(((long)ny_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_colx_, s>>>(work, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  k_cols_fft<T, +1><<<dim3((unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_coly_, s>>>(work, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  k_rows_c2r<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(work, out, d, tz_->plan, twp<T>(tz_), rb_rows_, scale);
+}
+
+template <class T>
+int Evaluator<T>::launch(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, cudaStream_t s,
+                         cudaEvent_t* ev) {
+  auto mark = [&](int i) {
+    if (ev) cudaEventRecord(ev[i], s);
+  };
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_};
+  const unsigned gcy = (unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_);
+  const unsigned gcx = (unsigned)(((long)ny_ * nzc_ + tc_ - 1) / tc_);
+  const long nphi = (rows_ + rb_phi_ - 1) / rb_phi_;
+  double* part_phi = part_;
+  double* part_mf = part_ + 2 * nphi;
+  double* part_fin = part_mf + 2 * gcx;
+  const bool any = M_ > 0 || mf_;
+  cudaMemsetAsync(status_, 0, sizeof(unsigned), s);
+  mark(0);
+  if (any) {
+    k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+    mark(1);
+    k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
+    mark(2);
+  } else {
+    mark(1);
+    mark(2);
+  }
+  if (M_ > 0) {
+    k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
+    mark(3);
+    k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+    mark(4);
+    const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
+    const unsigned gphi = (unsigned)nphi;
+    switch (model_) {
+      case MODEL_ROSENFELD: k_phi_rows<T, MODEL_ROSENFELD><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
+      case MODEL_RSLT: k_phi_rows<T, MODEL_RSLT><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
+      case MODEL_ESFMT: k_phi_rows<T, MODEL_ESFMT><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
+      case MODEL_WHITEBEAR_I: k_phi_rows<T, MODEL_WHITEBEAR_I><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
+      default: k_phi_rows<T, MODEL_WHITEBEAR_II><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
+    }
+    k_finish_reduce<<<1, 256, 0, s>>>(part_phi, nphi, 1, terms_ + 0);
+    mark(5);
+    k_cols_fft<T, -1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+    mark(6);
+  } else {
+    for (int i = 3; i <= 6; ++i) mark(i);
+  }
+  if (any) {
+    k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
+                                                 mf_ ? part_mf : nullptr);
+    if (mf_) k_finish_reduce<<<1, 256, 0, s>>>(part_mf, gcx, 1, terms_ + 1);
+    mark(7);
+    k_cols_fft<T, +1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(E_, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
+    mark(8);
+  } else {
+    mark(7);
+    mark(8);
+  }
+  const unsigned gfin = (unsigned)grid_blocks_rows();
+  k_final_rows<T><<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_), rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin);
+  k_finish_reduce<<<1, 256, 0, s>>>(part_fin, gfin, 4, terms_ + 2);
+  mark(9);
+  return 0;
+}
+
+template <class T>
+void Evaluator<T>::pass_bytes(double* by) const {
+  const double b = sizeof(T), N = (double)N_, Nc = (double)Nc_, M = M_;
+  const double C = 2 * Nc * b, W = Nc * b;
+  const bool any = M_ > 0 || mf_;
+  by[0] = any ? N * 8 + C : 0;                        // rows_r2c: rho (f64) -> A
+  by[1] = any ? 2 * C : 0;                            // y forward of A
+  by[2] = M_ ? C + M * W + M * C : 0;                 // xconv: A, weights -> C[a]
+  by[3] = M_ ? M * 2 * C : 0;                         // y inverse of C[a]
+  by[4] = M_ ? M * 2 * C : 0;                         // phi rows: C[a] -> D[a]
+  by[5] = M_ ? M * 2 * C : 0;                         // y forward of D[a]
+  by[6] = any ? M * (C + W) + (mf_ ? C + W : 0) + C : 0;  // xbackconv: D[a], weights, A, w_att -> E
+  by[7] = any ? 2 * C : 0;                            // y inverse of E
+  by[8] = (any ? C : 0) + 2 * N * 8;                  // final rows: E, rho (f64) -> dF (f64)
+}
+
+template <class T>
+int Evaluator<T>::finish(double dV, double mu, EvalTerms* out, cudaStream_t s) {
+  double h[8];
+  unsigned st = 0;
+  cudaMemcpyAsync(h, terms_, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(&st, status_, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return 5;
+  out->F_hs = M_ > 0 ? h[0] * dV : 0.0;
+  out->F_mf = mf_ ? 0.5 * dV * h[1] : 0.0;
+  out->F_id = h[2];
+  out->sum_rho = h[3];
+  out->sum_vext_rho = h[4];
+  out->sum_dF_rho = h[5];
+  out->F_ext = h[4] * dV - (h[3] * dV) * mu;
+  out->status = st;
+  out->Omega = ((out->F_id + out->F_hs) + out->F_mf) + out->F_ext;
+  return (cudaGetLastError() == cudaSuccess) ? 0 : 5;
+}
+
+template <class T>
+int Evaluator<T>::eval(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, EvalTerms* out, cudaStream_t s) {
+  int rc = launch(rho, vext, dF, dV, mu, ideal, s);
+  if (rc) return rc;
+  return finish(dV, mu, out, s);
+}
+
+template class Evaluator<float>;
+template class Evaluator<double>;
+
+}  // namespace cdft

@@ -1,0 +1,89 @@
+// Internal host-side declarations of the GB300 evaluation engine.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+#include "cdft_types.h"
+
+namespace cdft {
+
+struct Dims;
+
+// Twiddle tables for one transform length, in both precisions, on the device.
+struct FFTTable {
+  FFTPlan plan;
+  void* d64 = nullptr;  // double2[]
+  void* d32 = nullptr;  // float2[]
+  ~FFTTable();
+};
+std::shared_ptr<FFTTable> make_fft_table(int n, std::string* err);  // nullptr if n has a prime factor > 31
+
+// Host-side setup maths (cdft_setup.cpp).
+double bh_diameter_lj(double sigma, double eps, double rc, double kT);
+void fmt_weights_real(int nx, int ny, int nz, double dx, double hsd, std::vector<double> w[11]);
+void qf_kernel_real(int nx, int ny, int nz, double dx, double sigma, double eps, double rc, double kT, std::vector<double>& w_att,
+                    double& a_vdw);
+double fmt_phi_host(int model, double A, double B, const double fm19[19], double dphi19[19]);
+double bulk_muex(int model, double A, double B, double hsd, double rho);
+double bulk_fex(int model, double A, double B, double hsd, double rho);
+
+struct EvalTerms {
+  double F_id, F_hs, F_mf, F_ext, Omega;
+  double sum_rho, sum_vext_rho, sum_dF_rho;
+  unsigned status;
+};
+
+// Device buffers and launch sequence of one F+dF evaluation in precision T.
+template <class T>
+class Evaluator {
+ public:
+  typedef typename Cx<T>::type C;
+  Evaluator() {}
+  ~Evaluator();
+  // w_fmt: 11 real-space weights (host, FP64) or null; w_att: real-space MF kernel or null.
+  int init(int nx, int ny, int nz, int model, double hsd, double esA, double esB, const std::vector<double>* w_fmt,
+           const std::vector<double>* w_att, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s, std::string* err);
+  // rho (device FP64) -> dF (device FP64), scalar terms (host). Synchronous at the end.
+  int eval(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, EvalTerms* out, cudaStream_t s);
+  // Launches the pass sequence without host synchronisation; partial sums land in dev_terms.
+  // ev (optional, 10 events) are recorded before pass 0 and after each of the 9 passes.
+  int launch(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, cudaStream_t s,
+             cudaEvent_t* ev = nullptr);
+  // Algorithmic bytes each of the 9 passes must move (reads + writes once).
+  void pass_bytes(double* bytes) const;
+  int finish(double dV, double mu, EvalTerms* out, cudaStream_t s);
+  // Transforms used by DDFT and tests: real FP64 (device) -> spectrum (device C), and back (x scale).
+  void r2c(const double* in, C* out, cudaStream_t s);
+  void c2r(const C* in, double* out, T scale, cudaStream_t s);
+  C* spectrum_buffer() const { return A_; }
+  const T* weights() const { return w_; }
+  const T* w_att() const { return watt_; }
+  int M() const { return M_; }
+  double* dev_terms() const { return terms_; }
+  unsigned* dev_status() const { return status_; }
+  long grid_blocks_rows() const;
+
+ private:
+  int nx_ = 0, ny_ = 0, nz_ = 0, nzc_ = 0;
+  long N_ = 0, Nc_ = 0, rows_ = 0;
+  int model_ = -1, M_ = 0;
+  double hsd_ = 1, esA_ = 1, esB_ = 0;
+  bool mf_ = false;
+  FFTTable *tx_ = nullptr, *ty_ = nullptr, *tz_ = nullptr;
+  C* A_ = nullptr;    // forward-transformed density (after z, y)
+  C* Cf_ = nullptr;   // M weighted-density / derivative spectra
+  C* E_ = nullptr;    // back-convolution
+  T* w_ = nullptr;    // M compact weight spectra (w~_a / N, the non-zero component)
+  T* watt_ = nullptr; // compact mean-field kernel spectrum (w~_att / N)
+  double* part_ = nullptr;  // block partial sums
+  long part_len_ = 0;
+  double* terms_ = nullptr;  // reduced sums: [0] sum Phi, [1] Parseval MF, [2] F_id, [3] sum rho, [4] sum V rho, [5] sum dF rho
+  unsigned* status_ = nullptr;
+  int rb_rows_ = 16, rb_phi_ = 4, tc_ = 16;
+  size_t smem_rows_ = 0, smem_phi_ = 0, smem_colx_ = 0, smem_coly_ = 0, smem_xconv_ = 0, smem_xback_ = 0;
+};
+
+}  // namespace cdft

@@ -1,0 +1,433 @@
+// Device kernels of the F+dF evaluation (sm_103a). Layout in HBM follows the
+// reference's Lattice (include/Lattice.h:120-134): real fields row-major
+// pos = k + Nz*(j + Ny*i); half spectra kpos = kz + Nzc*(ky + Ny*kx) with
+// Nzc = Nz/2 + 1 (FFTW r2c layout). Transforms are unnormalised.
+//
+// Pass structure of one evaluation (T = float or double):
+//   rows_r2c     rho (f64) -> A            z-axis r2c, two rows per complex FFT
+//   cols_fft(y)  A                          y-axis forward
+//   xconv        A -> C[a], a < M          x-axis forward, x w_a, x-axis inverse
+//   cols_fft(y)  C[a]                       y-axis inverse (batched over a)
+//   phi_rows     C[a] -> D[a] (in place)   z-axis c2r, Phi/dPhi, z-axis r2c
+//   cols_fft(y)  D[a]                       y-axis forward (batched)
+//   xbackconv    D[a], A -> E              x-axis forward, sum_a D~ w_a (+ rho~ w_att),
+//                                           x-axis inverse
+//   cols_fft(y)  E                          y-axis inverse
+//   final_rows   E, rho -> dF (f64)         z-axis c2r + ideal/external terms
+#pragma once
+#include "cdft_fft.cuh"
+#include "cdft_phi.cuh"
+
+namespace cdft {
+
+struct Dims {
+  int nx, ny, nz, nzc;
+  long N, Nc;
+  long rows;  // nx*ny
+};
+
+// ----------------------------------------------------------- reductions ---
+struct Acc {  // Neumaier compensated FP64 accumulator
+  double s, c;
+  __device__ __forceinline__ void init() { s = 0; c = 0; }
+  __device__ __forceinline__ void add(double v) {
+    double t = s + v;
+    if (fabs(s) >= fabs(v)) c += (s - t) + v;
+    else c += (v - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ void merge(double s2, double c2) { add(s2); c += c2; }
+};
+
+// Block-wide merge of NV accumulators; thread 0 writes (s, c) pairs to
+// out[(blockIdx.x * NV + v) * 2 + {0,1}] (out indexed by the linear block id).
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(Acc* acc, double* out, long block_id) {
+  __shared__ double red[32][NV][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      double s2 = __shfl_down_sync(0xffffffffu, acc[v].s, o);
+      double c2 = __shfl_down_sync(0xffffffffu, acc[v].c, o);
+      acc[v].merge(s2, c2);
+    }
+    if (lane == 0) { red[warp][v][0] = acc[v].s; red[warp][v][1] = acc[v].c; }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int v = 0; v < NV; ++v) {
+      Acc t;
+      t.init();
+      for (int w = 0; w < nw; ++w) t.merge(red[w][v][0], red[w][v][1]);
+      out[(block_id * NV + v) * 2 + 0] = t.s;
+      out[(block_id * NV + v) * 2 + 1] = t.c;
+    }
+  }
+}
+
+// Sums nblk partial (s, c) pairs of NV values in a fixed order: out[v] = total.
+__global__ void k_finish_reduce(const double* __restrict__ part, long nblk, int nv, double* __restrict__ out);
+
+// ------------------------------------------------------------ row passes ---
+// z-axis r2c: rows of a real field (SRC = double or T) to half spectra.
+// Each block owns RB row pairs; pair r packs rows (2r, 2r+1) as re/im.
+template <class T, class SRC>
+__global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, typename Cx<T>::type* __restrict__ out, Dims d,
+                                                  FFTPlan pz, const typename Cx<T>::type* __restrict__ tw, int RB) {
+  typedef typename Cx<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  const int nz = d.nz, LP = nz + 1;
+  C* b1 = b0 + RB * LP;
+  const long pair0 = (long)blockIdx.x * RB;
+  for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+    const int r = e / nz, k = e - r * nz;
+    const long ra = 2 * (pair0 + r), rb = ra + 1;
+    T va = 0, vb = 0;
+    if (ra < d.rows) va = (T)in[ra * nz + k];
+    if (rb < d.rows) vb = (T)in[rb * nz + k];
+    b0[r * LP + k] = mk<T>(va, vb);
+  }
+  C* res = block_fft<-1, T>(b0, b1, RB, LP, pz, tw);
+  const int nzc = d.nzc;
+  for (int e = threadIdx.x; e < RB * nzc; e += blockDim.x) {
+    const int r = e / nzc, k = e - r * nzc;
+    const long ra = 2 * (pair0 + r), rb = ra + 1;
+    const C Z = res[r * LP + k];
+    const C W = res[r * LP + (k == 0 ? 0 : nz - k)];  // Z_{N-k}
+    // X = (Z + conj(W))/2, Y = (Z - conj(W))/(2i)
+    if (ra < d.rows) out[ra * nzc + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
+    if (rb < d.rows) out[rb * nzc + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+  }
+}
+
+// Loads the Hermitian-extended pair spectrum Z_k = A_k + i B_k (k < nz) into a
+// shared line, dropping Im of kz = 0 and kz = nz/2 as FFTW's c2r does.
+template <class T>
+__device__ __forceinline__ typename Cx<T>::type pair_spectrum(const typename Cx<T>::type* __restrict__ A, const typename Cx<T>::type* __restrict__ B,
+                                                              int k, int nz) {
+  typedef typename Cx<T>::type C;
+  const int nzc = nz / 2 + 1;
+  C a, b;
+  if (k < nzc) {
+    a = A ? A[k] : mk<T>(0, 0);
+    b = B ? B[k] : mk<T>(0, 0);
+    if (k == 0 || 2 * k == nz) { a.y = 0; b.y = 0; }
+  } else {
+    a = A ? A[nz - k] : mk<T>(0, 0);
+    b = B ? B[nz - k] : mk<T>(0, 0);
+    a.y = -a.y;
+    b.y = -b.y;
+  }
+  return mk<T>(a.x - b.y, a.y + b.x);
+}
+
+// z-axis c2r: half spectra rows to real rows (DST = double or T), times scale.
+template <class T, class DST>
+__global__ void __launch_bounds__(256) k_rows_c2r(const typename Cx<T>::type* __restrict__ in, DST* __restrict__ out, Dims d,
+                                                  FFTPlan pz, const typename Cx<T>::type* __restrict__ tw, int RB, T scale) {
+  typedef typename Cx<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  const int nz = d.nz, LP = nz + 1, nzc = d.nzc;
+  C* b1 = b0 + RB * LP;
+  const long pair0 = (long)blockIdx.x * RB;
+  for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+    const int r = e / nz, k = e - r * nz;
+    const long ra = 2 * (pair0 + r), rb = ra + 1;
+    const C* A = ra < d.rows ? in + ra * nzc : nullptr;
+    const C* B = rb < d.rows ? in + rb * nzc : nullptr;
+    b0[r * LP + k] = pair_spectrum<T>(A, B, k, nz);
+  }
+  C* res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
+  for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+    const int r = e / nz, k = e - r * nz;
+    const long ra = 2 * (pair0 + r), rb = ra + 1;
+    const C z = res[r * LP + k];
+    if (ra < d.rows) out[ra * nz + k] = (DST)(z.x * scale);
+    if (rb < d.rows) out[rb * nz + k] = (DST)(z.y * scale);
+  }
+}
+
+// --------------------------------------------------------- column passes ---
+// Columns of the half spectrum along x (axis 0, ncol = ny*nzc, stride ny*nzc)
+// or y (axis 1, ncol = nx*nzc, stride nzc). A block loads TC consecutive
+// columns (coalesced along kz), transforms them in shared memory, stores back.
+__device__ __forceinline__ long col_base(int axis, long c, const Dims& d) {
+  return axis == 0 ? c : (c / d.nzc) * (long)d.ny * d.nzc + (c % d.nzc);
+}
+
+template <class T>
+__device__ __forceinline__ void load_cols(typename Cx<T>::type* __restrict__ sm, const typename Cx<T>::type* __restrict__ g, int axis,
+                                          long c0, long ncol, int n, long stride, int TC, int LP, const Dims& d) {
+  for (int e = threadIdx.x; e < TC * n; e += blockDim.x) {
+    const int c = e % TC, i = e / TC;
+    const long col = c0 + c;
+    sm[c * LP + i] = (col < ncol) ? g[col_base(axis, col, d) + i * stride] : mk<T>(0, 0);
+  }
+}
+template <class T>
+__device__ __forceinline__ void store_cols(const typename Cx<T>::type* __restrict__ sm, typename Cx<T>::type* __restrict__ g, int axis,
+                                           long c0, long ncol, int n, long stride, int TC, int LP, const Dims& d) {
+  for (int e = threadIdx.x; e < TC * n; e += blockDim.x) {
+    const int c = e % TC, i = e / TC;
+    const long col = c0 + c;
+    if (col < ncol) g[col_base(axis, col, d) + i * stride] = sm[c * LP + i];
+  }
+}
+
+template <class T, int DIR>
+__global__ void __launch_bounds__(256) k_cols_fft(typename Cx<T>::type* __restrict__ data, long field_stride, int axis, Dims d,
+                                                  FFTPlan P, const typename Cx<T>::type* __restrict__ tw, int TC) {
+  typedef typename Cx<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = P.n, LP = n + 1;
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  C* b1 = b0 + TC * LP;
+  C* g = data + (long)blockIdx.y * field_stride;
+  const long ncol = axis == 0 ? (long)d.ny * d.nzc : (long)d.nx * d.nzc;
+  const long stride = axis == 0 ? (long)d.ny * d.nzc : (long)d.nzc;
+  const long c0 = (long)blockIdx.x * TC;
+  load_cols<T>(b0, g, axis, c0, ncol, n, stride, TC, LP, d);
+  C* res = block_fft<DIR, T>(b0, b1, TC, LP, P, tw);
+  store_cols<T>(res, g, axis, c0, ncol, n, stride, TC, LP, d);
+}
+
+// Weight parity: vector weights (a = 2, 3, 4) are odd, so their transform is
+// imaginary; all other FMT weights and the mean-field kernel are even (real).
+// w holds the one non-zero component per kpos.
+__device__ __forceinline__ bool weight_is_odd(int a) { return a >= 2 && a <= 4; }
+template <class C, class T>
+__device__ __forceinline__ C mul_weight(C z, T w, bool odd) {
+  if (odd) return mk<T>(-z.y * w, z.x * w);  // z * (i w)
+  return mk<T>(z.x * w, z.y * w);
+}
+
+// x-axis pass with the forward weights: C[a] = IFFT_x(FFT_x(A) . w_a).
+template <class T>
+__global__ void __launch_bounds__(256) k_xconv(const typename Cx<T>::type* __restrict__ A, typename Cx<T>::type* __restrict__ Cout,
+                                               const T* __restrict__ w, int M, Dims d, FFTPlan px,
+                                               const typename Cx<T>::type* __restrict__ tw, int TC) {
+  typedef typename Cx<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = px.n, LP = n + 1;
+  C* R = reinterpret_cast<C*>(smem_raw);
+  C* b0 = R + TC * LP;
+  C* b1 = b0 + TC * LP;
+  const long ncol = (long)d.ny * d.nzc, stride = ncol;
+  const long c0 = (long)blockIdx.x * TC;
+  load_cols<T>(b0, A, 0, c0, ncol, n, stride, TC, LP, d);
+  C* res = block_fft<-1, T>(b0, b1, TC, LP, px, tw);
+  for (int e = threadIdx.x; e < TC * n; e += blockDim.x) {
+    const int c = e % TC, i = e / TC;
+    R[c * LP + i] = res[c * LP + i];
+  }
+  for (int a = 0; a < M; ++a) {
+    const T* wa = w + (long)a * d.Nc;
+    const bool odd = weight_is_odd(a);
+    __syncthreads();
+    for (int e = threadIdx.x; e < TC * n; e += blockDim.x) {
+      const int c = e % TC, i = e / TC;
+      const long col = c0 + c;
+      const T wv = col < ncol ? __ldg(wa + i * stride + col) : (T)0;
+      b0[c * LP + i] = mul_weight(R[c * LP + i], wv, odd);
+    }
+    C* r2 = block_fft<+1, T>(b0, b1, TC, LP, px, tw);
+    store_cols<T>(r2, Cout + (long)a * d.Nc, 0, c0, ncol, n, stride, TC, LP, d);
+  }
+}
+
+// x-axis back-convolution: E = IFFT_x(sum_a FFT_x(D[a]) . w_a + FFT_x(A) . w_att).
+// With the mean field, each block also accumulates the Parseval sum
+// sum_k m(kz) |rho~|^2 w_att (m = 1 on the kz = 0 / Nyquist planes, else 2)
+// into part[blockIdx.x] for the interaction energy.
+template <class T>
+__global__ void __launch_bounds__(256) k_xbackconv(const typename Cx<T>::type* __restrict__ D, const typename Cx<T>::type* __restrict__ A,
+                                                   typename Cx<T>::type* __restrict__ E, const T* __restrict__ w,
+                                                   const T* __restrict__ watt, int M, Dims d, FFTPlan px,
+                                                   const typename Cx<T>::type* __restrict__ tw, int TC, double* __restrict__ part) {
+  typedef typename Cx<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = px.n, LP = n + 1;
+  C* S = reinterpret_cast<C*>(smem_raw);
+  C* b0 = S + TC * LP;
+  C* b1 = b0 + TC * LP;
+  const long ncol = (long)d.ny * d.nzc, stride = ncol;
+  const long c0 = (long)blockIdx.x * TC;
+  for (int e = threadIdx.x; e < TC * n; e += blockDim.x) {
+    const int c = e % TC, i = e / TC;
+    S[c * LP + i] = mk<T>(0, 0);
+  }
+  const int nsrc = M + (watt ? 1 : 0);
+  Acc acc;
+  acc.init();
+  for (int a = 0; a < nsrc; ++a) {
+    const bool is_mf = (a == M);
+    const C* src = is_mf ? A : D + (long)a * d.Nc;
+    const T* wa = is_mf ? watt : w + (long)a * d.Nc;
+    const bool odd = !is_mf && weight_is_odd(a);
+    __syncthreads();
+    load_cols<T>(b0, src, 0, c0, ncol, n, stride, TC, LP, d);
+    C* res = block_fft<-1, T>(b0, b1, TC, LP, px, tw);
+    for (int e = threadIdx.x; e < TC * n; e += blockDim.x) {
+      const int c = e % TC, i = e / TC;
+      const long col = c0 + c;
+      if (col < ncol) {
+        const T wv = __ldg(wa + i * stride + col);
+        const C z = res[c * LP + i];
+        S[c * LP + i] = cadd(S[c * LP + i], mul_weight(z, wv, odd));
+        if (is_mf) {
+          const int kz = (int)(col % d.nzc);
+          const double mult = (kz == 0 || 2 * kz == d.nz) ? 1.0 : 2.0;
+          acc.add(mult * ((double)z.x * (double)z.x + (double)z.y * (double)z.y) * (double)wv);
+        }
+      }
+    }
+  }
+  if (part) block_reduce_store<1>(&acc, part, blockIdx.x);
+  __syncthreads();
+  for (int e = threadIdx.x; e < TC * n; e += blockDim.x) {
+    const int c = e % TC, i = e / TC;
+    b0[c * LP + i] = S[c * LP + i];
+  }
+  C* r2 = block_fft<+1, T>(b0, b1, TC, LP, px, tw);
+  store_cols<T>(r2, E, 0, c0, ncol, n, stride, TC, LP, d);
+}
+
+// ------------------------------------------------- fused Phi on z rows ---
+// For RB rows (x, y): c2r of the M weighted-density rows (fields packed two
+// per complex line), Phi and dPhi at every point, r2c of the M derivative
+// rows written back over the inputs. Block partial of sum Phi -> part;
+// status bit 1: eta > 1 somewhere (Eta_Too_Large), bit 2: non-finite Phi.
+template <class T, int MODEL>
+__global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restrict__ Cf, Dims d, FFTPlan pz,
+                                                  const typename Cx<T>::type* __restrict__ tw, int RB, T hsd, T esA, T esB,
+                                                  double* __restrict__ part, unsigned* __restrict__ status) {
+  typedef typename Cx<T>::type C;
+  constexpr int M = ModelTraits<MODEL>::M;
+  constexpr int NP = (M + 1) / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nz = d.nz, LP = nz + 1, nzc = d.nzc;
+  const int L = NP * RB;
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  C* b1 = b0 + L * LP;
+  const long row0 = (long)blockIdx.x * RB;
+  // line index = r * NP + pair
+  for (int e = threadIdx.x; e < L * nz; e += blockDim.x) {
+    const int line = e / nz, k = e - line * nz;
+    const int r = line / NP, pr = line - r * NP;
+    const long row = row0 + r;
+    const C* Arow = nullptr;
+    const C* Brow = nullptr;
+    if (row < d.rows) {
+      Arow = Cf + (long)(2 * pr) * d.Nc + row * nzc;
+      if (2 * pr + 1 < M) Brow = Cf + (long)(2 * pr + 1) * d.Nc + row * nzc;
+    }
+    b0[line * LP + k] = pair_spectrum<T>(Arow, Brow, k, nz);
+  }
+  C* res = block_fft<+1, T>(b0, b1, L, LP, pz, tw);
+  C* other = (res == b0) ? b1 : b0;
+  Acc acc;
+  acc.init();
+  unsigned st = 0;
+  for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+    const int r = e / nz, k = e - r * nz;
+    if (row0 + r >= d.rows) continue;
+    T nv[11];
+#pragma unroll
+    for (int a = 0; a < M; ++a) {
+      const C z = res[(r * NP + a / 2) * LP + k];
+      nv[a] = (a & 1) ? z.y : z.x;
+    }
+    const T eta = nv[0];
+    const T phi = fmt_phi_point<T, MODEL>(nv, hsd, esA, esB);
+    if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
+    if (!isfinite(phi)) st |= 2u;
+    acc.add((double)phi);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const T im = (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0;
+      other[(r * NP + p) * LP + k] = mk<T>(nv[2 * p], im);
+    }
+  }
+  if (st) atomicOr(status, st);
+  block_reduce_store<1>(&acc, part, blockIdx.x);
+  C* res2 = block_fft<-1, T>(other, res, L, LP, pz, tw);
+  for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
+    const int line = e / nzc, k = e - line * nzc;
+    const int r = line / NP, pr = line - r * NP;
+    const long row = row0 + r;
+    if (row >= d.rows) continue;
+    const C Z = res2[line * LP + k];
+    const C W = res2[line * LP + (k == 0 ? 0 : nz - k)];
+    Cf[(long)(2 * pr) * d.Nc + row * nzc + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
+    if (2 * pr + 1 < M) Cf[(long)(2 * pr + 1) * d.Nc + row * nzc + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+  }
+}
+
+// ------------------------------------------------------ final z rows ---
+// c2r of E (the summed hard-sphere + mean-field back-convolution) and the
+// pointwise terms of DFT::calculateFreeEnergyAndDerivatives_internal_
+// (src/DFT.cpp:377-425) and Species::externalField (src/Species.cpp:51-61):
+//   dF = ln(rho) dV + c2r(E) dV + V_ext dV - mu dV
+// with FP64 partial sums: F_id = sum (rho ln rho - rho) dV, sum rho,
+// sum V_ext rho, sum dF rho (for the fixed-mass projection).
+template <class T>
+__global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* __restrict__ E, const double* __restrict__ rho,
+                                                    const double* __restrict__ vext, double* __restrict__ dF, Dims d, FFTPlan pz,
+                                                    const typename Cx<T>::type* __restrict__ tw, int RB, double dV, double mu,
+                                                    int have_fmt_or_mf, int ideal, double* __restrict__ part) {
+  typedef typename Cx<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  const int nz = d.nz, LP = nz + 1, nzc = d.nzc;
+  C* b1 = b0 + RB * LP;
+  const long pair0 = (long)blockIdx.x * RB;
+  C* res = b0;
+  if (have_fmt_or_mf) {
+    for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+      const int r = e / nz, k = e - r * nz;
+      const long ra = 2 * (pair0 + r), rb = ra + 1;
+      const C* Ar = ra < d.rows ? E + ra * nzc : nullptr;
+      const C* Br = rb < d.rows ? E + rb * nzc : nullptr;
+      b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
+    }
+    res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
+  }
+  Acc acc[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) acc[v].init();
+  for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
+    const int rr = e / nz, k = e - rr * nz;
+    const long row = 2 * pair0 + rr;
+    if (row >= d.rows) continue;
+    const long p = row * nz + k;
+    const double r0 = rho[p];
+    const double lr = log(r0);
+    double h = 0;
+    if (have_fmt_or_mf) {
+      const C z = res[(rr >> 1) * LP + k];
+      h = (double)((rr & 1) ? z.y : z.x);
+    }
+    const double ve = vext ? vext[p] : 0.0;
+    double f = ideal ? lr * dV : 0.0;
+    f += h * dV;
+    f += ve * dV;
+    f += -mu * dV;
+    dF[p] = f;
+    if (ideal) acc[0].add((r0 * lr - r0) * dV);
+    acc[1].add(r0);
+    acc[2].add(ve * r0);
+    acc[3].add(f * r0);
+  }
+  block_reduce_store<4>(acc, part, blockIdx.x);
+}
+
+// ----------------------------------------------------------- pointwise ---
+__global__ void k_scale(double* __restrict__ x, long n, const double* __restrict__ num, double den_scale, double target);
+__global__ void k_add_scalar(double* __restrict__ x, long n, const double* __restrict__ v, double scale);
+
+}  // namespace cdft

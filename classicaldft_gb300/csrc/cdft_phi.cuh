@@ -1,0 +1,156 @@
+// Pointwise FMT free-energy density Phi and its derivatives for one species,
+// folded into the per-species weighted-density derivatives used by the
+// back-convolution. Follows FMT::calculate_Phi / calculate_dPhi_wrt_fundamental_measures
+// (src/FMT.cpp:114-176), the model functions f1/f2/f3 and Phi3 of
+// include/FMT.h:139-643, and FMT_Species::set_fundamental_measure_derivatives
+// (include/Species.h:310-329): dPhi_s = dPhi_s0/d^2 + dPhi_s1/d + dPhi_s2, the
+// vector derivative carries the parity sign, off-diagonal tensor terms x2.
+#pragma once
+#include <cuda_runtime.h>
+#include "cdft_types.h"
+
+namespace cdft {
+
+template <int MODEL> struct ModelTraits { static constexpr bool tensor = MODEL >= MODEL_ESFMT; static constexpr int M = tensor ? 11 : 5; };
+
+template <class T> __device__ __forceinline__ T log1m(T e);
+template <> __device__ __forceinline__ double log1m<double>(double e) { return log(1.0 - e); }
+template <> __device__ __forceinline__ float log1m<float>(float e) { return log1pf(-e); }
+
+// f1, f2, f3 and first derivatives.
+template <class T, int MODEL>
+__device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, T& f3p) {
+  const T one = (T)1;
+  const T L = log1m<T>(e);
+  f1 = L;
+  f1p = -one / (one - e);
+  if (MODEL == MODEL_WHITEBEAR_II) {
+    if (e < (T)1e-12) {
+      f2 = one + e * (one + e * ((T)(10.0 / 9) + (T)(7.0 / 6) * e));
+      f2p = one + e * ((T)(20.0 / 9) + (T)3.5 * e);
+      f3 = (T)1.5 + (T)(7.0 / 3) * e + (T)3.25 * e * e + (T)4.2 * e * e * e;
+      f3p = (T)(7.0 / 3) + (T)7.5 * e + (T)12.6 * e * e;
+    } else {
+      f2 = (T)(1.0 / 3.0) + (T)(4.0 / 3.0) * (one / (one - e)) + ((T)2 / ((T)3 * e)) * L;
+      f2p = ((T)2 * ((T)3 * e - one) / ((T)3 * e * (one - e) * (one - e))) - ((T)2 / ((T)3 * e * e)) * L;
+      f3 = -((one - (T)3 * e + e * e) / (e * (one - e) * (one - e))) - (one / (e * e)) * L;
+      f3p = (((T)2 - (T)5 * e + (T)6 * e * e - e * e * e) / (e * e * (one - e) * (one - e) * (one - e))) + ((T)2 / (e * e * e)) * L;
+    }
+    return;
+  }
+  const T g = one / (one - e);
+  f2 = g;
+  f2p = g * g;
+  if (MODEL == MODEL_RSLT || MODEL == MODEL_WHITEBEAR_I) {
+    if (e < (T)1e-12) {
+      f3 = (T)1.5 + (T)(8.0 / 3) * e + (T)3.75 * e * e + (T)4.8 * e * e * e;
+      f3p = (T)(8.0 / 3) + (T)7.5 * e + (T)14.4 * e * e;
+    } else {
+      f3 = (one / (e * (one - e) * (one - e))) + (L / (e * e));
+      if (MODEL == MODEL_RSLT)
+        f3p = -(one / (e * e)) * (one / ((one - e) * (one - e) * (one - e))) * (e * e - (T)5 * e + (T)2) - ((T)2 / (e * e * e)) * L;
+      else
+        f3p = ((-(T)2 + (T)5 * e - e * e) / (e * e * (one - e) * (one - e) * (one - e))) - ((T)2 / (e * e * e)) * L;
+    }
+  } else {  // Rosenfeld and esFMT
+    f3 = g * g;
+    f3p = (T)2 * g * g * g;
+  }
+}
+
+// n[] holds the weighted densities in the order eta, s, v0, v1, v2, T00, T01,
+// T02, T11, T12, T22 (M = 11) or the first five (M = 5). On return n[] holds
+// dPhi/dn_a folded as described above. Returns Phi.
+template <class T, int MODEL>
+__device__ __forceinline__ T fmt_phi_point(T* n, T hsd, T A, T B) {
+  const T PI = (T)3.14159265358979323846;
+  const T s2 = n[1], s1 = n[1] / hsd, s0 = n[1] / (hsd * hsd);
+  const T eta = n[0];
+  T v2[3] = {n[2], n[3], n[4]};
+  T v1[3] = {n[2] / hsd, n[3] / hsd, n[4] / hsd};
+  const T v1_v2 = v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2];
+  const T v2_v2 = v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2];
+  T f1, f2, f3, f1p, f2p, f3p;
+  fmt_f<T, MODEL>(eta, f1, f2, f3, f1p, f2p, f3p);
+
+  T Phi3, dP3_dS2, dP3_dV2[3], dP3_dT[3][3];
+  T Tm[3][3];
+  if (ModelTraits<MODEL>::tensor) {
+    Tm[0][0] = n[5]; Tm[0][1] = Tm[1][0] = n[6]; Tm[0][2] = Tm[2][0] = n[7];
+    Tm[1][1] = n[8]; Tm[1][2] = Tm[2][1] = n[9]; Tm[2][2] = n[10];
+    T vT[3], TT[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) vT[i] = v2[0] * Tm[0][i] + v2[1] * Tm[1][i] + v2[2] * Tm[2][i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) TT[i][j] = Tm[i][0] * Tm[0][j] + Tm[i][1] * Tm[1][j] + Tm[i][2] * Tm[2][j];
+    const T vTv = v2[0] * vT[0] + v2[1] * vT[1] + v2[2] * vT[2];
+    const T T2 = TT[0][0] + TT[1][1] + TT[2][2];
+    T T3 = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) T3 += TT[i][j] * Tm[j][i];
+    const T a = (MODEL == MODEL_ESFMT) ? A : (T)1, b = (MODEL == MODEL_ESFMT) ? B : (T)-1;
+    Phi3 = (a / ((T)24 * PI)) * (s2 * s2 * s2 - (T)3 * s2 * v2_v2 + (T)3 * vTv - T3) + (b / ((T)24 * PI)) * (s2 * s2 * s2 - (T)3 * s2 * T2 + (T)2 * T3);
+    dP3_dS2 = (a / ((T)24 * PI)) * ((T)3 * s2 * s2 - (T)3 * v2_v2) + (b / ((T)24 * PI)) * ((T)3 * s2 * s2 - (T)3 * T2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dP3_dV2[k] = (a / ((T)24 * PI)) * (-(T)6 * s2 * v2[k] + (T)3 * vT[k] + (T)3 * vT[k]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        dP3_dT[j][k] = (a / ((T)8 * PI)) * (v2[j] * v2[k] - TT[k][j]) + (b / ((T)4 * PI)) * (-s2 * Tm[k][j] + TT[k][j]);
+  } else if (MODEL == MODEL_RSLT) {
+    if (s2 < (T)1e-20) {
+      Phi3 = 0; dP3_dS2 = 0; dP3_dV2[0] = dP3_dV2[1] = dP3_dV2[2] = 0;
+    } else {
+      const T psi = v2_v2 / (s2 * s2);
+      const T om = (T)1 - psi;
+      Phi3 = ((T)1 / ((T)36 * PI)) * s2 * s2 * s2 * om * om * om;
+      dP3_dS2 = ((T)1 / ((T)12 * PI)) * s2 * s2 * ((T)1 + psi) * om * om;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dP3_dV2[k] = -((T)1 / ((T)6 * PI)) * s2 * v2[k] * om * om;
+    }
+  } else {  // Rosenfeld
+    Phi3 = ((T)1 / ((T)24 * PI)) * (s2 * s2 * s2 - (T)3 * s2 * v2_v2);
+    dP3_dS2 = ((T)1 / ((T)24 * PI)) * ((T)3 * s2 * s2 - (T)3 * v2_v2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dP3_dV2[k] = ((T)1 / ((T)24 * PI)) * (-(T)6 * s2 * v2[k]);
+  }
+
+  T phi = 0;
+  phi -= ((T)1 / PI) * s0 * f1;
+  phi += ((T)1 / ((T)2 * PI)) * (s1 * s2 - v1_v2) * f2;
+  phi += Phi3 * f3;
+
+  T d_eta = 0;
+  d_eta -= ((T)1 / PI) * s0 * f1p;
+  d_eta += ((T)1 / ((T)2 * PI)) * (s1 * s2 - v1_v2) * f2p;
+  d_eta += Phi3 * f3p;
+  const T d_s0 = -((T)1 / PI) * f1;
+  const T d_s1 = ((T)1 / ((T)2 * PI)) * s2 * f2;
+  T d_s2 = ((T)1 / ((T)2 * PI)) * s1 * f2;
+  d_s2 += dP3_dS2 * f3;
+  n[0] = d_eta;
+  n[1] = (d_s0 / (hsd * hsd)) + (d_s1 / hsd) + d_s2;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const T d_v1 = ((T)1 / ((T)2 * PI)) * (-v2[k]) * f2;
+    T d_v2 = ((T)1 / ((T)2 * PI)) * (-v1[k]) * f2;
+    d_v2 += dP3_dV2[k] * f3;
+    n[2 + k] = -(d_v2 + d_v1 / hsd);
+  }
+  if (ModelTraits<MODEL>::tensor) {
+    n[5] = dP3_dT[0][0] * f3;
+    n[6] = (T)2 * (dP3_dT[0][1] * f3);
+    n[7] = (T)2 * (dP3_dT[0][2] * f3);
+    n[8] = dP3_dT[1][1] * f3;
+    n[9] = (T)2 * (dP3_dT[1][2] * f3);
+    n[10] = dP3_dT[2][2] * f3;
+  }
+  return phi;
+}
+
+}  // namespace cdft

@@ -1,0 +1,171 @@
+/*
+ * classicaldft_gb300 — C ABI of the GB300 (sm_103a) engine for classicalDFT's
+ * free-energy-and-derivative path and the FIRE2 / DDFT loops that drive it.
+ *
+ * One context = one single-species system (a Density on a periodic Lattice,
+ * one FMT_Species, an FMT model, optionally one LJ mean-field interaction,
+ * a chemical potential or a fixed mass) resident on one GPU. Every entry point
+ * returns CDFT_OK (0) or an error code; cdft_last_error() gives the message.
+ * Arrays are FP64 in the reference's row-major layout pos = k + Nz*(j + Ny*i)
+ * (include/Lattice.h:120-126). dF follows the reference's convention: it holds
+ * dOmega/drho_i * dV (include/Species.h:57, src/DFT.cpp:377-425).
+ * Host pointers are plain host memory; `on_device` = 1 means a CUDA device
+ * pointer on the context's device. A context is not thread-safe; use one per
+ * host thread. All work is ordered on the context's stream (cdft_set_stream).
+ */
+#ifndef CLASSICALDFT_GB300_CDFT_H
+#define CLASSICALDFT_GB300_CDFT_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return codes */
+#define CDFT_OK 0
+#define CDFT_ERR_ETA 1       /* eta > 1 at some site: Eta_Too_Large_Exception (include/FMT.h:649-663, src/FMT.cpp:289) */
+#define CDFT_ERR_NONFINITE 2 /* a non-finite free-energy density */
+#define CDFT_ERR_TIMEOUT 3   /* a device-side wait or iteration cap ran out */
+#define CDFT_ERR_ARG 4       /* bad argument (incommensurate lattice, hsd < dx, unsupported grid length, ...) */
+#define CDFT_ERR_CUDA 5      /* CUDA runtime error */
+#define CDFT_ERR_UPHILL 6    /* fireMinimizer2: "Cannot stop going uphill" (src/Minimizer.cpp:207) */
+#define CDFT_ERR_STATE 7     /* call out of order (e.g. cdft_fire_step before cdft_fire_init) */
+
+/* FMT models (include/FMT.h:139-643) */
+#define CDFT_MODEL_NONE (-1) /* ideal gas only (no FMT object) */
+#define CDFT_ROSENFELD 0
+#define CDFT_RSLT 1
+#define CDFT_ESFMT 2 /* esFMT(A, B) */
+#define CDFT_WHITEBEAR_I 3
+#define CDFT_WHITEBEAR_II 4
+
+/* Arithmetic of the bulk FFT / pointwise passes. Reductions are FP64 always. */
+#define CDFT_FP64 0
+#define CDFT_FP32 1
+
+typedef struct cdft_ctx cdft_ctx;
+
+typedef struct cdft_params {
+  int nx, ny, nz;  /* lattice points: Lattice(dx, L) with N = L/dx (include/Lattice.h:57-85) */
+  double dx;       /* lattice spacing (dx = dy = dz) */
+  int model;       /* CDFT_* model, or CDFT_MODEL_NONE */
+  double es_A, es_B; /* esFMT coefficients (CDFT_ESFMT only) */
+  double hsd;      /* FMT_Species hard-sphere diameter; <= 0 with lj: Barker-Henderson diameter at kT */
+  int lj;          /* 1: LJ(sigma, eps, rc) with setBH() and Interaction_Interpolation_QF(s, s, &lj, kT) */
+  double lj_sigma, lj_eps, lj_rc, kT;
+  double mu;         /* Species::setChemPotential (beta mu) */
+  double fixed_mass; /* > 0: Species::setFixedMass */
+  int precision;     /* CDFT_FP64 or CDFT_FP32 */
+} cdft_params;
+
+typedef struct cdft_info {
+  double hsd, a_vdw, dV, volume;
+  long N, Nc;
+  int nx, ny, nz;
+} cdft_info;
+
+/* Context life cycle. cdft_create builds the weights (FMT_Species::generateWeights,
+ * src/FMT_Species.cpp:310-496; Interaction_Base::initialize, src/Interaction.cpp:32-52)
+ * and allocates every device buffer of the path; later calls allocate nothing
+ * except the first cdft_fire_init / cdft_ddft_init, which allocate that loop's state. */
+int cdft_create(const cdft_params* p, cdft_ctx** out);
+int cdft_destroy(cdft_ctx* ctx);
+const char* cdft_last_error(const cdft_ctx* ctx);
+int cdft_set_stream(cdft_ctx* ctx, void* cuda_stream);
+int cdft_get_info(const cdft_ctx* ctx, cdft_info* out);
+int cdft_set_precision(cdft_ctx* ctx, int precision);
+
+/* Density::set / Species::set_density (include/Density.h:51-54, include/Species.h:45) */
+int cdft_set_density(cdft_ctx* ctx, const double* rho, int on_device);
+int cdft_get_density(const cdft_ctx* ctx, double* rho, int on_device);
+/* Density::vWall_ external field (include/Density.h:116); NULL clears it */
+int cdft_set_external_field(cdft_ctx* ctx, const double* v, int on_device);
+/* Species::setChemPotential / setFixedMass / getChemPotential (include/Species.h:24-31) */
+int cdft_set_chem_potential(cdft_ctx* ctx, double mu);
+int cdft_set_fixed_mass(cdft_ctx* ctx, double mass);
+int cdft_get_chem_potential(const cdft_ctx* ctx, double* mu);
+
+/* DFT::calculateFreeEnergyAndDerivatives(onlyFex) (include/DFT.h:77, src/DFT.cpp:360-425);
+ * only_fex = 1 leaves out the ideal-gas term, as the reference does.
+ * terms (may be NULL) receives 8 values: Omega, F_id, F_hs, F_mf, F_ext (the
+ * reference's get_f_* of include/DFT.h:121-124), mu after the call, the
+ * convergence monitor max|dF|/dV (Species::get_convergence_monitor,
+ * include/Species.h:55) and the number of atoms. dF (may be NULL) receives N
+ * values. Under fixed mass the context's density is rescaled first, as
+ * Species::beginForceCalculation does (src/Species.cpp:64-71).
+ * Returns CDFT_ERR_ETA where the reference throws Eta_Too_Large_Exception. */
+int cdft_eval(cdft_ctx* ctx, int only_fex, double* terms, double* dF, int on_device);
+
+/* Times each pass of one evaluation in the current precision with CUDA events
+ * on the context's stream (no reference counterpart; used by the benchmark's
+ * roofline). reps evaluations are timed; ms receives the mean time per pass
+ * (CDFT_NPASS values, in the order of the pass list in
+ * classicaldft_gb300/csrc/cdft_kernels.cuh) and bytes the algorithmic bytes each
+ * pass must move. Returns the number of passes through *npass. */
+#define CDFT_NPASS 9
+int cdft_time_passes(cdft_ctx* ctx, int reps, double* ms, double* bytes, int* npass);
+
+/* Bulk thermodynamics of the uniform fluid: out = {DFT::mu_times_beta,
+ * omega_times_beta_over_volume, fhelmholtz_times_beta_over_volume} (src/DFT.cpp:58-115). */
+int cdft_bulk(const cdft_ctx* ctx, double rho, double* out3);
+
+/* Potential1::getHSD(kT) of LJ(sigma, eps, rc) with setBH() (include/Potential1.h:73-83):
+ * the Barker-Henderson diameter int_0^{r0} (1 - exp(-V(r)/kT)) dr, integrated to 1e-15. */
+int cdft_bh_diameter(double sigma, double eps, double rc, double kT, double* out);
+
+/* Real-space weights for inspection: w11 (11*N: eta, s, v0..2, T00, T01, T02,
+ * T11, T12, T22 as FMT_Species holds them) and w_att (N, already / kT); either may be NULL. */
+int cdft_get_weights(const cdft_ctx* ctx, double* w11, double* w_att);
+
+/* fireMinimizer2 (include/Minimizer.h:80-182, src/Minimizer.cpp:117-327). */
+typedef struct cdft_fire_params {
+  double dt, dt_max, dt_min;        /* setTimeStep / setTimeStepMax; defaults 1e-3, 1e-2, 0 */
+  double alpha_start, f_alf;        /* setAlphaStart / setAlphaFac; defaults 0.1, 0.99 */
+  double f_dec, f_inc;              /* 0.5, 1.1 */
+  double force_limit;               /* Minimizer::setForceTerminationCriterion on |vv/V|; default 0.1 */
+  int n_delay, n_p_negative_max;    /* 5, 20 */
+  int initial_delay;                /* 1 */
+} cdft_fire_params;
+
+typedef struct cdft_fire_report {
+  long steps;        /* steps taken by this call */
+  long total_steps;  /* since cdft_fire_init */
+  long calls;        /* F+dF evaluations since cdft_fire_init */
+  double F;          /* Omega at the current state (fireMinimizer2::F_) */
+  double dt, dt_max, alpha;
+  double vv;         /* the energy-rate monitor vv_; Minimizer stops when |vv/V| < force_limit */
+  double fmax;       /* max |dF/dx|/dV in alias coordinates (fmax_) */
+  double resid;      /* max |dOmega/drho| = max|dF|/dV before alias conversion, last accepted evaluation */
+  int backtracks;    /* eta > 1 backtracks seen by this call */
+  int stop;          /* 0 max steps, 1 force limit, 2 residual target */
+} cdft_fire_report;
+
+int cdft_fire_default_params(cdft_fire_params* p);
+/* fireMinimizer2::fireMinimizer2: x = alias(rho), one evaluation, v = 0. */
+int cdft_fire_init(cdft_ctx* ctx, const cdft_fire_params* p);
+/* nsteps calls of fireMinimizer2::step(). */
+int cdft_fire_step(cdft_ctx* ctx, int nsteps, cdft_fire_report* rep);
+/* Minimizer::run / resume loop: steps until |vv/V| < force_limit or max_steps (> 0). */
+int cdft_fire_run(cdft_ctx* ctx, long max_steps, cdft_fire_report* rep);
+/* The same FIRE2 steps, stopping when max|dOmega/drho| <= resid_tol (the
+ * residual the reference's Species::get_convergence_monitor reports) or max_steps. */
+int cdft_fire_run_to_residual(cdft_ctx* ctx, double resid_tol, long max_steps, cdft_fire_report* rep);
+
+/* DDFT integrating-factor dynamics, single species, periodic (include/Minimizer.h:189-266, src/DDFT.cpp:42-351). */
+typedef struct cdft_ddft_report {
+  long steps;
+  double F;        /* Omega after the last step */
+  double time;     /* DDFT::get_time */
+  double dt;       /* current time step */
+  double mass;     /* sum rho dV (compensated FP64) */
+  double rhs_max;  /* DDFT::get_convergence_monitor (RHS_max_) */
+  int restarts;    /* time-step reductions in this call */
+} cdft_ddft_report;
+
+/* DDFT::DDFT then setTimeStep(dt), set_max_time_step(dt_max), set_tolerence_fixed_point(tol). */
+int cdft_ddft_init(cdft_ctx* ctx, double dt, double dt_max, double tol_fixed_point);
+/* nsteps calls of DDFT::step(). */
+int cdft_ddft_step(cdft_ctx* ctx, int nsteps, cdft_ddft_report* rep);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
