@@ -43,6 +43,11 @@ def workload():
             "reductions": "fp64 compensated", "l2": "flushed between timed steps (256 MB write)"}
 
 
+# DRAM bytes per launch (read + write) from one ncu capture of the named kernel on
+# this workload (profiles/k_xbackconv_128_fp32.md); None where none was taken.
+NCU_TRAFFIC = {("xbackconv", "fp32"): 153.4e6 + 3.6e6}
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -202,7 +207,7 @@ def main():
     peak, peak_kind = measured_peaks()
     top = max(passes, key=lambda p: p["ms"])
     achieved = top["bytes"] / (top["ms"] * 1e-3) / 1e9
-    N = np.prod(SHAPE)
+    N = int(np.prod(SHAPE))
     Nc = SHAPE[0] * SHAPE[1] * (SHAPE[2] // 2 + 1)
     B_dft = 4 * (N * (4 * 11 + 3) + Nc * (2 * 11 + 11))
     line = {"metric": METRIC, "value": world * 1e3 / ms32, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
@@ -213,7 +218,7 @@ def main():
                     "d2h_bytes_per_step": int(N * 8 + 8 * 8)},
             "roofline": {"bound": "hbm", "kernel": top["pass"], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": None},
+                         "traffic": NCU_TRAFFIC.get((top["pass"], "fp32"))},
             "eval_roofline": {"algorithmic_bytes_per_eval": B_dft, "achieved_gbs": B_dft / (ms32 * 1e-3) / 1e9,
                               "frac": B_dft / (ms32 * 1e-3) / 1e9 / peak},
             "fp64_evals_per_s": world * 1e3 / ms64, "fp64_ms_per_step": ms64,

@@ -31,7 +31,7 @@ C_FUNCTIONS = [
     "cdft_set_density", "cdft_get_density", "cdft_set_external_field", "cdft_set_chem_potential",
     "cdft_set_fixed_mass", "cdft_get_chem_potential", "cdft_eval", "cdft_bulk", "cdft_bh_diameter",
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
-    "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes",
+    "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -107,6 +107,7 @@ def lib():
             "cdft_fire_run_to_residual": ([vp, d, ctypes.c_long, P(FireReport)], i),
             "cdft_ddft_init": ([vp, d, d, d], i), "cdft_ddft_step": ([vp, i, P(DdftReport)], i),
             "cdft_time_passes": ([vp, i, dp, dp, P(i)], i),
+            "cdft_fmt_weights": ([i, i, i, d, d, dp], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -126,6 +127,15 @@ def bh_diameter(sigma, eps, rc, kT):
     if rc_:
         raise CDFTError(rc_, "bad arguments")
     return out.value
+
+
+def fmt_weights(shape, dx, hsd):
+    """FMT_Species::generateWeights on the host: the 11 real-space weight arrays."""
+    w = np.zeros((11,) + tuple(shape))
+    rc_ = lib().cdft_fmt_weights(shape[0], shape[1], shape[2], dx, hsd, _dptr(w))
+    if rc_:
+        raise CDFTError(rc_, "bad arguments (hsd < dx?)")
+    return w
 
 
 TERM_NAMES = ("Omega", "F_id", "F_hs", "F_mf", "F_ext", "mu", "resid", "N")

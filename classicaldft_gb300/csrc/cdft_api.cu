@@ -559,6 +559,19 @@ int cdft_bh_diameter(double sigma, double eps, double rc, double kT, double* out
   return CDFT_OK;
 }
 
+int cdft_fmt_weights(int nx, int ny, int nz, double dx, double hsd, double* w11) {
+  if (!w11 || nx < 1 || ny < 1 || nz < 1 || !(dx > 0)) return CDFT_ERR_ARG;
+  try {
+    std::vector<double> w[11];
+    fmt_weights_real(nx, ny, nz, dx, hsd, w);
+    const long N = (long)nx * ny * nz;
+    for (int a = 0; a < 11; ++a) std::memcpy(w11 + a * N, w[a].data(), N * sizeof(double));
+  } catch (std::exception&) {
+    return CDFT_ERR_ARG;
+  }
+  return CDFT_OK;
+}
+
 int cdft_get_weights(const cdft_ctx* c, double* w11, double* w_att) {
   if (!c) return CDFT_ERR_ARG;
   const long N = c->info.N;

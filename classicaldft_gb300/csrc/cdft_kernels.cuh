@@ -330,8 +330,7 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
   }
   C* res = block_fft<+1, T>(b0, b1, L, LP, pz, tw);
   C* other = (res == b0) ? b1 : b0;
-  Acc acc;
-  acc.init();
+  double psum = 0.0;  // per-thread partial (a few points); merged with compensation below
   unsigned st = 0;
   for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
     const int r = e / nz, k = e - r * nz;
@@ -346,7 +345,7 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
     const T phi = fmt_phi_point<T, MODEL>(nv, hsd, esA, esB);
     if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
     if (!isfinite(phi)) st |= 2u;
-    acc.add((double)phi);
+    psum += (double)phi;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       const T im = (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0;
@@ -354,6 +353,9 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
     }
   }
   if (st) atomicOr(status, st);
+  Acc acc;
+  acc.init();
+  acc.add(psum);
   block_reduce_store<1>(&acc, part, blockIdx.x);
   C* res2 = block_fft<-1, T>(other, res, L, LP, pz, tw);
   for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
@@ -397,31 +399,39 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     }
     res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
   }
-  Acc acc[4];
-#pragma unroll
-  for (int v = 0; v < 4; ++v) acc[v].init();
+  // Pointwise terms in the bulk precision T (FP64 in FP64 mode); each thread
+  // keeps plain FP64 partials of its few points, merged with compensation.
+  double ps[4] = {0.0, 0.0, 0.0, 0.0};
+  const T dVt = (T)dV, mut = (T)mu;
   for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
     const int rr = e / nz, k = e - rr * nz;
     const long row = 2 * pair0 + rr;
     if (row >= d.rows) continue;
     const long p = row * nz + k;
-    const double r0 = rho[p];
-    const double lr = log(r0);
-    double h = 0;
+    const double r0d = rho[p];
+    const T r0 = (T)r0d;
+    const T lr = log(r0);
+    T h = 0;
     if (have_fmt_or_mf) {
       const C z = res[(rr >> 1) * LP + k];
-      h = (double)((rr & 1) ? z.y : z.x);
+      h = (rr & 1) ? z.y : z.x;
     }
-    const double ve = vext ? vext[p] : 0.0;
-    double f = ideal ? lr * dV : 0.0;
-    f += h * dV;
-    f += ve * dV;
-    f += -mu * dV;
-    dF[p] = f;
-    if (ideal) acc[0].add((r0 * lr - r0) * dV);
-    acc[1].add(r0);
-    acc[2].add(ve * r0);
-    acc[3].add(f * r0);
+    const T ve = vext ? (T)vext[p] : (T)0;
+    T f = ideal ? lr * dVt : (T)0;
+    f += h * dVt;
+    f += ve * dVt;
+    f += -mut * dVt;
+    dF[p] = (double)f;
+    if (ideal) ps[0] += (double)((r0 * lr - r0) * dVt);
+    ps[1] += r0d;
+    ps[2] += (double)(ve * r0);
+    ps[3] += (double)f * r0d;
+  }
+  Acc acc[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    acc[v].init();
+    acc[v].add(ps[v]);
   }
   block_reduce_store<4>(acc, part, blockIdx.x);
 }

@@ -37,7 +37,10 @@ template <class F>
 double gauss10(F f, double a, double b) {
   const double c = 0.5 * (a + b), h = 0.5 * (b - a);
   double s = 0;
-  for (int i = 0; i < 5; ++i) s += kGLw[i] * (f(c - h * kGLx[i]) + f(c + h * kGLx[i]));
+  for (int i = 0; i < 5; ++i) {
+    s += kGLw[i] * f(c - h * kGLx[i]);
+    s += kGLw[i] * f(c + h * kGLx[i]);
+  }
   return s * h;
 }
 template <class F>

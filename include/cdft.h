@@ -111,6 +111,11 @@ int cdft_bulk(const cdft_ctx* ctx, double rho, double* out3);
  * the Barker-Henderson diameter int_0^{r0} (1 - exp(-V(r)/kT)) dr, integrated to 1e-15. */
 int cdft_bh_diameter(double sigma, double eps, double rc, double kT, double* out);
 
+/* FMT_Species::generateWeights on the host (src/FMT_Species.cpp:310-496), no
+ * context or GPU needed: the 11 real-space weight arrays (11*nx*ny*nz values) of a
+ * sphere of diameter hsd on an nx*ny*nz lattice of spacing dx. */
+int cdft_fmt_weights(int nx, int ny, int nz, double dx, double hsd, double* w11);
+
 /* Real-space weights for inspection: w11 (11*N: eta, s, v0..2, T00, T01, T02,
  * T11, T12, T22 as FMT_Species holds them) and w_att (N, already / kT); either may be NULL. */
 int cdft_get_weights(const cdft_ctx* ctx, double* w11, double* w_att);

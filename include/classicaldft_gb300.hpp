@@ -1,0 +1,334 @@
+// classicaldft_gb300.hpp — the reference's C++ class API over the GB300 C ABI.
+//
+// Header-only. Code written against jimlutsko/classicalDFT's DFT / Species /
+// FMT / Interaction / Minimizer classes for the free-energy-and-derivative
+// path compiles against this header with the same class names and method
+// signatures, and runs on the GPU through include/cdft.h
+// (link with classicaldft_gb300/libcdft.so and the CUDA runtime).
+//
+// Covered: Lattice/Density (include/Lattice.h, include/Density.h), FMT models
+// Rosenfeld / RSLT / esFMT / WhiteBearI / WhiteBearII (include/FMT.h),
+// FMT_Species (include/Species.h), LJ with setBH (include/Potential1.h),
+// Interaction_Interpolation_QF (include/Interaction.h), DFT (include/DFT.h),
+// fireMinimizer2 and DDFT (include/Minimizer.h), Eta_Too_Large_Exception.
+#ifndef CLASSICALDFT_GB300_HPP
+#define CLASSICALDFT_GB300_HPP
+
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cdft.h"
+
+namespace classicaldft_gb300 {
+
+class Eta_Too_Large_Exception : public std::runtime_error {
+ public:
+  Eta_Too_Large_Exception() : std::runtime_error("Eta too large in FMT::dPHI") {}
+};
+
+inline void check(int code, const cdft_ctx* ctx) {
+  if (code == CDFT_OK) return;
+  if (code == CDFT_ERR_ETA) throw Eta_Too_Large_Exception();
+  throw std::runtime_error(std::string("classicaldft_gb300: ") + (ctx ? cdft_last_error(ctx) : "error") + " (code " +
+                           std::to_string(code) + ")");
+}
+
+// include/Lattice.h:57-134
+class Lattice {
+ public:
+  Lattice(double dx, const double L[]) : dx_(dx) {
+    for (int a = 0; a < 3; ++a) {
+      n_[a] = long((L[a] + 1e-8 * dx) / dx);
+      if (std::fabs(L[a] - n_[a] * dx) > 1e-5 * dx) throw std::runtime_error("Box length incommensurate with lattice");
+    }
+  }
+  long Nx() const { return n_[0]; }
+  long Ny() const { return n_[1]; }
+  long Nz() const { return n_[2]; }
+  long Ntot() const { return n_[0] * n_[1] * n_[2]; }
+  long Nout() const { return n_[0] * n_[1] * (n_[2] / 2 + 1); }
+  double getDX() const { return dx_; }
+  double dV() const { return dx_ * dx_ * dx_; }
+  double getVolume() const { return Ntot() * dV(); }
+  double getX(int i) const { return dx_ * (i - double(n_[0]) / 2); }
+  double getY(int i) const { return dx_ * (i - double(n_[1]) / 2); }
+  double getZ(int i) const { return dx_ * (i - double(n_[2]) / 2); }
+  long pos(int i, int j, int k) const { return k + n_[2] * (j + n_[1] * i); }
+
+ protected:
+  double dx_;
+  long n_[3];
+};
+
+// include/Density.h:35-118 (the host copy of the field; the GPU holds the working copy)
+class Density : public Lattice {
+ public:
+  Density(double dx, const double L[]) : Lattice(dx, L), rho_(Ntot(), 0.0) {}
+  void set(long pos, double v) { rho_[pos] = v; }
+  void set(int i, int j, int k, double v) { rho_[pos(i, j, k)] = v; }
+  void set(const std::vector<double>& x) { rho_ = x; }
+  double get(long pos) const { return rho_[pos]; }
+  double getNumberAtoms() const {
+    double s = 0, c = 0;
+    for (double x : rho_) {
+      double t = s + x;
+      c += (std::fabs(s) >= std::fabs(x)) ? (s - t) + x : (x - t) + s;
+      s = t;
+    }
+    return (s + c) * dV();
+  }
+  const double* data() const { return rho_.data(); }
+  double* data() { return rho_.data(); }
+
+ private:
+  std::vector<double> rho_;
+};
+
+// include/FMT.h:139-643
+class FMT {
+ public:
+  virtual ~FMT() {}
+  virtual int model() const = 0;
+  virtual double A() const { return 1.0; }
+  virtual double B() const { return 0.0; }
+  bool needsTensor() const { return model() >= CDFT_ESFMT; }
+};
+class Rosenfeld : public FMT { public: int model() const override { return CDFT_ROSENFELD; } };
+class RSLT : public FMT { public: int model() const override { return CDFT_RSLT; } };
+class esFMT : public FMT {
+ public:
+  esFMT(double A = 1, double B = 0) : A_(A), B_(B) {}
+  int model() const override { return CDFT_ESFMT; }
+  double A() const override { return A_; }
+  double B() const override { return B_; }
+ private:
+  double A_, B_;
+};
+class WhiteBearI : public FMT { public: int model() const override { return CDFT_WHITEBEAR_I; } };
+class WhiteBearII : public FMT { public: int model() const override { return CDFT_WHITEBEAR_II; } };
+
+// include/Potential1.h:136-189 (Barker-Henderson split only)
+class LJ {
+ public:
+  LJ(double sigma, double eps, double rcut) : sigma_(sigma), eps_(eps), rcut_(rcut) {}
+  void setBH() { bh_ = true; }
+  double getHSD(double kT) const {
+    if (!bh_) throw std::runtime_error("only the Barker-Henderson split is on the GPU path");
+    double d = 0;
+    check(cdft_bh_diameter(sigma_, eps_, rcut_, kT, &d), nullptr);
+    return d;
+  }
+  double sigma() const { return sigma_; }
+  double eps() const { return eps_; }
+  double getRcut() const { return rcut_; }
+  bool isBH() const { return bh_; }
+ private:
+  double sigma_, eps_, rcut_;
+  bool bh_ = false;
+};
+
+// include/Species.h:13-380
+class FMT_Species {
+ public:
+  FMT_Species(Density& density, double hsd, double mu = 0, int seq = -1) : density_(density), hsd_(hsd), mu_(mu) {
+    (void)seq;
+  }
+  void setChemPotential(double m) { mu_ = m; fixedMass_ = -1; }
+  double getChemPotential() const { return mu_; }
+  void setFixedMass(double m) { fixedMass_ = m; if (m > 0.0) mu_ = 0.0; }
+  bool is_mass_fixed() const { return fixedMass_ > 0; }
+  double getHSD() const { return hsd_; }
+  Density& getDensity() { return density_; }
+  const Density& getLattice() const { return density_; }
+  std::vector<double>& getDF() { return dF_; }
+  double get_convergence_monitor() const {
+    double m = 0;
+    for (double x : dF_) m = std::max(m, std::fabs(x));
+    return m / density_.dV();
+  }
+  double fixedMass() const { return fixedMass_; }
+  void setMuInternal(double m) { mu_ = m; }
+
+ private:
+  Density& density_;
+  double hsd_, mu_;
+  double fixedMass_ = -1;
+  std::vector<double> dF_;
+};
+
+// include/Interaction.h:416-441 (self interaction of one species)
+class Interaction_Interpolation_QF {
+ public:
+  Interaction_Interpolation_QF(FMT_Species* s1, FMT_Species* s2, LJ* v, double kT) : s_(s1), v_(v), kT_(kT) {
+    if (s1 != s2) throw std::runtime_error("only the self interaction of one species is on the GPU path");
+  }
+  FMT_Species* species() const { return s_; }
+  LJ* potential() const { return v_; }
+  double kT() const { return kT_; }
+ private:
+  FMT_Species* s_;
+  LJ* v_;
+  double kT_;
+};
+
+// include/DFT.h:44-190
+class DFT {
+ public:
+  explicit DFT(FMT_Species* s = nullptr, int precision = CDFT_FP64) : s_(s), precision_(precision) {}
+  ~DFT() { if (ctx_) cdft_destroy(ctx_); }
+  DFT(const DFT&) = delete;
+  DFT& operator=(const DFT&) = delete;
+
+  void addSpecies(FMT_Species* s) { s_ = s; reset(); }
+  void addHardCoreContribution(FMT* fmt) { fmt_ = fmt; reset(); }
+  void addInteraction(Interaction_Interpolation_QF* i) { inter_ = i; reset(); }
+
+  double calculateFreeEnergyAndDerivatives(bool onlyFex) {
+    push();
+    double t[8];
+    std::vector<double>& dF = s_->getDF();
+    dF.resize(s_->getDensity().Ntot());
+    int rc = cdft_eval(context(), onlyFex ? 1 : 0, t, dF.data(), 0);
+    check(rc, ctx_);
+    pull(t);
+    return t[0];
+  }
+  double mu_times_beta(double rho) { double o[3]; check(cdft_bulk(context(), rho, o), ctx_); return o[0]; }
+  double omega_times_beta_over_volume(double rho) { double o[3]; check(cdft_bulk(context(), rho, o), ctx_); return o[1]; }
+  double fhelmholtz_times_beta_over_volume(double rho) { double o[3]; check(cdft_bulk(context(), rho, o), ctx_); return o[2]; }
+  double get_f_id() const { return F_[0]; }
+  double get_f_hs() const { return F_[1]; }
+  double get_f_mf() const { return F_[2]; }
+  double get_f_ext() const { return F_[3]; }
+  std::vector<double>& getDF(int) { return s_->getDF(); }
+  FMT_Species* getSpecies(int) const { return s_; }
+  double get_convergence_monitor() const { return s_->get_convergence_monitor(); }
+
+  // GPU handle for the minimizers
+  cdft_ctx* context() {
+    if (!ctx_) {
+      cdft_params p;
+      std::memset(&p, 0, sizeof(p));
+      const Density& d = s_->getDensity();
+      p.nx = (int)d.Nx(); p.ny = (int)d.Ny(); p.nz = (int)d.Nz(); p.dx = d.getDX();
+      p.model = fmt_ ? fmt_->model() : CDFT_MODEL_NONE;
+      p.es_A = fmt_ ? fmt_->A() : 1; p.es_B = fmt_ ? fmt_->B() : 0;
+      p.hsd = s_->getHSD();
+      if (inter_) {
+        p.lj = 1; p.lj_sigma = inter_->potential()->sigma(); p.lj_eps = inter_->potential()->eps();
+        p.lj_rc = inter_->potential()->getRcut(); p.kT = inter_->kT();
+      }
+      p.mu = s_->getChemPotential();
+      p.fixed_mass = s_->fixedMass();
+      p.precision = precision_;
+      check(cdft_create(&p, &ctx_), nullptr);
+    }
+    return ctx_;
+  }
+  void push() {
+    cdft_ctx* c = context();
+    check(cdft_set_density(c, s_->getDensity().data(), 0), c);
+    if (s_->is_mass_fixed()) check(cdft_set_fixed_mass(c, s_->fixedMass()), c);
+    else check(cdft_set_chem_potential(c, s_->getChemPotential()), c);
+  }
+  void pull_density() { check(cdft_get_density(ctx_, s_->getDensity().data(), 0), ctx_); }
+
+ private:
+  void reset() { if (ctx_) { cdft_destroy(ctx_); ctx_ = nullptr; } }
+  void pull(const double* t) {
+    F_[0] = t[1]; F_[1] = t[2]; F_[2] = t[3]; F_[3] = t[4];
+    s_->setMuInternal(t[5]);
+    pull_density();  // fixed mass rescales the density, as the reference's Density does
+  }
+  FMT_Species* s_;
+  FMT* fmt_ = nullptr;
+  Interaction_Interpolation_QF* inter_ = nullptr;
+  int precision_;
+  cdft_ctx* ctx_ = nullptr;
+  double F_[4] = {0, 0, 0, 0};
+};
+
+// include/Minimizer.h:80-182
+class fireMinimizer2 {
+ public:
+  explicit fireMinimizer2(DFT* dft) : dft_(dft) { cdft_fire_default_params(&p_); }
+  void setTimeStep(double dt) { p_.dt = dt; }
+  void setTimeStepMax(double dt) { p_.dt_max = dt; }
+  void setAlphaStart(double a) { p_.alpha_start = a; }
+  void setAlphaFac(double a) { p_.f_alf = a; }
+  void setForceTerminationCriterion(double v) { p_.force_limit = v; }
+  double step() {
+    start();
+    check(cdft_fire_step(dft_->context(), 1, &r_), dft_->context());
+    return r_.F;
+  }
+  void run(long maxSteps = -1) {
+    start();
+    check(cdft_fire_run(dft_->context(), maxSteps, &r_), dft_->context());
+    dft_->pull_density();
+  }
+  void resume(long maxSteps = -1) { run(maxSteps); }
+  double getF() const { return r_.F; }
+  double get_convergence_monitor() const { return std::fabs(r_.vv / dft_->getSpecies(0)->getDensity().getVolume()); }
+  const cdft_fire_report& report() const { return r_; }
+
+ private:
+  void start() {
+    if (!started_) {
+      dft_->push();
+      check(cdft_fire_init(dft_->context(), &p_), dft_->context());
+      started_ = true;
+    }
+  }
+  DFT* dft_;
+  cdft_fire_params p_;
+  cdft_fire_report r_{};
+  bool started_ = false;
+};
+
+// include/Minimizer.h:189-266 (periodic boundaries)
+class DDFT {
+ public:
+  DDFT(DFT* dft, bool showGraphics = false) : dft_(dft) {
+    (void)showGraphics;
+    const double dx = dft->getSpecies(0)->getDensity().getDX();
+    dt_ = 1e-4 * dx * dx;
+  }
+  void setTimeStep(double dt) { dt_ = dt; }
+  void set_max_time_step(double t) { dt_max_ = t; }
+  void set_tolerence_fixed_point(double e) { tol_ = e; }
+  double step() {
+    start();
+    check(cdft_ddft_step(dft_->context(), 1, &r_), dft_->context());
+    dft_->pull_density();
+    return r_.F;
+  }
+  void run(long maxSteps) {
+    start();
+    check(cdft_ddft_step(dft_->context(), (int)maxSteps, &r_), dft_->context());
+    dft_->pull_density();
+  }
+  double get_time() const { return r_.time; }
+  double getTimeStep() const { return r_.dt > 0 ? r_.dt : dt_; }
+  double get_convergence_monitor() const { return r_.rhs_max; }
+
+ private:
+  void start() {
+    if (!started_) {
+      dft_->push();
+      check(cdft_ddft_init(dft_->context(), dt_, dt_max_, tol_), dft_->context());
+      started_ = true;
+    }
+  }
+  DFT* dft_;
+  double dt_, dt_max_ = 1.0, tol_ = 1e-4;
+  cdft_ddft_report r_{};
+  bool started_ = false;
+};
+
+}  // namespace classicaldft_gb300
+
+#endif

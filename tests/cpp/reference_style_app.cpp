@@ -1,0 +1,38 @@
+// A reference-style application (the call sequence of a classicalDFT app) built
+// against include/classicaldft_gb300.hpp: config 1 (hard spheres, WhiteBearI,
+// 32^3 at dx = 0.2, rho = 0.7 (1 + noise)), one evaluation, then FIRE2 steps.
+// Prints "Omega F_hs mu steps F_final" for the test to compare.
+#include <cstdint>
+#include <cstdio>
+
+#include "classicaldft_gb300.hpp"
+
+using namespace classicaldft_gb300;
+
+static double splitmix_uniform(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  z = z ^ (z >> 31);
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+int main(int argc, char** argv) {
+  int fire_steps = argc > 1 ? std::atoi(argv[1]) : 20;
+  double L[3] = {6.4, 6.4, 6.4};
+  Density density(0.2, L);
+  uint64_t seed = 20240601;
+  for (long p = 0; p < density.Ntot(); ++p) density.set(p, 0.7 * (1.0 + 0.05 * (2.0 * splitmix_uniform(seed) - 1.0)));
+  FMT_Species species(density, 1.0, 0.0);
+  WhiteBearI fmt;
+  DFT dft(&species);
+  dft.addHardCoreContribution(&fmt);
+  species.setChemPotential(dft.mu_times_beta(0.7));
+  double F = dft.calculateFreeEnergyAndDerivatives(false);
+  double Fhs = dft.get_f_hs();
+  fireMinimizer2 fire(&dft);
+  fire.setForceTerminationCriterion(0.0);
+  fire.run(fire_steps);
+  std::printf("%.17g %.17g %.17g %ld %.17g\n", F, Fhs, species.getChemPotential(), fire.report().total_steps, fire.getF());
+  return 0;
+}

@@ -1,0 +1,42 @@
+"""The reference's C++ class API over the C ABI (include/classicaldft_gb300.hpp):
+a reference-style app compiles and links here; on a GPU it reproduces the
+reference's config-1 evaluation and FIRE2 trajectory."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+APP = os.path.join(ROOT, "tests", "cpp", "reference_style_app.cpp")
+
+
+def build_app(out):
+    import classicaldft_gb300 as cd
+    if not os.path.exists(cd.LIB_PATH):
+        from classicaldft_gb300 import build
+        build.build()
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), APP, "-o", out,
+           "-L", os.path.dirname(cd.LIB_PATH), "-lcdft", "-Wl,-rpath," + os.path.dirname(cd.LIB_PATH),
+           "-L/usr/local/cuda/lib64", "-lcudart"]
+    subprocess.check_call(cmd)
+
+
+def test_reference_style_app_builds(tmp_path):
+    build_app(str(tmp_path / "app"))
+    assert os.path.exists(str(tmp_path / "app"))
+
+
+@pytest.mark.gpu
+def test_reference_style_app_runs_config1(tmp_path):
+    exe = str(tmp_path / "app")
+    build_app(exe)
+    out = subprocess.check_output([exe, "20"], text=True).split()
+    F, Fhs, mu, steps, Ffin = float(out[0]), float(out[1]), float(out[2]), int(out[3]), float(out[4])
+    g = golden("eval_hs32")
+    assert abs(F - g["hs32.Omega"][0]) <= 1e-12 * abs(F)
+    assert abs(Fhs - g["hs32.F_hs"][0]) <= 1e-12 * abs(Fhs)
+    fire = golden("fire_hs32")
+    assert steps == 20
+    assert abs(Ffin - fire["fire32.F"][19]) <= 1e-12 * abs(Ffin)

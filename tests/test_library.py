@@ -33,10 +33,10 @@ def test_library_exports_every_declared_symbol():
 def test_bh_diameter_matches_reference(oracle):
     import classicaldft_gb300 as cd
     g = golden("bulk")
-    # the same integral to 1e-15 (summation order differs in the last bit)
+    # the same integral to 1e-15; the product and the oracle sum in the same order
     assert cd.bh_diameter(1.0, 1.0, 3.0, 0.8) == pytest.approx(g["bulk.lj_hsd_kT0.8"][0], rel=1e-15)
     assert cd.bh_diameter(1.0, 1.0, 3.0, 1.0) == pytest.approx(g["bulk.lj_hsd_kT1.0"][0], rel=1e-15)
-    assert cd.bh_diameter(1.0, 1.0, 2.5, 0.7) == pytest.approx(oracle.bh_diameter(2.5, 0.7), rel=1e-15)
+    assert cd.bh_diameter(1.0, 1.0, 2.5, 0.7) == oracle.bh_diameter(2.5, 0.7)
 
 
 def test_lattice_rules():
@@ -46,3 +46,14 @@ def test_lattice_rules():
     assert L.getX(0) == pytest.approx(-3.2)
     with pytest.raises(RuntimeError):
         cd.Lattice(0.3, [1.0, 1.0, 1.0])
+
+
+@pytest.mark.parametrize("tag,dx,n,hsd", [("w_d1_dx0.2_n16", 0.2, 16, 1.0), ("w_d0.9786_dx0.1_n16", 0.1, 16, 0.9786),
+                                          ("w_d1.3_dx0.25_n12", 0.25, 12, 1.3)])
+def test_product_weights_match_reference(tag, dx, n, hsd):
+    import numpy as np
+    import classicaldft_gb300 as cd
+    g = golden("weights")
+    w = cd.fmt_weights((n, n, n), dx, hsd)
+    for a in range(11):
+        np.testing.assert_allclose(w[a].ravel(), g[tag + ".w%d" % a], rtol=0, atol=1e-14)
