@@ -31,7 +31,7 @@ C_FUNCTIONS = [
     "cdft_set_density", "cdft_get_density", "cdft_set_external_field", "cdft_set_chem_potential",
     "cdft_set_fixed_mass", "cdft_get_chem_potential", "cdft_eval", "cdft_bulk", "cdft_bh_diameter",
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
-    "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights",
+    "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -108,6 +108,7 @@ def lib():
             "cdft_ddft_init": ([vp, d, d, d], i), "cdft_ddft_step": ([vp, i, P(DdftReport)], i),
             "cdft_time_passes": ([vp, i, dp, dp, P(i)], i),
             "cdft_fmt_weights": ([i, i, i, d, d, dp], i),
+            "cdft_number_of_atoms_noalloc": ([vp, ctypes.c_long, d, vp, dp], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

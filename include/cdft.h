@@ -170,6 +170,20 @@ int cdft_ddft_init(cdft_ctx* ctx, double dt, double dt_max, double tol_fixed_poi
 /* nsteps calls of DDFT::step(). */
 int cdft_ddft_step(cdft_ctx* ctx, int nsteps, cdft_ddft_report* rep);
 
+/* Number of atoms, sum(rho) * dV with FP64 compensated summation, of a density
+ * that is already on the device (rho: n doubles, a device pointer), written to
+ * *out (host). Allocates nothing: for callers that cannot call cudaMalloc (an
+ * application passing only pointers from its own memory pool, or code that must
+ * not allocate between launches it records into a CUDA graph). No counterpart in
+ * the reference. Its scratch is a 64 KiB file-scope device array that every GPU
+ * loading this library holds until exit; n above 2^25 (33,554,432) points is
+ * rejected with CDFT_ERR_ARG. The first call on a device resolves the array's
+ * address there (make it before any stream capture). Calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. The
+ * work runs on `stream` (NULL: the legacy default stream), which is synchronised
+ * before returning. */
+int cdft_number_of_atoms_noalloc(const double* rho, long n, double dV, void* stream, double* out);
+
 #ifdef __cplusplus
 }
 #endif
