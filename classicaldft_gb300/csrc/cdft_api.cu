@@ -185,8 +185,8 @@ struct FDdftRhs {
 template <class T>
 __global__ void k_ddft_prop(const typename Cx<T>::type* __restrict__ rk, const typename Cx<T>::type* __restrict__ R0,
                             const typename Cx<T>::type* __restrict__ R1, typename Cx<T>::type* __restrict__ out,
-                            const double* __restrict__ fac, int nx, int ny, int nzc, double dt) {
-  const long Nc = (long)nx * ny * nzc;
+                            const double* __restrict__ fac, int nx, int ny, int nzc, int pz, double dt) {
+  const long Nc = (long)nx * ny * pz;  // padded rows; columns kz >= nzc carry no data
   const double* Lx = fac;
   const double* Ly = Lx + nx;
   const double* Lz = Ly + ny;
@@ -194,15 +194,19 @@ __global__ void k_ddft_prop(const typename Cx<T>::type* __restrict__ rk, const t
   const double* fy = fx + nx;
   const double* fz = fy + ny;
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Nc; p += (long)gridDim.x * blockDim.x) {
-    const int iz = (int)(p % nzc);
-    const long t = p / nzc;
+    const int iz = (int)(p % pz);
+    const long t = p / pz;
     const int iy = (int)(t % ny), ix = (int)(t / ny);
+    if (iz >= nzc) {
+      out[p] = mk<T>(0, 0);
+      continue;
+    }
     const double Lam = Lx[ix] + Ly[iy] + Lz[iz];
     const double e = fx[ix] * fy[iy] * fz[iz];
     const double U0 = e;
     const double U1 = (p == 0 ? dt : (e - 1) / Lam);
     const double U2 = (p == 0 ? dt / 2 : (e - 1 - dt * Lam) / (Lam * Lam * dt));
-    const typename Cx<T>::type x = rk[p], a = R0[p], b = R1[p];
+    const typename Cx<T>::type x = rk[p], a = R0[p], b = R1[p];  // p == 0 is the k = 0 mode in either layout
     out[p] = mk<T>((T)(U0 * (double)x.x + U1 * (double)a.x + U2 * ((double)b.x - (double)a.x)),
                    (T)(U0 * (double)x.y + U1 * (double)a.y + U2 * ((double)b.y - (double)a.y)));
   }
@@ -335,6 +339,7 @@ static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
   EvalTerms t;
   if (c->precision == CDFT_FP64) rc = c->e64->eval(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, &t, c->stream);
   else rc = c->e32->eval(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, &t, c->stream);
+  if (rc == 3) return fail(c, CDFT_ERR_TIMEOUT, "a tensor copy did not complete within its wait limit");
   if (rc) return fail(c, CDFT_ERR_CUDA, std::string("evaluation launch failed: ") + cudaGetErrorString(cudaGetLastError()));
   if (c->fixed_mass > 0) {  // src/Species.cpp:97-109
     c->mu = t.sum_dF_rho / c->fixed_mass;
@@ -794,7 +799,8 @@ static int ddft_r2c(cdft_ctx* c, const double* real, void* spec) {
 int cdft_ddft_init(cdft_ctx* c, double dt, double dt_max, double tol) {
   if (!c) return CDFT_ERR_ARG;
   if (c->p.model < 0 && !c->p.lj) return fail(c, CDFT_ERR_ARG, "DDFT needs an FMT model or an interaction");
-  const long N = c->info.N, Nc = c->info.Nc;
+  const long N = c->info.N;
+  const long Nc = c->precision == CDFT_FP64 ? c->e64->spectrum_len() : c->e32->spectrum_len();  // padded rows
   const size_t cs = sizeof(double2);  // large enough for either precision
   if (!c->dd0) {
     CUDA_OR_FAIL(c, cudaMalloc(&c->dd0, N * sizeof(double)));
@@ -884,14 +890,15 @@ static int ddft_one_step(cdft_ctx* c, int* restarts) {
       rc = ddft_rhs(c, c->dd1, c->R1k, nullptr);
       if (rc) return rc;
       const int nx = c->p.nx, ny = c->p.ny, nzc = c->p.nz / 2 + 1;
-      const unsigned g = grid_for(c->info.Nc);
+      const int pz = c->precision == CDFT_FP64 ? c->e64->pitch() : c->e32->pitch();
+      const unsigned g = grid_for((long)nx * ny * pz);
       if (c->precision == CDFT_FP64) {
         k_ddft_prop<double><<<g, 256, 0, c->stream>>>((const double2*)c->rk0, (const double2*)c->R0k, (const double2*)c->R1k, (double2*)c->work,
-                                                       c->dfac, nx, ny, nzc, c->ddft_dt);
+                                                       c->dfac, nx, ny, nzc, pz, c->ddft_dt);
         c->e64->c2r((const double2*)c->work, c->ddn, 1.0 / (double)N, c->stream);
       } else {
         k_ddft_prop<float><<<g, 256, 0, c->stream>>>((const float2*)c->rk0, (const float2*)c->R0k, (const float2*)c->R1k, (float2*)c->work,
-                                                      c->dfac, nx, ny, nzc, c->ddft_dt);
+                                                      c->dfac, nx, ny, nzc, pz, c->ddft_dt);
         c->e32->c2r((const float2*)c->work, c->ddn, 1.0f / (float)N, c->stream);
       }
       double red[2];

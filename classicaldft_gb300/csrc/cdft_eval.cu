@@ -5,6 +5,7 @@
 #include <cstring>
 #include "cdft_internal.h"
 #include "cdft_kernels.cuh"
+#include "cdft_kernels_tma.cuh"
 
 namespace cdft {
 
@@ -147,26 +148,161 @@ static void r2c_f64(const double* in, double2* out, const Dims& d, FFTTable* tx,
   k_cols_fft<double, -1><<<dim3((unsigned)(((long)d.nx * d.nzc + TC - 1) / TC), 1), 256, sm_y, s>>>(out, 0, 1, d, ty->plan, twp<double>(ty), TC);
   const size_t sm_x = smem_bytes(TC, d.nx, sizeof(double2), 2);
   set_smem<double>(k_cols_fft<double, -1>, std::max(sm_x, sm_y));
-  k_cols_fft<double, -1><<<dim3((unsigned)(((long)d.ny * d.nzc + TC - 1) / TC), 1), 256, sm_x, s>>>(out, 0, 0, d, tx->plan, twp<double>(tx), TC);
+  k_cols_fft<double, -1><<<dim3((unsigned)(((long)d.ny * d.pz + TC - 1) / TC), 1), 256, sm_x, s>>>(out, 0, 0, d, tx->plan, twp<double>(tx), TC);
+}
+
+
+// ------------------------------------------------------- tensor maps ---
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                                   const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// rank-dimensional map over 4- or 8-byte elements; dims[0] innermost, strides in bytes for dims 1..rank-1.
+static bool encode_map(CUtensorMap* m, int elem_bytes, void* base, int rank, const uint64_t* dims, const uint64_t* strides,
+                       const uint32_t* box) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t gd[5], gs[4];
+  cuuint32_t bx[5], es[5];
+  for (int i = 0; i < rank; ++i) {
+    gd[i] = dims[i];
+    bx[i] = box[i];
+    es[i] = 1;
+    if (i > 0) gs[i - 1] = strides[i - 1];
+  }
+  const CUtensorMapDataType t = elem_bytes == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  return fn(m, t, (cuuint32_t)rank, base, gd, gs, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <class T>
+bool Evaluator<T>::setup_tma(std::string* err) {
+  (void)err;
+  constexpr int TC = TileCols<T>::value, E = ElemsPerComplex<T>::value;
+  if (nx_ > 256 || ny_ > 256 || nx_ < 8 || ny_ < 8) return false;
+  const uint64_t ncol = (uint64_t)ny_ * pz_;  // x-pass columns
+  const uint64_t cb = sizeof(C);              // complex bytes
+  bool ok = true;
+  {  // x-pass maps: {ncol*E, nx, fields}
+    uint64_t dims[3] = {ncol * E, (uint64_t)nx_, 1};
+    uint64_t str[2] = {ncol * cb, (uint64_t)Nc_ * cb};
+    uint32_t box[3] = {(uint32_t)(TC * E), (uint32_t)nx_, 1};
+    ok = ok && encode_map(&mapA_, 8, A_, 3, dims, str, box);
+    ok = ok && encode_map(&mapE_, 8, E_, 3, dims, str, box);
+    if (M_ > 0) {
+      dims[2] = (uint64_t)M_;
+      ok = ok && encode_map(&mapCf_, 8, Cf_, 3, dims, str, box);
+      uint64_t wd[3] = {ncol, (uint64_t)nx_, (uint64_t)M_};
+      uint64_t ws[2] = {ncol * sizeof(T), (uint64_t)Nc_ * sizeof(T)};
+      uint32_t wb[3] = {(uint32_t)TC, (uint32_t)nx_, 1};
+      ok = ok && encode_map(&mapW_, (int)sizeof(T), w_, 3, wd, ws, wb);
+    }
+    if (mf_) {
+      uint64_t wd[3] = {ncol, (uint64_t)nx_, 1};
+      uint64_t ws[2] = {ncol * sizeof(T), (uint64_t)Nc_ * sizeof(T)};
+      uint32_t wb[3] = {(uint32_t)TC, (uint32_t)nx_, 1};
+      ok = ok && encode_map(&mapWatt_, (int)sizeof(T), watt_, 3, wd, ws, wb);
+    }
+  }
+  {  // y-pass maps: {pz*E, ny, nx, fields}
+    uint64_t dims[4] = {(uint64_t)pz_ * E, (uint64_t)ny_, (uint64_t)nx_, 1};
+    uint64_t str[3] = {(uint64_t)pz_ * cb, (uint64_t)ny_ * pz_ * cb, (uint64_t)Nc_ * cb};
+    uint32_t box[4] = {(uint32_t)(TC * E), (uint32_t)ny_, 1, 1};
+    ok = ok && encode_map(&mapYA_, 8, A_, 4, dims, str, box);
+    ok = ok && encode_map(&mapYE_, 8, E_, 4, dims, str, box);
+    if (M_ > 0) {
+      dims[3] = (uint64_t)M_;
+      ok = ok && encode_map(&mapYC_, 8, Cf_, 4, dims, str, box);
+    }
+  }
+  if (!ok) return false;
+  const size_t tile_x = r128((size_t)nx_ * TC * sizeof(C)), tile_y = r128((size_t)ny_ * TC * sizeof(C)),
+               wt = r128((size_t)nx_ * TC * sizeof(T));
+  smem_ty_ = 3 * tile_y + 1024;
+  smem_tconv_ = 2 * tile_x + 2 * wt + 1024;
+  smem_tback_ = 3 * tile_x + 2 * wt + 1024;
+  if (std::max(smem_ty_, std::max(smem_tconv_, smem_tback_)) > 220 * 1024) return false;
+  cudaFuncSetAttribute(k_cols_y_tma<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ty_);
+  cudaFuncSetAttribute(k_cols_y_tma<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ty_);
+  cudaFuncSetAttribute(k_xconv_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tconv_);
+  cudaFuncSetAttribute(k_xbackconv_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tback_);
+  int nsm = 0, dev = 0, bps = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cols_y_tma<T, -1>, 256, smem_ty_);
+  bps = std::max(bps, 1);
+  const long ntile = (nzc_ + TC - 1) / TC;
+  grid_ty1_ = (int)std::min<long>((long)nx_ * ntile, (long)nsm * bps);
+  grid_tyM_ = (int)std::min<long>((long)std::max(M_, 1) * nx_ * ntile, (long)nsm * bps);
+  tma_ = true;
+  // fused Phi rows: one box of RB rows of all M fields, {pz*E, RB, M}
+  tma_phi_ = false;
+  if (M_ > 0 && (long)pz_ * E <= 256) {
+    constexpr int RB = PhiRows<T>::value;
+    const int NP = (M_ + 1) / 2, L = NP * RB;
+    uint64_t dims[3] = {(uint64_t)pz_ * E, (uint64_t)rows_, (uint64_t)M_};
+    uint64_t str[2] = {(uint64_t)pz_ * cb, (uint64_t)Nc_ * cb};
+    uint32_t box[3] = {(uint32_t)(pz_ * E), (uint32_t)RB, (uint32_t)M_};
+    smem_tphi_ = 2 * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * L * cb) + 1024;
+    if (smem_tphi_ <= 220 * 1024 && encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) {
+      auto set_phi = [&](auto kern) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tphi_);
+        int b2 = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, 256, smem_tphi_);
+        return std::max(b2, 1);
+      };
+      int bp;
+      switch (model_) {
+        case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB>); break;
+        case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB>); break;
+        case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB>); break;
+        case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB>); break;
+        default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB>); break;
+      }
+      const long ngroup = (rows_ + RB - 1) / RB;
+      grid_tphi_ = (int)std::min<long>(ngroup, (long)nsm * bp);
+      tma_phi_ = true;
+    }
+  }
+  return true;
 }
 
 template <class T>
 int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA, double esB, const std::vector<double>* w_fmt,
                        const std::vector<double>* w_att, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s, std::string* err) {
   nx_ = nx; ny_ = ny; nz_ = nz; nzc_ = nz / 2 + 1;
+  pz_ = (nzc_ + 3) / 4 * 4;
   N_ = (long)nx * ny * nz;
-  Nc_ = (long)nx * ny * nzc_;
+  Nc_ = (long)nx * ny * pz_;
   rows_ = (long)nx * ny;
   model_ = model;
   M_ = (model < 0) ? 0 : (model >= MODEL_ESFMT ? 11 : 5);
   hsd_ = hsd; esA_ = esA; esB_ = esB;
   mf_ = (w_att != nullptr);
   tx_ = tx; ty_ = ty; tz_ = tz;
-  Dims d{nx, ny, nz, nzc_, N_, Nc_, rows_};
+  Dims d{nx, ny, nz, nzc_, N_, Nc_, rows_, pz_};
   const size_t cs = sizeof(C);
   CK(cudaMalloc(&A_, Nc_ * cs));
   CK(cudaMalloc(&E_, Nc_ * cs));
-  if (M_ > 0) CK(cudaMalloc(&Cf_, (size_t)M_ * Nc_ * cs));
+  CK(cudaMemsetAsync(A_, 0, Nc_ * cs, s));
+  CK(cudaMemsetAsync(E_, 0, Nc_ * cs, s));
+  if (M_ > 0) {
+    CK(cudaMalloc(&Cf_, (size_t)M_ * Nc_ * cs));
+    CK(cudaMemsetAsync(Cf_, 0, (size_t)M_ * Nc_ * cs, s));
+  }
   // launch geometry and shared memory
   smem_rows_ = smem_bytes(rb_rows_, nz, cs, 2);
   // fused phi kernel: NP lines per row; shrink rows per block to fit 200 KB
@@ -196,8 +332,9 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_phi_rows<T, MODEL_WHITEBEAR_II>, smem_phi_);
   // partial-sum storage: phi blocks (1 value), x columns (1 value), final rows (4 values)
   const long nphi = (rows_ + rb_phi_ - 1) / rb_phi_;
-  const long ncolx = ((long)ny * nzc_ + tc_ - 1) / tc_;
-  part_len_ = 2 * (nphi + ncolx + 4 * grid_blocks_rows());
+  const long ncolx = ((long)ny * pz_ + 7) / 8 + 16;  // x-pass blocks of the widest grid (8 columns per tile)
+  // phi partials: at most one per row (both the row-group and the persistent grids stay below it)
+  part_len_ = 2 * (rows_ + ncolx + 4 * grid_blocks_rows());
   CK(cudaMalloc(&part_, part_len_ * sizeof(double)));
   CK(cudaMalloc(&terms_, 8 * sizeof(double)));
   CK(cudaMalloc(&status_, sizeof(unsigned)));
@@ -207,9 +344,11 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   double2* tmp_spec = nullptr;
   CK(cudaMalloc(&tmp_real, N_ * sizeof(double)));
   CK(cudaMalloc(&tmp_spec, Nc_ * sizeof(double2)));
+  CK(cudaMemsetAsync(tmp_spec, 0, Nc_ * sizeof(double2), s));
   const unsigned cgrid = (unsigned)std::min<long>((Nc_ + 255) / 256, 4096);
   if (M_ > 0) {
     CK(cudaMalloc(&w_, (size_t)M_ * Nc_ * sizeof(T)));
+    CK(cudaMemsetAsync(w_, 0, (size_t)M_ * Nc_ * sizeof(T), s));
     for (int a = 0; a < M_; ++a) {
       CK(cudaMemcpyAsync(tmp_real, w_fmt[a].data(), N_ * sizeof(double), cudaMemcpyHostToDevice, s));
       r2c_f64(tmp_real, tmp_spec, d, tx, ty, tz, s);
@@ -226,23 +365,24 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   CK(cudaGetLastError());
   cudaFree(tmp_real);
   cudaFree(tmp_spec);
+  if (!setup_tma(err)) tma_ = false;
   return 0;
 }
 
 template <class T>
 void Evaluator<T>::r2c(const double* in, C* out, cudaStream_t s) {
-  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_};
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
   k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(in, out, d, tz_->plan, twp<T>(tz_), rb_rows_);
   k_cols_fft<T, -1><<<dim3((unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_coly_, s>>>(out, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
-  k_cols_fft<T, -1><<<dim3((unsigned)(((long)ny_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_colx_, s>>>(out, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  k_cols_fft<T, -1><<<dim3((unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_), 1), 256, smem_colx_, s>>>(out, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
 }
 
 template <class T>
 void Evaluator<T>::c2r(const C* in, double* out, T scale, cudaStream_t s) {
-  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_};
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
   C* work = E_;
   cudaMemcpyAsync(work, in, Nc_ * sizeof(C), cudaMemcpyDeviceToDevice, s);
-  k_cols_fft<T, +1><<<dim3((unsigned)(((long)ny_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_colx_, s>>>(work, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  k_cols_fft<T, +1><<<dim3((unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_), 1), 256, smem_colx_, s>>>(work, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
   k_cols_fft<T, +1><<<dim3((unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_coly_, s>>>(work, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
   k_rows_c2r<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(work, out, d, tz_->plan, twp<T>(tz_), rb_rows_, scale);
 }
@@ -253,32 +393,56 @@ int Evaluator<T>::launch(const double* rho, const double* vext, double* dF, doub
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
   };
-  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_};
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
+  constexpr int TCt = TileCols<T>::value;
   const unsigned gcy = (unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_);
-  const unsigned gcx = (unsigned)(((long)ny_ * nzc_ + tc_ - 1) / tc_);
+  const unsigned gcx = (unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_);
+  const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
+  const unsigned gxb = tma_ ? gtx : gcx;
   const long nphi = (rows_ + rb_phi_ - 1) / rb_phi_;
   double* part_phi = part_;
-  double* part_mf = part_ + 2 * nphi;
-  double* part_fin = part_mf + 2 * gcx;
+  double* part_mf = part_ + 2 * rows_;
+  double* part_fin = part_mf + 2 * (long)std::max(gcx, gtx);
   const bool any = M_ > 0 || mf_;
+  auto yfwd = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
+    if (tma_) k_cols_y_tma<T, -1><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    else k_cols_fft<T, -1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  };
+  auto yinv = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
+    if (tma_) k_cols_y_tma<T, +1><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  };
   cudaMemsetAsync(status_, 0, sizeof(unsigned), s);
   mark(0);
   if (any) {
     k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
     mark(1);
-    k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
+    yfwd(A_, mapYA_, 1, grid_ty1_);
     mark(2);
   } else {
     mark(1);
     mark(2);
   }
   if (M_ > 0) {
-    k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
+    if (tma_) k_xconv_tma<T><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+    else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     mark(3);
-    k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+    yinv(Cf_, mapYC_, M_, grid_tyM_);
     mark(4);
     const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
     const unsigned gphi = (unsigned)nphi;
+    long phi_blocks = nphi;
+    if (tma_phi_) {
+      constexpr int RB = PhiRows<T>::value;
+      phi_blocks = grid_tphi_;
+      switch (model_) {
+        case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+      }
+    } else
     switch (model_) {
       case MODEL_ROSENFELD: k_phi_rows<T, MODEL_ROSENFELD><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
       case MODEL_RSLT: k_phi_rows<T, MODEL_RSLT><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
@@ -286,19 +450,23 @@ int Evaluator<T>::launch(const double* rho, const double* vext, double* dF, doub
       case MODEL_WHITEBEAR_I: k_phi_rows<T, MODEL_WHITEBEAR_I><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
       default: k_phi_rows<T, MODEL_WHITEBEAR_II><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
     }
-    k_finish_reduce<<<1, 256, 0, s>>>(part_phi, nphi, 1, terms_ + 0);
+    k_finish_reduce<<<1, 256, 0, s>>>(part_phi, phi_blocks, 1, terms_ + 0);
     mark(5);
-    k_cols_fft<T, -1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+    yfwd(Cf_, mapYC_, M_, grid_tyM_);
     mark(6);
   } else {
     for (int i = 3; i <= 6; ++i) mark(i);
   }
   if (any) {
-    k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
-                                                 mf_ ? part_mf : nullptr);
-    if (mf_) k_finish_reduce<<<1, 256, 0, s>>>(part_mf, gcx, 1, terms_ + 1);
+    if (tma_)
+      k_xbackconv_tma<T><<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan,
+                                                        twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
+    else
+      k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
+                                                   mf_ ? part_mf : nullptr);
+    if (mf_) k_finish_reduce<<<1, 256, 0, s>>>(part_mf, gxb, 1, terms_ + 1);
     mark(7);
-    k_cols_fft<T, +1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(E_, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
+    yinv(E_, mapYE_, 1, grid_ty1_);
     mark(8);
   } else {
     mark(7);
@@ -313,7 +481,7 @@ int Evaluator<T>::launch(const double* rho, const double* vext, double* dF, doub
 
 template <class T>
 void Evaluator<T>::pass_bytes(double* by) const {
-  const double b = sizeof(T), N = (double)N_, Nc = (double)Nc_, M = M_;
+  const double b = sizeof(T), N = (double)N_, Nc = (double)nx_ * ny_ * nzc_, M = M_;
   const double C = 2 * Nc * b, W = Nc * b;
   const bool any = M_ > 0 || mf_;
   by[0] = any ? N * 8 + C : 0;                        // rows_r2c: rho (f64) -> A
@@ -342,6 +510,7 @@ int Evaluator<T>::finish(double dV, double mu, EvalTerms* out, cudaStream_t s) {
   out->sum_dF_rho = h[5];
   out->F_ext = h[4] * dV - (h[3] * dV) * mu;
   out->status = st;
+  if (st & kStatusTimeout) return 3;
   out->Omega = ((out->F_id + out->F_hs) + out->F_mf) + out->F_ext;
   return (cudaGetLastError() == cudaSuccess) ? 0 : 5;
 }

@@ -6,6 +6,7 @@
 #include <memory>
 #include <string>
 #include <vector>
+#include <cuda.h>
 #include "cdft_types.h"
 
 namespace cdft {
@@ -54,6 +55,7 @@ class Evaluator {
              cudaEvent_t* ev = nullptr);
   // Algorithmic bytes each of the 9 passes must move (reads + writes once).
   void pass_bytes(double* bytes) const;
+  bool setup_tma(std::string* err);
   int finish(double dV, double mu, EvalTerms* out, cudaStream_t s);
   // Transforms used by DDFT and tests: real FP64 (device) -> spectrum (device C), and back (x scale).
   void r2c(const double* in, C* out, cudaStream_t s);
@@ -62,12 +64,15 @@ class Evaluator {
   const T* weights() const { return w_; }
   const T* w_att() const { return watt_; }
   int M() const { return M_; }
+  long spectrum_len() const { return Nc_; }  // complex values per spectrum (padded rows)
+  int pitch() const { return pz_; }
+  bool uses_tma() const { return tma_; }
   double* dev_terms() const { return terms_; }
   unsigned* dev_status() const { return status_; }
   long grid_blocks_rows() const;
 
  private:
-  int nx_ = 0, ny_ = 0, nz_ = 0, nzc_ = 0;
+  int nx_ = 0, ny_ = 0, nz_ = 0, nzc_ = 0, pz_ = 0;
   long N_ = 0, Nc_ = 0, rows_ = 0;
   int model_ = -1, M_ = 0;
   double hsd_ = 1, esA_ = 1, esB_ = 0;
@@ -84,6 +89,15 @@ class Evaluator {
   unsigned* status_ = nullptr;
   int rb_rows_ = 16, rb_phi_ = 4, tc_ = 16;
   size_t smem_rows_ = 0, smem_phi_ = 0, smem_colx_ = 0, smem_coly_ = 0, smem_xconv_ = 0, smem_xback_ = 0;
+  // tensor-copy path (cdft_kernels_tma.cuh)
+  bool tma_ = false;
+  CUtensorMap mapA_, mapCf_, mapE_, mapW_, mapWatt_, mapYA_, mapYC_, mapYE_;
+  size_t smem_ty_ = 0, smem_tconv_ = 0, smem_tback_ = 0;
+  int grid_ty1_ = 0, grid_tyM_ = 0;
+  bool tma_phi_ = false;
+  CUtensorMap mapR_;
+  size_t smem_tphi_ = 0;
+  int grid_tphi_ = 0;
 };
 
 }  // namespace cdft

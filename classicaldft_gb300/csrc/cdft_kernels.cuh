@@ -3,6 +3,10 @@
 // pos = k + Nz*(j + Ny*i); half spectra kpos = kz + Nzc*(ky + Ny*kx) with
 // Nzc = Nz/2 + 1 (FFTW r2c layout). Transforms are unnormalised.
 //
+// Internally the half spectrum's rows are padded to pz = round_up(Nzc, 4)
+// (kpos = kz + pz*(ky + Ny*kx)) so that every tensor-copy stride is a multiple
+// of 16 bytes; columns kz >= Nzc are padding and carry no data.
+//
 // Pass structure of one evaluation (T = float or double):
 //   rows_r2c     rho (f64) -> A            z-axis r2c, two rows per complex FFT
 //   cols_fft(y)  A                          y-axis forward
@@ -22,8 +26,9 @@ namespace cdft {
 
 struct Dims {
   int nx, ny, nz, nzc;
-  long N, Nc;
-  long rows;  // nx*ny
+  long N, Nc;  // Nc = nx*ny*pz: spectra are stored with a padded row pitch
+  long rows;   // nx*ny
+  int pz;      // row pitch of the half spectrum: nzc rounded up to a multiple of 4
 };
 
 // ----------------------------------------------------------- reductions ---
@@ -68,6 +73,42 @@ __device__ __forceinline__ void block_reduce_store(Acc* acc, double* out, long b
   }
 }
 
+// Block-wide plain FP64 sum of NV per-thread partials (a thread's partial
+// covers only a few points); thread 0 stores (sum, 0) pairs in the layout of
+// block_reduce_store. The compensated merge across blocks is k_finish_reduce.
+template <int NV>
+__device__ __forceinline__ void block_sum_store(double* v, double* out, long block_id) {
+  __shared__ double red[32][NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (lane == 0) red[warp][k] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    const int k = threadIdx.x;
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][k];
+    out[(block_id * NV + k) * 2 + 0] = t;
+    out[(block_id * NV + k) * 2 + 1] = 0.0;
+  }
+}
+
+// Kahan-compensated running sum in the bulk precision (a thread's few points).
+template <class T>
+struct KahanT {
+  T s = 0, c = 0;
+  __device__ __forceinline__ void add(T v) {
+    const T y = v - c;
+    const T t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 // Sums nblk partial (s, c) pairs of NV values in a fixed order: out[v] = total.
 __global__ void k_finish_reduce(const double* __restrict__ part, long nblk, int nv, double* __restrict__ out);
 
@@ -99,8 +140,8 @@ __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, ty
     const C Z = res[r * LP + k];
     const C W = res[r * LP + (k == 0 ? 0 : nz - k)];  // Z_{N-k}
     // X = (Z + conj(W))/2, Y = (Z - conj(W))/(2i)
-    if (ra < d.rows) out[ra * nzc + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
-    if (rb < d.rows) out[rb * nzc + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+    if (ra < d.rows) out[ra * d.pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
+    if (rb < d.rows) out[rb * d.pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
   }
 }
 
@@ -132,14 +173,14 @@ __global__ void __launch_bounds__(256) k_rows_c2r(const typename Cx<T>::type* __
   typedef typename Cx<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
-  const int nz = d.nz, LP = nz + 1, nzc = d.nzc;
+  const int nz = d.nz, LP = nz + 1;
   C* b1 = b0 + RB * LP;
   const long pair0 = (long)blockIdx.x * RB;
   for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
     const int r = e / nz, k = e - r * nz;
     const long ra = 2 * (pair0 + r), rb = ra + 1;
-    const C* A = ra < d.rows ? in + ra * nzc : nullptr;
-    const C* B = rb < d.rows ? in + rb * nzc : nullptr;
+    const C* A = ra < d.rows ? in + ra * d.pz : nullptr;
+    const C* B = rb < d.rows ? in + rb * d.pz : nullptr;
     b0[r * LP + k] = pair_spectrum<T>(A, B, k, nz);
   }
   C* res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
@@ -153,11 +194,11 @@ __global__ void __launch_bounds__(256) k_rows_c2r(const typename Cx<T>::type* __
 }
 
 // --------------------------------------------------------- column passes ---
-// Columns of the half spectrum along x (axis 0, ncol = ny*nzc, stride ny*nzc)
-// or y (axis 1, ncol = nx*nzc, stride nzc). A block loads TC consecutive
+// Columns of the half spectrum along x (axis 0, ncol = ny*pz, stride ny*pz)
+// or y (axis 1, ncol = nx*nzc, stride pz). A block loads TC consecutive
 // columns (coalesced along kz), transforms them in shared memory, stores back.
 __device__ __forceinline__ long col_base(int axis, long c, const Dims& d) {
-  return axis == 0 ? c : (c / d.nzc) * (long)d.ny * d.nzc + (c % d.nzc);
+  return axis == 0 ? c : (c / d.nzc) * (long)d.ny * d.pz + (c % d.nzc);
 }
 
 template <class T>
@@ -188,8 +229,8 @@ __global__ void __launch_bounds__(256) k_cols_fft(typename Cx<T>::type* __restri
   C* b0 = reinterpret_cast<C*>(smem_raw);
   C* b1 = b0 + TC * LP;
   C* g = data + (long)blockIdx.y * field_stride;
-  const long ncol = axis == 0 ? (long)d.ny * d.nzc : (long)d.nx * d.nzc;
-  const long stride = axis == 0 ? (long)d.ny * d.nzc : (long)d.nzc;
+  const long ncol = axis == 0 ? (long)d.ny * d.pz : (long)d.nx * d.nzc;
+  const long stride = axis == 0 ? (long)d.ny * d.pz : (long)d.pz;
   const long c0 = (long)blockIdx.x * TC;
   load_cols<T>(b0, g, axis, c0, ncol, n, stride, TC, LP, d);
   C* res = block_fft<DIR, T>(b0, b1, TC, LP, P, tw);
@@ -217,7 +258,7 @@ __global__ void __launch_bounds__(256) k_xconv(const typename Cx<T>::type* __res
   C* R = reinterpret_cast<C*>(smem_raw);
   C* b0 = R + TC * LP;
   C* b1 = b0 + TC * LP;
-  const long ncol = (long)d.ny * d.nzc, stride = ncol;
+  const long ncol = (long)d.ny * d.pz, stride = ncol;
   const long c0 = (long)blockIdx.x * TC;
   load_cols<T>(b0, A, 0, c0, ncol, n, stride, TC, LP, d);
   C* res = block_fft<-1, T>(b0, b1, TC, LP, px, tw);
@@ -255,7 +296,7 @@ __global__ void __launch_bounds__(256) k_xbackconv(const typename Cx<T>::type* _
   C* S = reinterpret_cast<C*>(smem_raw);
   C* b0 = S + TC * LP;
   C* b1 = b0 + TC * LP;
-  const long ncol = (long)d.ny * d.nzc, stride = ncol;
+  const long ncol = (long)d.ny * d.pz, stride = ncol;
   const long c0 = (long)blockIdx.x * TC;
   for (int e = threadIdx.x; e < TC * n; e += blockDim.x) {
     const int c = e % TC, i = e / TC;
@@ -279,8 +320,8 @@ __global__ void __launch_bounds__(256) k_xbackconv(const typename Cx<T>::type* _
         const T wv = __ldg(wa + i * stride + col);
         const C z = res[c * LP + i];
         S[c * LP + i] = cadd(S[c * LP + i], mul_weight(z, wv, odd));
-        if (is_mf) {
-          const int kz = (int)(col % d.nzc);
+        const int kz = (int)(col % d.pz);
+        if (is_mf && kz < d.nzc) {
           const double mult = (kz == 0 || 2 * kz == d.nz) ? 1.0 : 2.0;
           acc.add(mult * ((double)z.x * (double)z.x + (double)z.y * (double)z.y) * (double)wv);
         }
@@ -323,14 +364,14 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
     const C* Arow = nullptr;
     const C* Brow = nullptr;
     if (row < d.rows) {
-      Arow = Cf + (long)(2 * pr) * d.Nc + row * nzc;
-      if (2 * pr + 1 < M) Brow = Cf + (long)(2 * pr + 1) * d.Nc + row * nzc;
+      Arow = Cf + (long)(2 * pr) * d.Nc + row * d.pz;
+      if (2 * pr + 1 < M) Brow = Cf + (long)(2 * pr + 1) * d.Nc + row * d.pz;
     }
     b0[line * LP + k] = pair_spectrum<T>(Arow, Brow, k, nz);
   }
   C* res = block_fft<+1, T>(b0, b1, L, LP, pz, tw);
   C* other = (res == b0) ? b1 : b0;
-  double psum = 0.0;  // per-thread partial (a few points); merged with compensation below
+  KahanT<T> psum;  // per-thread partial (a few points); merged in FP64 below
   unsigned st = 0;
   for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
     const int r = e / nz, k = e - r * nz;
@@ -345,7 +386,7 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
     const T phi = fmt_phi_point<T, MODEL>(nv, hsd, esA, esB);
     if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
     if (!isfinite(phi)) st |= 2u;
-    psum += (double)phi;
+    psum.add(phi);
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       const T im = (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0;
@@ -353,10 +394,8 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
     }
   }
   if (st) atomicOr(status, st);
-  Acc acc;
-  acc.init();
-  acc.add(psum);
-  block_reduce_store<1>(&acc, part, blockIdx.x);
+  double pv = psum.value();
+  block_sum_store<1>(&pv, part, blockIdx.x);
   C* res2 = block_fft<-1, T>(other, res, L, LP, pz, tw);
   for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
     const int line = e / nzc, k = e - line * nzc;
@@ -365,8 +404,8 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
     if (row >= d.rows) continue;
     const C Z = res2[line * LP + k];
     const C W = res2[line * LP + (k == 0 ? 0 : nz - k)];
-    Cf[(long)(2 * pr) * d.Nc + row * nzc + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
-    if (2 * pr + 1 < M) Cf[(long)(2 * pr + 1) * d.Nc + row * nzc + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+    Cf[(long)(2 * pr) * d.Nc + row * d.pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
+    if (2 * pr + 1 < M) Cf[(long)(2 * pr + 1) * d.Nc + row * d.pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
   }
 }
 
@@ -393,23 +432,23 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
       const int r = e / nz, k = e - r * nz;
       const long ra = 2 * (pair0 + r), rb = ra + 1;
-      const C* Ar = ra < d.rows ? E + ra * nzc : nullptr;
-      const C* Br = rb < d.rows ? E + rb * nzc : nullptr;
+      const C* Ar = ra < d.rows ? E + ra * d.pz : nullptr;
+      const C* Br = rb < d.rows ? E + rb * d.pz : nullptr;
       b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
     res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
   }
   // Pointwise terms in the bulk precision T (FP64 in FP64 mode); each thread
-  // keeps plain FP64 partials of its few points, merged with compensation.
-  double ps[4] = {0.0, 0.0, 0.0, 0.0};
+  // keeps Kahan partials in T over its few points, merged in FP64 across the
+  // block and with compensation across blocks.
+  KahanT<T> ks[4];
   const T dVt = (T)dV, mut = (T)mu;
   for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
     const int rr = e / nz, k = e - rr * nz;
     const long row = 2 * pair0 + rr;
     if (row >= d.rows) continue;
     const long p = row * nz + k;
-    const double r0d = rho[p];
-    const T r0 = (T)r0d;
+    const T r0 = (T)rho[p];
     const T lr = log(r0);
     T h = 0;
     if (have_fmt_or_mf) {
@@ -422,18 +461,13 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     f += ve * dVt;
     f += -mut * dVt;
     dF[p] = (double)f;
-    if (ideal) ps[0] += (double)((r0 * lr - r0) * dVt);
-    ps[1] += r0d;
-    ps[2] += (double)(ve * r0);
-    ps[3] += (double)f * r0d;
+    if (ideal) ks[0].add((r0 * lr - r0) * dVt);
+    ks[1].add(r0);
+    ks[2].add(ve * r0);
+    ks[3].add(f * r0);
   }
-  Acc acc[4];
-#pragma unroll
-  for (int v = 0; v < 4; ++v) {
-    acc[v].init();
-    acc[v].add(ps[v]);
-  }
-  block_reduce_store<4>(acc, part, blockIdx.x);
+  double v[4] = {ks[0].value(), ks[1].value(), ks[2].value(), ks[3].value()};
+  block_sum_store<4>(v, part, blockIdx.x);
 }
 
 // ----------------------------------------------------------- pointwise ---

@@ -1,0 +1,484 @@
+// TMA-fed column passes (sm_103a). A tile is TC consecutive columns of the
+// padded half spectrum by the n points of the transform axis, stored row-major
+// [n][TC] in shared memory exactly as the tensor copy writes it. Threads map
+// column-fastest onto the tile, so every FFT stage reads and writes shared
+// memory without bank conflicts, and no padding is needed.
+//
+// Each kernel keeps two tiles in flight: while one is transformed, the tensor
+// engine brings the next one in, with an mbarrier per stage buffer. Results
+// leave through tensor stores from shared memory.
+#pragma once
+#include "cdft_kernels.cuh"
+#include "cdft_tma.cuh"
+
+namespace cdft {
+
+// Radix-P butterfly on column c of a row-major tile with TC columns.
+template <int DIR, class T, int P, int TC>
+__device__ __forceinline__ void tile_butterfly(const typename Cx<T>::type* __restrict__ x, typename Cx<T>::type* __restrict__ y, int c,
+                                               int q, int k, int m, int s, const typename Cx<T>::type* __restrict__ tw,
+                                               const typename Cx<T>::type* __restrict__ roots) {
+  typedef typename Cx<T>::type C;
+  C a[P];
+#pragma unroll
+  for (int j = 0; j < P; ++j) a[j] = x[(k + s * (q + m * j)) * TC + c];
+  if (P == 8) {
+    dft8<DIR, T>(a);
+  } else if (P == 4) {
+    dft4<DIR>(a);
+  } else if (P == 2) {
+    dft2<DIR>(a);
+  } else {
+    C w[P], b[P];
+#pragma unroll
+    for (int j = 0; j < P; ++j) w[j] = __ldg(reinterpret_cast<const C*>(roots + j));
+#pragma unroll
+    for (int t = 0; t < P; ++t) {
+      C acc = a[0];
+#pragma unroll
+      for (int j = 1; j < P; ++j) acc = cadd(acc, cmul_dir<DIR>(a[j], w[(j * t) % P]));
+      b[t] = acc;
+    }
+#pragma unroll
+    for (int t = 0; t < P; ++t) a[t] = b[t];
+  }
+  const C* twq = tw + q * P;
+  y[(k + s * (P * q)) * TC + c] = a[0];
+#pragma unroll
+  for (int t = 1; t < P; ++t) y[(k + s * (P * q + t)) * TC + c] = cmul_dir<DIR>(a[t], __ldg(reinterpret_cast<const C*>(twq + t)));
+}
+
+// Odd radices out of line: keeps their register arrays out of the kernels'
+// register budget (the power-of-two lengths only inline radices 8, 4, 2).
+template <int DIR, class T, int P, int TC>
+__device__ __noinline__ void tile_butterfly_odd(const typename Cx<T>::type* __restrict__ x, typename Cx<T>::type* __restrict__ y, int c,
+                                                int q, int k, int m, int s, const typename Cx<T>::type* __restrict__ tw,
+                                                const typename Cx<T>::type* __restrict__ roots) {
+  tile_butterfly<DIR, T, P, TC>(x, y, c, q, k, m, s, tw, roots);
+}
+
+template <int DIR, class T, int TC>
+__device__ __noinline__ void tile_butterfly_generic(const typename Cx<T>::type* __restrict__ x, typename Cx<T>::type* __restrict__ y,
+                                                    int c, int q, int k, int m, int s, int p, const typename Cx<T>::type* __restrict__ tw,
+                                                    const typename Cx<T>::type* __restrict__ roots) {
+  typedef typename Cx<T>::type C;
+  C in[kMaxRadix];
+  for (int j = 0; j < p; ++j) in[j] = x[(k + s * (q + m * j)) * TC + c];
+  const C* twq = tw + q * p;
+  for (int t = 0; t < p; ++t) {
+    C acc = in[0];
+    int idx = 0;
+    for (int j = 1; j < p; ++j) {
+      idx += t;
+      if (idx >= p) idx -= p;
+      acc = cadd(acc, cmul_dir<DIR>(in[j], roots[idx]));
+    }
+    y[(k + s * (p * q + t)) * TC + c] = (t == 0) ? acc : cmul_dir<DIR>(acc, twq[t]);
+  }
+}
+
+// Transforms the TC columns of the tile in b0 (b1 is scratch); returns the
+// buffer holding the result. Starts and ends with __syncthreads().
+template <int DIR, class T, int TC>
+__device__ typename Cx<T>::type* tile_fft(typename Cx<T>::type* b0, typename Cx<T>::type* b1, const FFTPlan& P,
+                                          const typename Cx<T>::type* __restrict__ table) {
+  typedef typename Cx<T>::type C;
+  C* src = b0;
+  C* dst = b1;
+  int len = P.n, s = 1;
+  for (int st = 0; st < P.nst; ++st) {
+    const int p = P.radix[st];
+    const int m = len / p;
+    const int items = TC * (P.n / p);
+    const C* tw = table + P.tw_off[st];
+    const C* rt = table + P.root_off[st];
+    __syncthreads();
+    for (int w = threadIdx.x; w < items; w += blockDim.x) {
+      const int c = w % TC, u = w / TC;
+      const int q = u / s, k = u - q * s;
+      switch (p) {
+        case 8: tile_butterfly<DIR, T, 8, TC>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 4: tile_butterfly<DIR, T, 4, TC>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 2: tile_butterfly<DIR, T, 2, TC>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 3: tile_butterfly_odd<DIR, T, 3, TC>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 5: tile_butterfly_odd<DIR, T, 5, TC>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 7: tile_butterfly_odd<DIR, T, 7, TC>(src, dst, c, q, k, m, s, tw, rt); break;
+        default: tile_butterfly_generic<DIR, T, TC>(src, dst, c, q, k, m, s, p, tw, rt); break;
+      }
+    }
+    C* t = src;
+    src = dst;
+    dst = t;
+    len = m;
+    s *= p;
+  }
+  __syncthreads();
+  return src;
+}
+
+// Tile geometry: TC complex columns make one 128-byte row.
+template <class T> struct TileCols;
+template <> struct TileCols<float> { static constexpr int value = 16; };
+template <> struct TileCols<double> { static constexpr int value = 8; };
+// rows per group of the fused Phi kernel
+template <class T> struct PhiRows;
+template <> struct PhiRows<float> { static constexpr int value = 4; };
+template <> struct PhiRows<double> { static constexpr int value = 2; };
+// 8-byte tensor elements per complex value (float2 = 1, double2 = 2)
+template <class T> struct ElemsPerComplex;
+template <> struct ElemsPerComplex<float> { static constexpr int value = 1; };
+template <> struct ElemsPerComplex<double> { static constexpr int value = 2; };
+
+// ---------------------------------------------------------------- y pass ---
+// Work item = (field f, plane x, column tile t): the tile [ny][TC] at kz0 = t*TC.
+// Tensor map (4D, 8-byte elements): {pz*E, ny, nx, nfield}.
+template <class T, int DIR>
+__global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUtensorMap map, Dims d, FFTPlan P,
+                                                    const typename Cx<T>::type* __restrict__ tw, int nfield, unsigned* __restrict__ status) {
+  typedef typename Cx<T>::type C;
+  constexpr int TC = TileCols<T>::value, E = ElemsPerComplex<T>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* sm = aligned_smem(smem_raw);
+  const int n = P.n;
+  const size_t tile_bytes = (size_t)n * TC * sizeof(C), tb = r128(tile_bytes);
+  C* stage[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + tb)};
+  C* work = reinterpret_cast<C*>(sm + 2 * tb);
+  __shared__ __align__(8) uint64_t bar[2];
+  const int ntile = (d.nzc + TC - 1) / TC;
+  const long total = (long)nfield * d.nx * ntile;
+  auto coords = [&](long item, int& kz0, int& x, int& f) {
+    const int t = (int)(item % ntile);
+    const long r = item / ntile;
+    x = (int)(r % d.nx);
+    f = (int)(r / d.nx);
+    kz0 = t * TC;
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](long item, int b) {
+    int kz0, x, f;
+    coords(item, kz0, x, f);
+    mbar_arrive_expect_tx(&bar[b], (unsigned)tile_bytes);
+    tma_load_4d(stage[b], &map, kz0 * E, 0, x, f, &bar[b]);
+  };
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < 2; ++b) {
+      const long item = blockIdx.x + (long)b * gridDim.x;
+      if (item < total) issue(item, b);
+    }
+  }
+  bool ok = true;
+  for (long k = 0;; ++k) {
+    const long item = blockIdx.x + k * gridDim.x;
+    if (item >= total) break;
+    const int b = (int)(k & 1);
+    ok = mbar_wait(&bar[b], (unsigned)((k >> 1) & 1), status);
+    if (!__syncthreads_and(ok)) break;
+    C* res = tile_fft<DIR, T, TC>(stage[b], work, P, tw);
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int kz0, x, f;
+      coords(item, kz0, x, f);
+      tma_store_4d(&map, kz0 * E, 0, x, f, res);
+      bulk_commit();
+      bulk_wait_read();
+      const long next = item + 2L * gridDim.x;
+      if (next < total) issue(next, b);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) bulk_wait_all();
+}
+
+// --------------------------------------------------------------- x passes ---
+// Column tiles of the x pass: TC consecutive columns of the (ny*pz) column
+// space, all nx rows. Maps (3D, rows = nx, third index = field):
+//   complex fields {ncol*E, nx, nf} (8-byte elements); real weights {ncol, nx, nw}.
+
+// C[a] = IFFT_x(FFT_x(A) . w_a) for a < M. The density spectrum lives in
+// registers; weight tiles are double-buffered; results leave by tensor store.
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xconv_tma(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW,
+                                                   const __grid_constant__ CUtensorMap mapC, int M, FFTPlan px,
+                                                   const typename Cx<T>::type* __restrict__ tw, unsigned* __restrict__ status) {
+  typedef typename Cx<T>::type C;
+  constexpr int TC = TileCols<T>::value, E = ElemsPerComplex<T>::value;
+  constexpr int PER = TC;  // complex values a thread owns: n*TC/256 <= TC for n <= 256
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* sm = aligned_smem(smem_raw);
+  const int n = px.n;
+  const size_t tile_bytes = (size_t)n * TC * sizeof(C), wbytes = (size_t)n * TC * sizeof(T);
+  const size_t tb = r128(tile_bytes), wb = r128(wbytes);
+  C* X = reinterpret_cast<C*>(sm);
+  C* Y = reinterpret_cast<C*>(sm + tb);
+  T* Wst[2] = {reinterpret_cast<T*>(sm + 2 * tb), reinterpret_cast<T*>(sm + 2 * tb + wb)};
+  __shared__ __align__(8) uint64_t bar[3];  // 0, 1: weights; 2: density tile
+  const int col0 = blockIdx.x * TC;
+  const int nel = n * TC;
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < 3; ++b) mbar_init(&bar[b], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(&bar[2], (unsigned)tile_bytes);
+    tma_load_3d(X, &mapA, col0 * E, 0, 0, &bar[2]);
+    for (int b = 0; b < 2 && b < M; ++b) {
+      mbar_arrive_expect_tx(&bar[b], (unsigned)wbytes);
+      tma_load_3d(Wst[b], &mapW, col0, 0, b, &bar[b]);
+    }
+  }
+  bool ok = mbar_wait(&bar[2], 0, status);
+  if (!__syncthreads_and(ok)) {
+    if (threadIdx.x == 0) bulk_wait_all();
+    return;
+  }
+  C* res = tile_fft<-1, T, TC>(X, Y, px, tw);
+  C R[PER];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int e = threadIdx.x + j * 256;
+    if (e < nel) R[j] = res[e];
+  }
+  for (int a = 0; a < M; ++a) {
+    const int b = a & 1;
+    ok = mbar_wait(&bar[b], (unsigned)((a >> 1) & 1), status);
+    if (!__syncthreads_and(ok)) break;
+    const bool odd = weight_is_odd(a);
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int e = threadIdx.x + j * 256;
+      if (e < nel) X[e] = mul_weight(R[j], Wst[b][e], odd);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && a + 2 < M) {
+      mbar_arrive_expect_tx(&bar[b], (unsigned)wbytes);
+      tma_load_3d(Wst[b], &mapW, col0, 0, a + 2, &bar[b]);
+    }
+    C* r2 = tile_fft<+1, T, TC>(X, Y, px, tw);
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store_3d(&mapC, col0 * E, 0, a, r2);
+      bulk_commit();
+      bulk_wait_read();
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) bulk_wait_all();
+}
+
+// E = IFFT_x(sum_a FFT_x(D[a]) . w_a + FFT_x(A) . w_att); sources are
+// double-buffered (spectrum tile + weight tile per stage), the sum lives in
+// registers. With the mean field, the Parseval sum for its energy goes to part.
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(const __grid_constant__ CUtensorMap mapD, const __grid_constant__ CUtensorMap mapW,
+                                                       const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapWatt,
+                                                       const __grid_constant__ CUtensorMap mapE, int M, int with_mf, Dims d, FFTPlan px,
+                                                       const typename Cx<T>::type* __restrict__ tw, double* __restrict__ part,
+                                                       unsigned* __restrict__ status) {
+  typedef typename Cx<T>::type C;
+  constexpr int TC = TileCols<T>::value, E = ElemsPerComplex<T>::value;
+  constexpr int PER = TC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* sm = aligned_smem(smem_raw);
+  const int n = px.n;
+  const size_t tile_bytes = (size_t)n * TC * sizeof(C), wbytes = (size_t)n * TC * sizeof(T);
+  const size_t tb = r128(tile_bytes), wb = r128(wbytes);
+  C* Dst[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + tb)};
+  C* Y = reinterpret_cast<C*>(sm + 2 * tb);
+  T* Wst[2] = {reinterpret_cast<T*>(sm + 3 * tb), reinterpret_cast<T*>(sm + 3 * tb + wb)};
+  __shared__ __align__(8) uint64_t bar[2];
+  const int col0 = blockIdx.x * TC;
+  const int nel = n * TC;
+  const int nsrc = M + (with_mf ? 1 : 0);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int a, int b) {
+    mbar_arrive_expect_tx(&bar[b], (unsigned)(tile_bytes + wbytes));
+    if (a < M) {
+      tma_load_3d(Dst[b], &mapD, col0 * E, 0, a, &bar[b]);
+      tma_load_3d(Wst[b], &mapW, col0, 0, a, &bar[b]);
+    } else {
+      tma_load_3d(Dst[b], &mapA, col0 * E, 0, 0, &bar[b]);
+      tma_load_3d(Wst[b], &mapWatt, col0, 0, 0, &bar[b]);
+    }
+  };
+  if (threadIdx.x == 0)
+    for (int b = 0; b < 2 && b < nsrc; ++b) issue(b, b);
+  C S[PER];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) S[j] = mk<T>(0, 0);
+  double pars = 0.0;
+  bool ok = true;
+  for (int a = 0; a < nsrc; ++a) {
+    const int b = a & 1;
+    ok = mbar_wait(&bar[b], (unsigned)((a >> 1) & 1), status);
+    if (!__syncthreads_and(ok)) break;
+    C* res = tile_fft<-1, T, TC>(Dst[b], Y, px, tw);
+    const bool is_mf = (a == M);
+    const bool odd = !is_mf && weight_is_odd(a);
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+      const int e = threadIdx.x + j * 256;
+      if (e < nel) {
+        const C z = res[e];
+        const T wv = Wst[b][e];
+        S[j] = cadd(S[j], mul_weight(z, wv, odd));
+        if (is_mf) {
+          const int col = col0 + (e % TC);
+          const int kz = col % d.pz;
+          if (kz < d.nzc && col < d.ny * d.pz) {
+            const double mult = (kz == 0 || 2 * kz == d.nz) ? 1.0 : 2.0;
+            pars += mult * ((double)z.x * (double)z.x + (double)z.y * (double)z.y) * (double)wv;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && a + 2 < nsrc) issue(a + 2, b);
+  }
+  if (part) {
+    Acc acc;
+    acc.init();
+    acc.add(pars);
+    block_reduce_store<1>(&acc, part, blockIdx.x);
+  }
+  if (!__syncthreads_and(ok)) {
+    if (threadIdx.x == 0) bulk_wait_all();
+    return;
+  }
+  C* X = Dst[0];
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    const int e = threadIdx.x + j * 256;
+    if (e < nel) X[e] = S[j];
+  }
+  C* r2 = tile_fft<+1, T, TC>(X, Y, px, tw);
+  fence_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tma_store_3d(&mapE, col0 * E, 0, 0, r2);
+    bulk_commit();
+    bulk_wait_all();
+  }
+}
+
+}  // namespace cdft
+
+namespace cdft {
+
+// ------------------------------------------------- fused Phi on z rows ---
+// Persistent: each block walks groups of RB consecutive rows (x, y). One
+// tensor copy brings the group's M field rows ({pz*E, rows, M}, box
+// {pz*E, RB, M}) while the previous group is computed. The M rows of a (x, y)
+// are paired into NP = ceil(M/2) complex lines; a group is a [nz][L] tile,
+// L = NP*RB lines, transformed column-wise (line-fastest, conflict-free):
+// c2r (z), Phi and dPhi per point, r2c (z), then the M derivative rows are
+// stored over the inputs.
+template <class T, int MODEL, int RB>
+__global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
+                                                      Dims d, FFTPlan pz_plan, const typename Cx<T>::type* __restrict__ tw, T hsd, T esA,
+                                                      T esB, double* __restrict__ part, unsigned* __restrict__ status) {
+  typedef typename Cx<T>::type C;
+  constexpr int M = ModelTraits<MODEL>::M;
+  constexpr int NP = (M + 1) / 2;
+  constexpr int L = NP * RB;
+  constexpr int E = ElemsPerComplex<T>::value;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* sm = aligned_smem(smem_raw);
+  const int nz = d.nz, nzc = d.nzc, pz = d.pz;
+  const size_t in_bytes = (size_t)M * RB * pz * sizeof(C), ib = r128(in_bytes);
+  const size_t zb = r128((size_t)nz * L * sizeof(C));
+  C* In[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + ib)};
+  C* Z0 = reinterpret_cast<C*>(sm + 2 * ib);
+  C* Z1 = reinterpret_cast<C*>(sm + 2 * ib + zb);
+  __shared__ __align__(8) uint64_t bar[2];
+  const long ngroup = (d.rows + RB - 1) / RB;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](long g, int b) {
+    mbar_arrive_expect_tx(&bar[b], (unsigned)in_bytes);
+    tma_load_3d(In[b], &mapR, 0, (int)(g * RB), 0, &bar[b]);
+  };
+  if (threadIdx.x == 0)
+    for (int b = 0; b < 2; ++b) {
+      const long g = blockIdx.x + (long)b * gridDim.x;
+      if (g < ngroup) issue(g, b);
+    }
+  KahanT<T> psum;
+  unsigned st = 0;
+  bool ok = true;
+  for (long it = 0;; ++it) {
+    const long g = blockIdx.x + it * gridDim.x;
+    if (g >= ngroup) break;
+    const int b = (int)(it & 1);
+    ok = mbar_wait(&bar[b], (unsigned)((it >> 1) & 1), status);
+    if (!__syncthreads_and(ok)) break;
+    const long row0 = g * RB;
+    const C* in = In[b];
+    // packed Hermitian spectra: line = r*NP + pair, element k of [nz][L]
+    for (int e = threadIdx.x; e < nz * L; e += blockDim.x) {
+      const int line = e % L, k = e / L;
+      const int r = line / NP, pr = line - r * NP;
+      const C* Arow = in + ((size_t)(2 * pr) * RB + r) * pz;
+      const C* Brow = (2 * pr + 1 < M) ? in + ((size_t)(2 * pr + 1) * RB + r) * pz : nullptr;
+      Z0[e] = pair_spectrum<T>(Arow, Brow, k, nz);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // In[b] consumed: bring the group after next
+      const long gn = g + 2L * gridDim.x;
+      if (gn < ngroup) issue(gn, b);
+    }
+    C* res = tile_fft<+1, T, L>(Z0, Z1, pz_plan, tw);
+    C* oth = (res == Z0) ? Z1 : Z0;
+    for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+      const int k = e % nz, r = e / nz;
+      if (row0 + r >= d.rows) continue;
+      T nv[11];
+#pragma unroll
+      for (int a = 0; a < M; ++a) {
+        const C z = res[k * L + r * NP + a / 2];
+        nv[a] = (a & 1) ? z.y : z.x;
+      }
+      const T eta = nv[0];
+      const T phi = fmt_phi_point<T, MODEL>(nv, hsd, esA, esB);
+      if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
+      if (!isfinite(phi)) st |= 2u;
+      psum.add(phi);
+#pragma unroll
+      for (int p = 0; p < NP; ++p) oth[k * L + r * NP + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
+    }
+    C* res2 = tile_fft<-1, T, L>(oth, res, pz_plan, tw);
+    for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
+      const int k = e % nzc, line = e / nzc;
+      const int r = line / NP, pr = line - r * NP;
+      const long row = row0 + r;
+      if (row >= d.rows) continue;
+      const C Z = res2[k * L + line];
+      const C W = res2[(k == 0 ? 0 : nz - k) * L + line];
+      Cf[(long)(2 * pr) * d.Nc + row * pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
+      if (2 * pr + 1 < M) Cf[(long)(2 * pr + 1) * d.Nc + row * pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+    }
+    __syncthreads();
+  }
+  if (st) atomicOr(status, st);
+  double pv = psum.value();
+  block_sum_store<1>(&pv, part, blockIdx.x);
+  (void)E;
+}
+
+}  // namespace cdft
