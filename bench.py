@@ -134,6 +134,35 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
+    """Wall seconds for FIRE2 (reference defaults dt = 1e-3, dt_max = 1e-2) to
+    reach max|dOmega/drho| <= tol on the droplet at fixed mass, graph-captured
+    on the device: plain FP64 evaluations vs the mixed policy (FP32 bulk phase,
+    then FP64 refinement). Both start from the tanh profile."""
+    import torch
+    hsd = cd.bh_diameter(1.0, 1.0, 3.0, KT)
+    mass = float(rho.sum()) * DX ** 3
+    out = {"start": "tanh droplet (no learned warm start)", "ensemble": "fixed mass", "tol": tol}
+    res = {}
+    for name, mixed in (("mixed", True), ("plain_fp64", False)):
+        c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT, fixed_mass=mass)
+        c.set_density(rho)
+        c.fire_init(force_limit=0.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = c.fire_run_device(tol, max_steps=max_steps, mixed=mixed, switch_tol=1e-12)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        t, _ = c.eval(want_dF=False)  # FP64 re-evaluation of the end state
+        res[name] = {"seconds": el, "steps": r["total_steps"], "fp32_steps": r["steps_fp32"], "resid": t["resid"],
+                     "Omega": t["Omega"], "converged": bool(t["resid"] <= tol)}
+        c.close()
+    out.update(res)
+    out["speedup_mixed_vs_plain"] = res["plain_fp64"]["seconds"] / res["mixed"]["seconds"]
+    out["omega_rel_diff"] = abs(res["mixed"]["Omega"] - res["plain_fp64"]["Omega"]) / abs(res["plain_fp64"]["Omega"])
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -141,6 +170,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fire", action="store_true", help="skip the time-to-residual legs")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -225,6 +255,8 @@ def main():
             "passes": [{"pass": p["pass"], "ms": round(p["ms"], 5), "GBs": round(p["bytes"] / max(p["ms"], 1e-9) / 1e6, 1)}
                        for p in passes],
             "clocks": clocks}
+    if not args.no_fire:
+        line["fire_to_resid_1e-8"] = fire_legs(cd, rho)
     if rank == 0 and not args.no_cpu_baseline:
         rate, n, el = cpu_baseline()
         line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",

@@ -31,7 +31,7 @@ C_FUNCTIONS = [
     "cdft_set_density", "cdft_get_density", "cdft_set_external_field", "cdft_set_chem_potential",
     "cdft_set_fixed_mass", "cdft_get_chem_potential", "cdft_eval", "cdft_bulk", "cdft_bh_diameter",
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
-    "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc",
+    "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -72,7 +72,8 @@ class FireReport(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_long), ("total_steps", ctypes.c_long), ("calls", ctypes.c_long),
                 ("F", ctypes.c_double), ("dt", ctypes.c_double), ("dt_max", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("vv", ctypes.c_double), ("fmax", ctypes.c_double),
-                ("resid", ctypes.c_double), ("backtracks", ctypes.c_int), ("stop", ctypes.c_int)]
+                ("resid", ctypes.c_double), ("backtracks", ctypes.c_int), ("stop", ctypes.c_int),
+                ("steps_fp32", ctypes.c_long)]
 
 
 class DdftReport(ctypes.Structure):
@@ -109,6 +110,7 @@ def lib():
             "cdft_time_passes": ([vp, i, dp, dp, P(i)], i),
             "cdft_fmt_weights": ([i, i, i, d, d, dp], i),
             "cdft_number_of_atoms_noalloc": ([vp, ctypes.c_long, d, vp, dp], i),
+            "cdft_fire_run_device": ([vp, d, d, ctypes.c_long, i, P(FireReport)], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -278,6 +280,12 @@ class Context:
     def fire_run_to_residual(self, tol, max_steps=100000):
         r = FireReport()
         self._check(lib().cdft_fire_run_to_residual(self._h, tol, max_steps, ctypes.byref(r)))
+        return self._rep(r)
+
+    def fire_run_device(self, tol, max_steps=-1, mixed=False, switch_tol=1e-6):
+        """Graph-captured FIRE2 to max|dOmega/drho| <= tol (FP64 test); mixed: FP32 bulk phase first."""
+        r = FireReport()
+        self._check(lib().cdft_fire_run_device(self._h, tol, switch_tol, max_steps, int(mixed), ctypes.byref(r)))
         return self._rep(r)
 
     # DDFT

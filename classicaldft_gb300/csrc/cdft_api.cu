@@ -13,6 +13,7 @@
 #include "../../include/cdft.h"
 #include "cdft_internal.h"
 #include "cdft_kernels.cuh"
+#include "cdft_ctx.h"
 
 using namespace cdft;
 
@@ -79,10 +80,6 @@ struct FAbsMax {
   __device__ void operator()(long i, double*, double* m) const { m[0] = fabs(a[i]); }
 };
 
-// FMT_Species alias maps (src/FMT_Species.cpp:29-93): rho = dmin + c y^2/(1+y^2).
-struct Alias {
-  double dmin, c;
-};
 __device__ __forceinline__ double alias_rho(const Alias& a, double y) { return a.dmin + a.c * y * y / (1 + y * y); }
 
 __global__ void k_alias_from_rho(const double* __restrict__ rho, double* __restrict__ x, long n, Alias a) {
@@ -223,53 +220,6 @@ unsigned grid_for(long n) { return (unsigned)std::max<long>(1, std::min<long>((n
 
 }  // namespace
 
-// ------------------------------------------------------------- context ---
-struct cdft_ctx {
-  cdft_params p{};
-  cdft_info info{};
-  std::string err;
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::shared_ptr<FFTTable> tx, ty, tz;
-  std::unique_ptr<Evaluator<double>> e64;
-  std::unique_ptr<Evaluator<float>> e32;
-  int precision = CDFT_FP64;
-  double mu = 0, fixed_mass = -1;
-  double* rho = nullptr;
-  double* dF = nullptr;
-  double* vext = nullptr;
-  double* red_part = nullptr;  // map-reduce partials
-  double* red_out = nullptr;   // finished values
-  double* host_out = nullptr;  // pinned copy of red_out
-  // FIRE state (fireMinimizer2 members)
-  bool fire_ready = false;
-  cdft_fire_params fp{};
-  double* fx[2] = {nullptr, nullptr};
-  double* fv[2] = {nullptr, nullptr};
-  double* fg[2] = {nullptr, nullptr};
-  int cur = 0;
-  double F = 0, dt = 0, dt_max = 0, alpha = 0, vv = 1, dt_best = 0, fmax = -1, resid = 0, vdotf = 0;
-  int Npos = 0, Nneg = 0, backtracks = 0;
-  unsigned it = 0;
-  long fire_steps = 0, calls = 0;
-  // DDFT state
-  bool ddft_ready = false;
-  double ddft_dt = 0, ddft_dt_max = 1, ddft_tol = 1e-4, ddft_time = 0, ddft_rhs = 1;
-  bool ddft_have_factors = false;
-  int ddft_successes = 0;
-  double *dd0 = nullptr, *dd1 = nullptr, *ddn = nullptr, *dR = nullptr, *dfac = nullptr;
-  void *rk0 = nullptr, *R0k = nullptr, *R1k = nullptr, *work = nullptr;
-  std::vector<double> Lx, Ly, Lz;
-
-  Alias alias() const {
-    Alias a;
-    a.dmin = 1e-18;  // SMALL_VALUE (include/Density.h:24)
-    const double etamin = a.dmin * (4 * M_PI * info.hsd * info.hsd * info.hsd / 3);
-    a.c = (1.0 - etamin) / info.dV;
-    return a;
-  }
-};
-
 static int fail(cdft_ctx* c, int code, const std::string& m) {
   if (c) c->err = m;
   return code;
@@ -362,6 +312,9 @@ static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
   return CDFT_OK;
 }
 
+int cdft_internal_fail(cdft_ctx* c, int code, const std::string& m) { return fail(c, code, m); }
+int cdft_internal_eval(cdft_ctx* c, double* terms8, int only_fex) { return eval_internal(c, terms8, only_fex); }
+
 extern "C" {
 
 int cdft_create(const cdft_params* p, cdft_ctx** out) {
@@ -413,6 +366,7 @@ int cdft_create(const cdft_params* p, cdft_ctx** out) {
 int cdft_destroy(cdft_ctx* c) {
   if (!c) return CDFT_OK;
   cudaStreamSynchronize(c->stream);
+  cdft_internal_fire_dev_free(c);
   c->e64.reset();
   c->e32.reset();
   cudaFree(c->rho); cudaFree(c->dF); cudaFree(c->vext); cudaFree(c->red_part); cudaFree(c->red_out); cudaFreeHost(c->host_out);
@@ -629,6 +583,8 @@ static int fire_accept(cdft_ctx* c, int s_idx) {
   return CDFT_OK;
 }
 
+extern "C++" int cdft_internal_fire_accept(cdft_ctx* c, int s_idx) { return fire_accept(c, s_idx); }
+
 int cdft_fire_init(cdft_ctx* c, const cdft_fire_params* p) {
   if (!c) return CDFT_ERR_ARG;
   cdft_fire_params d;
@@ -743,6 +699,7 @@ static void fire_report(const cdft_ctx* c, long steps, int bt, int stop, cdft_fi
   r->resid = c->resid;
   r->backtracks = bt;
   r->stop = stop;
+  r->steps_fp32 = 0;
 }
 
 static int fire_loop(cdft_ctx* c, long max_steps, double resid_tol, bool use_monitor, cdft_fire_report* rep) {

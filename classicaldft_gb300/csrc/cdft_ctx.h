@@ -1,0 +1,72 @@
+// Internal: the C ABI's context (one system on one GPU) and the device
+// FIRE2 engine's state, shared by cdft_api.cu and cdft_fire_dev.cu.
+#pragma once
+#include <cmath>
+#include <memory>
+#include <string>
+#include <vector>
+#include "../../include/cdft.h"
+#include "cdft_internal.h"
+
+// FMT_Species alias maps (src/FMT_Species.cpp:29-93): rho = dmin + c y^2/(1+y^2).
+struct Alias {
+  double dmin, c;
+};
+
+struct FireDevEngine;  // cdft_fire_dev.cu
+
+// ------------------------------------------------------------- context ---
+struct cdft_ctx {
+  cdft_params p{};
+  cdft_info info{};
+  std::string err;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::shared_ptr<cdft::FFTTable> tx, ty, tz;
+  std::unique_ptr<cdft::Evaluator<double>> e64;
+  std::unique_ptr<cdft::Evaluator<float>> e32;
+  int precision = CDFT_FP64;
+  double mu = 0, fixed_mass = -1;
+  double* rho = nullptr;
+  double* dF = nullptr;
+  double* vext = nullptr;
+  double* red_part = nullptr;  // map-reduce partials
+  double* red_out = nullptr;   // finished values
+  double* host_out = nullptr;  // pinned copy of red_out
+  // FIRE state (fireMinimizer2 members)
+  bool fire_ready = false;
+  cdft_fire_params fp{};
+  double* fx[2] = {nullptr, nullptr};
+  double* fv[2] = {nullptr, nullptr};
+  double* fg[2] = {nullptr, nullptr};
+  int cur = 0;
+  double F = 0, dt = 0, dt_max = 0, alpha = 0, vv = 1, dt_best = 0, fmax = -1, resid = 0, vdotf = 0;
+  int Npos = 0, Nneg = 0, backtracks = 0;
+  unsigned it = 0;
+  long fire_steps = 0, calls = 0;
+  // DDFT state
+  bool ddft_ready = false;
+  double ddft_dt = 0, ddft_dt_max = 1, ddft_tol = 1e-4, ddft_time = 0, ddft_rhs = 1;
+  bool ddft_have_factors = false;
+  int ddft_successes = 0;
+  double *dd0 = nullptr, *dd1 = nullptr, *ddn = nullptr, *dR = nullptr, *dfac = nullptr;
+  void *rk0 = nullptr, *R0k = nullptr, *R1k = nullptr, *work = nullptr;
+  std::vector<double> Lx, Ly, Lz;
+  // device FIRE2 engine (graph-captured steps)
+  FireDevEngine* fire_dev = nullptr;
+
+  Alias alias() const {
+    Alias a;
+    a.dmin = 1e-18;  // SMALL_VALUE (include/Density.h:24)
+    const double etamin = a.dmin * (4 * M_PI * info.hsd * info.hsd * info.hsd / 3);
+    a.c = (1.0 - etamin) / info.dV;
+    return a;
+  }
+};
+
+
+// helpers shared with cdft_fire_dev.cu
+int cdft_internal_fail(cdft_ctx* c, int code, const std::string& m);
+int cdft_internal_eval(cdft_ctx* c, double* terms8, int only_fex);
+int cdft_internal_fire_accept(cdft_ctx* c, int s_idx);
+void cdft_internal_fire_dev_free(cdft_ctx* c);

@@ -320,7 +320,9 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   }
   set_smem<T>(k_rows_r2c<T, double>, smem_rows_);
   set_smem<T>(k_rows_c2r<T, double>, smem_rows_);
-  set_smem<T>(k_final_rows<T>, smem_rows_);
+  set_smem<T>(k_final_rows<T, double>, smem_rows_);
+  set_smem<T>(k_final_rows<T, T>, smem_rows_);
+  set_smem<T>(k_rows_r2c<T, T>, smem_rows_);
   set_smem<T>(k_cols_fft<T, -1>, std::max(smem_colx_, smem_coly_));
   set_smem<T>(k_cols_fft<T, +1>, std::max(smem_colx_, smem_coly_));
   set_smem<T>(k_xconv<T>, smem_xconv_);
@@ -388,8 +390,8 @@ void Evaluator<T>::c2r(const C* in, double* out, T scale, cudaStream_t s) {
 }
 
 template <class T>
-int Evaluator<T>::launch(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, cudaStream_t s,
-                         cudaEvent_t* ev) {
+template <class RT>
+int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, double mu, int ideal, cudaStream_t s, cudaEvent_t* ev) {
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
   };
@@ -415,7 +417,7 @@ int Evaluator<T>::launch(const double* rho, const double* vext, double* dF, doub
   cudaMemsetAsync(status_, 0, sizeof(unsigned), s);
   mark(0);
   if (any) {
-    k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+    k_rows_r2c<T, RT><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
     mark(1);
     yfwd(A_, mapYA_, 1, grid_ty1_);
     mark(2);
@@ -473,7 +475,7 @@ int Evaluator<T>::launch(const double* rho, const double* vext, double* dF, doub
     mark(8);
   }
   const unsigned gfin = (unsigned)grid_blocks_rows();
-  k_final_rows<T><<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_), rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin);
+  k_final_rows<T, RT><<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_), rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin);
   k_finish_reduce<<<1, 256, 0, s>>>(part_fin, gfin, 4, terms_ + 2);
   mark(9);
   return 0;
@@ -524,5 +526,6 @@ int Evaluator<T>::eval(const double* rho, const double* vext, double* dF, double
 
 template class Evaluator<float>;
 template class Evaluator<double>;
+template int Evaluator<float>::launch<float>(const float*, const double*, float*, double, double, int, cudaStream_t, cudaEvent_t*);
 
 }  // namespace cdft

@@ -1,0 +1,589 @@
+// Device-resident FIRE2 (fireMinimizer2::step, src/Minimizer.cpp:160-327) for
+// runs to a residual target: the step's scalar logic runs in one-thread
+// control kernels over a FireState in device memory, the vector work in
+// grid kernels, and one whole step (control, vector passes, the F+dF
+// evaluation with its Species constraints, the alias conversion) is captured
+// once as a CUDA graph. The host launches the graph and reads the state every
+// few steps; no host round trip sits inside a step.
+//
+// The vectors (x, v, alias derivative, density, dF) are stored in the
+// arithmetic type S of the phase: FP32 for the bulk phase (GB300 runs FP64 at
+// a small fraction of its FP32 rate, and the alias maps are division-heavy),
+// FP64 for the refinement phase. The residual max|dOmega/drho| that ends a run
+// is always taken from an FP64 evaluation.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include "cdft_ctx.h"
+#include "cdft_kernels.cuh"
+#include "cdft_tma.cuh"
+
+using namespace cdft;
+
+struct FireConsts {
+  double dmin, c;  // alias map
+  double dV, volume;
+  double f_inc, f_dec, f_alf, alpha_start, dt_min;
+  int n_delay, n_neg_max, initial_delay;
+  double tol;  // residual target
+  double fixed_mass;
+  long N;
+};
+
+struct FireState {
+  double F, fold, dt, dt_max, alpha, vv, dt_best, fmax, resid, vdotf, vscale, coef, mu;
+  double omega, f_id, f_hs, f_mf, f_ext, natoms;
+  int Npos, Nneg, backtracks, cur, uphill, status, done, skip, failed;
+  unsigned it;
+  long steps, calls;
+  double red[8];
+};
+
+namespace {
+
+constexpr int kThreads = 256;
+unsigned grid_n(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + kThreads - 1) / kThreads, 152 * 8)); }
+
+// step start: fireMinimizer2::step up to SemiImplicitEuler (src/Minimizer.cpp:160-217)
+__global__ void k_fc_pre(FireState* st, FireConsts k) {
+  if (st->done) {
+    st->skip = 1;
+    return;
+  }
+  st->skip = 0;
+  st->it++;
+  const double P = -st->vdotf;
+  st->fold = st->F;
+  st->uphill = 0;
+  if (P > 0) {
+    st->Npos++;
+    st->Nneg = 0;
+    if (st->Npos > k.n_delay) {
+      st->dt = fmin(st->dt * k.f_inc, st->dt_max);
+      st->alpha = st->alpha * k.f_alf;
+    }
+  } else {
+    st->Npos = 0;
+    st->Nneg++;
+    if (st->Nneg > k.n_neg_max) {
+      st->status = CDFT_ERR_UPHILL;
+      st->done = 1;
+      st->skip = 1;
+      return;
+    }
+    if (!(k.initial_delay && st->it < (unsigned)k.n_delay)) {
+      if (st->dt * k.f_dec >= k.dt_min) st->dt *= k.f_dec;
+      st->alpha = k.alpha_start;
+    }
+    st->uphill = 1;
+    st->backtracks++;
+  }
+}
+
+template <class S>
+__device__ __forceinline__ void block_sums_to(double* v, int nv, double* part) {
+  // per-block plain FP64 tree of nv per-thread partials
+  __shared__ double red[32][4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = 0; k < nv; ++k) {
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (lane == 0) red[warp][k] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
+    part[blockIdx.x * 8 + threadIdx.x] = t;
+  }
+}
+template <class S>
+__device__ __forceinline__ void block_max_to(double* v, int nv, int off, double* part) {
+  __shared__ double red[32][4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  for (int k = 0; k < nv; ++k) {
+    for (int o = 16; o > 0; o >>= 1) v[k] = fmax(v[k], __shfl_down_sync(0xffffffffu, v[k], o));
+    if (lane == 0) red[warp][k] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, red[w][threadIdx.x]);
+    part[blockIdx.x * 8 + off + threadIdx.x] = t;
+  }
+}
+
+// SemiImplicitEuler first half (src/Minimizer.cpp:279-289) with the uphill
+// restart of step(): x' = x - dt/2 v (uphill), v' = (0.1 v if uphill else v) - dt g.
+template <class S>
+__global__ void __launch_bounds__(kThreads) k_fire_pre(S* x0, S* x1, S* v0, S* v1, const S* g0, const S* g1, const FireState* st, long n,
+                                                       double* part) {
+  if (st->skip) return;
+  const int cur = st->cur;
+  const S* x = cur ? x1 : x0;
+  const S* v = cur ? v1 : v0;
+  const S* g = cur ? g1 : g0;
+  S* xo = cur ? x0 : x1;
+  S* vo = cur ? v0 : v1;
+  const S dt = (S)st->dt, vs = (S)st->vscale;
+  const int up = st->uphill;
+  double acc[2] = {0, 0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    S xi = x[i], vi = v[i] * vs;
+    if (up) {
+      xi += vi * (S)(-0.5 * st->dt);
+      vi *= (S)0.1;
+    }
+    const S gi = g[i];
+    vi += gi * (-dt);
+    xo[i] = xi;
+    vo[i] = vi;
+    acc[0] += (double)(vi * vi);
+    acc[1] += (double)(gi * gi);
+  }
+  block_sums_to<S>(acc, 2, part);
+}
+
+// One block merges the per-block partials: 256-way strided sums (maxima),
+// then a fixed-order tree; the result goes to st->red[dst + k].
+__global__ void __launch_bounds__(256) k_fire_sum_finish(const double* part, int nblk, int off, int nv, FireState* st, int dst) {
+  __shared__ double ss[256], sc[256];
+  for (int k = 0; k < nv; ++k) {
+    Acc a;
+    a.init();
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) a.add(part[b * 8 + off + k]);
+    ss[threadIdx.x] = a.s;
+    sc[threadIdx.x] = a.c;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+      if ((int)threadIdx.x < o) {
+        Acc t;
+        t.s = ss[threadIdx.x];
+        t.c = sc[threadIdx.x];
+        t.merge(ss[threadIdx.x + o], sc[threadIdx.x + o]);
+        ss[threadIdx.x] = t.s;
+        sc[threadIdx.x] = t.c;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) st->red[dst + k] = ss[0] + sc[0];
+    __syncthreads();
+  }
+}
+__global__ void __launch_bounds__(256) k_fire_max_finish(const double* part, int nblk, int off, int nv, FireState* st, int dst) {
+  __shared__ double sm[256];
+  for (int k = 0; k < nv; ++k) {
+    double m = 0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) m = fmax(m, part[b * 8 + off + k]);
+    sm[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+      if ((int)threadIdx.x < o) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) st->red[dst + k] = sm[0];
+    __syncthreads();
+  }
+}
+
+// mixing coefficient sqrt(vnorm/fnorm), norms taken as the reference does (:283-293)
+__global__ void k_fc_mid(FireState* st) {
+  if (st->skip) return;
+  const double nv = sqrt(st->red[0]), nf = sqrt(st->red[1]);
+  st->coef = sqrt((nv * nv) / (nf * nf));
+}
+
+// v = (1-a) v - a c g; x += dt v; rho = alias(x) (:292-297, src/FMT_Species.cpp:29-45)
+template <class S>
+__global__ void __launch_bounds__(kThreads) k_fire_mix(S* x0, S* x1, S* v0, S* v1, const S* g0, const S* g1, S* rho, const FireState* st,
+                                                       long n, FireConsts k) {
+  if (st->skip) return;
+  const int cur = st->cur;
+  S* x = cur ? x0 : x1;  // the pending state
+  S* v = cur ? v0 : v1;
+  const S* g = cur ? g1 : g0;
+  const S a = (S)st->alpha, coef = (S)(st->alpha * st->coef), dt = (S)st->dt;
+  const S dmin = (S)k.dmin, c = (S)k.c;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    S vi = v[i] * ((S)1 - a);
+    vi += g[i] * (-coef);
+    const S xi = x[i] + vi * dt;
+    v[i] = vi;
+    x[i] = xi;
+    rho[i] = dmin + c * xi * xi / ((S)1 + xi * xi);
+  }
+}
+
+// Species::beginForceCalculation under fixed mass (src/Species.cpp:64-71)
+template <class S>
+__global__ void __launch_bounds__(kThreads) k_sum_rho(const S* rho, long n, const FireState* st, double* part) {
+  if (st->skip) return;
+  double acc[1] = {0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) acc[0] += (double)rho[i];
+  block_sums_to<S>(acc, 1, part);
+}
+template <class S>
+__global__ void k_scale_rho(S* rho, long n, const FireState* st, FireConsts k) {
+  if (st->skip) return;
+  const S f = (S)(k.fixed_mass / (st->red[6] * k.dV));
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) rho[i] *= f;
+}
+
+// Terms of DFT::calculateFreeEnergyAndDerivatives from the evaluator's sums;
+// fixed mass: mu = sum dF rho / M (src/Species.cpp:97-109).
+__global__ void k_eval_finish(const double* terms, const unsigned* status, FireState* st, FireConsts k, double mu, int has_fmt, int has_mf) {
+  if (st->skip) return;
+  const double dV = k.dV;
+  const double f_hs = has_fmt ? terms[0] * dV : 0.0;
+  const double f_mf = has_mf ? 0.5 * dV * terms[1] : 0.0;
+  const double f_id = terms[2];
+  const double f_ext = terms[4] * dV - (terms[3] * dV) * mu;
+  st->f_hs = f_hs;
+  st->f_mf = f_mf;
+  st->f_id = f_id;
+  st->f_ext = f_ext;
+  st->natoms = terms[3] * dV;
+  st->omega = ((f_id + f_hs) + f_mf) + f_ext;
+  st->failed = (*status & 1u) ? 1 : 0;
+  if (*status & kStatusTimeout) {
+    st->status = CDFT_ERR_TIMEOUT;
+    st->done = 1;
+  }
+  st->mu = (k.fixed_mass > 0) ? terms[5] / k.fixed_mass : mu;
+}
+template <class S>
+__global__ void k_sub_mu(S* dF, long n, const FireState* st, FireConsts k) {
+  if (st->skip || st->failed) return;
+  const S m = (S)(st->mu * k.dV);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) dF[i] = dF[i] - m;
+}
+
+// Minimizer::getDF_DX after the evaluation (src/Minimizer.cpp:90-115): alias
+// derivative into g of the pending state; sums v.g; maxima |dF|, |g|.
+template <class S>
+__global__ void __launch_bounds__(kThreads) k_fire_post(const S* dF, const S* x0, const S* x1, const S* v0, const S* v1, S* g0, S* g1,
+                                                        const FireState* st, long n, FireConsts k, double* part) {
+  if (st->skip || st->failed) return;
+  const int nxt = 1 - st->cur;
+  const S* x = nxt ? x1 : x0;
+  const S* v = nxt ? v1 : v0;
+  S* g = nxt ? g1 : g0;
+  const S c2 = (S)(2 * k.c);
+  double acc[1] = {0}, mx[2] = {0, 0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const S y = x[i], d = dF[i];
+    const S q = (S)1 + y * y;
+    const S ga = d * (c2 * y / (q * q));
+    g[i] = ga;
+    acc[0] += (double)(v[i] * ga);
+    mx[0] = fmax(mx[0], (double)fabs(d));
+    mx[1] = fmax(mx[1], (double)fabs(ga));
+  }
+  block_sums_to<S>(acc, 1, part);
+  block_max_to<S>(mx, 2, 1, part);
+}
+
+// step end: accept or back track (src/Minimizer.cpp:218-257)
+__global__ void k_fc_post(FireState* st, FireConsts k) {
+  if (st->skip) return;
+  st->calls++;
+  if (st->failed) {
+    st->vscale *= 0.5;
+    st->vdotf *= 0.5;
+    st->dt /= 2;
+    st->fmax = 1000;
+    st->backtracks++;
+  } else {
+    st->F = st->omega;
+    st->cur = 1 - st->cur;
+    st->vscale = 1.0;
+    st->vdotf = st->red[3];
+    st->resid = st->red[4] / k.dV;
+    st->fmax = st->red[5] / k.dV;
+    st->vv = st->vv * 0.9 + 0.1 * (fabs(st->F - st->fold) / st->dt);
+    st->dt_best = fmax(st->dt, st->dt_best);
+  }
+  if (st->backtracks >= 10) {
+    st->dt_max = fmin(st->dt_best, 0.9 * st->dt_max);
+    st->dt_best = 0;
+    st->backtracks = 0;
+  }
+  st->steps++;
+  if (!st->failed && k.tol > 0 && st->resid <= k.tol) st->done = 1;
+}
+
+template <class S>
+__global__ void k_convert(const double* a, S* b, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = (S)a[i];
+}
+template <class S>
+__global__ void k_convert_back(const S* a, double* b, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = (double)a[i];
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- engine ---
+struct FireDevEngine {
+  cudaStream_t stream = nullptr;
+  FireState* st = nullptr;      // device
+  FireState* host = nullptr;    // pinned
+  double* part = nullptr;       // 8 doubles per block
+  // FP32 phase arrays
+  float *x32[2] = {nullptr, nullptr}, *v32[2] = {nullptr, nullptr}, *g32[2] = {nullptr, nullptr}, *rho32 = nullptr, *dF32 = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int exec_prec = -1;
+  ~FireDevEngine() {
+    if (exec) cudaGraphExecDestroy(exec);
+    cudaFree(st); cudaFreeHost(host); cudaFree(part);
+    for (int i = 0; i < 2; ++i) { cudaFree(x32[i]); cudaFree(v32[i]); cudaFree(g32[i]); }
+    cudaFree(rho32); cudaFree(dF32);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+void cdft_internal_fire_dev_free(cdft_ctx* c) {
+  delete c->fire_dev;
+  c->fire_dev = nullptr;
+}
+
+static FireConsts consts_of(const cdft_ctx* c, double tol) {
+  FireConsts k;
+  const Alias a = c->alias();
+  k.dmin = a.dmin;
+  k.c = a.c;
+  k.dV = c->info.dV;
+  k.volume = c->info.volume;
+  k.f_inc = c->fp.f_inc;
+  k.f_dec = c->fp.f_dec;
+  k.f_alf = c->fp.f_alf;
+  k.alpha_start = c->fp.alpha_start;
+  k.dt_min = c->fp.dt_min;
+  k.n_delay = c->fp.n_delay;
+  k.n_neg_max = c->fp.n_p_negative_max;
+  k.initial_delay = c->fp.initial_delay;
+  k.tol = tol;
+  k.fixed_mass = c->fixed_mass;
+  k.N = c->info.N;
+  return k;
+}
+
+static void state_from_ctx(const cdft_ctx* c, FireState* h) {
+  std::memset(h, 0, sizeof(FireState));
+  h->F = c->F; h->dt = c->dt; h->dt_max = c->dt_max; h->alpha = c->alpha; h->vv = c->vv; h->dt_best = c->dt_best;
+  h->fmax = c->fmax; h->resid = c->resid; h->vdotf = c->vdotf; h->vscale = 1.0; h->mu = c->mu;
+  h->Npos = c->Npos; h->Nneg = c->Nneg; h->backtracks = c->backtracks; h->cur = c->cur; h->it = c->it;
+  h->steps = c->fire_steps; h->calls = c->calls;
+}
+static void ctx_from_state(cdft_ctx* c, const FireState* h) {
+  c->F = h->F; c->dt = h->dt; c->dt_max = h->dt_max; c->alpha = h->alpha; c->vv = h->vv; c->dt_best = h->dt_best;
+  c->fmax = h->fmax; c->resid = h->resid; c->vdotf = h->vdotf;
+  c->Npos = h->Npos; c->Nneg = h->Nneg; c->backtracks = h->backtracks; c->cur = h->cur; c->it = h->it;
+  c->fire_steps = h->steps; c->calls = h->calls;
+  if (c->fixed_mass > 0) c->mu = h->mu;
+}
+
+// Records one FIRE2 step on the engine's stream (to be captured).
+template <class S, class T>
+static void record_step(cdft_ctx* c, FireDevEngine* E, Evaluator<T>* ev, S* x[2], S* v[2], S* g[2], S* rho, S* dF, double tol) {
+  const long N = c->info.N;
+  const unsigned gn = grid_n(N);
+  const FireConsts k = consts_of(c, tol);
+  cudaStream_t s = E->stream;
+  k_fc_pre<<<1, 1, 0, s>>>(E->st, k);
+  k_fire_pre<S><<<gn, kThreads, 0, s>>>(x[0], x[1], v[0], v[1], g[0], g[1], E->st, N, E->part);
+  k_fire_sum_finish<<<1, 256, 0, s>>>(E->part, (int)gn, 0, 2, E->st, 0);
+  k_fc_mid<<<1, 1, 0, s>>>(E->st);
+  k_fire_mix<S><<<gn, kThreads, 0, s>>>(x[0], x[1], v[0], v[1], g[0], g[1], rho, E->st, N, k);
+  const double mu_eval = c->fixed_mass > 0 ? 0.0 : c->mu;
+  if (c->fixed_mass > 0) {
+    k_sum_rho<S><<<gn, kThreads, 0, s>>>(rho, N, E->st, E->part);
+    k_fire_sum_finish<<<1, 256, 0, s>>>(E->part, (int)gn, 0, 1, E->st, 6);
+    k_scale_rho<S><<<gn, kThreads, 0, s>>>(rho, N, E->st, k);
+  }
+  ev->template launch<S>(rho, c->vext, dF, c->info.dV, mu_eval, 1, s, nullptr);
+  k_eval_finish<<<1, 1, 0, s>>>(ev->dev_terms(), ev->dev_status(), E->st, k, mu_eval, ev->M() > 0 ? 1 : 0, ev->has_mf() ? 1 : 0);
+  if (c->fixed_mass > 0) k_sub_mu<S><<<gn, kThreads, 0, s>>>(dF, N, E->st, k);
+  k_fire_post<S><<<gn, kThreads, 0, s>>>(dF, x[0], x[1], v[0], v[1], g[0], g[1], E->st, N, k, E->part);
+  k_fire_sum_finish<<<1, 256, 0, s>>>(E->part, (int)gn, 0, 1, E->st, 3);
+  k_fire_max_finish<<<1, 256, 0, s>>>(E->part, (int)gn, 1, 2, E->st, 4);
+  k_fc_post<<<1, 1, 0, s>>>(E->st, k);
+}
+
+static int ensure_engine(cdft_ctx* c) {
+  if (c->fire_dev) return CDFT_OK;
+  FireDevEngine* E = new FireDevEngine();
+  c->fire_dev = E;
+  const long N = c->info.N;
+  if (cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) != cudaSuccess || cudaMalloc(&E->st, sizeof(FireState)) != cudaSuccess ||
+      cudaMallocHost(&E->host, sizeof(FireState)) != cudaSuccess || cudaMalloc(&E->part, (size_t)152 * 8 * 8 * sizeof(double)) != cudaSuccess)
+    return cdft_internal_fail(c, CDFT_ERR_CUDA, "device FIRE engine allocation failed");
+  (void)N;
+  return CDFT_OK;
+}
+
+static int ensure_fp32_arrays(cdft_ctx* c) {
+  FireDevEngine* E = c->fire_dev;
+  if (E->rho32) return CDFT_OK;
+  const size_t b = c->info.N * sizeof(float);
+  for (int i = 0; i < 2; ++i)
+    if (cudaMalloc(&E->x32[i], b) != cudaSuccess || cudaMalloc(&E->v32[i], b) != cudaSuccess || cudaMalloc(&E->g32[i], b) != cudaSuccess)
+      return cdft_internal_fail(c, CDFT_ERR_CUDA, "FP32 FIRE arrays");
+  if (cudaMalloc(&E->rho32, b) != cudaSuccess || cudaMalloc(&E->dF32, b) != cudaSuccess)
+    return cdft_internal_fail(c, CDFT_ERR_CUDA, "FP32 FIRE arrays");
+  return CDFT_OK;
+}
+
+// Runs graph-captured steps in precision `prec` until done (residual target,
+// uphill limit, timeout), max_steps, or - for the FP32 phase - until the
+// residual stops improving (stall) or drops below switch_tol.
+static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long max_steps, long* taken, int* stop) {
+  FireDevEngine* E = c->fire_dev;
+  const long N = c->info.N;
+  const unsigned gn = grid_n(N);
+  cudaStream_t s = E->stream;
+  // upload state; move vectors into the phase's storage
+  state_from_ctx(c, E->host);
+  cudaMemcpyAsync(E->st, E->host, sizeof(FireState), cudaMemcpyHostToDevice, s);
+  if (prec == CDFT_FP32) {
+    int rc = ensure_fp32_arrays(c);
+    if (rc) return rc;
+    for (int i = 0; i < 2; ++i) {
+      k_convert<float><<<gn, kThreads, 0, s>>>(c->fx[i], E->x32[i], N);
+      k_convert<float><<<gn, kThreads, 0, s>>>(c->fv[i], E->v32[i], N);
+      k_convert<float><<<gn, kThreads, 0, s>>>(c->fg[i], E->g32[i], N);
+    }
+  }
+  // capture one step
+  cudaGraph_t graph;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return cdft_internal_fail(c, CDFT_ERR_CUDA, "capture");
+  if (prec == CDFT_FP32) {
+    float* x[2] = {E->x32[0], E->x32[1]};
+    float* v[2] = {E->v32[0], E->v32[1]};
+    float* g[2] = {E->g32[0], E->g32[1]};
+    record_step<float, float>(c, E, c->e32.get(), x, v, g, E->rho32, E->dF32, prec == CDFT_FP64 ? tol : 0.0);
+  } else {
+    record_step<double, double>(c, E, c->e64.get(), c->fx, c->fv, c->fg, c->rho, c->dF, tol);
+  }
+  if (cudaStreamEndCapture(s, &graph) != cudaSuccess) return cdft_internal_fail(c, CDFT_ERR_CUDA, "capture end");
+  if (E->exec) cudaGraphExecDestroy(E->exec);
+  E->exec = nullptr;
+  if (cudaGraphInstantiate(&E->exec, graph, 0) != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return cdft_internal_fail(c, CDFT_ERR_CUDA, "graph instantiate");
+  }
+  cudaGraphDestroy(graph);
+  const int batch = 16;
+  long k = 0;
+  double best = 1e300;
+  long best_at = 0;
+  *stop = 0;
+  while (true) {
+    const long nb = (max_steps > 0) ? std::min<long>(batch, max_steps - k) : batch;
+    if (nb <= 0) break;
+    for (long j = 0; j < nb; ++j) cudaGraphLaunch(E->exec, s);
+    cudaMemcpyAsync(E->host, E->st, sizeof(FireState), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cdft_internal_fail(c, CDFT_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    const FireState& h = *E->host;
+    k = h.steps - c->fire_steps;
+    if (h.status) {
+      ctx_from_state(c, E->host);
+      *taken = k;
+      return cdft_internal_fail(c, h.status, h.status == CDFT_ERR_UPHILL ? "Cannot stop going uphill in Fire2" : "device wait timed out");
+    }
+    if (h.done) { *stop = 2; break; }
+    if (prec == CDFT_FP32) {
+      if (h.resid < best * 0.98) { best = h.resid; best_at = k; }
+      if (h.resid <= switch_tol) { *stop = 3; break; }
+      if (k - best_at > 400) { *stop = 4; break; }  // the FP32 residual has stalled
+    }
+    if (max_steps > 0 && k >= max_steps) break;
+  }
+  // download: scalars, and the FP32 phase's vectors back into FP64 storage
+  ctx_from_state(c, E->host);
+  if (prec == CDFT_FP32) {
+    for (int i = 0; i < 2; ++i) {
+      k_convert_back<float><<<gn, kThreads, 0, s>>>(E->x32[i], c->fx[i], N);
+      k_convert_back<float><<<gn, kThreads, 0, s>>>(E->v32[i], c->fv[i], N);
+      k_convert_back<float><<<gn, kThreads, 0, s>>>(E->g32[i], c->fg[i], N);
+    }
+    k_convert_back<float><<<gn, kThreads, 0, s>>>(E->rho32, c->rho, N);
+    k_convert_back<float><<<gn, kThreads, 0, s>>>(E->dF32, c->dF, N);
+  }
+  cudaStreamSynchronize(s);
+  *taken = k;
+  return CDFT_OK;
+}
+
+static void report_of(const cdft_ctx* c, long steps, int stop, cdft_fire_report* r, long steps32 = 0) {
+  if (!r) return;
+  r->steps_fp32 = steps32;
+  r->steps = steps;
+  r->total_steps = c->fire_steps;
+  r->calls = c->calls;
+  r->F = c->F;
+  r->dt = c->dt;
+  r->dt_max = c->dt_max;
+  r->alpha = c->alpha;
+  r->vv = c->vv;
+  r->fmax = c->fmax;
+  r->resid = c->resid;
+  r->backtracks = 0;
+  r->stop = stop;
+}
+
+__global__ void k_rho_from_alias_pub(const double* x, double* rho, long n, Alias a) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double y = x[i];
+    rho[i] = a.dmin + a.c * y * y / (1 + y * y);
+  }
+}
+
+// Re-evaluates in FP64 at the current alias state (the refinement phase's
+// first gradient): rho = alias(x[cur]), F, dF, g[cur], v.g, residual.
+static int refresh_fp64(cdft_ctx* c) {
+  int rc = cdft_set_precision(c, CDFT_FP64);
+  if (rc) return rc;
+  cudaStreamSynchronize(c->fire_dev->stream);
+  const long N = c->info.N;
+  k_rho_from_alias_pub<<<grid_n(N), kThreads, 0, c->stream>>>(c->fx[c->cur], c->rho, N, c->alias());
+  double t[8];
+  rc = cdft_internal_eval(c, t, 0);
+  if (rc) return rc;
+  c->F = t[0];
+  return cdft_internal_fire_accept(c, c->cur);
+}
+
+extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch_tol, long max_steps, int mixed, cdft_fire_report* rep) {
+  if (!c) return CDFT_ERR_ARG;
+  if (!c->fire_ready) return cdft_internal_fail(c, CDFT_ERR_STATE, "cdft_fire_init has not been called");
+  int rc = ensure_engine(c);
+  if (rc) return rc;
+  long total = 0, taken = 0, steps32 = 0;
+  int stop = 0;
+  if (mixed) {
+    rc = cdft_set_precision(c, CDFT_FP32);
+    if (rc) return rc;
+    rc = run_phase(c, CDFT_FP32, resid_tol, switch_tol, max_steps, &taken, &stop);
+    total += taken;
+    steps32 = taken;
+    if (rc) {
+      report_of(c, total, stop, rep, steps32);
+      return rc;
+    }
+    rc = refresh_fp64(c);
+    if (rc) return rc;
+    if (max_steps > 0 && total >= max_steps) {
+      report_of(c, total, 0, rep, steps32);
+      return CDFT_OK;
+    }
+    if (c->resid <= resid_tol) {
+      report_of(c, total, 2, rep, steps32);
+      return CDFT_OK;
+    }
+  }
+  rc = run_phase(c, CDFT_FP64, resid_tol, 0.0, max_steps > 0 ? max_steps - total : -1, &taken, &stop);
+  total += taken;
+  report_of(c, total, stop, rep, steps32);
+  return rc;
+}

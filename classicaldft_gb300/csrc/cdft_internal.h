@@ -51,8 +51,14 @@ class Evaluator {
   int eval(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, EvalTerms* out, cudaStream_t s);
   // Launches the pass sequence without host synchronisation; partial sums land in dev_terms.
   // ev (optional, 10 events) are recorded before pass 0 and after each of the 9 passes.
+  // RT: storage type of rho and dF (double, or T for an all-T pipeline).
+  template <class RT>
+  int launch(const RT* rho, const double* vext, RT* dF, double dV, double mu, int ideal, cudaStream_t s, cudaEvent_t* ev = nullptr);
   int launch(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, cudaStream_t s,
-             cudaEvent_t* ev = nullptr);
+             cudaEvent_t* ev = nullptr) {
+    return launch<double>(rho, vext, dF, dV, mu, ideal, s, ev);
+  }
+  bool has_mf() const { return mf_; }
   // Algorithmic bytes each of the 9 passes must move (reads + writes once).
   void pass_bytes(double* bytes) const;
   bool setup_tma(std::string* err);

@@ -416,9 +416,9 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
 //   dF = ln(rho) dV + c2r(E) dV + V_ext dV - mu dV
 // with FP64 partial sums: F_id = sum (rho ln rho - rho) dV, sum rho,
 // sum V_ext rho, sum dF rho (for the fixed-mass projection).
-template <class T>
-__global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* __restrict__ E, const double* __restrict__ rho,
-                                                    const double* __restrict__ vext, double* __restrict__ dF, Dims d, FFTPlan pz,
+template <class T, class RT = double>
+__global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* __restrict__ E, const RT* __restrict__ rho,
+                                                    const double* __restrict__ vext, RT* __restrict__ dF, Dims d, FFTPlan pz,
                                                     const typename Cx<T>::type* __restrict__ tw, int RB, double dV, double mu,
                                                     int have_fmt_or_mf, int ideal, double* __restrict__ part) {
   typedef typename Cx<T>::type C;
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     f += h * dVt;
     f += ve * dVt;
     f += -mut * dVt;
-    dF[p] = (double)f;
+    dF[p] = (RT)f;
     if (ideal) ks[0].add((r0 * lr - r0) * dVt);
     ks[1].add(r0);
     ks[2].add(ve * r0);

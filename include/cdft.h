@@ -141,6 +141,7 @@ typedef struct cdft_fire_report {
   double resid;      /* max |dOmega/drho| = max|dF|/dV before alias conversion, last accepted evaluation */
   int backtracks;    /* eta > 1 backtracks seen by this call */
   int stop;          /* 0 max steps, 1 force limit, 2 residual target */
+  long steps_fp32;   /* steps of this call taken in the FP32 bulk phase (cdft_fire_run_device, mixed) */
 } cdft_fire_report;
 
 int cdft_fire_default_params(cdft_fire_params* p);
@@ -153,6 +154,17 @@ int cdft_fire_run(cdft_ctx* ctx, long max_steps, cdft_fire_report* rep);
 /* The same FIRE2 steps, stopping when max|dOmega/drho| <= resid_tol (the
  * residual the reference's Species::get_convergence_monitor reports) or max_steps. */
 int cdft_fire_run_to_residual(cdft_ctx* ctx, double resid_tol, long max_steps, cdft_fire_report* rep);
+
+/* The same FIRE2 steps, run device-resident: the step's scalar logic runs in
+ * one-thread control kernels and one whole step (vector passes, evaluation,
+ * Species constraints, alias conversion) is captured once as a CUDA graph, so
+ * no host round trip sits inside a step; the host reads the state every 16
+ * steps. Stops when max|dOmega/drho| <= resid_tol (taken from an FP64
+ * evaluation), on the uphill limit, or after max_steps (> 0).
+ * mixed = 0: FP64 throughout. mixed = 1: an FP32 bulk phase (vectors and
+ * evaluations in FP32) until its residual drops below switch_tol or stops
+ * improving, then one FP64 evaluation at the same state and FP64 refinement. */
+int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, long max_steps, int mixed, cdft_fire_report* rep);
 
 /* DDFT integrating-factor dynamics, single species, periodic (include/Minimizer.h:189-266, src/DDFT.cpp:42-351). */
 typedef struct cdft_ddft_report {

@@ -1,0 +1,69 @@
+"""Device-resident, graph-captured FIRE2 (cdft_fire_run_device): the same
+steps as the host-driven path (which matches the reference's trajectory), and
+the mixed FP32 -> FP64 policy reaching the same minimum as plain FP64."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def droplet(shape, dx, R, rho_v=0.01, rho_l=0.75, w=0.5):
+    ax = [dx * (np.arange(m) - m / 2.0) for m in shape]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    r = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
+    return rho_v + (rho_l - rho_v) * 0.5 * (1 - np.tanh((r - R) / w))
+
+
+def test_device_fire_matches_reference_trajectory():
+    import classicaldft_gb300 as cd
+    from oracle import pyoracle
+    g = golden("fire_hs32")
+    c = cd.Context(32, 0.2, cd.WHITEBEAR_I, hsd=1.0)
+    c.set_chem_potential(c.bulk(0.7)["mu"])
+    c.set_density(pyoracle.fill_noise((32, 32, 32), 0.7, 0.05, 20240601))
+    c.fire_init(force_limit=0.0)
+    r = c.fire_run_device(0.0, max_steps=200)
+    assert r["total_steps"] == 200
+    assert r["dt"] == g["fire32.dt"][199] and r["alpha"] == g["fire32.alpha"][199]
+    assert abs(r["F"] - g["fire32.F"][199]) <= 1e-12 * abs(r["F"])
+    pos = g["fire32.pos"].astype(np.int64)
+    np.testing.assert_allclose(c.get_density().ravel()[pos], g["fire32.rho_final.sample"], rtol=0, atol=1e-12)
+
+
+def test_device_fire_fixed_mass_matches_host_path():
+    import classicaldft_gb300 as cd
+    rho = golden("eval_lj")["lj24.rho"].reshape(24, 24, 24)
+    hsd = golden("eval_lj")["lj24.hsd"][0]
+    runs = []
+    for device in (False, True):
+        c = cd.Context(24, 0.2, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.8, fixed_mass=rho.sum() * 0.2 ** 3)
+        c.set_density(rho)
+        c.fire_init(force_limit=0.0)
+        r = c.fire_run_device(0.0, max_steps=60) if device else c.fire_step(60)
+        runs.append((r, c.get_density()))
+    (rh, dh), (rd, dd) = runs
+    assert rh["dt"] == rd["dt"] and rh["alpha"] == rd["alpha"]
+    assert abs(rh["F"] - rd["F"]) <= 1e-12 * abs(rh["F"])
+    np.testing.assert_allclose(dd, dh, rtol=0, atol=1e-12)
+
+
+def test_mixed_precision_reaches_fp64_minimum():
+    import classicaldft_gb300 as cd
+    shape, dx = (32, 32, 32), 0.2
+    rho = droplet(shape, dx, R=1.8)
+    mass = rho.sum() * dx ** 3
+    hsd = cd.bh_diameter(1, 1, 3, 0.8)
+    res = {}
+    for mixed in (False, True):
+        c = cd.Context(shape, dx, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.8, fixed_mass=mass)
+        c.set_density(rho)
+        c.fire_init(force_limit=0.0, dt=1e-3, dt_max=1e-2)
+        r = c.fire_run_device(1e-8, max_steps=40000, mixed=mixed, switch_tol=2e-6)
+        assert r["resid"] <= 1e-8, r
+        t, dF = c.eval()
+        assert t["resid"] <= 1e-8
+        res[mixed] = (t["Omega"], c.get_density(), r["total_steps"])
+    assert abs(res[True][0] - res[False][0]) <= 1e-10 * abs(res[False][0])
+    np.testing.assert_allclose(res[True][1], res[False][1], rtol=0, atol=1e-6)
