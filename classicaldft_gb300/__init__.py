@@ -31,7 +31,7 @@ C_FUNCTIONS = [
     "cdft_set_density", "cdft_get_density", "cdft_set_external_field", "cdft_set_chem_potential",
     "cdft_set_fixed_mass", "cdft_get_chem_potential", "cdft_eval", "cdft_bulk", "cdft_bh_diameter",
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
-    "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device",
+    "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device", "cdft_find_coex",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -111,6 +111,7 @@ def lib():
             "cdft_fmt_weights": ([i, i, i, d, d, dp], i),
             "cdft_number_of_atoms_noalloc": ([vp, ctypes.c_long, d, vp, dp], i),
             "cdft_fire_run_device": ([vp, d, d, ctypes.c_long, i, P(FireReport)], i),
+            "cdft_find_coex": ([vp, d, d, d, dp], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -242,6 +243,12 @@ class Context:
         out = np.zeros(3)
         self._check(lib().cdft_bulk(self._h, rho, _dptr(out)))
         return {"mu": out[0], "omega": out[1], "fhelmholtz": out[2]}
+
+    def find_coex(self, xmax=1.0, dx=1e-3, tol=1e-8):
+        """DFT::findCoex: {x_vap, x_liq, mu, spinodal1, spinodal2}."""
+        out = np.zeros(5)
+        self._check(lib().cdft_find_coex(self._h, xmax, dx, tol, _dptr(out)))
+        return dict(zip(("x_vap", "x_liq", "mu", "spinodal1", "spinodal2"), out))
 
     def weights(self):
         w = np.zeros((11,) + self.shape)

@@ -460,6 +460,85 @@ int cdft_eval(cdft_ctx* c, int only_fex, double* terms, double* dF, int on_devic
   return rc;
 }
 
+// ------------------------------------------------ bulk phase equilibria ---
+// DFT::findSpinodal / find_density_from_mu / findCoex (src/DFT_Coex.cpp:53-196):
+// golden-section search for the stationary points of the pressure p = -omega,
+// bisection on mu, and bisection on the pressure difference along mu(x_vap) = mu(x_liq).
+namespace {
+struct Bulk {
+  const cdft_ctx* c;
+  double mu(double x) const { double o[3]; cdft_bulk(c, x, o); return o[0]; }
+  double p(double x) const { double o[3]; cdft_bulk(c, x, o); return -o[1]; }
+};
+bool spinodal(const Bulk& B, double xmax, double dx, double& xs1, double& xs2, double tol) {
+  double x = 2 * dx, p = B.p(2 * dx), dp = p - B.p(dx);
+  if (dp < 0) return false;
+  while (dp > 0 && x < xmax - dx) { dp = -p; x += dx; p = B.p(x); dp += p; }
+  if (x >= xmax - dx) return false;
+  const double r = (3 - std::sqrt(5.0)) / 2;
+  double a = x - 2 * dx, b = x, u = a + r * (b - a), v = b - r * (b - a), fu = B.p(u), fv = B.p(v);
+  do {
+    if (fu > fv) { b = v; v = u; fv = fu; u = a + r * (b - a); fu = B.p(u); }
+    else { a = u; u = v; fu = fv; v = b - r * (b - a); fv = B.p(v); }
+  } while (b - a > 1e-8);
+  xs1 = (a + b) / 2;
+  x = xs1;
+  p = B.p(x);
+  do { dp = -p; x += dx; p = B.p(x); dp += p; } while (dp < 0 && x < xmax - dx);
+  if (x >= xmax - dx) return false;
+  a = x - 2 * dx; b = x; u = a + r * (b - a); v = b - r * (b - a); fu = B.p(u); fv = B.p(v);
+  do {
+    if (fu < fv) { b = v; v = u; fv = fu; u = a + r * (b - a); fu = B.p(u); }
+    else { a = u; u = v; fu = fv; v = b - r * (b - a); fv = B.p(v); }
+  } while (b - a > tol);
+  xs2 = (a + b) / 2;
+  return true;
+}
+bool density_from_mu(const Bulk& B, double mu, double xmin, double xmax, double tol, double& out) {
+  double mu1 = B.mu(xmin), mu2 = B.mu(xmax);
+  if (mu1 > mu2) { std::swap(xmin, xmax); std::swap(mu1, mu2); }
+  if (mu2 < mu || mu1 > mu) return false;
+  do {
+    const double x = (xmin + xmax) / 2, m = B.mu(x);
+    if (m > mu) { xmax = x; mu2 = m; }
+    else { xmin = x; mu1 = m; }
+  } while (mu2 - mu1 > tol);
+  out = (xmin + xmax) / 2;
+  return true;
+}
+}  // namespace
+
+int cdft_find_coex(const cdft_ctx* c, double xmax, double dx, double tol, double* out) {
+  if (!c || !out || !(xmax > 0) || !(dx > 0) || !(tol > 0)) return CDFT_ERR_ARG;
+  const Bulk B{c};
+  double xs1, xs2;
+  if (!spinodal(B, xmax, dx, xs1, xs2, tol)) return CDFT_ERR_ARG;
+  double xvap = xs1, xliq;
+  if (!density_from_mu(B, B.mu(xvap), xs2, xmax - dx, tol, xliq)) return CDFT_ERR_ARG;
+  double dp1 = B.p(xvap) - B.p(xliq), dp2;
+  do {
+    dp2 = dp1;
+    xvap /= 1.1;
+    if (!density_from_mu(B, B.mu(xvap), xs2, xmax - dx, tol, xliq)) return CDFT_ERR_ARG;
+    dp1 = B.p(xvap) - B.p(xliq);
+  } while (xvap > 1e-16 && ((dp1 < 0) == (dp2 < 0)));
+  if (xvap < 1e-16) return CDFT_ERR_ARG;
+  double y1 = xvap, y2 = xvap * 1.1;
+  do {
+    const double y = (y1 + y2) / 2;
+    if (!density_from_mu(B, B.mu(y), xs2, xmax - dx, tol, xliq)) return CDFT_ERR_ARG;
+    const double dp = B.p(y) - B.p(xliq);
+    if ((dp < 0) == (dp1 < 0)) { y1 = y; dp1 = dp; }
+    else { y2 = y; dp2 = dp; }
+  } while (std::fabs(y2 - y1) > tol);
+  out[0] = (y1 + y2) / 2;
+  out[1] = xliq;
+  out[2] = B.mu(out[0]);
+  out[3] = xs1;
+  out[4] = xs2;
+  return CDFT_OK;
+}
+
 int cdft_time_passes(cdft_ctx* c, int reps, double* ms, double* bytes, int* npass) {
   if (!c || reps < 1) return CDFT_ERR_ARG;
   int rc = ensure_evaluator(c, c->precision);
@@ -779,6 +858,8 @@ int cdft_ddft_init(cdft_ctx* c, double dt, double dt_max, double tol) {
   double t[8];
   int rc = eval_internal(c, t);  // the constructor's evaluation (src/DDFT.cpp:52)
   if (rc) return rc;
+  rc = map_reduce<1, 0>(c, N, FSumRho{c->rho}, &c->ddft_mass0);
+  if (rc) return rc;
   c->ddft_dt = dt;
   c->ddft_dt_max = dt_max;
   c->ddft_tol = tol;
@@ -857,6 +938,14 @@ static int ddft_one_step(cdft_ctx* c, int* restarts) {
         k_ddft_prop<float><<<g, 256, 0, c->stream>>>((const float2*)c->rk0, (const float2*)c->R0k, (const float2*)c->R1k, (float2*)c->work,
                                                       c->dfac, nx, ny, nzc, pz, c->ddft_dt);
         c->e32->c2r((const float2*)c->work, c->ddn, 1.0f / (float)N, c->stream);
+      }
+      if (c->precision == CDFT_FP32) {
+        // FP32 transforms keep the k = 0 mode only to FP32 rounding: restore
+        // the run's mass with a uniform FP64 shift (compensated FP64 sum).
+        double m;
+        rc = map_reduce<1, 0>(c, N, FSumRho{c->ddn}, &m);
+        if (rc) return rc;
+        k_add_const<<<grid_for(N), 256, 0, c->stream>>>(c->ddn, N, (m - c->ddft_mass0) / (double)N);
       }
       double red[2];
       rc = map_reduce<0, 2>(c, N, FDdftDev{c->dd1, c->ddn}, red);

@@ -47,6 +47,7 @@ struct cdft_ctx {
   // DDFT state
   bool ddft_ready = false;
   double ddft_dt = 0, ddft_dt_max = 1, ddft_tol = 1e-4, ddft_time = 0, ddft_rhs = 1;
+  double ddft_mass0 = 0;  // sum rho of the run's start (FP32 mode restores it after each propagation)
   bool ddft_have_factors = false;
   int ddft_successes = 0;
   double *dd0 = nullptr, *dd1 = nullptr, *ddn = nullptr, *dR = nullptr, *dfac = nullptr;

@@ -495,7 +495,7 @@ static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long 
     if (prec == CDFT_FP32) {
       if (h.resid < best * 0.98) { best = h.resid; best_at = k; }
       if (h.resid <= switch_tol) { *stop = 3; break; }
-      if (k - best_at > 400) { *stop = 4; break; }  // the FP32 residual has stalled
+      if (k - best_at > 96) { *stop = 4; break; }  // the FP32 residual has stalled (its noise floor)
     }
     if (max_steps > 0 && k >= max_steps) break;
   }

@@ -107,6 +107,13 @@ int cdft_time_passes(cdft_ctx* ctx, int reps, double* ms, double* bytes, int* np
  * omega_times_beta_over_volume, fhelmholtz_times_beta_over_volume} (src/DFT.cpp:58-115). */
 int cdft_bulk(const cdft_ctx* ctx, double rho, double* out3);
 
+/* Bulk liquid-vapour coexistence of the context's functional:
+ * DFT::findSpinodal + DFT::findCoex (src/DFT_Coex.cpp:53-196). Searches densities
+ * up to xmax with step dx and tolerance tol; out = {x_vap, x_liq, mu_coex
+ * (= mu_times_beta(x_vap)), spinodal x1, spinodal x2}. CDFT_ERR_ARG when no
+ * coexistence is bracketed (e.g. above the critical temperature). */
+int cdft_find_coex(const cdft_ctx* ctx, double xmax, double dx, double tol, double* out5);
+
 /* Potential1::getHSD(kT) of LJ(sigma, eps, rc) with setBH() (include/Potential1.h:73-83):
  * the Barker-Henderson diameter int_0^{r0} (1 - exp(-V(r)/kT)) dr, integrated to 1e-15. */
 int cdft_bh_diameter(double sigma, double eps, double rc, double kT, double* out);
@@ -162,8 +169,9 @@ int cdft_fire_run_to_residual(cdft_ctx* ctx, double resid_tol, long max_steps, c
  * steps. Stops when max|dOmega/drho| <= resid_tol (taken from an FP64
  * evaluation), on the uphill limit, or after max_steps (> 0).
  * mixed = 0: FP64 throughout. mixed = 1: an FP32 bulk phase (vectors and
- * evaluations in FP32) until its residual drops below switch_tol or stops
- * improving, then one FP64 evaluation at the same state and FP64 refinement. */
+ * evaluations in FP32) until its residual drops below switch_tol or goes 96
+ * steps without a 2% improvement (its noise floor), then one FP64 evaluation
+ * at the same state and FP64 refinement. */
 int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, long max_steps, int mixed, cdft_fire_report* rep);
 
 /* DDFT integrating-factor dynamics, single species, periodic (include/Minimizer.h:189-266, src/DDFT.cpp:42-351). */
@@ -179,7 +187,10 @@ typedef struct cdft_ddft_report {
 
 /* DDFT::DDFT then setTimeStep(dt), set_max_time_step(dt_max), set_tolerence_fixed_point(tol). */
 int cdft_ddft_init(cdft_ctx* ctx, double dt, double dt_max, double tol_fixed_point);
-/* nsteps calls of DDFT::step(). */
+/* nsteps calls of DDFT::step(). In CDFT_FP32 mode every propagated density is
+ * shifted uniformly (in FP64) back to the mass sum(rho) dV the run started
+ * with, which the FP32 transforms keep only to ~1e-7 per step; CDFT_FP64 mode is
+ * the reference's arithmetic unchanged. */
 int cdft_ddft_step(cdft_ctx* ctx, int nsteps, cdft_ddft_report* rep);
 
 /* Number of atoms, sum(rho) * dV with FP64 compensated summation, of a density

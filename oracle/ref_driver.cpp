@@ -378,6 +378,20 @@ int main(int argc, char** argv) {
       put("ddft16.F", ddft.F); put("ddft16.t", ddft.t); put("ddft16.dt", ddft.dt);
       put("ddft16.mass", ddft.mass); put("ddft16.rhs", ddft.rhs);
       put("ddft16.rho_final", density_of(*S.d));
+    } else if (c == "coex") {
+      // bulk coexistence of the LJ fluid (WhiteBearI + QF at dx = 0.1): DFT::findCoex
+      std::vector<double> kts = {0.7, 0.8, 0.9}, xv, xl, mu, xs1, xs2;
+      for (double kT : kts) {
+        System S = make_system(0.1, 16, "WhiteBearI", true, kT);
+        double a, b, s1, s2;
+        S.dft->findSpinodal(1.0, 1e-3, s1, s2, 1e-8);
+        S.dft->findCoex(1.0, 1e-3, a, b, 1e-8);
+        xv.push_back(a); xl.push_back(b); mu.push_back(S.dft->mu_times_beta(a)); xs1.push_back(s1); xs2.push_back(s2);
+        put1("coex.hsd_kT" + std::to_string(kT).substr(0, 3), S.hsd);
+        put1("coex.avdw_kT" + std::to_string(kT).substr(0, 3), S.inter->getVDWParameter());
+      }
+      put("coex.kT", kts); put("coex.x_vap", xv); put("coex.x_liq", xl); put("coex.mu", mu);
+      put("coex.spinodal1", xs1); put("coex.spinodal2", xs2);
     } else if (c == "ddft_adapt16") {
       // default adaptive time step (dt grows x2 after 5 successes up to dtMax)
       System S = make_system(0.1, 16, "WhiteBearI", true, 0.8);

@@ -67,3 +67,24 @@ def test_mixed_precision_reaches_fp64_minimum():
         res[mixed] = (t["Omega"], c.get_density(), r["total_steps"])
     assert abs(res[True][0] - res[False][0]) <= 1e-10 * abs(res[False][0])
     np.testing.assert_allclose(res[True][1], res[False][1], rtol=0, atol=1e-6)
+
+
+def test_ddft_fp32_conserves_mass_and_tracks_fp64():
+    import classicaldft_gb300 as cd
+    from oracle import pyoracle
+    shape, dx = (48, 48, 48), 0.1
+    rho = pyoracle.fill_noise(shape, 0.3, 0.1, 21)
+    hsd = cd.bh_diameter(1, 1, 3, 0.8)
+    out = {}
+    for prec in (cd.FP64, cd.FP32):
+        c = cd.Context(shape, dx, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.8, precision=prec)
+        c.set_density(rho)
+        c.ddft_init(1e-4, 1e-4)
+        m0 = np.sum(rho) * dx ** 3
+        masses = [c.ddft_step(1)["mass"] for _ in range(10)]
+        out[prec] = (c.get_density(), masses, m0)
+    d64, m64, m0 = out[cd.FP64]
+    d32, m32, _ = out[cd.FP32]
+    assert max(abs(m - m0) for m in m32) <= 1e-12 * m0
+    assert max(abs(m - m0) for m in m64) <= 1e-12 * m0
+    assert np.abs(d32 - d64).max() <= 1e-5

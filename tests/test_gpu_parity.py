@@ -273,3 +273,17 @@ def test_reference_shaped_api(cd, oracle):
     fire.setForceTerminationCriterion(0.0)
     fire.run(5)
     assert fire.report["total_steps"] == 5
+
+
+def test_bulk_coexistence_matches_reference(cd):
+    g = golden("coex")
+    for i, kT in enumerate(g["coex.kT"]):
+        tag = "%.1f" % kT
+        c = cd.Context(16, 0.1, cd.WHITEBEAR_I, hsd=g["coex.hsd_kT" + tag][0], lj=True, kT=kT)
+        assert abs(c.info.a_vdw - g["coex.avdw_kT" + tag][0]) < 1e-12
+        r = c.find_coex(1.0, 1e-3, 1e-8)
+        assert abs(r["x_vap"] - g["coex.x_vap"][i]) < 1e-9
+        assert abs(r["x_liq"] - g["coex.x_liq"][i]) < 1e-9
+        assert abs(r["mu"] - g["coex.mu"][i]) < 1e-9
+        assert abs(r["spinodal1"] - g["coex.spinodal1"][i]) < 1e-8
+        assert abs(r["spinodal2"] - g["coex.spinodal2"][i]) < 1e-8
