@@ -258,6 +258,7 @@ def main():
     passes = c.time_passes(reps=5)
     c.set_precision(cd.FP64)
     ms64 = timed(max(3, args.steps // 10), 3, lambda: c.eval(want_dF=False))
+    passes64 = c.time_passes(reps=3)
     c.set_precision(cd.FP32)
     # e2e through the public API: host density in, host dF out, every step
     host_rho = rho.copy()
@@ -292,6 +293,7 @@ def main():
             "fp64_evals_per_s": world * 1e3 / ms64, "fp64_ms_per_step": ms64,
             "passes": [{"pass": p["pass"], "ms": round(p["ms"], 5), "GBs": round(p["bytes"] / max(p["ms"], 1e-9) / 1e6, 1)}
                        for p in passes],
+            "passes_fp64": [{"pass": p["pass"], "ms": round(p["ms"], 4)} for p in passes64],
             "clocks": clocks}
     if not args.no_fire:
         line["fire_to_resid_1e-8"] = fire_legs(cd, rho)

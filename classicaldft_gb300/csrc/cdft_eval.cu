@@ -256,7 +256,7 @@ bool Evaluator<T>::setup_tma(std::string* err) {
     uint64_t dims[3] = {(uint64_t)pz_ * E, (uint64_t)rows_, (uint64_t)M_};
     uint64_t str[2] = {(uint64_t)pz_ * cb, (uint64_t)Nc_ * cb};
     uint32_t box[3] = {(uint32_t)(pz_ * E), (uint32_t)RB, (uint32_t)M_};
-    smem_tphi_ = 2 * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * L * cb) + 1024;
+    smem_tphi_ = 2 * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L + 1) * cb) + 1024;
     if (smem_tphi_ <= 220 * 1024 && encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) {
       auto set_phi = [&](auto kern) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tphi_);

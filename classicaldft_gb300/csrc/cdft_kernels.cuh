@@ -350,6 +350,7 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
   typedef typename Cx<T>::type C;
   constexpr int M = ModelTraits<MODEL>::M;
   constexpr int NP = (M + 1) / 2;
+  const T ih = (T)(1.0 / (double)hsd), ih2 = (T)(1.0 / ((double)hsd * (double)hsd));
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nz = d.nz, LP = nz + 1, nzc = d.nzc;
   const int L = NP * RB;
@@ -383,7 +384,7 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
       nv[a] = (a & 1) ? z.y : z.x;
     }
     const T eta = nv[0];
-    const T phi = fmt_phi_point<T, MODEL>(nv, hsd, esA, esB);
+    const T phi = fmt_phi_point<T, MODEL>(nv, ih, ih2, esA, esB);
     if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
     if (!isfinite(phi)) st |= 2u;
     psum.add(phi);

@@ -14,6 +14,7 @@
 namespace cdft {
 
 // Radix-P butterfly on column c of a row-major tile with TC columns.
+// TC here is the tile's row pitch in complex elements (>= the column count).
 template <int DIR, class T, int P, int TC>
 __device__ __forceinline__ void tile_butterfly(const typename Cx<T>::type* __restrict__ x, typename Cx<T>::type* __restrict__ y, int c,
                                                int q, int k, int m, int s, const typename Cx<T>::type* __restrict__ tw,
@@ -77,9 +78,10 @@ __device__ __noinline__ void tile_butterfly_generic(const typename Cx<T>::type* 
   }
 }
 
-// Transforms the TC columns of the tile in b0 (b1 is scratch); returns the
-// buffer holding the result. Starts and ends with __syncthreads().
-template <int DIR, class T, int TC>
+// Transforms the TC columns of the tile in b0 (row pitch PITCH >= TC complex
+// values; b1 is scratch); returns the buffer holding the result. Starts and
+// ends with __syncthreads().
+template <int DIR, class T, int TC, int PITCH = TC>
 __device__ typename Cx<T>::type* tile_fft(typename Cx<T>::type* b0, typename Cx<T>::type* b1, const FFTPlan& P,
                                           const typename Cx<T>::type* __restrict__ table) {
   typedef typename Cx<T>::type C;
@@ -92,18 +94,26 @@ __device__ typename Cx<T>::type* tile_fft(typename Cx<T>::type* b0, typename Cx<
     const int items = TC * (P.n / p);
     const C* tw = table + P.tw_off[st];
     const C* rt = table + P.root_off[st];
+    const int sh = ((s & (s - 1)) == 0) ? __ffs(s) - 1 : -1;  // stride as a shift when a power of two
     __syncthreads();
     for (int w = threadIdx.x; w < items; w += blockDim.x) {
       const int c = w % TC, u = w / TC;
-      const int q = u / s, k = u - q * s;
+      int q, k;
+      if (sh >= 0) {
+        q = u >> sh;
+        k = u & (s - 1);
+      } else {
+        q = u / s;
+        k = u - q * s;
+      }
       switch (p) {
-        case 8: tile_butterfly<DIR, T, 8, TC>(src, dst, c, q, k, m, s, tw, rt); break;
-        case 4: tile_butterfly<DIR, T, 4, TC>(src, dst, c, q, k, m, s, tw, rt); break;
-        case 2: tile_butterfly<DIR, T, 2, TC>(src, dst, c, q, k, m, s, tw, rt); break;
-        case 3: tile_butterfly_odd<DIR, T, 3, TC>(src, dst, c, q, k, m, s, tw, rt); break;
-        case 5: tile_butterfly_odd<DIR, T, 5, TC>(src, dst, c, q, k, m, s, tw, rt); break;
-        case 7: tile_butterfly_odd<DIR, T, 7, TC>(src, dst, c, q, k, m, s, tw, rt); break;
-        default: tile_butterfly_generic<DIR, T, TC>(src, dst, c, q, k, m, s, p, tw, rt); break;
+        case 8: tile_butterfly<DIR, T, 8, PITCH>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 4: tile_butterfly<DIR, T, 4, PITCH>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 2: tile_butterfly<DIR, T, 2, PITCH>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 3: tile_butterfly_odd<DIR, T, 3, PITCH>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 5: tile_butterfly_odd<DIR, T, 5, PITCH>(src, dst, c, q, k, m, s, tw, rt); break;
+        case 7: tile_butterfly_odd<DIR, T, 7, PITCH>(src, dst, c, q, k, m, s, tw, rt); break;
+        default: tile_butterfly_generic<DIR, T, PITCH>(src, dst, c, q, k, m, s, p, tw, rt); break;
       }
     }
     C* t = src;
@@ -392,13 +402,15 @@ __global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CU
   typedef typename Cx<T>::type C;
   constexpr int M = ModelTraits<MODEL>::M;
   constexpr int NP = (M + 1) / 2;
+  const T ih = (T)(1.0 / (double)hsd), ih2 = (T)(1.0 / ((double)hsd * (double)hsd));
   constexpr int L = NP * RB;
+  constexpr int LPd = L + 1;  // odd row pitch: the per-point loops stride rows without bank conflicts
   constexpr int E = ElemsPerComplex<T>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* sm = aligned_smem(smem_raw);
   const int nz = d.nz, nzc = d.nzc, pz = d.pz;
   const size_t in_bytes = (size_t)M * RB * pz * sizeof(C), ib = r128(in_bytes);
-  const size_t zb = r128((size_t)nz * L * sizeof(C));
+  const size_t zb = r128((size_t)nz * LPd * sizeof(C));
   C* In[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + ib)};
   C* Z0 = reinterpret_cast<C*>(sm + 2 * ib);
   C* Z1 = reinterpret_cast<C*>(sm + 2 * ib + zb);
@@ -436,14 +448,14 @@ __global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CU
       const int r = line / NP, pr = line - r * NP;
       const C* Arow = in + ((size_t)(2 * pr) * RB + r) * pz;
       const C* Brow = (2 * pr + 1 < M) ? in + ((size_t)(2 * pr + 1) * RB + r) * pz : nullptr;
-      Z0[e] = pair_spectrum<T>(Arow, Brow, k, nz);
+      Z0[k * LPd + line] = pair_spectrum<T>(Arow, Brow, k, nz);
     }
     __syncthreads();
     if (threadIdx.x == 0) {  // In[b] consumed: bring the group after next
       const long gn = g + 2L * gridDim.x;
       if (gn < ngroup) issue(gn, b);
     }
-    C* res = tile_fft<+1, T, L>(Z0, Z1, pz_plan, tw);
+    C* res = tile_fft<+1, T, L, LPd>(Z0, Z1, pz_plan, tw);
     C* oth = (res == Z0) ? Z1 : Z0;
     for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
       const int k = e % nz, r = e / nz;
@@ -451,25 +463,25 @@ __global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CU
       T nv[11];
 #pragma unroll
       for (int a = 0; a < M; ++a) {
-        const C z = res[k * L + r * NP + a / 2];
+        const C z = res[k * LPd + r * NP + a / 2];
         nv[a] = (a & 1) ? z.y : z.x;
       }
       const T eta = nv[0];
-      const T phi = fmt_phi_point<T, MODEL>(nv, hsd, esA, esB);
+      const T phi = fmt_phi_point<T, MODEL>(nv, ih, ih2, esA, esB);
       if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
       if (!isfinite(phi)) st |= 2u;
       psum.add(phi);
 #pragma unroll
-      for (int p = 0; p < NP; ++p) oth[k * L + r * NP + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
+      for (int p = 0; p < NP; ++p) oth[k * LPd + r * NP + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
     }
-    C* res2 = tile_fft<-1, T, L>(oth, res, pz_plan, tw);
+    C* res2 = tile_fft<-1, T, L, LPd>(oth, res, pz_plan, tw);
     for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
       const int k = e % nzc, line = e / nzc;
       const int r = line / NP, pr = line - r * NP;
       const long row = row0 + r;
       if (row >= d.rows) continue;
-      const C Z = res2[k * L + line];
-      const C W = res2[(k == 0 ? 0 : nz - k) * L + line];
+      const C Z = res2[k * LPd + line];
+      const C W = res2[(k == 0 ? 0 : nz - k) * LPd + line];
       Cf[(long)(2 * pr) * d.Nc + row * pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
       if (2 * pr + 1 < M) Cf[(long)(2 * pr + 1) * d.Nc + row * pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
     }

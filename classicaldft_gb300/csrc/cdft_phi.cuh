@@ -17,13 +17,16 @@ template <class T> __device__ __forceinline__ T log1m(T e);
 template <> __device__ __forceinline__ double log1m<double>(double e) { return log(1.0 - e); }
 template <> __device__ __forceinline__ float log1m<float>(float e) { return log1pf(-e); }
 
-// f1, f2, f3 and first derivatives.
+// f1, f2, f3 and first derivatives. Divisions are replaced by products with
+// g = 1/(1 - eta) and ie = 1/eta (two reciprocals per point): GB300 runs FP64
+// division as a long FP64 instruction sequence.
 template <class T, int MODEL>
 __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, T& f3p) {
   const T one = (T)1;
   const T L = log1m<T>(e);
+  const T g = one / (one - e);
   f1 = L;
-  f1p = -one / (one - e);
+  f1p = -g;
   if (MODEL == MODEL_WHITEBEAR_II) {
     if (e < (T)1e-12) {
       f2 = one + e * (one + e * ((T)(10.0 / 9) + (T)(7.0 / 6) * e));
@@ -31,14 +34,14 @@ __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, 
       f3 = (T)1.5 + (T)(7.0 / 3) * e + (T)3.25 * e * e + (T)4.2 * e * e * e;
       f3p = (T)(7.0 / 3) + (T)7.5 * e + (T)12.6 * e * e;
     } else {
-      f2 = (T)(1.0 / 3.0) + (T)(4.0 / 3.0) * (one / (one - e)) + ((T)2 / ((T)3 * e)) * L;
-      f2p = ((T)2 * ((T)3 * e - one) / ((T)3 * e * (one - e) * (one - e))) - ((T)2 / ((T)3 * e * e)) * L;
-      f3 = -((one - (T)3 * e + e * e) / (e * (one - e) * (one - e))) - (one / (e * e)) * L;
-      f3p = (((T)2 - (T)5 * e + (T)6 * e * e - e * e * e) / (e * e * (one - e) * (one - e) * (one - e))) + ((T)2 / (e * e * e)) * L;
+      const T ie = one / e, g2 = g * g;
+      f2 = (T)(1.0 / 3.0) + (T)(4.0 / 3.0) * g + (T)(2.0 / 3.0) * ie * L;
+      f2p = (T)(2.0 / 3.0) * ((T)3 * e - one) * ie * g2 - (T)(2.0 / 3.0) * ie * ie * L;
+      f3 = -(one - (T)3 * e + e * e) * ie * g2 - ie * ie * L;
+      f3p = ((T)2 - (T)5 * e + (T)6 * e * e - e * e * e) * ie * ie * g2 * g + (T)2 * ie * ie * ie * L;
     }
     return;
   }
-  const T g = one / (one - e);
   f2 = g;
   f2p = g * g;
   if (MODEL == MODEL_RSLT || MODEL == MODEL_WHITEBEAR_I) {
@@ -46,11 +49,12 @@ __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, 
       f3 = (T)1.5 + (T)(8.0 / 3) * e + (T)3.75 * e * e + (T)4.8 * e * e * e;
       f3p = (T)(8.0 / 3) + (T)7.5 * e + (T)14.4 * e * e;
     } else {
-      f3 = (one / (e * (one - e) * (one - e))) + (L / (e * e));
+      const T ie = one / e, g2 = g * g;
+      f3 = ie * g2 + L * ie * ie;
       if (MODEL == MODEL_RSLT)
-        f3p = -(one / (e * e)) * (one / ((one - e) * (one - e) * (one - e))) * (e * e - (T)5 * e + (T)2) - ((T)2 / (e * e * e)) * L;
+        f3p = -ie * ie * g2 * g * (e * e - (T)5 * e + (T)2) - (T)2 * ie * ie * ie * L;
       else
-        f3p = ((-(T)2 + (T)5 * e - e * e) / (e * e * (one - e) * (one - e) * (one - e))) - ((T)2 / (e * e * e)) * L;
+        f3p = (-(T)2 + (T)5 * e - e * e) * ie * ie * g2 * g - (T)2 * ie * ie * ie * L;
     }
   } else {  // Rosenfeld and esFMT
     f3 = g * g;
@@ -60,14 +64,16 @@ __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, 
 
 // n[] holds the weighted densities in the order eta, s, v0, v1, v2, T00, T01,
 // T02, T11, T12, T22 (M = 11) or the first five (M = 5). On return n[] holds
-// dPhi/dn_a folded as described above. Returns Phi.
+// dPhi/dn_a folded as described above. Returns Phi. ih = 1/hsd, ih2 = 1/hsd^2.
 template <class T, int MODEL>
-__device__ __forceinline__ T fmt_phi_point(T* n, T hsd, T A, T B) {
-  const T PI = (T)3.14159265358979323846;
-  const T s2 = n[1], s1 = n[1] / hsd, s0 = n[1] / (hsd * hsd);
+__device__ __forceinline__ T fmt_phi_point(T* n, T ih, T ih2, T A, T B) {
+  const T i_pi = (T)(1.0 / 3.14159265358979323846);
+  const T i_2pi = (T)(0.5 / 3.14159265358979323846);
+  const T i_24pi = (T)(1.0 / (24 * 3.14159265358979323846));
+  const T s2 = n[1], s1 = n[1] * ih, s0 = n[1] * ih2;
   const T eta = n[0];
   T v2[3] = {n[2], n[3], n[4]};
-  T v1[3] = {n[2] / hsd, n[3] / hsd, n[4] / hsd};
+  T v1[3] = {n[2] * ih, n[3] * ih, n[4] * ih};
   const T v1_v2 = v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2];
   const T v2_v2 = v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2];
   T f1, f2, f3, f1p, f2p, f3p;
@@ -93,54 +99,55 @@ __device__ __forceinline__ T fmt_phi_point(T* n, T hsd, T A, T B) {
 #pragma unroll
       for (int j = 0; j < 3; ++j) T3 += TT[i][j] * Tm[j][i];
     const T a = (MODEL == MODEL_ESFMT) ? A : (T)1, b = (MODEL == MODEL_ESFMT) ? B : (T)-1;
-    Phi3 = (a / ((T)24 * PI)) * (s2 * s2 * s2 - (T)3 * s2 * v2_v2 + (T)3 * vTv - T3) + (b / ((T)24 * PI)) * (s2 * s2 * s2 - (T)3 * s2 * T2 + (T)2 * T3);
-    dP3_dS2 = (a / ((T)24 * PI)) * ((T)3 * s2 * s2 - (T)3 * v2_v2) + (b / ((T)24 * PI)) * ((T)3 * s2 * s2 - (T)3 * T2);
+    const T a24 = a * i_24pi, b24 = b * i_24pi;
+    Phi3 = a24 * (s2 * s2 * s2 - (T)3 * s2 * v2_v2 + (T)3 * vTv - T3) + b24 * (s2 * s2 * s2 - (T)3 * s2 * T2 + (T)2 * T3);
+    dP3_dS2 = a24 * ((T)3 * s2 * s2 - (T)3 * v2_v2) + b24 * ((T)3 * s2 * s2 - (T)3 * T2);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) dP3_dV2[k] = (a / ((T)24 * PI)) * (-(T)6 * s2 * v2[k] + (T)3 * vT[k] + (T)3 * vT[k]);
+    for (int k = 0; k < 3; ++k) dP3_dV2[k] = a24 * (-(T)6 * s2 * v2[k] + (T)3 * vT[k] + (T)3 * vT[k]);
+    const T a8 = (T)3 * a24, b4 = (T)6 * b24;  // A/(8 pi), B/(4 pi)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
-        dP3_dT[j][k] = (a / ((T)8 * PI)) * (v2[j] * v2[k] - TT[k][j]) + (b / ((T)4 * PI)) * (-s2 * Tm[k][j] + TT[k][j]);
+      for (int k = 0; k < 3; ++k) dP3_dT[j][k] = a8 * (v2[j] * v2[k] - TT[k][j]) + b4 * (-s2 * Tm[k][j] + TT[k][j]);
   } else if (MODEL == MODEL_RSLT) {
     if (s2 < (T)1e-20) {
       Phi3 = 0; dP3_dS2 = 0; dP3_dV2[0] = dP3_dV2[1] = dP3_dV2[2] = 0;
     } else {
       const T psi = v2_v2 / (s2 * s2);
       const T om = (T)1 - psi;
-      Phi3 = ((T)1 / ((T)36 * PI)) * s2 * s2 * s2 * om * om * om;
-      dP3_dS2 = ((T)1 / ((T)12 * PI)) * s2 * s2 * ((T)1 + psi) * om * om;
+      Phi3 = (T)(1.0 / (36 * 3.14159265358979323846)) * s2 * s2 * s2 * om * om * om;
+      dP3_dS2 = (T)(1.0 / (12 * 3.14159265358979323846)) * s2 * s2 * ((T)1 + psi) * om * om;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) dP3_dV2[k] = -((T)1 / ((T)6 * PI)) * s2 * v2[k] * om * om;
+      for (int k = 0; k < 3; ++k) dP3_dV2[k] = -(T)(1.0 / (6 * 3.14159265358979323846)) * s2 * v2[k] * om * om;
     }
   } else {  // Rosenfeld
-    Phi3 = ((T)1 / ((T)24 * PI)) * (s2 * s2 * s2 - (T)3 * s2 * v2_v2);
-    dP3_dS2 = ((T)1 / ((T)24 * PI)) * ((T)3 * s2 * s2 - (T)3 * v2_v2);
+    Phi3 = i_24pi * (s2 * s2 * s2 - (T)3 * s2 * v2_v2);
+    dP3_dS2 = i_24pi * ((T)3 * s2 * s2 - (T)3 * v2_v2);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) dP3_dV2[k] = ((T)1 / ((T)24 * PI)) * (-(T)6 * s2 * v2[k]);
+    for (int k = 0; k < 3; ++k) dP3_dV2[k] = i_24pi * (-(T)6 * s2 * v2[k]);
   }
 
   T phi = 0;
-  phi -= ((T)1 / PI) * s0 * f1;
-  phi += ((T)1 / ((T)2 * PI)) * (s1 * s2 - v1_v2) * f2;
+  phi -= i_pi * s0 * f1;
+  phi += i_2pi * (s1 * s2 - v1_v2) * f2;
   phi += Phi3 * f3;
 
   T d_eta = 0;
-  d_eta -= ((T)1 / PI) * s0 * f1p;
-  d_eta += ((T)1 / ((T)2 * PI)) * (s1 * s2 - v1_v2) * f2p;
+  d_eta -= i_pi * s0 * f1p;
+  d_eta += i_2pi * (s1 * s2 - v1_v2) * f2p;
   d_eta += Phi3 * f3p;
-  const T d_s0 = -((T)1 / PI) * f1;
-  const T d_s1 = ((T)1 / ((T)2 * PI)) * s2 * f2;
-  T d_s2 = ((T)1 / ((T)2 * PI)) * s1 * f2;
+  const T d_s0 = -i_pi * f1;
+  const T d_s1 = i_2pi * s2 * f2;
+  T d_s2 = i_2pi * s1 * f2;
   d_s2 += dP3_dS2 * f3;
   n[0] = d_eta;
-  n[1] = (d_s0 / (hsd * hsd)) + (d_s1 / hsd) + d_s2;
+  n[1] = d_s0 * ih2 + d_s1 * ih + d_s2;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const T d_v1 = ((T)1 / ((T)2 * PI)) * (-v2[k]) * f2;
-    T d_v2 = ((T)1 / ((T)2 * PI)) * (-v1[k]) * f2;
+    const T d_v1 = i_2pi * (-v2[k]) * f2;
+    T d_v2 = i_2pi * (-v1[k]) * f2;
     d_v2 += dP3_dV2[k] * f3;
-    n[2 + k] = -(d_v2 + d_v1 / hsd);
+    n[2 + k] = -(d_v2 + d_v1 * ih);
   }
   if (ModelTraits<MODEL>::tensor) {
     n[5] = dP3_dT[0][0] * f3;
