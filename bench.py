@@ -200,6 +200,44 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
     return out
 
 
+def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80, 96)):
+    """State-point sweep: n LJ droplets (kT ~ U[0.7, 0.94], mu = mu_coex(kT) + U[-0.2, 0.2],
+    R ~ U[2, 6] clamped to 0.4 L, cubic grids drawn from `grids`, dx = 0.1, fixed mass),
+    all minimised to max|dOmega/drho| <= tol with the mixed policy. Batched
+    (cdft_fire_run_batch, every context on its own stream) vs one after another
+    (cdft_fire_run_device); context set-up is outside both timings."""
+    import torch
+    from classicaldft_gb300 import statepoints as sp
+    pts = sp.sample_state_points(n, seed=seed, grids=grids)
+    out = {"points": n, "seed": seed, "tol": tol, "grids": sorted(p["n"] for p in pts),
+           "ensemble": "fixed mass droplets", "precision": "mixed (FP32 bulk, FP64 refinement)"}
+    ctxs = sp.build_contexts([dict(p) for p in pts])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps, status = cd.fire_run_batch(ctxs, tol, max_steps=max_steps, mixed=True)
+    torch.cuda.synchronize()
+    tb = time.perf_counter() - t0
+    out["batched_s"] = tb
+    out["converged"] = int(sum(1 for r, s in zip(reps, status) if s == 0 and r["resid"] <= tol))
+    out["total_steps"] = int(sum(r["total_steps"] for r in reps))
+    omega_b = [r["F"] for r in reps]
+    for c in ctxs:
+        c.close()
+    ctxs = sp.build_contexts([dict(p) for p in pts])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq = [c.fire_run_device(tol, max_steps=max_steps, mixed=True, switch_tol=2e-6) for c in ctxs]
+    torch.cuda.synchronize()
+    ts = time.perf_counter() - t0
+    for c in ctxs:
+        c.close()
+    out["sequential_s"] = ts
+    out["speedup_batched_vs_sequential"] = ts / tb
+    out["state_points_per_s"] = n / tb
+    out["same_minima"] = bool(all(a == r["F"] for a, r in zip(omega_b, seq)))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -209,6 +247,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fire", action="store_true", help="skip the time-to-residual legs")
     ap.add_argument("--no-ddft", action="store_true", help="skip the 256^3 DDFT leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the state-point sweep leg")
+    ap.add_argument("--sweep-points", type=int, default=16, help="state points in the sweep leg")
+    ap.add_argument("--sweep-grids", default="48,64,80,96",
+                    help="grid sizes the sweep draws from (the full range is 48,64,...,160)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -299,6 +341,9 @@ def main():
         line["fire_to_resid_1e-8"] = fire_legs(cd, rho)
     if not args.no_ddft:
         line["ddft_256"] = ddft_leg(cd)
+    if not args.no_batch:
+        line["statepoint_sweep"] = batch_leg(cd, n=args.sweep_points,
+                                             grids=tuple(int(g) for g in args.sweep_grids.split(",")))
     if rank == 0 and not args.no_cpu_baseline:
         rate, n, el = cpu_baseline()
         line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",

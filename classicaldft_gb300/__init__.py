@@ -32,6 +32,7 @@ C_FUNCTIONS = [
     "cdft_set_fixed_mass", "cdft_get_chem_potential", "cdft_eval", "cdft_bulk", "cdft_bh_diameter",
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
     "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device", "cdft_find_coex",
+    "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -112,6 +113,10 @@ def lib():
             "cdft_number_of_atoms_noalloc": ([vp, ctypes.c_long, d, vp, dp], i),
             "cdft_fire_run_device": ([vp, d, d, ctypes.c_long, i, P(FireReport)], i),
             "cdft_find_coex": ([vp, d, d, d, dp], i),
+            "cdft_fire_run_batch": ([P(vp), i, d, d, ctypes.c_long, i, P(FireReport), P(i)], i),
+            "cdft_autotune": ([vp, i, P(i), dp], i),
+            "cdft_get_radices": ([vp, P(i)], i),
+            "cdft_radix_candidates": ([i, P(i), i, P(i)], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -295,6 +300,19 @@ class Context:
         self._check(lib().cdft_fire_run_device(self._h, tol, switch_tol, max_steps, int(mixed), ctypes.byref(r)))
         return self._rep(r)
 
+    # FFT plans
+    def autotune(self, reps=5):
+        """Tunes the radix ordering of each axis; returns ({x, y, z orderings}, default ms, tuned ms)."""
+        r = (ctypes.c_int * 24)()
+        ms = np.zeros(2)
+        self._check(lib().cdft_autotune(self._h, reps, r, _dptr(ms)))
+        return _radices(r), float(ms[0]), float(ms[1])
+
+    def radices(self):
+        r = (ctypes.c_int * 24)()
+        self._check(lib().cdft_get_radices(self._h, r))
+        return _radices(r)
+
     # DDFT
     def ddft_init(self, dt, dt_max, tol=1e-4):
         self._check(lib().cdft_ddft_init(self._h, dt, dt_max, tol))
@@ -303,6 +321,40 @@ class Context:
         r = DdftReport()
         self._check(lib().cdft_ddft_step(self._h, n, ctypes.byref(r)))
         return self._rep(r)
+
+
+def _radices(r):
+    return {ax: [v for v in r[8 * a:8 * a + 8] if v] for a, ax in enumerate("xyz")}
+
+
+def radix_candidates(n):
+    """Radix orderings the autotuner tries for transform length n (host only)."""
+    cnt = ctypes.c_int()
+    code = lib().cdft_radix_candidates(n, None, 0, ctypes.byref(cnt))
+    if code:
+        raise CDFTError(code, "bad length")
+    out = (ctypes.c_int * (8 * cnt.value))()
+    lib().cdft_radix_candidates(n, out, cnt.value, ctypes.byref(cnt))
+    return [[v for v in out[8 * k:8 * k + 8] if v] for k in range(cnt.value)]
+
+
+def fire_run_batch(contexts, tol, max_steps=-1, mixed=True, switch_tol=2e-6):
+    """Device FIRE2 on many contexts at once (cdft_fire_run_batch).
+
+    Returns (reports, statuses): one report dict and one status code per context."""
+    n = len(contexts)
+    hs = (ctypes.c_void_p * n)(*[c._h for c in contexts])
+    reps = (FireReport * n)()
+    rcs = (ctypes.c_int * n)()
+    rc = lib().cdft_fire_run_batch(hs, n, tol, switch_tol, max_steps, int(mixed), reps, rcs)
+    out = [contexts[k]._rep(reps[k]) for k in range(n)]
+    status = [int(rcs[k]) for k in range(n)]
+    for k in range(n):
+        if status[k]:
+            out[k]["error"] = lib().cdft_last_error(contexts[k]._h).decode()
+    if rc and not any(status):
+        raise CDFTError(rc, "cdft_fire_run_batch")
+    return out, status
 
 
 # ------------------------------------------------- reference-shaped API ---

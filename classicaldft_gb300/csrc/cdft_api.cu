@@ -350,6 +350,13 @@ int cdft_create(const cdft_params* p, cdft_ctx** out) {
   c->ty = (p->ny == p->nx) ? c->tx : make_fft_table(p->ny, &err);
   c->tz = (p->nz == p->nx) ? c->tx : (p->nz == p->ny ? c->ty : make_fft_table(p->nz, &err));
   if (!c->tx || !c->ty || !c->tz) return CDFT_ERR_ARG;
+  std::array<std::vector<int>, 3> tuned;
+  if (cdft_internal_tuned_plans(c.get(), c->precision, &tuned)) {  // cdft_autotune ran for this shape
+    c->tx = make_fft_table(p->nx, &err, &tuned[0]);
+    c->ty = make_fft_table(p->ny, &err, &tuned[1]);
+    c->tz = make_fft_table(p->nz, &err, &tuned[2]);
+    if (!c->tx || !c->ty || !c->tz) return CDFT_ERR_ARG;
+  }
   const long N = c->info.N;
   if (cudaMalloc(&c->rho, N * sizeof(double)) != cudaSuccess || cudaMalloc(&c->dF, N * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->red_part, (size_t)152 * 8 * 16 * sizeof(double)) != cudaSuccess ||

@@ -1,6 +1,7 @@
 // Internal: the C ABI's context (one system on one GPU) and the device
 // FIRE2 engine's state, shared by cdft_api.cu and cdft_fire_dev.cu.
 #pragma once
+#include <array>
 #include <cmath>
 #include <memory>
 #include <string>
@@ -71,3 +72,6 @@ int cdft_internal_fail(cdft_ctx* c, int code, const std::string& m);
 int cdft_internal_eval(cdft_ctx* c, double* terms8, int only_fex);
 int cdft_internal_fire_accept(cdft_ctx* c, int s_idx);
 void cdft_internal_fire_dev_free(cdft_ctx* c);
+// plans cdft_autotune chose for the context's shape, model and precision (cdft_tune.cu)
+bool cdft_internal_tuned_plans(const cdft_ctx* c, int precision, std::array<std::vector<int>, 3>* plans);
+std::vector<std::vector<int>> cdft_internal_radix_candidates(int n);

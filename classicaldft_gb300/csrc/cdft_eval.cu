@@ -24,27 +24,42 @@ FFTTable::~FFTTable() {
   if (d32) cudaFree(d32);
 }
 
-std::shared_ptr<FFTTable> make_fft_table(int n, std::string* err) {
+std::vector<int> default_radices(int n) {
+  std::vector<int> r;
+  int m = n;
+  while (m > 1) {
+    int f = 0;
+    if (m % 8 == 0 && m != 16) f = 8;  // 16 = 4 x 4 keeps both stages radix 4
+    else if (m % 4 == 0) f = 4;
+    else if (m % 2 == 0) f = 2;
+    else {
+      for (int q = 3; q <= m; q += 2)
+        if (m % q == 0) { f = q; break; }
+    }
+    r.push_back(f);
+    m /= f;
+  }
+  return r;
+}
+
+std::shared_ptr<FFTTable> make_fft_table(int n, std::string* err, const std::vector<int>* radices) {
   auto t = std::make_shared<FFTTable>();
   FFTPlan& P = t->plan;
   std::memset(&P, 0, sizeof(P));
   P.n = n;
-  int m = n;
-  while (m > 1) {
-    int r = 0;
-    if (m % 8 == 0 && m != 16) r = 8;  // 16 = 4 x 4 keeps both stages radix 4
-    else if (m % 4 == 0) r = 4;
-    else if (m % 2 == 0) r = 2;
-    else {
-      for (int f = 3; f <= m; f += 2)
-        if (m % f == 0) { r = f; break; }
-    }
-    if (r > kMaxRadix || P.nst >= kMaxStages) {
+  const std::vector<int> rad = radices ? *radices : default_radices(n);
+  long prod = 1;
+  for (int r : rad) {
+    if (r < 2 || r > kMaxRadix || P.nst >= kMaxStages) {
       if (err) *err = "grid length " + std::to_string(n) + " has a prime factor above 31";
       return nullptr;
     }
     P.radix[P.nst++] = r;
-    m /= r;
+    prod *= r;
+  }
+  if (prod != n) {
+    if (err) *err = "radix ordering does not multiply to " + std::to_string(n);
+    return nullptr;
   }
   // table: for each stage the m*p twiddles exp(-2 pi i q t/len), then the p roots exp(-2 pi i t/p)
   std::vector<long double> re, im;
@@ -131,9 +146,19 @@ long Evaluator<T>::grid_blocks_rows() const {
 
 static size_t smem_bytes(int lines, int n, size_t csize, int nbuf) { return (size_t)nbuf * lines * (n + 1) * csize; }
 
+// The dynamic shared-memory limit is an attribute of the kernel, shared by
+// every context in the process: raise it to what this context needs, never
+// lower it below what another context (another grid) already launches with.
+template <class F>
+static void raise_smem(F f, size_t bytes) {
+  cudaFuncAttributes a;
+  if (cudaFuncGetAttributes(&a, f) == cudaSuccess && (size_t)a.maxDynamicSharedSizeBytes >= bytes) return;
+  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 template <class T, class F>
 static void set_smem(F f, size_t bytes) {
-  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  raise_smem(f, bytes);
 }
 
 // FP64 real -> full FP64 half spectrum with the double-precision kernels.
@@ -235,10 +260,10 @@ bool Evaluator<T>::setup_tma(std::string* err) {
   smem_tconv_ = 2 * tile_x + 2 * wt + 1024;
   smem_tback_ = 3 * tile_x + 2 * wt + 1024;
   if (std::max(smem_ty_, std::max(smem_tconv_, smem_tback_)) > 220 * 1024) return false;
-  cudaFuncSetAttribute(k_cols_y_tma<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ty_);
-  cudaFuncSetAttribute(k_cols_y_tma<T, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ty_);
-  cudaFuncSetAttribute(k_xconv_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tconv_);
-  cudaFuncSetAttribute(k_xbackconv_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tback_);
+  raise_smem(k_cols_y_tma<T, -1>, smem_ty_);
+  raise_smem(k_cols_y_tma<T, +1>, smem_ty_);
+  raise_smem(k_xconv_tma<T>, smem_tconv_);
+  raise_smem(k_xbackconv_tma<T>, smem_tback_);
   int nsm = 0, dev = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -259,7 +284,7 @@ bool Evaluator<T>::setup_tma(std::string* err) {
     smem_tphi_ = 2 * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L + 1) * cb) + 1024;
     if (smem_tphi_ <= 220 * 1024 && encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) {
       auto set_phi = [&](auto kern) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tphi_);
+        raise_smem(kern, smem_tphi_);
         int b2 = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, 256, smem_tphi_);
         return std::max(b2, 1);

@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
+#include <vector>
 #include "cdft_ctx.h"
 #include "cdft_kernels.cuh"
 #include "cdft_tma.cuh"
@@ -332,9 +334,11 @@ struct FireDevEngine {
   // FP32 phase arrays
   float *x32[2] = {nullptr, nullptr}, *v32[2] = {nullptr, nullptr}, *g32[2] = {nullptr, nullptr}, *rho32 = nullptr, *dF32 = nullptr;
   cudaGraphExec_t exec = nullptr;
+  cudaEvent_t done = nullptr;  // recorded after each batch's state read
   int exec_prec = -1;
   ~FireDevEngine() {
     if (exec) cudaGraphExecDestroy(exec);
+    if (done) cudaEventDestroy(done);
     cudaFree(st); cudaFreeHost(host); cudaFree(part);
     for (int i = 0; i < 2; ++i) { cudaFree(x32[i]); cudaFree(v32[i]); cudaFree(g32[i]); }
     cudaFree(rho32); cudaFree(dF32);
@@ -416,7 +420,8 @@ static int ensure_engine(cdft_ctx* c) {
   c->fire_dev = E;
   const long N = c->info.N;
   if (cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking) != cudaSuccess || cudaMalloc(&E->st, sizeof(FireState)) != cudaSuccess ||
-      cudaMallocHost(&E->host, sizeof(FireState)) != cudaSuccess || cudaMalloc(&E->part, (size_t)152 * 8 * 8 * sizeof(double)) != cudaSuccess)
+      cudaMallocHost(&E->host, sizeof(FireState)) != cudaSuccess || cudaMalloc(&E->part, (size_t)152 * 8 * 8 * sizeof(double)) != cudaSuccess ||
+      cudaEventCreateWithFlags(&E->done, cudaEventDisableTiming) != cudaSuccess)
     return cdft_internal_fail(c, CDFT_ERR_CUDA, "device FIRE engine allocation failed");
   (void)N;
   return CDFT_OK;
@@ -434,15 +439,31 @@ static int ensure_fp32_arrays(cdft_ctx* c) {
   return CDFT_OK;
 }
 
-// Runs graph-captured steps in precision `prec` until done (residual target,
-// uphill limit, timeout), max_steps, or - for the FP32 phase - until the
-// residual stops improving (stall) or drops below switch_tol.
-static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long max_steps, long* taken, int* stop) {
+// A phase runs graph-captured steps in one precision. It is split into
+// begin (upload the state, convert the vectors, capture one step), launch
+// (queue a batch of steps and an asynchronous read of the state), poll (read
+// the state after the batch and decide whether the phase is over) and end
+// (download the state, convert the vectors back), so that one host thread can
+// drive many contexts, each on its own stream.
+struct PhaseRun {
+  int prec = CDFT_FP64;
+  double tol = 0, switch_tol = 0;
+  long max_steps = -1, k = 0, best_at = 0, base = 0;
+  double best = 1e300;
+  int stop = 0;
+};
+
+static int phase_begin(cdft_ctx* c, PhaseRun* ph, int prec, double tol, double switch_tol, long max_steps) {
   FireDevEngine* E = c->fire_dev;
   const long N = c->info.N;
   const unsigned gn = grid_n(N);
   cudaStream_t s = E->stream;
-  // upload state; move vectors into the phase's storage
+  *ph = PhaseRun();
+  ph->prec = prec;
+  ph->tol = tol;
+  ph->switch_tol = switch_tol;
+  ph->max_steps = max_steps;
+  ph->base = c->fire_steps;
   state_from_ctx(c, E->host);
   cudaMemcpyAsync(E->st, E->host, sizeof(FireState), cudaMemcpyHostToDevice, s);
   if (prec == CDFT_FP32) {
@@ -454,14 +475,13 @@ static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long 
       k_convert<float><<<gn, kThreads, 0, s>>>(c->fg[i], E->g32[i], N);
     }
   }
-  // capture one step
   cudaGraph_t graph;
   if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return cdft_internal_fail(c, CDFT_ERR_CUDA, "capture");
   if (prec == CDFT_FP32) {
     float* x[2] = {E->x32[0], E->x32[1]};
     float* v[2] = {E->v32[0], E->v32[1]};
     float* g[2] = {E->g32[0], E->g32[1]};
-    record_step<float, float>(c, E, c->e32.get(), x, v, g, E->rho32, E->dF32, prec == CDFT_FP64 ? tol : 0.0);
+    record_step<float, float>(c, E, c->e32.get(), x, v, g, E->rho32, E->dF32, 0.0);
   } else {
     record_step<double, double>(c, E, c->e64.get(), c->fx, c->fv, c->fg, c->rho, c->dF, tol);
   }
@@ -473,35 +493,54 @@ static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long 
     return cdft_internal_fail(c, CDFT_ERR_CUDA, "graph instantiate");
   }
   cudaGraphDestroy(graph);
-  const int batch = 16;
-  long k = 0;
-  double best = 1e300;
-  long best_at = 0;
-  *stop = 0;
-  while (true) {
-    const long nb = (max_steps > 0) ? std::min<long>(batch, max_steps - k) : batch;
-    if (nb <= 0) break;
-    for (long j = 0; j < nb; ++j) cudaGraphLaunch(E->exec, s);
-    cudaMemcpyAsync(E->host, E->st, sizeof(FireState), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cdft_internal_fail(c, CDFT_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
-    const FireState& h = *E->host;
-    k = h.steps - c->fire_steps;
-    if (h.status) {
-      ctx_from_state(c, E->host);
-      *taken = k;
-      return cdft_internal_fail(c, h.status, h.status == CDFT_ERR_UPHILL ? "Cannot stop going uphill in Fire2" : "device wait timed out");
-    }
-    if (h.done) { *stop = 2; break; }
-    if (prec == CDFT_FP32) {
-      if (h.resid < best * 0.98) { best = h.resid; best_at = k; }
-      if (h.resid <= switch_tol) { *stop = 3; break; }
-      if (k - best_at > 96) { *stop = 4; break; }  // the FP32 residual has stalled (its noise floor)
-    }
-    if (max_steps > 0 && k >= max_steps) break;
+  return CDFT_OK;
+}
+
+// Queues up to `batch` steps and the state read; returns the number queued (0: step budget spent).
+static long phase_launch(cdft_ctx* c, PhaseRun* ph, int batch) {
+  FireDevEngine* E = c->fire_dev;
+  const long nb = (ph->max_steps > 0) ? std::min<long>(batch, ph->max_steps - ph->k) : batch;
+  if (nb <= 0) return 0;
+  for (long j = 0; j < nb; ++j) cudaGraphLaunch(E->exec, E->stream);
+  cudaMemcpyAsync(E->host, E->st, sizeof(FireState), cudaMemcpyDeviceToHost, E->stream);
+  cudaEventRecord(E->done, E->stream);
+  return nb;
+}
+
+// After the queued batch has completed: 1 if the phase is over, 0 to go on, < 0 never;
+// a device status (uphill, timeout) is returned through *rc.
+static int phase_poll(cdft_ctx* c, PhaseRun* ph, int* rc) {
+  FireDevEngine* E = c->fire_dev;
+  *rc = CDFT_OK;
+  if (cudaEventSynchronize(E->done) != cudaSuccess) {
+    *rc = cdft_internal_fail(c, CDFT_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    return 1;
   }
-  // download: scalars, and the FP32 phase's vectors back into FP64 storage
+  const FireState& h = *E->host;
+  ph->k = h.steps - ph->base;
+  if (h.status) {
+    ctx_from_state(c, E->host);
+    *rc = cdft_internal_fail(c, h.status, h.status == CDFT_ERR_UPHILL ? "Cannot stop going uphill in Fire2" : "device wait timed out");
+    return 1;
+  }
+  if (h.done) { ph->stop = 2; return 1; }
+  if (ph->prec == CDFT_FP32) {
+    if (h.resid < ph->best * 0.98) { ph->best = h.resid; ph->best_at = ph->k; }
+    if (h.resid <= ph->switch_tol) { ph->stop = 3; return 1; }
+    if (ph->k - ph->best_at > 96) { ph->stop = 4; return 1; }  // the FP32 residual has stalled (its noise floor)
+  }
+  if (ph->max_steps > 0 && ph->k >= ph->max_steps) return 1;
+  return 0;
+}
+
+// Downloads the scalars and moves the FP32 phase's vectors back into FP64 storage (asynchronous).
+static void phase_end(cdft_ctx* c, PhaseRun* ph) {
+  FireDevEngine* E = c->fire_dev;
+  const long N = c->info.N;
+  const unsigned gn = grid_n(N);
+  cudaStream_t s = E->stream;
   ctx_from_state(c, E->host);
-  if (prec == CDFT_FP32) {
+  if (ph->prec == CDFT_FP32) {
     for (int i = 0; i < 2; ++i) {
       k_convert_back<float><<<gn, kThreads, 0, s>>>(E->x32[i], c->fx[i], N);
       k_convert_back<float><<<gn, kThreads, 0, s>>>(E->v32[i], c->fv[i], N);
@@ -510,8 +549,23 @@ static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long 
     k_convert_back<float><<<gn, kThreads, 0, s>>>(E->rho32, c->rho, N);
     k_convert_back<float><<<gn, kThreads, 0, s>>>(E->dF32, c->dF, N);
   }
-  cudaStreamSynchronize(s);
-  *taken = k;
+}
+
+constexpr int kStepsPerRead = 16;
+
+// Runs one phase to its end on one context.
+static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long max_steps, long* taken, int* stop) {
+  PhaseRun ph;
+  int rc = phase_begin(c, &ph, prec, tol, switch_tol, max_steps);
+  if (rc) return rc;
+  while (phase_launch(c, &ph, kStepsPerRead) > 0) {
+    if (phase_poll(c, &ph, &rc)) break;
+  }
+  *taken = ph.k;
+  *stop = ph.stop;
+  if (rc) return rc;
+  phase_end(c, &ph);
+  cudaStreamSynchronize(c->fire_dev->stream);
   return CDFT_OK;
 }
 
@@ -586,4 +640,119 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
   total += taken;
   report_of(c, total, stop, rep, steps32);
   return rc;
+}
+
+// ------------------------------------------------------------ batches ---
+// Many independent systems (state points, possibly on different grids) run
+// their device FIRE2 concurrently: each context's graph-captured steps go to
+// its own stream, and one host thread polls every context's batch-end event,
+// queueing the next batch of a context as soon as its previous one has
+// finished. Small grids that cannot fill 152 SMs alone overlap on the GPU.
+namespace {
+struct BatchItem {
+  cdft_ctx* c = nullptr;
+  cudaStream_t saved_stream = nullptr;
+  PhaseRun ph;
+  int stage = 0;  // 0 FP32 bulk phase, 1 FP64 phase, 2 finished
+  long total = 0, steps32 = 0;
+  int rc = CDFT_OK;
+};
+}  // namespace
+
+static void batch_finish(BatchItem& b, cdft_fire_report* rep, int stop) {
+  report_of(b.c, b.total, stop, rep, b.steps32);
+  b.stage = 2;
+}
+
+// Starts the FP64 phase of an item, or finishes it when nothing is left to do.
+static void batch_start_fp64(BatchItem& b, double tol, long max_steps, cdft_fire_report* rep) {
+  if ((max_steps > 0 && b.total >= max_steps) || b.c->resid <= tol) {
+    batch_finish(b, rep, b.c->resid <= tol ? 2 : 0);
+    return;
+  }
+  b.rc = phase_begin(b.c, &b.ph, CDFT_FP64, tol, 0.0, max_steps > 0 ? max_steps - b.total : -1);
+  if (b.rc) { batch_finish(b, rep, 0); return; }
+  b.stage = 1;
+  if (phase_launch(b.c, &b.ph, kStepsPerRead) == 0) batch_finish(b, rep, 0);
+}
+
+extern "C" int cdft_fire_run_batch(cdft_ctx* const* ctx, int n, double resid_tol, double switch_tol, long max_steps, int mixed,
+                                   cdft_fire_report* reps, int* rcs) {
+  if (!ctx || n <= 0) return CDFT_ERR_ARG;
+  std::vector<BatchItem> items(n);
+  for (int i = 0; i < n; ++i) {
+    if (!ctx[i]) return CDFT_ERR_ARG;
+    for (int j = 0; j < i; ++j)
+      if (ctx[j] == ctx[i]) return cdft_internal_fail(ctx[i], CDFT_ERR_ARG, "a context appears twice in the batch");
+    if (!ctx[i]->fire_ready) return cdft_internal_fail(ctx[i], CDFT_ERR_STATE, "cdft_fire_init has not been called");
+  }
+  // allocation first (nothing may allocate while a stream is captured), and
+  // every context's own work on its engine's stream
+  for (int i = 0; i < n; ++i) {
+    BatchItem& b = items[i];
+    b.c = ctx[i];
+    int rc = ensure_engine(b.c);
+    if (!rc && mixed) rc = cdft_set_precision(b.c, CDFT_FP32);
+    if (!rc && mixed) rc = ensure_fp32_arrays(b.c);
+    if (!rc) rc = cdft_set_precision(b.c, CDFT_FP64);
+    if (rc) return rc;
+    cudaStreamSynchronize(b.c->stream);
+    b.saved_stream = b.c->stream;
+    b.c->stream = b.c->fire_dev->stream;
+  }
+  for (int i = 0; i < n; ++i) {
+    BatchItem& b = items[i];
+    cdft_fire_report* rep = reps ? &reps[i] : nullptr;
+    if (mixed) {
+      b.rc = cdft_set_precision(b.c, CDFT_FP32);
+      if (!b.rc) b.rc = phase_begin(b.c, &b.ph, CDFT_FP32, resid_tol, switch_tol, max_steps);
+      if (b.rc) { batch_finish(b, rep, 0); continue; }
+      b.stage = 0;
+      if (phase_launch(b.c, &b.ph, kStepsPerRead) == 0) { batch_finish(b, rep, 0); continue; }
+    } else {
+      batch_start_fp64(b, resid_tol, max_steps, rep);
+    }
+  }
+  for (;;) {
+    int active = 0, progressed = 0;
+    for (int i = 0; i < n; ++i) {
+      BatchItem& b = items[i];
+      if (b.stage == 2) continue;
+      ++active;
+      if (cudaEventQuery(b.c->fire_dev->done) == cudaErrorNotReady) continue;
+      ++progressed;
+      cdft_fire_report* rep = reps ? &reps[i] : nullptr;
+      int rc = CDFT_OK;
+      bool over = phase_poll(b.c, &b.ph, &rc) != 0;
+      if (!over && phase_launch(b.c, &b.ph, kStepsPerRead) == 0) over = true;
+      if (!over) continue;
+      b.total += b.ph.k;
+      if (rc) {
+        b.rc = rc;
+        batch_finish(b, rep, b.ph.stop);
+        continue;
+      }
+      phase_end(b.c, &b.ph);
+      if (b.stage == 0) {
+        b.steps32 = b.ph.k;
+        b.rc = refresh_fp64(b.c);
+        if (b.rc) { batch_finish(b, rep, 0); continue; }
+        batch_start_fp64(b, resid_tol, max_steps, rep);
+      } else {
+        cudaStreamSynchronize(b.c->fire_dev->stream);
+        batch_finish(b, rep, b.ph.stop);
+      }
+    }
+    if (!active) break;
+    if (!progressed) std::this_thread::yield();
+  }
+  int first = CDFT_OK;
+  for (int i = 0; i < n; ++i) {
+    BatchItem& b = items[i];
+    cudaStreamSynchronize(b.c->stream);
+    b.c->stream = b.saved_stream;
+    if (rcs) rcs[i] = b.rc;
+    if (b.rc && !first) first = b.rc;
+  }
+  return first;
 }

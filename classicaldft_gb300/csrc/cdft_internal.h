@@ -20,7 +20,11 @@ struct FFTTable {
   void* d32 = nullptr;  // float2[]
   ~FFTTable();
 };
-std::shared_ptr<FFTTable> make_fft_table(int n, std::string* err);  // nullptr if n has a prime factor > 31
+// Twiddle tables of the mixed-radix plan `radices` (default_radices(n) when
+// null; stages in order of execution, product n). nullptr if n has a prime
+// factor above 31 or the radices do not multiply to n.
+std::shared_ptr<FFTTable> make_fft_table(int n, std::string* err, const std::vector<int>* radices = nullptr);
+std::vector<int> default_radices(int n);
 
 // Host-side setup maths (cdft_setup.cpp).
 double bh_diameter_lj(double sigma, double eps, double rc, double kT);
@@ -70,6 +74,8 @@ class Evaluator {
   const T* weights() const { return w_; }
   const T* w_att() const { return watt_; }
   int M() const { return M_; }
+  // swap the transform plans (same lengths, another radix ordering)
+  void set_tables(FFTTable* tx, FFTTable* ty, FFTTable* tz) { tx_ = tx; ty_ = ty; tz_ = tz; }
   long spectrum_len() const { return Nc_; }  // complex values per spectrum (padded rows)
   int pitch() const { return pz_; }
   bool uses_tma() const { return tma_; }

@@ -174,6 +174,32 @@ int cdft_fire_run_to_residual(cdft_ctx* ctx, double resid_tol, long max_steps, c
  * at the same state and FP64 refinement. */
 int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, long max_steps, int mixed, cdft_fire_report* rep);
 
+/* cdft_fire_run_device on n independent contexts at once (state points of a
+ * parameter sweep, grids of different sizes). No counterpart in the reference,
+ * which solves one system per process. Each context's steps run on its own
+ * stream; one host thread queues a context's next 16 steps as soon as its
+ * previous ones have finished, so systems too small to fill the GPU overlap.
+ * Every context must have had cdft_fire_init and must appear once. reps[i] and
+ * rcs[i] (either array may be NULL) receive each context's report and status;
+ * the return value is the first non-zero status, or CDFT_OK. */
+int cdft_fire_run_batch(cdft_ctx* const* ctx, int n, double resid_tol, double switch_tol, long max_steps, int mixed,
+                        cdft_fire_report* reps, int* rcs);
+
+/* FFT-plan autotuner (no counterpart in the reference, which uses FFTW's
+ * planner). Times `reps` evaluations in the context's current precision for
+ * each candidate radix ordering of the z, then x, then y transforms, keeps
+ * the fastest, and remembers it for the grid, model and precision: later
+ * cdft_create calls with the same shape use the tuned plans. Overwrites the
+ * last evaluation's outputs (dF); the density and FIRE/DDFT state are kept.
+ * radices_out (3 x 8 ints, zero-padded, may be NULL) receives the x, y, z
+ * orderings; ms_out (2 doubles, may be NULL) the default and tuned ms per eval. */
+int cdft_autotune(cdft_ctx* ctx, int reps, int* radices_out, double* ms_out);
+/* The context's current x, y, z radix orderings (3 x 8 ints, zero-padded). */
+int cdft_get_radices(const cdft_ctx* ctx, int* radices_out);
+/* The orderings the autotuner tries for a transform length n (host only, no
+ * GPU): count receives the number of plans; out (max_plans x 8 ints) the first ones. */
+int cdft_radix_candidates(int n, int* out, int max_plans, int* count);
+
 /* DDFT integrating-factor dynamics, single species, periodic (include/Minimizer.h:189-266, src/DDFT.cpp:42-351). */
 typedef struct cdft_ddft_report {
   long steps;

@@ -1,6 +1,8 @@
 """CPU checks of the product library: it loads, exports every entry point
 include/cdft.h declares, and its host-only maths agrees with the oracle."""
 import ctypes
+
+import numpy as np
 import os
 import re
 
@@ -57,3 +59,15 @@ def test_product_weights_match_reference(tag, dx, n, hsd):
     w = cd.fmt_weights((n, n, n), dx, hsd)
     for a in range(11):
         np.testing.assert_allclose(w[a].ravel(), g[tag + ".w%d" % a], rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("n", [7, 16, 30, 48, 64, 80, 96, 112, 128, 144, 160, 256])
+def test_radix_candidates(n):
+    """Every plan the FFT autotuner tries is a factorisation of n into supported radices, the default first."""
+    import classicaldft_gb300 as cd
+    cands = cd.radix_candidates(n)
+    assert 1 <= len(cands) <= 12
+    assert len({tuple(c) for c in cands}) == len(cands)
+    for c in cands:
+        assert int(np.prod(c)) == n
+        assert all(r in (2, 4, 8) or (r % 2 == 1 and all(r % q for q in range(3, r, 2))) for r in c)
