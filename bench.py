@@ -44,8 +44,8 @@ def workload():
 
 
 # DRAM bytes per launch (read + write) from one ncu capture of the named kernel on
-# this workload (profiles/k_xbackconv_128_fp32.md); None where none was taken.
-NCU_TRAFFIC = {("xbackconv", "fp32"): 153.4e6 + 3.6e6}
+# this workload; None where none was taken.
+NCU_TRAFFIC = {("phi_rows", "fp32"): 98.1e6 + 43.9e6}
 
 
 def measured_peaks():

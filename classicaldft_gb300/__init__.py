@@ -32,7 +32,8 @@ C_FUNCTIONS = [
     "cdft_set_fixed_mass", "cdft_get_chem_potential", "cdft_eval", "cdft_bulk", "cdft_bh_diameter",
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
     "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device", "cdft_find_coex",
-    "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates",
+    "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates", "cdft_hessian_dot_v",
+    "cdft_newton_refine",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -74,7 +75,12 @@ class FireReport(ctypes.Structure):
                 ("F", ctypes.c_double), ("dt", ctypes.c_double), ("dt_max", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("vv", ctypes.c_double), ("fmax", ctypes.c_double),
                 ("resid", ctypes.c_double), ("backtracks", ctypes.c_int), ("stop", ctypes.c_int),
-                ("steps_fp32", ctypes.c_long)]
+                ("steps_fp32", ctypes.c_long), ("newton", ctypes.c_long), ("cg_iters", ctypes.c_long)]
+
+
+class NewtonReport(ctypes.Structure):
+    _fields_ = [("newton", ctypes.c_long), ("cg_iters", ctypes.c_long), ("evals", ctypes.c_long),
+                ("F", ctypes.c_double), ("resid", ctypes.c_double), ("stop", ctypes.c_int)]
 
 
 class DdftReport(ctypes.Structure):
@@ -115,6 +121,8 @@ def lib():
             "cdft_find_coex": ([vp, d, d, d, dp], i),
             "cdft_fire_run_batch": ([P(vp), i, d, d, ctypes.c_long, i, P(FireReport), P(i)], i),
             "cdft_autotune": ([vp, i, P(i), dp], i),
+            "cdft_hessian_dot_v": ([vp, vp, vp, i], i),
+            "cdft_newton_refine": ([vp, d, i, i, d, P(NewtonReport)], i),
             "cdft_get_radices": ([vp, P(i)], i),
             "cdft_radix_candidates": ([i, P(i), i, P(i)], i),
         }
@@ -295,10 +303,28 @@ class Context:
         return self._rep(r)
 
     def fire_run_device(self, tol, max_steps=-1, mixed=False, switch_tol=1e-6):
-        """Graph-captured FIRE2 to max|dOmega/drho| <= tol (FP64 test); mixed: FP32 bulk phase first."""
+        """Graph-captured FIRE2 to max|dOmega/drho| <= tol (FP64 test); mixed: FP32 bulk phase first
+        (True or 1: then FP64 FIRE2; 2: then Newton-Krylov refinement)."""
         r = FireReport()
         self._check(lib().cdft_fire_run_device(self._h, tol, switch_tol, max_steps, int(mixed), ctypes.byref(r)))
         return self._rep(r)
+
+    def newton_refine(self, tol, max_newton=12, max_cg=200, cg_rtol=1e-3):
+        """Newton-Krylov refinement with FP32 Hessian products and FP64 residuals (cdft_newton_refine)."""
+        r = NewtonReport()
+        self._check(lib().cdft_newton_refine(self._h, tol, max_newton, max_cg, cg_rtol, ctypes.byref(r)))
+        return self._rep(r)
+
+    def hessian_dot_v(self, v, out=None):
+        """Full Hessian of Omega times v at the current density (DFT::matrix_dot_v1).
+        v: numpy array (host) or CUDA float64 tensor (device; out must then be one too)."""
+        if hasattr(v, "data_ptr"):
+            self._check(lib().cdft_hessian_dot_v(self._h, ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(out.data_ptr()), 1))
+            return out
+        a = np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape)
+        o = np.empty(self.shape)
+        self._check(lib().cdft_hessian_dot_v(self._h, a.ctypes.data_as(ctypes.c_void_p), o.ctypes.data_as(ctypes.c_void_p), 0))
+        return o
 
     # FFT plans
     def autotune(self, reps=5):

@@ -374,12 +374,14 @@ int cdft_destroy(cdft_ctx* c) {
   if (!c) return CDFT_OK;
   cudaStreamSynchronize(c->stream);
   cdft_internal_fire_dev_free(c);
+  cdft_internal_newton_free(c);
   c->e64.reset();
   c->e32.reset();
   cudaFree(c->rho); cudaFree(c->dF); cudaFree(c->vext); cudaFree(c->red_part); cudaFree(c->red_out); cudaFreeHost(c->host_out);
   for (int i = 0; i < 2; ++i) { cudaFree(c->fx[i]); cudaFree(c->fv[i]); cudaFree(c->fg[i]); }
   cudaFree(c->dd0); cudaFree(c->dd1); cudaFree(c->ddn); cudaFree(c->dR); cudaFree(c->dfac);
   cudaFree(c->rk0); cudaFree(c->R0k); cudaFree(c->R1k); cudaFree(c->work);
+  cudaFree(c->hv_v); cudaFree(c->hv_out);
   delete c;
   return CDFT_OK;
 }
@@ -452,6 +454,36 @@ int cdft_set_fixed_mass(cdft_ctx* c, double m) {
 int cdft_get_chem_potential(const cdft_ctx* c, double* mu) {
   if (!c || !mu) return CDFT_ERR_ARG;
   *mu = c->mu;
+  return CDFT_OK;
+}
+
+// DFT::matrix_dot_v1 with the full Hessian (src/Dynamical_Matrix.cpp,
+// src/DFT.cpp:435-488; FMT::add_second_derivative src/FMT.cpp:437-567;
+// Interaction_Base::add_second_derivative src/Interaction.cpp:119-147), at the
+// context's current density.
+int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
+  if (!c || !v || !out) return CDFT_ERR_ARG;
+  int rc = ensure_evaluator(c, c->precision);
+  if (rc) return rc;
+  const size_t nb = c->info.N * sizeof(double);
+  if (!c->hv_v && (cudaMalloc(&c->hv_v, nb) != cudaSuccess || cudaMalloc(&c->hv_out, nb) != cudaSuccess))
+    return fail(c, CDFT_ERR_CUDA, "Hessian buffers");
+  const double* vd = v;
+  double* od = on_device ? out : c->hv_out;
+  if (!on_device) {
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->hv_v, v, nb, cudaMemcpyHostToDevice, c->stream));
+    vd = c->hv_v;
+  }
+  if (c->precision == CDFT_FP64) {
+    rc = c->e64->hess_prepare(c->rho, c->stream);
+    if (!rc) rc = c->e64->hess_apply<double>(vd, c->rho, od, c->info.dV, c->stream);
+  } else {
+    rc = c->e32->hess_prepare(c->rho, c->stream);
+    if (!rc) rc = c->e32->hess_apply<double>(vd, c->rho, od, c->info.dV, c->stream);
+  }
+  if (rc) return fail(c, CDFT_ERR_CUDA, "Hessian launch failed");
+  if (!on_device) CUDA_OR_FAIL(c, cudaMemcpyAsync(out, od, nb, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   return CDFT_OK;
 }
 
@@ -670,6 +702,19 @@ static int fire_accept(cdft_ctx* c, int s_idx) {
 }
 
 extern "C++" int cdft_internal_fire_accept(cdft_ctx* c, int s_idx) { return fire_accept(c, s_idx); }
+extern "C++" int cdft_internal_fire_resync(cdft_ctx* c) {
+  const long N = c->info.N;
+  const Alias a = c->alias();
+  const int k = c->cur;
+  k_alias_from_rho<<<grid_for(N), 256, 0, c->stream>>>(c->rho, c->fx[k], N, a);
+  k_rho_from_alias<<<grid_for(N), 256, 0, c->stream>>>(c->fx[k], c->rho, N, a);
+  CUDA_OR_FAIL(c, cudaMemsetAsync(c->fv[k], 0, N * sizeof(double), c->stream));
+  double t[8];
+  int rc = eval_internal(c, t);
+  if (rc) return rc;
+  c->F = t[0];
+  return fire_accept(c, k);
+}
 
 int cdft_fire_init(cdft_ctx* c, const cdft_fire_params* p) {
   if (!c) return CDFT_ERR_ARG;

@@ -15,6 +15,7 @@ struct Alias {
 };
 
 struct FireDevEngine;  // cdft_fire_dev.cu
+struct NewtonWork;     // cdft_newton.cu
 
 // ------------------------------------------------------------- context ---
 struct cdft_ctx {
@@ -54,8 +55,12 @@ struct cdft_ctx {
   double *dd0 = nullptr, *dd1 = nullptr, *ddn = nullptr, *dR = nullptr, *dfac = nullptr;
   void *rk0 = nullptr, *R0k = nullptr, *R1k = nullptr, *work = nullptr;
   std::vector<double> Lx, Ly, Lz;
+  // Hessian-vector product buffers (device, N doubles each; allocated on first use)
+  double *hv_v = nullptr, *hv_out = nullptr;
   // device FIRE2 engine (graph-captured steps)
   FireDevEngine* fire_dev = nullptr;
+  // Newton-Krylov refinement work arrays
+  NewtonWork* newton = nullptr;
 
   Alias alias() const {
     Alias a;
@@ -72,6 +77,9 @@ int cdft_internal_fail(cdft_ctx* c, int code, const std::string& m);
 int cdft_internal_eval(cdft_ctx* c, double* terms8, int only_fex);
 int cdft_internal_fire_accept(cdft_ctx* c, int s_idx);
 void cdft_internal_fire_dev_free(cdft_ctx* c);
+void cdft_internal_newton_free(cdft_ctx* c);
+// FIRE2 state re-derived from the current density: x = alias(rho), v = 0, one evaluation
+int cdft_internal_fire_resync(cdft_ctx* c);
 // plans cdft_autotune chose for the context's shape, model and precision (cdft_tune.cu)
 bool cdft_internal_tuned_plans(const cdft_ctx* c, int precision, std::array<std::vector<int>, 3>* plans);
 std::vector<std::vector<int>> cdft_internal_radix_candidates(int n);

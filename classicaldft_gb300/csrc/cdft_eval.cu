@@ -136,6 +136,7 @@ __global__ void k_compact(const double2* __restrict__ full, T* __restrict__ out,
 template <class T>
 Evaluator<T>::~Evaluator() {
   cudaFree(A_); cudaFree(Cf_); cudaFree(E_); cudaFree(w_); cudaFree(watt_); cudaFree(part_); cudaFree(terms_); cudaFree(status_);
+  cudaFree(NA_);
 }
 
 template <class T>
@@ -357,6 +358,14 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_phi_rows<T, MODEL_ESFMT>, smem_phi_);
   set_smem<T>(k_phi_rows<T, MODEL_WHITEBEAR_I>, smem_phi_);
   set_smem<T>(k_phi_rows<T, MODEL_WHITEBEAR_II>, smem_phi_);
+  set_smem<T>(k_hess_rows<T, MODEL_ROSENFELD>, smem_phi_);
+  set_smem<T>(k_hess_rows<T, MODEL_RSLT>, smem_phi_);
+  set_smem<T>(k_hess_rows<T, MODEL_ESFMT>, smem_phi_);
+  set_smem<T>(k_hess_rows<T, MODEL_WHITEBEAR_I>, smem_phi_);
+  set_smem<T>(k_hess_rows<T, MODEL_WHITEBEAR_II>, smem_phi_);
+  set_smem<T>(k_rows_c2r<T, T>, smem_rows_);
+  set_smem<T>(k_hess_final_rows<T, double>, smem_rows_);
+  set_smem<T>(k_hess_final_rows<T, T>, smem_rows_);
   // partial-sum storage: phi blocks (1 value), x columns (1 value), final rows (4 values)
   const long nphi = (rows_ + rb_phi_ - 1) / rb_phi_;
   const long ncolx = ((long)ny * pz_ + 7) / 8 + 16;  // x-pass blocks of the widest grid (8 columns per tile)
@@ -506,6 +515,81 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   return 0;
 }
 
+// ------------------------------------------------------------ Hessian ---
+template <class T>
+int Evaluator<T>::hess_prepare(const double* rho0, cudaStream_t s) {
+  if (M_ == 0) return 0;
+  if (!NA_ && cudaMalloc(&NA_, (size_t)M_ * N_ * sizeof(T)) != cudaSuccess) return 5;
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
+  const unsigned gcy = (unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_);
+  const unsigned gcx = (unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_);
+  constexpr int TCt = TileCols<T>::value;
+  const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
+  k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho0, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+  if (tma_) k_cols_y_tma<T, -1><<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_);
+  else k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  if (tma_) k_xconv_tma<T><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+  else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
+  if (tma_) k_cols_y_tma<T, +1><<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_);
+  else k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  for (int a = 0; a < M_; ++a)
+    k_rows_c2r<T, T><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(Cf_ + (long)a * Nc_, NA_ + (long)a * N_, d, tz_->plan,
+                                                                           twp<T>(tz_), rb_rows_, (T)1);
+  return cudaGetLastError() == cudaSuccess ? 0 : 5;
+}
+
+template <class T>
+template <class RT>
+int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV, cudaStream_t s) {
+  if (M_ > 0 && !NA_) return 7;
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
+  const unsigned gcy = (unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_);
+  const unsigned gcx = (unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_);
+  constexpr int TCt = TileCols<T>::value;
+  const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
+  const bool any = M_ > 0 || mf_;
+  auto yfwd = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
+    if (tma_) k_cols_y_tma<T, -1><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    else k_cols_fft<T, -1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  };
+  auto yinv = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
+    if (tma_) k_cols_y_tma<T, +1><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  };
+  if (any) {
+    k_rows_r2c<T, RT><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(v, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+    yfwd(A_, mapYA_, 1, grid_ty1_);
+  }
+  if (M_ > 0) {
+    if (tma_) k_xconv_tma<T><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+    else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
+    yinv(Cf_, mapYC_, M_, grid_tyM_);
+    const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
+    const unsigned g = (unsigned)((rows_ + rb_phi_ - 1) / rb_phi_);
+    switch (model_) {
+      case MODEL_ROSENFELD: k_hess_rows<T, MODEL_ROSENFELD><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
+      case MODEL_RSLT: k_hess_rows<T, MODEL_RSLT><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
+      case MODEL_ESFMT: k_hess_rows<T, MODEL_ESFMT><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
+      case MODEL_WHITEBEAR_I: k_hess_rows<T, MODEL_WHITEBEAR_I><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
+      default: k_hess_rows<T, MODEL_WHITEBEAR_II><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
+    }
+    yfwd(Cf_, mapYC_, M_, grid_tyM_);
+  }
+  double* part_mf = part_ + 2 * rows_;
+  if (any) {
+    if (tma_)
+      k_xbackconv_tma<T><<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_),
+                                                        mf_ ? part_mf : nullptr, status_);
+    else
+      k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
+                                                   mf_ ? part_mf : nullptr);
+    yinv(E_, mapYE_, 1, grid_ty1_);
+  }
+  k_hess_final_rows<T, RT><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(E_, rho0, v, out, d, tz_->plan, twp<T>(tz_), rb_rows_, dV,
+                                                                                 any ? 1 : 0);
+  return cudaGetLastError() == cudaSuccess ? 0 : 5;
+}
+
 template <class T>
 void Evaluator<T>::pass_bytes(double* by) const {
   const double b = sizeof(T), N = (double)N_, Nc = (double)nx_ * ny_ * nzc_, M = M_;
@@ -552,5 +636,8 @@ int Evaluator<T>::eval(const double* rho, const double* vext, double* dF, double
 template class Evaluator<float>;
 template class Evaluator<double>;
 template int Evaluator<float>::launch<float>(const float*, const double*, float*, double, double, int, cudaStream_t, cudaEvent_t*);
+template int Evaluator<float>::hess_apply<float>(const float*, const double*, float*, double, cudaStream_t);
+template int Evaluator<float>::hess_apply<double>(const double*, const double*, double*, double, cudaStream_t);
+template int Evaluator<double>::hess_apply<double>(const double*, const double*, double*, double, cudaStream_t);
 
 }  // namespace cdft

@@ -572,6 +572,8 @@ static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long 
 static void report_of(const cdft_ctx* c, long steps, int stop, cdft_fire_report* r, long steps32 = 0) {
   if (!r) return;
   r->steps_fp32 = steps32;
+  r->newton = 0;
+  r->cg_iters = 0;
   r->steps = steps;
   r->total_steps = c->fire_steps;
   r->calls = c->calls;
@@ -634,6 +636,16 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
     if (c->resid <= resid_tol) {
       report_of(c, total, 2, rep, steps32);
       return CDFT_OK;
+    }
+    if (mixed == 2) {  // Newton-Krylov refinement; FP64 FIRE2 only if it stalls
+      cdft_newton_report nr;
+      rc = cdft_newton_refine(c, resid_tol, 12, 200, 1e-3, &nr);
+      if (rc) return rc;
+      if (nr.stop == 2) {
+        report_of(c, total, 2, rep, steps32);
+        if (rep) rep->newton = nr.newton, rep->cg_iters = nr.cg_iters;
+        return CDFT_OK;
+      }
     }
   }
   rc = run_phase(c, CDFT_FP64, resid_tol, 0.0, max_steps > 0 ? max_steps - total : -1, &taken, &stop);

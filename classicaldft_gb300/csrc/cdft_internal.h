@@ -63,6 +63,13 @@ class Evaluator {
     return launch<double>(rho, vext, dF, dV, mu, ideal, s, ev);
   }
   bool has_mf() const { return mf_; }
+  // Hessian-vector products (DFT::matrix_dot_v_intern with the full Hessian):
+  // hess_prepare stores the M weighted densities of the state rho0 in real
+  // space (allocated on first use); hess_apply then maps v -> H v at that
+  // state, rho0 giving the ideal-gas term v/rho0. Asynchronous on s.
+  int hess_prepare(const double* rho0, cudaStream_t s);
+  template <class RT>
+  int hess_apply(const RT* v, const double* rho0, RT* out, double dV, cudaStream_t s);
   // Algorithmic bytes each of the 9 passes must move (reads + writes once).
   void pass_bytes(double* bytes) const;
   bool setup_tma(std::string* err);
@@ -99,6 +106,7 @@ class Evaluator {
   long part_len_ = 0;
   double* terms_ = nullptr;  // reduced sums: [0] sum Phi, [1] Parseval MF, [2] F_id, [3] sum rho, [4] sum V rho, [5] sum dF rho
   unsigned* status_ = nullptr;
+  T* NA_ = nullptr;  // Hessian: M weighted densities of the state, real space (M x N)
   int rb_rows_ = 16, rb_phi_ = 4, tc_ = 16;
   size_t smem_rows_ = 0, smem_phi_ = 0, smem_colx_ = 0, smem_coly_ = 0, smem_xconv_ = 0, smem_xback_ = 0;
   // tensor-copy path (cdft_kernels_tma.cuh)

@@ -410,6 +410,110 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
   }
 }
 
+// ---------------------------------------------------- Hessian z rows ---
+// The pointwise step of the Hessian-vector product (FMT::add_second_derivative,
+// src/FMT.cpp:437-567): the same row layout as k_phi_rows, with the M fields of
+// Cf holding the convolutions of v (z still in spectral form) and NA the M
+// weighted densities of the state in real space (M x N). Per point the folded
+// (d2Phi).Psi replaces Psi; the rows are transformed back over the inputs.
+template <class T, int MODEL>
+__global__ void __launch_bounds__(256) k_hess_rows(typename Cx<T>::type* __restrict__ Cf, const T* __restrict__ NA, Dims d, FFTPlan pz,
+                                                   const typename Cx<T>::type* __restrict__ tw, int RB, T hsd, T esA, T esB) {
+  typedef typename Cx<T>::type C;
+  constexpr int M = ModelTraits<MODEL>::M;
+  constexpr int NP = (M + 1) / 2;
+  const T ih = (T)(1.0 / (double)hsd), ih2 = (T)(1.0 / ((double)hsd * (double)hsd));
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nz = d.nz, LP = nz + 1, nzc = d.nzc;
+  const int L = NP * RB;
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  C* b1 = b0 + L * LP;
+  const long row0 = (long)blockIdx.x * RB;
+  for (int e = threadIdx.x; e < L * nz; e += blockDim.x) {
+    const int line = e / nz, k = e - line * nz;
+    const int r = line / NP, pr = line - r * NP;
+    const long row = row0 + r;
+    const C* Arow = nullptr;
+    const C* Brow = nullptr;
+    if (row < d.rows) {
+      Arow = Cf + (long)(2 * pr) * d.Nc + row * d.pz;
+      if (2 * pr + 1 < M) Brow = Cf + (long)(2 * pr + 1) * d.Nc + row * d.pz;
+    }
+    b0[line * LP + k] = pair_spectrum<T>(Arow, Brow, k, nz);
+  }
+  C* res = block_fft<+1, T>(b0, b1, L, LP, pz, tw);
+  C* other = (res == b0) ? b1 : b0;
+  for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+    const int r = e / nz, k = e - r * nz;
+    const long row = row0 + r;
+    if (row >= d.rows) continue;
+    T nv[11], pv[11];
+#pragma unroll
+    for (int a = 0; a < M; ++a) {
+      const C z = res[(r * NP + a / 2) * LP + k];
+      pv[a] = (a & 1) ? z.y : z.x;
+      nv[a] = NA[(long)a * d.N + row * nz + k];
+    }
+    fmt_d2phi_dot_point<T, MODEL>(nv, pv, ih, ih2, esA, esB);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const T im = (2 * p + 1 < M) ? pv[2 * p + 1] : (T)0;
+      other[(r * NP + p) * LP + k] = mk<T>(pv[2 * p], im);
+    }
+  }
+  C* res2 = block_fft<-1, T>(other, res, L, LP, pz, tw);
+  for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
+    const int line = e / nzc, k = e - line * nzc;
+    const int r = line / NP, pr = line - r * NP;
+    const long row = row0 + r;
+    if (row >= d.rows) continue;
+    const C Z = res2[line * LP + k];
+    const C W = res2[line * LP + (k == 0 ? 0 : nz - k)];
+    Cf[(long)(2 * pr) * d.Nc + row * d.pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
+    if (2 * pr + 1 < M) Cf[(long)(2 * pr + 1) * d.Nc + row * d.pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+  }
+}
+
+// Last step of the Hessian-vector product: c2r of E (FMT + mean-field
+// back-convolution of the Lambda fields) and the ideal-gas term,
+//   Hv = (v / rho + c2r(E)) dV   (DFT::matrix_dot_v_intern, src/DFT.cpp:455-462).
+template <class T, class RT>
+__global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::type* __restrict__ E, const double* __restrict__ rho,
+                                                         const RT* __restrict__ v, RT* __restrict__ out, Dims d, FFTPlan pz,
+                                                         const typename Cx<T>::type* __restrict__ tw, int RB, double dV, int have_fmt_or_mf) {
+  typedef typename Cx<T>::type C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  const int nz = d.nz, LP = nz + 1;
+  C* b1 = b0 + RB * LP;
+  const long pair0 = (long)blockIdx.x * RB;
+  C* res = b0;
+  if (have_fmt_or_mf) {
+    for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+      const int r = e / nz, k = e - r * nz;
+      const long ra = 2 * (pair0 + r), rb = ra + 1;
+      const C* Ar = ra < d.rows ? E + ra * d.pz : nullptr;
+      const C* Br = rb < d.rows ? E + rb * d.pz : nullptr;
+      b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
+    }
+    res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
+  }
+  const T dVt = (T)dV;
+  for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
+    const int rr = e / nz, k = e - rr * nz;
+    const long row = 2 * pair0 + rr;
+    if (row >= d.rows) continue;
+    const long p = row * nz + k;
+    T h = 0;
+    if (have_fmt_or_mf) {
+      const C z = res[(rr >> 1) * LP + k];
+      h = (rr & 1) ? z.y : z.x;
+    }
+    const T f = ((T)v[p] / (T)rho[p]) * dVt + h * dVt;
+    out[p] = (RT)f;
+  }
+}
+
 // ------------------------------------------------------ final z rows ---
 // c2r of E (the summed hard-sphere + mean-field back-convolution) and the
 // pointwise terms of DFT::calculateFreeEnergyAndDerivatives_internal_

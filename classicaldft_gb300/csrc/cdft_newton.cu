@@ -1,0 +1,256 @@
+// Mixed-precision Newton-Krylov refinement of a minimum (no counterpart in the
+// reference, whose minimisers are FIRE2 and DDFT). The residual is an FP64
+// evaluation (DFT::calculateFreeEnergyAndDerivatives); each Newton correction
+// solves H d = -dF with preconditioned conjugate gradients whose
+// Hessian-vector products (DFT::matrix_dot_v_intern, src/DFT.cpp:435-488) run
+// in the FP32 bulk precision: the correction only has to be accurate
+// relative to itself, so FP32 products suffice, while every accepted state is
+// judged by FP64. At fixed mass the system is solved on sum(d) = 0 (the
+// constraint Species::setFixedMass imposes) by projecting the operator, the
+// right-hand side and the preconditioned residuals. The preconditioner is the
+// inverse of the ideal-gas block of H, rho/dV.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+#include "cdft_ctx.h"
+
+using namespace cdft;
+
+namespace {
+constexpr int kT = 256;
+unsigned grid_of(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + kT - 1) / kT, 152 * 4)); }
+
+// Block sums of up to 3 values, FP64, one slot per block.
+template <int NV>
+__device__ void block_store(double* v, double* part) {
+  __shared__ double sh[NV][kT / 32];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double x = v[j];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) sh[j][threadIdx.x >> 5] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double s = 0;
+      for (int w = 0; w < kT / 32; ++w) s += sh[j][w];
+      part[blockIdx.x * NV + j] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_nk_init(const double* dF, float* r, float* dl, long n, double* part) {
+  double s = 0;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
+    const float x = (float)(-dF[i]);
+    r[i] = x;
+    dl[i] = 0.f;
+    s += x;
+  }
+  double v[1] = {s};
+  block_store<1>(v, part);
+}
+__global__ void k_nk_shift(float* x, long n, float c) {
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) x[i] -= c;
+}
+// z = (rho/dV) r; sums: z
+__global__ void __launch_bounds__(kT) k_nk_precond(const float* r, const double* rho, float* z, long n, double idV, double* part) {
+  double s = 0;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
+    const float x = (float)((double)r[i] * rho[i] * idV);
+    z[i] = x;
+    s += x;
+  }
+  double v[1] = {s};
+  block_store<1>(v, part);
+}
+// z -= zshift; sums: r.z, r.r
+__global__ void __launch_bounds__(kT) k_nk_rz(const float* r, float* z, long n, float zshift, double* part) {
+  double a = 0, b = 0;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
+    const float zz = z[i] - zshift;
+    z[i] = zz;
+    a += (double)r[i] * zz;
+    b += (double)r[i] * r[i];
+  }
+  double v[2] = {a, b};
+  block_store<2>(v, part);
+}
+__global__ void k_nk_p(float* p, const float* z, long n, float beta) {
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) p[i] = z[i] + beta * p[i];
+}
+// sums: q, p.q
+__global__ void __launch_bounds__(kT) k_nk_pq(const float* p, const float* q, long n, double* part) {
+  double a = 0, b = 0;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
+    a += q[i];
+    b += (double)p[i] * q[i];
+  }
+  double v[2] = {a, b};
+  block_store<2>(v, part);
+}
+__global__ void k_nk_update(float* dl, float* r, const float* p, const float* q, long n, float alpha, float qshift) {
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
+    dl[i] += alpha * p[i];
+    r[i] -= alpha * (q[i] - qshift);
+  }
+}
+// largest fraction of rho any point loses: max(-d/rho); sums slot holds the max
+__global__ void __launch_bounds__(kT) k_nk_loss(const double* rho, const float* dl, long n, double* part) {
+  double m = 0;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) m = fmax(m, -(double)dl[i] / rho[i]);
+  __shared__ double sh[kT / 32];
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0;
+    for (int w = 0; w < kT / 32; ++w) x = fmax(x, sh[w]);
+    part[blockIdx.x] = x;
+  }
+}
+__global__ void k_nk_step(double* rho, const double* rho0, const float* dl, long n, double s) {
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) rho[i] = rho0[i] + s * (double)dl[i];
+}
+}  // namespace
+
+struct NewtonWork {
+  float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dl = nullptr;
+  double* rho0 = nullptr;
+  double* part = nullptr;   // device, 3 x grid
+  double* hpart = nullptr;  // pinned
+  ~NewtonWork() {
+    cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(dl); cudaFree(rho0); cudaFree(part); cudaFreeHost(hpart);
+  }
+};
+
+void cdft_internal_newton_free(cdft_ctx* c) {
+  delete c->newton;
+  c->newton = nullptr;
+}
+
+// Sums the NV block partials of the last reduction (synchronises the stream).
+template <int NV>
+static bool sums(cdft_ctx* c, unsigned g, double* out) {
+  NewtonWork* W = c->newton;
+  if (cudaMemcpyAsync(W->hpart, W->part, (size_t)g * NV * sizeof(double), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return false;
+  for (int j = 0; j < NV; ++j) out[j] = 0;
+  for (unsigned b = 0; b < g; ++b)
+    for (int j = 0; j < NV; ++j) out[j] += W->hpart[b * NV + j];
+  return true;
+}
+
+extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int max_cg, double cg_rtol, cdft_newton_report* rep) {
+  if (!c || !(tol > 0) || max_newton <= 0 || max_cg <= 0 || !(cg_rtol > 0)) return CDFT_ERR_ARG;
+  const long N = c->info.N;
+  const double dV = c->info.dV;
+  const bool fixed = c->fixed_mass > 0;
+  int rc = cdft_set_precision(c, CDFT_FP32);  // the Hessian products' evaluator
+  if (!rc) rc = cdft_set_precision(c, CDFT_FP64);
+  if (rc) return rc;
+  const unsigned g = grid_of(N);
+  if (!c->newton) {
+    NewtonWork* W = new NewtonWork();
+    c->newton = W;
+    const size_t fb = N * sizeof(float);
+    if (cudaMalloc(&W->r, fb) != cudaSuccess || cudaMalloc(&W->z, fb) != cudaSuccess || cudaMalloc(&W->p, fb) != cudaSuccess ||
+        cudaMalloc(&W->q, fb) != cudaSuccess || cudaMalloc(&W->dl, fb) != cudaSuccess ||
+        cudaMalloc(&W->rho0, N * sizeof(double)) != cudaSuccess || cudaMalloc(&W->part, (size_t)g * 3 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&W->hpart, (size_t)g * 3 * sizeof(double)) != cudaSuccess) {
+      cdft_internal_newton_free(c);
+      return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton work arrays");
+    }
+  }
+  NewtonWork* W = c->newton;
+  cudaStream_t s = c->stream;
+  cdft_newton_report R{};
+  double t[8];
+  rc = cdft_internal_eval(c, t, 0);
+  ++R.evals;
+  if (rc) return rc;
+  double resid = t[6];
+  R.F = t[0];
+  int stop = 0;
+  for (int k = 0; k < max_newton && resid > tol; ++k) {
+    // Hessian at the current state; right-hand side -dF, projected at fixed mass
+    if (c->e32->hess_prepare(c->rho, s)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian prepare failed");
+    double sm[3];
+    k_nk_init<<<g, kT, 0, s>>>(c->dF, W->r, W->dl, N, W->part);
+    if (!sums<1>(c, g, sm)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");
+    if (fixed) k_nk_shift<<<g, kT, 0, s>>>(W->r, N, (float)(sm[0] / N));
+    auto precond = [&](double* rz_rr) -> bool {
+      k_nk_precond<<<g, kT, 0, s>>>(W->r, c->rho, W->z, N, 1.0 / dV, W->part);
+      double zs[1];
+      if (!sums<1>(c, g, zs)) return false;
+      k_nk_rz<<<g, kT, 0, s>>>(W->r, W->z, N, fixed ? (float)(zs[0] / N) : 0.f, W->part);
+      return sums<2>(c, g, rz_rr);
+    };
+    double rz_rr[2];
+    if (!precond(rz_rr)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");
+    cudaMemcpyAsync(W->p, W->z, N * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    double rz = rz_rr[0];
+    const double r0 = std::sqrt(rz_rr[1]);
+    int it = 0;
+    for (; it < max_cg; ++it) {
+      if (c->e32->hess_apply<float>(W->p, c->rho, W->q, dV, s)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian product failed");
+      k_nk_pq<<<g, kT, 0, s>>>(W->p, W->q, N, W->part);
+      double pq[2];
+      if (!sums<2>(c, g, pq)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");
+      if (!(pq[1] > 0)) break;  // not positive along p: keep the correction built so far
+      const double alpha = rz / pq[1];
+      k_nk_update<<<g, kT, 0, s>>>(W->dl, W->r, W->p, W->q, N, (float)alpha, fixed ? (float)(pq[0] / N) : 0.f);
+      double nz[2];
+      if (!precond(nz)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");
+      if (std::sqrt(nz[1]) <= cg_rtol * r0) { ++it; break; }
+      const double beta = nz[0] / rz;
+      rz = nz[0];
+      k_nk_p<<<g, kT, 0, s>>>(W->p, W->z, N, (float)beta);
+    }
+    R.cg_iters += it;
+    // step: at most half of any point's density, then halve until the FP64 residual drops
+    k_nk_loss<<<g, kT, 0, s>>>(c->rho, W->dl, N, W->part);
+    if (cudaMemcpyAsync(W->hpart, W->part, g * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");
+    double loss = 0;
+    for (unsigned b = 0; b < g; ++b) loss = std::max(loss, W->hpart[b]);
+    double step = loss > 0.5 ? 0.5 / loss : 1.0;
+    cudaMemcpyAsync(W->rho0, c->rho, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    bool accepted = false;
+    for (int ls = 0; ls < 6 && !accepted; ++ls, step *= 0.5) {
+      k_nk_step<<<g, kT, 0, s>>>(c->rho, W->rho0, W->dl, N, step);
+      rc = cdft_internal_eval(c, t, 0);
+      ++R.evals;
+      if (rc && rc != CDFT_ERR_ETA) return rc;
+      if (!rc && t[6] < resid) {
+        accepted = true;
+        resid = t[6];
+        R.F = t[0];
+      }
+    }
+    ++R.newton;
+    if (!accepted) {  // no decrease along the correction: back to the last state
+      cudaMemcpyAsync(c->rho, W->rho0, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      rc = cdft_internal_eval(c, t, 0);
+      ++R.evals;
+      if (rc) return rc;
+      resid = t[6];
+      R.F = t[0];
+      stop = 3;
+      break;
+    }
+  }
+  if (resid <= tol) stop = 2;
+  R.resid = resid;
+  R.stop = stop;
+  if (rep) *rep = R;
+  // keep the FIRE2 state consistent with the refined density
+  if (c->fire_ready) {
+    rc = cdft_internal_fire_resync(c);
+    if (rc) return rc;
+  }
+  return CDFT_OK;
+}

@@ -160,4 +160,245 @@ __device__ __forceinline__ T fmt_phi_point(T* n, T ih, T ih2, T A, T B) {
   return phi;
 }
 
+// ------------------------------------------------------------ Hessian ---
+// Second derivatives of f1, f2, f3 (include/FMT.h: Rosenfeld :163-199, RSLT
+// :284-289, WhiteBearI :530-556, WhiteBearII :604-632), the reference's forms.
+template <class T, int MODEL>
+__device__ __forceinline__ void fmt_fpp(T e, T L, T& f1pp, T& f2pp, T& f3pp) {
+  const T one = (T)1;
+  const T g = one / (one - e);
+  const T g2 = g * g;
+  f1pp = -g2;
+  f2pp = (T)2 * g2 * g;
+  f3pp = (T)6 * g2 * g2;
+  if (MODEL == MODEL_RSLT || MODEL == MODEL_WHITEBEAR_I) {
+    if (e < (T)1e-12) f3pp = (T)7.5 + (T)28.8 * e;
+    else {
+      const T ie = one / e, ie2 = ie * ie;
+      f3pp = ((T)6 - (T)21 * e + (T)26 * e * e - (T)5 * e * e * e) * ie2 * ie * g2 * g2 + (T)6 * L * ie2 * ie2;
+    }
+  } else if (MODEL == MODEL_WHITEBEAR_II) {
+    if (e < (T)1e-12) {
+      f2pp = (T)(20.0 / 9) + (T)7 * e;
+      f3pp = (T)7.5 + (T)25.2 * e;
+    } else {
+      const T ie = one / e, ie2 = ie * ie;
+      f2pp = (T)(2.0 / 3.0) * ((T)7 * e * e - (T)5 * e + (T)2) * ie2 * g2 * g + (T)(4.0 / 3.0) * ie2 * ie * L;
+      f3pp = -((T)6 - (T)21 * e + (T)26 * e * e - (T)19 * e * e * e + (T)2 * e * e * e * e) * ie2 * ie * g2 * g2 - (T)6 * ie2 * ie2 * L;
+    }
+  }
+}
+
+// sum_b (d2Phi/dn_a dn_b) psi_b for one point (FMT::calculate_d2Phi_dot_V,
+// src/FMT.cpp:181-280), in the folded per-species form: n[] are the M weighted
+// densities of the state, p[] the M convolutions of v with the same weights
+// (FMT::add_second_derivative's Psi, src/FMT.cpp:437-509, with s0 = s/d^2,
+// s1 = s/d, v1 = v/d expanded here). On return p[] holds the M fields the
+// back-convolution takes: the s slot sums the s0, s1, s2 rows with 1/d^2, 1/d,
+// 1; the vector slots carry the conjugated (odd) weights' sign; off-diagonal
+// tensor slots sum the (i,j) and (j,i) rows (src/FMT.cpp:530-566).
+template <class T, int MODEL>
+__device__ __forceinline__ void fmt_d2phi_dot_point(const T* n, T* p, T ih, T ih2, T A, T B) {
+  constexpr bool TEN = ModelTraits<MODEL>::tensor;
+  const T one = (T)1;
+  const T i_pi = (T)(1.0 / 3.14159265358979323846);
+  const T i_2pi = (T)(0.5 / 3.14159265358979323846);
+  const T i_24pi = (T)(1.0 / (24 * 3.14159265358979323846));
+  const T i_8pi = (T)(1.0 / (8 * 3.14159265358979323846));
+  const T eta = n[0];
+  const T s2 = n[1], s1 = n[1] * ih, s0 = n[1] * ih2;
+  T v2[3], v1[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) { v2[i] = n[2 + i]; v1[i] = n[2 + i] * ih; }
+  T Tm[3][3];
+  if (TEN) {
+    Tm[0][0] = n[5]; Tm[0][1] = Tm[1][0] = n[6]; Tm[0][2] = Tm[2][0] = n[7];
+    Tm[1][1] = n[8]; Tm[1][2] = Tm[2][1] = n[9]; Tm[2][2] = n[10];
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Tm[i][j] = (T)0;
+  }
+  // Psi in the 19-slot form
+  const T Pe = p[0], Ps2 = p[1], Ps1 = p[1] * ih, Ps0 = p[1] * ih2;
+  T Pv2[3], Pv1[3], PT[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) { Pv2[i] = p[2 + i]; Pv1[i] = p[2 + i] * ih; }
+  if (TEN) {
+    PT[0][0] = p[5]; PT[0][1] = PT[1][0] = p[6]; PT[0][2] = PT[2][0] = p[7];
+    PT[1][1] = p[8]; PT[1][2] = PT[2][1] = p[9]; PT[2][2] = p[10];
+  }
+  const T v1_v2 = v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2];
+  const T v2_v2 = v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2];
+  T f1, f2, f3, f1p, f2p, f3p, f1pp, f2pp, f3pp;
+  fmt_f<T, MODEL>(eta, f1, f2, f3, f1p, f2p, f3p);
+  fmt_fpp<T, MODEL>(eta, f1, f1pp, f2pp, f3pp);  // f1 = ln(1 - eta)
+
+  // Phi3 and its derivatives
+  T Phi3, d_S2, d_V2[3], d_T[3][3], dd_S2S2, dd_V2S2[3], dd_V2V2[3][3], dd_S2T[3][3];
+  const T a = (MODEL == MODEL_ESFMT) ? A : one, b = (MODEL == MODEL_ESFMT) ? B : -one;
+  if (TEN) {
+    T vT[3], TT[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) vT[i] = v2[0] * Tm[0][i] + v2[1] * Tm[1][i] + v2[2] * Tm[2][i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) TT[i][j] = Tm[i][0] * Tm[0][j] + Tm[i][1] * Tm[1][j] + Tm[i][2] * Tm[2][j];
+    const T vTv = v2[0] * vT[0] + v2[1] * vT[1] + v2[2] * vT[2];
+    const T T2 = TT[0][0] + TT[1][1] + TT[2][2];
+    T T3 = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) T3 += TT[i][j] * Tm[j][i];
+    const T a24 = a * i_24pi, b24 = b * i_24pi;
+    Phi3 = a24 * (s2 * s2 * s2 - (T)3 * s2 * v2_v2 + (T)3 * vTv - T3) + b24 * (s2 * s2 * s2 - (T)3 * s2 * T2 + (T)2 * T3);
+    d_S2 = a24 * ((T)3 * s2 * s2 - (T)3 * v2_v2) + b24 * ((T)3 * s2 * s2 - (T)3 * T2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d_V2[k] = a24 * (-(T)6 * s2 * v2[k] + (T)6 * vT[k]);
+    const T a8 = a * i_8pi, b4 = (T)2 * b * i_8pi;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        d_T[j][k] = a8 * (v2[j] * v2[k] - TT[k][j]) + b4 * (-s2 * Tm[k][j] + TT[k][j]);
+        dd_S2T[j][k] = b4 * (-Tm[k][j]);
+        dd_V2V2[j][k] = a24 * ((T)3 * Tm[j][k] + (T)3 * Tm[k][j] - (j == k ? (T)6 * s2 : (T)0));
+      }
+    dd_S2S2 = a24 * ((T)6 * s2) + b24 * ((T)6 * s2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dd_V2S2[k] = a24 * (-(T)6 * v2[k]);
+  } else if (MODEL == MODEL_RSLT) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { d_T[j][k] = 0; dd_S2T[j][k] = 0; dd_V2V2[j][k] = 0; }
+    if (s2 < (T)1e-20) {
+      Phi3 = 0; d_S2 = 0; dd_S2S2 = 0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { d_V2[k] = 0; dd_V2S2[k] = 0; }
+    } else {
+      const T is2 = one / s2;
+      const T psi = v2_v2 * is2 * is2;
+      const T om = one - psi;
+      Phi3 = (T)(1.0 / (36 * 3.14159265358979323846)) * s2 * s2 * s2 * om * om * om;
+      d_S2 = (T)(1.0 / (12 * 3.14159265358979323846)) * s2 * s2 * (one + psi) * om * om;
+      dd_S2S2 = (T)(1.0 / (6 * 3.14159265358979323846)) * s2 * om * (one + psi + (T)2 * psi * psi);
+      const T c36 = (T)(1.0 / (36 * 3.14159265358979323846));
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        d_V2[k] = -(T)(1.0 / (6 * 3.14159265358979323846)) * s2 * v2[k] * om * om;
+        dd_V2S2[k] = c36 * (-(T)6 * v2[k]) * om * (one + (T)3 * psi);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          dd_V2V2[i][j] = (i == j) ? c36 * (-(T)6 * s2) * om * (om - (T)4 * v2[i] * v2[i] * is2 * is2)
+                                   : c36 * ((T)24 * is2) * v2[i] * v2[j] * om;
+    }
+  } else {  // Rosenfeld
+    Phi3 = i_24pi * (s2 * s2 * s2 - (T)3 * s2 * v2_v2);
+    d_S2 = i_24pi * ((T)3 * s2 * s2 - (T)3 * v2_v2);
+    dd_S2S2 = i_24pi * ((T)6 * s2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { d_V2[k] = i_24pi * (-(T)6 * s2 * v2[k]); dd_V2S2[k] = i_24pi * (-(T)6 * v2[k]); }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { d_T[j][k] = 0; dd_S2T[j][k] = 0; dd_V2V2[j][k] = (j == k) ? i_24pi * (-(T)6 * s2) : (T)0; }
+  }
+
+  // r = (d2Phi) . Psi, 19 slots
+  T Re = (-i_pi * s0 * f1pp + i_2pi * (s1 * s2 - v1_v2) * f2pp + Phi3 * f3pp) * Pe;
+  Re += -i_pi * f1p * Ps0;
+  const T Rs0 = -i_pi * f1p * Pe;
+  Re += i_2pi * s2 * f2p * Ps1;
+  T Rs1 = i_2pi * s2 * f2p * Pe;
+  const T es2 = i_2pi * s1 * f2p + d_S2 * f3p;
+  Re += es2 * Ps2;
+  T Rs2 = es2 * Pe;
+  T Rv1[3], Rv2[3], RT[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Re += -i_2pi * v2[i] * f2p * Pv1[i];
+    Rv1[i] = -i_2pi * v2[i] * f2p * Pe;
+    const T ev2 = -i_2pi * v1[i] * f2p + d_V2[i] * f3p;
+    Re += ev2 * Pv2[i];
+    Rv2[i] = ev2 * Pe;
+  }
+  Rs1 += i_2pi * f2 * Ps2;
+  Rs2 += i_2pi * f2 * Ps1;
+  Rs2 += dd_S2S2 * f3 * Ps2;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Rs2 += dd_V2S2[i] * f3 * Pv2[i];
+    Rv2[i] += dd_V2S2[i] * f3 * Ps2;
+    Rv1[i] += -i_2pi * f2 * Pv2[i];
+    Rv2[i] += -i_2pi * f2 * Pv1[i];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Rv2[i] += dd_V2V2[i][j] * f3 * Pv2[j];
+  }
+  if (TEN) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) RT[i][j] = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        Re += d_T[i][j] * f3p * PT[i][j];
+        RT[i][j] += d_T[i][j] * f3p * Pe;
+        Rs2 += dd_S2T[i][j] * f3 * PT[i][j];
+        RT[i][j] += dd_S2T[i][j] * f3 * Ps2;
+      }
+    // dPhi3/dv2_i dT_jk = A (delta_ij v2_k + delta_ik v2_j) / 8pi
+    const T a8 = a * i_8pi;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          T c = 0;
+          if (i == j) c += v2[k];
+          if (i == k) c += v2[j];
+          if (i == j || i == k) {
+            Rv2[i] += a8 * c * f3 * PT[j][k];
+            RT[j][k] += a8 * c * f3 * Pv2[i];
+          }
+        }
+    // dPhi3/dT_jk dT_lm = [d_lk (-A + 2B) T_mj + d_mj (-A + 2B) T_kl - d_lk d_mj 2B s2] / 8pi
+    const T ab = (-a + (T)2 * b) * i_8pi, b2s = -(T)2 * b * s2 * i_8pi;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        T acc = 0;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) acc += ab * Tm[m][j] * PT[k][m];  // l = k
+#pragma unroll
+        for (int l = 0; l < 3; ++l) acc += ab * Tm[k][l] * PT[l][j];  // m = j
+        acc += b2s * PT[k][j];                                     // l = k, m = j
+        RT[j][k] += acc * f3;
+      }
+  }
+  // fold into the M back-convolution fields
+  p[0] = Re;
+  p[1] = Rs0 * ih2 + Rs1 * ih + Rs2;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) p[2 + i] = -(Rv1[i] * ih + Rv2[i]);
+  if (TEN) {
+    p[5] = RT[0][0];
+    p[6] = RT[0][1] + RT[1][0];
+    p[7] = RT[0][2] + RT[2][0];
+    p[8] = RT[1][1];
+    p[9] = RT[1][2] + RT[2][1];
+    p[10] = RT[2][2];
+  }
+}
+
 }  // namespace cdft

@@ -94,6 +94,15 @@ int cdft_get_chem_potential(const cdft_ctx* ctx, double* mu);
  * Returns CDFT_ERR_ETA where the reference throws Eta_Too_Large_Exception. */
 int cdft_eval(cdft_ctx* ctx, int only_fex, double* terms, double* dF, int on_device);
 
+/* DFT::matrix_dot_v1 with the full Hessian (src/Dynamical_Matrix.cpp;
+ * DFT::matrix_dot_v_intern, src/DFT.cpp:435-488): out = H v with H the second
+ * derivative of Omega in the reference's scaling (ideal gas dV v/rho,
+ * FMT::add_second_derivative src/FMT.cpp:437-567, the mean-field convolution
+ * src/Interaction.cpp:119-147), taken at the context's current density (the
+ * reference uses the fundamental measures of the last evaluation: call
+ * cdft_eval first for the same state). v and out hold N values. */
+int cdft_hessian_dot_v(cdft_ctx* ctx, const double* v, double* out, int on_device);
+
 /* Times each pass of one evaluation in the current precision with CUDA events
  * on the context's stream (no reference counterpart; used by the benchmark's
  * roofline). reps evaluations are timed; ms receives the mean time per pass
@@ -149,6 +158,7 @@ typedef struct cdft_fire_report {
   int backtracks;    /* eta > 1 backtracks seen by this call */
   int stop;          /* 0 max steps, 1 force limit, 2 residual target */
   long steps_fp32;   /* steps of this call taken in the FP32 bulk phase (cdft_fire_run_device, mixed) */
+  long newton, cg_iters; /* Newton-Krylov refinement of cdft_fire_run_device (mixed = 2): corrections, CG iterations */
 } cdft_fire_report;
 
 int cdft_fire_default_params(cdft_fire_params* p);
@@ -171,7 +181,9 @@ int cdft_fire_run_to_residual(cdft_ctx* ctx, double resid_tol, long max_steps, c
  * mixed = 0: FP64 throughout. mixed = 1: an FP32 bulk phase (vectors and
  * evaluations in FP32) until its residual drops below switch_tol or goes 96
  * steps without a 2% improvement (its noise floor), then one FP64 evaluation
- * at the same state and FP64 refinement. */
+ * at the same state and FP64 refinement. mixed = 2: the same FP32 bulk phase,
+ * then Newton-Krylov refinement (cdft_newton_refine: FP32 Hessian products,
+ * FP64 residuals), falling back to FP64 FIRE2 steps if it stalls. */
 int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, long max_steps, int mixed, cdft_fire_report* rep);
 
 /* cdft_fire_run_device on n independent contexts at once (state points of a
@@ -199,6 +211,24 @@ int cdft_get_radices(const cdft_ctx* ctx, int* radices_out);
 /* The orderings the autotuner tries for a transform length n (host only, no
  * GPU): count receives the number of plans; out (max_plans x 8 ints) the first ones. */
 int cdft_radix_candidates(int n, int* out, int max_plans, int* count);
+
+/* Newton-Krylov refinement of a minimum (no counterpart in the reference):
+ * Newton corrections H d = -dF solved by preconditioned conjugate gradients
+ * (at most max_cg iterations, to a relative residual cg_rtol) with FP32
+ * Hessian-vector products, each step accepted only when the FP64 residual
+ * max|dOmega/drho| decreases (halving the step up to 6 times). Fixed mass is
+ * kept exactly (corrections sum to zero). Stops at resid_tol or after
+ * max_newton corrections. The FIRE2 state, if any, is re-derived from the
+ * refined density. */
+typedef struct cdft_newton_report {
+  long newton;    /* Newton corrections taken */
+  long cg_iters;  /* conjugate-gradient iterations (FP32 Hessian products) */
+  long evals;     /* FP64 evaluations */
+  double F;       /* Omega at the final state */
+  double resid;   /* max|dOmega/drho| there (FP64) */
+  int stop;       /* 2 residual reached, 3 no decrease along a correction, 0 max_newton */
+} cdft_newton_report;
+int cdft_newton_refine(cdft_ctx* ctx, double resid_tol, int max_newton, int max_cg, double cg_rtol, cdft_newton_report* rep);
 
 /* DDFT integrating-factor dynamics, single species, periodic (include/Minimizer.h:189-266, src/DDFT.cpp:42-351). */
 typedef struct cdft_ddft_report {

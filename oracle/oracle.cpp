@@ -449,6 +449,121 @@ struct Model {
     if (!tensor()) return 0.0;
     return (esA() / (8 * M_PI)) * (m.v2[j] * m.v2[k] - m.TT[k][j]) + (esB() / (4 * M_PI)) * (-m.s2 * m.T[k][j] + m.TT[k][j]);
   }
+  // Second derivatives of f1, f2, f3 (include/FMT.h: Rosenfeld :163-199, RSLT :284-289,
+  // WhiteBearI :530-556, WhiteBearII :604-632).
+  void fpp(double e, double& f1pp, double& f2pp, double& f3pp) const {
+    f1pp = -1.0 / (1.0 - 2 * e + e * e);
+    const double g = 1.0 / (1.0 - e);
+    f2pp = 2 * g * g * g;
+    f3pp = 6 * g * g * g * g;
+    const double L = std::log(1 - e);
+    if (kind == ORC_RSLT) {
+      if (e < 1e-12) f3pp = 7.5 + 28.8 * e;
+      else f3pp = -(1.0 / (e * e * e)) * (1.0 / ((1.0 - e) * (1.0 - e) * (1.0 - e) * (1 - e))) * (5 * e * e * e - 26 * e * e + 21 * e - 6) +
+                  (6.0 / (e * e * e * e)) * L;
+    } else if (kind == ORC_WHITEBEAR_I) {
+      if (e < 1e-12) f3pp = 7.5 + 28.8 * e;
+      else f3pp = ((6 - 21 * e + 26 * e * e - 5 * e * e * e) / (e * e * e * (1 - e) * (1 - e) * (1 - e) * (1 - e))) + (6 * L) / (e * e * e * e);
+    } else if (kind == ORC_WHITEBEAR_II) {
+      if (e < 1e-12) f2pp = (20.0 / 9) + 7 * e;
+      else f2pp = (2 * (7 * e * e - 5 * e + 2) / (3 * e * e * (1 - e) * (1 - e) * (1 - e))) + (4.0 / (3.0 * e * e * e)) * L;
+      if (e < 1e-12) f3pp = 7.5 + 25.2 * e;
+      else f3pp = (-(6 - 21 * e + 26 * e * e - 19 * e * e * e + 2 * e * e * e * e) / (e * e * e * (1 - e) * (1 - e) * (1 - e) * (1 - e))) -
+                  (6.0 / (e * e * e * e)) * L;
+    }
+  }
+  // Second derivatives of Phi3 (Rosenfeld include/FMT.h:218-231, RSLT :313-345, esFMT :417-480).
+  double d2_S2S2(const FM& m) const {
+    if (kind == ORC_ROSENFELD) return (1.0 / (24 * M_PI)) * (6 * m.s2);
+    if (kind == ORC_RSLT) {
+      if (m.s2 < 1e-20) return 0.0;
+      const double psi = m.v2_v2 / (m.s2 * m.s2);
+      return (1.0 / (6 * M_PI)) * m.s2 * (1 - psi) * (1 + psi + 2 * psi * psi);
+    }
+    return (esA() / (24 * M_PI)) * (6 * m.s2) + (esB() / (24 * M_PI)) * (6 * m.s2);
+  }
+  double d2_V2S2(int i, const FM& m) const {
+    if (kind == ORC_RSLT) {
+      if (m.s2 < 1e-20) return 0.0;
+      const double psi = m.v2_v2 / (m.s2 * m.s2);
+      return (1.0 / (36 * M_PI)) * (-6 * m.v2[i]) * (1 - psi) * (1 + 3 * psi);
+    }
+    return (esA() / (24 * M_PI)) * (-6 * m.v2[i]);  // Rosenfeld: A = 1
+  }
+  double d2_V2V2(int i, int j, const FM& m) const {
+    if (kind == ORC_ROSENFELD) return i == j ? (1.0 / (24 * M_PI)) * (-6 * m.s2) : 0.0;
+    if (kind == ORC_RSLT) {
+      if (m.s2 < 1e-20) return 0.0;
+      const double psi = m.v2_v2 / (m.s2 * m.s2);
+      if (i == j) return (1.0 / (36 * M_PI)) * (-6 * m.s2) * (1 - psi) * (1 - psi - 4 * m.v2[i] * m.v2[i] / (m.s2 * m.s2));
+      return (1.0 / (36 * M_PI)) * (24 / m.s2) * m.v2[i] * m.v2[j] * (1 - psi);
+    }
+    return (esA() / (24 * M_PI)) * (3 * m.T[i][j] + 3 * m.T[j][i] - 6 * (i == j ? m.s2 : 0.0));
+  }
+  double d2_S2T(int j, int k, const FM& m) const { return tensor() ? (esB() / (4 * M_PI)) * (-m.T[k][j]) : 0.0; }
+  double d2_V2T(int i, int j, int k, const FM& m) const {
+    if (!tensor()) return 0.0;
+    double val = 0;
+    if (i == j) val += esA() * m.v2[k];
+    if (i == k) val += esA() * m.v2[j];
+    return val / (8 * M_PI);
+  }
+  double d2_TT(int j, int k, int l, int mm, const FM& m) const {
+    if (!tensor()) return 0.0;
+    const double A = esA(), B = esB();
+    double val = 0;
+    if (l == k) val += -A * m.T[mm][j] + 2 * B * m.T[mm][j];
+    if (mm == j) val += -A * m.T[k][l] + 2 * B * m.T[k][l];
+    if (l == k && mm == j) val += -2 * B * m.s2;
+    return val / (8 * M_PI);
+  }
+  // FMT::calculate_d2Phi_dot_V (src/FMT.cpp:181-280): r = (d2Phi/dn dn) . v, 19 slots.
+  void d2phi_dot(const FM& n, const FM& v, FM& r) const {
+    double f1, f2, f3, f1p, f2p, f3p, f1pp, f2pp, f3pp;
+    f(n.eta, f1, f2, f3, f1p, f2p, f3p);
+    fpp(n.eta, f1pp, f2pp, f3pp);
+    const double s0 = n.s0, s1 = n.s1, s2 = n.s2;
+    std::memset(&r, 0, sizeof(FM));
+    const double ip = 1 / M_PI, i2p = 1 / (2 * M_PI);
+    r.eta += (-ip * s0 * f1pp + i2p * (s1 * s2 - n.v1_v2) * f2pp + Phi3(n) * f3pp) * v.eta;
+    r.eta += -ip * f1p * v.s0;
+    r.s0 += -ip * f1p * v.eta;
+    r.eta += i2p * s2 * f2p * v.s1;
+    r.s1 += i2p * s2 * f2p * v.eta;
+    const double es2 = i2p * s1 * f2p + dPhi3_dS2(n) * f3p;
+    r.eta += es2 * v.s2;
+    r.s2 += es2 * v.eta;
+    for (int i = 0; i < 3; i++) {
+      r.eta += -i2p * n.v2[i] * f2p * v.v1[i];
+      r.v1[i] += -i2p * n.v2[i] * f2p * v.eta;
+    }
+    for (int i = 0; i < 3; i++) {
+      const double ev2 = -i2p * n.v1[i] * f2p + dPhi3_dV2(i, n) * f3p;
+      r.eta += ev2 * v.v2[i];
+      r.v2[i] += ev2 * v.eta;
+    }
+    r.s1 += i2p * f2 * v.s2;
+    r.s2 += i2p * f2 * v.s1;
+    r.s2 += d2_S2S2(n) * f3 * v.s2;
+    for (int i = 0; i < 3; i++) {
+      r.s2 += d2_V2S2(i, n) * f3 * v.v2[i];
+      r.v2[i] += d2_V2S2(i, n) * f3 * v.s2;
+      r.v1[i] += -i2p * f2 * v.v2[i];
+      r.v2[i] += -i2p * f2 * v.v1[i];
+      for (int j = 0; j < 3; j++) {
+        r.v2[i] += d2_V2V2(i, j, n) * f3 * v.v2[j];
+        r.eta += dPhi3_dT(i, j, n) * f3p * v.T[i][j];
+        r.T[i][j] += dPhi3_dT(i, j, n) * f3p * v.eta;
+        r.s2 += d2_S2T(i, j, n) * f3 * v.T[i][j];
+        r.T[i][j] += d2_S2T(i, j, n) * f3 * v.s2;
+        for (int k = 0; k < 3; k++) {
+          r.v2[i] += d2_V2T(i, j, k, n) * f3 * v.T[j][k];
+          r.T[j][k] += d2_V2T(i, j, k, n) * f3 * v.v2[i];
+          for (int l = 0; l < 3; l++) r.T[i][j] += d2_TT(i, j, k, l, n) * f3 * v.T[k][l];
+        }
+      }
+    }
+  }
   // FMT::calculate_Phi and calculate_dPhi_wrt_fundamental_measures (src/FMT.cpp:114-176)
   double phi(const FM& m, FM* d) const {
     double f1, f2, f3, f1p, f2p, f3p;
@@ -639,6 +754,83 @@ int eval(Ctx& c, double* rho, double* dF, double* terms) {
   return status;
 }
 
+// DFT::matrix_dot_v_intern (src/DFT.cpp:435-488) with the full Hessian: the
+// ideal-gas term dV v/rho, FMT::add_second_derivative (src/FMT.cpp:437-567) and
+// Interaction_Base::add_second_derivative (src/Interaction.cpp:119-147), at the
+// density rho (the state of the last evaluation in the reference).
+void hessian_dot_v(const Ctx& c, const double* rho, const double* v, double* out) {
+  const long N = c.N;
+  const double dV = c.dV;
+  for (long i = 0; i < N; ++i) out[i] = dV * v[i] / rho[i];
+  std::vector<cd> rhok, vk;
+  r2c(c, rho, rhok);
+  r2c(c, v, vk);
+  if (c.model.kind != ORC_NONE) {
+    const double h = c.hsd;
+    static const int TI[3][3] = {{5, 6, 7}, {6, 8, 9}, {7, 9, 10}};
+    // weighted densities of rho and convolutions of v with every weight
+    std::vector<std::vector<double>> n(11, std::vector<double>(N)), cv(11, std::vector<double>(N));
+    std::vector<cd> tmp(c.Nc);
+    for (int a = 0; a < 11; ++a) {
+      for (long k = 0; k < c.Nc; ++k) tmp[k] = rhok[k] * c.wk[a][k];
+      c2r(c, tmp, n[a].data());
+      for (long k = 0; k < c.Nc; ++k) tmp[k] = vk[k] * c.wk[a][k];
+      c2r(c, tmp, cv[a].data());
+    }
+    // Lambda_a(K) = sum_b d2Phi/dn_a dn_b Psi_b(K), 19 slots
+    std::vector<std::vector<double>> lam(19, std::vector<double>(N));
+    const bool T = c.model.tensor();
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < N; ++i) {
+      FM fm, ps, r;
+      std::memset(&fm, 0, sizeof(FM));
+      std::memset(&ps, 0, sizeof(FM));
+      const double S = n[1][i];
+      fm.eta = n[0][i]; fm.s0 = S / (h * h); fm.s1 = S / h; fm.s2 = S;
+      ps.eta = cv[0][i]; ps.s0 = cv[1][i] / (h * h); ps.s1 = cv[1][i] / h; ps.s2 = cv[1][i];
+      for (int j = 0; j < 3; j++) {
+        fm.v1[j] = n[2 + j][i] / h; fm.v2[j] = n[2 + j][i];
+        ps.v1[j] = cv[2 + j][i] / h; ps.v2[j] = cv[2 + j][i];
+        for (int k = 0; k < 3; k++) {
+          fm.T[j][k] = T ? n[TI[j][k]][i] : 0.0;
+          ps.T[j][k] = cv[TI[j][k]][i];
+        }
+      }
+      fm.derived();
+      c.model.d2phi_dot(fm, ps, r);
+      double r19[19];
+      r.to19(r19);
+      for (int a = 0; a < 19; ++a) lam[a][i] = r19[a];
+    }
+    // sum_a conv(Lambda_a, w_a) with conjugated weights, scaled as the reference does
+    std::vector<cd> acc(c.Nc, cd(0, 0)), t;
+    auto add_conv = [&](int slot, int w, double scale) {
+      r2c(c, lam[slot].data(), t);
+      for (long k = 0; k < c.Nc; ++k) acc[k] += scale * t[k] * std::conj(c.wk[w][k]);
+    };
+    add_conv(0, 0, 1.0);
+    add_conv(1, 1, 1.0 / (h * h));
+    add_conv(2, 1, 1.0 / h);
+    add_conv(3, 1, 1.0);
+    for (int j = 0; j < 3; j++) {
+      add_conv(4 + j, 2 + j, 1.0 / h);
+      add_conv(7 + j, 2 + j, 1.0);
+    }
+    for (int j = 0; j < 3; j++)
+      for (int k = 0; k < 3; k++) add_conv(10 + 3 * j + k, TI[j][k], 1.0);
+    std::vector<double> o(N);
+    c2r(c, acc, o.data());
+    for (long i = 0; i < N; ++i) out[i] += o[i] * dV;
+  }
+  if (c.lj) {
+    std::vector<cd> t(c.Nc);
+    for (long k = 0; k < c.Nc; ++k) t[k] = vk[k] * c.wattk[k];
+    std::vector<double> o(N);
+    c2r(c, t, o.data());
+    for (long i = 0; i < N; ++i) out[i] += o[i] * (dV / N);
+  }
+}
+
 // Alias maps for FMT_Species (src/FMT_Species.cpp:29-93); SMALL_VALUE = 1e-18 (include/Density.h:24).
 struct Alias {
   double dmin, c;
@@ -705,6 +897,8 @@ void orc_w_att(const orc_ctx* c, double* out) {
   if (c->lj) std::memcpy(out, c->watt.data(), sizeof(double) * c->N);
 }
 int orc_eval(orc_ctx* c, double* rho, double* dF, double* terms) { return eval(*c, rho, dF, terms); }
+
+void orc_hessian_dot_v(const orc_ctx* c, const double* rho, const double* v, double* out) { hessian_dot_v(*c, rho, v, out); }
 
 // DFT::mu_times_beta (src/DFT.cpp:58-71), Interaction_Base::Mu (src/Interaction.cpp:61-72)
 double orc_mu_times_beta(const orc_ctx* c, double rho) {

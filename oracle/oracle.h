@@ -63,6 +63,10 @@ int orc_fire(orc_ctx* c, double* rho, int nsteps, double dt0, double dt_max, dou
 int orc_ddft(orc_ctx* c, double* rho, int nsteps, double dt, double dt_max,
              double* rec_F, double* rec_t, double* rec_dt, double* rec_mass, double* rec_rhs);
 
+/* DFT::matrix_dot_v_intern with the full Hessian (src/DFT.cpp:435-488): out =
+   (d2Omega/drho drho) . v in the reference's scaling, at the density rho. */
+void orc_hessian_dot_v(const orc_ctx* c, const double* rho, const double* v, double* out);
+
 /* FFT helpers exposed for tests: unnormalised r2c / c2r of an nx*ny*nz grid
    (complex stored interleaved, nx*ny*(nz/2+1) values). */
 void orc_r2c(int nx, int ny, int nz, const double* in, double* out_c);

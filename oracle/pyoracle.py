@@ -58,6 +58,7 @@ def lib():
         L.orc_r2c.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.orc_c2r.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.orc_fill_noise.argtypes = [dp, ctypes.c_long, d, d, ctypes.c_uint64]
+        L.orc_hessian_dot_v.argtypes = [ctypes.c_void_p, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -151,6 +152,14 @@ class Oracle:
         st = lib().orc_eval(self._c, _p(r), _p(dF), _p(t))
         terms = dict(zip(["Omega", "F_id", "F_hs", "F_mf", "F_ext", "mu"], t))
         return st, terms, dF, r
+
+    def hessian_dot_v(self, rho, v):
+        """Full Hessian (ideal + FMT + mean field) times v at density rho (DFT::matrix_dot_v1)."""
+        r = np.ascontiguousarray(rho, dtype=np.float64).reshape(self.shape)
+        vv = np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape)
+        out = np.zeros(self.shape)
+        lib().orc_hessian_dot_v(self._c, _p(r), _p(vv), _p(out))
+        return out
 
     def mu_times_beta(self, rho):
         return lib().orc_mu_times_beta(self._c, rho)

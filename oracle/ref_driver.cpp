@@ -314,6 +314,34 @@ int main(int argc, char** argv) {
         S.s->setChemPotential(S.dft->mu_times_beta(0.6));
         record_eval(std::string("m16.") + m, S, true, {});
       }
+    } else if (c == "hessian") {
+      // DFT::matrix_dot_v1 (src/Dynamical_Matrix.cpp; DFT::matrix_dot_v_intern,
+      // src/DFT.cpp:435-488): the full Hessian (ideal gas + FMT + mean field)
+      // times a seeded vector, at the state of the preceding F+dF evaluation.
+      const char* models[] = {"Rosenfeld", "RSLT", "esFMT", "esFMT_A1_Bm1", "WhiteBearI", "WhiteBearII"};
+      for (const char* m : models) {
+        System S = make_system(0.2, 16, m, false, 1.0);
+        fill_noise(*S.d, 0.6, 0.2, 11);
+        S.s->setChemPotential(S.dft->mu_times_beta(0.6));
+        S.dft->calculateFreeEnergyAndDerivatives(false);
+        const long N = S.d->Ntot();
+        DFT_Vec v(N), r(N);
+        SplitMix64 g(77);
+        for (long i = 0; i < N; ++i) v.set(i, 0.3 * (2.0 * g.uniform() - 1.0));
+        S.dft->matrix_dot_v1(v, r, nullptr);
+        put(std::string("h16.") + m + ".Hv", vec_of(r));
+      }
+      System S = make_system(0.1, 16, "WhiteBearI", true, 0.8);
+      fill_noise(*S.d, 0.3, 0.1, 5);
+      S.s->setChemPotential(S.dft->mu_times_beta(0.3));
+      S.dft->calculateFreeEnergyAndDerivatives(false);
+      const long N = S.d->Ntot();
+      DFT_Vec v(N), r(N);
+      SplitMix64 g(77);
+      for (long i = 0; i < N; ++i) v.set(i, 0.3 * (2.0 * g.uniform() - 1.0));
+      S.dft->matrix_dot_v1(v, r, nullptr);
+      put("hlj16.Hv", vec_of(r));
+      put1("hlj16.hsd", S.hsd);
     } else if (c == "eval_hs32") {
       System S = make_system(0.2, 32, "WhiteBearI", false, 1.0);
       fill_noise(*S.d, 0.7, 0.05, 20240601);

@@ -20,7 +20,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 CASES = ["weights", "phi", "bulk", "eval_models16", "eval_hs32", "eval_lj", "fire_hs32", "fire_lj24",
-         "ddft_lj16", "ddft_adapt16", "coex"]
+         "ddft_lj16", "ddft_adapt16", "coex", "hessian"]
 
 
 def read_driver_output(path):

@@ -166,3 +166,48 @@ def test_fft_roundtrip_and_numpy(oracle):
         A = oracle.r2c(a)
         np.testing.assert_allclose(A, np.fft.rfftn(a), rtol=0, atol=1e-12)
         np.testing.assert_allclose(oracle.c2r(A, shape[2]) / a.size, a, rtol=0, atol=1e-13)
+
+
+def _hess_v(oracle, shape):
+    # the reference driver's v_i = 0.3 (2u - 1) from splitmix64(77)
+    return 0.3 * (oracle.fill_noise(shape, 1.0, 1.0, 77) - 1.0)
+
+
+@pytest.mark.parametrize("model,name,A,B", [("Rosenfeld", "Rosenfeld", 1, 0), ("RSLT", "RSLT", 1, 0), ("esFMT", "esFMT", 1, 0),
+                                            ("esFMT_A1_Bm1", "esFMT", 1, -1), ("WhiteBearI", "WhiteBearI", 1, 0),
+                                            ("WhiteBearII", "WhiteBearII", 1, 0)])
+def test_hessian_dot_v_models(oracle, model, name, A, B):
+    """Full Hessian times v (DFT::matrix_dot_v1) of every FMT model against the reference."""
+    g = golden("hessian")
+    shape = (16, 16, 16)
+    o = oracle.Oracle(16, 0.2, name, hsd=1.0, es_A=A, es_B=B)
+    rho = oracle.fill_noise(shape, 0.6, 0.2, 11)
+    h = o.hessian_dot_v(rho, _hess_v(oracle, shape))
+    ref = g["h16.%s.Hv" % model].reshape(shape)
+    assert np.max(np.abs(h - ref)) <= 1e-15 * max(1.0, np.max(np.abs(ref))) + 1e-16
+
+
+def test_hessian_dot_v_lj(oracle):
+    g = golden("hessian")
+    shape = (16, 16, 16)
+    hsd = float(g["hlj16.hsd"][0])
+    o = oracle.Oracle(16, 0.1, "WhiteBearI", hsd=hsd, lj=True, kT=0.8)
+    rho = oracle.fill_noise(shape, 0.3, 0.1, 5)
+    h = o.hessian_dot_v(rho, _hess_v(oracle, shape))
+    ref = g["hlj16.Hv"].reshape(shape)
+    assert np.max(np.abs(h - ref)) <= 1e-15
+
+
+def test_hessian_is_the_derivative_of_dF(oracle):
+    """Central difference of dF along v equals H.v (second-order accurate)."""
+    shape = (12, 12, 12)
+    o = oracle.Oracle(12, 0.2, "WhiteBearI", hsd=1.0)
+    o.set_mu(0.0)
+    rho = oracle.fill_noise(shape, 0.5, 0.2, 3)
+    v = _hess_v(oracle, shape) * rho
+    hv = o.hessian_dot_v(rho, v)
+    eps = 1e-5
+    dp = o.eval(rho + eps * v)[2]
+    dm = o.eval(rho - eps * v)[2]
+    fd = (dp - dm) / (2 * eps)
+    assert np.max(np.abs(fd - hv)) <= 1e-8 * np.max(np.abs(hv))
