@@ -171,32 +171,40 @@ def ddft_leg(cd, n=256, steps=3):
 
 
 def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
-    """Wall seconds for FIRE2 (reference defaults dt = 1e-3, dt_max = 1e-2) to
-    reach max|dOmega/drho| <= tol on the droplet at fixed mass, graph-captured
-    on the device: plain FP64 evaluations vs the mixed policy (FP32 bulk phase,
-    then FP64 refinement). Both start from the tanh profile."""
+    """Wall seconds to reach max|dOmega/drho| <= tol on the droplet at fixed mass,
+    every leg device-resident and starting from the same tanh profile, FIRE2 with
+    the reference defaults (dt = 1e-3, dt_max = 1e-2):
+      plain_fp64    FIRE2 with FP64 evaluations throughout;
+      mixed_fire    FP32 FIRE2 bulk phase to its noise floor, then FP64 FIRE2;
+      mixed_newton  FP32 FIRE2 bulk phase to resid 1e-4, then Newton-Krylov
+                    refinement (FP32 Hessian products, FP64 residuals).
+    Each end state is re-evaluated in FP64."""
     import torch
     hsd = cd.bh_diameter(1.0, 1.0, 3.0, KT)
     mass = float(rho.sum()) * DX ** 3
     out = {"start": "tanh droplet (no learned warm start)", "ensemble": "fixed mass", "tol": tol,
-           "switch": "FP32 phase until resid <= 2e-6 or 96 steps without a 2% improvement"}
+           "mixed_fire": "FP32 FIRE2 until resid <= 2e-6 or 96 steps without a 2% improvement, then FP64 FIRE2",
+           "mixed_newton": "FP32 FIRE2 until resid <= 1e-4, then Newton-Krylov (CG to 1e-3, FP32 Hessian products)"}
     res = {}
-    for name, mixed in (("mixed", True), ("plain_fp64", False)):
+    for name, mixed, sw in (("mixed_newton", 2, 1e-4), ("mixed_fire", 1, 2e-6), ("plain_fp64", 0, 2e-6)):
         c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT, fixed_mass=mass)
         c.set_density(rho)
         c.fire_init(force_limit=0.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = c.fire_run_device(tol, max_steps=max_steps, mixed=mixed, switch_tol=2e-6)
+        r = c.fire_run_device(tol, max_steps=max_steps, mixed=mixed, switch_tol=sw)
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         t, _ = c.eval(want_dF=False)  # FP64 re-evaluation of the end state
-        res[name] = {"seconds": el, "steps": r["total_steps"], "fp32_steps": r["steps_fp32"], "resid": t["resid"],
+        res[name] = {"seconds": el, "fire_steps": r["total_steps"], "fp32_steps": r["steps_fp32"],
+                     "newton": r["newton"], "cg_iters": r["cg_iters"], "resid": t["resid"],
                      "Omega": t["Omega"], "converged": bool(t["resid"] <= tol)}
         c.close()
     out.update(res)
-    out["speedup_mixed_vs_plain"] = res["plain_fp64"]["seconds"] / res["mixed"]["seconds"]
-    out["omega_rel_diff"] = abs(res["mixed"]["Omega"] - res["plain_fp64"]["Omega"]) / abs(res["plain_fp64"]["Omega"])
+    plain = res["plain_fp64"]
+    out["speedup_mixed_vs_plain"] = plain["seconds"] / res["mixed_newton"]["seconds"]
+    out["speedup_mixed_fire_vs_plain"] = plain["seconds"] / res["mixed_fire"]["seconds"]
+    out["omega_rel_diff"] = max(abs(res[k]["Omega"] - plain["Omega"]) / abs(plain["Omega"]) for k in ("mixed_newton", "mixed_fire"))
     return out
 
 
@@ -210,11 +218,12 @@ def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80,
     from classicaldft_gb300 import statepoints as sp
     pts = sp.sample_state_points(n, seed=seed, grids=grids)
     out = {"points": n, "seed": seed, "tol": tol, "grids": sorted(p["n"] for p in pts),
-           "ensemble": "fixed mass droplets", "precision": "mixed (FP32 bulk, FP64 refinement)"}
+           "ensemble": "fixed mass droplets",
+           "precision": "FP32 FIRE2 to resid 1e-4, then Newton-Krylov (FP32 Hessian products, FP64 residuals)"}
     ctxs = sp.build_contexts([dict(p) for p in pts])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    reps, status = cd.fire_run_batch(ctxs, tol, max_steps=max_steps, mixed=True)
+    reps, status = cd.fire_run_batch(ctxs, tol, max_steps=max_steps, mixed=2, switch_tol=1e-4)
     torch.cuda.synchronize()
     tb = time.perf_counter() - t0
     out["batched_s"] = tb
@@ -226,7 +235,7 @@ def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80,
     ctxs = sp.build_contexts([dict(p) for p in pts])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    seq = [c.fire_run_device(tol, max_steps=max_steps, mixed=True, switch_tol=2e-6) for c in ctxs]
+    seq = [c.fire_run_device(tol, max_steps=max_steps, mixed=2, switch_tol=1e-4) for c in ctxs]
     torch.cuda.synchronize()
     ts = time.perf_counter() - t0
     for c in ctxs:
@@ -235,6 +244,8 @@ def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80,
     out["speedup_batched_vs_sequential"] = ts / tb
     out["state_points_per_s"] = n / tb
     out["same_minima"] = bool(all(a == r["F"] for a, r in zip(omega_b, seq)))
+    out["newton_corrections"] = int(sum(r["newton"] for r in reps))
+    out["cg_iters"] = int(sum(r["cg_iters"] for r in reps))
     return out
 
 

@@ -365,7 +365,8 @@ def radix_candidates(n):
 
 
 def fire_run_batch(contexts, tol, max_steps=-1, mixed=True, switch_tol=2e-6):
-    """Device FIRE2 on many contexts at once (cdft_fire_run_batch).
+    """Device FIRE2 on many contexts at once (cdft_fire_run_batch); mixed as in
+    Context.fire_run_device (0 FP64, 1 FP32 then FP64 FIRE2, 2 FP32 then Newton-Krylov).
 
     Returns (reports, statuses): one report dict and one status code per context."""
     n = len(contexts)

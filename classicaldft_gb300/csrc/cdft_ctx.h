@@ -78,6 +78,7 @@ int cdft_internal_eval(cdft_ctx* c, double* terms8, int only_fex);
 int cdft_internal_fire_accept(cdft_ctx* c, int s_idx);
 void cdft_internal_fire_dev_free(cdft_ctx* c);
 void cdft_internal_newton_free(cdft_ctx* c);
+int cdft_internal_newton_ensure(cdft_ctx* c);
 // FIRE2 state re-derived from the current density: x = alias(rho), v = 0, one evaluation
 int cdft_internal_fire_resync(cdft_ctx* c);
 // plans cdft_autotune chose for the context's shape, model and precision (cdft_tune.cu)

@@ -552,6 +552,9 @@ static void phase_end(cdft_ctx* c, PhaseRun* ph) {
 }
 
 constexpr int kStepsPerRead = 16;
+// Newton-Krylov refinement of the mixed = 2 policy: corrections, CG iterations per correction, CG tolerance
+constexpr int kNewtonMax = 12, kNewtonCg = 200;
+constexpr double kNewtonRtol = 1e-3;
 
 // Runs one phase to its end on one context.
 static int run_phase(cdft_ctx* c, int prec, double tol, double switch_tol, long max_steps, long* taken, int* stop) {
@@ -639,7 +642,7 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
     }
     if (mixed == 2) {  // Newton-Krylov refinement; FP64 FIRE2 only if it stalls
       cdft_newton_report nr;
-      rc = cdft_newton_refine(c, resid_tol, 12, 200, 1e-3, &nr);
+      rc = cdft_newton_refine(c, resid_tol, kNewtonMax, kNewtonCg, kNewtonRtol, &nr);
       if (rc) return rc;
       if (nr.stop == 2) {
         report_of(c, total, 2, rep, steps32);
@@ -666,13 +669,17 @@ struct BatchItem {
   cudaStream_t saved_stream = nullptr;
   PhaseRun ph;
   int stage = 0;  // 0 FP32 bulk phase, 1 FP64 phase, 2 finished
-  long total = 0, steps32 = 0;
+  long total = 0, steps32 = 0, newton = 0, cg = 0;
   int rc = CDFT_OK;
 };
 }  // namespace
 
 static void batch_finish(BatchItem& b, cdft_fire_report* rep, int stop) {
   report_of(b.c, b.total, stop, rep, b.steps32);
+  if (rep) {
+    rep->newton = b.newton;
+    rep->cg_iters = b.cg;
+  }
   b.stage = 2;
 }
 
@@ -707,6 +714,7 @@ extern "C" int cdft_fire_run_batch(cdft_ctx* const* ctx, int n, double resid_tol
     if (!rc && mixed) rc = cdft_set_precision(b.c, CDFT_FP32);
     if (!rc && mixed) rc = ensure_fp32_arrays(b.c);
     if (!rc) rc = cdft_set_precision(b.c, CDFT_FP64);
+    if (!rc && mixed == 2) rc = cdft_internal_newton_ensure(b.c);
     if (rc) return rc;
     cudaStreamSynchronize(b.c->stream);
     b.saved_stream = b.c->stream;
@@ -749,6 +757,13 @@ extern "C" int cdft_fire_run_batch(cdft_ctx* const* ctx, int n, double resid_tol
         b.steps32 = b.ph.k;
         b.rc = refresh_fp64(b.c);
         if (b.rc) { batch_finish(b, rep, 0); continue; }
+        if (mixed == 2 && b.c->resid > resid_tol) {  // Newton-Krylov refinement on this context's stream
+          cdft_newton_report nr;
+          b.rc = cdft_newton_refine(b.c, resid_tol, kNewtonMax, kNewtonCg, kNewtonRtol, &nr);
+          if (b.rc) { batch_finish(b, rep, 0); continue; }
+          b.newton = nr.newton;
+          b.cg = nr.cg_iters;
+        }
         batch_start_fp64(b, resid_tol, max_steps, rep);
       } else {
         cudaStreamSynchronize(b.c->fire_dev->stream);

@@ -68,6 +68,7 @@ class Evaluator {
   // space (allocated on first use); hess_apply then maps v -> H v at that
   // state, rho0 giving the ideal-gas term v/rho0. Asynchronous on s.
   int hess_prepare(const double* rho0, cudaStream_t s);
+  bool hess_ready() const { return M_ == 0 || NA_ != nullptr; }
   template <class RT>
   int hess_apply(const RT* v, const double* rho0, RT* out, double dV, cudaStream_t s);
   // Algorithmic bytes each of the 9 passes must move (reads + writes once).

@@ -130,6 +130,29 @@ void cdft_internal_newton_free(cdft_ctx* c) {
   c->newton = nullptr;
 }
 
+// Work arrays (and the FP32 evaluator the Hessian products use), allocated once.
+int cdft_internal_newton_ensure(cdft_ctx* c) {
+  const int prec = c->precision;
+  int rc = cdft_set_precision(c, CDFT_FP32);
+  if (!rc) rc = cdft_set_precision(c, prec);
+  if (rc) return rc;
+  if (c->newton) return CDFT_OK;
+  const long N = c->info.N;
+  const unsigned g = grid_of(N);
+  NewtonWork* W = new NewtonWork();
+  c->newton = W;
+  const size_t fb = N * sizeof(float);
+  if (cudaMalloc(&W->r, fb) != cudaSuccess || cudaMalloc(&W->z, fb) != cudaSuccess || cudaMalloc(&W->p, fb) != cudaSuccess ||
+      cudaMalloc(&W->q, fb) != cudaSuccess || cudaMalloc(&W->dl, fb) != cudaSuccess ||
+      cudaMalloc(&W->rho0, N * sizeof(double)) != cudaSuccess || cudaMalloc(&W->part, (size_t)g * 3 * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&W->hpart, (size_t)g * 3 * sizeof(double)) != cudaSuccess) {
+    cdft_internal_newton_free(c);
+    return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton work arrays");
+  }
+  if (!c->e32->hess_ready() && c->e32->hess_prepare(c->rho, c->stream)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian buffers");
+  return CDFT_OK;
+}
+
 // Sums the NV block partials of the last reduction (synchronises the stream).
 template <int NV>
 static bool sums(cdft_ctx* c, unsigned g, double* out) {
@@ -152,18 +175,8 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
   if (!rc) rc = cdft_set_precision(c, CDFT_FP64);
   if (rc) return rc;
   const unsigned g = grid_of(N);
-  if (!c->newton) {
-    NewtonWork* W = new NewtonWork();
-    c->newton = W;
-    const size_t fb = N * sizeof(float);
-    if (cudaMalloc(&W->r, fb) != cudaSuccess || cudaMalloc(&W->z, fb) != cudaSuccess || cudaMalloc(&W->p, fb) != cudaSuccess ||
-        cudaMalloc(&W->q, fb) != cudaSuccess || cudaMalloc(&W->dl, fb) != cudaSuccess ||
-        cudaMalloc(&W->rho0, N * sizeof(double)) != cudaSuccess || cudaMalloc(&W->part, (size_t)g * 3 * sizeof(double)) != cudaSuccess ||
-        cudaMallocHost(&W->hpart, (size_t)g * 3 * sizeof(double)) != cudaSuccess) {
-      cdft_internal_newton_free(c);
-      return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton work arrays");
-    }
-  }
+  rc = cdft_internal_newton_ensure(c);
+  if (rc) return rc;
   NewtonWork* W = c->newton;
   cudaStream_t s = c->stream;
   cdft_newton_report R{};
@@ -225,7 +238,8 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
       rc = cdft_internal_eval(c, t, 0);
       ++R.evals;
       if (rc && rc != CDFT_ERR_ETA) return rc;
-      if (!rc && t[6] < resid) {
+      // accept a lower FP64 residual, or (far from the minimum) a real decrease of Omega
+      if (!rc && (t[6] < resid || t[0] < R.F - 1e-13 * std::fabs(R.F))) {
         accepted = true;
         resid = t[6];
         R.F = t[0];

@@ -191,6 +191,8 @@ int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, lon
  * which solves one system per process. Each context's steps run on its own
  * stream; one host thread queues a context's next 16 steps as soon as its
  * previous ones have finished, so systems too small to fill the GPU overlap.
+ * mixed is cdft_fire_run_device's (0, 1 or 2; with 2 a context's Newton-Krylov
+ * refinement runs on its own stream while the others' steps continue).
  * Every context must have had cdft_fire_init and must appear once. reps[i] and
  * rcs[i] (either array may be NULL) receive each context's report and status;
  * the return value is the first non-zero status, or CDFT_OK. */
