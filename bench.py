@@ -177,16 +177,19 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
       plain_fp64    FIRE2 with FP64 evaluations throughout;
       mixed_fire    FP32 FIRE2 bulk phase to its noise floor, then FP64 FIRE2;
       mixed_newton  FP32 FIRE2 bulk phase to resid 1e-4, then Newton-Krylov
-                    refinement (FP32 Hessian products, FP64 residuals).
+                    refinement (FP32 Hessian products, FP64 residuals);
+      newton        Newton-Krylov from the start (FP32 Hessian products, FP64
+                    residuals and line search).
     Each end state is re-evaluated in FP64."""
     import torch
     hsd = cd.bh_diameter(1.0, 1.0, 3.0, KT)
     mass = float(rho.sum()) * DX ** 3
     out = {"start": "tanh droplet (no learned warm start)", "ensemble": "fixed mass", "tol": tol,
            "mixed_fire": "FP32 FIRE2 until resid <= 2e-6 or 96 steps without a 2% improvement, then FP64 FIRE2",
-           "mixed_newton": "FP32 FIRE2 until resid <= 1e-4, then Newton-Krylov (CG to 1e-3, FP32 Hessian products)"}
+           "mixed_newton": "FP32 FIRE2 until resid <= 1e-4, then Newton-Krylov (CG to 1e-3, FP32 Hessian products)",
+           "newton": "Newton-Krylov from the tanh profile (CG to 1e-3, FP32 Hessian products, FP64 residuals)"}
     res = {}
-    for name, mixed, sw in (("mixed_newton", 2, 1e-4), ("mixed_fire", 1, 2e-6), ("plain_fp64", 0, 2e-6)):
+    for name, mixed, sw in (("newton", 3, 1e-4), ("mixed_newton", 2, 1e-4), ("mixed_fire", 1, 2e-6), ("plain_fp64", 0, 2e-6)):
         c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT, fixed_mass=mass)
         c.set_density(rho)
         c.fire_init(force_limit=0.0)
@@ -202,28 +205,30 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
         c.close()
     out.update(res)
     plain = res["plain_fp64"]
-    out["speedup_mixed_vs_plain"] = plain["seconds"] / res["mixed_newton"]["seconds"]
+    out["speedup_mixed_vs_plain"] = plain["seconds"] / res["newton"]["seconds"]
+    out["speedup_mixed_newton_vs_plain"] = plain["seconds"] / res["mixed_newton"]["seconds"]
     out["speedup_mixed_fire_vs_plain"] = plain["seconds"] / res["mixed_fire"]["seconds"]
-    out["omega_rel_diff"] = max(abs(res[k]["Omega"] - plain["Omega"]) / abs(plain["Omega"]) for k in ("mixed_newton", "mixed_fire"))
+    out["omega_rel_diff"] = max(abs(res[k]["Omega"] - plain["Omega"]) / abs(plain["Omega"])
+                                for k in ("newton", "mixed_newton", "mixed_fire"))
     return out
 
 
 def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80, 96)):
     """State-point sweep: n LJ droplets (kT ~ U[0.7, 0.94], mu = mu_coex(kT) + U[-0.2, 0.2],
     R ~ U[2, 6] clamped to 0.4 L, cubic grids drawn from `grids`, dx = 0.1, fixed mass),
-    all minimised to max|dOmega/drho| <= tol with the mixed policy. Batched
-    (cdft_fire_run_batch, every context on its own stream) vs one after another
-    (cdft_fire_run_device); context set-up is outside both timings."""
+    all minimised to max|dOmega/drho| <= tol by Newton-Krylov (FIRE2 fallback). Batched
+    (cdft_fire_run_batch: contexts spread over host threads, each on its own stream)
+    vs one after another (cdft_fire_run_device); context set-up is outside both timings."""
     import torch
     from classicaldft_gb300 import statepoints as sp
     pts = sp.sample_state_points(n, seed=seed, grids=grids)
     out = {"points": n, "seed": seed, "tol": tol, "grids": sorted(p["n"] for p in pts),
            "ensemble": "fixed mass droplets",
-           "precision": "FP32 FIRE2 to resid 1e-4, then Newton-Krylov (FP32 Hessian products, FP64 residuals)"}
+           "precision": "Newton-Krylov from the tanh profile (FP32 Hessian products, FP64 residuals), FIRE2 fallback"}
     ctxs = sp.build_contexts([dict(p) for p in pts])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    reps, status = cd.fire_run_batch(ctxs, tol, max_steps=max_steps, mixed=2, switch_tol=1e-4)
+    reps, status = cd.fire_run_batch(ctxs, tol, max_steps=max_steps, mixed=3, switch_tol=1e-4)
     torch.cuda.synchronize()
     tb = time.perf_counter() - t0
     out["batched_s"] = tb
@@ -235,7 +240,7 @@ def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80,
     ctxs = sp.build_contexts([dict(p) for p in pts])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    seq = [c.fire_run_device(tol, max_steps=max_steps, mixed=2, switch_tol=1e-4) for c in ctxs]
+    seq = [c.fire_run_device(tol, max_steps=max_steps, mixed=3, switch_tol=1e-4) for c in ctxs]
     torch.cuda.synchronize()
     ts = time.perf_counter() - t0
     for c in ctxs:

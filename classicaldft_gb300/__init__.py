@@ -33,7 +33,7 @@ C_FUNCTIONS = [
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
     "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device", "cdft_find_coex",
     "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates", "cdft_hessian_dot_v",
-    "cdft_newton_refine",
+    "cdft_newton_refine", "cdft_tc_gemm_bf16",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -123,6 +123,7 @@ def lib():
             "cdft_autotune": ([vp, i, P(i), dp], i),
             "cdft_hessian_dot_v": ([vp, vp, vp, i], i),
             "cdft_newton_refine": ([vp, d, i, i, d, P(NewtonReport)], i),
+            "cdft_tc_gemm_bf16": ([vp, vp, vp, vp, vp, vp, ctypes.c_long, i, i, i, vp, vp], i),
             "cdft_get_radices": ([vp, P(i)], i),
             "cdft_radix_candidates": ([i, P(i), i, P(i)], i),
         }

@@ -261,14 +261,18 @@ bool Evaluator<T>::setup_tma(std::string* err) {
   smem_tconv_ = 2 * tile_x + 2 * wt + 1024;
   smem_tback_ = 3 * tile_x + 2 * wt + 1024;
   if (std::max(smem_ty_, std::max(smem_tconv_, smem_tback_)) > 220 * 1024) return false;
-  raise_smem(k_cols_y_tma<T, -1>, smem_ty_);
-  raise_smem(k_cols_y_tma<T, +1>, smem_ty_);
-  raise_smem(k_xconv_tma<T>, smem_tconv_);
-  raise_smem(k_xbackconv_tma<T>, smem_tback_);
+  raise_smem(k_cols_y_tma<T, -1, 0>, smem_ty_);
+  raise_smem(k_cols_y_tma<T, +1, 0>, smem_ty_);
+  raise_smem(k_xconv_tma<T, 0>, smem_tconv_);
+  raise_smem(k_xbackconv_tma<T, 0>, smem_tback_);
+  raise_smem(k_cols_y_tma<T, -1, 128>, smem_ty_);
+  raise_smem(k_cols_y_tma<T, +1, 128>, smem_ty_);
+  raise_smem(k_xconv_tma<T, 128>, smem_tconv_);
+  raise_smem(k_xbackconv_tma<T, 128>, smem_tback_);
   int nsm = 0, dev = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cols_y_tma<T, -1>, 256, smem_ty_);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cols_y_tma<T, -1, 0>, 256, smem_ty_);
   bps = std::max(bps, 1);
   const long ntile = (nzc_ + TC - 1) / TC;
   grid_ty1_ = (int)std::min<long>((long)nx_ * ntile, (long)nsm * bps);
@@ -292,11 +296,11 @@ bool Evaluator<T>::setup_tma(std::string* err) {
       };
       int bp;
       switch (model_) {
-        case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB>); break;
-        case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB>); break;
-        case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB>); break;
-        case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB>); break;
-        default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB>); break;
+        case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 128>, smem_tphi_); break;
+        case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_RSLT, RB, 128>, smem_tphi_); break;
+        case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_ESFMT, RB, 128>, smem_tphi_); break;
+        case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 128>, smem_tphi_); break;
+        default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 128>, smem_tphi_); break;
       }
       const long ngroup = (rows_ + RB - 1) / RB;
       grid_tphi_ = (int)std::min<long>(ngroup, (long)nsm * bp);
@@ -319,6 +323,7 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   hsd_ = hsd; esA_ = esA; esB_ = esB;
   mf_ = (w_att != nullptr);
   tx_ = tx; ty_ = ty; tz_ = tz;
+  fixed_plans();
   Dims d{nx, ny, nz, nzc_, N_, Nc_, rows_, pz_};
   const size_t cs = sizeof(C);
   CK(cudaMalloc(&A_, Nc_ * cs));
@@ -441,11 +446,11 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   double* part_fin = part_mf + 2 * (long)std::max(gcx, gtx);
   const bool any = M_ > 0 || mf_;
   auto yfwd = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) k_cols_y_tma<T, -1><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    if (tma_) (fy_ ? k_cols_y_tma<T, -1, 128> : k_cols_y_tma<T, -1, 0>)<<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
     else k_cols_fft<T, -1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   auto yinv = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) k_cols_y_tma<T, +1><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    if (tma_) (fy_ ? k_cols_y_tma<T, +1, 128> : k_cols_y_tma<T, +1, 0>)<<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
     else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   cudaMemsetAsync(status_, 0, sizeof(unsigned), s);
@@ -460,7 +465,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     mark(2);
   }
   if (M_ > 0) {
-    if (tma_) k_xconv_tma<T><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+    if (tma_) (fx_ ? k_xconv_tma<T, 128> : k_xconv_tma<T, 0>)<<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     mark(3);
     yinv(Cf_, mapYC_, M_, grid_tyM_);
@@ -472,11 +477,11 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
       constexpr int RB = PhiRows<T>::value;
       phi_blocks = grid_tphi_;
       switch (model_) {
-        case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB><<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_ROSENFELD: (fz_ ? k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 128> : k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_RSLT: (fz_ ? k_phi_rows_tma<T, MODEL_RSLT, RB, 128> : k_phi_rows_tma<T, MODEL_RSLT, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_ESFMT: (fz_ ? k_phi_rows_tma<T, MODEL_ESFMT, RB, 128> : k_phi_rows_tma<T, MODEL_ESFMT, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_WHITEBEAR_I: (fz_ ? k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 128> : k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        default: (fz_ ? k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 128> : k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
       }
     } else
     switch (model_) {
@@ -495,7 +500,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   }
   if (any) {
     if (tma_)
-      k_xbackconv_tma<T><<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan,
+      (fx_ ? k_xbackconv_tma<T, 128> : k_xbackconv_tma<T, 0>)<<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan,
                                                         twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
@@ -526,11 +531,11 @@ int Evaluator<T>::hess_prepare(const double* rho0, cudaStream_t s) {
   constexpr int TCt = TileCols<T>::value;
   const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
   k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho0, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
-  if (tma_) k_cols_y_tma<T, -1><<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_);
+  if (tma_) (fy_ ? k_cols_y_tma<T, -1, 128> : k_cols_y_tma<T, -1, 0>)<<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_);
   else k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
-  if (tma_) k_xconv_tma<T><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+  if (tma_) (fx_ ? k_xconv_tma<T, 128> : k_xconv_tma<T, 0>)<<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
   else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
-  if (tma_) k_cols_y_tma<T, +1><<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_);
+  if (tma_) (fy_ ? k_cols_y_tma<T, +1, 128> : k_cols_y_tma<T, +1, 0>)<<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_);
   else k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   for (int a = 0; a < M_; ++a)
     k_rows_c2r<T, T><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(Cf_ + (long)a * Nc_, NA_ + (long)a * N_, d, tz_->plan,
@@ -549,11 +554,11 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
   const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
   const bool any = M_ > 0 || mf_;
   auto yfwd = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) k_cols_y_tma<T, -1><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    if (tma_) (fy_ ? k_cols_y_tma<T, -1, 128> : k_cols_y_tma<T, -1, 0>)<<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
     else k_cols_fft<T, -1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   auto yinv = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) k_cols_y_tma<T, +1><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    if (tma_) (fy_ ? k_cols_y_tma<T, +1, 128> : k_cols_y_tma<T, +1, 0>)<<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
     else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   if (any) {
@@ -561,7 +566,7 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
     yfwd(A_, mapYA_, 1, grid_ty1_);
   }
   if (M_ > 0) {
-    if (tma_) k_xconv_tma<T><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+    if (tma_) (fx_ ? k_xconv_tma<T, 128> : k_xconv_tma<T, 0>)<<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     yinv(Cf_, mapYC_, M_, grid_tyM_);
     const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
@@ -578,7 +583,7 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
   double* part_mf = part_ + 2 * rows_;
   if (any) {
     if (tma_)
-      k_xbackconv_tma<T><<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_),
+      (fx_ ? k_xbackconv_tma<T, 128> : k_xbackconv_tma<T, 0>)<<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_),
                                                         mf_ ? part_mf : nullptr, status_);
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
@@ -588,6 +593,21 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
   k_hess_final_rows<T, RT><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(E_, rho0, v, out, d, tz_->plan, twp<T>(tz_), rb_rows_, dV,
                                                                                  any ? 1 : 0);
   return cudaGetLastError() == cudaSuccess ? 0 : 5;
+}
+
+template <class T>
+void Evaluator<T>::fixed_plans() {
+  auto is_default128 = [](const FFTTable* t) {
+    if (!t || t->plan.n != 128) return false;
+    const std::vector<int> d = default_radices(128);
+    if ((int)d.size() != t->plan.nst) return false;
+    for (int i = 0; i < t->plan.nst; ++i)
+      if (t->plan.radix[i] != d[i]) return false;
+    return true;
+  };
+  fx_ = is_default128(tx_);
+  fy_ = is_default128(ty_);
+  fz_ = is_default128(tz_);
 }
 
 template <class T>

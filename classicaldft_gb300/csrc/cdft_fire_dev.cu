@@ -12,6 +12,7 @@
 // FP64 for the refinement phase. The residual max|dOmega/drho| that ends a run
 // is always taken from an FP64 evaluation.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -554,6 +555,7 @@ static void phase_end(cdft_ctx* c, PhaseRun* ph) {
 constexpr int kStepsPerRead = 16;
 // Newton-Krylov refinement of the mixed = 2 policy: corrections, CG iterations per correction, CG tolerance
 constexpr int kNewtonMax = 12, kNewtonCg = 200;
+constexpr int kNewtonMax3 = 40;  // Newton from an arbitrary start (mixed = 3)
 constexpr double kNewtonRtol = 1e-3;
 
 // Runs one phase to its end on one context.
@@ -616,10 +618,25 @@ static int refresh_fp64(cdft_ctx* c) {
 extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch_tol, long max_steps, int mixed, cdft_fire_report* rep) {
   if (!c) return CDFT_ERR_ARG;
   if (!c->fire_ready) return cdft_internal_fail(c, CDFT_ERR_STATE, "cdft_fire_init has not been called");
+  if (mixed < 0 || mixed > 3) return cdft_internal_fail(c, CDFT_ERR_ARG, "mixed must be 0, 1, 2 or 3");
   int rc = ensure_engine(c);
   if (rc) return rc;
   long total = 0, taken = 0, steps32 = 0;
   int stop = 0;
+  long nk = 0, ncg = 0;
+  if (mixed == 3) {  // Newton-Krylov from the current state; the mixed = 2 path if it stalls
+    cdft_newton_report nr;
+    rc = cdft_newton_refine(c, resid_tol, kNewtonMax3, kNewtonCg, kNewtonRtol, &nr);
+    if (rc) return rc;
+    if (nr.stop == 2) {
+      report_of(c, 0, 2, rep, 0);
+      if (rep) rep->newton = nr.newton, rep->cg_iters = nr.cg_iters;
+      return CDFT_OK;
+    }
+    nk = nr.newton;
+    ncg = nr.cg_iters;
+    mixed = 2;
+  }
   if (mixed) {
     rc = cdft_set_precision(c, CDFT_FP32);
     if (rc) return rc;
@@ -644,9 +661,11 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
       cdft_newton_report nr;
       rc = cdft_newton_refine(c, resid_tol, kNewtonMax, kNewtonCg, kNewtonRtol, &nr);
       if (rc) return rc;
+      nk += nr.newton;
+      ncg += nr.cg_iters;
       if (nr.stop == 2) {
         report_of(c, total, 2, rep, steps32);
-        if (rep) rep->newton = nr.newton, rep->cg_iters = nr.cg_iters;
+        if (rep) rep->newton = nk, rep->cg_iters = ncg;
         return CDFT_OK;
       }
     }
@@ -654,6 +673,7 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
   rc = run_phase(c, CDFT_FP64, resid_tol, 0.0, max_steps > 0 ? max_steps - total : -1, &taken, &stop);
   total += taken;
   report_of(c, total, stop, rep, steps32);
+  if (rep) rep->newton = nk, rep->cg_iters = ncg;
   return rc;
 }
 
@@ -695,9 +715,55 @@ static void batch_start_fp64(BatchItem& b, double tol, long max_steps, cdft_fire
   if (phase_launch(b.c, &b.ph, kStepsPerRead) == 0) batch_finish(b, rep, 0);
 }
 
+// mixed = 3: Newton-Krylov per context is host-driven (a synchronisation per CG
+// iteration), so contexts are spread over host threads, each context on its own
+// stream, and the GPU interleaves their kernels.
+static int batch_newton(cdft_ctx* const* ctx, int n, double resid_tol, double switch_tol, long max_steps, cdft_fire_report* reps,
+                        int* rcs) {
+  std::vector<cudaStream_t> saved(n);
+  for (int i = 0; i < n; ++i) {
+    cdft_ctx* c = ctx[i];
+    int rc = ensure_engine(c);
+    if (!rc) rc = cdft_set_precision(c, CDFT_FP32);
+    if (!rc) rc = ensure_fp32_arrays(c);
+    if (!rc) rc = cdft_set_precision(c, CDFT_FP64);
+    if (!rc) rc = cdft_internal_newton_ensure(c);
+    if (rc) return rc;
+    cudaStreamSynchronize(c->stream);
+    saved[i] = c->stream;
+    c->stream = c->fire_dev->stream;
+  }
+  std::atomic<int> next(0);
+  std::vector<int> st(n, CDFT_OK);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto work = [&]() {
+    cudaSetDevice(dev);
+    for (;;) {
+      const int i = next.fetch_add(1);
+      if (i >= n) break;
+      cdft_fire_report r{};
+      st[i] = cdft_fire_run_device(ctx[i], resid_tol, switch_tol, max_steps, 3, &r);
+      if (reps) reps[i] = r;
+    }
+  };
+  const int nt = std::min(n, 8);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nt; ++t) pool.emplace_back(work);
+  for (auto& t : pool) t.join();
+  int first = CDFT_OK;
+  for (int i = 0; i < n; ++i) {
+    cudaStreamSynchronize(ctx[i]->stream);
+    ctx[i]->stream = saved[i];
+    if (rcs) rcs[i] = st[i];
+    if (st[i] && !first) first = st[i];
+  }
+  return first;
+}
+
 extern "C" int cdft_fire_run_batch(cdft_ctx* const* ctx, int n, double resid_tol, double switch_tol, long max_steps, int mixed,
                                    cdft_fire_report* reps, int* rcs) {
-  if (!ctx || n <= 0) return CDFT_ERR_ARG;
+  if (!ctx || n <= 0 || mixed < 0 || mixed > 3) return CDFT_ERR_ARG;
   std::vector<BatchItem> items(n);
   for (int i = 0; i < n; ++i) {
     if (!ctx[i]) return CDFT_ERR_ARG;
@@ -705,6 +771,7 @@ extern "C" int cdft_fire_run_batch(cdft_ctx* const* ctx, int n, double resid_tol
       if (ctx[j] == ctx[i]) return cdft_internal_fail(ctx[i], CDFT_ERR_ARG, "a context appears twice in the batch");
     if (!ctx[i]->fire_ready) return cdft_internal_fail(ctx[i], CDFT_ERR_STATE, "cdft_fire_init has not been called");
   }
+  if (mixed == 3) return batch_newton(ctx, n, resid_tol, switch_tol, max_steps, reps, rcs);
   // allocation first (nothing may allocate while a stream is captured), and
   // every context's own work on its engine's stream
   for (int i = 0; i < n; ++i) {

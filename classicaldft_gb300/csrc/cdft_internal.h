@@ -83,7 +83,10 @@ class Evaluator {
   const T* w_att() const { return watt_; }
   int M() const { return M_; }
   // swap the transform plans (same lengths, another radix ordering)
-  void set_tables(FFTTable* tx, FFTTable* ty, FFTTable* tz) { tx_ = tx; ty_ = ty; tz_ = tz; }
+  void set_tables(FFTTable* tx, FFTTable* ty, FFTTable* tz) {
+    tx_ = tx; ty_ = ty; tz_ = tz;
+    fixed_plans();
+  }
   long spectrum_len() const { return Nc_; }  // complex values per spectrum (padded rows)
   int pitch() const { return pz_; }
   bool uses_tma() const { return tma_; }
@@ -116,6 +119,9 @@ class Evaluator {
   size_t smem_ty_ = 0, smem_tconv_ = 0, smem_tback_ = 0;
   int grid_ty1_ = 0, grid_tyM_ = 0;
   bool tma_phi_ = false;
+  // the tensor-copy kernels' compile-time plans (length 128, default radix order) apply to x / y / z
+  bool fx_ = false, fy_ = false, fz_ = false;
+  void fixed_plans();
   CUtensorMap mapR_;
   size_t smem_tphi_ = 0;
   int grid_tphi_ = 0;

@@ -126,6 +126,79 @@ __device__ typename Cx<T>::type* tile_fft(typename Cx<T>::type* b0, typename Cx<
   return src;
 }
 
+// ---- fixed-length transforms: the plan of length NF (default radix order,
+// largest radix first, as make_fft_table builds it) resolved at compile time,
+// so every stride, trip count and twiddle offset is a constant.
+__host__ __device__ constexpr int fx_radix(int n, int i) {
+  int m = n;
+  for (int st = 0; m > 1; ++st) {
+    int f = 0;
+    if (m % 8 == 0 && m != 16) f = 8;
+    else if (m % 4 == 0) f = 4;
+    else if (m % 2 == 0) f = 2;
+    else {
+      for (int q = 3; q <= m; q += 2)
+        if (m % q == 0) { f = q; break; }
+    }
+    if (st == i) return f;
+    m /= f;
+  }
+  return 0;
+}
+__host__ __device__ constexpr int fx_len(int n, int i) {
+  int len = n;
+  for (int st = 0; st < i; ++st) len /= fx_radix(n, st);
+  return len;
+}
+// offset of stage i's twiddles in the table: each earlier stage holds len twiddles and p roots
+__host__ __device__ constexpr int fx_twoff(int n, int i) {
+  int off = 0, len = n;
+  for (int st = 0; st < i; ++st) {
+    const int p = fx_radix(n, st);
+    off += len + p;
+    len /= p;
+  }
+  return off;
+}
+
+template <int DIR, class T, int TC, int PITCH, int NF, int ST>
+__device__ __forceinline__ void fx_stage(const typename Cx<T>::type* __restrict__ src, typename Cx<T>::type* __restrict__ dst,
+                                         const typename Cx<T>::type* __restrict__ table) {
+  constexpr int p = fx_radix(NF, ST), len = fx_len(NF, ST), m = len / p, s = NF / len;
+  constexpr int items = TC * (NF / p);
+  const typename Cx<T>::type* tw = table + fx_twoff(NF, ST);
+  const typename Cx<T>::type* rt = tw + len;
+#pragma unroll 2
+  for (int w = threadIdx.x; w < items; w += 256) {
+    const int c = w % TC, u = w / TC;
+    const int q = u / s, k = u % s;
+    if constexpr (p == 2 || p == 4 || p == 8) tile_butterfly<DIR, T, p, PITCH>(src, dst, c, q, k, m, s, tw, rt);
+    else if constexpr (p == 3 || p == 5 || p == 7) tile_butterfly_odd<DIR, T, p, PITCH>(src, dst, c, q, k, m, s, tw, rt);
+    else tile_butterfly_generic<DIR, T, PITCH>(src, dst, c, q, k, m, s, p, tw, rt);
+  }
+}
+
+template <int DIR, class T, int TC, int PITCH, int NF, int ST = 0>
+__device__ __forceinline__ typename Cx<T>::type* tile_fft_fixed(typename Cx<T>::type* b0, typename Cx<T>::type* b1,
+                                                                const typename Cx<T>::type* __restrict__ table) {
+  __syncthreads();
+  if constexpr (fx_radix(NF, ST) == 0) {
+    return b0;
+  } else {
+    fx_stage<DIR, T, TC, PITCH, NF, ST>(b0, b1, table);
+    return tile_fft_fixed<DIR, T, TC, PITCH, NF, ST + 1>(b1, b0, table);
+  }
+}
+
+// The transform of a tile: the compile-time plan when NF > 0 (launched only
+// when the runtime plan is that default plan of length NF), else the runtime plan.
+template <int DIR, class T, int TC, int PITCH, int NF>
+__device__ __forceinline__ typename Cx<T>::type* tfft(typename Cx<T>::type* b0, typename Cx<T>::type* b1, const FFTPlan& P,
+                                                      const typename Cx<T>::type* __restrict__ table) {
+  if constexpr (NF > 0) return tile_fft_fixed<DIR, T, TC, PITCH, NF>(b0, b1, table);
+  else return tile_fft<DIR, T, TC, PITCH>(b0, b1, P, table);
+}
+
 // Tile geometry: TC complex columns make one 128-byte row.
 template <class T> struct TileCols;
 template <> struct TileCols<float> { static constexpr int value = 16; };
@@ -142,7 +215,7 @@ template <> struct ElemsPerComplex<double> { static constexpr int value = 2; };
 // ---------------------------------------------------------------- y pass ---
 // Work item = (field f, plane x, column tile t): the tile [ny][TC] at kz0 = t*TC.
 // Tensor map (4D, 8-byte elements): {pz*E, ny, nx, nfield}.
-template <class T, int DIR>
+template <class T, int DIR, int NF = 0>
 __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUtensorMap map, Dims d, FFTPlan P,
                                                     const typename Cx<T>::type* __restrict__ tw, int nfield, unsigned* __restrict__ status) {
   typedef typename Cx<T>::type C;
@@ -188,7 +261,7 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
     const int b = (int)(k & 1);
     ok = mbar_wait(&bar[b], (unsigned)((k >> 1) & 1), status);
     if (!__syncthreads_and(ok)) break;
-    C* res = tile_fft<DIR, T, TC>(stage[b], work, P, tw);
+    C* res = tfft<DIR, T, TC, TC, NF>(stage[b], work, P, tw);
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -212,7 +285,7 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
 
 // C[a] = IFFT_x(FFT_x(A) . w_a) for a < M. The density spectrum lives in
 // registers; weight tiles are double-buffered; results leave by tensor store.
-template <class T>
+template <class T, int NF = 0>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xconv_tma(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW,
                                                    const __grid_constant__ CUtensorMap mapC, int M, FFTPlan px,
                                                    const typename Cx<T>::type* __restrict__ tw, unsigned* __restrict__ status) {
@@ -248,7 +321,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xconv_tma(const
     if (threadIdx.x == 0) bulk_wait_all();
     return;
   }
-  C* res = tile_fft<-1, T, TC>(X, Y, px, tw);
+  C* res = tfft<-1, T, TC, TC, NF>(X, Y, px, tw);
   C R[PER];
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
@@ -270,7 +343,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xconv_tma(const
       mbar_arrive_expect_tx(&bar[b], (unsigned)wbytes);
       tma_load_3d(Wst[b], &mapW, col0, 0, a + 2, &bar[b]);
     }
-    C* r2 = tile_fft<+1, T, TC>(X, Y, px, tw);
+    C* r2 = tfft<+1, T, TC, TC, NF>(X, Y, px, tw);
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -286,7 +359,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xconv_tma(const
 // E = IFFT_x(sum_a FFT_x(D[a]) . w_a + FFT_x(A) . w_att); sources are
 // double-buffered (spectrum tile + weight tile per stage), the sum lives in
 // registers. With the mean field, the Parseval sum for its energy goes to part.
-template <class T>
+template <class T, int NF = 0>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(const __grid_constant__ CUtensorMap mapD, const __grid_constant__ CUtensorMap mapW,
                                                        const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapWatt,
                                                        const __grid_constant__ CUtensorMap mapE, int M, int with_mf, Dims d, FFTPlan px,
@@ -334,7 +407,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(c
     const int b = a & 1;
     ok = mbar_wait(&bar[b], (unsigned)((a >> 1) & 1), status);
     if (!__syncthreads_and(ok)) break;
-    C* res = tile_fft<-1, T, TC>(Dst[b], Y, px, tw);
+    C* res = tfft<-1, T, TC, TC, NF>(Dst[b], Y, px, tw);
     const bool is_mf = (a == M);
     const bool odd = !is_mf && weight_is_odd(a);
 #pragma unroll
@@ -373,7 +446,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(c
     const int e = threadIdx.x + j * 256;
     if (e < nel) X[e] = S[j];
   }
-  C* r2 = tile_fft<+1, T, TC>(X, Y, px, tw);
+  C* r2 = tfft<+1, T, TC, TC, NF>(X, Y, px, tw);
   fence_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -395,7 +468,7 @@ namespace cdft {
 // L = NP*RB lines, transformed column-wise (line-fastest, conflict-free):
 // c2r (z), Phi and dPhi per point, r2c (z), then the M derivative rows are
 // stored over the inputs.
-template <class T, int MODEL, int RB>
+template <class T, int MODEL, int RB, int NF = 0>
 __global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
                                                       Dims d, FFTPlan pz_plan, const typename Cx<T>::type* __restrict__ tw, T hsd, T esA,
                                                       T esB, double* __restrict__ part, unsigned* __restrict__ status) {
@@ -455,7 +528,7 @@ __global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CU
       const long gn = g + 2L * gridDim.x;
       if (gn < ngroup) issue(gn, b);
     }
-    C* res = tile_fft<+1, T, L, LPd>(Z0, Z1, pz_plan, tw);
+    C* res = tfft<+1, T, L, LPd, NF>(Z0, Z1, pz_plan, tw);
     C* oth = (res == Z0) ? Z1 : Z0;
     for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
       const int k = e % nz, r = e / nz;
@@ -474,7 +547,7 @@ __global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CU
 #pragma unroll
       for (int p = 0; p < NP; ++p) oth[k * LPd + r * NP + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
     }
-    C* res2 = tile_fft<-1, T, L, LPd>(oth, res, pz_plan, tw);
+    C* res2 = tfft<-1, T, L, LPd, NF>(oth, res, pz_plan, tw);
     for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
       const int k = e % nzc, line = e / nzc;
       const int r = line / NP, pr = line - r * NP;

@@ -183,7 +183,9 @@ int cdft_fire_run_to_residual(cdft_ctx* ctx, double resid_tol, long max_steps, c
  * steps without a 2% improvement (its noise floor), then one FP64 evaluation
  * at the same state and FP64 refinement. mixed = 2: the same FP32 bulk phase,
  * then Newton-Krylov refinement (cdft_newton_refine: FP32 Hessian products,
- * FP64 residuals), falling back to FP64 FIRE2 steps if it stalls. */
+ * FP64 residuals), falling back to FP64 FIRE2 steps if it stalls. mixed = 3:
+ * Newton-Krylov from the current state (up to 40 corrections), falling back to
+ * the mixed = 2 path if it stalls. */
 int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, long max_steps, int mixed, cdft_fire_report* rep);
 
 /* cdft_fire_run_device on n independent contexts at once (state points of a
@@ -191,8 +193,10 @@ int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, lon
  * which solves one system per process. Each context's steps run on its own
  * stream; one host thread queues a context's next 16 steps as soon as its
  * previous ones have finished, so systems too small to fill the GPU overlap.
- * mixed is cdft_fire_run_device's (0, 1 or 2; with 2 a context's Newton-Krylov
- * refinement runs on its own stream while the others' steps continue).
+ * mixed is cdft_fire_run_device's (0 to 3; with 2 a context's Newton-Krylov
+ * refinement runs on its own stream while the others' steps continue; with 3
+ * the contexts are spread over up to 8 host threads, each driving its
+ * contexts' Newton iterations on their own streams).
  * Every context must have had cdft_fire_init and must appear once. reps[i] and
  * rcs[i] (either array may be NULL) receive each context's report and status;
  * the return value is the first non-zero status, or CDFT_OK. */
@@ -231,6 +235,16 @@ typedef struct cdft_newton_report {
   int stop;       /* 2 residual reached, 3 no decrease along a correction, 0 max_newton */
 } cdft_newton_report;
 int cdft_newton_refine(cdft_ctx* ctx, double resid_tol, int max_newton, int max_cg, double cg_rtol, cdft_newton_report* rep);
+
+/* BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory) for the
+ * neural-operator warm start; no counterpart in the reference.
+ * Y = act(X . W + bias + add) with X (M x K) and W (K x N) BF16 row-major,
+ * bias (N), add (M x N), Y and the optional pre-activation Z (M x N) FP32; all
+ * device pointers, X 16-byte aligned; bias, add and Z may be NULL; act 0 none,
+ * 1 GELU. K in {16, 32, 48, 64}, N in {32, 64, 128}. A device wait that runs
+ * out sets bits in *status_dev (a device unsigned); asynchronous on stream. */
+int cdft_tc_gemm_bf16(const void* X, const void* W, const float* bias, const float* add, float* Y, float* Z, long M, int K, int N,
+                      int act, void* status_dev, void* stream);
 
 /* DDFT integrating-factor dynamics, single species, periodic (include/Minimizer.h:189-266, src/DDFT.cpp:42-351). */
 typedef struct cdft_ddft_report {

@@ -75,3 +75,35 @@ def test_batch_newton_matches_sequential(cd):
         assert b["F"] == a["F"] and b["newton"] == a["newton"] and b["cg_iters"] == a["cg_iters"]
     for c in ctxs:
         c.close()
+
+
+def test_direct_newton_policy(cd):
+    """mixed = 3: Newton-Krylov from the tanh profile lands on the FP64 FIRE2 minimum."""
+    a = _droplet_ctx(cd)
+    a.fire_run_device(1e-8, max_steps=20000, mixed=0)
+    ta, _ = a.eval(want_dF=False)
+    b = _droplet_ctx(cd)
+    rb = b.fire_run_device(1e-8, max_steps=20000, mixed=3)
+    tb, _ = b.eval(want_dF=False)
+    assert rb["stop"] == 2 and tb["resid"] <= 1e-8 and rb["newton"] >= 1
+    assert abs(tb["Omega"] - ta["Omega"]) <= 1e-10 * abs(ta["Omega"])
+    a.close()
+    b.close()
+
+
+def test_batch_direct_newton_matches_sequential(cd):
+    from classicaldft_gb300 import statepoints as sp
+    pts = sp.sample_state_points(4, seed=8, grids=(48, 64))
+    alone = []
+    for p in pts:
+        (c,) = sp.build_contexts([dict(p)])
+        alone.append(c.fire_run_device(1e-8, max_steps=20000, mixed=3))
+        c.close()
+    ctxs = sp.build_contexts([dict(p) for p in pts])
+    reps, status = cd.fire_run_batch(ctxs, 1e-8, max_steps=20000, mixed=3)
+    assert status == [0] * 4, [r.get("error") for r in reps]
+    for a, b in zip(alone, reps):
+        assert b["stop"] == 2 and b["resid"] <= 1e-8
+        assert b["F"] == a["F"] and b["newton"] == a["newton"] and b["cg_iters"] == a["cg_iters"]
+    for c in ctxs:
+        c.close()
