@@ -254,6 +254,61 @@ def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80,
     return out
 
 
+def warm_start_leg(cd, n_train=24, n_test=4, steps=300, tol=1e-8):
+    """Neural-operator warm start: converged 128^3 droplets around the benchmark
+    point (kT ~ U[0.75, 0.9], rho_v ~ U[0.005, 0.04], rho_l ~ U[0.6, 0.8],
+    R ~ U[3, 5], fixed mass) from the Newton-Krylov solver, a 4-layer FNO (width 32,
+    12 modes per axis, BF16 tcgen05 GEMMs) trained on them, then the benchmark
+    droplet solved from the operator's prediction vs from the tanh profile."""
+    import torch
+    from classicaldft_gb300 import fno
+    out = {"train": n_train, "test": n_test, "steps": steps, "width": fno.WIDTH, "modes": fno.MODES, "layers": fno.LAYERS}
+    t0 = time.perf_counter()
+    samples = fno.solve_droplets(fno.sample_droplets(n_train + n_test, seed=11), SHAPE, DX)
+    out["data_s"] = time.perf_counter() - t0
+    train, test = samples[:n_train], samples[n_train:]
+    model = fno.FNO3d()
+    log = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fno.train(model, train, SHAPE, steps=steps, log=log)
+    torch.cuda.synchronize()
+    out["train_s"] = time.perf_counter() - t0
+    out["loss"] = [round(l, 6) for _, l in log]
+    # held-out error of log rho: operator vs the seed alone
+    e_seed, e_fno = [], []
+    for seed, kT, rho in test:
+        pred = fno.predict(model, seed, kT, SHAPE)
+        up = np.exp(fno.upsample(np.log(seed), SHAPE).numpy())
+        lr = np.log(rho)
+        e_fno.append(float(np.sqrt(np.mean((np.log(pred) - lr) ** 2))))
+        e_seed.append(float(np.sqrt(np.mean((np.log(up) - lr) ** 2))))
+    out["test_rms_log_error"] = {"operator": e_fno, "seed": e_seed}
+    # the benchmark droplet, cold (tanh) vs warm (operator) start, Newton-Krylov both
+    rho0 = droplet()
+    mass = float(rho0.sum()) * DX ** 3
+    hsd = cd.bh_diameter(1.0, 1.0, 3.0, KT)
+    res = {}
+    for name in ("cold", "warm"):
+        c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT, fixed_mass=mass)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        start = rho0 if name == "cold" else fno.predict(model, fno.coarse_seed(SHAPE, DX, RHO_V, RHO_L, R_DROP), KT, SHAPE)
+        c.set_density(start)
+        c.fire_init(force_limit=0.0)
+        r = c.fire_run_device(tol, max_steps=20000, mixed=3)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        t, _ = c.eval(want_dF=False)
+        res[name] = {"seconds": el, "newton": r["newton"], "cg_iters": r["cg_iters"], "fire_steps": r["total_steps"],
+                     "resid": t["resid"], "Omega": t["Omega"]}
+        c.close()
+    out.update(res)
+    out["speedup_warm_vs_cold"] = res["cold"]["seconds"] / res["warm"]["seconds"]
+    out["omega_rel_diff"] = abs(res["warm"]["Omega"] - res["cold"]["Omega"]) / abs(res["cold"]["Omega"])
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -265,6 +320,7 @@ def main():
     ap.add_argument("--no-ddft", action="store_true", help="skip the 256^3 DDFT leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the state-point sweep leg")
     ap.add_argument("--sweep-points", type=int, default=16, help="state points in the sweep leg")
+    ap.add_argument("--no-fno", action="store_true", help="skip the neural-operator warm-start leg")
     ap.add_argument("--sweep-grids", default="48,64,80,96",
                     help="grid sizes the sweep draws from (the full range is 48,64,...,160)")
     args = ap.parse_args()
@@ -357,6 +413,8 @@ def main():
         line["fire_to_resid_1e-8"] = fire_legs(cd, rho)
     if not args.no_ddft:
         line["ddft_256"] = ddft_leg(cd)
+    if not args.no_fno:
+        line["warm_start"] = warm_start_leg(cd)
     if not args.no_batch:
         line["statepoint_sweep"] = batch_leg(cd, n=args.sweep_points,
                                              grids=tuple(int(g) for g in args.sweep_grids.split(",")))

@@ -181,9 +181,24 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
   cudaStream_t s = c->stream;
   cdft_newton_report R{};
   double t[8];
-  rc = cdft_internal_eval(c, t, 0);
-  ++R.evals;
-  if (rc) return rc;
+  // Residuals far from the solution come from FP32 evaluations (their noise,
+  // ~1e-6, is far below the residual); from kFp64Below on, and for every
+  // residual that can end the run, from FP64.
+  constexpr double kFp64Below = 1e-4;
+  bool fp64 = false;
+  auto evaluate = [&](bool use64) -> int {
+    int e = cdft_set_precision(c, use64 ? CDFT_FP64 : CDFT_FP32);
+    if (!e) e = cdft_internal_eval(c, t, 0);
+    ++R.evals;
+    return e;
+  };
+  rc = evaluate(false);
+  if (rc && rc != CDFT_ERR_ETA) return rc;
+  if (rc || t[6] <= kFp64Below) {
+    fp64 = true;
+    rc = evaluate(true);
+    if (rc) return rc;
+  }
   double resid = t[6];
   R.F = t[0];
   int stop = 0;
@@ -206,6 +221,8 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
     cudaMemcpyAsync(W->p, W->z, N * sizeof(float), cudaMemcpyDeviceToDevice, s);
     double rz = rz_rr[0];
     const double r0 = std::sqrt(rz_rr[1]);
+    // forcing term: a loose linear solve while the residual is large (inexact Newton)
+    const double eta = std::min(0.1, std::max(cg_rtol, resid));
     int it = 0;
     for (; it < max_cg; ++it) {
       if (c->e32->hess_apply<float>(W->p, c->rho, W->q, dV, s)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian product failed");
@@ -217,7 +234,7 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
       k_nk_update<<<g, kT, 0, s>>>(W->dl, W->r, W->p, W->q, N, (float)alpha, fixed ? (float)(pq[0] / N) : 0.f);
       double nz[2];
       if (!precond(nz)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");
-      if (std::sqrt(nz[1]) <= cg_rtol * r0) { ++it; break; }
+      if (std::sqrt(nz[1]) <= eta * r0) { ++it; break; }
       const double beta = nz[0] / rz;
       rz = nz[0];
       k_nk_p<<<g, kT, 0, s>>>(W->p, W->z, N, (float)beta);
@@ -235,11 +252,10 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
     bool accepted = false;
     for (int ls = 0; ls < 6 && !accepted; ++ls, step *= 0.5) {
       k_nk_step<<<g, kT, 0, s>>>(c->rho, W->rho0, W->dl, N, step);
-      rc = cdft_internal_eval(c, t, 0);
-      ++R.evals;
+      rc = evaluate(fp64);
       if (rc && rc != CDFT_ERR_ETA) return rc;
       // accept a lower FP64 residual, or (far from the minimum) a real decrease of Omega
-      if (!rc && (t[6] < resid || t[0] < R.F - 1e-13 * std::fabs(R.F))) {
+      if (!rc && (t[6] < resid || t[0] < R.F - (fp64 ? 1e-13 : 1e-6) * std::fabs(R.F))) {
         accepted = true;
         resid = t[6];
         R.F = t[0];
@@ -248,14 +264,27 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
     ++R.newton;
     if (!accepted) {  // no decrease along the correction: back to the last state
       cudaMemcpyAsync(c->rho, W->rho0, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
-      rc = cdft_internal_eval(c, t, 0);
-      ++R.evals;
+      rc = evaluate(true);
       if (rc) return rc;
+      fp64 = true;
       resid = t[6];
       R.F = t[0];
       stop = 3;
       break;
     }
+    if (!fp64 && resid <= kFp64Below) {  // close enough: FP64 residuals from here on
+      fp64 = true;
+      rc = evaluate(true);
+      if (rc) return rc;
+      resid = t[6];
+      R.F = t[0];
+    }
+  }
+  if (!fp64) {  // the run ends on an FP64 residual
+    rc = evaluate(true);
+    if (rc) return rc;
+    resid = t[6];
+    R.F = t[0];
   }
   if (resid <= tol) stop = 2;
   R.resid = resid;
