@@ -305,6 +305,28 @@ def warm_start_leg(cd, n_train=24, n_test=4, steps=300, tol=1e-8):
         c.close()
     out.update(res)
     out["speedup_warm_vs_cold"] = res["cold"]["seconds"] / res["warm"]["seconds"]
+    # the operator's pointwise layer on the tensor cores: Y = GELU(X W + b + add), 128^3 rows, K = N = 32
+    M, K, N = int(np.prod(SHAPE)), fno.WIDTH, fno.WIDTH
+    x = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+    w = (torch.randn(K, N, device="cuda") / K ** 0.5).to(torch.bfloat16)
+    b = torch.zeros(N, device="cuda")
+    add = torch.randn(M, N, device="cuda")
+    for _ in range(3):
+        fno.tc_gemm(x, w, b, add, act=1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    e0.record()
+    for _ in range(reps):
+        fno.tc_gemm(x, w, b, add, act=1)
+    e1.record()
+    e1.synchronize()
+    fno.check_status()
+    ms = e0.elapsed_time(e1) / reps
+    by = M * K * 2 + M * N * 4 * 2 + K * N * 2 + N * 4  # X in, add in, Y out
+    peaks = measured_peaks()
+    out["tc_gemm"] = {"kernel": "k_gemm_bf16<32,32> (tcgen05.mma kind::f16, TMEM accumulator)", "rows": M, "K": K, "N": N,
+                      "ms": ms, "GBs": by / (ms * 1e-3) / 1e9, "TFLOPs": 2.0 * M * K * N / (ms * 1e-3) / 1e12,
+                      "hbm_frac": by / (ms * 1e-3) / 1e9 / peaks[0], "bound": "hbm (16 flop/byte)"}
     out["omega_rel_diff"] = abs(res["warm"]["Omega"] - res["cold"]["Omega"]) / abs(res["cold"]["Omega"])
     return out
 

@@ -33,7 +33,7 @@ C_FUNCTIONS = [
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
     "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device", "cdft_find_coex",
     "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates", "cdft_hessian_dot_v",
-    "cdft_newton_refine", "cdft_tc_gemm_bf16",
+    "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -76,6 +76,11 @@ class FireReport(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("vv", ctypes.c_double), ("fmax", ctypes.c_double),
                 ("resid", ctypes.c_double), ("backtracks", ctypes.c_int), ("stop", ctypes.c_int),
                 ("steps_fp32", ctypes.c_long), ("newton", ctypes.c_long), ("cg_iters", ctypes.c_long)]
+
+
+class NewtonParams(ctypes.Structure):
+    _fields_ = [("max_newton", ctypes.c_int), ("max_cg", ctypes.c_int), ("cg_rtol", ctypes.c_double),
+                ("eta_max", ctypes.c_double), ("fp32_above", ctypes.c_double)]
 
 
 class NewtonReport(ctypes.Structure):
@@ -124,6 +129,7 @@ def lib():
             "cdft_hessian_dot_v": ([vp, vp, vp, i], i),
             "cdft_newton_refine": ([vp, d, i, i, d, P(NewtonReport)], i),
             "cdft_tc_gemm_bf16": ([vp, vp, vp, vp, vp, vp, ctypes.c_long, i, i, i, vp, vp], i),
+            "cdft_newton_refine_ex": ([vp, d, P(NewtonParams), P(NewtonReport)], i),
             "cdft_get_radices": ([vp, P(i)], i),
             "cdft_radix_candidates": ([i, P(i), i, P(i)], i),
         }
@@ -310,10 +316,11 @@ class Context:
         self._check(lib().cdft_fire_run_device(self._h, tol, switch_tol, max_steps, int(mixed), ctypes.byref(r)))
         return self._rep(r)
 
-    def newton_refine(self, tol, max_newton=12, max_cg=200, cg_rtol=1e-3):
-        """Newton-Krylov refinement with FP32 Hessian products and FP64 residuals (cdft_newton_refine)."""
+    def newton_refine(self, tol, max_newton=12, max_cg=200, cg_rtol=1e-3, eta_max=0.1, fp32_above=1e-4):
+        """Newton-Krylov refinement with FP32 Hessian products, FP32 then FP64 residuals (cdft_newton_refine_ex)."""
+        p = NewtonParams(max_newton, max_cg, cg_rtol, eta_max, fp32_above)
         r = NewtonReport()
-        self._check(lib().cdft_newton_refine(self._h, tol, max_newton, max_cg, cg_rtol, ctypes.byref(r)))
+        self._check(lib().cdft_newton_refine_ex(self._h, tol, ctypes.byref(p), ctypes.byref(r)))
         return self._rep(r)
 
     def hessian_dot_v(self, v, out=None):

@@ -53,21 +53,48 @@ __global__ void __launch_bounds__(256) k_map_reduce(long n, F f, double* __restr
   }
 }
 
-__global__ void k_finish_map_reduce(const double* __restrict__ part, int nblk, int ns, int nm, double* __restrict__ out) {
-  // deterministic single-block finish: sums in block order, maxima
-  if (threadIdx.x == 0) {
-    for (int v = 0; v < ns; ++v) {
-      Acc a;
-      a.init();
-      for (int b = 0; b < nblk; ++b) a.merge(part[(b * ns + v) * 2], part[(b * ns + v) * 2 + 1]);
-      out[v] = a.s + a.c;
+// Deterministic finish of the block partials, 256 threads: thread t merges blocks
+// t, t + 256, ... in order, then a fixed-shape tree combines the threads. (A
+// single thread merging ~1000 compensated pairs is a serial chain of FP64
+// operations, which GB300's FP64 pipe makes slow.)
+constexpr int kFinishThreads = 256;
+__global__ void __launch_bounds__(kFinishThreads) k_finish_map_reduce(const double* __restrict__ part, int nblk, int ns, int nm,
+                                                                      double* __restrict__ out) {
+  __shared__ double sh_s[kFinishThreads], sh_c[kFinishThreads];
+  const int tid = threadIdx.x;
+  for (int v = 0; v < ns; ++v) {
+    Acc a;
+    a.init();
+    for (int b = tid; b < nblk; b += kFinishThreads) a.merge(part[(b * ns + v) * 2], part[(b * ns + v) * 2 + 1]);
+    sh_s[tid] = a.s;
+    sh_c[tid] = a.c;
+    __syncthreads();
+    for (int o = kFinishThreads / 2; o > 0; o >>= 1) {
+      if (tid < o) {
+        Acc x;
+        x.s = sh_s[tid];
+        x.c = sh_c[tid];
+        x.merge(sh_s[tid + o], sh_c[tid + o]);
+        sh_s[tid] = x.s;
+        sh_c[tid] = x.c;
+      }
+      __syncthreads();
     }
-    const double* pm = part + (long)nblk * 2 * ns;
-    for (int v = 0; v < nm; ++v) {
-      double t = -INFINITY;
-      for (int b = 0; b < nblk; ++b) t = fmax(t, pm[b * nm + v]);
-      out[ns + v] = t;
+    if (tid == 0) out[v] = sh_s[0] + sh_c[0];
+    __syncthreads();
+  }
+  const double* pm = part + (long)nblk * 2 * ns;
+  for (int v = 0; v < nm; ++v) {
+    double t = -INFINITY;
+    for (int b = tid; b < nblk; b += kFinishThreads) t = fmax(t, pm[b * nm + v]);
+    sh_s[tid] = t;
+    __syncthreads();
+    for (int o = kFinishThreads / 2; o > 0; o >>= 1) {
+      if (tid < o) sh_s[tid] = fmax(sh_s[tid], sh_s[tid + o]);
+      __syncthreads();
     }
+    if (tid == 0) out[ns + v] = sh_s[0];
+    __syncthreads();
   }
 }
 
@@ -78,6 +105,13 @@ struct FSumRho {
 struct FAbsMax {
   const double* a;
   __device__ void operator()(long i, double*, double* m) const { m[0] = fabs(a[i]); }
+};
+struct FSqAbsMax {  // sum a^2 and max |a|
+  const double* a;
+  __device__ void operator()(long i, double* s, double* m) const {
+    s[0] = a[i] * a[i];
+    m[0] = fabs(a[i]);
+  }
 };
 
 __device__ __forceinline__ double alias_rho(const Alias& a, double y) { return a.dmin + a.c * y * y / (1 + y * y); }
@@ -265,7 +299,7 @@ template <int NS, int NM, class F>
 static int map_reduce(cdft_ctx* c, long n, F f, double* host_out) {
   const unsigned g = grid_for(n);
   k_map_reduce<NS, NM, F><<<g, 256, 0, c->stream>>>(n, f, c->red_part);
-  k_finish_map_reduce<<<1, 32, 0, c->stream>>>(c->red_part, (int)g, NS, NM, c->red_out);
+  k_finish_map_reduce<<<1, kFinishThreads, 0, c->stream>>>(c->red_part, (int)g, NS, NM, c->red_out);
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->host_out, c->red_out, (NS + NM) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   std::memcpy(host_out, c->host_out, (NS + NM) * sizeof(double));
@@ -274,11 +308,73 @@ static int map_reduce(cdft_ctx* c, long n, F f, double* host_out) {
 
 // One evaluation on the context's density: Species::beginForceCalculation,
 // DFT::calculateFreeEnergyAndDerivatives_internal_, Species::endForceCalculation.
+// Grand-canonical evaluation as one graph launch and one synchronisation:
+// the pass sequence, max|dF| and the copies of every sum to pinned memory.
+static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
+  const long N = c->info.N;
+  const double dV = c->info.dV;
+  if (!c->eval_exec || c->eg_prec != c->precision || c->eg_only_fex != only_fex || c->eg_vext != c->vext || c->eg_mu != c->mu ||
+      c->eg_plan_gen != c->plan_gen) {
+    if (c->eval_exec) cudaGraphExecDestroy(c->eval_exec);
+    c->eval_exec = nullptr;
+    if (!c->cap_stream) CUDA_OR_FAIL(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    if (!c->host_status) CUDA_OR_FAIL(c, cudaMallocHost(&c->host_status, sizeof(unsigned)));
+    cudaStream_t s = c->cap_stream;
+    cudaGraph_t g;
+    CUDA_OR_FAIL(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc;
+    if (c->precision == CDFT_FP64) rc = c->e64->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s);
+    else rc = c->e32->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s);
+    const unsigned gr = grid_for(N);
+    k_map_reduce<1, 1, FSqAbsMax><<<gr, 256, 0, s>>>(N, FSqAbsMax{c->dF}, c->red_part);
+    k_finish_map_reduce<<<1, kFinishThreads, 0, s>>>(c->red_part, (int)gr, 1, 1, c->red_out);
+    const double* dterms = c->precision == CDFT_FP64 ? c->e64->dev_terms() : c->e32->dev_terms();
+    const unsigned* dst = c->precision == CDFT_FP64 ? c->e64->dev_status() : c->e32->dev_status();
+    cudaMemcpyAsync(c->host_out, dterms, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(c->host_out + 8, c->red_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(c->host_status, dst, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (rc || ce != cudaSuccess) return fail(c, CDFT_ERR_CUDA, "evaluation graph capture failed");
+    const cudaError_t ie = cudaGraphInstantiate(&c->eval_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      c->eval_exec = nullptr;
+      return fail(c, CDFT_ERR_CUDA, "evaluation graph instantiate failed");
+    }
+    c->eg_prec = c->precision;
+    c->eg_only_fex = only_fex;
+    c->eg_vext = c->vext;
+    c->eg_mu = c->mu;
+    c->eg_plan_gen = c->plan_gen;
+  }
+  CUDA_OR_FAIL(c, cudaGraphLaunch(c->eval_exec, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  EvalTerms t;
+  int rc = c->precision == CDFT_FP64 ? c->e64->terms_from(c->host_out, *c->host_status, dV, c->mu, &t)
+                                     : c->e32->terms_from(c->host_out, *c->host_status, dV, c->mu, &t);
+  if (rc == 3) return fail(c, CDFT_ERR_TIMEOUT, "a tensor copy did not complete within its wait limit");
+  if (rc) return fail(c, CDFT_ERR_CUDA, "evaluation failed");
+  if (terms8) {
+    terms8[0] = t.Omega;
+    terms8[1] = t.F_id;
+    terms8[2] = t.F_hs;
+    terms8[3] = t.F_mf;
+    terms8[4] = t.F_ext;
+    terms8[5] = c->mu;
+    terms8[6] = c->host_out[9] / dV;
+    terms8[7] = t.sum_rho * dV;
+  }
+  c->last_dF_l2 = std::sqrt(c->host_out[8]) / dV;
+  if (t.status & 1u) return fail(c, CDFT_ERR_ETA, "Eta too large in FMT::dPHI");
+  return CDFT_OK;
+}
+
 static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
   const long N = c->info.N;
   const double dV = c->info.dV;
   int rc = ensure_evaluator(c, c->precision);
   if (rc) return rc;
+  if (c->fixed_mass <= 0) return eval_graph(c, terms8, only_fex);
   if (c->fixed_mass > 0) {  // src/Species.cpp:64-71
     double s;
     rc = map_reduce<1, 0>(c, N, FSumRho{c->rho}, &s);
@@ -295,9 +391,11 @@ static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
     c->mu = t.sum_dF_rho / c->fixed_mass;
     k_add_const<<<grid_for(N), 256, 0, c->stream>>>(c->dF, N, c->mu * dV);
   }
-  double mx;
-  rc = map_reduce<0, 1>(c, N, FAbsMax{c->dF}, &mx);
+  double sq_mx[2];
+  rc = map_reduce<1, 1>(c, N, FSqAbsMax{c->dF}, sq_mx);
   if (rc) return rc;
+  const double mx = sq_mx[1];
+  c->last_dF_l2 = std::sqrt(sq_mx[0]) / dV;
   if (terms8) {
     terms8[0] = t.Omega;
     terms8[1] = t.F_id;
@@ -382,6 +480,9 @@ int cdft_destroy(cdft_ctx* c) {
   cudaFree(c->dd0); cudaFree(c->dd1); cudaFree(c->ddn); cudaFree(c->dR); cudaFree(c->dfac);
   cudaFree(c->rk0); cudaFree(c->R0k); cudaFree(c->R1k); cudaFree(c->work);
   cudaFree(c->hv_v); cudaFree(c->hv_out);
+  if (c->eval_exec) cudaGraphExecDestroy(c->eval_exec);
+  if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+  cudaFreeHost(c->host_status);
   delete c;
   return CDFT_OK;
 }

@@ -55,6 +55,18 @@ struct cdft_ctx {
   double *dd0 = nullptr, *dd1 = nullptr, *ddn = nullptr, *dR = nullptr, *dfac = nullptr;
   void *rk0 = nullptr, *R0k = nullptr, *R1k = nullptr, *work = nullptr;
   std::vector<double> Lx, Ly, Lz;
+  // Graph of the whole grand-canonical evaluation (passes, reductions, copies
+  // of the sums to pinned memory), captured on cap_stream and replayed on
+  // stream; re-captured when its inputs change (precision, only_fex, the
+  // external-field pointer, mu, the transform plans).
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t eval_exec = nullptr;
+  int eg_prec = -1, eg_only_fex = -1;
+  const double* eg_vext = nullptr;
+  double eg_mu = 0;
+  unsigned plan_gen = 0, eg_plan_gen = ~0u;
+  unsigned* host_status = nullptr;  // pinned
+  double last_dF_l2 = 0;            // ||dF||_2 / dV of the last evaluation
   // Hessian-vector product buffers (device, N doubles each; allocated on first use)
   double *hv_v = nullptr, *hv_out = nullptr;
   // device FIRE2 engine (graph-captured steps)
@@ -79,6 +91,8 @@ int cdft_internal_fire_accept(cdft_ctx* c, int s_idx);
 void cdft_internal_fire_dev_free(cdft_ctx* c);
 void cdft_internal_newton_free(cdft_ctx* c);
 int cdft_internal_newton_ensure(cdft_ctx* c);
+void cdft_internal_newton_save(cdft_ctx* c);
+void cdft_internal_newton_restore(cdft_ctx* c);
 // FIRE2 state re-derived from the current density: x = alias(rho), v = 0, one evaluation
 int cdft_internal_fire_resync(cdft_ctx* c);
 // plans cdft_autotune chose for the context's shape, model and precision (cdft_tune.cu)

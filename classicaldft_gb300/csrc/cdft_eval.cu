@@ -291,7 +291,7 @@ bool Evaluator<T>::setup_tma(std::string* err) {
       auto set_phi = [&](auto kern) {
         raise_smem(kern, smem_tphi_);
         int b2 = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, 256, smem_tphi_);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, PhiThreads<T>::value, smem_tphi_);
         return std::max(b2, 1);
       };
       int bp;
@@ -477,11 +477,11 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
       constexpr int RB = PhiRows<T>::value;
       phi_blocks = grid_tphi_;
       switch (model_) {
-        case MODEL_ROSENFELD: (fz_ ? k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 128> : k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_RSLT: (fz_ ? k_phi_rows_tma<T, MODEL_RSLT, RB, 128> : k_phi_rows_tma<T, MODEL_RSLT, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_ESFMT: (fz_ ? k_phi_rows_tma<T, MODEL_ESFMT, RB, 128> : k_phi_rows_tma<T, MODEL_ESFMT, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_WHITEBEAR_I: (fz_ ? k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 128> : k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        default: (fz_ ? k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 128> : k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 0>)<<<grid_tphi_, 256, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_ROSENFELD: (fz_ ? k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 128> : k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_RSLT: (fz_ ? k_phi_rows_tma<T, MODEL_RSLT, RB, 128> : k_phi_rows_tma<T, MODEL_RSLT, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_ESFMT: (fz_ ? k_phi_rows_tma<T, MODEL_ESFMT, RB, 128> : k_phi_rows_tma<T, MODEL_ESFMT, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_WHITEBEAR_I: (fz_ ? k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 128> : k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        default: (fz_ ? k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 128> : k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
       }
     } else
     switch (model_) {
@@ -633,6 +633,11 @@ int Evaluator<T>::finish(double dV, double mu, EvalTerms* out, cudaStream_t s) {
   cudaMemcpyAsync(h, terms_, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
   cudaMemcpyAsync(&st, status_, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) return 5;
+  return terms_from(h, st, dV, mu, out);
+}
+
+template <class T>
+int Evaluator<T>::terms_from(const double* h, unsigned st, double dV, double mu, EvalTerms* out) const {
   out->F_hs = M_ > 0 ? h[0] * dV : 0.0;
   out->F_mf = mf_ ? 0.5 * dV * h[1] : 0.0;
   out->F_id = h[2];

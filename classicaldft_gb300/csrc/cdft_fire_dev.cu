@@ -624,17 +624,28 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
   long total = 0, taken = 0, steps32 = 0;
   int stop = 0;
   long nk = 0, ncg = 0;
-  if (mixed == 3) {  // Newton-Krylov from the current state; the mixed = 2 path if it stalls
-    cdft_newton_report nr;
-    rc = cdft_newton_refine(c, resid_tol, kNewtonMax3, kNewtonCg, kNewtonRtol, &nr);
+  if (mixed == 3) {
+    // Newton-Krylov from the current state: first the fast settings (loose CG while the
+    // residual is large, FP32 residuals above 1e-4); if that stalls, again from the same
+    // start with FP64 residuals and CG to 1e-3 throughout; then the mixed = 2 path.
+    cdft_newton_params fast{kNewtonMax3, kNewtonCg, kNewtonRtol, 0.1, 1e-4};
+    cdft_newton_params safe{kNewtonMax3, kNewtonCg, kNewtonRtol, 0.0, 0.0};
+    rc = cdft_internal_newton_ensure(c);
     if (rc) return rc;
-    if (nr.stop == 2) {
-      report_of(c, 0, 2, rep, 0);
-      if (rep) rep->newton = nr.newton, rep->cg_iters = nr.cg_iters;
-      return CDFT_OK;
+    cdft_internal_newton_save(c);
+    for (const cdft_newton_params* p : {&fast, &safe}) {
+      if (p == &safe) cdft_internal_newton_restore(c);
+      cdft_newton_report nr;
+      rc = cdft_newton_refine_ex(c, resid_tol, p, &nr);
+      if (rc) return rc;
+      nk += nr.newton;
+      ncg += nr.cg_iters;
+      if (nr.stop == 2) {
+        report_of(c, 0, 2, rep, 0);
+        if (rep) rep->newton = nk, rep->cg_iters = ncg;
+        return CDFT_OK;
+      }
     }
-    nk = nr.newton;
-    ncg = nr.cg_iters;
     mixed = 2;
   }
   if (mixed) {

@@ -75,6 +75,8 @@ class Evaluator {
   void pass_bytes(double* bytes) const;
   bool setup_tma(std::string* err);
   int finish(double dV, double mu, EvalTerms* out, cudaStream_t s);
+  // the host side of finish: raw device sums h[8] and status -> terms
+  int terms_from(const double* h, unsigned st, double dV, double mu, EvalTerms* out) const;
   // Transforms used by DDFT and tests: real FP64 (device) -> spectrum (device C), and back (x scale).
   void r2c(const double* in, C* out, cudaStream_t s);
   void c2r(const C* in, double* out, T scale, cudaStream_t s);

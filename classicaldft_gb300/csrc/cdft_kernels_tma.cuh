@@ -161,7 +161,7 @@ __host__ __device__ constexpr int fx_twoff(int n, int i) {
   return off;
 }
 
-template <int DIR, class T, int TC, int PITCH, int NF, int ST>
+template <int DIR, class T, int TC, int PITCH, int NF, int ST, int NTH>
 __device__ __forceinline__ void fx_stage(const typename Cx<T>::type* __restrict__ src, typename Cx<T>::type* __restrict__ dst,
                                          const typename Cx<T>::type* __restrict__ table) {
   constexpr int p = fx_radix(NF, ST), len = fx_len(NF, ST), m = len / p, s = NF / len;
@@ -169,7 +169,7 @@ __device__ __forceinline__ void fx_stage(const typename Cx<T>::type* __restrict_
   const typename Cx<T>::type* tw = table + fx_twoff(NF, ST);
   const typename Cx<T>::type* rt = tw + len;
 #pragma unroll 2
-  for (int w = threadIdx.x; w < items; w += 256) {
+  for (int w = threadIdx.x; w < items; w += NTH) {
     const int c = w % TC, u = w / TC;
     const int q = u / s, k = u % s;
     if constexpr (p == 2 || p == 4 || p == 8) tile_butterfly<DIR, T, p, PITCH>(src, dst, c, q, k, m, s, tw, rt);
@@ -178,24 +178,24 @@ __device__ __forceinline__ void fx_stage(const typename Cx<T>::type* __restrict_
   }
 }
 
-template <int DIR, class T, int TC, int PITCH, int NF, int ST = 0>
+template <int DIR, class T, int TC, int PITCH, int NF, int NTH, int ST = 0>
 __device__ __forceinline__ typename Cx<T>::type* tile_fft_fixed(typename Cx<T>::type* b0, typename Cx<T>::type* b1,
                                                                 const typename Cx<T>::type* __restrict__ table) {
   __syncthreads();
   if constexpr (fx_radix(NF, ST) == 0) {
     return b0;
   } else {
-    fx_stage<DIR, T, TC, PITCH, NF, ST>(b0, b1, table);
-    return tile_fft_fixed<DIR, T, TC, PITCH, NF, ST + 1>(b1, b0, table);
+    fx_stage<DIR, T, TC, PITCH, NF, ST, NTH>(b0, b1, table);
+    return tile_fft_fixed<DIR, T, TC, PITCH, NF, NTH, ST + 1>(b1, b0, table);
   }
 }
 
 // The transform of a tile: the compile-time plan when NF > 0 (launched only
 // when the runtime plan is that default plan of length NF), else the runtime plan.
-template <int DIR, class T, int TC, int PITCH, int NF>
+template <int DIR, class T, int TC, int PITCH, int NF, int NTH = 256>
 __device__ __forceinline__ typename Cx<T>::type* tfft(typename Cx<T>::type* b0, typename Cx<T>::type* b1, const FFTPlan& P,
                                                       const typename Cx<T>::type* __restrict__ table) {
-  if constexpr (NF > 0) return tile_fft_fixed<DIR, T, TC, PITCH, NF>(b0, b1, table);
+  if constexpr (NF > 0) return tile_fft_fixed<DIR, T, TC, PITCH, NF, NTH>(b0, b1, table);
   else return tile_fft<DIR, T, TC, PITCH>(b0, b1, P, table);
 }
 
@@ -468,8 +468,12 @@ namespace cdft {
 // L = NP*RB lines, transformed column-wise (line-fastest, conflict-free):
 // c2r (z), Phi and dPhi per point, r2c (z), then the M derivative rows are
 // stored over the inputs.
+// threads per block of the fused Phi pass (512 threads with two blocks per SM
+// measured no faster in FP32 than 256)
+template <class T> struct PhiThreads { static constexpr int value = 256; };
+
 template <class T, int MODEL, int RB, int NF = 0>
-__global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
+__global__ void __launch_bounds__(PhiThreads<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
                                                       Dims d, FFTPlan pz_plan, const typename Cx<T>::type* __restrict__ tw, T hsd, T esA,
                                                       T esB, double* __restrict__ part, unsigned* __restrict__ status) {
   typedef typename Cx<T>::type C;
@@ -528,7 +532,7 @@ __global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CU
       const long gn = g + 2L * gridDim.x;
       if (gn < ngroup) issue(gn, b);
     }
-    C* res = tfft<+1, T, L, LPd, NF>(Z0, Z1, pz_plan, tw);
+    C* res = tfft<+1, T, L, LPd, NF, PhiThreads<T>::value>(Z0, Z1, pz_plan, tw);
     C* oth = (res == Z0) ? Z1 : Z0;
     for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
       const int k = e % nz, r = e / nz;
@@ -547,7 +551,7 @@ __global__ void __launch_bounds__(256) k_phi_rows_tma(const __grid_constant__ CU
 #pragma unroll
       for (int p = 0; p < NP; ++p) oth[k * LPd + r * NP + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
     }
-    C* res2 = tfft<-1, T, L, LPd, NF>(oth, res, pz_plan, tw);
+    C* res2 = tfft<-1, T, L, LPd, NF, PhiThreads<T>::value>(oth, res, pz_plan, tw);
     for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
       const int k = e % nzc, line = e / nzc;
       const int r = line / NP, pr = line - r * NP;

@@ -118,10 +118,12 @@ __global__ void k_nk_step(double* rho, const double* rho0, const float* dl, long
 struct NewtonWork {
   float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dl = nullptr;
   double* rho0 = nullptr;
+  double* start = nullptr;  // a saved starting density (cdft_internal_newton_save / _restore)
   double* part = nullptr;   // device, 3 x grid
   double* hpart = nullptr;  // pinned
   ~NewtonWork() {
-    cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(dl); cudaFree(rho0); cudaFree(part); cudaFreeHost(hpart);
+    cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(dl); cudaFree(rho0); cudaFree(start); cudaFree(part);
+    cudaFreeHost(hpart);
   }
 };
 
@@ -144,13 +146,22 @@ int cdft_internal_newton_ensure(cdft_ctx* c) {
   const size_t fb = N * sizeof(float);
   if (cudaMalloc(&W->r, fb) != cudaSuccess || cudaMalloc(&W->z, fb) != cudaSuccess || cudaMalloc(&W->p, fb) != cudaSuccess ||
       cudaMalloc(&W->q, fb) != cudaSuccess || cudaMalloc(&W->dl, fb) != cudaSuccess ||
-      cudaMalloc(&W->rho0, N * sizeof(double)) != cudaSuccess || cudaMalloc(&W->part, (size_t)g * 3 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&W->rho0, N * sizeof(double)) != cudaSuccess || cudaMalloc(&W->start, N * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&W->part, (size_t)g * 3 * sizeof(double)) != cudaSuccess ||
       cudaMallocHost(&W->hpart, (size_t)g * 3 * sizeof(double)) != cudaSuccess) {
     cdft_internal_newton_free(c);
     return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton work arrays");
   }
   if (!c->e32->hess_ready() && c->e32->hess_prepare(c->rho, c->stream)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian buffers");
   return CDFT_OK;
+}
+
+// Saves / restores the context's density (a Newton run that stalls is retried from the same start).
+void cdft_internal_newton_save(cdft_ctx* c) {
+  cudaMemcpyAsync(c->newton->start, c->rho, c->info.N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+}
+void cdft_internal_newton_restore(cdft_ctx* c) {
+  cudaMemcpyAsync(c->rho, c->newton->start, c->info.N * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
 }
 
 // Sums the NV block partials of the last reduction (synchronises the stream).
@@ -167,7 +178,20 @@ static bool sums(cdft_ctx* c, unsigned g, double* out) {
 }
 
 extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int max_cg, double cg_rtol, cdft_newton_report* rep) {
-  if (!c || !(tol > 0) || max_newton <= 0 || max_cg <= 0 || !(cg_rtol > 0)) return CDFT_ERR_ARG;
+  cdft_newton_params p;
+  p.max_newton = max_newton;
+  p.max_cg = max_cg;
+  p.cg_rtol = cg_rtol;
+  p.eta_max = 0.1;
+  p.fp32_above = 1e-4;
+  return cdft_newton_refine_ex(c, tol, &p, rep);
+}
+
+extern "C" int cdft_newton_refine_ex(cdft_ctx* c, double tol, const cdft_newton_params* prm, cdft_newton_report* rep) {
+  if (!c || !prm) return CDFT_ERR_ARG;
+  const int max_newton = prm->max_newton, max_cg = prm->max_cg;
+  const double cg_rtol = prm->cg_rtol, eta_max = prm->eta_max, fp32_above = prm->fp32_above;
+  if (!(tol > 0) || max_newton <= 0 || max_cg <= 0 || !(cg_rtol > 0) || !(eta_max >= 0) || !(fp32_above >= 0)) return CDFT_ERR_ARG;
   const long N = c->info.N;
   const double dV = c->info.dV;
   const bool fixed = c->fixed_mass > 0;
@@ -184,22 +208,23 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
   // Residuals far from the solution come from FP32 evaluations (their noise,
   // ~1e-6, is far below the residual); from kFp64Below on, and for every
   // residual that can end the run, from FP64.
-  constexpr double kFp64Below = 1e-4;
-  bool fp64 = false;
+  const double kFp64Below = fp32_above;
+  bool fp64 = fp32_above <= 0;
   auto evaluate = [&](bool use64) -> int {
     int e = cdft_set_precision(c, use64 ? CDFT_FP64 : CDFT_FP32);
     if (!e) e = cdft_internal_eval(c, t, 0);
     ++R.evals;
     return e;
   };
-  rc = evaluate(false);
+  rc = evaluate(fp64);
   if (rc && rc != CDFT_ERR_ETA) return rc;
-  if (rc || t[6] <= kFp64Below) {
+  if (!fp64 && (rc || t[6] <= kFp64Below)) {
     fp64 = true;
     rc = evaluate(true);
     if (rc) return rc;
   }
   double resid = t[6];
+  double l2 = c->last_dF_l2;
   R.F = t[0];
   int stop = 0;
   for (int k = 0; k < max_newton && resid > tol; ++k) {
@@ -222,14 +247,22 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
     double rz = rz_rr[0];
     const double r0 = std::sqrt(rz_rr[1]);
     // forcing term: a loose linear solve while the residual is large (inexact Newton)
-    const double eta = std::min(0.1, std::max(cg_rtol, resid));
+    const double eta = eta_max > 0 ? std::max(cg_rtol, std::min(eta_max, resid)) : cg_rtol;
     int it = 0;
     for (; it < max_cg; ++it) {
       if (c->e32->hess_apply<float>(W->p, c->rho, W->q, dV, s)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian product failed");
       k_nk_pq<<<g, kT, 0, s>>>(W->p, W->q, N, W->part);
       double pq[2];
       if (!sums<2>(c, g, pq)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");
-      if (!(pq[1] > 0)) break;  // not positive along p: keep the correction built so far
+      if (!(pq[1] > 0)) {  // not positive along p: keep the correction built so far
+        if (it == 0) {
+          // negative curvature along the preconditioned gradient itself: step along that
+          // descent direction instead (the line search below sizes it on Omega)
+          k_nk_update<<<g, kT, 0, s>>>(W->dl, W->r, W->p, W->q, N, (float)(rz / std::max(std::fabs(pq[1]), 1e-300)), 0.f);
+          ++it;
+        }
+        break;
+      }
       const double alpha = rz / pq[1];
       k_nk_update<<<g, kT, 0, s>>>(W->dl, W->r, W->p, W->q, N, (float)alpha, fixed ? (float)(pq[0] / N) : 0.f);
       double nz[2];
@@ -254,10 +287,11 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
       k_nk_step<<<g, kT, 0, s>>>(c->rho, W->rho0, W->dl, N, step);
       rc = evaluate(fp64);
       if (rc && rc != CDFT_ERR_ETA) return rc;
-      // accept a lower FP64 residual, or (far from the minimum) a real decrease of Omega
-      if (!rc && (t[6] < resid || t[0] < R.F - (fp64 ? 1e-13 : 1e-6) * std::fabs(R.F))) {
+      // accept a lower residual (max or 2-norm), or (far from the minimum) a real decrease of Omega
+      if (!rc && (t[6] < resid || c->last_dF_l2 < l2 || t[0] < R.F - (fp64 ? 1e-13 : 1e-6) * std::fabs(R.F))) {
         accepted = true;
         resid = t[6];
+        l2 = c->last_dF_l2;
         R.F = t[0];
       }
     }
@@ -277,6 +311,7 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
       rc = evaluate(true);
       if (rc) return rc;
       resid = t[6];
+      l2 = c->last_dF_l2;
       R.F = t[0];
     }
   }

@@ -80,18 +80,35 @@ __device__ __forceinline__ uint32_t kmajor_off(int row, int k, int rows) {
 __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
 
 // K multiple of 16 (<= 64), N multiple of 32 (<= 128), M any (rows past M are zero-filled, not written).
+// Dynamic shared memory: the X tile, W^T, and a 32 x 33 FP32 staging block per warp through which the
+// accumulator rows are turned into coalesced row-major stores.
+template <int N, int K>
+__host__ __device__ constexpr size_t smem_bytes() {
+  return (size_t)2 * kRows * K * 2 + (size_t)N * K * 2 + (size_t)4 * 32 * 33 * 4;  // two X tiles (double buffer)
+}
+
+// 16-byte asynchronous copy global -> shared; zero-fills when `valid` is false
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 template <int N, int K>
 __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restrict__ X, const __nv_bfloat16* __restrict__ W,
                                                    const float* __restrict__ bias, const float* __restrict__ add, float* __restrict__ Y,
                                                    float* __restrict__ Z, long M, int act, unsigned* __restrict__ status) {
   static_assert(K % 16 == 0 && K <= 64 && N % 32 == 0 && N <= 128, "tile shape");
   constexpr int TCOLS = N <= 32 ? 32 : (N <= 64 ? 64 : 128);  // power of two >= 32
-  __shared__ __align__(1024) unsigned char sx[kRows * K * 2];
-  __shared__ __align__(1024) unsigned char sw[N * K * 2];
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* sxb[2] = {smem_raw, smem_raw + (size_t)kRows * K * 2};
+  unsigned char* sw = smem_raw + (size_t)2 * kRows * K * 2;
+  float* ep = reinterpret_cast<float*>(sw + (size_t)N * K * 2);
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_base;
   __shared__ int stop;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  float* my = ep + warp * 32 * 33;
   // W^T (N rows of K) into the canonical layout, once
   for (int e = tid; e < N * K; e += blockDim.x) {
     const int n = e / K, k = e - n * K;
@@ -113,19 +130,28 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restri
   const long ntile = (M + kRows - 1) / kRows;
   constexpr uint32_t idesc = instr_desc(N);
   unsigned phase = 0;
-  for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
-    const long row0 = t * kRows;
-    // X tile: 16-byte chunks (8 BF16 along K) per thread
+  // X tile t into buffer b: 16-byte chunks (8 BF16 along K), asynchronous, rows past M zero-filled
+  auto load_tile = [&](long t, unsigned char* buf) {
+    const long r0 = t * kRows;
     for (int e = tid; e < kRows * (K / 8); e += blockDim.x) {
       const int r = e / (K / 8), k8 = (e - r * (K / 8)) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (row0 + r < M) v = *reinterpret_cast<const uint4*>(X + (row0 + r) * K + k8);
-      *reinterpret_cast<uint4*>(sx + kmajor_off(r, k8, kRows)) = v;
+      const bool valid = r0 + r < M;
+      cp_async16(buf + kmajor_off(r, k8, kRows), X + (valid ? (r0 + r) * K + k8 : 0), valid);
     }
+    cp_async_commit();
+  };
+  if (blockIdx.x < ntile) load_tile(blockIdx.x, sxb[0]);
+  int b = 0;
+  for (long t = blockIdx.x; t < ntile; t += gridDim.x, b ^= 1) {
+    const long row0 = t * kRows;
+    unsigned char* sx = sxb[b];
+    cp_async_wait_all();  // this tile's copies (the only group in flight)
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
+    // the next tile streams into the other buffer while this one is multiplied and stored
+    if (t + gridDim.x < ntile) load_tile(t + gridDim.x, sxb[b ^ 1]);
     if (tid == 0) {
       const uint32_t ax = smem_u32(sx), aw = smem_u32(sw);
 #pragma unroll
@@ -139,27 +165,32 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restri
     fence_after();
     __syncthreads();
     if (stop) break;
-    // epilogue: warp w owns accumulator lanes 32w..32w+31 (rows of the tile)
-    const long row = row0 + warp * 32 + lane;
+    // epilogue: warp w owns accumulator lanes 32w..32w+31 (rows of the tile); each 32-column
+    // block goes through the warp's staging block so that a store instruction writes one row
 #pragma unroll
     for (int c0 = 0; c0 < N; c0 += 32) {
       uint32_t v[32];
       tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (row < M) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          float z = __uint_as_float(v[j]);
-          if (bias) z += bias[c0 + j];
-          if (add) z += add[row * N + c0 + j];
-          if (Z) Z[row * N + c0 + j] = z;
-          Y[row * N + c0 + j] = act ? gelu(z) : z;
-        }
+      for (int j = 0; j < 32; ++j) my[lane * 33 + j] = __uint_as_float(v[j]);
+      __syncwarp();
+      const int col = c0 + lane;
+      const float bc = bias ? bias[col] : 0.f;
+      for (int r = 0; r < 32; ++r) {
+        const long row = row0 + warp * 32 + r;
+        if (row >= M) break;
+        float z = my[r * 33 + lane] + bc;
+        if (add) z += add[row * N + col];
+        if (Z) Z[row * N + col] = z;
+        Y[row * N + col] = act ? gelu(z) : z;
       }
+      __syncwarp();
     }
     fence_before();
     __syncthreads();  // the tile buffer and the accumulator are reused by the next tile
     fence_after();
   }
+  cp_async_wait_all();  // no copy may still target shared memory when the CTA exits
   if (stop && tid == 0) {
     atomicOr(status, kStatusTcTimeout);
     mbar_wait(&bar, phase ^ 1u, nullptr);  // bounded: the MMAs still in flight before their columns are freed
@@ -183,7 +214,13 @@ static int launch_gemm(const void* X, const void* W, const float* bias, const fl
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const long ntile = (M + kRows - 1) / kRows;
   const unsigned grid = (unsigned)std::min<long>(ntile, (long)nsm * 4);
-  k_gemm_bf16<N, K><<<grid, 128, 0, s>>>(reinterpret_cast<const __nv_bfloat16*>(X), reinterpret_cast<const __nv_bfloat16*>(W), bias, add,
+  constexpr size_t sm = smem_bytes<N, K>();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gemm_bf16<N, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  k_gemm_bf16<N, K><<<grid, 128, sm, s>>>(reinterpret_cast<const __nv_bfloat16*>(X), reinterpret_cast<const __nv_bfloat16*>(W), bias, add,
                                           Y, Z, M, act, status);
   return cudaGetLastError() == cudaSuccess ? CDFT_OK : CDFT_ERR_CUDA;
 }

@@ -100,6 +100,7 @@ static float time_evals(cdft_ctx* c, int reps, cudaEvent_t e0, cudaEvent_t e1) {
 }
 
 static void install(cdft_ctx* c, const std::shared_ptr<FFTTable> t[3]) {
+  ++c->plan_gen;  // captured evaluation graphs hold the old plans
   c->tx = t[0];
   c->ty = t[1];
   c->tz = t[2];

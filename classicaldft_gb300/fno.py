@@ -146,9 +146,9 @@ class FNO3d(torch.nn.Module):
         return out[:, 0]
 
 
-def upsample(coarse, shape):
+def upsample(coarse, shape, device="cpu"):
     """Spectral (zero-padded Fourier) interpolation of a periodic coarse field to `shape`."""
-    c = torch.as_tensor(coarse, dtype=torch.float64)
+    c = torch.as_tensor(coarse, dtype=torch.float64, device=device)
     C = torch.fft.rfftn(c)
     n = c.shape
     F = torch.zeros(shape[0], shape[1], shape[2] // 2 + 1, dtype=C.dtype, device=C.device)
@@ -166,7 +166,7 @@ def features(seed_coarse, kT, shape, device):
     """Per-point input features: [log seed (upsampled), kT, 1, 0, ...] as an (N, K_IN) FP32 tensor,
     and the upsampled seed itself."""
     # interpolate log(seed): smooth, and positive after exp whatever the interpolant's ringing
-    up = torch.exp(upsample(np.log(seed_coarse), shape)).to(device=device, dtype=torch.float32)
+    up = torch.exp(upsample(np.log(seed_coarse), shape, device)).to(dtype=torch.float32)
     N = up.numel()
     f = torch.zeros(N, K_IN, device=device)
     f[:, 0] = torch.log(up).reshape(-1)

@@ -235,6 +235,16 @@ typedef struct cdft_newton_report {
   int stop;       /* 2 residual reached, 3 no decrease along a correction, 0 max_newton */
 } cdft_newton_report;
 int cdft_newton_refine(cdft_ctx* ctx, double resid_tol, int max_newton, int max_cg, double cg_rtol, cdft_newton_report* rep);
+/* The same with every parameter explicit. eta_max > 0 makes the CG tolerance
+ * of a correction max(cg_rtol, min(eta_max, resid)) (loose while the residual is
+ * large); 0 keeps cg_rtol. Residuals above fp32_above come from FP32
+ * evaluations (0: FP64 throughout). cdft_newton_refine uses eta_max = 0.1,
+ * fp32_above = 1e-4. */
+typedef struct cdft_newton_params {
+  int max_newton, max_cg;
+  double cg_rtol, eta_max, fp32_above;
+} cdft_newton_params;
+int cdft_newton_refine_ex(cdft_ctx* ctx, double resid_tol, const cdft_newton_params* p, cdft_newton_report* rep);
 
 /* BF16 tensor-core GEMM (tcgen05, FP32 accumulation in tensor memory) for the
  * neural-operator warm start; no counterpart in the reference.

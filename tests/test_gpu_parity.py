@@ -287,3 +287,25 @@ def test_bulk_coexistence_matches_reference(cd):
         assert abs(r["mu"] - g["coex.mu"][i]) < 1e-9
         assert abs(r["spinodal1"] - g["coex.spinodal1"][i]) < 1e-8
         assert abs(r["spinodal2"] - g["coex.spinodal2"][i]) < 1e-8
+
+
+def test_large_grid_properties(cd, oracle):
+    """Sizes past what the oracle finishes quickly: 256^3 (FP32) and 192 x 160 x 144 (FP64).
+    A uniform density gives the bulk values everywhere; translating the density by whole
+    lattice sites translates dF (periodic), in both precisions."""
+    for shape, prec, tol in (((256, 256, 256), cd.FP32, 1e-5), ((192, 160, 144), cd.FP64, 1e-12)):
+        c = cd.Context(shape, 0.1, cd.WHITEBEAR_I, hsd=None, lj=True, kT=0.9, precision=prec)
+        mu = c.bulk(0.3)["mu"]
+        c.set_chem_potential(mu)
+        c.set_density(np.full(shape, 0.4))
+        terms, dF = c.eval()
+        b = c.bulk(0.4)
+        assert abs(dF.mean() / c.info.dV - (b["mu"] - mu)) < (1e-6 if prec == cd.FP32 else 1e-7)
+        assert np.ptp(dF) / c.info.dV < (1e-5 if prec == cd.FP32 else 1e-12)
+        rho = oracle.fill_noise(shape, 0.3, 0.3, 21)
+        c.set_density(rho)
+        _, d0 = c.eval()
+        c.set_density(np.roll(rho, (3, -5, 7), axis=(0, 1, 2)))
+        _, d1 = c.eval()
+        assert np.max(np.abs(np.roll(d0, (3, -5, 7), axis=(0, 1, 2)) - d1)) <= tol * np.max(np.abs(d0))
+        c.close()

@@ -71,3 +71,15 @@ def test_radix_candidates(n):
     for c in cands:
         assert int(np.prod(c)) == n
         assert all(r in (2, 4, 8) or (r % 2 == 1 and all(r % q for q in range(3, r, 2))) for r in c)
+
+
+def test_create_rejects_bad_systems_before_touching_the_gpu():
+    """Grid lengths with a prime factor above 31 and hsd < dx are refused (CDFT_ERR_ARG = 4)
+    before any device allocation, as the reference refuses them in its constructors."""
+    import classicaldft_gb300 as cd
+    L = cd.lib()
+    for nx, hsd in ((37, 1.0), (32, 0.05)):
+        p = cd.Params(nx, 32, 32, 0.1, cd.WHITEBEAR_I, 1.0, 0.0, hsd, 0, 1.0, 1.0, 3.0, 1.0, 0.0, -1.0, cd.FP64)
+        h = ctypes.c_void_p()
+        assert L.cdft_create(ctypes.byref(p), ctypes.byref(h)) == 4
+        assert not h.value
