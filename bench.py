@@ -213,7 +213,7 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
     return out
 
 
-def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80, 96)):
+def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80, 96), rank=0, world=1, dist=None):
     """State-point sweep: n LJ droplets (kT ~ U[0.7, 0.94], mu = mu_coex(kT) + U[-0.2, 0.2],
     R ~ U[2, 6] clamped to 0.4 L, cubic grids drawn from `grids`, dx = 0.1, fixed mass),
     all minimised to max|dOmega/drho| <= tol by Newton-Krylov (FIRE2 fallback). Batched
@@ -221,22 +221,41 @@ def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80,
     vs one after another (cdft_fire_run_device); context set-up is outside both timings."""
     import torch
     from classicaldft_gb300 import statepoints as sp
-    pts = sp.sample_state_points(n, seed=seed, grids=grids)
-    out = {"points": n, "seed": seed, "tol": tol, "grids": sorted(p["n"] for p in pts),
+    pts_all = sp.sample_state_points(n, seed=seed, grids=grids)
+    # replicas only: with several GPUs each rank takes its share of the points (no exchange)
+    pts = [pts_all[i] for i in sp.shard(pts_all, rank, world)] if world > 1 else pts_all
+    out = {"points": n, "ranks": world, "seed": seed, "tol": tol, "grids": sorted(p["n"] for p in pts),
            "ensemble": "fixed mass droplets",
            "precision": "Newton-Krylov from the tanh profile (FP32 Hessian products, FP64 residuals), FIRE2 fallback"}
     ctxs = sp.build_contexts([dict(p) for p in pts])
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     reps, status = cd.fire_run_batch(ctxs, tol, max_steps=max_steps, mixed=3, switch_tol=1e-4)
     torch.cuda.synchronize()
     tb = time.perf_counter() - t0
+    conv = sum(1 for r, s in zip(reps, status) if s == 0 and r["resid"] <= tol)
+    steps = sum(r["total_steps"] for r in reps)
+    nk = sum(r["newton"] for r in reps)
+    ncg = sum(r["cg_iters"] for r in reps)
+    if dist:  # the job's time is the slowest rank's; tallies add up
+        t = torch.tensor([tb, conv, steps, nk, ncg], dtype=torch.float64, device="cuda")
+        tmax = t[:1].clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        tb, conv, steps, nk, ncg = float(tmax.item()), int(t[1].item()), int(t[2].item()), int(t[3].item()), int(t[4].item())
     out["batched_s"] = tb
-    out["converged"] = int(sum(1 for r, s in zip(reps, status) if s == 0 and r["resid"] <= tol))
-    out["total_steps"] = int(sum(r["total_steps"] for r in reps))
+    out["converged"] = int(conv)
+    out["total_steps"] = int(steps)
+    out["newton_corrections"] = int(nk)
+    out["cg_iters"] = int(ncg)
+    out["state_points_per_s"] = n / tb
     omega_b = [r["F"] for r in reps]
     for c in ctxs:
         c.close()
+    if world > 1:  # the one-after-another comparison is a single-GPU measurement
+        return out
     ctxs = sp.build_contexts([dict(p) for p in pts])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -247,10 +266,7 @@ def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80,
         c.close()
     out["sequential_s"] = ts
     out["speedup_batched_vs_sequential"] = ts / tb
-    out["state_points_per_s"] = n / tb
     out["same_minima"] = bool(all(a == r["F"] for a, r in zip(omega_b, seq)))
-    out["newton_corrections"] = int(sum(r["newton"] for r in reps))
-    out["cg_iters"] = int(sum(r["cg_iters"] for r in reps))
     return out
 
 
@@ -431,15 +447,18 @@ def main():
                        for p in passes],
             "passes_fp64": [{"pass": p["pass"], "ms": round(p["ms"], 4)} for p in passes64],
             "clocks": clocks}
-    if not args.no_fire:
+    if not args.no_batch:  # sharded over the ranks when there are several
+        sweep = batch_leg(cd, n=args.sweep_points, grids=tuple(int(g) for g in args.sweep_grids.split(",")),
+                          rank=rank, world=world, dist=dist)
+        if rank == 0:
+            line["statepoint_sweep"] = sweep
+    # the single-GPU legs below are reported by rank 0 only (the other replicas skip them)
+    if rank == 0 and not args.no_fire:
         line["fire_to_resid_1e-8"] = fire_legs(cd, rho)
-    if not args.no_ddft:
+    if rank == 0 and not args.no_ddft:
         line["ddft_256"] = ddft_leg(cd)
-    if not args.no_fno:
+    if rank == 0 and not args.no_fno:
         line["warm_start"] = warm_start_leg(cd)
-    if not args.no_batch:
-        line["statepoint_sweep"] = batch_leg(cd, n=args.sweep_points,
-                                             grids=tuple(int(g) for g in args.sweep_grids.split(",")))
     if rank == 0 and not args.no_cpu_baseline:
         rate, n, el = cpu_baseline()
         line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",

@@ -106,13 +106,54 @@ struct FAbsMax {
   const double* a;
   __device__ void operator()(long i, double*, double* m) const { m[0] = fabs(a[i]); }
 };
-struct FSqAbsMax {  // sum a^2 and max |a|
-  const double* a;
-  __device__ void operator()(long i, double* s, double* m) const {
-    s[0] = a[i] * a[i];
-    m[0] = fabs(a[i]);
+// max |dF| (the residual) and sum dF^2 (its 2-norm, for the Newton line search):
+// plain FP64 sums, one multiply-add per point, deterministic block and tree order.
+__global__ void __launch_bounds__(256) k_dF_norms(const double* __restrict__ a, long n, double* __restrict__ part) {
+  double sq = 0, mx = 0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double v = a[i];
+    sq = fma(v, v, sq);
+    mx = fmax(mx, fabs(v));
   }
-};
+  __shared__ double s_sq[256], s_mx[256];
+  s_sq[threadIdx.x] = sq;
+  s_mx[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      s_sq[threadIdx.x] += s_sq[threadIdx.x + o];
+      s_mx[threadIdx.x] = fmax(s_mx[threadIdx.x], s_mx[threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s_sq[0];
+    part[2 * blockIdx.x + 1] = s_mx[0];
+  }
+}
+// out[0] = sum dF^2, out[1] = max |dF|
+__global__ void __launch_bounds__(256) k_dF_norms_finish(const double* __restrict__ part, int nblk, double* __restrict__ out) {
+  double sq = 0, mx = 0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+    sq += part[2 * b];
+    mx = fmax(mx, part[2 * b + 1]);
+  }
+  __shared__ double s_sq[256], s_mx[256];
+  s_sq[threadIdx.x] = sq;
+  s_mx[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      s_sq[threadIdx.x] += s_sq[threadIdx.x + o];
+      s_mx[threadIdx.x] = fmax(s_mx[threadIdx.x], s_mx[threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = s_sq[0];
+    out[1] = s_mx[0];
+  }
+}
 
 __device__ __forceinline__ double alias_rho(const Alias& a, double y) { return a.dmin + a.c * y * y / (1 + y * y); }
 
@@ -326,8 +367,8 @@ static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
     if (c->precision == CDFT_FP64) rc = c->e64->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s);
     else rc = c->e32->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s);
     const unsigned gr = grid_for(N);
-    k_map_reduce<1, 1, FSqAbsMax><<<gr, 256, 0, s>>>(N, FSqAbsMax{c->dF}, c->red_part);
-    k_finish_map_reduce<<<1, kFinishThreads, 0, s>>>(c->red_part, (int)gr, 1, 1, c->red_out);
+    k_dF_norms<<<gr, 256, 0, s>>>(c->dF, N, c->red_part);
+    k_dF_norms_finish<<<1, 256, 0, s>>>(c->red_part, (int)gr, c->red_out);
     const double* dterms = c->precision == CDFT_FP64 ? c->e64->dev_terms() : c->e32->dev_terms();
     const unsigned* dst = c->precision == CDFT_FP64 ? c->e64->dev_status() : c->e32->dev_status();
     cudaMemcpyAsync(c->host_out, dterms, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -392,8 +433,15 @@ static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
     k_add_const<<<grid_for(N), 256, 0, c->stream>>>(c->dF, N, c->mu * dV);
   }
   double sq_mx[2];
-  rc = map_reduce<1, 1>(c, N, FSqAbsMax{c->dF}, sq_mx);
-  if (rc) return rc;
+  {
+    const unsigned gr = grid_for(N);
+    k_dF_norms<<<gr, 256, 0, c->stream>>>(c->dF, N, c->red_part);
+    k_dF_norms_finish<<<1, 256, 0, c->stream>>>(c->red_part, (int)gr, c->red_out);
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->host_out, c->red_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+    sq_mx[0] = c->host_out[0];
+    sq_mx[1] = c->host_out[1];
+  }
   const double mx = sq_mx[1];
   c->last_dF_l2 = std::sqrt(sq_mx[0]) / dV;
   if (terms8) {

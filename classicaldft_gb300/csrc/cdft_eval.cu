@@ -354,6 +354,10 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_final_rows<T, double>, smem_rows_);
   set_smem<T>(k_final_rows<T, T>, smem_rows_);
   set_smem<T>(k_rows_r2c<T, T>, smem_rows_);
+  set_smem<T>(k_final_rows<T, double, 128>, smem_rows_);
+  set_smem<T>(k_final_rows<T, T, 128>, smem_rows_);
+  set_smem<T>(k_rows_r2c<T, T, 128>, smem_rows_);
+  set_smem<T>(k_rows_r2c<T, double, 128>, smem_rows_);
   set_smem<T>(k_cols_fft<T, -1>, std::max(smem_colx_, smem_coly_));
   set_smem<T>(k_cols_fft<T, +1>, std::max(smem_colx_, smem_coly_));
   set_smem<T>(k_xconv<T>, smem_xconv_);
@@ -456,7 +460,8 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   cudaMemsetAsync(status_, 0, sizeof(unsigned), s);
   mark(0);
   if (any) {
-    k_rows_r2c<T, RT><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+    (fz_ ? k_rows_r2c<T, RT, 128> : k_rows_r2c<T, RT, 0>)<<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan,
+                                                                                                       twp<T>(tz_), rb_rows_);
     mark(1);
     yfwd(A_, mapYA_, 1, grid_ty1_);
     mark(2);
@@ -514,7 +519,8 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     mark(8);
   }
   const unsigned gfin = (unsigned)grid_blocks_rows();
-  k_final_rows<T, RT><<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_), rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin);
+  (fz_ ? k_final_rows<T, RT, 128> : k_final_rows<T, RT, 0>)<<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_),
+                                                                                         rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin);
   k_finish_reduce<<<1, 256, 0, s>>>(part_fin, gfin, 4, terms_ + 2);
   mark(9);
   return 0;

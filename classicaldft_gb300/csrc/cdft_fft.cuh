@@ -169,4 +169,75 @@ __device__ typename Cx<T>::type* block_fft(typename Cx<T>::type* buf0, typename 
   return src;
 }
 
+// The same transform with the plan of length NF resolved at compile time (the
+// default radix order of make_fft_table; radix_at / len_at / twoff_at restate
+// that order as constant expressions).
+__host__ __device__ constexpr int radix_at(int n, int i) {
+  int m = n;
+  for (int st = 0; m > 1; ++st) {
+    int f = 0;
+    if (m % 8 == 0 && m != 16) f = 8;
+    else if (m % 4 == 0) f = 4;
+    else if (m % 2 == 0) f = 2;
+    else {
+      for (int q = 3; q <= m; q += 2)
+        if (m % q == 0) { f = q; break; }
+    }
+    if (st == i) return f;
+    m /= f;
+  }
+  return 0;
+}
+__host__ __device__ constexpr int len_at(int n, int i) {
+  int len = n;
+  for (int st = 0; st < i; ++st) len /= radix_at(n, st);
+  return len;
+}
+__host__ __device__ constexpr int twoff_at(int n, int i) {
+  int off = 0, len = n;
+  for (int st = 0; st < i; ++st) {
+    const int p = radix_at(n, st);
+    off += len + p;
+    len /= p;
+  }
+  return off;
+}
+
+template <int DIR, class T, int NF, int ST = 0>
+__device__ __forceinline__ typename Cx<T>::type* block_fft_fixed(typename Cx<T>::type* src, typename Cx<T>::type* dst, int L, int LP,
+                                                                 const typename Cx<T>::type* __restrict__ table) {
+  typedef typename Cx<T>::type C;
+  __syncthreads();
+  if constexpr (radix_at(NF, ST) == 0) {
+    return src;
+  } else {
+    constexpr int p = radix_at(NF, ST), len = len_at(NF, ST), m = len / p, s = NF / len, per_line = m * s;
+    const C* tw = table + twoff_at(NF, ST);
+    const C* rt = tw + len;
+    const int total = L * per_line;
+    for (int w = threadIdx.x; w < total; w += blockDim.x) {
+      const int line = w / per_line, u = w - line * per_line;
+      const int q = u / s, k = u - q * s;
+      const C* xl = src + line * LP;
+      C* yl = dst + line * LP;
+      if constexpr (p == 2 || p == 3 || p == 4 || p == 5 || p == 7 || p == 8) butterfly<DIR, T, p>(xl, yl, q, k, m, s, tw, rt);
+      else butterfly_generic<DIR, T>(xl, yl, q, k, m, s, p, tw, rt);
+    }
+    return block_fft_fixed<DIR, T, NF, ST + 1>(dst, src, L, LP, table);
+  }
+}
+
+// Runtime plan when NF == 0, the compile-time plan of length NF otherwise.
+template <int DIR, class T, int NF>
+__device__ __forceinline__ typename Cx<T>::type* block_fft_nf(typename Cx<T>::type* b0, typename Cx<T>::type* b1, int L, int LP,
+                                                              const FFTPlan& P, const typename Cx<T>::type* __restrict__ table) {
+  if constexpr (NF > 0) {
+    typename Cx<T>::type* r = block_fft_fixed<DIR, T, NF>(b0, b1, L, LP, table);
+    __syncthreads();
+    return r;
+  } else {
+    return block_fft<DIR, T>(b0, b1, L, LP, P, table);
+  }
+}
+
 }  // namespace cdft

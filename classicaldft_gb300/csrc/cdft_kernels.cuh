@@ -115,7 +115,7 @@ __global__ void k_finish_reduce(const double* __restrict__ part, long nblk, int 
 // ------------------------------------------------------------ row passes ---
 // z-axis r2c: rows of a real field (SRC = double or T) to half spectra.
 // Each block owns RB row pairs; pair r packs rows (2r, 2r+1) as re/im.
-template <class T, class SRC>
+template <class T, class SRC, int NF = 0>
 __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, typename Cx<T>::type* __restrict__ out, Dims d,
                                                   FFTPlan pz, const typename Cx<T>::type* __restrict__ tw, int RB) {
   typedef typename Cx<T>::type C;
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, ty
     if (rb < d.rows) vb = (T)in[rb * nz + k];
     b0[r * LP + k] = mk<T>(va, vb);
   }
-  C* res = block_fft<-1, T>(b0, b1, RB, LP, pz, tw);
+  C* res = block_fft_nf<-1, T, NF>(b0, b1, RB, LP, pz, tw);
   const int nzc = d.nzc;
   for (int e = threadIdx.x; e < RB * nzc; e += blockDim.x) {
     const int r = e / nzc, k = e - r * nzc;
@@ -167,7 +167,7 @@ __device__ __forceinline__ typename Cx<T>::type pair_spectrum(const typename Cx<
 }
 
 // z-axis c2r: half spectra rows to real rows (DST = double or T), times scale.
-template <class T, class DST>
+template <class T, class DST, int NF = 0>
 __global__ void __launch_bounds__(256) k_rows_c2r(const typename Cx<T>::type* __restrict__ in, DST* __restrict__ out, Dims d,
                                                   FFTPlan pz, const typename Cx<T>::type* __restrict__ tw, int RB, T scale) {
   typedef typename Cx<T>::type C;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r(const typename Cx<T>::type* __
     const C* B = rb < d.rows ? in + rb * d.pz : nullptr;
     b0[r * LP + k] = pair_spectrum<T>(A, B, k, nz);
   }
-  C* res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
+  C* res = block_fft_nf<+1, T, NF>(b0, b1, RB, LP, pz, tw);
   for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
     const int r = e / nz, k = e - r * nz;
     const long ra = 2 * (pair0 + r), rb = ra + 1;
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(256) k_hess_rows(typename Cx<T>::type* __restr
 // Last step of the Hessian-vector product: c2r of E (FMT + mean-field
 // back-convolution of the Lambda fields) and the ideal-gas term,
 //   Hv = (v / rho + c2r(E)) dV   (DFT::matrix_dot_v_intern, src/DFT.cpp:455-462).
-template <class T, class RT>
+template <class T, class RT, int NF = 0>
 __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::type* __restrict__ E, const double* __restrict__ rho,
                                                          const RT* __restrict__ v, RT* __restrict__ out, Dims d, FFTPlan pz,
                                                          const typename Cx<T>::type* __restrict__ tw, int RB, double dV, int have_fmt_or_mf) {
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
       const C* Br = rb < d.rows ? E + rb * d.pz : nullptr;
       b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
-    res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
+    res = block_fft_nf<+1, T, NF>(b0, b1, RB, LP, pz, tw);
   }
   const T dVt = (T)dV;
   for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
 //   dF = ln(rho) dV + c2r(E) dV + V_ext dV - mu dV
 // with FP64 partial sums: F_id = sum (rho ln rho - rho) dV, sum rho,
 // sum V_ext rho, sum dF rho (for the fixed-mass projection).
-template <class T, class RT = double>
+template <class T, class RT = double, int NF = 0>
 __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* __restrict__ E, const RT* __restrict__ rho,
                                                     const double* __restrict__ vext, RT* __restrict__ dF, Dims d, FFTPlan pz,
                                                     const typename Cx<T>::type* __restrict__ tw, int RB, double dV, double mu,
@@ -541,7 +541,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
       const C* Br = rb < d.rows ? E + rb * d.pz : nullptr;
       b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
-    res = block_fft<+1, T>(b0, b1, RB, LP, pz, tw);
+    res = block_fft_nf<+1, T, NF>(b0, b1, RB, LP, pz, tw);
   }
   // Pointwise terms in the bulk precision T (FP64 in FP64 mode); each thread
   // keeps Kahan partials in T over its few points, merged in FP64 across the

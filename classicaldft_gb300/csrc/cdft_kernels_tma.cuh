@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(c
   C S[PER];
 #pragma unroll
   for (int j = 0; j < PER; ++j) S[j] = mk<T>(0, 0);
-  double pars = 0.0;
+  KahanT<T> pars;  // the mean-field energy by Parseval: compensated in the bulk precision, merged in FP64
   bool ok = true;
   for (int a = 0; a < nsrc; ++a) {
     const int b = a & 1;
@@ -421,8 +421,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(c
           const int col = col0 + (e % TC);
           const int kz = col % d.pz;
           if (kz < d.nzc && col < d.ny * d.pz) {
-            const double mult = (kz == 0 || 2 * kz == d.nz) ? 1.0 : 2.0;
-            pars += mult * ((double)z.x * (double)z.x + (double)z.y * (double)z.y) * (double)wv;
+            const T mult = (kz == 0 || 2 * kz == d.nz) ? (T)1 : (T)2;
+            pars.add(mult * (z.x * z.x + z.y * z.y) * wv);
           }
         }
       }
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(c
   if (part) {
     Acc acc;
     acc.init();
-    acc.add(pars);
+    acc.add(pars.value());
     block_reduce_store<1>(&acc, part, blockIdx.x);
   }
   if (!__syncthreads_and(ok)) {
@@ -485,7 +485,8 @@ __global__ void __launch_bounds__(PhiThreads<T>::value) k_phi_rows_tma(const __g
   constexpr int E = ElemsPerComplex<T>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* sm = aligned_smem(smem_raw);
-  const int nz = d.nz, nzc = d.nzc, pz = d.pz;
+  // with a compile-time plan the row length is a constant too (the divisions below fold)
+  const int nz = NF > 0 ? NF : d.nz, nzc = NF > 0 ? NF / 2 + 1 : d.nzc, pz = d.pz;
   const size_t in_bytes = (size_t)M * RB * pz * sizeof(C), ib = r128(in_bytes);
   const size_t zb = r128((size_t)nz * LPd * sizeof(C));
   C* In[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + ib)};

@@ -117,3 +117,19 @@ def solve(points, tol=1e-8, max_steps=-1, mixed=True, switch_tol=2e-6, **kw):
     ctxs = build_contexts(points, **kw)
     reps, status = fire_run_batch(ctxs, tol, max_steps=max_steps, mixed=mixed, switch_tol=switch_tol)
     return ctxs, reps, status
+
+
+def shard(points, rank, world):
+    """Replicas-only split of a sweep over `world` GPUs: longest-processing-time
+    greedy on the grid cost N^3 log N (largest first, each to the least-loaded
+    rank, ties to the lowest rank). Deterministic; every point lands on exactly
+    one rank. Returns the indices of `rank`'s points, in sweep order."""
+    cost = [p["n"] ** 3 * math.log2(p["n"]) for p in points]
+    order = sorted(range(len(points)), key=lambda i: (-cost[i], i))
+    load = [0.0] * world
+    owner = [0] * len(points)
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        owner[i] = r
+        load[r] += cost[i]
+    return [i for i in range(len(points)) if owner[i] == rank]
