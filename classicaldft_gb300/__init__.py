@@ -33,7 +33,7 @@ C_FUNCTIONS = [
     "cdft_get_weights", "cdft_fire_default_params", "cdft_fire_init", "cdft_fire_step", "cdft_fire_run",
     "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device", "cdft_find_coex",
     "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates", "cdft_hessian_dot_v",
-    "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex",
+    "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex", "cdft_ddft_matrix_dot_v",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -127,6 +127,7 @@ def lib():
             "cdft_fire_run_batch": ([P(vp), i, d, d, ctypes.c_long, i, P(FireReport), P(i)], i),
             "cdft_autotune": ([vp, i, P(i), dp], i),
             "cdft_hessian_dot_v": ([vp, vp, vp, i], i),
+            "cdft_ddft_matrix_dot_v": ([vp, vp, vp, i], i),
             "cdft_newton_refine": ([vp, d, i, i, d, P(NewtonReport)], i),
             "cdft_tc_gemm_bf16": ([vp, vp, vp, vp, vp, vp, ctypes.c_long, i, i, i, vp, vp], i),
             "cdft_newton_refine_ex": ([vp, d, P(NewtonParams), P(NewtonReport)], i),
@@ -332,6 +333,13 @@ class Context:
         a = np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape)
         o = np.empty(self.shape)
         self._check(lib().cdft_hessian_dot_v(self._h, a.ctypes.data_as(ctypes.c_void_p), o.ctypes.data_as(ctypes.c_void_p), 0))
+        return o
+
+    def ddft_matrix_dot_v(self, v):
+        """DDFT dynamical matrix times v, g . (H v), at the current density (DDFT::matrix_dot_v1)."""
+        a = np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape)
+        o = np.empty(self.shape)
+        self._check(lib().cdft_ddft_matrix_dot_v(self._h, a.ctypes.data_as(ctypes.c_void_p), o.ctypes.data_as(ctypes.c_void_p), 0))
         return o
 
     # FFT plans

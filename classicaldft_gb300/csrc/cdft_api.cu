@@ -610,28 +610,83 @@ int cdft_get_chem_potential(const cdft_ctx* c, double* mu) {
 // src/DFT.cpp:435-488; FMT::add_second_derivative src/FMT.cpp:437-567;
 // Interaction_Base::add_second_derivative src/Interaction.cpp:119-147), at the
 // context's current density.
-int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
-  if (!c || !v || !out) return CDFT_ERR_ARG;
+// DDFT::g_dot_x (src/DDFT.cpp:320-351), forward differences: the DDFT mobility
+// operator gx = sum_axes D [(rho+ + rho0)(x+ - x0) - (rho0 + rho-)(x0 - x-)], D = 1/(2 dx^2).
+__global__ void k_g_dot_x(const double* __restrict__ rho, const double* __restrict__ x, double* __restrict__ gx, int nx, int ny, int nz,
+                          double dx) {
+  const long N = (long)nx * ny * nz;
+  const double D = 1.0 / (2 * dx * dx);
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < N; p += (long)gridDim.x * blockDim.x) {
+    const int k = (int)(p % nz);
+    const long t = p / nz;
+    const int j = (int)(t % ny), i = (int)(t / ny);
+    auto at = [&](int a, int b, int c) -> long {
+      a = (a + nx) % nx; b = (b + ny) % ny; c = (c + nz) % nz;
+      return c + (long)nz * (b + (long)ny * a);
+    };
+    const long px = at(i + 1, j, k), mx = at(i - 1, j, k), py = at(i, j + 1, k), my = at(i, j - 1, k), pz = at(i, j, k + 1),
+               mz = at(i, j, k - 1);
+    const double x0 = x[p], d0 = rho[p];
+    double g = D * ((rho[px] + d0) * (x[px] - x0) - (d0 + rho[mx]) * (x0 - x[mx]));
+    g += D * ((rho[py] + d0) * (x[py] - x0) - (d0 + rho[my]) * (x0 - x[my]));
+    g += D * ((rho[pz] + d0) * (x[pz] - x0) - (d0 + rho[mz]) * (x0 - x[mz]));
+    gx[p] = g;
+  }
+}
+
+// H v between device arrays on the context's stream (asynchronous).
+static int hessian_device(cdft_ctx* c, const double* vd, double* od) {
+  int rc = c->precision == CDFT_FP64 ? c->e64->hess_prepare(c->rho, c->stream) : c->e32->hess_prepare(c->rho, c->stream);
+  if (!rc)
+    rc = c->precision == CDFT_FP64 ? c->e64->hess_apply<double>(vd, c->rho, od, c->info.dV, c->stream)
+                                   : c->e32->hess_apply<double>(vd, c->rho, od, c->info.dV, c->stream);
+  return rc ? fail(c, CDFT_ERR_CUDA, "Hessian launch failed") : CDFT_OK;
+}
+
+static int hessian_buffers(cdft_ctx* c) {
   int rc = ensure_evaluator(c, c->precision);
   if (rc) return rc;
   const size_t nb = c->info.N * sizeof(double);
   if (!c->hv_v && (cudaMalloc(&c->hv_v, nb) != cudaSuccess || cudaMalloc(&c->hv_out, nb) != cudaSuccess))
     return fail(c, CDFT_ERR_CUDA, "Hessian buffers");
+  return CDFT_OK;
+}
+
+int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
+  if (!c || !v || !out) return CDFT_ERR_ARG;
+  int rc = hessian_buffers(c);
+  if (rc) return rc;
+  const size_t nb = c->info.N * sizeof(double);
   const double* vd = v;
   double* od = on_device ? out : c->hv_out;
   if (!on_device) {
     CUDA_OR_FAIL(c, cudaMemcpyAsync(c->hv_v, v, nb, cudaMemcpyHostToDevice, c->stream));
     vd = c->hv_v;
   }
-  if (c->precision == CDFT_FP64) {
-    rc = c->e64->hess_prepare(c->rho, c->stream);
-    if (!rc) rc = c->e64->hess_apply<double>(vd, c->rho, od, c->info.dV, c->stream);
-  } else {
-    rc = c->e32->hess_prepare(c->rho, c->stream);
-    if (!rc) rc = c->e32->hess_apply<double>(vd, c->rho, od, c->info.dV, c->stream);
-  }
-  if (rc) return fail(c, CDFT_ERR_CUDA, "Hessian launch failed");
+  rc = hessian_device(c, vd, od);
+  if (rc) return rc;
   if (!on_device) CUDA_OR_FAIL(c, cudaMemcpyAsync(out, od, nb, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  return CDFT_OK;
+}
+
+// DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): g . (H v) at the current density.
+int cdft_ddft_matrix_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
+  if (!c || !v || !out) return CDFT_ERR_ARG;
+  int rc = hessian_buffers(c);
+  if (rc) return rc;
+  const size_t nb = c->info.N * sizeof(double);
+  // v (device) -> H v in hv_out -> g . (H v) in hv_v (v is no longer needed) or the caller's array
+  if (on_device) {
+    rc = hessian_device(c, v, c->hv_out);
+  } else {
+    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->hv_v, v, nb, cudaMemcpyHostToDevice, c->stream));
+    rc = hessian_device(c, c->hv_v, c->hv_out);
+  }
+  if (rc) return rc;
+  double* gd = on_device ? out : c->hv_v;
+  k_g_dot_x<<<grid_for(c->info.N), 256, 0, c->stream>>>(c->rho, c->hv_out, gd, c->p.nx, c->p.ny, c->p.nz, c->p.dx);
+  if (!on_device) CUDA_OR_FAIL(c, cudaMemcpyAsync(out, gd, nb, cudaMemcpyDeviceToHost, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   return CDFT_OK;
 }

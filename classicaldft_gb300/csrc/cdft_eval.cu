@@ -126,6 +126,37 @@ __global__ void k_finish_reduce(const double* __restrict__ part, long nblk, int 
   }
 }
 
+// All sums of one evaluation in one launch: warp w finishes sum w of the three
+// partial-sum segments (Phi: 1 value, mean field: 1, final rows: 4) — each lane
+// merges blocks lane, lane + 32, ... in order, then a fixed shuffle tree. Short,
+// independent FP64 chains per warp instead of three single-block kernels.
+struct FinishSeg {
+  const double* part;
+  long nblk;
+  int nv;
+  double* out;
+};
+__global__ void __launch_bounds__(192) k_finish_terms(FinishSeg s0, FinishSeg s1, FinishSeg s2) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const FinishSeg* segs[3] = {&s0, &s1, &s2};
+  int v = w;
+  const FinishSeg* sg = nullptr;
+  for (int i = 0; i < 3; ++i) {
+    if (segs[i]->nv <= 0 || !segs[i]->part) continue;
+    if (v < segs[i]->nv) { sg = segs[i]; break; }
+    v -= segs[i]->nv;
+  }
+  if (!sg) return;
+  Acc a;
+  a.init();
+  for (long b = lane; b < sg->nblk; b += 32) a.merge(sg->part[(b * sg->nv + v) * 2], sg->part[(b * sg->nv + v) * 2 + 1]);
+  for (int o = 16; o > 0; o >>= 1) {
+    const double s2 = __shfl_down_sync(0xffffffffu, a.s, o), c2 = __shfl_down_sync(0xffffffffu, a.c, o);
+    if (lane < o) a.merge(s2, c2);
+  }
+  if (lane == 0) sg->out[v] = a.s + a.c;
+}
+
 template <class T>
 __global__ void k_compact(const double2* __restrict__ full, T* __restrict__ out, long n, int odd, double scale) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -477,10 +508,10 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     mark(4);
     const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
     const unsigned gphi = (unsigned)nphi;
-    long phi_blocks = nphi;
+    phi_blocks_last_ = nphi;
     if (tma_phi_) {
       constexpr int RB = PhiRows<T>::value;
-      phi_blocks = grid_tphi_;
+      phi_blocks_last_ = grid_tphi_;
       switch (model_) {
         case MODEL_ROSENFELD: (fz_ ? k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 128> : k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
         case MODEL_RSLT: (fz_ ? k_phi_rows_tma<T, MODEL_RSLT, RB, 128> : k_phi_rows_tma<T, MODEL_RSLT, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
@@ -496,7 +527,6 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
       case MODEL_WHITEBEAR_I: k_phi_rows<T, MODEL_WHITEBEAR_I><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
       default: k_phi_rows<T, MODEL_WHITEBEAR_II><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
     }
-    k_finish_reduce<<<1, 256, 0, s>>>(part_phi, phi_blocks, 1, terms_ + 0);
     mark(5);
     yfwd(Cf_, mapYC_, M_, grid_tyM_);
     mark(6);
@@ -510,7 +540,6 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
                                                    mf_ ? part_mf : nullptr);
-    if (mf_) k_finish_reduce<<<1, 256, 0, s>>>(part_mf, gxb, 1, terms_ + 1);
     mark(7);
     yinv(E_, mapYE_, 1, grid_ty1_);
     mark(8);
@@ -521,7 +550,12 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   const unsigned gfin = (unsigned)grid_blocks_rows();
   (fz_ ? k_final_rows<T, RT, 128> : k_final_rows<T, RT, 0>)<<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_),
                                                                                          rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin);
-  k_finish_reduce<<<1, 256, 0, s>>>(part_fin, gfin, 4, terms_ + 2);
+  {
+    const FinishSeg sphi{part_phi, phi_blocks_last_, M_ > 0 ? 1 : 0, terms_ + 0};
+    const FinishSeg smf{part_mf, (long)gxb, mf_ ? 1 : 0, terms_ + 1};
+    const FinishSeg sfin{part_fin, (long)gfin, 4, terms_ + 2};
+    k_finish_terms<<<1, 192, 0, s>>>(sphi, smf, sfin);
+  }
   mark(9);
   return 0;
 }

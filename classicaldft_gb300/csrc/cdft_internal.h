@@ -112,6 +112,7 @@ class Evaluator {
   long part_len_ = 0;
   double* terms_ = nullptr;  // reduced sums: [0] sum Phi, [1] Parseval MF, [2] F_id, [3] sum rho, [4] sum V rho, [5] sum dF rho
   unsigned* status_ = nullptr;
+  long phi_blocks_last_ = 0;  // blocks of the last Phi launch (its partial sums)
   T* NA_ = nullptr;  // Hessian: M weighted densities of the state, real space (M x N)
   int rb_rows_ = 16, rb_phi_ = 4, tc_ = 16;
   size_t smem_rows_ = 0, smem_phi_ = 0, smem_colx_ = 0, smem_coly_ = 0, smem_xconv_ = 0, smem_xback_ = 0;

@@ -96,6 +96,36 @@ __device__ __forceinline__ void block_sum_store(double* v, double* out, long blo
   }
 }
 
+// FP64 <-> FP32 conversions on the integer pipes. GB300 runs F2F conversions
+// through its small FP64 unit, which made them the bottleneck of the row passes
+// that read the FP64 density and write the FP64 dF. Both are exact restatements
+// of IEEE round-to-nearest-even conversion for values in FP32's normal range;
+// zeros, subnormals, infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ float cvt_f32(double x) {
+  const unsigned long long d = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((d >> 52) & 0x7FF) - 1023 + 127;
+  if (e <= 0 || e >= 255) return (float)x;
+  unsigned int u = ((unsigned int)(d >> 63) << 31) | ((unsigned int)e << 23) | (unsigned int)((d >> 29) & 0x7FFFFFu);
+  const unsigned long long rest = d & 0x1FFFFFFFull;  // the 29 bits dropped
+  if (rest > 0x10000000ull || (rest == 0x10000000ull && (u & 1u))) u += 1u;  // a carry moves into the exponent correctly
+  return __uint_as_float(u);
+}
+__device__ __forceinline__ double cvt_f64(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) | ((unsigned long long)(e + 896u) << 52) |
+                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+// value of type D from type S: the integer-pipe conversions between FP64 and FP32, plain casts otherwise
+template <class D, class S>
+__device__ __forceinline__ D conv(S x) { return (D)x; }
+template <>
+__device__ __forceinline__ float conv<float, double>(double x) { return cvt_f32(x); }
+template <>
+__device__ __forceinline__ double conv<double, float>(float x) { return cvt_f64(x); }
+
 // Kahan-compensated running sum in the bulk precision (a thread's few points).
 template <class T>
 struct KahanT {
@@ -128,8 +158,8 @@ __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, ty
     const int r = e / nz, k = e - r * nz;
     const long ra = 2 * (pair0 + r), rb = ra + 1;
     T va = 0, vb = 0;
-    if (ra < d.rows) va = (T)in[ra * nz + k];
-    if (rb < d.rows) vb = (T)in[rb * nz + k];
+    if (ra < d.rows) va = conv<T>(in[ra * nz + k]);
+    if (rb < d.rows) vb = conv<T>(in[rb * nz + k]);
     b0[r * LP + k] = mk<T>(va, vb);
   }
   C* res = block_fft_nf<-1, T, NF>(b0, b1, RB, LP, pz, tw);
@@ -509,8 +539,8 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
       const C z = res[(rr >> 1) * LP + k];
       h = (rr & 1) ? z.y : z.x;
     }
-    const T f = ((T)v[p] / (T)rho[p]) * dVt + h * dVt;
-    out[p] = (RT)f;
+    const T f = (conv<T>(v[p]) / conv<T>(rho[p])) * dVt + h * dVt;
+    out[p] = conv<RT>(f);
   }
 }
 
@@ -529,7 +559,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
   typedef typename Cx<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
-  const int nz = d.nz, LP = nz + 1, nzc = d.nzc;
+  const int nz = NF > 0 ? NF : d.nz, LP = nz + 1, nzc = NF > 0 ? NF / 2 + 1 : d.nzc;
   C* b1 = b0 + RB * LP;
   const long pair0 = (long)blockIdx.x * RB;
   C* res = b0;
@@ -553,7 +583,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     const long row = 2 * pair0 + rr;
     if (row >= d.rows) continue;
     const long p = row * nz + k;
-    const T r0 = (T)rho[p];
+    const T r0 = conv<T>(rho[p]);
     const T lr = log(r0);
     T h = 0;
     if (have_fmt_or_mf) {
@@ -565,7 +595,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     f += h * dVt;
     f += ve * dVt;
     f += -mut * dVt;
-    dF[p] = (RT)f;
+    dF[p] = conv<RT>(f);
     if (ideal) ks[0].add((r0 * lr - r0) * dVt);
     ks[1].add(r0);
     ks[2].add(ve * r0);

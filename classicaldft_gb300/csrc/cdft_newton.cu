@@ -13,6 +13,7 @@
 #include <cmath>
 #include <vector>
 #include "cdft_ctx.h"
+#include "cdft_kernels.cuh"
 
 using namespace cdft;
 
@@ -40,41 +41,44 @@ __device__ void block_store(double* v, double* part) {
     }
 }
 
+// The vector passes keep FP32 (Kahan-compensated) per-thread sums and convert
+// FP64 <-> FP32 on the integer pipes: per-point FP64 arithmetic would run on
+// GB300's small FP64 unit. Block sums are FP64.
 __global__ void __launch_bounds__(kT) k_nk_init(const double* dF, float* r, float* dl, long n, double* part) {
-  double s = 0;
+  KahanT<float> s;
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
-    const float x = (float)(-dF[i]);
+    const float x = -conv<float>(dF[i]);
     r[i] = x;
     dl[i] = 0.f;
-    s += x;
+    s.add(x);
   }
-  double v[1] = {s};
+  double v[1] = {s.value()};
   block_store<1>(v, part);
 }
 __global__ void k_nk_shift(float* x, long n, float c) {
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) x[i] -= c;
 }
 // z = (rho/dV) r; sums: z
-__global__ void __launch_bounds__(kT) k_nk_precond(const float* r, const double* rho, float* z, long n, double idV, double* part) {
-  double s = 0;
+__global__ void __launch_bounds__(kT) k_nk_precond(const float* r, const double* rho, float* z, long n, float idV, double* part) {
+  KahanT<float> s;
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
-    const float x = (float)((double)r[i] * rho[i] * idV);
+    const float x = r[i] * conv<float>(rho[i]) * idV;
     z[i] = x;
-    s += x;
+    s.add(x);
   }
-  double v[1] = {s};
+  double v[1] = {s.value()};
   block_store<1>(v, part);
 }
 // z -= zshift; sums: r.z, r.r
 __global__ void __launch_bounds__(kT) k_nk_rz(const float* r, float* z, long n, float zshift, double* part) {
-  double a = 0, b = 0;
+  KahanT<float> a, b;
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
     const float zz = z[i] - zshift;
     z[i] = zz;
-    a += (double)r[i] * zz;
-    b += (double)r[i] * r[i];
+    a.add(r[i] * zz);
+    b.add(r[i] * r[i]);
   }
-  double v[2] = {a, b};
+  double v[2] = {a.value(), b.value()};
   block_store<2>(v, part);
 }
 __global__ void k_nk_p(float* p, const float* z, long n, float beta) {
@@ -82,12 +86,12 @@ __global__ void k_nk_p(float* p, const float* z, long n, float beta) {
 }
 // sums: q, p.q
 __global__ void __launch_bounds__(kT) k_nk_pq(const float* p, const float* q, long n, double* part) {
-  double a = 0, b = 0;
+  KahanT<float> a, b;
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
-    a += q[i];
-    b += (double)p[i] * q[i];
+    a.add(q[i]);
+    b.add(p[i] * q[i]);
   }
-  double v[2] = {a, b};
+  double v[2] = {a.value(), b.value()};
   block_store<2>(v, part);
 }
 __global__ void k_nk_update(float* dl, float* r, const float* p, const float* q, long n, float alpha, float qshift) {
@@ -98,16 +102,16 @@ __global__ void k_nk_update(float* dl, float* r, const float* p, const float* q,
 }
 // largest fraction of rho any point loses: max(-d/rho); sums slot holds the max
 __global__ void __launch_bounds__(kT) k_nk_loss(const double* rho, const float* dl, long n, double* part) {
-  double m = 0;
-  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) m = fmax(m, -(double)dl[i] / rho[i]);
-  __shared__ double sh[kT / 32];
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  float m = 0.f;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) m = fmaxf(m, -dl[i] / conv<float>(rho[i]));
+  __shared__ float sh[kT / 32];
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double x = 0;
-    for (int w = 0; w < kT / 32; ++w) x = fmax(x, sh[w]);
-    part[blockIdx.x] = x;
+    float x = 0.f;
+    for (int w = 0; w < kT / 32; ++w) x = fmaxf(x, sh[w]);
+    part[blockIdx.x] = (double)x;
   }
 }
 __global__ void k_nk_step(double* rho, const double* rho0, const float* dl, long n, double s) {
@@ -235,7 +239,7 @@ extern "C" int cdft_newton_refine_ex(cdft_ctx* c, double tol, const cdft_newton_
     if (!sums<1>(c, g, sm)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");
     if (fixed) k_nk_shift<<<g, kT, 0, s>>>(W->r, N, (float)(sm[0] / N));
     auto precond = [&](double* rz_rr) -> bool {
-      k_nk_precond<<<g, kT, 0, s>>>(W->r, c->rho, W->z, N, 1.0 / dV, W->part);
+      k_nk_precond<<<g, kT, 0, s>>>(W->r, c->rho, W->z, N, (float)(1.0 / dV), W->part);
       double zs[1];
       if (!sums<1>(c, g, zs)) return false;
       k_nk_rz<<<g, kT, 0, s>>>(W->r, W->z, N, fixed ? (float)(zs[0] / N) : 0.f, W->part);

@@ -102,6 +102,10 @@ int cdft_eval(cdft_ctx* ctx, int only_fex, double* terms, double* dF, int on_dev
  * reference uses the fundamental measures of the last evaluation: call
  * cdft_eval first for the same state). v and out hold N values. */
 int cdft_hessian_dot_v(cdft_ctx* ctx, const double* v, double* out, int on_device);
+/* DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): the DDFT dynamical matrix
+ * times v, g . (H v), with DDFT::g_dot_x's forward-difference mobility operator
+ * (src/DDFT.cpp:320-351), at the context's current density. */
+int cdft_ddft_matrix_dot_v(cdft_ctx* ctx, const double* v, double* out, int on_device);
 
 /* Times each pass of one evaluation in the current precision with CUDA events
  * on the context's stream (no reference counterpart; used by the benchmark's

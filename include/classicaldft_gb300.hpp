@@ -207,6 +207,21 @@ class DFT {
   FMT_Species* getSpecies(int) const { return s_; }
   double get_convergence_monitor() const { return s_->get_convergence_monitor(); }
 
+  // Dynamical_Matrix::matrix_dot_v1 (src/Dynamical_Matrix.cpp): the full Hessian of Omega
+  // (DFT::matrix_dot_v_intern, src/DFT.cpp:435-488) times v, at the current density.
+  void matrix_dot_v1(const std::vector<double>& v, std::vector<double>& result) {
+    push();
+    result.resize(v.size());
+    check(cdft_hessian_dot_v(context(), v.data(), result.data(), 0), ctx_);
+  }
+  // DFT::findCoex (src/DFT_Coex.cpp:159-196): coexisting vapour and liquid densities.
+  void findCoex(double xmax, double dx, double& x1, double& x2, double tol = 1e-8) {
+    double o[5];
+    check(cdft_find_coex(context(), xmax, dx, tol, o), ctx_);
+    x1 = o[0];
+    x2 = o[1];
+  }
+
   // GPU handle for the minimizers
   cdft_ctx* context() {
     if (!ctx_) {

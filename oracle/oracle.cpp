@@ -900,6 +900,32 @@ int orc_eval(orc_ctx* c, double* rho, double* dF, double* terms) { return eval(*
 
 void orc_hessian_dot_v(const orc_ctx* c, const double* rho, const double* v, double* out) { hessian_dot_v(*c, rho, v, out); }
 
+// DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): g . (H v), with DDFT::g_dot_x
+// (:320-351, forward differences): gx = sum_axes D [(rho+ + rho0)(x+ - x0) - (rho0 + rho-)(x0 - x-)], D = 1/(2 dx^2).
+void orc_ddft_matrix_dot_v(const orc_ctx* c, const double* rho, const double* v, double* out) {
+  const int nx = c->p.nx, ny = c->p.ny, nz = c->p.nz;
+  const long N = c->N;
+  std::vector<double> hv(N);
+  hessian_dot_v(*c, rho, v, hv.data());
+  const double D = 1.0 / (2 * c->p.dx * c->p.dx);
+  auto idx = [&](int i, int j, int k) { return (long)((k + nz) % nz) + (long)nz * (((j + ny) % ny) + (long)ny * ((i + nx) % nx)); };
+  const int off[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++)
+      for (int k = 0; k < nz; k++) {
+        const long p = idx(i, j, k);
+        const double x0 = hv[p], d0 = rho[p];
+        double g = 0;
+        for (int a = 0; a < 3; a++) {
+          const long pp = idx(i + off[a][0], j + off[a][1], k + off[a][2]);
+          const long pm = idx(i - off[a][0], j - off[a][1], k - off[a][2]);
+          g += D * ((rho[pp] + d0) * (hv[pp] - x0) - (d0 + rho[pm]) * (x0 - hv[pm]));
+        }
+        out[p] = g;
+      }
+}
+
 // DFT::mu_times_beta (src/DFT.cpp:58-71), Interaction_Base::Mu (src/Interaction.cpp:61-72)
 double orc_mu_times_beta(const orc_ctx* c, double rho) {
   Neumaier mu;

@@ -66,6 +66,8 @@ int orc_ddft(orc_ctx* c, double* rho, int nsteps, double dt, double dt_max,
 /* DFT::matrix_dot_v_intern with the full Hessian (src/DFT.cpp:435-488): out =
    (d2Omega/drho drho) . v in the reference's scaling, at the density rho. */
 void orc_hessian_dot_v(const orc_ctx* c, const double* rho, const double* v, double* out);
+/* DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): g_dot_x of the full Hessian times v. */
+void orc_ddft_matrix_dot_v(const orc_ctx* c, const double* rho, const double* v, double* out);
 
 /* FFT helpers exposed for tests: unnormalised r2c / c2r of an nx*ny*nz grid
    (complex stored interleaved, nx*ny*(nz/2+1) values). */

@@ -59,6 +59,7 @@ def lib():
         L.orc_c2r.argtypes = [ctypes.c_int] * 3 + [dp, dp]
         L.orc_fill_noise.argtypes = [dp, ctypes.c_long, d, d, ctypes.c_uint64]
         L.orc_hessian_dot_v.argtypes = [ctypes.c_void_p, dp, dp, dp]
+        L.orc_ddft_matrix_dot_v.argtypes = [ctypes.c_void_p, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -159,6 +160,14 @@ class Oracle:
         vv = np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape)
         out = np.zeros(self.shape)
         lib().orc_hessian_dot_v(self._c, _p(r), _p(vv), _p(out))
+        return out
+
+    def ddft_matrix_dot_v(self, rho, v):
+        """DDFT dynamical matrix times v: g_dot_x(H v) (DDFT::matrix_dot_v_intern)."""
+        r = np.ascontiguousarray(rho, dtype=np.float64).reshape(self.shape)
+        vv = np.ascontiguousarray(v, dtype=np.float64).reshape(self.shape)
+        out = np.zeros(self.shape)
+        lib().orc_ddft_matrix_dot_v(self._c, _p(r), _p(vv), _p(out))
         return out
 
     def mu_times_beta(self, rho):

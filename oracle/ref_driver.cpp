@@ -342,6 +342,11 @@ int main(int argc, char** argv) {
       S.dft->matrix_dot_v1(v, r, nullptr);
       put("hlj16.Hv", vec_of(r));
       put1("hlj16.hsd", S.hsd);
+      // DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): g . (H v), the DDFT dynamical matrix
+      DDFT ddft(S.dft, false);
+      DFT_Vec gr(N);
+      ddft.matrix_dot_v1(v, gr, nullptr);
+      put("hlj16.GHv", vec_of(gr));
     } else if (c == "eval_hs32") {
       System S = make_system(0.2, 32, "WhiteBearI", false, 1.0);
       fill_noise(*S.d, 0.7, 0.05, 20240601);

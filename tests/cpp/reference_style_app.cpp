@@ -1,9 +1,10 @@
 // A reference-style application (the call sequence of a classicalDFT app) built
 // against include/classicaldft_gb300.hpp: config 1 (hard spheres, WhiteBearI,
 // 32^3 at dx = 0.2, rho = 0.7 (1 + noise)), one evaluation, then FIRE2 steps.
-// Prints "Omega F_hs mu steps F_final" for the test to compare.
+// Prints "Omega F_hs mu steps F_final sum(Hv) sum|Hv|" for the test to compare.
 #include <cstdint>
 #include <cstdio>
+#include <vector>
 
 #include "classicaldft_gb300.hpp"
 
@@ -30,9 +31,17 @@ int main(int argc, char** argv) {
   species.setChemPotential(dft.mu_times_beta(0.7));
   double F = dft.calculateFreeEnergyAndDerivatives(false);
   double Fhs = dft.get_f_hs();
+  // Hessian . v at this density (DFT::matrix_dot_v1), v_i = 0.3 (2u - 1) from splitmix64(77)
+  std::vector<double> v(density.Ntot()), Hv;
+  uint64_t vs = 77;
+  for (auto& x : v) x = 0.3 * (2.0 * splitmix_uniform(vs) - 1.0);
+  dft.matrix_dot_v1(v, Hv);
+  double hsum = 0, habs = 0;
+  for (double x : Hv) { hsum += x; habs += x < 0 ? -x : x; }
   fireMinimizer2 fire(&dft);
   fire.setForceTerminationCriterion(0.0);
   fire.run(fire_steps);
-  std::printf("%.17g %.17g %.17g %ld %.17g\n", F, Fhs, species.getChemPotential(), fire.report().total_steps, fire.getF());
+  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g\n", F, Fhs, species.getChemPotential(), fire.report().total_steps, fire.getF(),
+              hsum, habs);
   return 0;
 }

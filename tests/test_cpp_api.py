@@ -40,3 +40,13 @@ def test_reference_style_app_runs_config1(tmp_path):
     fire = golden("fire_hs32")
     assert steps == 20
     assert abs(Ffin - fire["fire32.F"][19]) <= 1e-12 * abs(Ffin)
+    # Hessian . v through the C++ mirror, against the oracle at the same density
+    from oracle import pyoracle
+    shape = (32, 32, 32)
+    rho = pyoracle.fill_noise(shape, 0.7, 0.05, 20240601)
+    v = 0.3 * (pyoracle.fill_noise(shape, 1.0, 1.0, 77) - 1.0)
+    o = pyoracle.Oracle(32, 0.2, "WhiteBearI", hsd=1.0)
+    hv = o.hessian_dot_v(rho, v)
+    hsum, habs = float(out[5]), float(out[6])
+    assert abs(habs - np.abs(hv).sum()) <= 1e-11 * np.abs(hv).sum()
+    assert abs(hsum - hv.sum()) <= 1e-11 * np.abs(hv).sum()

@@ -89,3 +89,26 @@ def test_hessian_symmetric_and_derivative_of_dF(cd, oracle):
     fd = (dp - dm) / (2 * eps)
     assert np.max(np.abs(fd - hv)) <= 1e-7 * np.max(np.abs(hv))
     c.close()
+
+
+def test_ddft_dynamical_matrix_vs_reference(cd, oracle):
+    g = golden("hessian")
+    shape = (16, 16, 16)
+    c = cd.Context(shape, 0.1, cd.WHITEBEAR_I, hsd=float(g["hlj16.hsd"][0]), lj=True, kT=0.8)
+    rho = oracle.fill_noise(shape, 0.3, 0.1, 5)
+    c.set_density(rho)
+    out = c.ddft_matrix_dot_v(_v(oracle, shape))
+    ref = g["hlj16.GHv"].reshape(shape)
+    assert np.max(np.abs(out - ref)) <= 1e-12 * np.max(np.abs(ref))
+    # and at a size the golden does not cover, against the oracle
+    shape = (40, 36, 30)
+    c2 = cd.Context(shape, 0.1, cd.WHITEBEAR_I, hsd=float(g["hlj16.hsd"][0]), lj=True, kT=0.8)
+    rho = oracle.fill_noise(shape, 0.3, 0.2, 6)
+    v = _v(oracle, shape, 8) * rho
+    c2.set_density(rho)
+    out = c2.ddft_matrix_dot_v(v)
+    o = oracle.Oracle(shape, 0.1, "WhiteBearI", hsd=float(g["hlj16.hsd"][0]), lj=True, kT=0.8)
+    ref = o.ddft_matrix_dot_v(rho, v)
+    assert np.max(np.abs(out - ref)) <= 1e-12 * np.max(np.abs(ref))
+    c.close()
+    c2.close()

@@ -211,3 +211,14 @@ def test_hessian_is_the_derivative_of_dF(oracle):
     dm = o.eval(rho - eps * v)[2]
     fd = (dp - dm) / (2 * eps)
     assert np.max(np.abs(fd - hv)) <= 1e-8 * np.max(np.abs(hv))
+
+
+def test_ddft_dynamical_matrix_dot_v(oracle):
+    """DDFT::matrix_dot_v1 (g . H v) of the LJ fluid against the reference."""
+    g = golden("hessian")
+    shape = (16, 16, 16)
+    o = oracle.Oracle(16, 0.1, "WhiteBearI", hsd=float(g["hlj16.hsd"][0]), lj=True, kT=0.8)
+    rho = oracle.fill_noise(shape, 0.3, 0.1, 5)
+    out = o.ddft_matrix_dot_v(rho, _hess_v(oracle, shape))
+    ref = g["hlj16.GHv"].reshape(shape)
+    assert np.max(np.abs(out - ref)) <= 1e-13 * np.max(np.abs(ref))
