@@ -80,7 +80,7 @@ class FireReport(ctypes.Structure):
 
 class NewtonParams(ctypes.Structure):
     _fields_ = [("max_newton", ctypes.c_int), ("max_cg", ctypes.c_int), ("cg_rtol", ctypes.c_double),
-                ("eta_max", ctypes.c_double), ("fp32_above", ctypes.c_double)]
+                ("eta_max", ctypes.c_double), ("fp32_above", ctypes.c_double), ("host_cg", ctypes.c_int)]
 
 
 class NewtonReport(ctypes.Structure):
@@ -317,9 +317,9 @@ class Context:
         self._check(lib().cdft_fire_run_device(self._h, tol, switch_tol, max_steps, int(mixed), ctypes.byref(r)))
         return self._rep(r)
 
-    def newton_refine(self, tol, max_newton=12, max_cg=200, cg_rtol=1e-3, eta_max=0.1, fp32_above=1e-4):
+    def newton_refine(self, tol, max_newton=12, max_cg=200, cg_rtol=1e-3, eta_max=0.1, fp32_above=1e-4, host_cg=False):
         """Newton-Krylov refinement with FP32 Hessian products, FP32 then FP64 residuals (cdft_newton_refine_ex)."""
-        p = NewtonParams(max_newton, max_cg, cg_rtol, eta_max, fp32_above)
+        p = NewtonParams(max_newton, max_cg, cg_rtol, eta_max, fp32_above, int(host_cg))
         r = NewtonReport()
         self._check(lib().cdft_newton_refine_ex(self._h, tol, ctypes.byref(p), ctypes.byref(r)))
         return self._rep(r)

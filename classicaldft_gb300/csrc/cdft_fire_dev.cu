@@ -628,8 +628,8 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
     // Newton-Krylov from the current state: first the fast settings (loose CG while the
     // residual is large, FP32 residuals above 1e-4); if that stalls, again from the same
     // start with FP64 residuals and CG to 1e-3 throughout; then the mixed = 2 path.
-    cdft_newton_params fast{kNewtonMax3, kNewtonCg, kNewtonRtol, 0.1, 1e-4};
-    cdft_newton_params safe{kNewtonMax3, kNewtonCg, kNewtonRtol, 0.0, 0.0};
+    cdft_newton_params fast{kNewtonMax3, kNewtonCg, kNewtonRtol, 0.1, 1e-4, 0};
+    cdft_newton_params safe{2 * kNewtonMax3, kNewtonCg, kNewtonRtol, 0.0, 0.0, 0};  // slow, steady: allow more corrections
     rc = cdft_internal_newton_ensure(c);
     if (rc) return rc;
     cdft_internal_newton_save(c);

@@ -11,6 +11,7 @@
 // inverse of the ideal-gas block of H, rho/dV.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 #include "cdft_ctx.h"
 #include "cdft_kernels.cuh"
@@ -41,18 +42,18 @@ __device__ void block_store(double* v, double* part) {
     }
 }
 
-// The vector passes keep FP32 (Kahan-compensated) per-thread sums and convert
-// FP64 <-> FP32 on the integer pipes: per-point FP64 arithmetic would run on
-// GB300's small FP64 unit. Block sums are FP64.
+// The CG sums accumulate in FP64: the projections onto sum(d) = 0 subtract
+// means of nearly cancelling sums, and FP32 partial sums there left the hardest
+// state points of a sweep unconverged. Conversions run on the integer pipes.
 __global__ void __launch_bounds__(kT) k_nk_init(const double* dF, float* r, float* dl, long n, double* part) {
-  KahanT<float> s;
+  double s = 0;
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
     const float x = -conv<float>(dF[i]);
     r[i] = x;
     dl[i] = 0.f;
-    s.add(x);
+    s += conv<double>(x);
   }
-  double v[1] = {s.value()};
+  double v[1] = {s};
   block_store<1>(v, part);
 }
 __global__ void k_nk_shift(float* x, long n, float c) {
@@ -60,25 +61,26 @@ __global__ void k_nk_shift(float* x, long n, float c) {
 }
 // z = (rho/dV) r; sums: z
 __global__ void __launch_bounds__(kT) k_nk_precond(const float* r, const double* rho, float* z, long n, float idV, double* part) {
-  KahanT<float> s;
+  double s = 0;
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
     const float x = r[i] * conv<float>(rho[i]) * idV;
     z[i] = x;
-    s.add(x);
+    s += conv<double>(x);
   }
-  double v[1] = {s.value()};
+  double v[1] = {s};
   block_store<1>(v, part);
 }
 // z -= zshift; sums: r.z, r.r
 __global__ void __launch_bounds__(kT) k_nk_rz(const float* r, float* z, long n, float zshift, double* part) {
-  KahanT<float> a, b;
+  double a = 0, b = 0;
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
     const float zz = z[i] - zshift;
     z[i] = zz;
-    a.add(r[i] * zz);
-    b.add(r[i] * r[i]);
+    const double rd = conv<double>(r[i]);
+    a = fma(rd, conv<double>(zz), a);
+    b = fma(rd, rd, b);
   }
-  double v[2] = {a.value(), b.value()};
+  double v[2] = {a, b};
   block_store<2>(v, part);
 }
 __global__ void k_nk_p(float* p, const float* z, long n, float beta) {
@@ -86,12 +88,13 @@ __global__ void k_nk_p(float* p, const float* z, long n, float beta) {
 }
 // sums: q, p.q
 __global__ void __launch_bounds__(kT) k_nk_pq(const float* p, const float* q, long n, double* part) {
-  KahanT<float> a, b;
+  double a = 0, b = 0;
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
-    a.add(q[i]);
-    b.add(p[i] * q[i]);
+    const double qd = conv<double>(q[i]);
+    a += qd;
+    b = fma(conv<double>(p[i]), qd, b);
   }
-  double v[2] = {a.value(), b.value()};
+  double v[2] = {a, b};
   block_store<2>(v, part);
 }
 __global__ void k_nk_update(float* dl, float* r, const float* p, const float* q, long n, float alpha, float qshift) {
@@ -119,13 +122,138 @@ __global__ void k_nk_step(double* rho, const double* rho0, const float* dl, long
 }
 }  // namespace
 
+// ---- device-driven conjugate gradients: one CUDA graph whose WHILE node runs
+// the CG iterations with every scalar (alpha, beta, projections, the stopping
+// test) kept on the device, so an iteration has no host round trip. Each pass of
+// the body increments a counter that ends the loop after max_it + 2 passes
+// whatever the state, so the loop is bounded by construction.
+struct CgDev {
+  double rz, r0, eta, alpha, qshift, zshift, beta;
+  int it, done, upd, max_it, fixed, passes;
+  long N;
+};
+
+namespace {
+// FP64 tree over the NV block partials part[b * NV + j]; thread 0 gets the totals
+template <int NV>
+__device__ void fin_sums(const double* part, int nblk, double* tot) {
+  __shared__ double sh[NV][256];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double a = 0;
+    for (int b = threadIdx.x; b < nblk; b += 256) a += part[b * NV + j];
+    sh[j][threadIdx.x] = a;
+  }
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+#pragma unroll
+      for (int j = 0; j < NV; ++j) sh[j][threadIdx.x] += sh[j][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) tot[j] = sh[j][0];
+}
+
+__global__ void __launch_bounds__(256) k_cg_fin_pq(const double* part, int nblk, CgDev* st) {
+  if (st->done) return;
+  double t[2];
+  fin_sums<2>(part, nblk, t);
+  if (threadIdx.x) return;
+  const double qsum = t[0], pq = t[1];
+  if (!(pq > 0)) {  // not positive along p: stop; at the first iteration step along p itself
+    st->upd = st->it == 0 ? 1 : 0;
+    st->alpha = st->rz / fmax(fabs(pq), 1e-300);
+    st->qshift = 0;
+    if (st->upd) st->it = 1;
+    st->done = 1;
+  } else {
+    st->upd = 1;
+    st->alpha = st->rz / pq;
+    st->qshift = st->fixed ? qsum / (double)st->N : 0.0;
+  }
+}
+__global__ void k_cg_update(float* dl, float* r, const float* p, const float* q, long n, const CgDev* st) {
+  if (!st->upd) return;
+  const float alpha = (float)st->alpha, qs = (float)st->qshift;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
+    dl[i] += alpha * p[i];
+    r[i] -= alpha * (q[i] - qs);
+  }
+}
+__global__ void __launch_bounds__(kT) k_cg_precond(const float* r, const double* rho, float* z, long n, float idV, double* part, const CgDev* st) {
+  if (st->done) return;
+  double s = 0;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
+    const float x = r[i] * conv<float>(rho[i]) * idV;
+    z[i] = x;
+    s += conv<double>(x);
+  }
+  double v[1] = {s};
+  block_store<1>(v, part);
+}
+__global__ void __launch_bounds__(256) k_cg_fin_z(const double* part, int nblk, CgDev* st) {
+  if (st->done) return;
+  double t[1];
+  fin_sums<1>(part, nblk, t);
+  if (threadIdx.x == 0) st->zshift = st->fixed ? t[0] / (double)st->N : 0.0;
+}
+__global__ void __launch_bounds__(kT) k_cg_rz(const float* r, float* z, long n, double* part, const CgDev* st) {
+  if (st->done) return;
+  const float zshift = (float)st->zshift;
+  double a = 0, b = 0;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) {
+    const float zz = z[i] - zshift;
+    z[i] = zz;
+    const double rd = conv<double>(r[i]);
+    a = fma(rd, conv<double>(zz), a);
+    b = fma(rd, rd, b);
+  }
+  double v[2] = {a, b};
+  block_store<2>(v, part);
+}
+__global__ void __launch_bounds__(256) k_cg_fin_rz(const double* part, int nblk, CgDev* st) {
+  if (st->done) return;
+  double t[2];
+  fin_sums<2>(part, nblk, t);
+  if (threadIdx.x) return;
+  st->it += 1;
+  if (sqrt(t[1]) <= st->eta * st->r0 || st->it >= st->max_it) {
+    st->done = 1;
+  } else {
+    st->beta = t[0] / st->rz;
+    st->rz = t[0];
+  }
+}
+__global__ void k_cg_p(float* p, const float* z, long n, const CgDev* st) {
+  if (st->done) return;
+  const float beta = (float)st->beta;
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) p[i] = z[i] + beta * p[i];
+}
+__global__ void k_cg_tail(CgDev* st, cudaGraphConditionalHandle h) {
+  st->passes += 1;
+  cudaGraphSetConditional(h, (!st->done && st->passes < st->max_it + 2) ? 1u : 0u);
+}
+}  // namespace
+
 struct NewtonWork {
   float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dl = nullptr;
   double* rho0 = nullptr;
   double* start = nullptr;  // a saved starting density (cdft_internal_newton_save / _restore)
   double* part = nullptr;   // device, 3 x grid
   double* hpart = nullptr;  // pinned
+  CgDev* cg = nullptr;      // device CG state
+  CgDev* hcg = nullptr;     // pinned copy
+  cudaGraphExec_t cg_exec = nullptr;
+  unsigned cg_plan_gen = ~0u;
+  cudaStream_t cg_stream = nullptr;  // capture stream of the CG graph
+  bool cg_ok = true;                 // false: the graph could not be built; host-driven CG
   ~NewtonWork() {
+    if (cg_exec) cudaGraphExecDestroy(cg_exec);
+    if (cg_stream) cudaStreamDestroy(cg_stream);
+    cudaFree(cg);
+    cudaFreeHost(hcg);
     cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(dl); cudaFree(rho0); cudaFree(start); cudaFree(part);
     cudaFreeHost(hpart);
   }
@@ -152,12 +280,65 @@ int cdft_internal_newton_ensure(cdft_ctx* c) {
       cudaMalloc(&W->q, fb) != cudaSuccess || cudaMalloc(&W->dl, fb) != cudaSuccess ||
       cudaMalloc(&W->rho0, N * sizeof(double)) != cudaSuccess || cudaMalloc(&W->start, N * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&W->part, (size_t)g * 3 * sizeof(double)) != cudaSuccess ||
-      cudaMallocHost(&W->hpart, (size_t)g * 3 * sizeof(double)) != cudaSuccess) {
+      cudaMallocHost(&W->hpart, (size_t)g * 3 * sizeof(double)) != cudaSuccess || cudaMalloc(&W->cg, sizeof(CgDev)) != cudaSuccess ||
+      cudaMallocHost(&W->hcg, sizeof(CgDev)) != cudaSuccess || cudaStreamCreateWithFlags(&W->cg_stream, cudaStreamNonBlocking) != cudaSuccess) {
     cdft_internal_newton_free(c);
     return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton work arrays");
   }
   if (!c->e32->hess_ready() && c->e32->hess_prepare(c->rho, c->stream)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian buffers");
   return CDFT_OK;
+}
+
+// Builds (once per set of transform plans) the graph of the device-driven CG loop.
+static bool build_cg_graph(cdft_ctx* c) {
+  NewtonWork* W = c->newton;
+  if (W->cg_exec && W->cg_plan_gen == c->plan_gen) return true;
+  if (W->cg_exec) cudaGraphExecDestroy(W->cg_exec);
+  W->cg_exec = nullptr;
+  const long N = c->info.N;
+  const double dV = c->info.dV;
+  const unsigned g = grid_of(N);
+  cudaGraph_t graph = nullptr;
+  if (cudaGraphCreate(&graph, 0) != cudaSuccess) return false;
+  cudaGraphConditionalHandle h;
+  bool ok = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  alignas(cudaGraphNodeParams) unsigned char npb[sizeof(cudaGraphNodeParams)];  // zero-initialised, as the API requires
+  std::memset(npb, 0, sizeof(npb));
+  cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(npb);
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  ok = ok && cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np) == cudaSuccess;
+  if (ok) {
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    cudaStream_t s = W->cg_stream;
+    ok = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      bool launch_ok = c->e32->hess_apply<float>(W->p, c->rho, W->q, dV, s) == 0;
+      k_nk_pq<<<g, kT, 0, s>>>(W->p, W->q, N, W->part);
+      k_cg_fin_pq<<<1, 256, 0, s>>>(W->part, (int)g, W->cg);
+      k_cg_update<<<g, kT, 0, s>>>(W->dl, W->r, W->p, W->q, N, W->cg);
+      k_cg_precond<<<g, kT, 0, s>>>(W->r, c->rho, W->z, N, (float)(1.0 / dV), W->part, W->cg);
+      k_cg_fin_z<<<1, 256, 0, s>>>(W->part, (int)g, W->cg);
+      k_cg_rz<<<g, kT, 0, s>>>(W->r, W->z, N, W->part, W->cg);
+      k_cg_fin_rz<<<1, 256, 0, s>>>(W->part, (int)g, W->cg);
+      k_cg_p<<<g, kT, 0, s>>>(W->p, W->z, N, W->cg);
+      k_cg_tail<<<1, 1, 0, s>>>(W->cg, h);
+      cudaGraph_t captured = nullptr;
+      ok = cudaStreamEndCapture(s, &captured) == cudaSuccess && launch_ok;
+    }
+  }
+  ok = ok && cudaGraphInstantiate(&W->cg_exec, graph, 0) == cudaSuccess;
+  cudaGraphDestroy(graph);
+  cudaGetLastError();  // a failed build falls back to host-driven CG; clear its error
+  if (!ok) {
+    W->cg_exec = nullptr;
+    return false;
+  }
+  W->cg_plan_gen = c->plan_gen;
+  return true;
 }
 
 // Saves / restores the context's density (a Newton run that stalls is retried from the same start).
@@ -188,6 +369,7 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
   p.cg_rtol = cg_rtol;
   p.eta_max = 0.1;
   p.fp32_above = 1e-4;
+  p.host_cg = 0;
   return cdft_newton_refine_ex(c, tol, &p, rep);
 }
 
@@ -250,10 +432,28 @@ extern "C" int cdft_newton_refine_ex(cdft_ctx* c, double tol, const cdft_newton_
     cudaMemcpyAsync(W->p, W->z, N * sizeof(float), cudaMemcpyDeviceToDevice, s);
     double rz = rz_rr[0];
     const double r0 = std::sqrt(rz_rr[1]);
+    bool max_cg_done = false;  // the device-driven loop ran the CG iterations
     // forcing term: a loose linear solve while the residual is large (inexact Newton)
     const double eta = eta_max > 0 ? std::max(cg_rtol, std::min(eta_max, resid)) : cg_rtol;
     int it = 0;
-    for (; it < max_cg; ++it) {
+    const bool use_graph = !prm->host_cg && W->cg_ok && (build_cg_graph(c) || (W->cg_ok = false));
+    if (use_graph) {
+      CgDev& hc = *W->hcg;
+      std::memset(&hc, 0, sizeof(CgDev));
+      hc.rz = rz;
+      hc.r0 = r0;
+      hc.eta = eta;
+      hc.max_it = max_cg;
+      hc.fixed = fixed ? 1 : 0;
+      hc.N = N;
+      cudaMemcpyAsync(W->cg, W->hcg, sizeof(CgDev), cudaMemcpyHostToDevice, s);
+      if (cudaGraphLaunch(W->cg_exec, s) != cudaSuccess) return cdft_internal_fail(c, CDFT_ERR_CUDA, "CG graph launch failed");
+      cudaMemcpyAsync(W->hcg, W->cg, sizeof(CgDev), cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cdft_internal_fail(c, CDFT_ERR_CUDA, "CG graph failed");
+      it = W->hcg->it;
+      max_cg_done = true;
+    }
+    for (; !max_cg_done && it < max_cg; ++it) {
       if (c->e32->hess_apply<float>(W->p, c->rho, W->q, dV, s)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian product failed");
       k_nk_pq<<<g, kT, 0, s>>>(W->p, W->q, N, W->part);
       double pq[2];

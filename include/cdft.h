@@ -243,10 +243,11 @@ int cdft_newton_refine(cdft_ctx* ctx, double resid_tol, int max_newton, int max_
  * of a correction max(cg_rtol, min(eta_max, resid)) (loose while the residual is
  * large); 0 keeps cg_rtol. Residuals above fp32_above come from FP32
  * evaluations (0: FP64 throughout). cdft_newton_refine uses eta_max = 0.1,
- * fp32_above = 1e-4. */
+ * fp32_above = 1e-4, host_cg = 0. */
 typedef struct cdft_newton_params {
   int max_newton, max_cg;
   double cg_rtol, eta_max, fp32_above;
+  int host_cg; /* 1: drive the CG iterations from the host instead of the device graph */
 } cdft_newton_params;
 int cdft_newton_refine_ex(cdft_ctx* ctx, double resid_tol, const cdft_newton_params* p, cdft_newton_report* rep);
 
