@@ -214,8 +214,9 @@ class Context:
 
     def set_density(self, rho):
         """rho: numpy array (host) or an object with data_ptr() (a CUDA tensor, float64, contiguous)."""
-        if hasattr(rho, "data_ptr"):
-            self._check(lib().cdft_set_density(self._h, ctypes.c_void_p(rho.data_ptr()), 1))
+        if hasattr(rho, "data_ptr"):  # a torch tensor: device, or (pinned) host memory
+            on_dev = 1 if getattr(rho, "is_cuda", True) else 0
+            self._check(lib().cdft_set_density(self._h, ctypes.c_void_p(rho.data_ptr()), on_dev))
         else:
             a = np.ascontiguousarray(rho, dtype=np.float64)
             assert a.size == self.N
@@ -246,10 +247,12 @@ class Context:
 
     def eval(self, want_dF=True, only_fex=False, dF_out=None):
         """One F+dF evaluation. Returns (terms dict, dF numpy array or None).
-        dF_out may be a CUDA tensor (float64, N elements) to receive dF on the device."""
+        dF_out may be a torch float64 tensor of N elements: a CUDA tensor receives dF on the
+        device, a (pinned) CPU tensor on the host."""
         t = np.zeros(8)
-        if dF_out is not None:
-            code = lib().cdft_eval(self._h, int(only_fex), _dptr(t), ctypes.c_void_p(dF_out.data_ptr()), 1)
+        if dF_out is not None:  # a torch tensor: device, or (pinned) host memory
+            on_dev = 1 if getattr(dF_out, "is_cuda", True) else 0
+            code = lib().cdft_eval(self._h, int(only_fex), _dptr(t), ctypes.c_void_p(dF_out.data_ptr()), on_dev)
             dF = None
         elif want_dF:
             dF = np.empty(self.shape)

@@ -182,14 +182,15 @@ def coarse_seed(shape_fine, dx, rho_v, rho_l, R, width=0.5, factor=4):
     return droplet(n, dx * factor, rho_v, rho_l, R, width)
 
 
-def predict(model, seed_coarse, kT, shape, device="cuda"):
-    """Warm-start density (numpy FP64) for the fine grid."""
+def predict(model, seed_coarse, kT, shape, device="cuda", on_device=False):
+    """Warm-start density for the fine grid: numpy FP64, or (on_device) a CUDA FP64
+    tensor that Context.set_density takes without a host round trip."""
     with torch.no_grad():
         f, up = features(seed_coarse, kT, shape, device)
         out = model(f, shape)
-        rho = up.reshape(-1) * torch.exp(out)
+        rho = (up.reshape(-1) * torch.exp(out)).reshape(shape).double()
     check_status()
-    return rho.reshape(shape).double().cpu().numpy()
+    return rho if on_device else rho.cpu().numpy()
 
 
 def train(model, samples, shape, steps=300, lr=3e-3, device="cuda", log=None):
