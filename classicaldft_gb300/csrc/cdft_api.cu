@@ -291,6 +291,7 @@ struct FDdftDev {
   }
 };
 
+constexpr long kRedPartLen = 152 * 8 * 16;  // doubles in red_part: 16 per block of the largest grid_for grid
 unsigned grid_for(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + 255) / 256, 152 * 8)); }
 
 }  // namespace
@@ -364,11 +365,18 @@ static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
     cudaGraph_t g;
     CUDA_OR_FAIL(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     int rc;
-    if (c->precision == CDFT_FP64) rc = c->e64->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s);
-    else rc = c->e32->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s);
-    const unsigned gr = grid_for(N);
-    k_dF_norms<<<gr, 256, 0, s>>>(c->dF, N, c->red_part);
-    k_dF_norms_finish<<<1, 256, 0, s>>>(c->red_part, (int)gr, c->red_out);
+    // the final row pass stores the dF-norm partials itself when they fit red_part
+    const long fb = c->precision == CDFT_FP64 ? c->e64->final_blocks() : c->e32->final_blocks();
+    double* nrm = 2 * fb <= kRedPartLen ? c->red_part : nullptr;
+    if (c->precision == CDFT_FP64) rc = c->e64->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s, nullptr, nrm);
+    else rc = c->e32->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s, nullptr, nrm);
+    if (nrm) {
+      k_dF_norms_finish<<<1, 256, 0, s>>>(c->red_part, (int)fb, c->red_out);
+    } else {
+      const unsigned gr = grid_for(N);
+      k_dF_norms<<<gr, 256, 0, s>>>(c->dF, N, c->red_part);
+      k_dF_norms_finish<<<1, 256, 0, s>>>(c->red_part, (int)gr, c->red_out);
+    }
     const double* dterms = c->precision == CDFT_FP64 ? c->e64->dev_terms() : c->e32->dev_terms();
     const unsigned* dst = c->precision == CDFT_FP64 ? c->e64->dev_status() : c->e32->dev_status();
     cudaMemcpyAsync(c->host_out, dterms, 8 * sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -505,7 +513,7 @@ int cdft_create(const cdft_params* p, cdft_ctx** out) {
   }
   const long N = c->info.N;
   if (cudaMalloc(&c->rho, N * sizeof(double)) != cudaSuccess || cudaMalloc(&c->dF, N * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&c->red_part, (size_t)152 * 8 * 16 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->red_part, (size_t)kRedPartLen * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->red_out, 16 * sizeof(double)) != cudaSuccess || cudaMallocHost(&c->host_out, 16 * sizeof(double)) != cudaSuccess)
     return CDFT_ERR_CUDA;
   cudaMemset(c->rho, 0, N * sizeof(double));

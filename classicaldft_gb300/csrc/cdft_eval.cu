@@ -317,7 +317,7 @@ bool Evaluator<T>::setup_tma(std::string* err) {
     uint64_t dims[3] = {(uint64_t)pz_ * E, (uint64_t)rows_, (uint64_t)M_};
     uint64_t str[2] = {(uint64_t)pz_ * cb, (uint64_t)Nc_ * cb};
     uint32_t box[3] = {(uint32_t)(pz_ * E), (uint32_t)RB, (uint32_t)M_};
-    smem_tphi_ = 2 * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L + 1) * cb) + 1024;
+    smem_tphi_ = PhiBufs<T>::value * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L + 1) * cb) + 1024;
     if (smem_tphi_ <= 220 * 1024 && encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) {
       auto set_phi = [&](auto kern) {
         raise_smem(kern, smem_tphi_);
@@ -465,7 +465,8 @@ void Evaluator<T>::c2r(const C* in, double* out, T scale, cudaStream_t s) {
 
 template <class T>
 template <class RT>
-int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, double mu, int ideal, cudaStream_t s, cudaEvent_t* ev) {
+int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, double mu, int ideal, cudaStream_t s, cudaEvent_t* ev,
+                         double* nrm) {
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
   };
@@ -549,7 +550,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   }
   const unsigned gfin = (unsigned)grid_blocks_rows();
   (fz_ ? k_final_rows<T, RT, 128> : k_final_rows<T, RT, 0>)<<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_),
-                                                                                         rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin);
+                                                                                         rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin, nrm);
   {
     const FinishSeg sphi{part_phi, phi_blocks_last_, M_ > 0 ? 1 : 0, terms_ + 0};
     const FinishSeg smf{part_mf, (long)gxb, mf_ ? 1 : 0, terms_ + 1};
@@ -700,7 +701,8 @@ int Evaluator<T>::eval(const double* rho, const double* vext, double* dF, double
 
 template class Evaluator<float>;
 template class Evaluator<double>;
-template int Evaluator<float>::launch<float>(const float*, const double*, float*, double, double, int, cudaStream_t, cudaEvent_t*);
+template int Evaluator<float>::launch<float>(const float*, const double*, float*, double, double, int, cudaStream_t, cudaEvent_t*,
+                                             double*);
 template int Evaluator<float>::hess_apply<float>(const float*, const double*, float*, double, cudaStream_t);
 template int Evaluator<float>::hess_apply<double>(const double*, const double*, double*, double, cudaStream_t);
 template int Evaluator<double>::hess_apply<double>(const double*, const double*, double*, double, cudaStream_t);

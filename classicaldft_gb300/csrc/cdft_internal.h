@@ -56,12 +56,16 @@ class Evaluator {
   // Launches the pass sequence without host synchronisation; partial sums land in dev_terms.
   // ev (optional, 10 events) are recorded before pass 0 and after each of the 9 passes.
   // RT: storage type of rho and dF (double, or T for an all-T pipeline).
+  // nrm (optional, 2 * final_blocks() doubles): the final row pass also stores
+  // per block (sum dF^2, max |dF|) there, the partials k_dF_norms would make.
   template <class RT>
-  int launch(const RT* rho, const double* vext, RT* dF, double dV, double mu, int ideal, cudaStream_t s, cudaEvent_t* ev = nullptr);
+  int launch(const RT* rho, const double* vext, RT* dF, double dV, double mu, int ideal, cudaStream_t s, cudaEvent_t* ev = nullptr,
+             double* nrm = nullptr);
   int launch(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, cudaStream_t s,
-             cudaEvent_t* ev = nullptr) {
-    return launch<double>(rho, vext, dF, dV, mu, ideal, s, ev);
+             cudaEvent_t* ev = nullptr, double* nrm = nullptr) {
+    return launch<double>(rho, vext, dF, dV, mu, ideal, s, ev, nrm);
   }
+  long final_blocks() const { return grid_blocks_rows(); }
   bool has_mf() const { return mf_; }
   // Hessian-vector products (DFT::matrix_dot_v_intern with the full Hessian):
   // hess_prepare stores the M weighted densities of the state rho0 in real

@@ -21,6 +21,7 @@
 #pragma once
 #include "cdft_fft.cuh"
 #include "cdft_phi.cuh"
+#include "cdft_convert.cuh"
 
 namespace cdft {
 
@@ -96,28 +97,6 @@ __device__ __forceinline__ void block_sum_store(double* v, double* out, long blo
   }
 }
 
-// FP64 <-> FP32 conversions on the integer pipes. GB300 runs F2F conversions
-// through its small FP64 unit, which made them the bottleneck of the row passes
-// that read the FP64 density and write the FP64 dF. Both are exact restatements
-// of IEEE round-to-nearest-even conversion for values in FP32's normal range;
-// zeros, subnormals, infinities and NaNs take the hardware conversion.
-__device__ __forceinline__ float cvt_f32(double x) {
-  const unsigned long long d = (unsigned long long)__double_as_longlong(x);
-  const int e = (int)((d >> 52) & 0x7FF) - 1023 + 127;
-  if (e <= 0 || e >= 255) return (float)x;
-  unsigned int u = ((unsigned int)(d >> 63) << 31) | ((unsigned int)e << 23) | (unsigned int)((d >> 29) & 0x7FFFFFu);
-  const unsigned long long rest = d & 0x1FFFFFFFull;  // the 29 bits dropped
-  if (rest > 0x10000000ull || (rest == 0x10000000ull && (u & 1u))) u += 1u;  // a carry moves into the exponent correctly
-  return __uint_as_float(u);
-}
-__device__ __forceinline__ double cvt_f64(float f) {
-  const unsigned int u = __float_as_uint(f);
-  const unsigned int e = (u >> 23) & 0xFFu;
-  if (e == 0u || e == 0xFFu) return (double)f;
-  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) | ((unsigned long long)(e + 896u) << 52) |
-                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)d);
-}
 // value of type D from type S: the integer-pipe conversions between FP64 and FP32, plain casts otherwise
 template <class D, class S>
 __device__ __forceinline__ D conv(S x) { return (D)x; }
@@ -138,6 +117,93 @@ struct KahanT {
   }
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
+
+// Block-wide merge of NV per-thread Kahan partials, stored like block_sum_store.
+// FP32 partials merge across the warp in FP32 with error-free sums (Knuth's
+// TwoSum: the rounding error of every merge goes into the compensation term),
+// so the small FP64 unit sees one conversion and one add per warp and value
+// instead of a conversion and five adds per thread. FP64 partials take the
+// plain FP64 path.
+template <int NV, class T>
+__device__ __forceinline__ void block_kahan_store(const KahanT<T>* ks, double* out, long block_id) {
+  if constexpr (sizeof(T) == 8) {
+    double v[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = ks[k].value();
+    block_sum_store<NV>(v, out, block_id);
+  } else {
+    __shared__ double red[32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      float s = ks[k].s, c = ks[k].c;  // value s - c
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_down_sync(0xffffffffu, s, o);
+        const float c2 = __shfl_down_sync(0xffffffffu, c, o);
+        const float t = s + s2;
+        const float bb = t - s;
+        const float e = (s - (t - bb)) + (s2 - bb);  // s + s2 = t + e exactly
+        c = (c + c2) - e;
+        s = t;
+      }
+      if (lane == 0) red[warp][k] = cvt_f64(s) - cvt_f64(c);
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+      const int k = threadIdx.x;
+      double t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][k];
+      out[(block_id * NV + k) * 2 + 0] = t;
+      out[(block_id * NV + k) * 2 + 1] = 0.0;
+    }
+  }
+}
+
+// Block-wide (sum of squares, max) of the per-thread partials q (Kahan) and
+// mx; thread 0 stores out[2 * block_id] = sum, out[2 * block_id + 1] = max,
+// the layout the dF-norm finish reads. FP32 partials merge in FP32 as in
+// block_kahan_store.
+template <class T>
+__device__ __forceinline__ void block_norms_store(const KahanT<T>& q, T mx, double* out, long block_id) {
+  __shared__ double red_s[32], red_m[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if constexpr (sizeof(T) == 8) {
+    double v = q.value();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_down_sync(0xffffffffu, v, o);
+      const double m2 = __shfl_down_sync(0xffffffffu, mx, o);
+      mx = m2 > mx ? m2 : mx;
+    }
+    if (lane == 0) { red_s[warp] = v; red_m[warp] = mx; }
+  } else {
+    float s = q.s, c = q.c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float s2 = __shfl_down_sync(0xffffffffu, s, o);
+      const float c2 = __shfl_down_sync(0xffffffffu, c, o);
+      const float m2 = __shfl_down_sync(0xffffffffu, mx, o);
+      const float t = s + s2;
+      const float bb = t - s;
+      const float e = (s - (t - bb)) + (s2 - bb);
+      c = (c + c2) - e;
+      s = t;
+      mx = m2 > mx ? m2 : mx;
+    }
+    if (lane == 0) { red_s[warp] = cvt_f64(s) - cvt_f64(c); red_m[warp] = cvt_f64(mx); }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0, m = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t += red_s[w];
+      m = red_m[w] > m ? red_m[w] : m;
+    }
+    out[2 * block_id] = t;
+    out[2 * block_id + 1] = m;
+  }
+}
 
 // Sums nblk partial (s, c) pairs of NV values in a fixed order: out[v] = total.
 __global__ void k_finish_reduce(const double* __restrict__ part, long nblk, int nv, double* __restrict__ out);
@@ -425,8 +491,7 @@ __global__ void __launch_bounds__(256) k_phi_rows(typename Cx<T>::type* __restri
     }
   }
   if (st) atomicOr(status, st);
-  double pv = psum.value();
-  block_sum_store<1>(&pv, part, blockIdx.x);
+  block_kahan_store<1>(&psum, part, blockIdx.x);
   C* res2 = block_fft<-1, T>(other, res, L, LP, pz, tw);
   for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
     const int line = e / nzc, k = e - line * nzc;
@@ -555,7 +620,8 @@ template <class T, class RT = double, int NF = 0>
 __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* __restrict__ E, const RT* __restrict__ rho,
                                                     const double* __restrict__ vext, RT* __restrict__ dF, Dims d, FFTPlan pz,
                                                     const typename Cx<T>::type* __restrict__ tw, int RB, double dV, double mu,
-                                                    int have_fmt_or_mf, int ideal, double* __restrict__ part) {
+                                                    int have_fmt_or_mf, int ideal, double* __restrict__ part,
+                                                    double* __restrict__ nrm) {
   typedef typename Cx<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
@@ -577,6 +643,8 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
   // keeps Kahan partials in T over its few points, merged in FP64 across the
   // block and with compensation across blocks.
   KahanT<T> ks[4];
+  KahanT<T> kq;  // sum of dF^2 and max |dF| when nrm is set (the residual norms, fused here)
+  T mx = 0;
   const T dVt = (T)dV, mut = (T)mu;
   for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
     const int rr = e / nz, k = e - rr * nz;
@@ -584,7 +652,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     if (row >= d.rows) continue;
     const long p = row * nz + k;
     const T r0 = conv<T>(rho[p]);
-    const T lr = log(r0);
+    const T lr = ln_t<T>(r0);
     T h = 0;
     if (have_fmt_or_mf) {
       const C z = res[(rr >> 1) * LP + k];
@@ -600,9 +668,14 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     ks[1].add(r0);
     ks[2].add(ve * r0);
     ks[3].add(f * r0);
+    if (nrm) {
+      kq.add(f * f);
+      const T af = f < (T)0 ? -f : f;
+      mx = af > mx ? af : mx;
+    }
   }
-  double v[4] = {ks[0].value(), ks[1].value(), ks[2].value(), ks[3].value()};
-  block_sum_store<4>(v, part, blockIdx.x);
+  block_kahan_store<4>(ks, part, blockIdx.x);
+  if (nrm) block_norms_store<T>(kq, mx, nrm, blockIdx.x);
 }
 
 // ----------------------------------------------------------- pointwise ---

@@ -430,12 +430,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(c
     __syncthreads();
     if (threadIdx.x == 0 && a + 2 < nsrc) issue(a + 2, b);
   }
-  if (part) {
-    Acc acc;
-    acc.init();
-    acc.add(pars.value());
-    block_reduce_store<1>(&acc, part, blockIdx.x);
-  }
+  if (part) block_kahan_store<1>(&pars, part, blockIdx.x);
   if (!__syncthreads_and(ok)) {
     if (threadIdx.x == 0) bulk_wait_all();
     return;
@@ -471,9 +466,16 @@ namespace cdft {
 // threads per block of the fused Phi pass (512 threads with two blocks per SM
 // measured no faster in FP32 than 256)
 template <class T> struct PhiThreads { static constexpr int value = 256; };
+// input buffers of the fused Phi pass. One suffices when a group's compute
+// (two FFTs and the functional, ~10 us) outlasts its load (24 KB): the load of
+// the next group is issued as soon as the current one has been unpacked. In
+// FP32 that frees the shared memory for a third resident block per SM.
+template <class T> struct PhiBufs { static constexpr int value = sizeof(T) == 4 ? 1 : 2; };
+// minimum resident blocks the register allocation must allow
+template <class T> struct PhiMinBlocks { static constexpr int value = sizeof(T) == 4 ? 3 : 1; };
 
 template <class T, int MODEL, int RB, int NF = 0>
-__global__ void __launch_bounds__(PhiThreads<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
+__global__ void __launch_bounds__(PhiThreads<T>::value, PhiMinBlocks<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
                                                       Dims d, FFTPlan pz_plan, const typename Cx<T>::type* __restrict__ tw, T hsd, T esA,
                                                       T esB, double* __restrict__ part, unsigned* __restrict__ status) {
   typedef typename Cx<T>::type C;
@@ -489,14 +491,15 @@ __global__ void __launch_bounds__(PhiThreads<T>::value) k_phi_rows_tma(const __g
   const int nz = NF > 0 ? NF : d.nz, nzc = NF > 0 ? NF / 2 + 1 : d.nzc, pz = d.pz;
   const size_t in_bytes = (size_t)M * RB * pz * sizeof(C), ib = r128(in_bytes);
   const size_t zb = r128((size_t)nz * LPd * sizeof(C));
-  C* In[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + ib)};
-  C* Z0 = reinterpret_cast<C*>(sm + 2 * ib);
-  C* Z1 = reinterpret_cast<C*>(sm + 2 * ib + zb);
-  __shared__ __align__(8) uint64_t bar[2];
+  constexpr int NB = PhiBufs<T>::value;
+  C* In[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + (NB - 1) * ib)};
+  C* Z0 = reinterpret_cast<C*>(sm + NB * ib);
+  C* Z1 = reinterpret_cast<C*>(sm + NB * ib + zb);
+  __shared__ __align__(8) uint64_t bar[NB];
   const long ngroup = (d.rows + RB - 1) / RB;
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) mbar_init(&bar[b], 1);
     fence_mbar_init();
   }
   __syncthreads();
@@ -505,7 +508,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value) k_phi_rows_tma(const __g
     tma_load_3d(In[b], &mapR, 0, (int)(g * RB), 0, &bar[b]);
   };
   if (threadIdx.x == 0)
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NB; ++b) {
       const long g = blockIdx.x + (long)b * gridDim.x;
       if (g < ngroup) issue(g, b);
     }
@@ -515,8 +518,8 @@ __global__ void __launch_bounds__(PhiThreads<T>::value) k_phi_rows_tma(const __g
   for (long it = 0;; ++it) {
     const long g = blockIdx.x + it * gridDim.x;
     if (g >= ngroup) break;
-    const int b = (int)(it & 1);
-    ok = mbar_wait(&bar[b], (unsigned)((it >> 1) & 1), status);
+    const int b = (int)(it % NB);
+    ok = mbar_wait(&bar[b], (unsigned)((it / NB) & 1), status);
     if (!__syncthreads_and(ok)) break;
     const long row0 = g * RB;
     const C* in = In[b];
@@ -529,8 +532,8 @@ __global__ void __launch_bounds__(PhiThreads<T>::value) k_phi_rows_tma(const __g
       Z0[k * LPd + line] = pair_spectrum<T>(Arow, Brow, k, nz);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {  // In[b] consumed: bring the group after next
-      const long gn = g + 2L * gridDim.x;
+    if (threadIdx.x == 0) {  // In[b] consumed: bring the group NB steps ahead
+      const long gn = g + (long)NB * gridDim.x;
       if (gn < ngroup) issue(gn, b);
     }
     C* res = tfft<+1, T, L, LPd, NF, PhiThreads<T>::value>(Z0, Z1, pz_plan, tw);
@@ -566,8 +569,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value) k_phi_rows_tma(const __g
     __syncthreads();
   }
   if (st) atomicOr(status, st);
-  double pv = psum.value();
-  block_sum_store<1>(&pv, part, blockIdx.x);
+  block_kahan_store<1>(&psum, part, blockIdx.x);
   (void)E;
 }
 

@@ -16,6 +16,10 @@ template <int MODEL> struct ModelTraits { static constexpr bool tensor = MODEL >
 template <class T> __device__ __forceinline__ T log1m(T e);
 template <> __device__ __forceinline__ double log1m<double>(double e) { return log(1.0 - e); }
 template <> __device__ __forceinline__ float log1m<float>(float e) { return log1pf(-e); }
+// natural logarithm in the argument's own precision (logf for FP32, never a promotion to FP64)
+template <class T> __device__ __forceinline__ T ln_t(T x);
+template <> __device__ __forceinline__ double ln_t<double>(double x) { return log(x); }
+template <> __device__ __forceinline__ float ln_t<float>(float x) { return logf(x); }
 
 // f1, f2, f3 and first derivatives. Divisions are replaced by products with
 // g = 1/(1 - eta) and ie = 1/eta (two reciprocals per point): GB300 runs FP64
