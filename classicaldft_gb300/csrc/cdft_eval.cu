@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include "cdft_internal.h"
 #include "cdft_kernels.cuh"
 #include "cdft_kernels_tma.cuh"
@@ -22,6 +23,16 @@ namespace cdft {
 FFTTable::~FFTTable() {
   if (d64) cudaFree(d64);
   if (d32) cudaFree(d32);
+}
+
+// Calls f(std::integral_constant<int, NF>) with the compile-time plan length NF
+// of an axis (128, 256, or 0 for the runtime plan): the kernels are instantiated
+// once per length.
+template <class F>
+inline void with_nf(int nf, F&& f) {
+  if (nf == 128) f(std::integral_constant<int, 128>());
+  else if (nf == 256) f(std::integral_constant<int, 256>());
+  else f(std::integral_constant<int, 0>());
 }
 
 std::vector<int> default_radices(int n) {
@@ -297,9 +308,13 @@ bool Evaluator<T>::setup_tma(std::string* err) {
   raise_smem(k_xconv_tma<T, 0>, smem_tconv_);
   raise_smem(k_xbackconv_tma<T, 0>, smem_tback_);
   raise_smem(k_cols_y_tma<T, -1, 128>, smem_ty_);
+  raise_smem(k_cols_y_tma<T, -1, 256>, smem_ty_);
   raise_smem(k_cols_y_tma<T, +1, 128>, smem_ty_);
+  raise_smem(k_cols_y_tma<T, +1, 256>, smem_ty_);
   raise_smem(k_xconv_tma<T, 128>, smem_tconv_);
+  raise_smem(k_xconv_tma<T, 256>, smem_tconv_);
   raise_smem(k_xbackconv_tma<T, 128>, smem_tback_);
+  raise_smem(k_xbackconv_tma<T, 256>, smem_tback_);
   int nsm = 0, dev = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -309,36 +324,51 @@ bool Evaluator<T>::setup_tma(std::string* err) {
   grid_ty1_ = (int)std::min<long>((long)nx_ * ntile, (long)nsm * bps);
   grid_tyM_ = (int)std::min<long>((long)std::max(M_, 1) * nx_ * ntile, (long)nsm * bps);
   tma_ = true;
-  // fused Phi rows: one box of RB rows of all M fields, {pz*E, RB, M}
+  setup_phi_tma();
+  return true;
+}
+
+// The fused Phi pass: one box of RB rows of all M fields, {pz*E, RB, M}; RB
+// follows the z plan (fewer rows for 256-point rows, so that three blocks fit
+// an SM). Re-run whenever the z plan changes.
+template <class T>
+bool Evaluator<T>::setup_phi_tma() {
   tma_phi_ = false;
-  if (M_ > 0 && (long)pz_ * E <= 256) {
-    constexpr int RB = PhiRows<T>::value;
+  constexpr int E = ElemsPerComplex<T>::value;
+  if (!tma_ || M_ == 0 || (long)pz_ * E > 256) return false;
+  int nsm = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const uint64_t cb = sizeof(C);
+  bool ok = false;
+  with_nf(fz_, [&](auto nf_) {
+    constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
     const int NP = (M_ + 1) / 2, L = NP * RB;
     uint64_t dims[3] = {(uint64_t)pz_ * E, (uint64_t)rows_, (uint64_t)M_};
     uint64_t str[2] = {(uint64_t)pz_ * cb, (uint64_t)Nc_ * cb};
     uint32_t box[3] = {(uint32_t)(pz_ * E), (uint32_t)RB, (uint32_t)M_};
     smem_tphi_ = PhiBufs<T>::value * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L + 1) * cb) + 1024;
-    if (smem_tphi_ <= 220 * 1024 && encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) {
-      auto set_phi = [&](auto kern) {
-        raise_smem(kern, smem_tphi_);
-        int b2 = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, PhiThreads<T>::value, smem_tphi_);
-        return std::max(b2, 1);
-      };
-      int bp;
-      switch (model_) {
-        case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 128>, smem_tphi_); break;
-        case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_RSLT, RB, 128>, smem_tphi_); break;
-        case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_ESFMT, RB, 128>, smem_tphi_); break;
-        case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 128>, smem_tphi_); break;
-        default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 0>); raise_smem(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 128>, smem_tphi_); break;
-      }
-      const long ngroup = (rows_ + RB - 1) / RB;
-      grid_tphi_ = (int)std::min<long>(ngroup, (long)nsm * bp);
-      tma_phi_ = true;
+    if (smem_tphi_ > 220 * 1024 || !encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) return;
+    auto set_phi = [&](auto kern) {
+      raise_smem(kern, smem_tphi_);
+      int b2 = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, PhiThreads<T>::value, smem_tphi_);
+      return std::max(b2, 1);
+    };
+    int bp;
+    switch (model_) {
+      case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF>); break;
+      case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF>); break;
+      case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF>); break;
+      case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF>); break;
+      default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF>); break;
     }
-  }
-  return true;
+    const long ngroup = (rows_ + RB - 1) / RB;
+    grid_tphi_ = (int)std::min<long>(ngroup, (long)nsm * bp);
+    ok = true;
+  });
+  tma_phi_ = ok;
+  return ok;
 }
 
 template <class T>
@@ -386,9 +416,13 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_final_rows<T, T>, smem_rows_);
   set_smem<T>(k_rows_r2c<T, T>, smem_rows_);
   set_smem<T>(k_final_rows<T, double, 128>, smem_rows_);
+  set_smem<T>(k_final_rows<T, double, 256>, smem_rows_);
   set_smem<T>(k_final_rows<T, T, 128>, smem_rows_);
+  set_smem<T>(k_final_rows<T, T, 256>, smem_rows_);
   set_smem<T>(k_rows_r2c<T, T, 128>, smem_rows_);
   set_smem<T>(k_rows_r2c<T, double, 128>, smem_rows_);
+  set_smem<T>(k_rows_r2c<T, T, 256>, smem_rows_);
+  set_smem<T>(k_rows_r2c<T, double, 256>, smem_rows_);
   set_smem<T>(k_cols_fft<T, -1>, std::max(smem_colx_, smem_coly_));
   set_smem<T>(k_cols_fft<T, +1>, std::max(smem_colx_, smem_coly_));
   set_smem<T>(k_xconv<T>, smem_xconv_);
@@ -407,7 +441,6 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_hess_final_rows<T, double>, smem_rows_);
   set_smem<T>(k_hess_final_rows<T, T>, smem_rows_);
   // partial-sum storage: phi blocks (1 value), x columns (1 value), final rows (4 values)
-  const long nphi = (rows_ + rb_phi_ - 1) / rb_phi_;
   const long ncolx = ((long)ny * pz_ + 7) / 8 + 16;  // x-pass blocks of the widest grid (8 columns per tile)
   // phi partials: at most one per row (both the row-group and the persistent grids stay below it)
   part_len_ = 2 * (rows_ + ncolx + 4 * grid_blocks_rows());
@@ -482,18 +515,18 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   double* part_fin = part_mf + 2 * (long)std::max(gcx, gtx);
   const bool any = M_ > 0 || mf_;
   auto yfwd = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) (fy_ ? k_cols_y_tma<T, -1, 128> : k_cols_y_tma<T, -1, 0>)<<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, -1, decltype(nf_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
     else k_cols_fft<T, -1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   auto yinv = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) (fy_ ? k_cols_y_tma<T, +1, 128> : k_cols_y_tma<T, +1, 0>)<<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, +1, decltype(nf_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
     else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   cudaMemsetAsync(status_, 0, sizeof(unsigned), s);
   mark(0);
   if (any) {
-    (fz_ ? k_rows_r2c<T, RT, 128> : k_rows_r2c<T, RT, 0>)<<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan,
-                                                                                                       twp<T>(tz_), rb_rows_);
+    with_nf(fz_, [&](auto nf_) { k_rows_r2c<T, RT, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan,
+                                                                                                       twp<T>(tz_), rb_rows_); });
     mark(1);
     yfwd(A_, mapYA_, 1, grid_ty1_);
     mark(2);
@@ -502,7 +535,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     mark(2);
   }
   if (M_ > 0) {
-    if (tma_) (fx_ ? k_xconv_tma<T, 128> : k_xconv_tma<T, 0>)<<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+    if (tma_) with_nf(fx_, [&](auto nf_) { k_xconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     mark(3);
     yinv(Cf_, mapYC_, M_, grid_tyM_);
@@ -511,14 +544,13 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     const unsigned gphi = (unsigned)nphi;
     phi_blocks_last_ = nphi;
     if (tma_phi_) {
-      constexpr int RB = PhiRows<T>::value;
       phi_blocks_last_ = grid_tphi_;
       switch (model_) {
-        case MODEL_ROSENFELD: (fz_ ? k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 128> : k_phi_rows_tma<T, MODEL_ROSENFELD, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_RSLT: (fz_ ? k_phi_rows_tma<T, MODEL_RSLT, RB, 128> : k_phi_rows_tma<T, MODEL_RSLT, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_ESFMT: (fz_ ? k_phi_rows_tma<T, MODEL_ESFMT, RB, 128> : k_phi_rows_tma<T, MODEL_ESFMT, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        case MODEL_WHITEBEAR_I: (fz_ ? k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 128> : k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
-        default: (fz_ ? k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 128> : k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, 0>)<<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); break;
+        case MODEL_ROSENFELD: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_ROSENFELD, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
+        case MODEL_RSLT: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_RSLT, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
+        case MODEL_ESFMT: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_ESFMT, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
+        case MODEL_WHITEBEAR_I: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_WHITEBEAR_I, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
+        default: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_WHITEBEAR_II, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
       }
     } else
     switch (model_) {
@@ -536,8 +568,8 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   }
   if (any) {
     if (tma_)
-      (fx_ ? k_xbackconv_tma<T, 128> : k_xbackconv_tma<T, 0>)<<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan,
-                                                        twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
+      with_nf(fx_, [&](auto nf_) { k_xbackconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan,
+                                                        twp<T>(tx_), mf_ ? part_mf : nullptr, status_); });
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
                                                    mf_ ? part_mf : nullptr);
@@ -549,8 +581,8 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     mark(8);
   }
   const unsigned gfin = (unsigned)grid_blocks_rows();
-  (fz_ ? k_final_rows<T, RT, 128> : k_final_rows<T, RT, 0>)<<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_),
-                                                                                         rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin, nrm);
+  with_nf(fz_, [&](auto nf_) { k_final_rows<T, RT, decltype(nf_)::value><<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_),
+                                                                                         rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin, nrm); });
   {
     const FinishSeg sphi{part_phi, phi_blocks_last_, M_ > 0 ? 1 : 0, terms_ + 0};
     const FinishSeg smf{part_mf, (long)gxb, mf_ ? 1 : 0, terms_ + 1};
@@ -572,11 +604,11 @@ int Evaluator<T>::hess_prepare(const double* rho0, cudaStream_t s) {
   constexpr int TCt = TileCols<T>::value;
   const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
   k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho0, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
-  if (tma_) (fy_ ? k_cols_y_tma<T, -1, 128> : k_cols_y_tma<T, -1, 0>)<<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_);
+  if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, -1, decltype(nf_)::value><<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_); });
   else k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
-  if (tma_) (fx_ ? k_xconv_tma<T, 128> : k_xconv_tma<T, 0>)<<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+  if (tma_) with_nf(fx_, [&](auto nf_) { k_xconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
   else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
-  if (tma_) (fy_ ? k_cols_y_tma<T, +1, 128> : k_cols_y_tma<T, +1, 0>)<<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_);
+  if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, +1, decltype(nf_)::value><<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_); });
   else k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   for (int a = 0; a < M_; ++a)
     k_rows_c2r<T, T><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(Cf_ + (long)a * Nc_, NA_ + (long)a * N_, d, tz_->plan,
@@ -595,11 +627,11 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
   const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
   const bool any = M_ > 0 || mf_;
   auto yfwd = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) (fy_ ? k_cols_y_tma<T, -1, 128> : k_cols_y_tma<T, -1, 0>)<<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, -1, decltype(nf_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
     else k_cols_fft<T, -1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   auto yinv = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) (fy_ ? k_cols_y_tma<T, +1, 128> : k_cols_y_tma<T, +1, 0>)<<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_);
+    if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, +1, decltype(nf_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
     else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   if (any) {
@@ -607,7 +639,7 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
     yfwd(A_, mapYA_, 1, grid_ty1_);
   }
   if (M_ > 0) {
-    if (tma_) (fx_ ? k_xconv_tma<T, 128> : k_xconv_tma<T, 0>)<<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_);
+    if (tma_) with_nf(fx_, [&](auto nf_) { k_xconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     yinv(Cf_, mapYC_, M_, grid_tyM_);
     const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
@@ -624,8 +656,8 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
   double* part_mf = part_ + 2 * rows_;
   if (any) {
     if (tma_)
-      (fx_ ? k_xbackconv_tma<T, 128> : k_xbackconv_tma<T, 0>)<<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_),
-                                                        mf_ ? part_mf : nullptr, status_);
+      with_nf(fx_, [&](auto nf_) { k_xbackconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_),
+                                                        mf_ ? part_mf : nullptr, status_); });
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
                                                    mf_ ? part_mf : nullptr);
@@ -638,17 +670,18 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
 
 template <class T>
 void Evaluator<T>::fixed_plans() {
-  auto is_default128 = [](const FFTTable* t) {
-    if (!t || t->plan.n != 128) return false;
-    const std::vector<int> d = default_radices(128);
-    if ((int)d.size() != t->plan.nst) return false;
+  // the compile-time plan length of an axis: 128 or 256 with the default radix order, else 0
+  auto fixed_len = [](const FFTTable* t) {
+    if (!t || (t->plan.n != 128 && t->plan.n != 256)) return 0;
+    const std::vector<int> d = default_radices(t->plan.n);
+    if ((int)d.size() != t->plan.nst) return 0;
     for (int i = 0; i < t->plan.nst; ++i)
-      if (t->plan.radix[i] != d[i]) return false;
-    return true;
+      if (t->plan.radix[i] != d[i]) return 0;
+    return t->plan.n;
   };
-  fx_ = is_default128(tx_);
-  fy_ = is_default128(ty_);
-  fz_ = is_default128(tz_);
+  fx_ = fixed_len(tx_);
+  fy_ = fixed_len(ty_);
+  fz_ = fixed_len(tz_);
 }
 
 template <class T>

@@ -92,6 +92,7 @@ class Evaluator {
   void set_tables(FFTTable* tx, FFTTable* ty, FFTTable* tz) {
     tx_ = tx; ty_ = ty; tz_ = tz;
     fixed_plans();
+    if (tma_) setup_phi_tma();
   }
   long spectrum_len() const { return Nc_; }  // complex values per spectrum (padded rows)
   int pitch() const { return pz_; }
@@ -127,8 +128,9 @@ class Evaluator {
   int grid_ty1_ = 0, grid_tyM_ = 0;
   bool tma_phi_ = false;
   // the tensor-copy kernels' compile-time plans (length 128, default radix order) apply to x / y / z
-  bool fx_ = false, fy_ = false, fz_ = false;
+  int fx_ = 0, fy_ = 0, fz_ = 0;  // compile-time plan length per axis (128, 256) or 0
   void fixed_plans();
+  bool setup_phi_tma();
   CUtensorMap mapR_;
   size_t smem_tphi_ = 0;
   int grid_tphi_ = 0;

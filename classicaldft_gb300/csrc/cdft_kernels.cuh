@@ -625,7 +625,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
   typedef typename Cx<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
-  const int nz = NF > 0 ? NF : d.nz, LP = nz + 1, nzc = NF > 0 ? NF / 2 + 1 : d.nzc;
+  const int nz = NF > 0 ? NF : d.nz, LP = nz + 1;
   C* b1 = b0 + RB * LP;
   const long pair0 = (long)blockIdx.x * RB;
   C* res = b0;

@@ -207,6 +207,10 @@ template <> struct TileCols<double> { static constexpr int value = 8; };
 template <class T> struct PhiRows;
 template <> struct PhiRows<float> { static constexpr int value = 4; };
 template <> struct PhiRows<double> { static constexpr int value = 2; };
+// rows per group for a compile-time row length: half as many for 256-point rows
+template <class T, int NF> struct PhiRowsFor {
+  static constexpr int value = NF == 256 ? (PhiRows<T>::value > 1 ? PhiRows<T>::value / 2 : 1) : PhiRows<T>::value;
+};
 // 8-byte tensor elements per complex value (float2 = 1, double2 = 2)
 template <class T> struct ElemsPerComplex;
 template <> struct ElemsPerComplex<float> { static constexpr int value = 1; };
@@ -260,6 +264,9 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
     if (item >= total) break;
     const int b = (int)(k & 1);
     ok = mbar_wait(&bar[b], (unsigned)((k >> 1) & 1), status);
+    // the previous tile's store must have read its source (work, or its stage
+    // buffer) before this tile's transform writes work
+    if (threadIdx.x == 0) bulk_wait_read();
     if (!__syncthreads_and(ok)) break;
     C* res = tfft<DIR, T, TC, TC, NF>(stage[b], work, P, tw);
     fence_async_smem();
@@ -269,11 +276,12 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
       coords(item, kz0, x, f);
       tma_store_4d(&map, kz0 * E, 0, x, f, res);
       bulk_commit();
-      bulk_wait_read();
       const long next = item + 2L * gridDim.x;
-      if (next < total) issue(next, b);
+      if (next < total) {
+        if (res == stage[b]) bulk_wait_read();  // the store reads the buffer about to be refilled
+        issue(next, b);
+      }
     }
-    __syncthreads();
   }
   if (threadIdx.x == 0) bulk_wait_all();
 }
@@ -328,30 +336,35 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xconv_tma(const
     const int e = threadIdx.x + j * 256;
     if (e < nel) R[j] = res[e];
   }
+  C* prev = nullptr;  // the buffer the last tensor store reads
   for (int a = 0; a < M; ++a) {
     const int b = a & 1;
     ok = mbar_wait(&bar[b], (unsigned)((a >> 1) & 1), status);
     if (!__syncthreads_and(ok)) break;
     const bool odd = weight_is_odd(a);
+    // fill the buffer the previous store does not read; the transform's first
+    // stage writes the other one, so that store must have read it by then
+    C* in = (prev == X) ? Y : X;
+    C* other = (in == X) ? Y : X;
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
       const int e = threadIdx.x + j * 256;
-      if (e < nel) X[e] = mul_weight(R[j], Wst[b][e], odd);
+      if (e < nel) in[e] = mul_weight(R[j], Wst[b][e], odd);
     }
+    if (threadIdx.x == 0) bulk_wait_read();
     __syncthreads();
     if (threadIdx.x == 0 && a + 2 < M) {
       mbar_arrive_expect_tx(&bar[b], (unsigned)wbytes);
       tma_load_3d(Wst[b], &mapW, col0, 0, a + 2, &bar[b]);
     }
-    C* r2 = tfft<+1, T, TC, TC, NF>(X, Y, px, tw);
+    C* r2 = tfft<+1, T, TC, TC, NF>(in, other, px, tw);
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
       tma_store_3d(&mapC, col0 * E, 0, a, r2);
       bulk_commit();
-      bulk_wait_read();
     }
-    __syncthreads();
+    prev = r2;
   }
   if (threadIdx.x == 0) bulk_wait_all();
 }

@@ -150,6 +150,32 @@ def test_config2_128_fp64_and_fp32_vs_oracle(cd, oracle):
     assert np.abs(dF32 - dFo).max() <= 2e-6 * np.abs(dFo).max()
 
 
+@pytest.mark.parametrize("shape", [(256, 16, 256), (16, 256, 24)])
+def test_256_point_axes_vs_oracle(cd, oracle, shape):
+    """Axes of 256 points run the compile-time 256-point plans (x and z in the first shape,
+    y in the second): FP64 at the reference bars. In FP32 the error of dF is relative to the
+    terms that cancel in it near equilibrium (ln rho + c1 against mu, each of order |mu| dV),
+    so the FP32 bar on dF is 2e-6 of the larger of max|dF| and |mu| dV."""
+    dx = 0.1
+    hsd = oracle.bh_diameter(3.0, 0.9)
+    o = oracle.Oracle(shape, dx, "WhiteBearI", hsd=hsd, lj=True, kT=0.9)
+    rho = oracle.fill_noise(shape, 0.4, 0.3, 77)
+    mu = o.mu_times_beta(0.4)
+    o.set_mu(mu)
+    st, t, dFo, _ = o.eval(rho)
+    c = cd.Context(shape, dx, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.9, mu=mu)
+    c.set_density(rho)
+    terms, dF = c.eval()
+    for k in ("Omega", "F_id", "F_hs", "F_mf", "F_ext"):
+        assert abs(terms[k] - t[k]) <= 1e-12 * max(1.0, abs(t[k])), (k, terms[k], t[k])
+    np.testing.assert_allclose(dF, dFo, rtol=0, atol=dF_tol(dx))
+    c.set_precision(cd.FP32)
+    terms32, dF32 = c.eval()
+    assert abs(terms32["Omega"] - t["Omega"]) <= 2e-6 * abs(t["Omega"])
+    assert np.abs(dF32 - dFo).max() <= 2e-6 * max(np.abs(dFo).max(), abs(mu) * dx ** 3)
+    c.close()
+
+
 def test_bulk_limit(cd):
     # uniform density: Omega/V equals the bulk grand potential density and dF/dV equals mu(rho) - mu,
     # up to the lattice weights' own sum-rule error (sum w_eta = pi d^3/6 only to ~3e-9 relative)
