@@ -311,6 +311,19 @@ static int ensure_evaluator(cdft_ctx* c, int precision) {
   if ((precision == CDFT_FP64 && c->e64) || (precision == CDFT_FP32 && c->e32)) return CDFT_OK;
   std::vector<double> w[11], watt;
   const bool fmt = c->p.model >= 0;
+  std::string err;
+  int rc;
+  if (precision == CDFT_FP32 && c->e64) {  // round the FP64 evaluator's weight spectra instead of recomputing them
+    c->e32.reset(new Evaluator<float>());
+    rc = c->e32->init(nx, ny, nz, c->p.model, c->info.hsd, c->p.es_A, c->p.es_B, nullptr, nullptr, c->tx.get(), c->ty.get(),
+                      c->tz.get(), c->stream, &err, fmt ? c->e64->weight_spectra() : nullptr,
+                      c->p.lj ? c->e64->att_spectrum() : nullptr);
+    if (rc) {
+      c->e32.reset();
+      return fail(c, rc, err);
+    }
+    return CDFT_OK;
+  }
   try {
     if (fmt) fmt_weights_real(nx, ny, nz, c->p.dx, c->info.hsd, w);
     if (c->p.lj) {
@@ -320,8 +333,6 @@ static int ensure_evaluator(cdft_ctx* c, int precision) {
   } catch (std::exception& e) {
     return fail(c, CDFT_ERR_ARG, e.what());
   }
-  std::string err;
-  int rc;
   if (precision == CDFT_FP64) {
     c->e64.reset(new Evaluator<double>());
     rc = c->e64->init(nx, ny, nz, c->p.model, c->info.hsd, c->p.es_A, c->p.es_B, fmt ? w : nullptr, c->p.lj ? &watt : nullptr, c->tx.get(),
@@ -355,10 +366,12 @@ static int map_reduce(cdft_ctx* c, long n, F f, double* host_out) {
 static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
   const long N = c->info.N;
   const double dV = c->info.dV;
-  if (!c->eval_exec || c->eg_prec != c->precision || c->eg_only_fex != only_fex || c->eg_vext != c->vext || c->eg_mu != c->mu ||
-      c->eg_plan_gen != c->plan_gen) {
-    if (c->eval_exec) cudaGraphExecDestroy(c->eval_exec);
-    c->eval_exec = nullptr;
+  const int gi = c->precision == CDFT_FP64 ? 1 : 0;
+  cudaGraphExec_t& exec = c->eval_exec[gi];
+  if (!exec || c->eg_only_fex[gi] != only_fex || c->eg_vext[gi] != c->vext || c->eg_mu[gi] != c->mu ||
+      c->eg_plan_gen[gi] != c->plan_gen) {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
     if (!c->cap_stream) CUDA_OR_FAIL(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
     if (!c->host_status) CUDA_OR_FAIL(c, cudaMallocHost(&c->host_status, sizeof(unsigned)));
     cudaStream_t s = c->cap_stream;
@@ -384,19 +397,18 @@ static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
     cudaMemcpyAsync(c->host_status, dst, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
     const cudaError_t ce = cudaStreamEndCapture(s, &g);
     if (rc || ce != cudaSuccess) return fail(c, CDFT_ERR_CUDA, "evaluation graph capture failed");
-    const cudaError_t ie = cudaGraphInstantiate(&c->eval_exec, g, 0);
+    const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
     if (ie != cudaSuccess) {
-      c->eval_exec = nullptr;
+      exec = nullptr;
       return fail(c, CDFT_ERR_CUDA, "evaluation graph instantiate failed");
     }
-    c->eg_prec = c->precision;
-    c->eg_only_fex = only_fex;
-    c->eg_vext = c->vext;
-    c->eg_mu = c->mu;
-    c->eg_plan_gen = c->plan_gen;
+    c->eg_only_fex[gi] = only_fex;
+    c->eg_vext[gi] = c->vext;
+    c->eg_mu[gi] = c->mu;
+    c->eg_plan_gen[gi] = c->plan_gen;
   }
-  CUDA_OR_FAIL(c, cudaGraphLaunch(c->eval_exec, c->stream));
+  CUDA_OR_FAIL(c, cudaGraphLaunch(exec, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   EvalTerms t;
   int rc = c->precision == CDFT_FP64 ? c->e64->terms_from(c->host_out, *c->host_status, dV, c->mu, &t)
@@ -536,7 +548,8 @@ int cdft_destroy(cdft_ctx* c) {
   cudaFree(c->dd0); cudaFree(c->dd1); cudaFree(c->ddn); cudaFree(c->dR); cudaFree(c->dfac);
   cudaFree(c->rk0); cudaFree(c->R0k); cudaFree(c->R1k); cudaFree(c->work);
   cudaFree(c->hv_v); cudaFree(c->hv_out);
-  if (c->eval_exec) cudaGraphExecDestroy(c->eval_exec);
+  for (cudaGraphExec_t ge : c->eval_exec)
+    if (ge) cudaGraphExecDestroy(ge);
   if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
   cudaFreeHost(c->host_status);
   delete c;

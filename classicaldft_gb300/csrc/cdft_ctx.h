@@ -60,11 +60,13 @@ struct cdft_ctx {
   // stream; re-captured when its inputs change (precision, only_fex, the
   // external-field pointer, mu, the transform plans).
   cudaStream_t cap_stream = nullptr;
-  cudaGraphExec_t eval_exec = nullptr;
-  int eg_prec = -1, eg_only_fex = -1;
-  const double* eg_vext = nullptr;
-  double eg_mu = 0;
-  unsigned plan_gen = 0, eg_plan_gen = ~0u;
+  // captured evaluation graphs, one per bulk precision (index: precision == CDFT_FP64),
+  // with the settings each was captured under
+  cudaGraphExec_t eval_exec[2] = {nullptr, nullptr};
+  int eg_only_fex[2] = {-1, -1};
+  const double* eg_vext[2] = {nullptr, nullptr};
+  double eg_mu[2] = {0, 0};
+  unsigned plan_gen = 0, eg_plan_gen[2] = {~0u, ~0u};
   unsigned* host_status = nullptr;  // pinned
   double last_dF_l2 = 0;            // ||dF||_2 / dV of the last evaluation
   // Hessian-vector product buffers (device, N doubles each; allocated on first use)

@@ -173,6 +173,10 @@ __global__ void k_compact(const double2* __restrict__ full, T* __restrict__ out,
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     out[i] = (T)((odd ? full[i].y : full[i].x) * scale);
 }
+template <class T>
+__global__ void k_round_spectra(const double* __restrict__ in, T* __restrict__ out, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) out[i] = (T)in[i];
+}
 
 // ------------------------------------------------------------ Evaluator ---
 template <class T>
@@ -373,7 +377,8 @@ bool Evaluator<T>::setup_phi_tma() {
 
 template <class T>
 int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA, double esB, const std::vector<double>* w_fmt,
-                       const std::vector<double>* w_att, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s, std::string* err) {
+                       const std::vector<double>* w_att, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s, std::string* err,
+                       const double* dev_w, const double* dev_watt) {
   nx_ = nx; ny_ = ny; nz_ = nz; nzc_ = nz / 2 + 1;
   pz_ = (nzc_ + 3) / 4 * 4;
   N_ = (long)nx * ny * nz;
@@ -382,7 +387,7 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   model_ = model;
   M_ = (model < 0) ? 0 : (model >= MODEL_ESFMT ? 11 : 5);
   hsd_ = hsd; esA_ = esA; esB_ = esB;
-  mf_ = (w_att != nullptr);
+  mf_ = (w_att != nullptr) || (dev_watt != nullptr);
   tx_ = tx; ty_ = ty; tz_ = tz;
   fixed_plans();
   Dims d{nx, ny, nz, nzc_, N_, Nc_, rows_, pz_};
@@ -448,6 +453,22 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   CK(cudaMalloc(&terms_, 8 * sizeof(double)));
   CK(cudaMalloc(&status_, sizeof(unsigned)));
   CK(cudaMemsetAsync(terms_, 0, 8 * sizeof(double), s));
+  if (M_ > 0 && dev_w) {  // weight spectra rounded from an FP64 evaluator's
+    const unsigned cg = (unsigned)std::min<long>(((long)M_ * Nc_ + 255) / 256, 4096);
+    CK(cudaMalloc(&w_, (size_t)M_ * Nc_ * sizeof(T)));
+    k_round_spectra<T><<<cg, 256, 0, s>>>(dev_w, w_, (long)M_ * Nc_);
+  }
+  if (mf_ && dev_watt) {
+    const unsigned cg = (unsigned)std::min<long>((Nc_ + 255) / 256, 4096);
+    CK(cudaMalloc(&watt_, Nc_ * sizeof(T)));
+    k_round_spectra<T><<<cg, 256, 0, s>>>(dev_watt, watt_, Nc_);
+  }
+  if ((M_ == 0 || dev_w) && (!mf_ || dev_watt)) {
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    if (!setup_tma(err)) tma_ = false;
+    return 0;
+  }
   // weight spectra: FP64 r2c on the device, keep the non-zero component, fold 1/N
   double* tmp_real = nullptr;
   double2* tmp_spec = nullptr;
@@ -455,7 +476,7 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   CK(cudaMalloc(&tmp_spec, Nc_ * sizeof(double2)));
   CK(cudaMemsetAsync(tmp_spec, 0, Nc_ * sizeof(double2), s));
   const unsigned cgrid = (unsigned)std::min<long>((Nc_ + 255) / 256, 4096);
-  if (M_ > 0) {
+  if (M_ > 0 && !dev_w) {
     CK(cudaMalloc(&w_, (size_t)M_ * Nc_ * sizeof(T)));
     CK(cudaMemsetAsync(w_, 0, (size_t)M_ * Nc_ * sizeof(T), s));
     for (int a = 0; a < M_; ++a) {
@@ -464,7 +485,7 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
       k_compact<T><<<cgrid, 256, 0, s>>>(tmp_spec, w_ + (long)a * Nc_, Nc_, (a >= 2 && a <= 4) ? 1 : 0, 1.0 / (double)N_);
     }
   }
-  if (mf_) {
+  if (mf_ && !dev_watt) {
     CK(cudaMalloc(&watt_, Nc_ * sizeof(T)));
     CK(cudaMemcpyAsync(tmp_real, w_att->data(), N_ * sizeof(double), cudaMemcpyHostToDevice, s));
     r2c_f64(tmp_real, tmp_spec, d, tx, ty, tz, s);

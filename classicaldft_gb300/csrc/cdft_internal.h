@@ -50,7 +50,13 @@ class Evaluator {
   ~Evaluator();
   // w_fmt: 11 real-space weights (host, FP64) or null; w_att: real-space MF kernel or null.
   int init(int nx, int ny, int nz, int model, double hsd, double esA, double esB, const std::vector<double>* w_fmt,
-           const std::vector<double>* w_att, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s, std::string* err);
+           const std::vector<double>* w_att, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s, std::string* err,
+           const double* dev_w = nullptr, const double* dev_watt = nullptr);
+  // dev_w / dev_watt (optional): the compact FP64 weight spectra of an FP64 evaluator of the
+  // same system (M x Nc and Nc values); when given they are rounded to T on the device in
+  // place of w_fmt / w_att (the same values the host path gives: both round one FP64 product).
+  const T* weight_spectra() const { return w_; }
+  const T* att_spectrum() const { return watt_; }
   // rho (device FP64) -> dF (device FP64), scalar terms (host). Synchronous at the end.
   int eval(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, EvalTerms* out, cudaStream_t s);
   // Launches the pass sequence without host synchronisation; partial sums land in dev_terms.
