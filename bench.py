@@ -352,6 +352,14 @@ def warm_start_leg(cd, n_train=24, n_test=4, steps=300, tol=1e-8):
         c.close()
     out.update(res)
     out["speedup_warm_vs_cold"] = res["cold"]["seconds"] / res["warm"]["seconds"]
+    seed = fno.coarse_seed(SHAPE, DX, RHO_V, RHO_L, R_DROP)
+    for _ in range(2):
+        fno.predict(model, seed, KT, SHAPE, on_device=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fno.predict(model, seed, KT, SHAPE, on_device=True)
+    torch.cuda.synchronize()
+    out["predict_ms"] = (time.perf_counter() - t0) * 1e3  # inside the warm timing above
     # the operator's pointwise layer on the tensor cores: Y = GELU(X W + b + add), 128^3 rows, K = N = 32
     M, K, N = int(np.prod(SHAPE)), fno.WIDTH, fno.WIDTH
     x = torch.randn(M, K, device="cuda").to(torch.bfloat16)

@@ -8,13 +8,13 @@ counterpart in the reference.
 Layout (channels-last, one row per lattice point, so every pointwise layer is a
 GEMM over the N = 128^3 rows):
   lift      [seed, kT, 1, 0 ...] (16 channels) -> width 32      tensor-core GEMM
-  4 blocks  v <- GELU(v W + b + SpectralConv(v))                 tensor-core GEMM + FFT
+  4 blocks  v <- GELU(v W + b + SpectralConv(v))                 tensor-core GEMM + truncated DFTs
   project   32 -> 32 (GELU) -> 32 (column 0 used)                tensor-core GEMMs
   output    log rho = log seed_up + out  (positive by construction)
 The pointwise GEMMs run on the BF16 tcgen05 kernel (cdft_tc_gemm_bf16, FP32
 accumulation in tensor memory) forward and, for the activations' gradient,
-backward; the spectral convolutions (12 modes per axis) and the weight
-gradients are plain library operations.
+backward; the spectral convolutions (12 modes per axis, as truncated DFTs in
+library GEMMs) and the weight gradients are plain library operations.
 """
 import ctypes
 import math
@@ -98,8 +98,41 @@ def tc_linear(x, w, b, add=None, act=0):
     return _TCLinear.apply(x, w, b, add, act)
 
 
+_DFT_CACHE = {}
+
+
+def _dft_mats(shape, m, device):
+    """Truncated DFT matrices of a (n0, n1, n2) grid keeping kx, ky in [0, m) and [n - m, n)
+    and kz in [0, m): forward Fz (2m x n2, real: cos rows then -sin rows), Fy (2m x n1) and
+    Fx (2m x n0) complex; inverse Gx (n0 x 2m), Gy (n1 x 2m) complex and Gz (n2 x 2m, real),
+    Gz carrying the half-spectrum weights (1 for kz = 0, 2 above) and the 1/N of the inverse."""
+    key = (tuple(shape), m, str(device))
+    if key not in _DFT_CACHE:
+        n0, n1, n2 = shape
+
+        def full(n):  # kept wave numbers along a full axis, and the phases
+            k = np.concatenate([np.arange(m), np.arange(n - m, n)])
+            return np.exp(-2j * np.pi * np.outer(k, np.arange(n)) / n)
+
+        th = 2 * np.pi * np.outer(np.arange(m), np.arange(n2)) / n2  # (m, n2)
+        Fz = np.concatenate([np.cos(th), -np.sin(th)], axis=0)
+        w = np.where(np.arange(m) == 0, 1.0, 2.0)[:, None] / float(n0 * n1 * n2)
+        Gz = np.concatenate([w * np.cos(th), -w * np.sin(th)], axis=0).T  # (n2, 2m)
+        Fx, Fy = full(n0), full(n1)
+        c = lambda a: torch.as_tensor(a, dtype=torch.complex64, device=device)
+        r = lambda a: torch.as_tensor(a, dtype=torch.float32, device=device)
+        _DFT_CACHE[key] = (r(Fz), c(Fy), c(Fx), c(Fx.conj().T), c(Fy.conj().T), r(Gz))
+    return _DFT_CACHE[key]
+
+
 class SpectralConv3d(torch.nn.Module):
-    """Fourier layer: rfftn, complex channel mixing on the 4 x MODES^3 lowest modes, irfftn."""
+    """Fourier layer: complex channel mixing on the 4 x MODES^3 lowest modes of the real 3D
+    transform (the four (kx, ky) corners, kz < MODES), back to real space.
+
+    Only the kept modes are ever formed: the transform is three truncated DFTs taken as GEMMs
+    straight on the channels-last (N, C) activations (z, then y, then x; and back), so a layer
+    reads and writes its activations once, with no full-grid FFT and no transposed copies.
+    The result equals irfftn(mix(rfftn(v))) with every other mode zero."""
 
     def __init__(self, width, modes):
         super().__init__()
@@ -107,19 +140,27 @@ class SpectralConv3d(torch.nn.Module):
         self.m = modes
         self.w = torch.nn.Parameter(scale * torch.randn(4, width, width, modes, modes, modes, 2))
 
+    def mixing(self):
+        """The weights as (2m, 2m, m, C_in, C_out) complex, corners in the kept-mode order."""
+        W = torch.view_as_complex(self.w).permute(0, 3, 4, 5, 1, 2)  # (4, x, y, z, i, o)
+        top = torch.cat([W[0], W[2]], dim=1)  # kx < m: ky < m, then ky >= n - m
+        bot = torch.cat([W[1], W[3]], dim=1)  # kx >= n - m
+        return torch.cat([top, bot], dim=0)
+
     def forward(self, v, shape):  # v: (N, C) channels-last
         n0, n1, n2 = shape
-        C = v.shape[1]
-        x = v.t().reshape(1, C, n0, n1, n2)
-        X = torch.fft.rfftn(x, dim=(2, 3, 4))
-        out = torch.zeros_like(X)
         m = self.m
-        W = torch.view_as_complex(self.w)
-        for q, (sx, sy) in enumerate(((slice(0, m), slice(0, m)), (slice(n0 - m, n0), slice(0, m)),
-                                      (slice(0, m), slice(n1 - m, n1)), (slice(n0 - m, n0), slice(n1 - m, n1)))):
-            out[:, :, sx, sy, :m] = torch.einsum("bixyz,ioxyz->boxyz", X[:, :, sx, sy, :m], W[q])
-        y = torch.fft.irfftn(out, s=(n0, n1, n2), dim=(2, 3, 4))
-        return y.reshape(C, -1).t()
+        C = v.shape[1]
+        Fz, Fy, Fx, Gx, Gy, Gz = _dft_mats(shape, m, v.device)
+        a = torch.matmul(Fz, v.reshape(n0 * n1, n2, C))                       # (n0 n1, 2m, C)
+        xz = torch.complex(a[:, :m], a[:, m:]).reshape(n0, n1, m * C)          # z: kz < m
+        xy = torch.matmul(Fy, xz)                                              # y: (n0, 2m, m C)
+        xx = torch.matmul(Fx, xy.reshape(n0, 2 * m * m * C)).reshape(2 * m, 2 * m, m, 1, C)
+        out = torch.matmul(xx, self.mixing()).reshape(2 * m, 2 * m * m * C)   # channel mixing per mode
+        y1 = torch.matmul(Gx, out).reshape(n0, 2 * m, m * C)                   # x back: (n0, 2m, m C)
+        y2 = torch.matmul(Gy, y1).reshape(n0 * n1, m, C)                       # y back: (n0, n1, m C)
+        b = torch.cat([y2.real, y2.imag], dim=1)                               # (n0 n1, 2m, C)
+        return torch.matmul(Gz, b).reshape(n0 * n1 * n2, C)                    # z back, real
 
 
 class FNO3d(torch.nn.Module):

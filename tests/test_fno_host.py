@@ -34,3 +34,28 @@ def test_droplet_sampler_is_seeded():
     assert a == fno.sample_droplets(8, 3) and a != fno.sample_droplets(8, 4)
     for p in a:
         assert 0.75 <= p["kT"] <= 0.9 and 3.0 <= p["R"] <= 5.0 and p["rho_v"] < p["rho_l"]
+
+
+def test_spectral_conv_equals_fft_formulation():
+    """The truncated-DFT Fourier layer equals irfftn(mix(rfftn(v))) with only the kept modes."""
+    from classicaldft_gb300 import fno
+    torch.manual_seed(3)
+    shape, C, m = (12, 10, 16), 4, 3
+    layer = fno.SpectralConv3d(C, m)
+    with torch.no_grad():
+        layer.w.mul_(50.0)
+    v = torch.randn(int(np.prod(shape)), C)
+    y = layer(v, shape)
+    n0, n1, n2 = shape
+    X = torch.fft.rfftn(v.t().reshape(1, C, n0, n1, n2), dim=(2, 3, 4))
+    out = torch.zeros_like(X)
+    W = torch.view_as_complex(layer.w.detach())
+    for q, (sx, sy) in enumerate(((slice(0, m), slice(0, m)), (slice(n0 - m, n0), slice(0, m)),
+                                  (slice(0, m), slice(n1 - m, n1)), (slice(n0 - m, n0), slice(n1 - m, n1)))):
+        out[:, :, sx, sy, :m] = torch.einsum("bixyz,ioxyz->boxyz", X[:, :, sx, sy, :m], W[q])
+    ref = torch.fft.irfftn(out, s=shape, dim=(2, 3, 4)).reshape(C, -1).t()
+    assert torch.max(torch.abs(y.detach() - ref)) <= 1e-5 * torch.max(torch.abs(ref))
+    # gradients flow to the input and to the weights
+    v.requires_grad_(True)
+    layer(v, shape).square().sum().backward()
+    assert v.grad is not None and layer.w.grad is not None and torch.isfinite(layer.w.grad).all()
