@@ -359,16 +359,17 @@ bool Evaluator<T>::setup_phi_tma() {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, PhiThreads<T>::value, smem_tphi_);
       return std::max(b2, 1);
     };
-    int bp;
+    int bp, bh;  // resident blocks per SM of the Phi and of the Hessian instances
     switch (model_) {
-      case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF>); break;
-      case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF>); break;
-      case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF>); break;
-      case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF>); break;
-      default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF>); break;
+      case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, true>); break;
+      case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF, true>); break;
+      case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, true>); break;
+      case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, true>); break;
+      default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, true>); break;
     }
     const long ngroup = (rows_ + RB - 1) / RB;
     grid_tphi_ = (int)std::min<long>(ngroup, (long)nsm * bp);
+    grid_thess_ = (int)std::min<long>(ngroup, (long)nsm * bh);
     ok = true;
   });
   tma_phi_ = ok;
@@ -445,6 +446,10 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_rows_c2r<T, T>, smem_rows_);
   set_smem<T>(k_hess_final_rows<T, double>, smem_rows_);
   set_smem<T>(k_hess_final_rows<T, T>, smem_rows_);
+  set_smem<T>(k_hess_final_rows<T, double, 128>, smem_rows_);
+  set_smem<T>(k_hess_final_rows<T, T, 128>, smem_rows_);
+  set_smem<T>(k_hess_final_rows<T, double, 256>, smem_rows_);
+  set_smem<T>(k_hess_final_rows<T, T, 256>, smem_rows_);
   // partial-sum storage: phi blocks (1 value), x columns (1 value), final rows (4 values)
   const long ncolx = ((long)ny * pz_ + 7) / 8 + 16;  // x-pass blocks of the widest grid (8 columns per tile)
   // phi partials: at most one per row (both the row-group and the persistent grids stay below it)
@@ -656,7 +661,9 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
     else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   if (any) {
-    k_rows_r2c<T, RT><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(v, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+    with_nf(fz_, [&](auto nf_) {
+      k_rows_r2c<T, RT, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(v, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+    });
     yfwd(A_, mapYA_, 1, grid_ty1_);
   }
   if (M_ > 0) {
@@ -665,6 +672,18 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
     yinv(Cf_, mapYC_, M_, grid_tyM_);
     const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
     const unsigned g = (unsigned)((rows_ + rb_phi_ - 1) / rb_phi_);
+    if (tma_phi_) {
+      with_nf(fz_, [&](auto nf_) {
+        constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
+        switch (model_) {
+          case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+        }
+      });
+    } else
     switch (model_) {
       case MODEL_ROSENFELD: k_hess_rows<T, MODEL_ROSENFELD><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
       case MODEL_RSLT: k_hess_rows<T, MODEL_RSLT><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
@@ -684,8 +703,10 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
                                                    mf_ ? part_mf : nullptr);
     yinv(E_, mapYE_, 1, grid_ty1_);
   }
-  k_hess_final_rows<T, RT><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(E_, rho0, v, out, d, tz_->plan, twp<T>(tz_), rb_rows_, dV,
-                                                                                 any ? 1 : 0);
+  with_nf(fz_, [&](auto nf_) {
+    k_hess_final_rows<T, RT, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(E_, rho0, v, out, d, tz_->plan,
+                                                                                                      twp<T>(tz_), rb_rows_, dV, any ? 1 : 0);
+  });
   return cudaGetLastError() == cudaSuccess ? 0 : 5;
 }
 

@@ -139,7 +139,7 @@ class Evaluator {
   bool setup_phi_tma();
   CUtensorMap mapR_;
   size_t smem_tphi_ = 0;
-  int grid_tphi_ = 0;
+  int grid_tphi_ = 0, grid_thess_ = 0;
 };
 
 }  // namespace cdft

@@ -217,9 +217,11 @@ __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, ty
   typedef typename Cx<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
-  const int nz = d.nz, LP = nz + 1;
+  const int nz = NF > 0 ? NF : d.nz, LP = nz + 1;
   C* b1 = b0 + RB * LP;
   const long pair0 = (long)blockIdx.x * RB;
+  // unrolled so that several rows' loads are in flight before their shared stores
+#pragma unroll 4
   for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
     const int r = e / nz, k = e - r * nz;
     const long ra = 2 * (pair0 + r), rb = ra + 1;
@@ -229,7 +231,7 @@ __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, ty
     b0[r * LP + k] = mk<T>(va, vb);
   }
   C* res = block_fft_nf<-1, T, NF>(b0, b1, RB, LP, pz, tw);
-  const int nzc = d.nzc;
+  const int nzc = NF > 0 ? NF / 2 + 1 : d.nzc;
   for (int e = threadIdx.x; e < RB * nzc; e += blockDim.x) {
     const int r = e / nzc, k = e - r * nzc;
     const long ra = 2 * (pair0 + r), rb = ra + 1;
@@ -579,11 +581,12 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
   typedef typename Cx<T>::type C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
-  const int nz = d.nz, LP = nz + 1;
+  const int nz = NF > 0 ? NF : d.nz, LP = nz + 1;
   C* b1 = b0 + RB * LP;
   const long pair0 = (long)blockIdx.x * RB;
   C* res = b0;
   if (have_fmt_or_mf) {
+#pragma unroll 4
     for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
       const int r = e / nz, k = e - r * nz;
       const long ra = 2 * (pair0 + r), rb = ra + 1;
@@ -630,6 +633,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
   const long pair0 = (long)blockIdx.x * RB;
   C* res = b0;
   if (have_fmt_or_mf) {
+#pragma unroll 4
     for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
       const int r = e / nz, k = e - r * nz;
       const long ra = 2 * (pair0 + r), rb = ra + 1;

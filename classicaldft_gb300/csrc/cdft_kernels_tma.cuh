@@ -487,10 +487,15 @@ template <class T> struct PhiBufs { static constexpr int value = sizeof(T) == 4 
 // minimum resident blocks the register allocation must allow
 template <class T> struct PhiMinBlocks { static constexpr int value = sizeof(T) == 4 ? 3 : 1; };
 
-template <class T, int MODEL, int RB, int NF = 0>
-__global__ void __launch_bounds__(PhiThreads<T>::value, PhiMinBlocks<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
+// HESS: the z-row step of the Hessian-vector product instead (FMT::add_second_derivative,
+// src/FMT.cpp:437-567): Cf holds the convolutions of v, NA the M weighted densities of the
+// linearisation state in real space (M x N); per point the folded (d2Phi).Psi replaces Psi.
+// No energy sum and no eta checks then (part and the status bits of the point loop unused).
+template <class T, int MODEL, int RB, int NF = 0, bool HESS = false>
+__global__ void __launch_bounds__(PhiThreads<T>::value, HESS ? 2 : PhiMinBlocks<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
                                                       Dims d, FFTPlan pz_plan, const typename Cx<T>::type* __restrict__ tw, T hsd, T esA,
-                                                      T esB, double* __restrict__ part, unsigned* __restrict__ status) {
+                                                      T esB, double* __restrict__ part, unsigned* __restrict__ status,
+                                                      const T* __restrict__ NA = nullptr) {
   typedef typename Cx<T>::type C;
   constexpr int M = ModelTraits<MODEL>::M;
   constexpr int NP = (M + 1) / 2;
@@ -560,11 +565,18 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, PhiMinBlocks<T>::value) 
         const C z = res[k * LPd + r * NP + a / 2];
         nv[a] = (a & 1) ? z.y : z.x;
       }
-      const T eta = nv[0];
-      const T phi = fmt_phi_point<T, MODEL>(nv, ih, ih2, esA, esB);
-      if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
-      if (!isfinite(phi)) st |= 2u;
-      psum.add(phi);
+      if constexpr (HESS) {
+        T nd[11];
+#pragma unroll
+        for (int a = 0; a < M; ++a) nd[a] = NA[(long)a * d.N + (row0 + r) * nz + k];
+        fmt_d2phi_dot_point<T, MODEL>(nd, nv, ih, ih2, esA, esB);
+      } else {
+        const T eta = nv[0];
+        const T phi = fmt_phi_point<T, MODEL>(nv, ih, ih2, esA, esB);
+        if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
+        if (!isfinite(phi)) st |= 2u;
+        psum.add(phi);
+      }
 #pragma unroll
       for (int p = 0; p < NP; ++p) oth[k * LPd + r * NP + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
     }
@@ -581,8 +593,10 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, PhiMinBlocks<T>::value) 
     }
     __syncthreads();
   }
-  if (st) atomicOr(status, st);
-  block_kahan_store<1>(&psum, part, blockIdx.x);
+  if constexpr (!HESS) {
+    if (st) atomicOr(status, st);
+    block_kahan_store<1>(&psum, part, blockIdx.x);
+  }
   (void)E;
 }
 
