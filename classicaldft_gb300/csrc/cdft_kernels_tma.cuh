@@ -471,7 +471,8 @@ namespace cdft {
 // ------------------------------------------------- fused Phi on z rows ---
 // Persistent: each block walks groups of RB consecutive rows (x, y). One
 // tensor copy brings the group's M field rows ({pz*E, rows, M}, box
-// {pz*E, RB, M}) while the previous group is computed. The M rows of a (x, y)
+// {pz*E, RB, M}) while an earlier group is computed (PhiBufs input buffers:
+// the next group's copy is issued as soon as a buffer has been unpacked). The M rows of a (x, y)
 // are paired into NP = ceil(M/2) complex lines; a group is a [nz][L] tile,
 // L = NP*RB lines, transformed column-wise (line-fastest, conflict-free):
 // c2r (z), Phi and dPhi per point, r2c (z), then the M derivative rows are
