@@ -361,11 +361,18 @@ bool Evaluator<T>::setup_phi_tma() {
     };
     int bp, bh;  // resident blocks per SM of the Phi and of the Hessian instances
     switch (model_) {
-      case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, true>); break;
-      case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF, true>); break;
-      case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, true>); break;
-      case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, true>); break;
-      default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, true>); break;
+      case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiHess>); break;
+      case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiHess>); break;
+      case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiHess>); break;
+      case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiHess>); break;
+      default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiHess>); break;
+    }
+    switch (model_) {  // the weighted-density store of the Hessian set-up runs on the Phi grid
+      case MODEL_ROSENFELD: raise_smem(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiStoreN>, smem_tphi_); break;
+      case MODEL_RSLT: raise_smem(k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiStoreN>, smem_tphi_); break;
+      case MODEL_ESFMT: raise_smem(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiStoreN>, smem_tphi_); break;
+      case MODEL_WHITEBEAR_I: raise_smem(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiStoreN>, smem_tphi_); break;
+      default: raise_smem(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiStoreN>, smem_tphi_); break;
     }
     const long ngroup = (rows_ + RB - 1) / RB;
     grid_tphi_ = (int)std::min<long>(ngroup, (long)nsm * bp);
@@ -629,16 +636,33 @@ int Evaluator<T>::hess_prepare(const double* rho0, cudaStream_t s) {
   const unsigned gcx = (unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_);
   constexpr int TCt = TileCols<T>::value;
   const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
-  k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho0, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+  with_nf(fz_, [&](auto nf_) {
+    k_rows_r2c<T, double, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho0, A_, d, tz_->plan, twp<T>(tz_),
+                                                                                                    rb_rows_);
+  });
   if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, -1, decltype(nf_)::value><<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_); });
   else k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   if (tma_) with_nf(fx_, [&](auto nf_) { k_xconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
   else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
   if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, +1, decltype(nf_)::value><<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_); });
   else k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
-  for (int a = 0; a < M_; ++a)
-    k_rows_c2r<T, T><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(Cf_ + (long)a * Nc_, NA_ + (long)a * N_, d, tz_->plan,
-                                                                           twp<T>(tz_), rb_rows_, (T)1);
+  if (tma_phi_) {  // one tensor-copied pass: z c2r of all M fields, stored as the weighted densities
+    with_nf(fz_, [&](auto nf_) {
+      constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
+      const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
+      switch (model_) {
+        case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+        case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+        case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+        case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+        default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+      }
+    });
+  } else {
+    for (int a = 0; a < M_; ++a)
+      k_rows_c2r<T, T><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(Cf_ + (long)a * Nc_, NA_ + (long)a * N_, d, tz_->plan,
+                                                                             twp<T>(tz_), rb_rows_, (T)1);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : 5;
 }
 
@@ -676,11 +700,11 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
       with_nf(fz_, [&](auto nf_) {
         constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
         switch (model_) {
-          case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-          case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-          case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-          case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-          default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, true><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
+          default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
         }
       });
     } else

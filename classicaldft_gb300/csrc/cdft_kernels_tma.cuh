@@ -488,15 +488,21 @@ template <class T> struct PhiBufs { static constexpr int value = sizeof(T) == 4 
 // minimum resident blocks the register allocation must allow
 template <class T> struct PhiMinBlocks { static constexpr int value = sizeof(T) == 4 ? 3 : 1; };
 
-// HESS: the z-row step of the Hessian-vector product instead (FMT::add_second_derivative,
-// src/FMT.cpp:437-567): Cf holds the convolutions of v, NA the M weighted densities of the
-// linearisation state in real space (M x N); per point the folded (d2Phi).Psi replaces Psi.
-// No energy sum and no eta checks then (part and the status bits of the point loop unused).
-template <class T, int MODEL, int RB, int NF = 0, bool HESS = false>
-__global__ void __launch_bounds__(PhiThreads<T>::value, HESS ? 2 : PhiMinBlocks<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
+// MODE selects what the pass does per point after the z c2r:
+//   kPhiEval  Phi and dPhi (the evaluation; Phi summed into part);
+//   kPhiHess  the z-row step of the Hessian-vector product (FMT::add_second_derivative,
+//             src/FMT.cpp:437-567): Cf holds the convolutions of v, NA the M weighted densities
+//             of the linearisation state in real space (M x N); the folded (d2Phi).Psi replaces
+//             Psi;
+//   kPhiStoreN  stores the M weighted densities into NA (M x N) and ends there: the set-up of
+//             the Hessian products at a state (no r2c, Cf left as it is).
+// Only kPhiEval sums energies and checks eta (part and those status bits unused otherwise).
+constexpr int kPhiEval = 0, kPhiHess = 1, kPhiStoreN = 2;
+template <class T, int MODEL, int RB, int NF = 0, int MODE = kPhiEval>
+__global__ void __launch_bounds__(PhiThreads<T>::value, MODE == kPhiHess ? 2 : PhiMinBlocks<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
                                                       Dims d, FFTPlan pz_plan, const typename Cx<T>::type* __restrict__ tw, T hsd, T esA,
                                                       T esB, double* __restrict__ part, unsigned* __restrict__ status,
-                                                      const T* __restrict__ NA = nullptr) {
+                                                      T* __restrict__ NA = nullptr) {
   typedef typename Cx<T>::type C;
   constexpr int M = ModelTraits<MODEL>::M;
   constexpr int NP = (M + 1) / 2;
@@ -556,6 +562,19 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, HESS ? 2 : PhiMinBlocks<
       if (gn < ngroup) issue(gn, b);
     }
     C* res = tfft<+1, T, L, LPd, NF, PhiThreads<T>::value>(Z0, Z1, pz_plan, tw);
+    if constexpr (MODE == kPhiStoreN) {
+      for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
+        const int k = e % nz, r = e / nz;
+        if (row0 + r >= d.rows) continue;
+#pragma unroll
+        for (int a = 0; a < M; ++a) {
+          const C z = res[k * LPd + r * NP + a / 2];
+          NA[(long)a * d.N + (row0 + r) * nz + k] = (a & 1) ? z.y : z.x;
+        }
+      }
+      __syncthreads();
+      continue;
+    }
     C* oth = (res == Z0) ? Z1 : Z0;
     for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
       const int k = e % nz, r = e / nz;
@@ -566,7 +585,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, HESS ? 2 : PhiMinBlocks<
         const C z = res[k * LPd + r * NP + a / 2];
         nv[a] = (a & 1) ? z.y : z.x;
       }
-      if constexpr (HESS) {
+      if constexpr (MODE == kPhiHess) {
         T nd[11];
 #pragma unroll
         for (int a = 0; a < M; ++a) nd[a] = NA[(long)a * d.N + (row0 + r) * nz + k];
@@ -594,7 +613,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, HESS ? 2 : PhiMinBlocks<
     }
     __syncthreads();
   }
-  if constexpr (!HESS) {
+  if constexpr (MODE == kPhiEval) {
     if (st) atomicOr(status, st);
     block_kahan_store<1>(&psum, part, blockIdx.x);
   }
