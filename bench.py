@@ -313,6 +313,13 @@ def warm_start_leg(cd, n_train=24, n_test=4, steps=300, tol=1e-8):
     samples = fno.solve_droplets(fno.sample_droplets(n_train + n_test, seed=11), SHAPE, DX)
     out["data_s"] = time.perf_counter() - t0
     train, test = samples[:n_train], samples[n_train:]
+    # one-time costs of the first training steps in a process (library kernels compiled for
+    # this GPU on first use, allocator growth), kept out of train_s and reported apart
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fno.train(fno.FNO3d(), train[:1], SHAPE, steps=2)
+    torch.cuda.synchronize()
+    out["first_use_s"] = time.perf_counter() - t0
     model = fno.FNO3d()
     log = []
     torch.cuda.synchronize()
