@@ -1174,16 +1174,24 @@ static int ddft_rhs(cdft_ctx* c, const double* rho, void* spec, double* rmax) {
 }
 
 // DDFT::step (src/DDFT.cpp:113-182), single species, periodic boundaries.
-static int ddft_one_step(cdft_ctx* c, int* restarts) {
+// The reference evaluates at the step's start, at every fixed-point iterate and at
+// the end. Two of those evaluations repeat one already made at the same density, and
+// (without fixed mass, whose rescaling is not bit-idempotent) are reused bit for bit:
+// the start of a step that follows another in the same call (dF_current: the last
+// step's final evaluation is at this density), and the first iterate of every pass,
+// which starts from d1 = d0, so its right-hand side is the step's first one.
+static int ddft_one_step(cdft_ctx* c, int* restarts, bool dF_current) {
   const long N = c->info.N;
   const size_t nb = N * sizeof(double);
+  const bool reuse = c->fixed_mass <= 0;
   if (!c->ddft_have_factors) {
     double tmp = c->ddft_dt;
     c->ddft_dt = 0;
     ddft_change_timestep(c, tmp);
   }
   double t[8];
-  int rc = eval_internal(c, t);
+  int rc = CDFT_OK;
+  if (!(reuse && dF_current)) rc = eval_internal(c, t);
   if (rc) return rc;
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->dd0, c->rho, nb, cudaMemcpyDeviceToDevice, c->stream));
   CUDA_OR_FAIL(c, cudaMemcpyAsync(c->dd1, c->rho, nb, cudaMemcpyDeviceToDevice, c->stream));
@@ -1199,13 +1207,18 @@ static int ddft_one_step(cdft_ctx* c, int* restarts) {
     double deviation = 1;
     restart = false;
     for (int i = 0; i < 100 && deviation > c->ddft_tol && !restart; i++) {
-      CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rho, c->dd1, nb, cudaMemcpyDeviceToDevice, c->stream));
-      rc = eval_internal(c, t);
-      if (rc) return rc;
-      rc = ddft_rhs(c, c->dd1, c->R1k, nullptr);
-      if (rc) return rc;
       const int nx = c->p.nx, ny = c->p.ny, nzc = c->p.nz / 2 + 1;
       const int pz = c->precision == CDFT_FP64 ? c->e64->pitch() : c->e32->pitch();
+      if (i == 0 && reuse) {  // d1 = d0: the right-hand side of the step's start
+        const size_t sb = (size_t)nx * ny * pz * (c->precision == CDFT_FP64 ? sizeof(double2) : sizeof(float2));
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->R1k, c->R0k, sb, cudaMemcpyDeviceToDevice, c->stream));
+      } else {
+        CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rho, c->dd1, nb, cudaMemcpyDeviceToDevice, c->stream));
+        rc = eval_internal(c, t);
+        if (rc) return rc;
+        rc = ddft_rhs(c, c->dd1, c->R1k, nullptr);
+        if (rc) return rc;
+      }
       const unsigned g = grid_for((long)nx * ny * pz);
       if (c->precision == CDFT_FP64) {
         k_ddft_prop<double><<<g, 256, 0, c->stream>>>((const double2*)c->rk0, (const double2*)c->R0k, (const double2*)c->R1k, (double2*)c->work,
@@ -1261,7 +1274,7 @@ int cdft_ddft_step(cdft_ctx* c, int nsteps, cdft_ddft_report* rep) {
   if (!c->ddft_ready) return fail(c, CDFT_ERR_STATE, "cdft_ddft_init has not been called");
   int restarts = 0;
   for (int k = 0; k < nsteps; ++k) {
-    int rc = ddft_one_step(c, &restarts);
+    int rc = ddft_one_step(c, &restarts, k > 0);
     if (rc) return rc;
   }
   if (rep) {
