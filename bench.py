@@ -243,7 +243,7 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
     return out
 
 
-def batch_leg(cd, n=16, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80, 96), rank=0, world=1, dist=None):
+def batch_leg(cd, n=64, seed=2024, tol=1e-8, max_steps=20000, grids=(48, 64, 80, 96, 112, 128, 144, 160), rank=0, world=1, dist=None):
     """State-point sweep: n LJ droplets (kT ~ U[0.7, 0.94], mu = mu_coex(kT) + U[-0.2, 0.2],
     R ~ U[2, 6] clamped to 0.4 L, cubic grids drawn from `grids`, dx = 0.1, fixed mass),
     all minimised to max|dOmega/drho| <= tol by Newton-Krylov (FIRE2 fallback). Batched
@@ -403,9 +403,9 @@ def main():
     ap.add_argument("--no-fire", action="store_true", help="skip the time-to-residual legs")
     ap.add_argument("--no-ddft", action="store_true", help="skip the 256^3 DDFT leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the state-point sweep leg")
-    ap.add_argument("--sweep-points", type=int, default=16, help="state points in the sweep leg")
+    ap.add_argument("--sweep-points", type=int, default=64, help="state points in the sweep leg")
     ap.add_argument("--no-fno", action="store_true", help="skip the neural-operator warm-start leg")
-    ap.add_argument("--sweep-grids", default="48,64,80,96",
+    ap.add_argument("--sweep-grids", default="48,64,80,96,112,128,144,160",
                     help="grid sizes the sweep draws from (the full range is 48,64,...,160)")
     args = ap.parse_args()
     if args.impl == "reference":

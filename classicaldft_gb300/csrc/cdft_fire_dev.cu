@@ -627,14 +627,17 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
   if (mixed == 3) {
     // Newton-Krylov from the current state: first the fast settings (loose CG while the
     // residual is large, FP32 residuals above 1e-4); if that stalls, again from the same
-    // start with FP64 residuals and CG to 1e-3 throughout; then the mixed = 2 path.
+    // start with FP64 residuals throughout (a path whose last corrections stalled in the
+    // FP32-to-FP64 hand-over near 1e-7 converges this way), then with CG to 1e-3
+    // throughout as well; then the mixed = 2 path.
     cdft_newton_params fast{kNewtonMax3, kNewtonCg, kNewtonRtol, 0.1, 1e-4, 0};
+    cdft_newton_params fp64{2 * kNewtonMax3, kNewtonCg, kNewtonRtol, 0.1, 0.0, 0};
     cdft_newton_params safe{2 * kNewtonMax3, kNewtonCg, kNewtonRtol, 0.0, 0.0, 0};  // slow, steady: allow more corrections
     rc = cdft_internal_newton_ensure(c);
     if (rc) return rc;
     cdft_internal_newton_save(c);
-    for (const cdft_newton_params* p : {&fast, &safe}) {
-      if (p == &safe) cdft_internal_newton_restore(c);
+    for (const cdft_newton_params* p : {&fast, &fp64, &safe}) {
+      if (p != &fast) cdft_internal_newton_restore(c);
       cdft_newton_report nr;
       rc = cdft_newton_refine_ex(c, resid_tol, p, &nr);
       if (rc) return rc;

@@ -188,8 +188,10 @@ int cdft_fire_run_to_residual(cdft_ctx* ctx, double resid_tol, long max_steps, c
  * at the same state and FP64 refinement. mixed = 2: the same FP32 bulk phase,
  * then Newton-Krylov refinement (cdft_newton_refine: FP32 Hessian products,
  * FP64 residuals), falling back to FP64 FIRE2 steps if it stalls. mixed = 3:
- * Newton-Krylov from the current state (up to 40 corrections), falling back to
- * the mixed = 2 path if it stalls. */
+ * Newton-Krylov from the current state (up to 40 corrections; if that stalls,
+ * again from the same start with FP64 residuals throughout, then with CG to
+ * 1e-3 throughout, up to 80 corrections each), falling back to the mixed = 2
+ * path if all stall. */
 int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, long max_steps, int mixed, cdft_fire_report* rep);
 
 /* cdft_fire_run_device on n independent contexts at once (state points of a
