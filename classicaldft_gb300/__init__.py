@@ -34,6 +34,7 @@ C_FUNCTIONS = [
     "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device", "cdft_find_coex",
     "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates", "cdft_hessian_dot_v",
     "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex", "cdft_ddft_matrix_dot_v",
+    "cdft_density_write", "cdft_density_read", "cdft_density_write_vtk",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -133,6 +134,9 @@ def lib():
             "cdft_newton_refine_ex": ([vp, d, P(NewtonParams), P(NewtonReport)], i),
             "cdft_get_radices": ([vp, P(i)], i),
             "cdft_radix_candidates": ([i, P(i), i, P(i)], i),
+            "cdft_density_write": ([ctypes.c_char_p, dp, ctypes.c_long], i),
+            "cdft_density_read": ([ctypes.c_char_p, dp, ctypes.c_long], i),
+            "cdft_density_write_vtk": ([ctypes.c_char_p, dp, i, i, i], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -161,6 +165,33 @@ def fmt_weights(shape, dx, hsd):
     if rc_:
         raise CDFTError(rc_, "bad arguments (hsd < dx?)")
     return w
+
+
+def write_density(path, rho):
+    """Density::writeDensity: the density as an Armadillo arma_binary column vector."""
+    a = np.ascontiguousarray(rho, dtype=np.float64)
+    code = lib().cdft_density_write(os.fsencode(path), _dptr(a), a.size)
+    if code:
+        raise CDFTError(code, "could not write %s" % path)
+
+
+def read_density(path, shape):
+    """Density::readDensity: a density written by write_density (or the reference), as an array of `shape`."""
+    a = np.empty(tuple(shape))
+    code = lib().cdft_density_read(os.fsencode(path), _dptr(a), a.size)
+    if code:
+        raise CDFTError(code, "could not read %d values from %s" % (a.size, path))
+    return a
+
+
+def write_vtk(path, rho):
+    """Density::write_VTK_File: the reference's legacy-VTK ASCII file of a (nx, ny, nz) density."""
+    a = np.ascontiguousarray(rho, dtype=np.float64)
+    if a.ndim != 3:
+        raise ValueError("rho must be a 3D array")
+    code = lib().cdft_density_write_vtk(os.fsencode(path), _dptr(a), *a.shape)
+    if code:
+        raise CDFTError(code, "could not write %s" % path)
 
 
 TERM_NAMES = ("Omega", "F_id", "F_hs", "F_mf", "F_ext", "mu", "resid", "N")

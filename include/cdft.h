@@ -131,6 +131,18 @@ int cdft_find_coex(const cdft_ctx* ctx, double xmax, double dx, double tol, doub
  * the Barker-Henderson diameter int_0^{r0} (1 - exp(-V(r)/kT)) dr, integrated to 1e-15. */
 int cdft_bh_diameter(double sigma, double eps, double rc, double kT, double* out);
 
+/* Density files, host only (no context or GPU needed); rho is the row-major
+ * pos = k + Nz*(j + Ny*i) density of n = Nx*Ny*Nz values.
+ * Density::writeDensity (src/Density.cpp:227-231): Armadillo's arma_binary
+ * column vector ("ARMA_MAT_BIN_FN008\n", "<n> 1\n", n native doubles).
+ * Density::readDensity (src/Density.cpp:233-244): reads that format; CDFT_ERR_ARG
+ * when the file cannot be opened (the reference throws) or does not hold n values.
+ * Density::write_VTK_File (src/Density.cpp:197-225): the legacy-VTK ASCII file of the
+ * reference's VisIt writer (".vtk" appended when missing). */
+int cdft_density_write(const char* path, const double* rho, long n);
+int cdft_density_read(const char* path, double* rho, long n);
+int cdft_density_write_vtk(const char* path, const double* rho, int nx, int ny, int nz);
+
 /* FMT_Species::generateWeights on the host (src/FMT_Species.cpp:310-496), no
  * context or GPU needed: the 11 real-space weight arrays (11*nx*ny*nz values) of a
  * sphere of diameter hsd on an nx*ny*nz lattice of spacing dx. */

@@ -82,6 +82,19 @@ class Density : public Lattice {
   }
   const double* data() const { return rho_.data(); }
   double* data() { return rho_.data(); }
+  // src/Density.cpp:197-244: Armadillo binary snapshot, and the VisIt-writer VTK file
+  void writeDensity(const std::string& filename) const {
+    if (cdft_density_write(filename.c_str(), rho_.data(), (long)rho_.size()) != CDFT_OK)
+      throw std::runtime_error("could not write " + filename);
+  }
+  void readDensity(const char* filename) {
+    if (cdft_density_read(filename, rho_.data(), (long)rho_.size()) != CDFT_OK)
+      throw std::runtime_error(std::string("Could not open input file ") + filename + " ... aborting ... ");
+  }
+  void write_VTK_File(const std::string& filename) const {
+    if (cdft_density_write_vtk(filename.c_str(), rho_.data(), (int)Nx(), (int)Ny(), (int)Nz()) != CDFT_OK)
+      throw std::runtime_error("could not write " + filename);
+  }
 
  private:
   std::vector<double> rho_;

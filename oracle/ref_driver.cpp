@@ -207,6 +207,31 @@ static void case_phi() {
   }
 }
 
+// Density::write_VTK_File (src/Density.cpp:197-225, the reference's VisIt writer
+// src/visit_writer.cpp) on two small seeded densities: 4x3x5 (the last line of values
+// partly filled) and 3x3x3 (27 values: every line full). The files go next to the
+// output file as <out>.a.vtk and <out>.b.vtk; the densities go into the output.
+static void case_files(const std::string& out) {
+  SplitMix64 g(4242);
+  struct Box { const char* tag; double dx; double L[3]; };
+  const Box boxes[2] = {{"a", 0.25, {1.0, 0.75, 1.25}}, {"b", 0.5, {1.5, 1.5, 1.5}}};
+  for (const Box& b : boxes) {
+    double L[3] = {b.L[0], b.L[1], b.L[2]};
+    Density d(b.dx, L);
+    std::vector<double> rho;
+    for (long i = 0; i < d.Nx(); ++i)
+      for (long j = 0; j < d.Ny(); ++j)
+        for (long k = 0; k < d.Nz(); ++k) {
+          const double v = 0.05 + 0.8 * g.uniform();
+          d.set((int)i, (int)j, (int)k, v);
+        }
+    for (long p = 0; p < d.Ntot(); ++p) rho.push_back(d.get_density_real().get(p));
+    put(std::string("files.") + b.tag + ".rho", rho);
+    put(std::string("files.") + b.tag + ".shape", {(double)d.Nx(), (double)d.Ny(), (double)d.Nz()});
+    d.write_VTK_File(out + "." + b.tag + ".vtk");
+  }
+}
+
 // Bulk thermodynamics of one species (hard spheres, and LJ mean field).
 static void case_bulk() {
   const char* models[] = {"Rosenfeld", "RSLT", "esFMT", "WhiteBearI", "WhiteBearII"};
@@ -437,6 +462,8 @@ int main(int argc, char** argv) {
       put("ddfta.F", ddft.F); put("ddfta.t", ddft.t); put("ddfta.dt", ddft.dt);
       put("ddfta.mass", ddft.mass); put("ddfta.rhs", ddft.rhs);
       put("ddfta.rho_final", density_of(*S.d));
+    } else if (c == "files") {
+      case_files(argv[2]);
     } else {
       std::fprintf(stderr, "unknown case %s\n", c.c_str());
       return 2;

@@ -1,7 +1,8 @@
 // A reference-style application (the call sequence of a classicalDFT app) built
 // against include/classicaldft_gb300.hpp: config 1 (hard spheres, WhiteBearI,
 // 32^3 at dx = 0.2, rho = 0.7 (1 + noise)), one evaluation, then FIRE2 steps.
-// Prints "Omega F_hs mu steps F_final sum(Hv) sum|Hv|" for the test to compare.
+// Prints "Omega F_hs mu steps F_final sum(Hv) sum|Hv| max|snapshot - density|" for the test to compare.
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <vector>
@@ -41,7 +42,14 @@ int main(int argc, char** argv) {
   fireMinimizer2 fire(&dft);
   fire.setForceTerminationCriterion(0.0);
   fire.run(fire_steps);
-  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g\n", F, Fhs, species.getChemPotential(), fire.report().total_steps, fire.getF(),
-              hsum, habs);
+  // the density files (src/Density.cpp:197-244): snapshot round trip, and the VTK file
+  density.writeDensity("snapshot.dat");
+  Density back(0.2, L);
+  back.readDensity("snapshot.dat");
+  double snap_diff = 0;
+  for (long p = 0; p < density.Ntot(); ++p) snap_diff = std::max(snap_diff, std::fabs(back.get(p) - density.get(p)));
+  density.write_VTK_File("snapshot");
+  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g %.17g\n", F, Fhs, species.getChemPotential(), fire.report().total_steps,
+              fire.getF(), hsum, habs, snap_diff);
   return 0;
 }

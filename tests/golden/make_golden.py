@@ -5,11 +5,12 @@ lie in the reference checkout, with oracle/refshim standing in for the
 FFTW3 / GSL / Boost / Armadillo libraries that are not installed) and packs
 each driver case into <case>.npz. Run from the repository root:
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference] [--cases c1,c2,...]
 
 The fixtures are committed; the GPU machines never run this script.
 """
 import os
+import shutil
 import struct
 import subprocess
 import sys
@@ -20,7 +21,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 CASES = ["weights", "phi", "bulk", "eval_models16", "eval_hs32", "eval_lj", "fire_hs32", "fire_lj24",
-         "ddft_lj16", "ddft_adapt16", "coex", "hessian"]
+         "ddft_lj16", "ddft_adapt16", "coex", "hessian", "files"]
+# cases that also leave files next to their output: copied here as <case>.<suffix>
+FILE_OUTPUTS = {"files": [".a.vtk", ".b.vtk"]}
 
 
 def read_driver_output(path):
@@ -41,15 +44,23 @@ def read_driver_output(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = sys.argv[1:]
+    cases = CASES
+    if "--cases" in args:
+        i = args.index("--cases")
+        cases = args[i + 1].split(",")
+        del args[i:i + 2]
+    ref = args[0] if args else "/root/reference"
     subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + ref])
     drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
     with tempfile.TemporaryDirectory() as tmp:  # FIRE writes snapshot files into the cwd
-        for case in CASES:
+        for case in cases:
             out = os.path.join(tmp, case + ".bin")
             subprocess.check_call([drv, case, out], cwd=tmp)
             arrays = read_driver_output(out)
             np.savez_compressed(os.path.join(HERE, case + ".npz"), **arrays)
+            for suffix in FILE_OUTPUTS.get(case, []):
+                shutil.copyfile(out + suffix, os.path.join(HERE, case + suffix))
             print(case, len(arrays), "arrays")
 
 

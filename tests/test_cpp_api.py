@@ -32,7 +32,7 @@ def test_reference_style_app_builds(tmp_path):
 def test_reference_style_app_runs_config1(tmp_path):
     exe = str(tmp_path / "app")
     build_app(exe)
-    out = subprocess.check_output([exe, "20"], text=True).split()
+    out = subprocess.check_output([exe, "20"], text=True, cwd=str(tmp_path)).split()
     F, Fhs, mu, steps, Ffin = float(out[0]), float(out[1]), float(out[2]), int(out[3]), float(out[4])
     g = golden("eval_hs32")
     assert abs(F - g["hs32.Omega"][0]) <= 1e-12 * abs(F)
@@ -50,3 +50,6 @@ def test_reference_style_app_runs_config1(tmp_path):
     hsum, habs = float(out[5]), float(out[6])
     assert abs(habs - np.abs(hv).sum()) <= 1e-11 * np.abs(hv).sum()
     assert abs(hsum - hv.sum()) <= 1e-11 * np.abs(hv).sum()
+    # Density::writeDensity / readDensity round trip and write_VTK_File through the mirror
+    assert float(out[7]) == 0.0
+    assert (tmp_path / "snapshot.vtk").read_bytes().startswith(b"# vtk DataFile Version 2.0\nWritten using VisIt writer\nASCII\n")
