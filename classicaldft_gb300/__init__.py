@@ -55,7 +55,8 @@ class Params(ctypes.Structure):
                 ("model", ctypes.c_int), ("es_A", ctypes.c_double), ("es_B", ctypes.c_double),
                 ("hsd", ctypes.c_double), ("lj", ctypes.c_int), ("lj_sigma", ctypes.c_double),
                 ("lj_eps", ctypes.c_double), ("lj_rc", ctypes.c_double), ("kT", ctypes.c_double),
-                ("mu", ctypes.c_double), ("fixed_mass", ctypes.c_double), ("precision", ctypes.c_int)]
+                ("mu", ctypes.c_double), ("fixed_mass", ctypes.c_double), ("precision", ctypes.c_int),
+                ("ao_rp", ctypes.c_double), ("ao_reservoir", ctypes.c_double)]
 
 
 class Info(ctypes.Structure):
@@ -201,12 +202,15 @@ class Context:
     """One system resident on the current CUDA device (the C ABI's cdft_ctx)."""
 
     def __init__(self, shape, dx, model=WHITEBEAR_I, hsd=1.0, lj=False, kT=1.0, rc=3.0, sigma=1.0, eps=1.0,
-                 mu=0.0, fixed_mass=-1.0, precision=FP64, es_A=1.0, es_B=0.0):
+                 mu=0.0, fixed_mass=-1.0, precision=FP64, es_A=1.0, es_B=0.0, ao_rp=0.0, ao_reservoir=0.0):
+        """ao_rp > 0: the species is an FMT_AO_Species, colloids with ideal polymers of radius
+        ao_rp at reservoir density ao_reservoir (src/FMT_Species.cpp:645-738)."""
         if isinstance(shape, int):
             shape = (shape, shape, shape)
         self.shape = tuple(int(s) for s in shape)
         p = Params(self.shape[0], self.shape[1], self.shape[2], dx, model, es_A, es_B,
-                   hsd if hsd is not None else -1.0, int(bool(lj)), sigma, eps, rc, kT, mu, fixed_mass, precision)
+                   hsd if hsd is not None else -1.0, int(bool(lj)), sigma, eps, rc, kT, mu, fixed_mass, precision,
+                   ao_rp, ao_reservoir)
         h = ctypes.c_void_p()
         code = lib().cdft_create(ctypes.byref(p), ctypes.byref(h))
         if code:

@@ -306,6 +306,20 @@ static int fail(cdft_ctx* c, int code, const std::string& m) {
     if (e_ != cudaSuccess) return fail(c, CDFT_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// FMT_AO_Species: the polymer weights (FMT_Species::generateWeights at diameter 2 Rp,
+// src/FMT_Species.cpp:645-664) computed on the host and handed to an evaluator.
+template <class T>
+static int ensure_ao_host(cdft_ctx* c, Evaluator<T>* e, std::string* err) {
+  std::vector<double> wp[11];
+  try {
+    fmt_weights_real(c->p.nx, c->p.ny, c->p.nz, c->p.dx, 2 * c->p.ao_rp, wp);
+  } catch (std::exception& ex) {
+    *err = ex.what();
+    return CDFT_ERR_ARG;
+  }
+  return e->enable_ao(2 * c->p.ao_rp, c->p.ao_reservoir, wp, nullptr, c->stream, err);
+}
+
 static int ensure_evaluator(cdft_ctx* c, int precision) {
   const int nx = c->p.nx, ny = c->p.ny, nz = c->p.nz;
   if ((precision == CDFT_FP64 && c->e64) || (precision == CDFT_FP32 && c->e32)) return CDFT_OK;
@@ -318,6 +332,9 @@ static int ensure_evaluator(cdft_ctx* c, int precision) {
     rc = c->e32->init(nx, ny, nz, c->p.model, c->info.hsd, c->p.es_A, c->p.es_B, nullptr, nullptr, c->tx.get(), c->ty.get(),
                       c->tz.get(), c->stream, &err, fmt ? c->e64->weight_spectra() : nullptr,
                       c->p.lj ? c->e64->att_spectrum() : nullptr);
+    if (!rc && c->p.ao_rp > 0)
+      rc = c->e64->has_ao() ? c->e32->enable_ao(2 * c->p.ao_rp, c->p.ao_reservoir, nullptr, c->e64->ao_spectra(), c->stream, &err)
+                            : ensure_ao_host(c, c->e32.get(), &err);
     if (rc) {
       c->e32.reset();
       return fail(c, rc, err);
@@ -337,11 +354,13 @@ static int ensure_evaluator(cdft_ctx* c, int precision) {
     c->e64.reset(new Evaluator<double>());
     rc = c->e64->init(nx, ny, nz, c->p.model, c->info.hsd, c->p.es_A, c->p.es_B, fmt ? w : nullptr, c->p.lj ? &watt : nullptr, c->tx.get(),
                       c->ty.get(), c->tz.get(), c->stream, &err);
+    if (!rc && c->p.ao_rp > 0) rc = ensure_ao_host(c, c->e64.get(), &err);
     if (rc) c->e64.reset();
   } else {
     c->e32.reset(new Evaluator<float>());
     rc = c->e32->init(nx, ny, nz, c->p.model, c->info.hsd, c->p.es_A, c->p.es_B, fmt ? w : nullptr, c->p.lj ? &watt : nullptr, c->tx.get(),
                       c->ty.get(), c->tz.get(), c->stream, &err);
+    if (!rc && c->p.ao_rp > 0) rc = ensure_ao_host(c, c->e32.get(), &err);
     if (rc) c->e32.reset();
   }
   if (rc) return fail(c, rc, err);
@@ -505,6 +524,8 @@ int cdft_create(const cdft_params* p, cdft_ctx** out) {
   c->info.hsd = p->hsd;
   if (p->lj && p->hsd <= 0) c->info.hsd = bh_diameter_lj(p->lj_sigma, p->lj_eps, p->lj_rc, p->kT);
   if (p->model >= 0 && !(c->info.hsd >= p->dx)) return CDFT_ERR_ARG;  // generateWeights throws for hsd < dx
+  if (p->ao_rp > 0 && (p->model < 0 || !(2 * p->ao_rp >= p->dx) || !(p->ao_reservoir >= 0)))
+    return fail(nullptr, CDFT_ERR_ARG, "the AO model needs an FMT model, polymer diameter >= dx and a reservoir density >= 0");
   if (p->lj) {
     std::vector<double> w;
     double a;
@@ -675,6 +696,7 @@ static int hessian_buffers(cdft_ctx* c) {
 
 int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
   if (!c || !v || !out) return CDFT_ERR_ARG;
+  if (c->p.ao_rp > 0) return fail(c, CDFT_ERR_ARG, "Hessian products are not built for the AO model");
   int rc = hessian_buffers(c);
   if (rc) return rc;
   const size_t nb = c->info.N * sizeof(double);
@@ -694,6 +716,7 @@ int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device)
 // DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): g . (H v) at the current density.
 int cdft_ddft_matrix_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
   if (!c || !v || !out) return CDFT_ERR_ARG;
+  if (c->p.ao_rp > 0) return fail(c, CDFT_ERR_ARG, "Hessian products are not built for the AO model");
   int rc = hessian_buffers(c);
   if (rc) return rc;
   const size_t nb = c->info.N * sizeof(double);
@@ -843,11 +866,16 @@ int cdft_bulk(const cdft_ctx* c, double rho, double* out3) {
     s = t;
   };
   add(std::log(rho));
-  if (m >= 0) add(bulk_muex(m, c->p.es_A, c->p.es_B, c->info.hsd, rho));
+  const bool ao = m >= 0 && c->p.ao_rp > 0;
+  if (m >= 0)  // FMT::BulkMuex, with the AO term when the species is FMT_AO_Species (src/FMT.cpp:616-673)
+    add(bulk_muex(m, c->p.es_A, c->p.es_B, c->info.hsd, rho) +
+        (ao ? bulk_muex_ao(m, c->p.es_A, c->p.es_B, c->info.hsd, 2 * c->p.ao_rp, c->p.ao_reservoir, rho) : 0.0));
   if (c->p.lj) add(0.5 * c->info.a_vdw * rho + 0.5 * c->info.a_vdw * rho);
   const double mu = s + cc;
   double F = rho * std::log(rho) - rho;  // fhelmholtz_times_beta_over_volume (src/DFT.cpp:90-115)
-  if (m >= 0) F += bulk_fex(m, c->p.es_A, c->p.es_B, c->info.hsd, rho);
+  if (m >= 0)
+    F += bulk_fex(m, c->p.es_A, c->p.es_B, c->info.hsd, rho) +
+         (ao ? bulk_fex_ao(m, c->p.es_A, c->p.es_B, c->info.hsd, 2 * c->p.ao_rp, c->p.ao_reservoir, rho) : 0.0);
   if (c->p.lj) F += 0.5 * c->info.a_vdw * rho * rho;
   out3[0] = mu;
   out3[1] = F - rho * mu;

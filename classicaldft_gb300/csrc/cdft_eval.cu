@@ -147,12 +147,12 @@ struct FinishSeg {
   int nv;
   double* out;
 };
-__global__ void __launch_bounds__(192) k_finish_terms(FinishSeg s0, FinishSeg s1, FinishSeg s2) {
+__global__ void __launch_bounds__(224) k_finish_terms(FinishSeg s0, FinishSeg s1, FinishSeg s2, FinishSeg s3) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const FinishSeg* segs[3] = {&s0, &s1, &s2};
+  const FinishSeg* segs[4] = {&s0, &s1, &s2, &s3};
   int v = w;
   const FinishSeg* sg = nullptr;
-  for (int i = 0; i < 3; ++i) {
+  for (int i = 0; i < 4; ++i) {
     if (segs[i]->nv <= 0 || !segs[i]->part) continue;
     if (v < segs[i]->nv) { sg = segs[i]; break; }
     v -= segs[i]->nv;
@@ -178,11 +178,82 @@ __global__ void k_round_spectra(const double* __restrict__ in, T* __restrict__ o
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) out[i] = (T)in[i];
 }
 
+// ------------------------------------------------------------------ AO ---
+// FMT_AO_Species (src/FMT_Species.cpp:694-738, include/Species.h:428-443, src/FMT.cpp:393-421).
+// Psi~ = sum_a w~p_a S_a: the polymer weights times the spectra of the polymer-folded
+// derivative fields (FMT_Weighted_Density::add_weight_schur_dPhi_to_arg: no conjugate, the
+// vector parity is in the fields' sign).
+template <class T>
+__global__ void k_ao_psi(const typename Cx<T>::type* __restrict__ S, const T* __restrict__ w, int M, long Nc,
+                         typename Cx<T>::type* __restrict__ psi) {
+  typedef typename Cx<T>::type C;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < Nc; i += (long)gridDim.x * blockDim.x) {
+    C acc = mk<T>(0, 0);
+    for (int a = 0; a < M; ++a) acc = cadd(acc, mul_weight(S[(long)a * Nc + i], w[(long)a * Nc + i], weight_is_odd(a)));
+    psi[i] = acc;
+  }
+}
+// x <- exp(-x) in place, with the block partials of sum exp(-x) (the AO free energy)
+template <class T>
+__global__ void __launch_bounds__(256) k_ao_exp(T* __restrict__ x, long n, double* __restrict__ part) {
+  KahanT<T> acc;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const T e = exp_t<T>(-x[i]);
+    x[i] = e;
+    acc.add(e);
+  }
+  block_kahan_store<1>(&acc, part, blockIdx.x);
+}
+// Upsilon~_a = w~p_a e~ (FMT_Weighted_Density::convoluteWith of exp(-Psi) with the polymer weights)
+template <class T>
+__global__ void k_ao_upsilon(const typename Cx<T>::type* __restrict__ e, const T* __restrict__ w, int M, long Nc,
+                             typename Cx<T>::type* __restrict__ S) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < Nc; i += (long)gridDim.x * blockDim.x) {
+    const typename Cx<T>::type z = e[i];
+    for (int a = 0; a < M; ++a) S[(long)a * Nc + i] = mul_weight(z, w[(long)a * Nc + i], weight_is_odd(a));
+  }
+}
+// per point: X_a <- reservoir * [sum_b d2Phi(n)/dn_a dn_b Upsilon_b] folded with the colloid
+// diameter, Upsilon read with the polymer diameter (FMT::calculateFreeEnergyAndDerivatives'
+// AO part, src/FMT.cpp:393-421); the reference's later x reservoir x dV is folded here and in
+// the final row pass's dV.
+template <class T, int MODEL>
+__global__ void __launch_bounds__(256) k_ao_force(const T* __restrict__ NA, T* __restrict__ X, long N, T ih, T ih2, T A, T B, T iph,
+                                                  T iph2, T res) {
+  constexpr int M = ModelTraits<MODEL>::M;
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < N; p += (long)gridDim.x * blockDim.x) {
+    T nd[11], up[11];
+#pragma unroll
+    for (int a = 0; a < 11; ++a) {
+      nd[a] = a < M ? NA[(long)a * N + p] : (T)0;
+      up[a] = a < M ? X[(long)a * N + p] : (T)0;
+    }
+    fmt_d2phi_dot_point<T, MODEL>(nd, up, ih, ih2, A, B, iph, iph2);
+    if (ModelTraits<MODEL>::tensor) {
+      // The reference stores the result's tensor through setFundamentalMeasures_AO
+      // (include/Species.h:406-426), whose writes of (j, k) and (k, j) land in the same
+      // symmetric slot, the second overwriting the first: an off-diagonal slot carries one
+      // of the two equal entries, where the folded form above sums both. Kept as the
+      // reference computes it.
+      up[6] *= (T)0.5;
+      up[7] *= (T)0.5;
+      up[9] *= (T)0.5;
+    }
+#pragma unroll
+    for (int a = 0; a < M; ++a) X[(long)a * N + p] = res * up[a];
+  }
+}
+template <class T>
+__global__ void k_spec_add(typename Cx<T>::type* __restrict__ dst, const typename Cx<T>::type* __restrict__ src, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) dst[i] = cadd(dst[i], src[i]);
+}
+
 // ------------------------------------------------------------ Evaluator ---
 template <class T>
 Evaluator<T>::~Evaluator() {
   cudaFree(A_); cudaFree(Cf_); cudaFree(E_); cudaFree(w_); cudaFree(watt_); cudaFree(part_); cudaFree(terms_); cudaFree(status_);
   cudaFree(NA_);
+  cudaFree(wao_); cudaFree(XA_); cudaFree(S_); cudaFree(psi_); cudaFree(psir_); cudaFree(part_ao_);
 }
 
 template <class T>
@@ -384,6 +455,130 @@ bool Evaluator<T>::setup_phi_tma() {
 }
 
 template <class T>
+int Evaluator<T>::enable_ao(double hsdp, double reservoir, const std::vector<double>* w_ao, const double* dev_wao, cudaStream_t s,
+                            std::string* err) {
+  if (M_ == 0) {
+    if (err) *err = "the AO model needs an FMT model";
+    return 4;
+  }
+  if (!tma_phi_) {
+    if (err) *err = "the AO model runs on the tensor-copied Phi pass, which this grid does not fit in this precision";
+    return 4;
+  }
+  if (!w_ao && !dev_wao) return 4;
+  const size_t cs = sizeof(C);
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
+  const unsigned cgrid = (unsigned)std::min<long>(((long)M_ * Nc_ + 255) / 256, 4096);
+  CK(cudaMalloc(&wao_, (size_t)M_ * Nc_ * sizeof(T)));
+  if (dev_wao) {
+    k_round_spectra<T><<<cgrid, 256, 0, s>>>(dev_wao, wao_, (long)M_ * Nc_);
+  } else {  // the polymer weights as the colloid ones: FP64 r2c, the non-zero component, 1/N folded in
+    double* tmp_real = nullptr;
+    double2* tmp_spec = nullptr;
+    CK(cudaMalloc(&tmp_real, N_ * sizeof(double)));
+    CK(cudaMalloc(&tmp_spec, Nc_ * sizeof(double2)));
+    CK(cudaMemsetAsync(tmp_spec, 0, Nc_ * sizeof(double2), s));
+    const unsigned g1 = (unsigned)std::min<long>((Nc_ + 255) / 256, 4096);
+    for (int a = 0; a < M_; ++a) {
+      CK(cudaMemcpyAsync(tmp_real, w_ao[a].data(), N_ * sizeof(double), cudaMemcpyHostToDevice, s));
+      r2c_f64(tmp_real, tmp_spec, d, tx_, ty_, tz_, s);
+      k_compact<T><<<g1, 256, 0, s>>>(tmp_spec, wao_ + (long)a * Nc_, Nc_, (a >= 2 && a <= 4) ? 1 : 0, 1.0 / (double)N_);
+    }
+    CK(cudaStreamSynchronize(s));
+    cudaFree(tmp_real);
+    cudaFree(tmp_spec);
+  }
+  if (!NA_) CK(cudaMalloc(&NA_, (size_t)M_ * N_ * sizeof(T)));
+  CK(cudaMalloc(&XA_, (size_t)M_ * N_ * sizeof(T)));
+  CK(cudaMalloc(&S_, (size_t)M_ * Nc_ * cs));
+  CK(cudaMemsetAsync(S_, 0, (size_t)M_ * Nc_ * cs, s));  // padding columns stay zero
+  CK(cudaMalloc(&psi_, Nc_ * cs));
+  CK(cudaMemsetAsync(psi_, 0, Nc_ * cs, s));
+  CK(cudaMalloc(&psir_, N_ * sizeof(T)));
+  gao_ = (int)std::min<long>((N_ + 255) / 256, 152 * 8);
+  CK(cudaMalloc(&part_ao_, 2 * (size_t)gao_ * sizeof(double)));
+  int nsm = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  with_nf(fz_, [&](auto nf_) {
+    constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
+    auto set_ao = [&](auto kern) {
+      raise_smem(kern, smem_tphi_);
+      int b = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, PhiThreads<T>::value, smem_tphi_);
+      return std::max(b, 1);
+    };
+    int b;
+    switch (model_) {
+      case MODEL_ROSENFELD: b = set_ao(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiAO>); break;
+      case MODEL_RSLT: b = set_ao(k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiAO>); break;
+      case MODEL_ESFMT: b = set_ao(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiAO>); break;
+      case MODEL_WHITEBEAR_I: b = set_ao(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiAO>); break;
+      default: b = set_ao(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiAO>); break;
+    }
+    grid_tao_ = (int)std::min<long>((rows_ + RB - 1) / RB, (long)nsm * b);
+  });
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  ao_hp_ = hsdp;
+  ao_res_ = reservoir;
+  ao_ = true;
+  return 0;
+}
+
+// The AO passes between the Phi pass (which left the polymer-folded derivative fields in
+// XA and the weighted densities in NA) and the y forward pass of the derivative spectra:
+// Psi = c2r(sum_a w~p_a FFT(XA_a)), e = exp(-Psi) (summed for the free energy),
+// Upsilon_a = c2r(w~p_a FFT(e)), then per point reservoir x (d2Phi . Upsilon) folded for
+// the colloid, whose z r2c is added to the derivative spectra in Cf: the back-convolution
+// with the colloid weights then carries the AO force into dF (src/FMT.cpp:393-421).
+template <class T>
+void Evaluator<T>::ao_block(cudaStream_t s) {
+  Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
+  const unsigned gcy = (unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_);
+  const unsigned gcx = (unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_);
+  const unsigned gr = (unsigned)grid_blocks_rows();
+  const unsigned ge = (unsigned)std::min<long>((Nc_ + 255) / 256, 152 * 8);
+  const unsigned gp = (unsigned)std::min<long>((N_ + 255) / 256, 152 * 8);
+  auto rows_fwd = [&](const T* in, C* out) {
+    with_nf(fz_, [&](auto nf_) {
+      k_rows_r2c<T, T, decltype(nf_)::value><<<gr, 256, smem_rows_, s>>>(in, out, d, tz_->plan, twp<T>(tz_), rb_rows_);
+    });
+  };
+  // spectra of the polymer-folded derivative fields
+  for (int a = 0; a < M_; ++a) rows_fwd(XA_ + (long)a * N_, S_ + (long)a * Nc_);
+  k_cols_fft<T, -1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(S_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  k_cols_fft<T, -1><<<dim3(gcx, M_), 256, smem_colx_, s>>>(S_, Nc_, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  // Psi, exp(-Psi) and its sum
+  k_ao_psi<T><<<ge, 256, 0, s>>>(S_, wao_, M_, Nc_, psi_);
+  k_cols_fft<T, +1><<<dim3(gcx, 1), 256, smem_colx_, s>>>(psi_, Nc_, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  k_cols_fft<T, +1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(psi_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  k_rows_c2r<T, T><<<gr, 256, smem_rows_, s>>>(psi_, psir_, d, tz_->plan, twp<T>(tz_), rb_rows_, (T)1);
+  k_ao_exp<T><<<gao_, 256, 0, s>>>(psir_, N_, part_ao_);
+  // Upsilon_a = w~p_a (.) FFT(exp(-Psi)), back to real space in XA
+  rows_fwd(psir_, psi_);
+  k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(psi_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  k_cols_fft<T, -1><<<dim3(gcx, 1), 256, smem_colx_, s>>>(psi_, Nc_, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  k_ao_upsilon<T><<<ge, 256, 0, s>>>(psi_, wao_, M_, Nc_, S_);
+  k_cols_fft<T, +1><<<dim3(gcx, M_), 256, smem_colx_, s>>>(S_, Nc_, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(S_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  for (int a = 0; a < M_; ++a)
+    k_rows_c2r<T, T><<<gr, 256, smem_rows_, s>>>(S_ + (long)a * Nc_, XA_ + (long)a * N_, d, tz_->plan, twp<T>(tz_), rb_rows_, (T)1);
+  // reservoir x (d2Phi(n) . Upsilon) per point, then its z spectra added to the derivative spectra
+  const T ih = (T)(1.0 / hsd_), ih2 = (T)(1.0 / (hsd_ * hsd_)), iph = (T)(1.0 / ao_hp_), iph2 = (T)(1.0 / (ao_hp_ * ao_hp_));
+  const T a = (T)esA_, b = (T)esB_, res = (T)ao_res_;
+  switch (model_) {
+    case MODEL_ROSENFELD: k_ao_force<T, MODEL_ROSENFELD><<<gp, 256, 0, s>>>(NA_, XA_, N_, ih, ih2, a, b, iph, iph2, res); break;
+    case MODEL_RSLT: k_ao_force<T, MODEL_RSLT><<<gp, 256, 0, s>>>(NA_, XA_, N_, ih, ih2, a, b, iph, iph2, res); break;
+    case MODEL_ESFMT: k_ao_force<T, MODEL_ESFMT><<<gp, 256, 0, s>>>(NA_, XA_, N_, ih, ih2, a, b, iph, iph2, res); break;
+    case MODEL_WHITEBEAR_I: k_ao_force<T, MODEL_WHITEBEAR_I><<<gp, 256, 0, s>>>(NA_, XA_, N_, ih, ih2, a, b, iph, iph2, res); break;
+    default: k_ao_force<T, MODEL_WHITEBEAR_II><<<gp, 256, 0, s>>>(NA_, XA_, N_, ih, ih2, a, b, iph, iph2, res); break;
+  }
+  for (int a2 = 0; a2 < M_; ++a2) rows_fwd(XA_ + (long)a2 * N_, S_ + (long)a2 * Nc_);
+  k_spec_add<T><<<ge, 256, 0, s>>>(Cf_, S_, (long)M_ * Nc_);
+}
+
+template <class T>
 int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA, double esB, const std::vector<double>* w_fmt,
                        const std::vector<double>* w_att, FFTTable* tx, FFTTable* ty, FFTTable* tz, cudaStream_t s, std::string* err,
                        const double* dev_w, const double* dev_watt) {
@@ -578,6 +773,21 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     phi_blocks_last_ = nphi;
     if (tma_phi_) {
       phi_blocks_last_ = grid_tphi_;
+      if (ao_) {  // FMT_AO_Species: the Phi pass also leaves NA and the polymer-folded fields
+        const T iph = (T)(1.0 / ao_hp_), iph2 = (T)(1.0 / (ao_hp_ * ao_hp_));
+        phi_blocks_last_ = grid_tao_;
+        with_nf(fz_, [&](auto nf_) {
+          constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
+          switch (model_) {
+            case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
+            case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
+            case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
+            case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
+            default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
+          }
+        });
+        ao_block(s);
+      } else
       switch (model_) {
         case MODEL_ROSENFELD: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_ROSENFELD, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
         case MODEL_RSLT: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_RSLT, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
@@ -620,7 +830,8 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     const FinishSeg sphi{part_phi, phi_blocks_last_, M_ > 0 ? 1 : 0, terms_ + 0};
     const FinishSeg smf{part_mf, (long)gxb, mf_ ? 1 : 0, terms_ + 1};
     const FinishSeg sfin{part_fin, (long)gfin, 4, terms_ + 2};
-    k_finish_terms<<<1, 192, 0, s>>>(sphi, smf, sfin);
+    const FinishSeg sao{part_ao_, (long)gao_, ao_ ? 1 : 0, terms_ + 6};
+    k_finish_terms<<<1, 224, 0, s>>>(sphi, smf, sfin, sao);
   }
   mark(9);
   return 0;
@@ -779,6 +990,8 @@ int Evaluator<T>::finish(double dV, double mu, EvalTerms* out, cudaStream_t s) {
 template <class T>
 int Evaluator<T>::terms_from(const double* h, unsigned st, double dV, double mu, EvalTerms* out) const {
   out->F_hs = M_ > 0 ? h[0] * dV : 0.0;
+  // FMT_AO_Species::free_energy_post_process (src/FMT_Species.cpp:694-738): rho_p (N - sum exp(-Psi)), x dV
+  if (ao_) out->F_hs = (h[0] + ao_res_ * ((double)N_ - h[6])) * dV;
   out->F_mf = mf_ ? 0.5 * dV * h[1] : 0.0;
   out->F_id = h[2];
   out->sum_rho = h[3];

@@ -34,6 +34,9 @@ void qf_kernel_real(int nx, int ny, int nz, double dx, double sigma, double eps,
 double fmt_phi_host(int model, double A, double B, const double fm19[19], double dphi19[19]);
 double bulk_muex(int model, double A, double B, double hsd, double rho);
 double bulk_fex(int model, double A, double B, double hsd, double rho);
+// the AO (polymer) terms of the same, src/FMT.cpp:640-700
+double bulk_muex_ao(int model, double A, double B, double hsd, double hsdp, double rhop, double rho);
+double bulk_fex_ao(int model, double A, double B, double hsd, double hsdp, double rhop, double rho);
 
 struct EvalTerms {
   double F_id, F_hs, F_mf, F_ext, Omega;
@@ -83,6 +86,14 @@ class Evaluator {
   int hess_apply(const RT* v, const double* rho0, RT* out, double dV, cudaStream_t s);
   // Algorithmic bytes each of the 9 passes must move (reads + writes once).
   void pass_bytes(double* bytes) const;
+  // FMT_AO_Species (src/FMT_Species.cpp:645-738, src/FMT.cpp:340-421), after init: ideal
+  // polymers of diameter hsdp at reservoir density `reservoir`. w_ao: the polymer weights in
+  // real space (host), or dev_wao: an FP64 evaluator's compact polymer spectra to round.
+  // Every later evaluation adds the AO free energy to F_hs and its force to dF.
+  int enable_ao(double hsdp, double reservoir, const std::vector<double>* w_ao, const double* dev_wao, cudaStream_t s,
+                std::string* err);
+  bool has_ao() const { return ao_; }
+  const T* ao_spectra() const { return wao_; }
   bool setup_tma(std::string* err);
   int finish(double dV, double mu, EvalTerms* out, cudaStream_t s);
   // the host side of finish: raw device sums h[8] and status -> terms
@@ -125,6 +136,18 @@ class Evaluator {
   unsigned* status_ = nullptr;
   long phi_blocks_last_ = 0;  // blocks of the last Phi launch (its partial sums)
   T* NA_ = nullptr;  // Hessian: M weighted densities of the state, real space (M x N)
+  // AO: polymer weight spectra (M x Nc), the real fields of the AO passes (M x N), their spectra
+  // (M x Nc), Psi's spectrum and real field, and the block partials of sum exp(-Psi)
+  void ao_block(cudaStream_t s);
+  bool ao_ = false;
+  double ao_hp_ = 0, ao_res_ = 0;
+  T* wao_ = nullptr;
+  T* XA_ = nullptr;
+  C* S_ = nullptr;
+  C* psi_ = nullptr;
+  T* psir_ = nullptr;
+  double* part_ao_ = nullptr;
+  int gao_ = 0, grid_tao_ = 0;
   int rb_rows_ = 16, rb_phi_ = 4, tc_ = 16;
   size_t smem_rows_ = 0, smem_phi_ = 0, smem_colx_ = 0, smem_coly_ = 0, smem_xconv_ = 0, smem_xback_ = 0;
   // tensor-copy path (cdft_kernels_tma.cuh)

@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(256) k_hess_rows(typename Cx<T>::type* __restr
       pv[a] = (a & 1) ? z.y : z.x;
       nv[a] = NA[(long)a * d.N + row * nz + k];
     }
-    fmt_d2phi_dot_point<T, MODEL>(nv, pv, ih, ih2, esA, esB);
+    fmt_d2phi_dot_point<T, MODEL>(nv, pv, ih, ih2, esA, esB, ih, ih2);
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       const T im = (2 * p + 1 < M) ? pv[2 * p + 1] : (T)0;

@@ -495,14 +495,17 @@ template <class T> struct PhiMinBlocks { static constexpr int value = sizeof(T) 
 //             of the linearisation state in real space (M x N); the folded (d2Phi).Psi replaces
 //             Psi;
 //   kPhiStoreN  stores the M weighted densities into NA (M x N) and ends there: the set-up of
-//             the Hessian products at a state (no r2c, Cf left as it is).
-// Only kPhiEval sums energies and checks eta (part and those status bits unused otherwise).
-constexpr int kPhiEval = 0, kPhiHess = 1, kPhiStoreN = 2;
+//             the Hessian products at a state (no r2c, Cf left as it is);
+//   kPhiAO    kPhiEval for an FMT_AO_Species, which also stores the M weighted densities
+//             into NA and the derivative fields folded with the polymer diameter (inverse
+//             iph, iph^2 = iph2) into XA, both M x N in real space, for the AO passes.
+// kPhiEval and kPhiAO sum energies and check eta (part and those status bits unused otherwise).
+constexpr int kPhiEval = 0, kPhiHess = 1, kPhiStoreN = 2, kPhiAO = 3;
 template <class T, int MODEL, int RB, int NF = 0, int MODE = kPhiEval>
-__global__ void __launch_bounds__(PhiThreads<T>::value, MODE == kPhiHess ? 2 : PhiMinBlocks<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
+__global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MODE == kPhiAO) ? 2 : PhiMinBlocks<T>::value) k_phi_rows_tma(const __grid_constant__ CUtensorMap mapR, typename Cx<T>::type* __restrict__ Cf,
                                                       Dims d, FFTPlan pz_plan, const typename Cx<T>::type* __restrict__ tw, T hsd, T esA,
                                                       T esB, double* __restrict__ part, unsigned* __restrict__ status,
-                                                      T* __restrict__ NA = nullptr) {
+                                                      T* __restrict__ NA = nullptr, T* __restrict__ XA = nullptr, T iph = 0, T iph2 = 0) {
   typedef typename Cx<T>::type C;
   constexpr int M = ModelTraits<MODEL>::M;
   constexpr int NP = (M + 1) / 2;
@@ -589,13 +592,23 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, MODE == kPhiHess ? 2 : P
         T nd[11];
 #pragma unroll
         for (int a = 0; a < M; ++a) nd[a] = NA[(long)a * d.N + (row0 + r) * nz + k];
-        fmt_d2phi_dot_point<T, MODEL>(nd, nv, ih, ih2, esA, esB);
+        fmt_d2phi_dot_point<T, MODEL>(nd, nv, ih, ih2, esA, esB, ih, ih2);
       } else {
+        const long idx = (row0 + r) * nz + k;
+        if constexpr (MODE == kPhiAO) {
+#pragma unroll
+          for (int a = 0; a < M; ++a) NA[(long)a * d.N + idx] = nv[a];
+        }
+        T ao4[4];
         const T eta = nv[0];
-        const T phi = fmt_phi_point<T, MODEL>(nv, ih, ih2, esA, esB);
+        const T phi = fmt_phi_point<T, MODEL>(nv, ih, ih2, esA, esB, MODE == kPhiAO ? ao4 : nullptr, iph, iph2);
         if (eta > (T)0.5 && (T)1 - eta < (T)0) st |= 1u;
         if (!isfinite(phi)) st |= 2u;
         psum.add(phi);
+        if constexpr (MODE == kPhiAO) {
+#pragma unroll
+          for (int a = 0; a < M; ++a) XA[(long)a * d.N + idx] = (a >= 1 && a <= 4) ? ao4[a - 1] : nv[a];
+        }
       }
 #pragma unroll
       for (int p = 0; p < NP; ++p) oth[k * LPd + r * NP + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
@@ -613,7 +626,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, MODE == kPhiHess ? 2 : P
     }
     __syncthreads();
   }
-  if constexpr (MODE == kPhiEval) {
+  if constexpr (MODE == kPhiEval || MODE == kPhiAO) {
     if (st) atomicOr(status, st);
     block_kahan_store<1>(&psum, part, blockIdx.x);
   }

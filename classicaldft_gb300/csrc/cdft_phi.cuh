@@ -20,6 +20,10 @@ template <> __device__ __forceinline__ float log1m<float>(float e) { return log1
 template <class T> __device__ __forceinline__ T ln_t(T x);
 template <> __device__ __forceinline__ double ln_t<double>(double x) { return log(x); }
 template <> __device__ __forceinline__ float ln_t<float>(float x) { return logf(x); }
+// exponential in the argument's own precision
+template <class T> __device__ __forceinline__ T exp_t(T x);
+template <> __device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
+template <> __device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
 
 // f1, f2, f3 and first derivatives. Divisions are replaced by products with
 // g = 1/(1 - eta) and ie = 1/eta (two reciprocals per point): GB300 runs FP64
@@ -69,8 +73,13 @@ __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, 
 // n[] holds the weighted densities in the order eta, s, v0, v1, v2, T00, T01,
 // T02, T11, T12, T22 (M = 11) or the first five (M = 5). On return n[] holds
 // dPhi/dn_a folded as described above. Returns Phi. ih = 1/hsd, ih2 = 1/hsd^2.
+// ao (optional): the s and v slots folded with the polymer diameter d_p instead
+// (ao[0] = dPhi/ds0 / d_p^2 + dPhi/ds1 / d_p + dPhi/ds2, ao[1 + k] = -(dPhi/dv2_k +
+// dPhi/dv1_k / d_p)): FMT_AO_Species::set_fundamental_measure_derivatives,
+// src/FMT_Species.cpp:667-691; iph = 1/d_p, iph2 = 1/d_p^2. The eta and tensor
+// slots are the same for both species.
 template <class T, int MODEL>
-__device__ __forceinline__ T fmt_phi_point(T* n, T ih, T ih2, T A, T B) {
+__device__ __forceinline__ T fmt_phi_point(T* n, T ih, T ih2, T A, T B, T* ao = nullptr, T iph = 0, T iph2 = 0) {
   const T i_pi = (T)(1.0 / 3.14159265358979323846);
   const T i_2pi = (T)(0.5 / 3.14159265358979323846);
   const T i_24pi = (T)(1.0 / (24 * 3.14159265358979323846));
@@ -146,12 +155,14 @@ __device__ __forceinline__ T fmt_phi_point(T* n, T ih, T ih2, T A, T B) {
   d_s2 += dP3_dS2 * f3;
   n[0] = d_eta;
   n[1] = d_s0 * ih2 + d_s1 * ih + d_s2;
+  if (ao) ao[0] = d_s0 * iph2 + d_s1 * iph + d_s2;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const T d_v1 = i_2pi * (-v2[k]) * f2;
     T d_v2 = i_2pi * (-v1[k]) * f2;
     d_v2 += dP3_dV2[k] * f3;
     n[2 + k] = -(d_v2 + d_v1 * ih);
+    if (ao) ao[1 + k] = -(d_v2 + d_v1 * iph);
   }
   if (ModelTraits<MODEL>::tensor) {
     n[5] = dP3_dT[0][0] * f3;
@@ -201,8 +212,11 @@ __device__ __forceinline__ void fmt_fpp(T e, T L, T& f1pp, T& f2pp, T& f3pp) {
 // back-convolution takes: the s slot sums the s0, s1, s2 rows with 1/d^2, 1/d,
 // 1; the vector slots carry the conjugated (odd) weights' sign; off-diagonal
 // tensor slots sum the (i,j) and (j,i) rows (src/FMT.cpp:530-566).
+// pih, pih2: the diameter p[] is read with (1/d, 1/d^2 of its weights): the
+// colloid's for the Hessian, the polymer's for the AO force, where p[] holds
+// the polymer-weighted convolutions of exp(-Psi) (src/FMT.cpp:393-421).
 template <class T, int MODEL>
-__device__ __forceinline__ void fmt_d2phi_dot_point(const T* n, T* p, T ih, T ih2, T A, T B) {
+__device__ __forceinline__ void fmt_d2phi_dot_point(const T* n, T* p, T ih, T ih2, T A, T B, T pih, T pih2) {
   constexpr bool TEN = ModelTraits<MODEL>::tensor;
   const T one = (T)1;
   const T i_pi = (T)(1.0 / 3.14159265358979323846);
@@ -225,10 +239,10 @@ __device__ __forceinline__ void fmt_d2phi_dot_point(const T* n, T* p, T ih, T ih
       for (int j = 0; j < 3; ++j) Tm[i][j] = (T)0;
   }
   // Psi in the 19-slot form
-  const T Pe = p[0], Ps2 = p[1], Ps1 = p[1] * ih, Ps0 = p[1] * ih2;
+  const T Pe = p[0], Ps2 = p[1], Ps1 = p[1] * pih, Ps0 = p[1] * pih2;
   T Pv2[3], Pv1[3], PT[3][3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) { Pv2[i] = p[2 + i]; Pv1[i] = p[2 + i] * ih; }
+  for (int i = 0; i < 3; ++i) { Pv2[i] = p[2 + i]; Pv1[i] = p[2 + i] * pih; }
   if (TEN) {
     PT[0][0] = p[5]; PT[0][1] = PT[1][0] = p[6]; PT[0][2] = PT[2][0] = p[7];
     PT[1][1] = p[8]; PT[1][2] = PT[2][1] = p[9]; PT[2][2] = p[10];

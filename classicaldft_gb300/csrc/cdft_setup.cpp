@@ -276,29 +276,58 @@ void fmt_weights_real(int nx, int ny, int nz, double dx, double hsd, std::vector
 }
 
 // ------------------------------------------------- bulk thermodynamics ---
+// A value and its derivative along one direction, for exact forward-mode
+// differentiation of the host functional (the AO bulk chemical potential needs
+// the second derivative of Phi along the uniform measures).
+struct Dual {
+  double v = 0, d = 0;
+  Dual() = default;
+  Dual(double x) : v(x) {}
+  Dual(double x, double dx) : v(x), d(dx) {}
+};
+inline Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+inline Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+inline Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+inline Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+inline Dual operator/(Dual a, Dual b) { return Dual(a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)); }
+inline Dual operator+(double a, Dual b) { return Dual(a) + b; }
+inline Dual operator-(double a, Dual b) { return Dual(a) - b; }
+inline Dual operator*(double a, Dual b) { return Dual(a * b.v, a * b.d); }
+inline Dual operator/(double a, Dual b) { return Dual(a) / b; }
+inline Dual operator+(Dual a, double b) { return a + Dual(b); }
+inline Dual operator-(Dual a, double b) { return a - Dual(b); }
+inline Dual operator*(Dual a, double b) { return Dual(a.v * b, a.d * b); }
+inline Dual operator/(Dual a, double b) { return Dual(a.v / b, a.d / b); }
+inline Dual& operator+=(Dual& a, Dual b) { return a = a + b; }
+inline Dual& operator-=(Dual& a, Dual b) { return a = a - b; }
+inline bool operator<(Dual a, double b) { return a.v < b; }
+inline Dual log(Dual a) { return Dual(std::log(a.v), a.d / a.v); }
+
 // FMT on the 19 fundamental measures (FMT::calculate_Phi / calculate_dPhi, src/FMT.cpp:114-176).
-double fmt_phi_host(int model, double A, double B, const double f[19], double d[19]) {
-  const double eta = f[0], s0 = f[1], s1 = f[2], s2 = f[3];
-  const double* v1 = f + 4;
-  const double* v2 = f + 7;
-  double T[3][3];
+template <class R>
+R fmt_phi_t(int model, double A, double B, const R f[19], R d[19]) {
+  using std::log;
+  const R eta = f[0], s0 = f[1], s1 = f[2], s2 = f[3];
+  const R* v1 = f + 4;
+  const R* v2 = f + 7;
+  R T[3][3];
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) T[i][j] = f[10 + 3 * i + j];
-  double vT[3], TT[3][3];
+  R vT[3], TT[3][3];
   for (int i = 0; i < 3; i++) vT[i] = v2[0] * T[0][i] + v2[1] * T[1][i] + v2[2] * T[2][i];
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) TT[i][j] = T[i][0] * T[0][j] + T[i][1] * T[1][j] + T[i][2] * T[2][j];
-  const double v1_v2 = v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2];
-  const double v2_v2 = v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2];
-  const double vTv = v2[0] * vT[0] + v2[1] * vT[1] + v2[2] * vT[2];
-  const double T2 = TT[0][0] + TT[1][1] + TT[2][2];
-  double T3 = 0;
+  const R v1_v2 = v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2];
+  const R v2_v2 = v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2];
+  const R vTv = v2[0] * vT[0] + v2[1] * vT[1] + v2[2] * vT[2];
+  const R T2 = TT[0][0] + TT[1][1] + TT[2][2];
+  R T3 = 0.0;
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) T3 += TT[i][j] * T[j][i];
   // f-functions
-  const double L = std::log(1.0 - eta);
-  double f1 = L, f1p = -1.0 / (1.0 - eta), f2, f2p, f3, f3p;
-  const double g = 1.0 / (1.0 - eta);
+  const R L = log(1.0 - eta);
+  R f1 = L, f1p = -1.0 / (1.0 - eta), f2, f2p, f3, f3p;
+  const R g = 1.0 / (1.0 - eta);
   if (model == MODEL_WHITEBEAR_II) {
     if (eta < 1e-12) {
       f2 = 1 + eta * (1 + eta * ((10.0 / 9) + (7.0 / 6) * eta));
@@ -329,7 +358,9 @@ double fmt_phi_host(int model, double A, double B, const double f[19], double d[
       f3p = 2 * g * g * g;
     }
   }
-  double P3, dS2, dV2[3], dT[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  R P3, dS2, dV2[3], dT[3][3];
+  for (int j = 0; j < 3; j++)
+    for (int k = 0; k < 3; k++) dT[j][k] = 0.0;
   const bool tensor = model >= MODEL_ESFMT;
   if (tensor) {
     const double a = model == MODEL_ESFMT ? A : 1.0, b = model == MODEL_ESFMT ? B : -1.0;
@@ -340,9 +371,9 @@ double fmt_phi_host(int model, double A, double B, const double f[19], double d[
       for (int k = 0; k < 3; k++) dT[j][k] = (a / (8 * M_PI)) * (v2[j] * v2[k] - TT[k][j]) + (b / (4 * M_PI)) * (-s2 * T[k][j] + TT[k][j]);
   } else if (model == MODEL_RSLT) {
     if (s2 < 1e-20) {
-      P3 = dS2 = dV2[0] = dV2[1] = dV2[2] = 0;
+      P3 = dS2 = dV2[0] = dV2[1] = dV2[2] = 0.0;
     } else {
-      const double psi = v2_v2 / (s2 * s2);
+      const R psi = v2_v2 / (s2 * s2);
       P3 = (1.0 / (36 * M_PI)) * s2 * s2 * s2 * (1 - psi) * (1 - psi) * (1 - psi);
       dS2 = (1.0 / (12 * M_PI)) * s2 * s2 * (1 + psi) * (1 - psi) * (1 - psi);
       for (int k = 0; k < 3; k++) dV2[k] = -(1.0 / (6 * M_PI)) * s2 * v2[k] * (1 - psi) * (1 - psi);
@@ -352,12 +383,12 @@ double fmt_phi_host(int model, double A, double B, const double f[19], double d[
     dS2 = (1.0 / (24 * M_PI)) * (3 * s2 * s2 - 3 * v2_v2);
     for (int k = 0; k < 3; k++) dV2[k] = (1.0 / (24 * M_PI)) * (-6 * s2 * v2[k]);
   }
-  double phi = 0;
+  R phi = 0.0;
   phi -= (1 / M_PI) * s0 * f1;
   phi += (1 / (2 * M_PI)) * (s1 * s2 - v1_v2) * f2;
   phi += P3 * f3;
   if (d) {
-    std::memset(d, 0, 19 * sizeof(double));
+    for (int i = 0; i < 19; i++) d[i] = 0.0;
     d[0] -= (1 / M_PI) * s0 * f1p;
     d[0] += (1 / (2 * M_PI)) * (s1 * s2 - v1_v2) * f2p;
     d[0] += P3 * f3p;
@@ -376,6 +407,11 @@ double fmt_phi_host(int model, double A, double B, const double f[19], double d[
   }
   return phi;
 }
+
+
+// The same in FP64, and along a direction (Dual: value and derivative, exact
+// forward-mode differentiation) for the AO bulk terms below.
+double fmt_phi_host(int model, double A, double B, const double f[19], double d[19]) { return fmt_phi_t<double>(model, A, B, f, d); }
 
 static void uniform_measures(double rho, double d, double f[19]) {  // FundamentalMeasures::fillUniform
   std::memset(f, 0, 19 * sizeof(double));
@@ -400,6 +436,35 @@ double bulk_fex(int model, double A, double B, double hsd, double rho) {
   double f[19];
   uniform_measures(rho, hsd, f);
   return fmt_phi_host(model, A, B, f, nullptr);
+}
+
+// The AO terms of FMT::BulkMuex / BulkFex (src/FMT.cpp:640-700) for colloids of
+// diameter hsd and polymers of diameter hsdp at reservoir density rhop:
+//   arg(rho) = sum_i dPhi_i(n(rho)) wp_i,  wp = the uniform measures of unit density
+//   and diameter hsdp;  f_AO = rhop (1 - exp(-arg));
+//   mu_AO = rhop exp(-arg) sum_i (d2Phi(n) . w)_i wp_i = rhop exp(-arg) d arg / d rho,
+// since the uniform measures n(rho) = rho w are linear in rho: the second derivative
+// along w is the rho-derivative of arg, taken here exactly by forward differentiation.
+static Dual ao_arg(int model, double A, double B, double hsd, double hsdp, double rho) {
+  double fu[19], wp[19];
+  uniform_measures(rho, hsd, fu);
+  double w1[19];
+  uniform_measures(1.0, hsd, w1);
+  Dual f[19], d[19];
+  for (int i = 0; i < 19; i++) f[i] = Dual(fu[i], w1[i]);
+  fmt_phi_t<Dual>(model, A, B, f, d);
+  uniform_measures(1.0, hsdp, wp);
+  Dual arg = 0.0;
+  for (int i = 0; i < 19; i++) arg += d[i] * wp[i];
+  return arg;
+}
+double bulk_muex_ao(int model, double A, double B, double hsd, double hsdp, double rhop, double rho) {
+  const Dual a = ao_arg(model, A, B, hsd, hsdp, rho);
+  return rhop * a.d * std::exp(-a.v);
+}
+double bulk_fex_ao(int model, double A, double B, double hsd, double hsdp, double rhop, double rho) {
+  const Dual a = ao_arg(model, A, B, hsd, hsdp, rho);
+  return rhop - rhop * std::exp(-a.v);
 }
 
 }  // namespace cdft

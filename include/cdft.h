@@ -54,6 +54,8 @@ typedef struct cdft_params {
   double mu;         /* Species::setChemPotential (beta mu) */
   double fixed_mass; /* > 0: Species::setFixedMass */
   int precision;     /* CDFT_FP64 or CDFT_FP32 */
+  double ao_rp;        /* > 0: FMT_AO_Species (src/FMT_Species.cpp:645-738): ideal polymers of radius ao_rp */
+  double ao_reservoir; /*   at reservoir density ao_reservoir (the Asakura-Oosawa model); needs an FMT model */
 } cdft_params;
 
 typedef struct cdft_info {

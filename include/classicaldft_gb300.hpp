@@ -149,6 +149,10 @@ class FMT_Species {
   FMT_Species(Density& density, double hsd, double mu = 0, int seq = -1) : density_(density), hsd_(hsd), mu_(mu) {
     (void)seq;
   }
+  virtual ~FMT_Species() {}
+  // the polymer radius and reservoir density of an FMT_AO_Species (0 for a plain FMT_Species)
+  virtual double aoRp() const { return 0.0; }
+  virtual double getReservoirDensity() const { return 0.0; }
   void setChemPotential(double m) { mu_ = m; fixedMass_ = -1; }
   double getChemPotential() const { return mu_; }
   void setFixedMass(double m) { fixedMass_ = m; if (m > 0.0) mu_ = 0.0; }
@@ -170,6 +174,19 @@ class FMT_Species {
   double hsd_, mu_;
   double fixedMass_ = -1;
   std::vector<double> dF_;
+};
+
+// include/Species.h:380-461, src/FMT_Species.cpp:645-738: hard-sphere colloids with ideal
+// polymers of radius Rp at the given reservoir density (the Asakura-Oosawa model)
+class FMT_AO_Species : public FMT_Species {
+ public:
+  FMT_AO_Species(Density& density, double hsd, double Rp, double reservoir_density, double mu = 0, int seq = -1)
+      : FMT_Species(density, hsd, mu, seq), Rp_(Rp), reservoir_(reservoir_density) {}
+  double aoRp() const override { return Rp_; }
+  double getReservoirDensity() const override { return reservoir_; }
+  double getHSDP() const { return 2 * Rp_; }
+ private:
+  double Rp_, reservoir_;
 };
 
 // include/Interaction.h:416-441 (self interaction of one species)
@@ -252,6 +269,8 @@ class DFT {
       p.mu = s_->getChemPotential();
       p.fixed_mass = s_->fixedMass();
       p.precision = precision_;
+      p.ao_rp = s_->aoRp();
+      p.ao_reservoir = s_->getReservoirDensity();
       check(cdft_create(&p, &ctx_), nullptr);
     }
     return ctx_;

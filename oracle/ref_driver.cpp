@@ -462,6 +462,35 @@ int main(int argc, char** argv) {
       put("ddfta.F", ddft.F); put("ddfta.t", ddft.t); put("ddfta.dt", ddft.dt);
       put("ddfta.mass", ddft.mass); put("ddfta.rhs", ddft.rhs);
       put("ddfta.rho_final", density_of(*S.d));
+    } else if (c == "ao") {
+      // FMT_AO_Species (src/FMT_Species.cpp:645-738, src/FMT.cpp:340-421): hard-sphere colloids
+      // (d = 1) with ideal polymers of radius Rp = 0.35 at reservoir density 0.4 (the
+      // Asakura-Oosawa model), one F+dF evaluation each for a model without and with the
+      // tensor measures, and the bulk mu / omega with the AO terms (src/FMT.cpp:616-709).
+      const char* models[] = {"Rosenfeld", "WhiteBearI"};
+      for (const char* m : models) {
+        double L[3] = {3.2, 3.2, 3.2};
+        Density* d = new Density(0.2, L);
+        FMT_AO_Species* s = new FMT_AO_Species(*d, 1.0, 0.35, 0.4, 0.0, 0);
+        FMT* fmt = make_fmt(m);
+        DFT* dft = new DFT(s);
+        dft->addHardCoreContribution(fmt);
+        fill_noise(*d, 0.4, 0.2, 13);
+        s->setChemPotential(dft->mu_times_beta(0.4));
+        double F = dft->calculateFreeEnergyAndDerivatives(false);
+        const std::string tag = std::string("ao16.") + m;
+        put1(tag + ".Omega", F);
+        put1(tag + ".F_id", dft->get_f_id());
+        put1(tag + ".F_hs", dft->get_f_hs());
+        put1(tag + ".F_ext", dft->get_f_ext());
+        put1(tag + ".mu", s->getChemPotential());
+        put(tag + ".dF", vec_of(dft->getDF(0)));
+        put(tag + ".rho", density_of(*d));
+        std::vector<double> mu, om;
+        for (double r : {0.05, 0.2, 0.4, 0.6}) { mu.push_back(dft->mu_times_beta(r)); om.push_back(dft->omega_times_beta_over_volume(r)); }
+        put(tag + ".bulk_mu", mu);
+        put(tag + ".bulk_omega", om);
+      }
     } else if (c == "files") {
       case_files(argv[2]);
     } else {
