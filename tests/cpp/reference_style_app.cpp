@@ -1,7 +1,7 @@
 // A reference-style application (the call sequence of a classicalDFT app) built
 // against include/classicaldft_gb300.hpp: config 1 (hard spheres, WhiteBearI,
 // 32^3 at dx = 0.2, rho = 0.7 (1 + noise)), one evaluation, then FIRE2 steps.
-// Prints "Omega F_hs mu steps F_final sum(Hv) sum|Hv| max|snapshot - density|" for the test to compare.
+// Prints "Omega F_hs mu steps F_final sum(Hv) sum|Hv| max|snapshot - density| Omega_AO" for the test to compare.
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -49,7 +49,21 @@ int main(int argc, char** argv) {
   double snap_diff = 0;
   for (long p = 0; p < density.Ntot(); ++p) snap_diff = std::max(snap_diff, std::fabs(back.get(p) - density.get(p)));
   density.write_VTK_File("snapshot");
-  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g %.17g\n", F, Fhs, species.getChemPotential(), fire.report().total_steps,
-              fire.getF(), hsum, habs, snap_diff);
+  // optional: an FMT_AO_Species system (WhiteBearI, d = 1, Rp = 0.35, reservoir 0.4) on the
+  // 16^3, dx = 0.2 density read from the snapshot argv[2]
+  double FA = 0;
+  if (argc > 2) {
+    double LA[3] = {3.2, 3.2, 3.2};
+    Density dA(0.2, LA);
+    dA.readDensity(argv[2]);
+    FMT_AO_Species sa(dA, 1.0, 0.35, 0.4, 0.0, 0);
+    WhiteBearI fmtA;
+    DFT dftA(&sa);
+    dftA.addHardCoreContribution(&fmtA);
+    sa.setChemPotential(dftA.mu_times_beta(0.4));
+    FA = dftA.calculateFreeEnergyAndDerivatives(false);
+  }
+  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g %.17g %.17g\n", F, Fhs, species.getChemPotential(), fire.report().total_steps,
+              fire.getF(), hsum, habs, snap_diff, FA);
   return 0;
 }

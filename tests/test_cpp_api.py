@@ -32,7 +32,10 @@ def test_reference_style_app_builds(tmp_path):
 def test_reference_style_app_runs_config1(tmp_path):
     exe = str(tmp_path / "app")
     build_app(exe)
-    out = subprocess.check_output([exe, "20"], text=True, cwd=str(tmp_path)).split()
+    import classicaldft_gb300 as cd
+    ao = golden("ao")
+    cd.write_density(str(tmp_path / "ao_rho.dat"), ao["ao16.WhiteBearI.rho"])
+    out = subprocess.check_output([exe, "20", str(tmp_path / "ao_rho.dat")], text=True, cwd=str(tmp_path)).split()
     F, Fhs, mu, steps, Ffin = float(out[0]), float(out[1]), float(out[2]), int(out[3]), float(out[4])
     g = golden("eval_hs32")
     assert abs(F - g["hs32.Omega"][0]) <= 1e-12 * abs(F)
@@ -53,3 +56,5 @@ def test_reference_style_app_runs_config1(tmp_path):
     # Density::writeDensity / readDensity round trip and write_VTK_File through the mirror
     assert float(out[7]) == 0.0
     assert (tmp_path / "snapshot.vtk").read_bytes().startswith(b"# vtk DataFile Version 2.0\nWritten using VisIt writer\nASCII\n")
+    # FMT_AO_Species through the mirror, on a density handed over as a reference snapshot file
+    assert abs(float(out[8]) - ao["ao16.WhiteBearI.Omega"][0]) <= 1e-12 * abs(ao["ao16.WhiteBearI.Omega"][0])
