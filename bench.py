@@ -101,6 +101,8 @@ class Clocks:
 
 
 def cpu_baseline(budget_s=15.0, steps=None):
+    # every host core: torchrun sets OMP_NUM_THREADS=1 for its ranks, and only one rank runs this
+    os.environ["OMP_NUM_THREADS"] = str(os.cpu_count())
     from oracle import pyoracle
     o = pyoracle.Oracle(SHAPE, DX, "WhiteBearI", hsd=None, lj=True, kT=KT)
     o.set_mu(o.mu_times_beta(RHO_V))
@@ -121,10 +123,8 @@ def run_reference(args):
     if rank != 0:
         return
     steps = max(1, args.steps)
-    for _ in range(min(args.warmup, 1)):
-        pass
-    rate, n, el = cpu_baseline(steps=steps)
-    cores = os.cpu_count()
+    rate, n, el = cpu_baseline(steps=steps)  # its first evaluation is an untimed warm-up
+    cores = int(os.environ["OMP_NUM_THREADS"])
     line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": "evals/s", "n_gpus": args.gpus,
             "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * el / n, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload(),
@@ -511,7 +511,7 @@ def main():
         line["warm_start"] = warm_start_leg(cd)
     if rank == 0 and not args.no_cpu_baseline:
         rate, n, el = cpu_baseline()
-        line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",
+        line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
                                 "sample": "%d FP64 F+dF evaluations of the same 128^3 system by the oracle in %.1f s" % (n, el)}
     if rank == 0:
         print(json.dumps(line), flush=True)
