@@ -513,6 +513,12 @@ def main():
         rate, n, el = cpu_baseline()
         line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
                                 "sample": "%d FP64 F+dF evaluations of the same 128^3 system by the oracle in %.1f s" % (n, el)}
+        fr = line.get("fire_to_resid_1e-8")
+        if fr:  # the CPU time to resid 1e-8, extrapolated: one FP64 evaluation per FIRE2 step
+            steps = fr["plain_fp64"]["fire_steps"]
+            fr["cpu_oracle_plain_fp64_extrapolated_s"] = steps / rate
+            fr["cpu_note"] = ("%d FIRE2 steps of the GPU's plain FP64 run x the oracle's seconds per FP64 evaluation "
+                              "(the BLAS-1 work of a step left out), labelled extrapolated" % steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
