@@ -100,3 +100,17 @@ def test_ao_fire_lowers_omega(cd):
     t1, _ = c.eval(want_dF=False)
     assert r["newton"] == 0 and t1["Omega"] < t0["Omega"] and t1["resid"] < t0["resid"]
     c.close()
+
+
+def test_ao_ddft_conserves_mass(cd):
+    """DDFT steps on the AO functional: the integrating-factor step keeps the mass."""
+    g = golden("ao")
+    c = cd.Context(16, 0.2, cd.WHITEBEAR_I, hsd=1.0, ao_rp=RP, ao_reservoir=RES)
+    c.set_chem_potential(c.bulk(0.4)["mu"])
+    rho = g["ao16.WhiteBearI.rho"].reshape(16, 16, 16)
+    c.set_density(rho)
+    c.ddft_init(1e-4, 1e-3)
+    r = c.ddft_step(20)
+    m0 = rho.sum() * 0.2 ** 3
+    assert abs(r["mass"] - m0) <= 1e-12 * m0 and np.isfinite(r["F"])
+    c.close()
