@@ -201,7 +201,7 @@ def eval_256_leg(cd, steps=10):
                        for p in passes]}
 
 
-def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
+def fire_legs(cd, rho, tol=1e-8, max_steps=20000, legs=("newton", "mixed_newton", "mixed_fire", "plain_fp64")):
     """Wall seconds to reach max|dOmega/drho| <= tol on the droplet at fixed mass,
     every leg device-resident and starting from the same tanh profile, FIRE2 with
     the reference defaults (dt = 1e-3, dt_max = 1e-2):
@@ -221,6 +221,8 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
            "newton": "Newton-Krylov from the tanh profile (CG to 1e-3, FP32 Hessian products, FP64 residuals)"}
     res = {}
     for name, mixed, sw in (("newton", 3, 1e-4), ("mixed_newton", 2, 1e-4), ("mixed_fire", 1, 2e-6), ("plain_fp64", 0, 2e-6)):
+        if name not in legs:
+            continue
         c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT, fixed_mass=mass)
         c.set_density(rho)
         c.fire_init(force_limit=0.0)
@@ -235,6 +237,8 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000):
                      "Omega": t["Omega"], "converged": bool(t["resid"] <= tol)}
         c.close()
     out.update(res)
+    if len(res) < 4:  # a subset of the legs (e.g. for a profile): no ratios
+        return out
     plain = res["plain_fp64"]
     out["speedup_mixed_vs_plain"] = plain["seconds"] / res["newton"]["seconds"]
     out["speedup_mixed_newton_vs_plain"] = plain["seconds"] / res["mixed_newton"]["seconds"]
@@ -402,6 +406,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fire", action="store_true", help="skip the time-to-residual legs")
+    ap.add_argument("--fire-legs", default="newton,mixed_newton,mixed_fire,plain_fp64",
+                    help="time-to-residual legs to run (a subset reports no speed-ups)")
     ap.add_argument("--no-ddft", action="store_true", help="skip the 256^3 DDFT leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the state-point sweep leg")
     ap.add_argument("--sweep-points", type=int, default=64, help="state points in the sweep leg")
@@ -503,7 +509,7 @@ def main():
             line["statepoint_sweep"] = sweep
     # the single-GPU legs below are reported by rank 0 only (the other replicas skip them)
     if rank == 0 and not args.no_fire:
-        line["fire_to_resid_1e-8"] = fire_legs(cd, rho)
+        line["fire_to_resid_1e-8"] = fire_legs(cd, rho, legs=tuple(args.fire_legs.split(",")))
     if rank == 0 and not args.no_ddft:
         line["eval_256"] = eval_256_leg(cd)
         line["ddft_256"] = ddft_leg(cd)
@@ -514,7 +520,7 @@ def main():
         line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
                                 "sample": "%d FP64 F+dF evaluations of the same 128^3 system by the oracle in %.1f s" % (n, el)}
         fr = line.get("fire_to_resid_1e-8")
-        if fr:  # the CPU time to resid 1e-8, extrapolated: one FP64 evaluation per FIRE2 step
+        if fr and "plain_fp64" in fr:  # the CPU time to resid 1e-8, extrapolated: one FP64 evaluation per FIRE2 step
             steps = fr["plain_fp64"]["fire_steps"]
             fr["cpu_oracle_plain_fp64_extrapolated_s"] = steps / rate
             fr["cpu_note"] = ("%d FIRE2 steps of the GPU's plain FP64 run x the oracle's seconds per FP64 evaluation "
