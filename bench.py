@@ -201,6 +201,32 @@ def eval_256_leg(cd, steps=10):
                        for p in passes]}
 
 
+def spectral_leg(cd, rho):
+    """The spectral drivers at 128^3 on the droplet functional (host clock around each
+    call; every call synchronises): Log_Det (order 20, 2 probes = 40 Hessian products) on
+    the droplet density in FP64 and FP32, and Eigenvalues on the uniform fluid at
+    rho = 0.3 (its smallest eigenvalue, the unstable k = 0 mode, to a residual of 1e-8)."""
+    n = 128
+    out = {"grid": [n, n, n]}
+    hsd = cd.bh_diameter(1.0, 1.0, 3.0, KT)
+    for prec in ("FP64", "FP32"):
+        c = cd.Context((n, n, n), DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT, precision=getattr(cd, prec))
+        c.set_density(rho)
+        c.log_det(2, 0.2, 1e-4, 1, 1)  # warm-up (buffers, weighted densities)
+        t0 = time.perf_counter()
+        val, var = c.log_det(20, 0.2, 1e-4, 1234, 2)
+        el = time.perf_counter() - t0
+        out["log_det_" + prec.lower()] = {"seconds": el, "hessian_products": 40, "products_per_s": 40 / el, "log_det": val}
+        c.close()
+    c = cd.Context((n, n, n), DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT)
+    c.set_density(np.full((n, n, n), 0.3))
+    t0 = time.perf_counter()
+    lam, _, rep = c.eigenvalue(tol=1e-8, max_matvecs=3000)
+    out["eigenvalue_uniform_fp64"] = {"seconds": time.perf_counter() - t0, "eigenvalue": lam, **rep}
+    c.close()
+    return out
+
+
 def fire_legs(cd, rho, tol=1e-8, max_steps=20000, legs=("newton", "mixed_newton", "mixed_fire", "plain_fp64")):
     """Wall seconds to reach max|dOmega/drho| <= tol on the droplet at fixed mass,
     every leg device-resident and starting from the same tanh profile, FIRE2 with
@@ -412,6 +438,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the state-point sweep leg")
     ap.add_argument("--sweep-points", type=int, default=64, help="state points in the sweep leg")
     ap.add_argument("--no-fno", action="store_true", help="skip the neural-operator warm-start leg")
+    ap.add_argument("--no-spectral", action="store_true", help="skip the Log_Det / Eigenvalues leg")
     ap.add_argument("--sweep-grids", default="48,64,80,96,112,128,144,160",
                     help="grid sizes the sweep draws from (the full range is 48,64,...,160)")
     args = ap.parse_args()
@@ -513,6 +540,8 @@ def main():
     if rank == 0 and not args.no_ddft:
         line["eval_256"] = eval_256_leg(cd)
         line["ddft_256"] = ddft_leg(cd)
+    if rank == 0 and not args.no_spectral:
+        line["spectral_128"] = spectral_leg(cd, rho)
     if rank == 0 and not args.no_fno:
         line["warm_start"] = warm_start_leg(cd)
     if rank == 0 and not args.no_cpu_baseline:

@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(HERE, "libcdft.so")
 OK, ERR_ETA, ERR_NONFINITE, ERR_TIMEOUT, ERR_ARG, ERR_CUDA, ERR_UPHILL, ERR_STATE = range(8)
 MODEL_NONE, ROSENFELD, RSLT_MODEL, ESFMT, WHITEBEAR_I, WHITEBEAR_II = -1, 0, 1, 2, 3, 4
 FP64, FP32 = 0, 1
+MATRIX_HESSIAN, MATRIX_DDFT = 0, 1
 
 C_FUNCTIONS = [
     "cdft_create", "cdft_destroy", "cdft_last_error", "cdft_set_stream", "cdft_get_info", "cdft_set_precision",
@@ -34,7 +35,8 @@ C_FUNCTIONS = [
     "cdft_fire_run_to_residual", "cdft_ddft_init", "cdft_ddft_step", "cdft_time_passes", "cdft_fmt_weights", "cdft_number_of_atoms_noalloc", "cdft_fire_run_device", "cdft_find_coex",
     "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates", "cdft_hessian_dot_v",
     "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex", "cdft_ddft_matrix_dot_v",
-    "cdft_density_write", "cdft_density_read", "cdft_density_write_vtk",
+    "cdft_density_write", "cdft_density_read", "cdft_density_write_vtk", "cdft_log_det", "cdft_eigenvalue",
+    "cdft_arnoldi_largest",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -96,6 +98,11 @@ class DdftReport(ctypes.Structure):
                 ("restarts", ctypes.c_int)]
 
 
+class EigenReport(ctypes.Structure):
+    _fields_ = [("matvecs", ctypes.c_long), ("restarts", ctypes.c_int), ("converged", ctypes.c_int),
+                ("residual", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -138,6 +145,9 @@ def lib():
             "cdft_density_write": ([ctypes.c_char_p, dp, ctypes.c_long], i),
             "cdft_density_read": ([ctypes.c_char_p, dp, ctypes.c_long], i),
             "cdft_density_write_vtk": ([ctypes.c_char_p, dp, i, i, i], i),
+            "cdft_log_det": ([vp, i, i, d, d, ctypes.c_long, i, i, dp, dp], i),
+            "cdft_eigenvalue": ([vp, d, d, i, vp, vp, ctypes.c_long, dp, vp, i, P(EigenReport)], i),
+            "cdft_arnoldi_largest": ([vp, d, i, i, i, ctypes.c_long, d, vp, dp, vp, i, P(EigenReport)], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -379,6 +389,53 @@ class Context:
         o = np.empty(self.shape)
         self._check(lib().cdft_ddft_matrix_dot_v(self._h, a.ctypes.data_as(ctypes.c_void_p), o.ctypes.data_as(ctypes.c_void_p), 0))
         return o
+
+    # spectral drivers (Log_Det, Eigenvalues, Arnoldi on the Hessian)
+    def log_det(self, order, lam_max, lam_min, seed, num_samples, has_zero_eigenvalue=False, matrix=MATRIX_HESSIAN):
+        """Log_Det(matrix, order, lam_max, lam_min).calculate_log_det(seed, num_samples,
+        has_zero_eigenvalue) at the current density; returns (log_det, variance)."""
+        val, var = ctypes.c_double(), ctypes.c_double()
+        self._check(lib().cdft_log_det(self._h, matrix, order, lam_max, lam_min, seed, num_samples, int(has_zero_eigenvalue),
+                                       ctypes.byref(val), ctypes.byref(var)))
+        return val.value, var.value
+
+    @staticmethod
+    def _eigen_rep(r):
+        return {"matvecs": r.matvecs, "restarts": r.restarts, "converged": bool(r.converged), "residual": r.residual}
+
+    def _host_vec(self, v):
+        if v is None:
+            return None, None
+        a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        if a.size != int(np.prod(self.shape)):
+            raise ValueError("expected %d values" % int(np.prod(self.shape)))
+        return a, a.ctypes.data_as(ctypes.c_void_p)
+
+    def eigenvalue(self, scale=1e6, tol=1e-6, change_sign=False, vshift=None, guess=None, max_matvecs=20000):
+        """Eigenvalues(dft).calculate_eigenvector with set_scale / set_tolerence /
+        set_change_sign / set_vshift: the smallest eigenvalue of the Hessian plus
+        vshift vshift^T / 2 (the largest with change_sign); returns (eigenvalue, unit
+        eigenvector, report)."""
+        vs, vsp = self._host_vec(vshift)
+        gs, gsp = self._host_vec(guess)
+        val = ctypes.c_double()
+        vec = np.empty(self.shape)
+        r = EigenReport()
+        self._check(lib().cdft_eigenvalue(self._h, scale, tol, int(change_sign), vsp, gsp, max_matvecs, ctypes.byref(val),
+                                          vec.ctypes.data_as(ctypes.c_void_p), 0, ctypes.byref(r)))
+        return val.value, vec, self._eigen_rep(r)
+
+    def arnoldi(self, shift, k, p, all_k=True, max_steps=1000, tol=1e-8, guess=None):
+        """Arnoldi(dft).determine_largest_eigenpairs(shift, k, p, all_k, max_steps, tol):
+        the k eigenpairs of H + shift of largest magnitude; returns (eigenvalues without
+        the shift, eigenvectors (k, *shape), report)."""
+        gs, gsp = self._host_vec(guess)
+        vals = np.empty(k)
+        vecs = np.empty((k,) + tuple(self.shape))
+        r = EigenReport()
+        self._check(lib().cdft_arnoldi_largest(self._h, shift, k, p, int(all_k), max_steps, tol, gsp, _dptr(vals),
+                                               vecs.ctypes.data_as(ctypes.c_void_p), 0, ctypes.byref(r)))
+        return vals, vecs, self._eigen_rep(r)
 
     # FFT plans
     def autotune(self, reps=5):

@@ -713,6 +713,28 @@ int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device)
   return CDFT_OK;
 }
 
+// y = M x between device arrays, M the Hessian (matrix 0) or the DDFT matrix g . H
+// (matrix 1), for the spectral drivers; prepare = true first stores the weighted
+// densities of the current density. x and y must not be the context's hv_out.
+// (C++ linkage: an internal helper between the ABI's entry points.)
+}  // extern "C"
+int cdft_internal_matvec(cdft_ctx* c, int matrix, const double* x, double* y, bool prepare) {
+  if (c->p.ao_rp > 0) return fail(c, CDFT_ERR_ARG, "Hessian products are not built for the AO model");
+  int rc = hessian_buffers(c);
+  if (rc) return rc;
+  if (prepare) {
+    rc = c->precision == CDFT_FP64 ? c->e64->hess_prepare(c->rho, c->stream) : c->e32->hess_prepare(c->rho, c->stream);
+    if (rc) return fail(c, CDFT_ERR_CUDA, "Hessian prepare failed");
+  }
+  double* hv = matrix == 0 ? y : c->hv_out;
+  rc = c->precision == CDFT_FP64 ? c->e64->hess_apply<double>(x, c->rho, hv, c->info.dV, c->stream)
+                                 : c->e32->hess_apply<double>(x, c->rho, hv, c->info.dV, c->stream);
+  if (rc) return fail(c, CDFT_ERR_CUDA, "Hessian launch failed");
+  if (matrix != 0) k_g_dot_x<<<grid_for(c->info.N), 256, 0, c->stream>>>(c->rho, hv, y, c->p.nx, c->p.ny, c->p.nz, c->p.dx);
+  return cudaGetLastError() == cudaSuccess ? CDFT_OK : fail(c, CDFT_ERR_CUDA, "matrix product launch failed");
+}
+extern "C" {
+
 // DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): g . (H v) at the current density.
 int cdft_ddft_matrix_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
   if (!c || !v || !out) return CDFT_ERR_ARG;

@@ -97,6 +97,8 @@ void cdft_internal_newton_save(cdft_ctx* c);
 void cdft_internal_newton_restore(cdft_ctx* c);
 // FIRE2 state re-derived from the current density: x = alias(rho), v = 0, one evaluation
 int cdft_internal_fire_resync(cdft_ctx* c);
+// y = M x on the device (M: 0 the Hessian, 1 the DDFT matrix g . H; cdft_api.cu)
+int cdft_internal_matvec(cdft_ctx* c, int matrix, const double* x, double* y, bool prepare);
 // plans cdft_autotune chose for the context's shape, model and precision (cdft_tune.cu)
 bool cdft_internal_tuned_plans(const cdft_ctx* c, int precision, std::array<std::vector<int>, 3>* plans);
 std::vector<std::vector<int>> cdft_internal_radix_candidates(int n);

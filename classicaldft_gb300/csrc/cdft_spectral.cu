@@ -1,0 +1,565 @@
+// Spectral drivers on the matrices of the path (consumers of the Hessian product):
+//   Log_Det::calculate_log_det          (include/Log_Det.h, src/Log_Det.cpp:23-166)
+//   Eigenvalues::calculate_eigenvector  (include/Eigenvalues.h, src/Eigenvalues.cpp)
+//   Arnoldi::determine_largest_eigenpairs (include/Arnoldi.h, src/Arnoldi.cpp:72-283)
+// Every vector lives on the device and every product is the context's Hessian pass;
+// the host holds only scalars and the small projected matrices.
+//
+// Log_Det keeps the reference's estimator exactly: the Chebyshev coefficients of log,
+// the three-term recurrence and Hutchinson's trace with the +-1 vectors that
+// std::mt19937(seed) and uniform_int_distribution<>(0, 1) give, drawn in point order
+// (the host draws sample i + 1 while the device runs sample i). Eigenvalues and Arnoldi
+// compute what the reference computes (the smallest eigenvalue of the signed, scaled and
+// rank-one shifted Hessian; the k eigenpairs of H + shift of largest magnitude) with a
+// thick-restart Lanczos iteration, fully re-orthogonalised, instead of nlopt's L-BFGS on
+// the Rayleigh quotient and Armadillo's complex implicitly restarted Arnoldi: the
+// Hessian is symmetric, so its Krylov projection is symmetric and real.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+#include "cdft_ctx.h"
+
+namespace {
+
+constexpr int kDotBlocks = 512;  // partial sums per dot product (fixed: the sums are deterministic)
+constexpr int kRitzChunk = 16;   // Ritz vectors formed per pass of the basis
+
+// part[i * kDotBlocks + b] = block b's share of V_i . w for i < nv (V_i = V + i * N)
+__global__ void __launch_bounds__(256) k_dots(const double* __restrict__ V, int nv, const double* __restrict__ w, long N,
+                                              double* __restrict__ part) {
+  __shared__ double red[8];
+  const int i = blockIdx.y;
+  const double* v = V + (long)i * N;
+  double acc = 0;
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) acc += v[p] * w[p];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int k = 0; k < 8; ++k) s += red[k];
+    part[(long)i * kDotBlocks + blockIdx.x] = s;
+  }
+  (void)nv;
+}
+// out[i] = sum of part[i * kDotBlocks ...] in a fixed tree order; one block per vector
+__global__ void __launch_bounds__(256) k_dots_finish(const double* __restrict__ part, double* __restrict__ out) {
+  __shared__ double red[8];
+  const double* q = part + (long)blockIdx.x * kDotBlocks;
+  double acc = 0;
+  for (int b = threadIdx.x; b < kDotBlocks; b += 256) acc += q[b];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int k = 0; k < 8; ++k) s += red[k];
+    out[blockIdx.x] = s;
+  }
+}
+// w -= sum_{i < nv} h_i V_i (h on the device)
+__global__ void __launch_bounds__(256) k_sub_proj(const double* __restrict__ V, int nv, const double* __restrict__ h, double* __restrict__ w,
+                                                  long N) {
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) {
+    double s = 0;
+    for (int i = 0; i < nv; ++i) s += h[i] * V[(long)i * N + p];
+    w[p] -= s;
+  }
+}
+// y <- a * y + b * (s . x) * s + c * x, with the dot s . x read from the device
+// (Eigenvalues::calculate_gradients' vshift term, src/Eigenvalues.cpp:47-51, and the shift)
+__global__ void __launch_bounds__(256) k_op_finish(double* __restrict__ y, const double* __restrict__ x, const double* __restrict__ s,
+                                                   const double* __restrict__ sdotx, double a, double b, double c, long N) {
+  const double bs = s ? b * sdotx[0] : 0.0;
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) {
+    double v = a * y[p] + c * x[p];
+    if (s) v += bs * s[p];
+    y[p] = v;
+  }
+}
+// dst = src / sqrt(nrm2[0])
+__global__ void __launch_bounds__(256) k_normalise(const double* __restrict__ src, double* __restrict__ dst, const double* __restrict__ nrm2,
+                                                   long N) {
+  const double f = 1.0 / sqrt(nrm2[0]);
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) dst[p] = src[p] * f;
+}
+// out_q = sum_j V_j S[j * ldS + q] for q < nq (nq <= kRitzChunk), S in device memory
+__global__ void __launch_bounds__(256) k_ritz(const double* __restrict__ V, int nj, const double* __restrict__ S, int ldS, int nq,
+                                              double* __restrict__ out, long N) {
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) {
+    double acc[kRitzChunk];
+#pragma unroll
+    for (int q = 0; q < kRitzChunk; ++q) acc[q] = 0;
+    for (int j = 0; j < nj; ++j) {
+      const double v = V[(long)j * N + p];
+#pragma unroll
+      for (int q = 0; q < kRitzChunk; ++q)
+        if (q < nq) acc[q] += v * S[j * ldS + q];
+    }
+#pragma unroll
+    for (int q = 0; q < kRitzChunk; ++q)
+      if (q < nq) out[(long)q * N + p] = acc[q];
+  }
+}
+// a seeded start vector: splitmix64 of (seed, point), uniform in [-1, 1)
+__global__ void __launch_bounds__(256) k_seed_vector(double* __restrict__ x, long N, unsigned long long seed) {
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) {
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ULL * (unsigned long long)(p + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    x[p] = 2.0 * ((double)(z >> 11) * (1.0 / 9007199254740992.0)) - 1.0;
+  }
+}
+
+// Chebyshev steps of Log_Det::calculate_log_det (src/Log_Det.cpp:104-137). r = M x
+// from the matrix pass; the matrix the estimator expands is A x = sg r + z sum(x)
+// (sg = -1 for a dynamic matrix, z = lam_mid / N when it has a zero eigenvalue).
+// First term: w1 = al (A v) + be v; u = c0 v + c1 w1.
+__global__ void __launch_bounds__(256) k_cheb_first(const double* __restrict__ r, const double* __restrict__ v, const double* __restrict__ sum_v,
+                                                    double sg, double z, double al, double be, double c0, double c1, double* __restrict__ w1,
+                                                    double* __restrict__ u, long N) {
+  const double zs = z * sum_v[0];
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) {
+    const double x = v[p];
+    const double w = (sg * r[p] + zs) * al + be * x;
+    w1[p] = w;
+    u[p] = c0 * x + c1 * w;
+  }
+}
+// Next term, in place over w0: w2 = al (A w1) + be w1 - w0; u += ck w2.
+__global__ void __launch_bounds__(256) k_cheb_next(const double* __restrict__ r, const double* __restrict__ w1, const double* __restrict__ sum_w1,
+                                                   double sg, double z, double al, double be, double ck, double* __restrict__ w0,
+                                                   double* __restrict__ u, long N) {
+  const double zs = z * sum_w1[0];
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) {
+    const double w = (sg * r[p] + zs) * al + be * w1[p] - w0[p];
+    w0[p] = w;
+    u[p] += ck * w;
+  }
+}
+// part[b] = block b's share of sum(x)
+__global__ void __launch_bounds__(256) k_sum(const double* __restrict__ x, long N, double* __restrict__ part) {
+  __shared__ double red[8];
+  double acc = 0;
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) acc += x[p];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int k = 0; k < 8; ++k) s += red[k];
+    part[blockIdx.x] = s;
+  }
+}
+
+}  // namespace
+
+#define SP_CK(c, x)                                                                        \
+  do {                                                                                     \
+    cudaError_t e_ = (x);                                                                  \
+    if (e_ != cudaSuccess) return cdft_internal_fail(c, CDFT_ERR_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+namespace {
+
+unsigned sp_grid(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + 255) / 256, 152 * 8)); }
+
+// Device work arrays of one driver call (freed on return).
+struct DevBuf {
+  std::vector<void*> ptrs;
+  ~DevBuf() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  double* get(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(double)) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return (double*)p;
+  }
+};
+
+// out[0..nv) = V_i . w (device), through part (nv * kDotBlocks doubles)
+void dots(const double* V, int nv, const double* w, long N, double* part, double* out, cudaStream_t s) {
+  k_dots<<<dim3(kDotBlocks, nv), 256, 0, s>>>(V, nv, w, N, part);
+  k_dots_finish<<<nv, 256, 0, s>>>(part, out);
+}
+
+// Symmetric eigen-decomposition of the n x n matrix A (row-major) by cyclic Jacobi
+// rotations: eigenvalues in w, eigenvectors in the columns of Z (row-major, Z[i * n + k]).
+void jacobi_eigen(std::vector<double> A, int n, std::vector<double>& w, std::vector<double>& Z) {
+  Z.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) Z[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0, diag = 0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) (i == j ? diag : off) += A[(size_t)i * n + j] * A[(size_t)i * n + j];
+    if (off <= 1e-30 * diag || off == 0) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[(size_t)p * n + q];
+        if (apq == 0) continue;
+        const double app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q];
+        const double theta = (aqq - app) / (2 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+        const double cs = 1 / std::sqrt(t * t + 1), sn = t * cs;
+        for (int k = 0; k < n; ++k) {  // A <- J^T A J
+          const double akp = A[(size_t)k * n + p], akq = A[(size_t)k * n + q];
+          A[(size_t)k * n + p] = cs * akp - sn * akq;
+          A[(size_t)k * n + q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double apk = A[(size_t)p * n + k], aqk = A[(size_t)q * n + k];
+          A[(size_t)p * n + k] = cs * apk - sn * aqk;
+          A[(size_t)q * n + k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double zkp = Z[(size_t)k * n + p], zkq = Z[(size_t)k * n + q];
+          Z[(size_t)k * n + p] = cs * zkp - sn * zkq;
+          Z[(size_t)k * n + q] = sn * zkp + cs * zkq;
+        }
+      }
+  }
+  w.resize(n);
+  for (int i = 0; i < n; ++i) w[i] = A[(size_t)i * n + i];
+}
+
+// Log_Det::get_coefficients (src/Log_Det.cpp:32-57): the Chebyshev coefficients of
+// log(0.5 (b - a) x + 0.5 (b + a)) on [-1, 1] at the order + 1 Chebyshev nodes.
+std::vector<double> log_cheb_coefficients(int order, double a, double b) {
+  std::vector<double> c(order + 1, 0.0);
+  for (int k = 0; k <= order; ++k) {
+    const double xk = std::cos(M_PI * (k + 0.5) / (order + 1));
+    double Tm2 = 0, Tm1 = 0, T = 1;
+    for (int j = 0; j <= order; ++j) {
+      T = j == 0 ? 1.0 : j == 1 ? xk : 2 * xk * Tm1 - Tm2;
+      c[j] += std::log(0.5 * (b - a) * xk + 0.5 * (b + a)) * T;
+      Tm2 = Tm1;
+      Tm1 = T;
+    }
+  }
+  for (int j = 0; j <= order; ++j) c[j] *= (j == 0 ? 1.0 : 2.0) / (order + 1);
+  return c;
+}
+
+}  // namespace
+
+int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_min, long seed, int num_samples, int has_zero_eigenvalue,
+                 double* log_det, double* variance) {
+  if (!c || !log_det) return CDFT_ERR_ARG;
+  if ((matrix != CDFT_MATRIX_HESSIAN && matrix != CDFT_MATRIX_DDFT) || order < 1 || num_samples < 1 || !(lam_max > lam_min) ||
+      !(lam_min + lam_max > 0))
+    return cdft_internal_fail(c, CDFT_ERR_ARG, "log_det: needs order >= 1, num_samples >= 1 and lam_max > lam_min with lam_min + lam_max > 0");
+  const long N = c->info.N;
+  const double scale = 1.0 / (lam_min + lam_max), a = lam_min * scale, b = lam_max * scale, lam_mid = 0.5 * (lam_max + lam_min);
+  const std::vector<double> cf = log_cheb_coefficients(order, a, b);
+  const double sg = matrix == CDFT_MATRIX_DDFT ? -1.0 : 1.0, z = has_zero_eigenvalue ? lam_mid / (double)N : 0.0;
+  cudaStream_t s = c->stream;
+  DevBuf buf;
+  double *v = buf.get(N), *w0 = buf.get(N), *w1 = buf.get(N), *u = buf.get(N), *r = buf.get(N), *part = buf.get(kDotBlocks),
+         *scal = buf.get(2 + (size_t)num_samples);
+  if (!v || !w0 || !w1 || !u || !r || !part || !scal) return cdft_internal_fail(c, CDFT_ERR_CUDA, "log_det: out of device memory");
+  SP_CK(c, cudaMemsetAsync(scal, 0, (2 + (size_t)num_samples) * sizeof(double), s));  // sum(x) stays 0 without a zero eigenvalue
+  // two pinned +-1 vectors: the host draws the next sample while the device runs this one
+  double* hv[2] = {nullptr, nullptr};
+  for (auto& h : hv)
+    if (cudaMallocHost(&h, N * sizeof(double)) != cudaSuccess) {
+      for (auto& g : hv)
+        if (g) cudaFreeHost(g);
+      return cdft_internal_fail(c, CDFT_ERR_CUDA, "log_det: pinned buffers");
+    }
+  struct Pinned {
+    double** p;
+    ~Pinned() { cudaFreeHost(p[0]); cudaFreeHost(p[1]); }
+  } pinned{hv};
+  cudaEvent_t copied[2];
+  cudaEventCreateWithFlags(&copied[0], cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&copied[1], cudaEventDisableTiming);
+  struct Ev {
+    cudaEvent_t* e;
+    ~Ev() { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
+  } evs{copied};
+  if (seed <= 0) seed = (long)std::random_device{}();
+  std::mt19937 rng((unsigned long)seed);
+  std::uniform_int_distribution<> distrib(0, 1);
+  auto draw = [&](double* h) {
+    for (long p = 0; p < N; ++p) h[p] = distrib(rng) > 0 ? 1.0 : -1.0;
+  };
+  draw(hv[0]);
+  const unsigned g = sp_grid(N);
+  bool prepared = false;
+  auto matvec = [&](const double* x, double* y) -> int {
+    int rc = cdft_internal_matvec(c, matrix, x, y, !prepared);
+    prepared = true;
+    return rc;
+  };
+  auto sum_of = [&](const double* x, double* out) {
+    k_sum<<<kDotBlocks, 256, 0, s>>>(x, N, part);
+    k_dots_finish<<<1, 256, 0, s>>>(part, out);
+  };
+  for (int i = 0; i < num_samples; ++i) {
+    const int cur = i & 1;
+    SP_CK(c, cudaMemcpyAsync(v, hv[cur], N * sizeof(double), cudaMemcpyHostToDevice, s));
+    SP_CK(c, cudaEventRecord(copied[cur], s));
+    int rc = matvec(v, r);
+    if (rc) return rc;
+    if (z != 0) sum_of(v, scal);
+    k_cheb_first<<<g, 256, 0, s>>>(r, v, scal, sg, z, scale * 2.0 / (b - a), -(b + a) / (b - a), cf[0], cf[1], w1, u, N);
+    double *p0 = w0, *p1 = w1;  // w0 holds the term before w1: v for k = 2
+    SP_CK(c, cudaMemcpyAsync(p0, v, N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (i + 1 < num_samples) {  // draw the next vector into the other pinned buffer once its last copy is done
+      SP_CK(c, cudaEventSynchronize(copied[cur ^ 1]));
+      draw(hv[cur ^ 1]);
+    }
+    for (int k = 2; k <= order; ++k) {
+      rc = matvec(p1, r);
+      if (rc) return rc;
+      if (z != 0) sum_of(p1, scal);
+      k_cheb_next<<<g, 256, 0, s>>>(r, p1, scal, sg, z, scale * 4.0 / (b - a), -2.0 * (b + a) / (b - a), cf[k], p0, u, N);
+      std::swap(p0, p1);
+    }
+    dots(v, 1, u, N, part, scal + 2 + i, s);
+    SP_CK(c, cudaGetLastError());
+  }
+  std::vector<double> vu(num_samples);
+  SP_CK(c, cudaMemcpyAsync(vu.data(), scal + 2, num_samples * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SP_CK(c, cudaStreamSynchronize(s));
+  // the reference's running sums (src/Log_Det.cpp:139-161)
+  double acc = 0, acc2 = 0, var = 0;
+  for (int i = 1; i <= num_samples; ++i) {
+    acc += vu[i - 1];
+    acc2 += vu[i - 1] * vu[i - 1];
+    const double av = acc / i, av2 = acc2 / i;
+    var = std::sqrt(std::fabs(av2 - av * av));
+  }
+  double ld = acc / num_samples;
+  if (has_zero_eigenvalue) ld -= std::log(lam_mid);
+  ld -= (double)N * std::log(scale);
+  *log_det = ld;
+  if (variance) *variance = var;
+  return CDFT_OK;
+}
+
+namespace {
+
+// The symmetric operator the eigen drivers iterate on:
+// y = a (H x + 0.5 (vshift . x) vshift) + shift x, H the context's Hessian.
+struct SymOp {
+  cdft_ctx* c;
+  double a, shift;
+  const double* vshift;  // device, or null
+  double *part, *sdot;
+  bool prepared;
+  long matvecs;
+  int apply(const double* x, double* y) {
+    const long N = c->info.N;
+    int rc = cdft_internal_matvec(c, CDFT_MATRIX_HESSIAN, x, y, !prepared);
+    if (rc) return rc;
+    prepared = true;
+    ++matvecs;
+    if (vshift) dots(vshift, 1, x, N, part, sdot, c->stream);
+    k_op_finish<<<sp_grid(N), 256, 0, c->stream>>>(y, x, vshift, sdot, a, 0.5 * a, shift, N);
+    return CDFT_OK;
+  }
+};
+
+enum class Want { Smallest, LargestMagnitude };
+
+struct LanczosResult {
+  std::vector<double> theta, resid;  // wanted Ritz values of the operator and their residual norms
+  bool converged = false;
+  int restarts = 0;
+};
+
+// Thick-restart Lanczos with full (twice-applied) re-orthogonalisation for the nev wanted
+// eigenpairs of a symmetric operator; the basis V (ncv + 1 vectors) and the Ritz vectors
+// stay on the device, the projected ncv x ncv matrix on the host. x0 is the (device)
+// start vector. Converged when every wanted pair (only the first with all = false) has
+// |residual| <= tol |theta - shift|, or (degenerate_rule) lies within tol of the first
+// discarded Ritz value (the stopping rule of src/Arnoldi.cpp:240-262). vecs (nev * N, device) receives the
+// Ritz vectors, unit norm.
+int lanczos(cdft_ctx* c, SymOp& op, Want want, int nev, int ncv, double tol, bool all, bool degenerate_rule, long max_matvecs,
+            int max_restarts, const double* x0, double* vecs, LanczosResult* out) {
+  const long N = c->info.N;
+  cudaStream_t s = c->stream;
+  const unsigned g = sp_grid(N);
+  DevBuf buf;
+  double* V = buf.get((size_t)(ncv + 1) * N);
+  double* Y = buf.get((size_t)ncv * N);
+  double* w = buf.get(N);
+  double* part = buf.get((size_t)(ncv + 1) * kDotBlocks);
+  double* dh = buf.get(2 * (size_t)(ncv + 1) + 2);
+  double* dS = buf.get((size_t)ncv * ncv);
+  if (!V || !Y || !w || !part || !dh || !dS) return cdft_internal_fail(c, CDFT_ERR_CUDA, "eigen solver: out of device memory");
+  op.part = part;
+  op.sdot = dh + 2 * (ncv + 1) + 1;
+  const int ob = ncv + 1, onrm = 2 * (ncv + 1);
+  // v0 = x0 / |x0|
+  dots(x0, 1, x0, N, part, dh + onrm, s);
+  k_normalise<<<g, 256, 0, s>>>(x0, V, dh + onrm, N);
+  std::vector<double> H((size_t)ncv * ncv, 0.0), hh(2 * (size_t)(ncv + 1) + 1), theta, Z;
+  int nkeep = 0;
+  for (;;) {
+    int m = ncv;
+    double beta = 0;
+    for (int j = nkeep; j < ncv; ++j) {
+      double* vj = V + (long)j * N;
+      int rc = op.apply(vj, w);
+      if (rc) return rc;
+      dots(V, j + 1, w, N, part, dh, s);
+      k_sub_proj<<<g, 256, 0, s>>>(V, j + 1, dh, w, N);
+      dots(V, j + 1, w, N, part, dh + ob, s);
+      k_sub_proj<<<g, 256, 0, s>>>(V, j + 1, dh + ob, w, N);
+      dots(w, 1, w, N, part, dh + onrm, s);
+      k_normalise<<<g, 256, 0, s>>>(w, V + (long)(j + 1) * N, dh + onrm, N);
+      SP_CK(c, cudaMemcpyAsync(hh.data(), dh, hh.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+      SP_CK(c, cudaStreamSynchronize(s));
+      double hnorm = 0;
+      for (int i = 0; i <= j; ++i) {
+        const double h = hh[i] + hh[ob + i];
+        H[(size_t)i * ncv + j] = H[(size_t)j * ncv + i] = h;
+        hnorm = std::max(hnorm, std::fabs(h));
+      }
+      beta = std::sqrt(std::max(hh[onrm], 0.0));
+      if (!std::isfinite(beta)) return cdft_internal_fail(c, CDFT_ERR_NONFINITE, "eigen solver: non-finite Krylov vector");
+      if (beta <= 1e-14 * hnorm) {  // an invariant subspace: its Ritz pairs are exact
+        m = j + 1;
+        beta = 0;
+        break;
+      }
+    }
+    std::vector<double> Hm((size_t)m * m);
+    for (int i = 0; i < m; ++i)
+      for (int k = 0; k < m; ++k) Hm[(size_t)i * m + k] = H[(size_t)i * ncv + k];
+    jacobi_eigen(Hm, m, theta, Z);
+    std::vector<int> idx(m);
+    for (int i = 0; i < m; ++i) idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
+      return want == Want::Smallest ? theta[x] < theta[y] : std::fabs(theta[x]) > std::fabs(theta[y]);
+    });
+    const int nw = std::min(nev, m);
+    out->theta.assign(nw, 0.0);
+    out->resid.assign(nw, 0.0);
+    bool conv = true;
+    for (int i = 0; i < nw; ++i) {
+      const int q = idx[i];
+      out->theta[i] = theta[q];
+      out->resid[i] = beta * std::fabs(Z[(size_t)(m - 1) * m + q]);
+      const bool degenerate = degenerate_rule && m > nw && std::fabs(theta[q] - theta[idx[nw]]) <= tol;
+      if (out->resid[i] > tol * std::fabs(theta[q] - op.shift) && !degenerate && (all || i == 0)) conv = false;
+    }
+    out->converged = conv;
+    const bool stop = conv || beta == 0 || op.matvecs >= max_matvecs || out->restarts >= max_restarts;
+    // the Ritz vectors to keep: the wanted ones for output, or about half the basis to restart with
+    const int nk = stop ? nw : std::min(m - 1, std::max(nw + (m - nw) / 2, nw));
+    std::vector<double> Ssel((size_t)m * nk);
+    for (int j = 0; j < m; ++j)
+      for (int q = 0; q < nk; ++q) Ssel[(size_t)j * nk + q] = Z[(size_t)j * m + idx[q]];
+    SP_CK(c, cudaMemcpyAsync(dS, Ssel.data(), Ssel.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    double* dst = stop ? vecs : Y;
+    for (int q0 = 0; q0 < nk; q0 += kRitzChunk)
+      k_ritz<<<g, 256, 0, s>>>(V, m, dS + q0, nk, std::min(kRitzChunk, nk - q0), dst + (long)q0 * N, N);
+    if (stop) {
+      for (int q = 0; q < nk; ++q) {
+        dots(vecs + (long)q * N, 1, vecs + (long)q * N, N, part, dh + onrm, s);
+        k_normalise<<<g, 256, 0, s>>>(vecs + (long)q * N, vecs + (long)q * N, dh + onrm, N);
+      }
+      SP_CK(c, cudaStreamSynchronize(s));  // dS is host-visible until here
+      SP_CK(c, cudaGetLastError());
+      return CDFT_OK;
+    }
+    // thick restart: V <- [Ritz vectors, the last Krylov direction]; H <- diag(theta) plus
+    // the couplings the next column recomputes
+    SP_CK(c, cudaMemcpyAsync(V, Y, (size_t)nk * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    SP_CK(c, cudaMemcpyAsync(V + (long)nk * N, V + (long)m * N, N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    SP_CK(c, cudaStreamSynchronize(s));
+    std::fill(H.begin(), H.end(), 0.0);
+    for (int q = 0; q < nk; ++q) H[(size_t)q * ncv + q] = theta[idx[q]];
+    nkeep = nk;
+    ++out->restarts;
+  }
+}
+
+// the start vector: the caller's guess (host or device) or the seeded one
+int start_vector(cdft_ctx* c, const double* guess, int on_device, long seed, double* x0) {
+  const long N = c->info.N;
+  if (guess)
+    SP_CK(c, cudaMemcpyAsync(x0, guess, N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  else
+    k_seed_vector<<<sp_grid(N), 256, 0, c->stream>>>(x0, N, (unsigned long long)seed);
+  return CDFT_OK;
+}
+
+}  // namespace
+
+// Eigenvalues::calculate_eigenvector (src/Eigenvalues.cpp:66-99; objective :43-64): the
+// smallest eigenvalue of sg scale (H + vshift vshift^T / 2), sg = -1 with change_sign,
+// reported as the reference reports it (divided by scale, sign restored).
+int cdft_eigenvalue(cdft_ctx* c, double scale, double tol, int change_sign, const double* vshift, const double* guess, long max_matvecs,
+                    double* eigval, double* eigvec, int on_device, cdft_eigen_report* rep) {
+  if (!c || !eigval) return CDFT_ERR_ARG;
+  const long N = c->info.N;
+  if (!(scale > 0) || !(tol > 0) || max_matvecs < 1 || N < 2)
+    return cdft_internal_fail(c, CDFT_ERR_ARG, "eigenvalue: needs scale > 0, tol > 0 and max_matvecs >= 1");
+  DevBuf buf;
+  double *x0 = buf.get(N), *vec = buf.get(N), *vs = vshift ? buf.get(N) : nullptr;
+  if (!x0 || !vec || (vshift && !vs)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "eigenvalue: out of device memory");
+  if (vshift)
+    SP_CK(c, cudaMemcpyAsync(vs, vshift, N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  int rc = start_vector(c, guess, on_device, 20240601, x0);
+  if (rc) return rc;
+  const double a = (change_sign ? -1.0 : 1.0) * scale;
+  SymOp op{c, a, 0.0, vs, nullptr, nullptr, false, 0};
+  const int ncv = (int)std::min<long>(24, N);
+  LanczosResult r;
+  rc = lanczos(c, op, Want::Smallest, 1, ncv, tol, true, false, max_matvecs, 1 << 30, x0, vec, &r);
+  if (rc) return rc;
+  *eigval = r.theta[0] / a;
+  if (eigvec)
+    SP_CK(c, cudaMemcpyAsync(eigvec, vec, N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+  SP_CK(c, cudaStreamSynchronize(c->stream));
+  if (rep) {
+    rep->matvecs = op.matvecs;
+    rep->restarts = r.restarts;
+    rep->converged = r.converged ? 1 : 0;
+    rep->residual = r.resid[0] / std::fabs(a);
+  }
+  return CDFT_OK;
+}
+
+// Arnoldi::determine_largest_eigenpairs (src/Arnoldi.cpp:72-283): the k eigenpairs of
+// H + shift of largest magnitude, from a k + p dimensional Krylov basis restarted at most
+// max_steps times; eigenvalues reported without the shift, in that order.
+int cdft_arnoldi_largest(cdft_ctx* c, double shift, int k, int p, int all_k, long max_steps, double tol, const double* guess,
+                         double* eigvals, double* eigvecs, int on_device, cdft_eigen_report* rep) {
+  if (!c || !eigvals) return CDFT_ERR_ARG;
+  const long N = c->info.N;
+  if (k < 1 || p < 1 || (long)k + p > N || max_steps < 1 || !(tol > 0))
+    return cdft_internal_fail(c, CDFT_ERR_ARG, "arnoldi: needs k >= 1, p >= 1, k + p <= N, max_steps >= 1 and tol > 0");
+  DevBuf buf;
+  double *x0 = buf.get(N), *vecs = buf.get((size_t)k * N);
+  if (!x0 || !vecs) return cdft_internal_fail(c, CDFT_ERR_CUDA, "arnoldi: out of device memory");
+  int rc = start_vector(c, guess, on_device, 20240601, x0);
+  if (rc) return rc;
+  SymOp op{c, 1.0, shift, nullptr, nullptr, nullptr, false, 0};
+  LanczosResult r;
+  rc = lanczos(c, op, Want::LargestMagnitude, k, k + p, tol, all_k != 0, true, 1L << 62, (int)std::min<long>(max_steps, 1 << 30), x0,
+               vecs, &r);
+  if (rc) return rc;
+  const int nw = (int)r.theta.size();
+  for (int i = 0; i < k; ++i) eigvals[i] = i < nw ? r.theta[i] - shift : NAN;
+  if (eigvecs)
+    SP_CK(c, cudaMemcpyAsync(eigvecs, vecs, (size_t)nw * N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             c->stream));
+  SP_CK(c, cudaStreamSynchronize(c->stream));
+  if (rep) {
+    rep->matvecs = op.matvecs;
+    rep->restarts = r.restarts;
+    rep->converged = r.converged ? 1 : 0;
+    rep->residual = r.resid.empty() ? 0 : r.resid[0];
+  }
+  if (!r.converged) return cdft_internal_fail(c, CDFT_ERR_TIMEOUT, "IRArnoldi method: Exceeded max iterations");
+  return CDFT_OK;
+}

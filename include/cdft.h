@@ -109,6 +109,55 @@ int cdft_hessian_dot_v(cdft_ctx* ctx, const double* v, double* out, int on_devic
  * (src/DDFT.cpp:320-351), at the context's current density. */
 int cdft_ddft_matrix_dot_v(cdft_ctx* ctx, const double* v, double* out, int on_device);
 
+/* Spectral drivers on those matrices (the reference's consumers of Dynamical_Matrix,
+ * include/Dynamical_Matrix.h), at the context's current density. Every vector stays
+ * on the device; each product is one Hessian pass in the context's precision. */
+#define CDFT_MATRIX_HESSIAN 0 /* DFT: the Hessian of Omega (Dynamical_Matrix::is_dynamic() false) */
+#define CDFT_MATRIX_DDFT 1    /* DDFT: g . H (is_dynamic() true; Log_Det expands -g . H) */
+
+/* Log_Det(matrix, order, lam_max, lam_min).calculate_log_det(seed, num_samples,
+ * has_zero_eigenvalue, variance) (include/Log_Det.h:21-51, src/Log_Det.cpp:23-166): the
+ * stochastic Chebyshev estimate of log det of the matrix whose spectrum lies in
+ * [lam_min, lam_max], with the reference's +-1 probe vectors for the same seed
+ * (std::mt19937(seed), uniform_int_distribution<>(0, 1), point order; seed <= 0 draws
+ * one from std::random_device). variance (may be NULL) receives the reference's spread
+ * sqrt|<(v.u)^2> - <v.u>^2|. Periodic lattices: every point is active. */
+int cdft_log_det(cdft_ctx* ctx, int matrix, int order, double lam_max, double lam_min, long seed, int num_samples,
+                 int has_zero_eigenvalue, double* log_det, double* variance);
+
+typedef struct cdft_eigen_report {
+  long matvecs;    /* Hessian products used */
+  int restarts;    /* restarts of the Krylov basis */
+  int converged;   /* 1 when the stopping rule was met */
+  double residual; /* |H y - lambda y| of the (first) returned pair, in the matrix's own units */
+} cdft_eigen_report;
+
+/* Eigenvalues(dft).calculate_eigenvector (include/Eigenvalues.h:16-57,
+ * src/Eigenvalues.cpp:43-99) with set_scale(scale), set_tolerence(tol),
+ * set_change_sign(change_sign), set_vshift(vshift) (NULL: none): the smallest eigenvalue
+ * of s (H + vshift vshift^T / 2), s = scale (change_sign = 0) or -scale (1), returned as
+ * the reference's get_eigenvalue() does (divided by scale, sign restored; so change_sign
+ * gives the largest eigenvalue of H + vshift vshift^T / 2), with its unit eigenvector
+ * (eigvec, N values, may be NULL). Stops when |residual| <= tol |lambda| (the reference
+ * stops nlopt's L-BFGS at a relative change tol of the Rayleigh quotient), or after
+ * about max_matvecs products (checked at restarts; rep->converged = 0 then). guess (N
+ * values, may be NULL) is the start vector, as set_eigen_vec_. Hessian only. */
+int cdft_eigenvalue(cdft_ctx* ctx, double scale, double tol, int change_sign, const double* vshift, const double* guess,
+                    long max_matvecs, double* eigval, double* eigvec, int on_device, cdft_eigen_report* rep);
+
+/* Arnoldi(dft).determine_largest_eigenpairs(shift, k, p, compute_all_k_largest,
+ * maxSteps, tol) (include/Arnoldi.h:19-84, src/Arnoldi.cpp:72-283): the k eigenpairs of
+ * H + shift of largest magnitude, in that order, from a (k + p)-vector Krylov basis;
+ * eigvals (k values) are reported without the shift and eigvecs (k * N values, may be
+ * NULL) are unit vectors. A pair has converged when its Ritz estimate is at most
+ * tol |lambda| or it is degenerate (within tol) with the largest discarded Ritz value;
+ * all_k = 0 asks only for the first. Returns CDFT_ERR_TIMEOUT after max_steps restarts
+ * without convergence (the reference throws; the outputs then hold the last estimates).
+ * The reference stores the first Ritz value under every index (src/Arnoldi.cpp:207);
+ * here eigvals[i] is the i-th pair's own value. Hessian only. */
+int cdft_arnoldi_largest(cdft_ctx* ctx, double shift, int k, int p, int all_k, long max_steps, double tol, const double* guess,
+                         double* eigvals, double* eigvecs, int on_device, cdft_eigen_report* rep);
+
 /* Times each pass of one evaluation in the current precision with CUDA events
  * on the context's stream (no reference counterpart; used by the benchmark's
  * roofline). reps evaluations are timed; ms receives the mean time per pass

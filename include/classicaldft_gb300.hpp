@@ -376,6 +376,104 @@ class DDFT {
   bool started_ = false;
 };
 
+// include/Log_Det.h:21-51 (src/Log_Det.cpp): on the DFT's Hessian or the DDFT matrix.
+class Log_Det {
+ public:
+  Log_Det(DFT& dft, int order, double lam_max, double lam_min, bool verbose = false)
+      : dft_(&dft), matrix_(CDFT_MATRIX_HESSIAN), order_(order), lam_max_(lam_max), lam_min_(lam_min) { (void)verbose; }
+  Log_Det(DFT& dft, const DDFT&, int order, double lam_max, double lam_min, bool verbose = false)
+      : dft_(&dft), matrix_(CDFT_MATRIX_DDFT), order_(order), lam_max_(lam_max), lam_min_(lam_min) { (void)verbose; }
+  double calculate_log_det(long seed, int num_samples, bool has_zero_eigenvalue, double& variance) {
+    dft_->push();
+    double v = 0;
+    check(cdft_log_det(dft_->context(), matrix_, order_, lam_max_, lam_min_, seed, num_samples, has_zero_eigenvalue ? 1 : 0, &v, &variance),
+          dft_->context());
+    return v;
+  }
+
+ private:
+  DFT* dft_;
+  int matrix_, order_;
+  double lam_max_, lam_min_;
+};
+
+// include/Eigenvalues.h:16-57 (src/Eigenvalues.cpp) on the DFT's Hessian.
+class Eigenvalues {
+ public:
+  explicit Eigenvalues(DFT& dft, bool verbose = false) : dft_(&dft) { (void)verbose; }
+  void set_scale(double d) { scale_ = d; }
+  void set_tolerence(double d) { tol_ = d; }
+  void set_change_sign(bool b) { change_sign_ = b; }
+  void set_vshift(const std::vector<double>& v) { vshift_ = v; }
+  void set_eigen_vec_(const std::vector<double>& v) { eigen_vec_ = v; }
+  double get_scale() const { return scale_; }
+  double get_tolerence() const { return tol_; }
+  bool get_change_sign() const { return change_sign_; }
+  double get_eigenvalue() const { return eigen_val_; }
+  int get_num_eval() const { return (int)rep_.matvecs; }
+  int get_return_code() const { return rep_.converged; }
+  const std::vector<double>& get_eigen_vec() const { return eigen_vec_; }
+  void calculate_eigenvector(long max_matvecs = 1000000) {
+    dft_->push();
+    cdft_ctx* c = dft_->context();
+    std::vector<double> out(dft_->getSpecies(0)->getDensity().Ntot());
+    const double* guess = eigen_vec_.size() == out.size() ? eigen_vec_.data() : nullptr;
+    check(cdft_eigenvalue(c, scale_, tol_, change_sign_ ? 1 : 0, vshift_.size() == out.size() ? vshift_.data() : nullptr, guess, max_matvecs,
+                          &eigen_val_, out.data(), 0, &rep_),
+          c);
+    eigen_vec_.swap(out);
+  }
+  void clear() { eigen_vec_.clear(); }
+
+ private:
+  DFT* dft_;
+  double scale_ = 1e6, tol_ = 1e-6, eigen_val_ = 0;
+  bool change_sign_ = false;
+  std::vector<double> vshift_, eigen_vec_;
+  cdft_eigen_report rep_{};
+};
+
+// include/Arnoldi.h:19-84 (src/Arnoldi.cpp) on the DFT's Hessian.
+class Arnoldi {
+ public:
+  explicit Arnoldi(DFT& dft, bool verbose = false) : dft_(&dft) { (void)verbose; }
+  void set_initial_guess(const std::vector<double>& v) { guess_ = v; }
+  void determine_largest_eigenpairs(double shift, int k, int p, bool compute_all_k_largest = true, long maxSteps = 1000000,
+                                    double tol = 1e-8) {
+    dft_->push();
+    cdft_ctx* c = dft_->context();
+    const long N = dft_->getSpecies(0)->getDensity().Ntot();
+    vals_.assign(k, 0.0);
+    vecs_.assign((size_t)k * N, 0.0);
+    executed_ = true;
+    const int rc = cdft_arnoldi_largest(c, shift, k, p, compute_all_k_largest ? 1 : 0, maxSteps, tol,
+                                        guess_.size() == (size_t)N ? guess_.data() : nullptr, vals_.data(), vecs_.data(), 0, &rep_);
+    success_ = rc == CDFT_OK;
+    check(rc, c);
+  }
+  bool is_success() const {
+    if (!executed_) throw std::runtime_error("Arnoldi: Solver has yet not been executed");
+    return success_;
+  }
+  double get_eigenvalue(int i) const {
+    if (!executed_) throw std::runtime_error("Arnoldi: Solver has yet not been executed");
+    if (i < 0 || i >= (int)vals_.size()) throw std::runtime_error("Arnoldi: Requesting eigenvalue that has not been computed (index larger than k)");
+    return vals_[i];
+  }
+  std::vector<double> get_eigenvector(int i) const {
+    if (!executed_) throw std::runtime_error("Arnoldi: Solver has yet not been executed");
+    if (i < 0 || i >= (int)vals_.size()) throw std::runtime_error("Arnoldi: Requesting eigenvector that has not been computed (index larger than k)");
+    const size_t N = vecs_.size() / vals_.size();
+    return std::vector<double>(vecs_.begin() + (long)(i * N), vecs_.begin() + (long)((i + 1) * N));
+  }
+
+ private:
+  DFT* dft_;
+  std::vector<double> guess_, vals_, vecs_;
+  cdft_eigen_report rep_{};
+  bool executed_ = false, success_ = false;
+};
+
 }  // namespace classicaldft_gb300
 
 #endif

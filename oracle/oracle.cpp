@@ -6,6 +6,7 @@
 #include <complex>
 #include <cstdint>
 #include <cstring>
+#include <random>
 #include <stdexcept>
 #include <vector>
 #ifdef _OPENMP
@@ -1192,6 +1193,74 @@ int orc_ddft(orc_ctx* c, double* rho, int nsteps, double dt_init, double dt_max,
     if (rec_rhs) rec_rhs[s] = rhs_max;
   }
   return nsteps;
+}
+
+// Log_Det::calculate_log_det (src/Log_Det.cpp:84-166) with the coefficients of
+// Log_Det::get_coefficients (:32-57): a Chebyshev expansion of log on the spectrum
+// [lam_min, lam_max] scaled by 1/(lam_min + lam_max), traced by Hutchinson with +-1
+// vectors from std::mt19937(seed) and uniform_int_distribution<>(0, 1), drawn in
+// point order, sample after sample. dynamic = 1 uses -(g . H), the DDFT matrix the
+// reference negates (is_dynamic). has_zero adds lam_mid * sum(v) / N to every entry.
+double orc_log_det(const orc_ctx* c, const double* rho, int dynamic, int order, double lam_max, double lam_min, long seed, int num_samples,
+                   int has_zero, double* variance) {
+  const long N = c->N;
+  const double scale = 1.0 / (lam_min + lam_max), a = lam_min * scale, b = lam_max * scale, lam_mid = 0.5 * (lam_max + lam_min);
+  std::vector<double> cf(order + 1, 0.0);
+  for (int k = 0; k <= order; ++k) {
+    const double xk = std::cos(M_PI * (k + 0.5) / (order + 1));
+    double Tm2 = 0, Tm1 = 0, T = 1;
+    for (int j = 0; j <= order; ++j) {
+      T = j == 0 ? 1.0 : j == 1 ? xk : 2 * xk * Tm1 - Tm2;
+      cf[j] += std::log(0.5 * (b - a) * xk + 0.5 * (b + a)) * T;
+      Tm2 = Tm1;
+      Tm1 = T;
+    }
+  }
+  for (int j = 0; j <= order; ++j) cf[j] *= (j == 0 ? 1.0 : 2.0) / (order + 1);
+  std::vector<double> v(N), w0(N), w1(N), w2(N), u(N), r(N);
+  auto op = [&](const std::vector<double>& x, std::vector<double>& y) {
+    if (dynamic) {
+      orc_ddft_matrix_dot_v(c, rho, x.data(), y.data());
+      for (double& t : y) t = -t;
+    } else {
+      hessian_dot_v(*c, rho, x.data(), y.data());
+    }
+    if (has_zero) {
+      double s = 0;
+      for (double t : x) s += t;
+      for (double& t : y) t += lam_mid * s / N;
+    }
+  };
+  std::mt19937 rng((unsigned long)seed);
+  std::uniform_int_distribution<> distrib(0, 1);
+  double log_det = 0, var_log_det = 0;
+  for (int i = 1; i <= num_samples; ++i) {
+    for (long p = 0; p < N; ++p) v[p] = distrib(rng) > 0 ? 1 : -1;
+    op(v, r);
+    for (long p = 0; p < N; ++p) {
+      w0[p] = v[p];
+      w1[p] = r[p] * scale * (2.0 / (b - a)) - (b + a) / (b - a) * v[p];
+      u[p] = cf[0] * w0[p] + cf[1] * w1[p];
+    }
+    for (int k = 2; k <= order; ++k) {
+      op(w1, r);
+      for (long p = 0; p < N; ++p) {
+        w2[p] = r[p] * scale * (4.0 / (b - a)) - 2 * (b + a) / (b - a) * w1[p] - w0[p];
+        u[p] += cf[k] * w2[p];
+      }
+      w0.swap(w1);
+      w1.swap(w2);
+    }
+    double vu = 0;
+    for (long p = 0; p < N; ++p) vu += v[p] * u[p];
+    log_det += vu;
+    var_log_det += vu * vu;
+    const double av = log_det / i, av2 = var_log_det / i;
+    if (variance) *variance = std::sqrt(std::fabs(av2 - av * av));
+  }
+  log_det /= num_samples;
+  if (has_zero) log_det -= std::log(lam_mid);
+  return log_det - N * std::log(scale);
 }
 
 }  // extern "C"

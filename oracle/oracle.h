@@ -69,6 +69,12 @@ void orc_hessian_dot_v(const orc_ctx* c, const double* rho, const double* v, dou
 /* DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): g_dot_x of the full Hessian times v. */
 void orc_ddft_matrix_dot_v(const orc_ctx* c, const double* rho, const double* v, double* out);
 
+/* Log_Det::calculate_log_det (src/Log_Det.cpp:84-166) of the Hessian (dynamic = 0) or
+   of -(DDFT matrix) (dynamic = 1) at the density rho; variance (may be NULL) as the
+   reference reports it. */
+double orc_log_det(const orc_ctx* c, const double* rho, int dynamic, int order, double lam_max, double lam_min, long seed, int num_samples,
+                   int has_zero, double* variance);
+
 /* FFT helpers exposed for tests: unnormalised r2c / c2r of an nx*ny*nz grid
    (complex stored interleaved, nx*ny*(nz/2+1) values). */
 void orc_r2c(int nx, int ny, int nz, const double* in, double* out_c);

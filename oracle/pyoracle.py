@@ -60,6 +60,8 @@ def lib():
         L.orc_fill_noise.argtypes = [dp, ctypes.c_long, d, d, ctypes.c_uint64]
         L.orc_hessian_dot_v.argtypes = [ctypes.c_void_p, dp, dp, dp]
         L.orc_ddft_matrix_dot_v.argtypes = [ctypes.c_void_p, dp, dp, dp]
+        L.orc_log_det.restype = d
+        L.orc_log_det.argtypes = [ctypes.c_void_p, dp, ctypes.c_int, ctypes.c_int, d, d, ctypes.c_long, ctypes.c_int, ctypes.c_int, dp]
         _lib = L
     return _lib
 
@@ -169,6 +171,14 @@ class Oracle:
         out = np.zeros(self.shape)
         lib().orc_ddft_matrix_dot_v(self._c, _p(r), _p(vv), _p(out))
         return out
+
+    def log_det(self, rho, order, lam_max, lam_min, seed, num_samples, has_zero=False, dynamic=False):
+        """Log_Det::calculate_log_det of the Hessian (or of the negated DDFT matrix with
+        dynamic=True) at density rho; returns (log_det, variance)."""
+        r = np.ascontiguousarray(rho, dtype=np.float64).reshape(self.shape)
+        var = np.zeros(1)
+        val = lib().orc_log_det(self._c, _p(r), int(dynamic), order, lam_max, lam_min, seed, num_samples, int(has_zero), _p(var))
+        return val, var[0]
 
     def mu_times_beta(self, rho):
         return lib().orc_mu_times_beta(self._c, rho)

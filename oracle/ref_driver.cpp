@@ -24,6 +24,7 @@ using namespace std;
 #include "DFT.h"
 #include "FMT.h"
 #include "Interaction.h"
+#include "Log_Det.h"
 #include "Minimizer.h"
 #include "Potential1.h"
 
@@ -281,6 +282,41 @@ static System make_system(double dx, int n, const std::string& model, bool lj, d
   return S;
 }
 
+// The dense matrix of a Dynamical_Matrix (include/Dynamical_Matrix.h): column j =
+// matrix_dot_v1 of the j-th unit vector (src/Dynamical_Matrix.cpp), stored column-major.
+static std::vector<double> dense_matrix(const Dynamical_Matrix& m, long N) {
+  std::vector<double> H((size_t)N * N);
+  DFT_Vec e(N), r(N);
+  for (long j = 0; j < N; ++j) {
+    e.zeros(N);
+    e.set(j, 1.0);
+    m.matrix_dot_v1(e, r, nullptr);
+    for (long i = 0; i < N; ++i) H[(size_t)j * N + i] = r.get(i);
+  }
+  return H;
+}
+// Largest eigenvalue of a + b H (H dense, symmetric, column-major) by power iteration
+// from a seeded start; used only to bracket spectra for Log_Det.
+static double power_extreme(const std::vector<double>& H, long N, double a, double b, int iters) {
+  std::vector<double> x(N), y(N);
+  SplitMix64 g(99);
+  for (long i = 0; i < N; ++i) x[i] = 2.0 * g.uniform() - 1.0;
+  double lam = 0;
+  for (int it = 0; it < iters; ++it) {
+    double nx = 0;
+    for (long i = 0; i < N; ++i) nx += x[i] * x[i];
+    nx = std::sqrt(nx);
+    for (long i = 0; i < N; ++i) x[i] /= nx;
+    for (long i = 0; i < N; ++i) y[i] = a * x[i];
+    for (long j = 0; j < N; ++j)
+      for (long i = 0; i < N; ++i) y[i] += b * H[(size_t)j * N + i] * x[j];
+    lam = 0;
+    for (long i = 0; i < N; ++i) lam += x[i] * y[i];
+    x.swap(y);
+  }
+  return lam;
+}
+
 static void record_eval(const std::string& tag, System& S, bool full_fields, const std::vector<double>& pos) {
   double F = S.dft->calculateFreeEnergyAndDerivatives(false);
   put1(tag + ".Omega", F);
@@ -493,6 +529,62 @@ int main(int argc, char** argv) {
       }
     } else if (c == "files") {
       case_files(argv[2]);
+    } else if (c == "spectral") {
+      // Pins of the spectral drivers (Eigenvalues, Arnoldi, Log_Det consume matrix_dot_v1):
+      // the dense Hessian of a hard-sphere state and of an LJ state (tests/golden/make_golden.py
+      // takes their eigenvalues with LAPACK and keeps those), and Log_Det::calculate_log_det
+      // (src/Log_Det.cpp:84-166) of the hard-sphere DFT matrix and of its DDFT matrix.
+      System S = make_system(0.2, 16, "WhiteBearI", false, 1.0);
+      fill_noise(*S.d, 0.6, 0.2, 11);
+      S.s->setChemPotential(S.dft->mu_times_beta(0.6));
+      S.dft->calculateFreeEnergyAndDerivatives(false);
+      const long N = S.d->Ntot();
+      std::vector<double> H = dense_matrix(*S.dft, N);
+      put("sp16.H", H);
+      const double lmax = power_extreme(H, N, 0.0, 1.0, 400);
+      const double lmin = lmax - power_extreme(H, N, lmax, -1.0, 4000);
+      const double lam_max = 1.02 * lmax, lam_min = 0.9 * lmin;
+      put("sp16.logdet.bounds", {lam_min, lam_max});
+      for (int order : {10, 40}) {
+        Log_Det ld(*S.dft, order, lam_max, lam_min, false);
+        double var = 0;
+        const double val = ld.calculate_log_det(1234, 3, false, var);
+        put(std::string("sp16.logdet.o") + std::to_string(order), {val, var});
+      }
+      {
+        Log_Det ld(*S.dft, 20, lam_max, lam_min, false);
+        double var = 0;
+        const double val = ld.calculate_log_det(77, 2, true, var);
+        put("sp16.logdet.zero", {val, var});
+      }
+      DDFT ddft(S.dft, false);
+      // the dominant eigenvalue of -g.H (the matrix Log_Det uses for a dynamic matrix) by
+      // power iteration through the reference's own product
+      double gmax = 0;
+      {
+        DFT_Vec x(N), y(N);
+        SplitMix64 g(5);
+        for (long i = 0; i < N; ++i) x.set(i, 2.0 * g.uniform() - 1.0);
+        for (int it = 0; it < 300; ++it) {
+          x.MultBy(1.0 / x.euclidean_norm());
+          ddft.matrix_dot_v1(x, y, nullptr);
+          y.MultBy(-1.0);
+          gmax = x.dotWith(y);
+          x.set(y);
+        }
+      }
+      const double g_max = 1.05 * gmax, g_min = 1e-3 * gmax;
+      put("sp16.logdet.ddft.bounds", {g_min, g_max});
+      Log_Det lg(ddft, 16, g_max, g_min, false);
+      double var = 0;
+      const double val = lg.calculate_log_det(4321, 2, true, var);
+      put("sp16.logdet.ddft", {val, var});
+      System T = make_system(0.1, 16, "WhiteBearI", true, 0.8);
+      fill_noise(*T.d, 0.3, 0.1, 5);
+      T.s->setChemPotential(T.dft->mu_times_beta(0.3));
+      T.dft->calculateFreeEnergyAndDerivatives(false);
+      put("splj16.H", dense_matrix(*T.dft, N));
+      put1("splj16.hsd", T.hsd);
     } else {
       std::fprintf(stderr, "unknown case %s\n", c.c_str());
       return 2;

@@ -1,7 +1,8 @@
 // A reference-style application (the call sequence of a classicalDFT app) built
 // against include/classicaldft_gb300.hpp: config 1 (hard spheres, WhiteBearI,
 // 32^3 at dx = 0.2, rho = 0.7 (1 + noise)), one evaluation, then FIRE2 steps.
-// Prints "Omega F_hs mu steps F_final sum(Hv) sum|Hv| max|snapshot - density| Omega_AO" for the test to compare.
+// Prints "Omega F_hs mu steps F_final sum(Hv) sum|Hv| max|snapshot - density| Omega_AO log_det
+// lambda_max" for the test to compare.
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -39,6 +40,16 @@ int main(int argc, char** argv) {
   dft.matrix_dot_v1(v, Hv);
   double hsum = 0, habs = 0;
   for (double x : Hv) { hsum += x; habs += x < 0 ? -x : x; }
+  // the spectral drivers at this density: Log_Det (order 6, one probe, seed 1234, spectrum
+  // bracket [0.005, 0.2]) and Eigenvalues with change_sign (the largest eigenvalue)
+  Log_Det ld(dft, 6, 0.2, 0.005);
+  double ld_var = 0;
+  const double logdet = ld.calculate_log_det(1234, 1, false, ld_var);
+  Eigenvalues eig(dft);
+  eig.set_change_sign(true);
+  eig.set_tolerence(1e-10);
+  eig.calculate_eigenvector();
+  const double lam_max = eig.get_eigenvalue();
   fireMinimizer2 fire(&dft);
   fire.setForceTerminationCriterion(0.0);
   fire.run(fire_steps);
@@ -63,7 +74,7 @@ int main(int argc, char** argv) {
     sa.setChemPotential(dftA.mu_times_beta(0.4));
     FA = dftA.calculateFreeEnergyAndDerivatives(false);
   }
-  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g %.17g %.17g\n", F, Fhs, species.getChemPotential(), fire.report().total_steps,
-              fire.getF(), hsum, habs, snap_diff, FA);
+  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", F, Fhs, species.getChemPotential(),
+              fire.report().total_steps, fire.getF(), hsum, habs, snap_diff, FA, logdet, lam_max);
   return 0;
 }

@@ -21,7 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 CASES = ["weights", "phi", "bulk", "eval_models16", "eval_hs32", "eval_lj", "fire_hs32", "fire_lj24",
-         "ddft_lj16", "ddft_adapt16", "coex", "hessian", "files", "ao"]
+         "ddft_lj16", "ddft_adapt16", "coex", "hessian", "files", "ao", "spectral"]
 # cases that also leave files next to their output: copied here as <case>.<suffix>
 FILE_OUTPUTS = {"files": [".a.vtk", ".b.vtk"]}
 
@@ -43,6 +43,36 @@ def read_driver_output(path):
     return out
 
 
+def spectral_post(arrays):
+    """The dense Hessians the driver wrote (column j = matrix_dot_v1 of the j-th unit
+    vector) are replaced by what the spectral-driver tests compare with: every
+    eigenvalue (LAPACK, of the symmetrised matrix), the asymmetry, the eigenvectors of
+    the isolated extreme eigenvalues, and the extreme eigenvalues of H + vshift vshift^T / 2
+    (Eigenvalues::calculate_gradients, src/Eigenvalues.cpp) for a seeded vshift."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    for tag in ("sp16", "splj16"):
+        H = arrays.pop(tag + ".H")
+        n = int(round(np.sqrt(H.size)))
+        H = H.reshape(n, n).T
+        arrays[tag + ".asym"] = np.array([np.abs(H - H.T).max()])
+        Hs = 0.5 * (H + H.T)
+        w, V = np.linalg.eigh(Hs)
+        arrays[tag + ".eig"] = w
+        for name, i in (("evec_min", 0), ("evec_max", n - 1)):
+            v = V[:, i] * np.sign(V[np.argmax(np.abs(V[:, i])), i])
+            arrays[tag + "." + name] = v
+        s = pyoracle.fill_noise((16, 16, 16), 1.0, 1.0, 31).ravel() - 1.0
+        s *= np.sqrt(2 * 0.01) / np.linalg.norm(s)
+        arrays[tag + ".vshift"] = s
+        ws = np.linalg.eigvalsh(Hs + 0.5 * np.outer(s, s))
+        arrays[tag + ".eig_vshift"] = np.concatenate([ws[:8], ws[-8:]])
+    return arrays
+
+
+POST = {"spectral": spectral_post}
+
+
 def main():
     args = sys.argv[1:]
     cases = CASES
@@ -58,6 +88,8 @@ def main():
             out = os.path.join(tmp, case + ".bin")
             subprocess.check_call([drv, case, out], cwd=tmp)
             arrays = read_driver_output(out)
+            if case in POST:
+                arrays = POST[case](arrays)
             np.savez_compressed(os.path.join(HERE, case + ".npz"), **arrays)
             for suffix in FILE_OUTPUTS.get(case, []):
                 shutil.copyfile(out + suffix, os.path.join(HERE, case + suffix))

@@ -58,3 +58,13 @@ def test_reference_style_app_runs_config1(tmp_path):
     assert (tmp_path / "snapshot.vtk").read_bytes().startswith(b"# vtk DataFile Version 2.0\nWritten using VisIt writer\nASCII\n")
     # FMT_AO_Species through the mirror, on a density handed over as a reference snapshot file
     assert abs(float(out[8]) - ao["ao16.WhiteBearI.Omega"][0]) <= 1e-12 * abs(ao["ao16.WhiteBearI.Omega"][0])
+    # Log_Det and Eigenvalues through the mirror, at the starting density: the log det
+    # against the oracle's restatement (same probes), the largest eigenvalue against the
+    # Python binding's
+    ref_ld, _ = o.log_det(rho, 6, 0.2, 0.005, 1234, 1)
+    assert abs(float(out[9]) - ref_ld) <= 1e-10 * abs(ref_ld)
+    c = cd.Context(32, 0.2, cd.WHITEBEAR_I, hsd=1.0)
+    c.set_density(rho)
+    lam, _, _ = c.eigenvalue(tol=1e-10, change_sign=True)
+    c.close()
+    assert abs(float(out[10]) - lam) <= 1e-9 * lam

@@ -222,3 +222,35 @@ def test_ddft_dynamical_matrix_dot_v(oracle):
     out = o.ddft_matrix_dot_v(rho, _hess_v(oracle, shape))
     ref = g["hlj16.GHv"].reshape(shape)
     assert np.max(np.abs(out - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("tag,order,seed,samples,has_zero,dynamic",
+                         [("o10", 10, 1234, 3, False, False), ("o40", 40, 1234, 3, False, False),
+                          ("zero", 20, 77, 2, True, False), ("ddft", 16, 4321, 2, True, True)])
+def test_log_det_vs_reference(oracle, tag, order, seed, samples, has_zero, dynamic):
+    """Log_Det::calculate_log_det (src/Log_Det.cpp:84-166), compiled from the reference,
+    against the oracle's restatement: same seed, same +-1 probes, same recurrence."""
+    g = golden("spectral")
+    o = oracle.Oracle(16, 0.2, "WhiteBearI", hsd=1.0)
+    rho = oracle.fill_noise((16, 16, 16), 0.6, 0.2, 11)
+    lo, hi = g["sp16.logdet.ddft.bounds" if dynamic else "sp16.logdet.bounds"]
+    val, var = o.log_det(rho, order, hi, lo, seed, samples, has_zero=has_zero, dynamic=dynamic)
+    ref = g["sp16.logdet." + tag]
+    assert abs(val - ref[0]) <= 1e-12 * abs(ref[0])
+    assert abs(var - ref[1]) <= 1e-9 * abs(ref[1])
+
+
+@pytest.mark.parametrize("tag,dx,rho0,amp,seed,lj", [("sp16", 0.2, 0.6, 0.2, 11, False), ("splj16", 0.1, 0.3, 0.1, 5, True)])
+def test_spectrum_pins_oracle_hessian(oracle, tag, dx, rho0, amp, seed, lj):
+    """The reference's dense Hessians (their LAPACK eigenpairs in the golden file) and the
+    oracle's Hessian product: H y = lambda y for the isolated extreme pairs."""
+    g = golden("spectral")
+    kw = dict(hsd=float(g["splj16.hsd"][0]), lj=True, kT=0.8) if lj else dict(hsd=1.0)
+    o = oracle.Oracle(16, dx, "WhiteBearI", **kw)
+    rho = oracle.fill_noise((16, 16, 16), rho0, amp, seed)
+    eig = g[tag + ".eig"]
+    assert g[tag + ".asym"][0] <= 1e-15 * np.abs(eig).max()
+    for name, lam in (("evec_min", eig[0]), ("evec_max", eig[-1])):
+        y = g[tag + "." + name]
+        hy = o.hessian_dot_v(rho, y.reshape(16, 16, 16)).ravel()
+        assert np.linalg.norm(hy - lam * y) <= 1e-12 * np.abs(eig).max()
