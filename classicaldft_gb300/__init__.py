@@ -36,7 +36,7 @@ C_FUNCTIONS = [
     "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates", "cdft_hessian_dot_v",
     "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex", "cdft_ddft_matrix_dot_v",
     "cdft_density_write", "cdft_density_read", "cdft_density_write_vtk", "cdft_log_det", "cdft_eigenvalue",
-    "cdft_arnoldi_largest",
+    "cdft_arnoldi_largest", "cdft_set_boundary",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -145,6 +145,7 @@ def lib():
             "cdft_density_write": ([ctypes.c_char_p, dp, ctypes.c_long], i),
             "cdft_density_read": ([ctypes.c_char_p, dp, ctypes.c_long], i),
             "cdft_density_write_vtk": ([ctypes.c_char_p, dp, i, i, i], i),
+            "cdft_set_boundary": ([vp, i, i], i),
             "cdft_log_det": ([vp, i, i, d, d, ctypes.c_long, i, i, dp, dp], i),
             "cdft_eigenvalue": ([vp, d, d, i, vp, vp, ctypes.c_long, dp, vp, i, P(EigenReport)], i),
             "cdft_arnoldi_largest": ([vp, d, i, i, i, ctypes.c_long, d, vp, dp, vp, i, P(EigenReport)], i),
@@ -284,6 +285,11 @@ class Context:
 
     def set_fixed_mass(self, m):
         self._check(lib().cdft_set_fixed_mass(self._h, m))
+
+    def set_boundary(self, fixed_background=False, homogeneous=False):
+        """Species::setFixedBackground / setHomogeneousBoundary: dF on the planes i, j, k = 0
+        set to zero, or to its mean over those planes, after each evaluation."""
+        self._check(lib().cdft_set_boundary(self._h, int(fixed_background), int(homogeneous)))
 
     def chem_potential(self):
         v = ctypes.c_double()

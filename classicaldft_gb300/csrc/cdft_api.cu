@@ -102,6 +102,17 @@ struct FSumRho {
   const double* r;
   __device__ void operator()(long i, double* s, double*) const { s[0] = r[i]; }
 };
+// Species::endForceCalculation's boundary sum (src/Species.cpp:88-91) and the fixed-mass
+// sum dF . rho taken after it (:100-102)
+struct FBoundarySum {
+  const double* a;
+  int ny, nz;
+  __device__ void operator()(long i, double* s, double*) const { s[0] = cdft_on_boundary(i, ny, nz) ? a[i] : 0.0; }
+};
+struct FSumDot {
+  const double *a, *b;
+  __device__ void operator()(long i, double* s, double*) const { s[0] = a[i] * b[i]; }
+};
 struct FAbsMax {
   const double* a;
   __device__ void operator()(long i, double*, double* m) const { m[0] = fabs(a[i]); }
@@ -449,12 +460,22 @@ static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
   return CDFT_OK;
 }
 
+__global__ void k_boundary_set(double* __restrict__ a, long N, int ny, int nz, double value) {
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < N; p += (long)gridDim.x * blockDim.x)
+    if (cdft_on_boundary(p, ny, nz)) a[p] = value;
+}
+void cdft_internal_boundary_set(cdft_ctx* c, double* a, double value) {
+  k_boundary_set<<<grid_for(c->info.N), 256, 0, c->stream>>>(a, c->info.N, c->p.ny, c->p.nz, value);
+}
+
 static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
   const long N = c->info.N;
   const double dV = c->info.dV;
   int rc = ensure_evaluator(c, c->precision);
   if (rc) return rc;
-  if (c->fixed_mass <= 0) return eval_graph(c, terms8, only_fex);
+  if (c->fixed_mass <= 0 && !c->fixed_bg && !c->homo_bd) return eval_graph(c, terms8, only_fex);
+  if (c->fixed_bg && c->fixed_mass > 0)  // src/Species.cpp:75-76
+    return fail(c, CDFT_ERR_ARG, "Cannot have both fixed background and fixed mass .... aborting");
   if (c->fixed_mass > 0) {  // src/Species.cpp:64-71
     double s;
     rc = map_reduce<1, 0>(c, N, FSumRho{c->rho}, &s);
@@ -467,6 +488,17 @@ static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
   else rc = c->e32->eval(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, &t, c->stream);
   if (rc == 3) return fail(c, CDFT_ERR_TIMEOUT, "a tensor copy did not complete within its wait limit");
   if (rc) return fail(c, CDFT_ERR_CUDA, std::string("evaluation launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+  if (c->fixed_bg) cdft_internal_boundary_set(c, c->dF, 0.0);  // src/Species.cpp:78-82
+  if (c->homo_bd) {                                            // src/Species.cpp:84-95
+    double sb;
+    rc = map_reduce<1, 0>(c, N, FBoundarySum{c->dF, c->p.ny, c->p.nz}, &sb);
+    if (rc) return rc;
+    cdft_internal_boundary_set(c, c->dF, sb / (double)cdft_n_boundary(c->p.nx, c->p.ny, c->p.nz));
+    if (c->fixed_mass > 0) {  // the fixed-mass sum sees the averaged boundary
+      rc = map_reduce<1, 0>(c, N, FSumDot{c->dF, c->rho}, &t.sum_dF_rho);
+      if (rc) return rc;
+    }
+  }
   if (c->fixed_mass > 0) {  // src/Species.cpp:97-109
     c->mu = t.sum_dF_rho / c->fixed_mass;
     k_add_const<<<grid_for(N), 256, 0, c->stream>>>(c->dF, N, c->mu * dV);
@@ -647,6 +679,12 @@ int cdft_get_chem_potential(const cdft_ctx* c, double* mu) {
   *mu = c->mu;
   return CDFT_OK;
 }
+int cdft_set_boundary(cdft_ctx* c, int fixed_background, int homogeneous) {
+  if (!c) return CDFT_ERR_ARG;
+  c->fixed_bg = fixed_background ? 1 : 0;
+  c->homo_bd = homogeneous ? 1 : 0;
+  return CDFT_OK;
+}
 
 // DFT::matrix_dot_v1 with the full Hessian (src/Dynamical_Matrix.cpp,
 // src/DFT.cpp:435-488; FMT::add_second_derivative src/FMT.cpp:437-567;
@@ -694,6 +732,19 @@ static int hessian_buffers(cdft_ctx* c) {
   return CDFT_OK;
 }
 
+// The product's input on the device: the caller's array, or hv_v holding a copy (from the
+// host, or with its boundary entries zeroed under a fixed background, as
+// Dynamical_Matrix::matrix_dot_v1 zeroes them, src/Dynamical_Matrix.cpp).
+static int product_input(cdft_ctx* c, const double* v, int on_device, const double** vd) {
+  *vd = v;
+  if (on_device && !c->fixed_bg) return CDFT_OK;
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->hv_v, v, c->info.N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  c->stream));
+  if (c->fixed_bg) cdft_internal_boundary_set(c, c->hv_v, 0.0);
+  *vd = c->hv_v;
+  return CDFT_OK;
+}
+
 int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
   if (!c || !v || !out) return CDFT_ERR_ARG;
   if (c->p.ao_rp > 0) return fail(c, CDFT_ERR_ARG, "Hessian products are not built for the AO model");
@@ -702,12 +753,11 @@ int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device)
   const size_t nb = c->info.N * sizeof(double);
   const double* vd = v;
   double* od = on_device ? out : c->hv_out;
-  if (!on_device) {
-    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->hv_v, v, nb, cudaMemcpyHostToDevice, c->stream));
-    vd = c->hv_v;
-  }
+  rc = product_input(c, v, on_device, &vd);
+  if (rc) return rc;
   rc = hessian_device(c, vd, od);
   if (rc) return rc;
+  if (c->fixed_bg) cdft_internal_boundary_set(c, od, 0.0);  // src/DFT.cpp:480-487
   if (!on_device) CUDA_OR_FAIL(c, cudaMemcpyAsync(out, od, nb, cudaMemcpyDeviceToHost, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   return CDFT_OK;
@@ -727,10 +777,18 @@ int cdft_internal_matvec(cdft_ctx* c, int matrix, const double* x, double* y, bo
     if (rc) return fail(c, CDFT_ERR_CUDA, "Hessian prepare failed");
   }
   double* hv = matrix == 0 ? y : c->hv_out;
+  if (c->fixed_bg) {  // zero boundary entries in, zero boundary entries out
+    rc = product_input(c, x, 1, &x);
+    if (rc) return rc;
+  }
   rc = c->precision == CDFT_FP64 ? c->e64->hess_apply<double>(x, c->rho, hv, c->info.dV, c->stream)
                                  : c->e32->hess_apply<double>(x, c->rho, hv, c->info.dV, c->stream);
   if (rc) return fail(c, CDFT_ERR_CUDA, "Hessian launch failed");
-  if (matrix != 0) k_g_dot_x<<<grid_for(c->info.N), 256, 0, c->stream>>>(c->rho, hv, y, c->p.nx, c->p.ny, c->p.nz, c->p.dx);
+  if (c->fixed_bg) cdft_internal_boundary_set(c, hv, 0.0);
+  if (matrix != 0) {
+    k_g_dot_x<<<grid_for(c->info.N), 256, 0, c->stream>>>(c->rho, hv, y, c->p.nx, c->p.ny, c->p.nz, c->p.dx);
+    if (c->fixed_bg) cdft_internal_boundary_set(c, y, 0.0);
+  }
   return cudaGetLastError() == cudaSuccess ? CDFT_OK : fail(c, CDFT_ERR_CUDA, "matrix product launch failed");
 }
 extern "C" {
@@ -742,16 +800,16 @@ int cdft_ddft_matrix_dot_v(cdft_ctx* c, const double* v, double* out, int on_dev
   int rc = hessian_buffers(c);
   if (rc) return rc;
   const size_t nb = c->info.N * sizeof(double);
-  // v (device) -> H v in hv_out -> g . (H v) in hv_v (v is no longer needed) or the caller's array
-  if (on_device) {
-    rc = hessian_device(c, v, c->hv_out);
-  } else {
-    CUDA_OR_FAIL(c, cudaMemcpyAsync(c->hv_v, v, nb, cudaMemcpyHostToDevice, c->stream));
-    rc = hessian_device(c, c->hv_v, c->hv_out);
-  }
+  // v -> H v in hv_out -> g . (H v) in hv_v (v is no longer needed) or the caller's array
+  const double* vd = v;
+  rc = product_input(c, v, on_device, &vd);
   if (rc) return rc;
+  rc = hessian_device(c, vd, c->hv_out);
+  if (rc) return rc;
+  if (c->fixed_bg) cdft_internal_boundary_set(c, c->hv_out, 0.0);
   double* gd = on_device ? out : c->hv_v;
   k_g_dot_x<<<grid_for(c->info.N), 256, 0, c->stream>>>(c->rho, c->hv_out, gd, c->p.nx, c->p.ny, c->p.nz, c->p.dx);
+  if (c->fixed_bg) cdft_internal_boundary_set(c, gd, 0.0);  // src/DDFT.cpp:333-338
   if (!on_device) CUDA_OR_FAIL(c, cudaMemcpyAsync(out, gd, nb, cudaMemcpyDeviceToHost, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
   return CDFT_OK;
@@ -1162,6 +1220,7 @@ static int ddft_r2c(cdft_ctx* c, const double* real, void* spec) {
 int cdft_ddft_init(cdft_ctx* c, double dt, double dt_max, double tol) {
   if (!c) return CDFT_ERR_ARG;
   if (c->p.model < 0 && !c->p.lj) return fail(c, CDFT_ERR_ARG, "DDFT needs an FMT model or an interaction");
+  if (c->fixed_bg || c->homo_bd) return fail(c, CDFT_ERR_ARG, "the DDFT step is not built for boundary modes");
   const long N = c->info.N;
   const long Nc = c->precision == CDFT_FP64 ? c->e64->spectrum_len() : c->e32->spectrum_len();  // padded rows
   const size_t cs = sizeof(double2);  // large enough for either precision
@@ -1321,6 +1380,7 @@ static int ddft_one_step(cdft_ctx* c, int* restarts, bool dF_current) {
 
 int cdft_ddft_step(cdft_ctx* c, int nsteps, cdft_ddft_report* rep) {
   if (!c) return CDFT_ERR_ARG;
+  if (c->fixed_bg || c->homo_bd) return fail(c, CDFT_ERR_ARG, "the DDFT step is not built for boundary modes");
   if (!c->ddft_ready) return fail(c, CDFT_ERR_STATE, "cdft_ddft_init has not been called");
   int restarts = 0;
   for (int k = 0; k < nsteps; ++k) {

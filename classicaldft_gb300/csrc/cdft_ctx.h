@@ -29,6 +29,7 @@ struct cdft_ctx {
   std::unique_ptr<cdft::Evaluator<float>> e32;
   int precision = CDFT_FP64;
   double mu = 0, fixed_mass = -1;
+  int fixed_bg = 0, homo_bd = 0;  // Species::setFixedBackground / setHomogeneousBoundary
   double* rho = nullptr;
   double* dF = nullptr;
   double* vext = nullptr;
@@ -97,6 +98,14 @@ void cdft_internal_newton_save(cdft_ctx* c);
 void cdft_internal_newton_restore(cdft_ctx* c);
 // FIRE2 state re-derived from the current density: x = alias(rho), v = 0, one evaluation
 int cdft_internal_fire_resync(cdft_ctx* c);
+// Lattice::is_boundary_point (include/Lattice.h:184-196): the planes i = 0, j = 0, k = 0
+__host__ __device__ inline bool cdft_on_boundary(long p, int ny, int nz) {
+  const long t = p / nz;
+  return p % nz == 0 || t % ny == 0 || t / ny == 0;
+}
+inline long cdft_n_boundary(int nx, int ny, int nz) { return (long)nx * ny + (long)nx * nz + (long)ny * nz - nx - ny - nz + 1; }
+// a[p] = value on the boundary points (device, asynchronous on the context's stream)
+void cdft_internal_boundary_set(cdft_ctx* c, double* a, double value);
 // y = M x on the device (M: 0 the Hessian, 1 the DDFT matrix g . H; cdft_api.cu)
 int cdft_internal_matvec(cdft_ctx* c, int matrix, const double* x, double* y, bool prepare);
 // plans cdft_autotune chose for the context's shape, model and precision (cdft_tune.cu)

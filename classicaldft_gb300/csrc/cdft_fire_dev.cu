@@ -261,6 +261,15 @@ __global__ void k_sub_mu(S* dF, long n, const FireState* st, FireConsts k) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) dF[i] = dF[i] - m;
 }
 
+// Species::endForceCalculation with a fixed background (src/Species.cpp:78-82): dF = 0 on
+// the boundary planes
+template <class S>
+__global__ void k_zero_boundary(S* dF, long n, int ny, int nz, const FireState* st) {
+  if (st->skip || st->failed) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    if (cdft_on_boundary(i, ny, nz)) dF[i] = (S)0;
+}
+
 // Minimizer::getDF_DX after the evaluation (src/Minimizer.cpp:90-115): alias
 // derivative into g of the pending state; sums v.g; maxima |dF|, |g|.
 template <class S>
@@ -409,6 +418,7 @@ static void record_step(cdft_ctx* c, FireDevEngine* E, Evaluator<T>* ev, S* x[2]
   ev->template launch<S>(rho, c->vext, dF, c->info.dV, mu_eval, 1, s, nullptr);
   k_eval_finish<<<1, 1, 0, s>>>(ev->dev_terms(), ev->dev_status(), E->st, k, mu_eval, ev->M() > 0 ? 1 : 0, ev->has_mf() ? 1 : 0);
   if (c->fixed_mass > 0) k_sub_mu<S><<<gn, kThreads, 0, s>>>(dF, N, E->st, k);
+  if (c->fixed_bg) k_zero_boundary<S><<<gn, kThreads, 0, s>>>(dF, N, c->p.ny, c->p.nz, E->st);
   k_fire_post<S><<<gn, kThreads, 0, s>>>(dF, x[0], x[1], v[0], v[1], g[0], g[1], E->st, N, k, E->part);
   k_fire_sum_finish<<<1, 256, 0, s>>>(E->part, (int)gn, 0, 1, E->st, 3);
   k_fire_max_finish<<<1, 256, 0, s>>>(E->part, (int)gn, 1, 2, E->st, 4);
@@ -620,6 +630,8 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
   if (!c->fire_ready) return cdft_internal_fail(c, CDFT_ERR_STATE, "cdft_fire_init has not been called");
   if (mixed < 0 || mixed > 3) return cdft_internal_fail(c, CDFT_ERR_ARG, "mixed must be 0, 1, 2 or 3");
   if (mixed >= 2 && c->p.ao_rp > 0) mixed = 1;  // no Hessian products for the AO model: the FIRE2 policy
+  if (c->homo_bd) return cdft_internal_fail(c, CDFT_ERR_ARG, "the homogeneous boundary is built for the host-stepped FIRE2 calls only");
+  if (mixed >= 2 && c->fixed_bg) mixed = 1;  // Newton-Krylov is not built for a fixed background
   int rc = ensure_engine(c);
   if (rc) return rc;
   long total = 0, taken = 0, steps32 = 0;
@@ -785,6 +797,7 @@ extern "C" int cdft_fire_run_batch(cdft_ctx* const* ctx, int n, double resid_tol
     for (int j = 0; j < i; ++j)
       if (ctx[j] == ctx[i]) return cdft_internal_fail(ctx[i], CDFT_ERR_ARG, "a context appears twice in the batch");
     if (!ctx[i]->fire_ready) return cdft_internal_fail(ctx[i], CDFT_ERR_STATE, "cdft_fire_init has not been called");
+    if (ctx[i]->fixed_bg || ctx[i]->homo_bd) return cdft_internal_fail(ctx[i], CDFT_ERR_ARG, "the batched driver is not built for boundary modes");
   }
   if (mixed == 3) return batch_newton(ctx, n, resid_tol, switch_tol, max_steps, reps, rcs);
   // allocation first (nothing may allocate while a stream is captured), and

@@ -376,6 +376,7 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
 extern "C" int cdft_newton_refine_ex(cdft_ctx* c, double tol, const cdft_newton_params* prm, cdft_newton_report* rep) {
   if (!c || !prm) return CDFT_ERR_ARG;
   if (c->p.ao_rp > 0) return cdft_internal_fail(c, CDFT_ERR_ARG, "Newton-Krylov needs Hessian products, which are not built for the AO model");
+  if (c->fixed_bg || c->homo_bd) return cdft_internal_fail(c, CDFT_ERR_ARG, "Newton-Krylov is not built for boundary modes");
   const int max_newton = prm->max_newton, max_cg = prm->max_cg;
   const double cg_rtol = prm->cg_rtol, eta_max = prm->eta_max, fp32_above = prm->fp32_above;
   if (!(tol > 0) || max_newton <= 0 || max_cg <= 0 || !(cg_rtol > 0) || !(eta_max >= 0) || !(fp32_above >= 0)) return CDFT_ERR_ARG;

@@ -284,8 +284,12 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
   if (seed <= 0) seed = (long)std::random_device{}();
   std::mt19937 rng((unsigned long)seed);
   std::uniform_int_distribution<> distrib(0, 1);
+  const int ny = c->p.ny, nz = c->p.nz;
   auto draw = [&](double* h) {
     for (long p = 0; p < N; ++p) h[p] = distrib(rng) > 0 ? 1.0 : -1.0;
+    if (c->fixed_bg)  // Log_Det::set_boundary_points_to_zero (src/Log_Det.cpp:58-64, :99)
+      for (long p = 0; p < N; ++p)
+        if (cdft_on_boundary(p, ny, nz)) h[p] = 0.0;
   };
   draw(hv[0]);
   const unsigned g = sp_grid(N);
@@ -336,7 +340,8 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
   }
   double ld = acc / num_samples;
   if (has_zero_eigenvalue) ld -= std::log(lam_mid);
-  ld -= (double)N * std::log(scale);
+  const long n_active = N - (c->fixed_bg ? cdft_n_boundary(c->p.nx, ny, nz) : 0);  // src/Log_Det.cpp:89
+  ld -= (double)n_active * std::log(scale);
   *log_det = ld;
   if (variance) *variance = var;
   return CDFT_OK;
@@ -489,6 +494,7 @@ int start_vector(cdft_ctx* c, const double* guess, int on_device, long seed, dou
     SP_CK(c, cudaMemcpyAsync(x0, guess, N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
   else
     k_seed_vector<<<sp_grid(N), 256, 0, c->stream>>>(x0, N, (unsigned long long)seed);
+  if (c->fixed_bg) cdft_internal_boundary_set(c, x0, 0.0);  // src/Eigenvalues.cpp:77-81
   return CDFT_OK;
 }
 

@@ -85,6 +85,21 @@ int cdft_set_chem_potential(cdft_ctx* ctx, double mu);
 int cdft_set_fixed_mass(cdft_ctx* ctx, double mass);
 int cdft_get_chem_potential(const cdft_ctx* ctx, double* mu);
 
+/* Species::setFixedBackground / setHomogeneousBoundary (include/Species.h:24-25). The
+ * boundary is the planes i = 0, j = 0 and k = 0 (Lattice::is_boundary_point,
+ * include/Lattice.h:184-196). fixed_background = 1: after each evaluation dF = 0 there
+ * (Species::endForceCalculation, src/Species.cpp:78-82), so the minimizers leave those
+ * densities where they are; Hessian products take and give zero boundary entries
+ * (Dynamical_Matrix::matrix_dot_v1, src/DFT.cpp:441-487, src/DDFT.cpp:330-338); Log_Det
+ * zeroes its probes there and counts only the other points (src/Log_Det.cpp:88-100);
+ * Eigenvalues and Arnoldi start from a vector that is zero there. homogeneous = 1: dF on
+ * the boundary is replaced by its mean over the boundary (src/Species.cpp:84-95).
+ * A fixed background with a fixed mass makes the next evaluation fail with CDFT_ERR_ARG
+ * (the reference throws). Not built with either mode: the DDFT step, the batched driver,
+ * Newton-Krylov (cdft_fire_run_device takes its FIRE2 policy), and the homogeneous mode in
+ * cdft_fire_run_device (CDFT_ERR_ARG; the host-stepped FIRE2 calls take both modes). */
+int cdft_set_boundary(cdft_ctx* ctx, int fixed_background, int homogeneous);
+
 /* DFT::calculateFreeEnergyAndDerivatives(onlyFex) (include/DFT.h:77, src/DFT.cpp:360-425);
  * only_fex = 1 leaves out the ideal-gas term, as the reference does.
  * terms (may be NULL) receives 8 values: Omega, F_id, F_hs, F_mf, F_ext (the

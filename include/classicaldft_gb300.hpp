@@ -10,7 +10,9 @@
 // Rosenfeld / RSLT / esFMT / WhiteBearI / WhiteBearII (include/FMT.h),
 // FMT_Species (include/Species.h), LJ with setBH (include/Potential1.h),
 // Interaction_Interpolation_QF (include/Interaction.h), DFT (include/DFT.h),
-// fireMinimizer2 and DDFT (include/Minimizer.h), Eta_Too_Large_Exception.
+// fireMinimizer2 and DDFT (include/Minimizer.h), Log_Det (include/Log_Det.h),
+// Eigenvalues (include/Eigenvalues.h), Arnoldi (include/Arnoldi.h),
+// Eta_Too_Large_Exception.
 #ifndef CLASSICALDFT_GB300_HPP
 #define CLASSICALDFT_GB300_HPP
 
@@ -157,6 +159,12 @@ class FMT_Species {
   double getChemPotential() const { return mu_; }
   void setFixedMass(double m) { fixedMass_ = m; if (m > 0.0) mu_ = 0.0; }
   bool is_mass_fixed() const { return fixedMass_ > 0; }
+  // include/Species.h:24-29 (src/Species.cpp:74-95)
+  void setFixedBackground(bool fixed) { fixedBackground_ = fixed; }
+  void setHomogeneousBoundary(bool homo) { homogeneousBoundary_ = homo; }
+  bool is_background_fixed() const { return fixedBackground_; }
+  bool is_fixed_boundary() const { return fixedBackground_; }
+  bool is_boundary_homogeneous() const { return homogeneousBoundary_; }
   double getHSD() const { return hsd_; }
   Density& getDensity() { return density_; }
   const Density& getLattice() const { return density_; }
@@ -173,6 +181,7 @@ class FMT_Species {
   Density& density_;
   double hsd_, mu_;
   double fixedMass_ = -1;
+  bool fixedBackground_ = false, homogeneousBoundary_ = false;
   std::vector<double> dF_;
 };
 
@@ -278,6 +287,7 @@ class DFT {
   void push() {
     cdft_ctx* c = context();
     check(cdft_set_density(c, s_->getDensity().data(), 0), c);
+    check(cdft_set_boundary(c, s_->is_background_fixed() ? 1 : 0, s_->is_boundary_homogeneous() ? 1 : 0), c);
     if (s_->is_mass_fixed()) check(cdft_set_fixed_mass(c, s_->fixedMass()), c);
     else check(cdft_set_chem_potential(c, s_->getChemPotential()), c);
   }

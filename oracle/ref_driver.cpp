@@ -529,6 +529,48 @@ int main(int argc, char** argv) {
       }
     } else if (c == "files") {
       case_files(argv[2]);
+    } else if (c == "boundary") {
+      // Species::setFixedBackground / setHomogeneousBoundary (src/Species.cpp:74-95): the
+      // boundary planes i = 0, j = 0, k = 0 in the evaluation, the Hessian
+      // (src/DFT.cpp:441-487, Dynamical_Matrix::matrix_dot_v1), FIRE2 and Log_Det.
+      const long N = 16 * 16 * 16;
+      {
+        System S = make_system(0.2, 16, "WhiteBearI", false, 1.0);
+        fill_noise(*S.d, 0.6, 0.2, 11);
+        S.s->setChemPotential(S.dft->mu_times_beta(0.6));
+        S.s->setFixedBackground(true);
+        record_eval("bfix", S, true, {});
+        DFT_Vec v(N), r(N);
+        SplitMix64 g(77);
+        for (long i = 0; i < N; ++i) v.set(i, 0.3 * (2.0 * g.uniform() - 1.0));
+        S.dft->matrix_dot_v1(v, r, nullptr);
+        put("bfix.Hv", vec_of(r));
+        Log_Det ld(*S.dft, 10, 0.16, 0.008, false);
+        double var = 0;
+        const double val = ld.calculate_log_det(1234, 2, false, var);
+        put("bfix.logdet", {val, var});
+        FireProbe fire(S.dft);
+        fire.setForceTerminationCriterion(0.0);
+        fire.run(30);
+        put("bfix.fire.F", fire.F);
+        put("bfix.fire.rho", density_of(*S.d));
+      }
+      {
+        System S = make_system(0.2, 16, "WhiteBearI", false, 1.0);
+        fill_noise(*S.d, 0.6, 0.2, 11);
+        S.s->setChemPotential(S.dft->mu_times_beta(0.6));
+        S.s->setHomogeneousBoundary(true);
+        record_eval("bhom", S, true, {});
+      }
+      {
+        System S = make_system(0.2, 16, "WhiteBearI", false, 1.0);
+        fill_noise(*S.d, 0.6, 0.2, 11);
+        const double mass = S.d->getNumberAtoms();
+        S.s->setFixedMass(0.98 * mass);
+        S.s->setHomogeneousBoundary(true);
+        put1("bhomfm.fixed_mass", 0.98 * mass);
+        record_eval("bhomfm", S, true, {});
+      }
     } else if (c == "spectral") {
       // Pins of the spectral drivers (Eigenvalues, Arnoldi, Log_Det consume matrix_dot_v1):
       // the dense Hessian of a hard-sphere state and of an LJ state (tests/golden/make_golden.py

@@ -21,7 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 CASES = ["weights", "phi", "bulk", "eval_models16", "eval_hs32", "eval_lj", "fire_hs32", "fire_lj24",
-         "ddft_lj16", "ddft_adapt16", "coex", "hessian", "files", "ao", "spectral"]
+         "ddft_lj16", "ddft_adapt16", "coex", "hessian", "files", "ao", "spectral", "boundary"]
 # cases that also leave files next to their output: copied here as <case>.<suffix>
 FILE_OUTPUTS = {"files": [".a.vtk", ".b.vtk"]}
 
