@@ -67,7 +67,9 @@ typedef struct cdft_info {
 /* Context life cycle. cdft_create builds the weights (FMT_Species::generateWeights,
  * src/FMT_Species.cpp:310-496; Interaction_Base::initialize, src/Interaction.cpp:32-52)
  * and allocates every device buffer of the path; later calls allocate nothing
- * except the first cdft_fire_init / cdft_ddft_init, which allocate that loop's state. */
+ * except the first cdft_fire_init / cdft_ddft_init (that loop's state), the first
+ * Hessian product (its two vectors and the weighted densities) and the spectral
+ * drivers (their Krylov bases and probe buffers, for the duration of the call). */
 int cdft_create(const cdft_params* p, cdft_ctx** out);
 int cdft_destroy(cdft_ctx* ctx);
 const char* cdft_last_error(const cdft_ctx* ctx);
