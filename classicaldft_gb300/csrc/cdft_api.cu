@@ -242,6 +242,7 @@ struct FDdftRhs {
   double* R;
   int nx, ny, nz;
   double dx, dV;
+  int fixed;  // a fixed background: g.x = 0 on the boundary (src/DDFT.cpp:333-338)
   __device__ void operator()(long p, double*, double* m) const {
     const int k = (int)(p % nz);
     const long t = p / nz;
@@ -257,6 +258,7 @@ struct FDdftRhs {
     g += D * ((rho[py] + d0) * (dF[py] - x0) - (d0 + rho[my]) * (x0 - dF[my]));
     g += D * ((rho[pz] + d0) * (dF[pz] - x0) - (d0 + rho[mz]) * (x0 - dF[mz]));
     g *= 1.0 / dV;
+    if (fixed && cdft_on_boundary(p, ny, nz)) g = 0.0;
     m[0] = fabs(g);
     const double L = 1.0 / (dx * dx);
     R[p] = g + (-L * (rho[px] + rho[mx] - 2 * d0) - L * (rho[py] + rho[my] - 2 * d0) - L * (rho[pz] + rho[mz] - 2 * d0));
@@ -463,6 +465,10 @@ static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
 __global__ void k_boundary_set(double* __restrict__ a, long N, int ny, int nz, double value) {
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < N; p += (long)gridDim.x * blockDim.x)
     if (cdft_on_boundary(p, ny, nz)) a[p] = value;
+}
+__global__ void k_boundary_copy(double* __restrict__ a, const double* __restrict__ b, long N, int ny, int nz) {
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < N; p += (long)gridDim.x * blockDim.x)
+    if (cdft_on_boundary(p, ny, nz)) a[p] = b[p];
 }
 void cdft_internal_boundary_set(cdft_ctx* c, double* a, double value) {
   k_boundary_set<<<grid_for(c->info.N), 256, 0, c->stream>>>(a, c->info.N, c->p.ny, c->p.nz, value);
@@ -1220,7 +1226,6 @@ static int ddft_r2c(cdft_ctx* c, const double* real, void* spec) {
 int cdft_ddft_init(cdft_ctx* c, double dt, double dt_max, double tol) {
   if (!c) return CDFT_ERR_ARG;
   if (c->p.model < 0 && !c->p.lj) return fail(c, CDFT_ERR_ARG, "DDFT needs an FMT model or an interaction");
-  if (c->fixed_bg || c->homo_bd) return fail(c, CDFT_ERR_ARG, "the DDFT step is not built for boundary modes");
   const long N = c->info.N;
   const long Nc = c->precision == CDFT_FP64 ? c->e64->spectrum_len() : c->e32->spectrum_len();  // padded rows
   const size_t cs = sizeof(double2);  // large enough for either precision
@@ -1275,7 +1280,7 @@ static void ddft_change_timestep(cdft_ctx* c, double ndt) {
 
 static int ddft_rhs(cdft_ctx* c, const double* rho, void* spec, double* rmax) {
   double m;
-  FDdftRhs f{rho, c->dF, c->dR, c->p.nx, c->p.ny, c->p.nz, c->p.dx, c->info.dV};
+  FDdftRhs f{rho, c->dF, c->dR, c->p.nx, c->p.ny, c->p.nz, c->p.dx, c->info.dV, c->fixed_bg};
   int rc = map_reduce<0, 1>(c, c->info.N, f, &m);
   if (rc) return rc;
   if (rmax) *rmax = m / c->info.dV;
@@ -1346,6 +1351,8 @@ static int ddft_one_step(cdft_ctx* c, int* restarts, bool dF_current) {
         if (rc) return rc;
         k_add_const<<<grid_for(N), 256, 0, c->stream>>>(c->ddn, N, (m - c->ddft_mass0) / (double)N);
       }
+      if (c->fixed_bg)  // the boundary keeps the iterate's densities (src/DDFT.cpp:280-281)
+        k_boundary_copy<<<grid_for(N), 256, 0, c->stream>>>(c->ddn, c->dd1, N, c->p.ny, c->p.nz);
       double red[2];
       rc = map_reduce<0, 2>(c, N, FDdftDev{c->dd1, c->ddn}, red);
       if (rc) return rc;
@@ -1380,7 +1387,6 @@ static int ddft_one_step(cdft_ctx* c, int* restarts, bool dF_current) {
 
 int cdft_ddft_step(cdft_ctx* c, int nsteps, cdft_ddft_report* rep) {
   if (!c) return CDFT_ERR_ARG;
-  if (c->fixed_bg || c->homo_bd) return fail(c, CDFT_ERR_ARG, "the DDFT step is not built for boundary modes");
   if (!c->ddft_ready) return fail(c, CDFT_ERR_STATE, "cdft_ddft_init has not been called");
   int restarts = 0;
   for (int k = 0; k < nsteps; ++k) {

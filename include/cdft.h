@@ -94,12 +94,14 @@ int cdft_get_chem_potential(const cdft_ctx* ctx, double* mu);
  * densities where they are; Hessian products take and give zero boundary entries
  * (Dynamical_Matrix::matrix_dot_v1, src/DFT.cpp:441-487, src/DDFT.cpp:330-338); Log_Det
  * zeroes its probes there and counts only the other points (src/Log_Det.cpp:88-100);
- * Eigenvalues and Arnoldi start from a vector that is zero there. homogeneous = 1: dF on
- * the boundary is replaced by its mean over the boundary (src/Species.cpp:84-95).
- * A fixed background with a fixed mass makes the next evaluation fail with CDFT_ERR_ARG
- * (the reference throws). Not built with either mode: the DDFT step, the batched driver,
- * Newton-Krylov (cdft_fire_run_device takes its FIRE2 policy), and the homogeneous mode in
- * cdft_fire_run_device (CDFT_ERR_ARG; the host-stepped FIRE2 calls take both modes). */
+ * Eigenvalues and Arnoldi start from a vector that is zero there; the DDFT step's g . dF
+ * is zero there and the boundary densities stay as they are (src/DDFT.cpp:280-281).
+ * homogeneous = 1: dF on the boundary is replaced by its mean over the boundary
+ * (src/Species.cpp:84-95). A fixed background with a fixed mass makes the next
+ * evaluation fail with CDFT_ERR_ARG (the reference throws). Not built with either mode:
+ * the batched driver, Newton-Krylov (cdft_fire_run_device takes its FIRE2 policy), and
+ * the homogeneous mode in cdft_fire_run_device (CDFT_ERR_ARG; the host-stepped FIRE2
+ * calls take both modes). */
 int cdft_set_boundary(cdft_ctx* ctx, int fixed_background, int homogeneous);
 
 /* DFT::calculateFreeEnergyAndDerivatives(onlyFex) (include/DFT.h:77, src/DFT.cpp:360-425);

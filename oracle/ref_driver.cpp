@@ -571,6 +571,21 @@ int main(int argc, char** argv) {
         put1("bhomfm.fixed_mass", 0.98 * mass);
         record_eval("bhomfm", S, true, {});
       }
+      // DDFT with each boundary mode (src/DDFT.cpp:280-281, 333-338): the LJ system of ddft_lj16
+      for (int mode = 0; mode < 2; ++mode) {
+        System S = make_system(0.1, 16, "WhiteBearI", true, 0.8);
+        fill_noise(*S.d, 0.3, 0.1, 5);
+        if (mode == 0) S.s->setFixedBackground(true);
+        else S.s->setHomogeneousBoundary(true);
+        DDFTProbe ddft(S.dft);
+        ddft.setTimeStep(1e-4);
+        ddft.set_max_time_step(1e-4);
+        ddft.setForceTerminationCriterion(0.0);
+        ddft.run(10);
+        const std::string tag = mode == 0 ? "bddft_fix" : "bddft_hom";
+        put(tag + ".F", ddft.F); put(tag + ".mass", ddft.mass); put(tag + ".dt", ddft.dt);
+        put(tag + ".rho_final", density_of(*S.d));
+      }
     } else if (c == "spectral") {
       // Pins of the spectral drivers (Eigenvalues, Arnoldi, Log_Det consume matrix_dot_v1):
       // the dense Hessian of a hard-sphere state and of an LJ state (tests/golden/make_golden.py

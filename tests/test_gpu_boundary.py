@@ -124,10 +124,32 @@ def test_fire_with_fixed_background(cd, oracle):
     c.close()
 
 
+@pytest.mark.parametrize("tag,fixed", [("bddft_fix", True), ("bddft_hom", False)])
+def test_ddft_with_boundary_mode(cd, oracle, tag, fixed):
+    """10 DDFT steps of the LJ system of ddft_lj16 (dt = 1e-4 fixed) with each mode: g . dF
+    vanishes on a fixed boundary and its densities stay (the mass then changes); the
+    homogeneous boundary only changes dF."""
+    g = golden("boundary")
+    c = cd.Context(SHAPE, 0.1, cd.WHITEBEAR_I, hsd=golden("eval_lj")["lj24.hsd"][0], lj=True, kT=0.8)
+    rho0 = oracle.fill_noise(SHAPE, 0.3, 0.1, 5)
+    c.set_density(rho0)
+    c.set_boundary(fixed_background=fixed, homogeneous=not fixed)
+    c.ddft_init(1e-4, 1e-4)
+    F, mass = [], []
+    for _ in range(10):
+        r = c.ddft_step(1)
+        F.append(r["F"]); mass.append(r["mass"])
+    np.testing.assert_allclose(F, g[tag + ".F"], rtol=1e-12)
+    np.testing.assert_allclose(mass, g[tag + ".mass"], rtol=1e-13)
+    rho = c.get_density().ravel()
+    np.testing.assert_allclose(rho, g[tag + ".rho_final"], rtol=1e-10)
+    if fixed:
+        assert np.all(rho[boundary_mask()] == rho0.ravel()[boundary_mask()])
+    c.close()
+
+
 def test_boundary_modes_report_what_is_not_built(cd, oracle):
     c = context(cd, oracle, homo=True)
-    with pytest.raises(cd.CDFTError):
-        c.ddft_init(1e-4, 1e-3)
     c.fire_init(force_limit=0.0)
     with pytest.raises(cd.CDFTError):
         c.fire_run_device(1e-8, max_steps=10)
