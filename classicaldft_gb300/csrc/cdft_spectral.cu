@@ -1,5 +1,5 @@
 // Spectral drivers on the matrices of the path (consumers of the Hessian product):
-//   Log_Det::calculate_log_det          (include/Log_Det.h, src/Log_Det.cpp:23-166)
+//   Log_Det::calculate_log_det          (include/Log_Det.h, src/Log_Det.cpp:22-166)
 //   Eigenvalues::calculate_eigenvector  (include/Eigenvalues.h, src/Eigenvalues.cpp)
 //   Arnoldi::determine_largest_eigenpairs (include/Arnoldi.h, src/Arnoldi.cpp:72-283)
 // Every vector lives on the device and every product is the context's Hessian pass;
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256) k_sub_proj(const double* __restrict__ V, 
   }
 }
 // y <- a * y + b * (s . x) * s + c * x, with the dot s . x read from the device
-// (Eigenvalues::calculate_gradients' vshift term, src/Eigenvalues.cpp:47-51, and the shift)
+// (Eigenvalues::calculate_gradients' vshift term, src/Eigenvalues.cpp:49-50, and the shift)
 __global__ void __launch_bounds__(256) k_op_finish(double* __restrict__ y, const double* __restrict__ x, const double* __restrict__ s,
                                                    const double* __restrict__ sdotx, double a, double b, double c, long N) {
   const double bs = s ? b * sdotx[0] : 0.0;
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) k_seed_vector(double* __restrict__ x, lon
   }
 }
 
-// Chebyshev steps of Log_Det::calculate_log_det (src/Log_Det.cpp:104-137). r = M x
+// Chebyshev steps of Log_Det::calculate_log_det (src/Log_Det.cpp:113-144). r = M x
 // from the matrix pass; the matrix the estimator expands is A x = sg r + z sum(x)
 // (sg = -1 for a dynamic matrix, z = lam_mid / N when it has a zero eigenvalue).
 // First term: w1 = al (A v) + be v; u = c0 v + c1 w1.
@@ -226,7 +226,7 @@ void jacobi_eigen(std::vector<double> A, int n, std::vector<double>& w, std::vec
   for (int i = 0; i < n; ++i) w[i] = A[(size_t)i * n + i];
 }
 
-// Log_Det::get_coefficients (src/Log_Det.cpp:32-57): the Chebyshev coefficients of
+// Log_Det::get_coefficients (src/Log_Det.cpp:34-57): the Chebyshev coefficients of
 // log(0.5 (b - a) x + 0.5 (b + a)) on [-1, 1] at the order + 1 Chebyshev nodes.
 std::vector<double> log_cheb_coefficients(int order, double a, double b) {
   std::vector<double> c(order + 1, 0.0);
@@ -287,7 +287,7 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
   const int ny = c->p.ny, nz = c->p.nz;
   auto draw = [&](double* h) {
     for (long p = 0; p < N; ++p) h[p] = distrib(rng) > 0 ? 1.0 : -1.0;
-    if (c->fixed_bg)  // Log_Det::set_boundary_points_to_zero (src/Log_Det.cpp:58-64, :99)
+    if (c->fixed_bg)  // Log_Det::set_boundary_points_to_zero (src/Log_Det.cpp:59-64, 111)
       for (long p = 0; p < N; ++p)
         if (cdft_on_boundary(p, ny, nz)) h[p] = 0.0;
   };
@@ -330,7 +330,7 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
   std::vector<double> vu(num_samples);
   SP_CK(c, cudaMemcpyAsync(vu.data(), scal + 2, num_samples * sizeof(double), cudaMemcpyDeviceToHost, s));
   SP_CK(c, cudaStreamSynchronize(s));
-  // the reference's running sums (src/Log_Det.cpp:139-161)
+  // the reference's running sums (src/Log_Det.cpp:145-165)
   double acc = 0, acc2 = 0, var = 0;
   for (int i = 1; i <= num_samples; ++i) {
     acc += vu[i - 1];
@@ -340,7 +340,7 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
   }
   double ld = acc / num_samples;
   if (has_zero_eigenvalue) ld -= std::log(lam_mid);
-  const long n_active = N - (c->fixed_bg ? cdft_n_boundary(c->p.nx, ny, nz) : 0);  // src/Log_Det.cpp:89
+  const long n_active = N - (c->fixed_bg ? cdft_n_boundary(c->p.nx, ny, nz) : 0);  // src/Log_Det.cpp:91
   ld -= (double)n_active * std::log(scale);
   *log_det = ld;
   if (variance) *variance = var;
@@ -383,7 +383,7 @@ struct LanczosResult {
 // stay on the device, the projected ncv x ncv matrix on the host. x0 is the (device)
 // start vector. Converged when every wanted pair (only the first with all = false) has
 // |residual| <= tol |theta - shift|, or (degenerate_rule) lies within tol of the first
-// discarded Ritz value (the stopping rule of src/Arnoldi.cpp:240-262). vecs (nev * N, device) receives the
+// discarded Ritz value (the stopping rule of src/Arnoldi.cpp:247-263). vecs (nev * N, device) receives the
 // Ritz vectors, unit norm.
 int lanczos(cdft_ctx* c, SymOp& op, Want want, int nev, int ncv, double tol, bool all, bool degenerate_rule, long max_matvecs,
             int max_restarts, const double* x0, double* vecs, LanczosResult* out) {
@@ -494,13 +494,13 @@ int start_vector(cdft_ctx* c, const double* guess, int on_device, long seed, dou
     SP_CK(c, cudaMemcpyAsync(x0, guess, N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
   else
     k_seed_vector<<<sp_grid(N), 256, 0, c->stream>>>(x0, N, (unsigned long long)seed);
-  if (c->fixed_bg) cdft_internal_boundary_set(c, x0, 0.0);  // src/Eigenvalues.cpp:77-81
+  if (c->fixed_bg) cdft_internal_boundary_set(c, x0, 0.0);  // src/Eigenvalues.cpp:75-83
   return CDFT_OK;
 }
 
 }  // namespace
 
-// Eigenvalues::calculate_eigenvector (src/Eigenvalues.cpp:66-99; objective :43-64): the
+// Eigenvalues::calculate_eigenvector (src/Eigenvalues.cpp:69-99; objective :44-66): the
 // smallest eigenvalue of sg scale (H + vshift vshift^T / 2), sg = -1 with change_sign,
 // reported as the reference reports it (divided by scale, sign restored).
 int cdft_eigenvalue(cdft_ctx* c, double scale, double tol, int change_sign, const double* vshift, const double* guess, long max_matvecs,

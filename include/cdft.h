@@ -93,7 +93,7 @@ int cdft_get_chem_potential(const cdft_ctx* ctx, double* mu);
  * (Species::endForceCalculation, src/Species.cpp:78-82), so the minimizers leave those
  * densities where they are; Hessian products take and give zero boundary entries
  * (Dynamical_Matrix::matrix_dot_v1, src/DFT.cpp:441-487, src/DDFT.cpp:330-338); Log_Det
- * zeroes its probes there and counts only the other points (src/Log_Det.cpp:88-100);
+ * zeroes its probes there and counts only the other points (src/Log_Det.cpp:91, 111);
  * Eigenvalues and Arnoldi start from a vector that is zero there; the DDFT step's g . dF
  * is zero there and the boundary densities stay as they are (src/DDFT.cpp:280-281).
  * homogeneous = 1: dF on the boundary is replaced by its mean over the boundary
@@ -135,7 +135,7 @@ int cdft_ddft_matrix_dot_v(cdft_ctx* ctx, const double* v, double* out, int on_d
 #define CDFT_MATRIX_DDFT 1    /* DDFT: g . H (is_dynamic() true; Log_Det expands -g . H) */
 
 /* Log_Det(matrix, order, lam_max, lam_min).calculate_log_det(seed, num_samples,
- * has_zero_eigenvalue, variance) (include/Log_Det.h:21-51, src/Log_Det.cpp:23-166): the
+ * has_zero_eigenvalue, variance) (include/Log_Det.h:21-51, src/Log_Det.cpp:22-166): the
  * stochastic Chebyshev estimate of log det of the matrix whose spectrum lies in
  * [lam_min, lam_max], with the reference's +-1 probe vectors for the same seed
  * (std::mt19937(seed), uniform_int_distribution<>(0, 1), point order; seed <= 0 draws
@@ -152,7 +152,7 @@ typedef struct cdft_eigen_report {
 } cdft_eigen_report;
 
 /* Eigenvalues(dft).calculate_eigenvector (include/Eigenvalues.h:16-57,
- * src/Eigenvalues.cpp:43-99) with set_scale(scale), set_tolerence(tol),
+ * src/Eigenvalues.cpp:44-99) with set_scale(scale), set_tolerence(tol),
  * set_change_sign(change_sign), set_vshift(vshift) (NULL: none): the smallest eigenvalue
  * of s (H + vshift vshift^T / 2), s = scale (change_sign = 0) or -scale (1), returned as
  * the reference's get_eigenvalue() does (divided by scale, sign restored; so change_sign
@@ -172,7 +172,7 @@ int cdft_eigenvalue(cdft_ctx* ctx, double scale, double tol, int change_sign, co
  * tol |lambda| or it is degenerate (within tol) with the largest discarded Ritz value;
  * all_k = 0 asks only for the first. Returns CDFT_ERR_TIMEOUT after max_steps restarts
  * without convergence (the reference throws; the outputs then hold the last estimates).
- * The reference stores the first Ritz value under every index (src/Arnoldi.cpp:207);
+ * The reference stores the first Ritz value under every index (src/Arnoldi.cpp:210);
  * here eigvals[i] is the i-th pair's own value. Hessian only. */
 int cdft_arnoldi_largest(cdft_ctx* ctx, double shift, int k, int p, int all_k, long max_steps, double tol, const double* guess,
                          double* eigvals, double* eigvecs, int on_device, cdft_eigen_report* rep);

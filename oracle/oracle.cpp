@@ -1196,7 +1196,7 @@ int orc_ddft(orc_ctx* c, double* rho, int nsteps, double dt_init, double dt_max,
 }
 
 // Log_Det::calculate_log_det (src/Log_Det.cpp:84-166) with the coefficients of
-// Log_Det::get_coefficients (:32-57): a Chebyshev expansion of log on the spectrum
+// Log_Det::get_coefficients (:34-57): a Chebyshev expansion of log on the spectrum
 // [lam_min, lam_max] scaled by 1/(lam_min + lam_max), traced by Hutchinson with +-1
 // vectors from std::mt19937(seed) and uniform_int_distribution<>(0, 1), drawn in
 // point order, sample after sample. dynamic = 1 uses -(g . H), the DDFT matrix the
