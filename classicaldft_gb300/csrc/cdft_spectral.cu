@@ -8,8 +8,8 @@
 // Log_Det keeps the reference's estimator exactly: the Chebyshev coefficients of log,
 // the three-term recurrence and Hutchinson's trace with the +-1 vectors that
 // std::mt19937(seed) and uniform_int_distribution<>(0, 1) give, drawn in point order
-// (the host draws sample i + 1 while the device runs sample i). Eigenvalues and Arnoldi
-// compute what the reference computes (the smallest eigenvalue of the signed, scaled and
+// (the host draws sample i + 1 while the device runs sample i's queued products).
+// Eigenvalues and Arnoldi compute what the reference computes (the smallest eigenvalue of the signed, scaled and
 // rank-one shifted Hessian; the k eigenpairs of H + shift of largest magnitude) with a
 // thick-restart Lanczos iteration, fully re-orthogonalised, instead of nlopt's L-BFGS on
 // the Rayleigh quotient and Armadillo's complex implicitly restarted Arnoldi: the
@@ -313,10 +313,6 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
     k_cheb_first<<<g, 256, 0, s>>>(r, v, scal, sg, z, scale * 2.0 / (b - a), -(b + a) / (b - a), cf[0], cf[1], w1, u, N);
     double *p0 = w0, *p1 = w1;  // w0 holds the term before w1: v for k = 2
     SP_CK(c, cudaMemcpyAsync(p0, v, N * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    if (i + 1 < num_samples) {  // draw the next vector into the other pinned buffer once its last copy is done
-      SP_CK(c, cudaEventSynchronize(copied[cur ^ 1]));
-      draw(hv[cur ^ 1]);
-    }
     for (int k = 2; k <= order; ++k) {
       rc = matvec(p1, r);
       if (rc) return rc;
@@ -326,6 +322,10 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
     }
     dots(v, 1, u, N, part, scal + 2 + i, s);
     SP_CK(c, cudaGetLastError());
+    if (i + 1 < num_samples) {  // with this sample's products queued, draw the next probe into the other pinned buffer
+      SP_CK(c, cudaEventSynchronize(copied[cur ^ 1]));  // (once the copy that last read it is done)
+      draw(hv[cur ^ 1]);
+    }
   }
   std::vector<double> vu(num_samples);
   SP_CK(c, cudaMemcpyAsync(vu.data(), scal + 2, num_samples * sizeof(double), cudaMemcpyDeviceToHost, s));
