@@ -2,14 +2,22 @@
 WhiteBearI FMT + QF mean field of the cut-and-shifted LJ, kT = 0.8, dx = 0.1),
 one JSON line on stdout.
 
-`value`  FP32-bulk evaluations/s with the density resident in HBM (FP64
-         reductions), timed with CUDA events per step; L2 flushed between steps.
-`e2e`    the same evaluation through the public C ABI from host buffers
+`value`  FP64 evaluations/s (the reference's precision) with the density resident
+         in HBM, timed with CUDA events per step; L2 flushed between steps.
+`e2e`    the same FP64 evaluation through the public C ABI from host buffers
          (host density in, host dF out, copies inside the timed region).
-Extra keys: the FP64 rate, a per-pass breakdown with roofline fractions, the
-oracle CPU baseline. With --impl reference the FP64 CPU oracle (the port of the
-reference's path; the reference itself needs FFTW/GSL/Boost/Armadillo, absent
-on the GPU machines) is timed on all host cores.
+`roofline`  the dominant FP64 pass against the device's FP64 FMA rate, measured in
+         the same run (GB300's FP64 unit, not HBM, bounds the FP64 passes), with its
+         HBM fraction beside it.
+`fp32`   the FP32-bulk evaluation of the same system (FP64 reductions): its rate,
+         its error against FP64 on the same density, its HBM roofline.
+Extra keys: per-pass breakdowns, the time-to-residual legs (their converged
+densities checked by the FP64 oracle in the CPU leg), the 256^3 evaluation and
+DDFT legs (FP32 against an FP64 run of the same trajectory), the state-point
+sweep, the spectral drivers, the learned warm start, and the oracle CPU baseline.
+With --impl reference the FP64 CPU oracle (the port of the reference's path; the
+reference itself needs FFTW/GSL/Boost/Armadillo, absent on the GPU machines) is
+timed on all host cores.
 Multi-GPU: replicas only (each rank evaluates its own system); value is the sum.
 """
 import argparse
@@ -39,13 +47,25 @@ def droplet():
 def workload():
     return {"workload": "LJ droplet F+dF evaluation, 128^3, dx=0.1, WhiteBearI + QF mean field, kT=0.8, "
                         "rho_v=0.01, rho_l=0.75, R=4, w=0.5, grand canonical at mu(rho_v)",
-            "grid": list(SHAPE), "model": "WhiteBearI", "interaction": "QF", "precision_bulk": "fp32",
-            "reductions": "fp64 compensated", "l2": "flushed between timed steps (256 MB write)"}
+            "grid": list(SHAPE), "model": "WhiteBearI", "interaction": "QF", "precision": "fp64 throughout",
+            "l2": "flushed between timed steps (256 MB write)"}
 
 
 # DRAM bytes per launch (read + write) from one ncu capture of the named kernel on
 # this workload; None where none was taken.
 NCU_TRAFFIC = {("phi_rows", "fp32"): 98.1e6 + 39.7e6}
+# FP64 work per launch of a pass (ncu: smsp__sass_thread_inst_executed_op_{dadd,dmul}_pred_on.sum
+# + 2 x ..._dfma_pred_on.sum) on this workload; None where none was taken.
+NCU_FP64_FLOPS = {}
+
+
+def fp64_fma_peak(cd):
+    """The device's sustained FP64 FMA rate in TFLOP/s, measured now (cdft_fp64_fma_rate)."""
+    import ctypes
+    v = ctypes.c_double()
+    if cd.lib().cdft_fp64_fma_rate(ctypes.byref(v), None) != 0:
+        return None
+    return v.value
 
 
 def measured_peaks():
@@ -118,6 +138,21 @@ def cpu_baseline(budget_s=15.0, steps=None):
     return n / el, n, el
 
 
+def oracle_pins(kept):
+    """The CPU leg's check of the converged 128^3 droplets: one FP64 oracle evaluation
+    (fixed mass, the same hard-sphere diameter) of each end density the time-to-residual
+    legs reached, its Omega against the GPU's and its own max|dOmega/drho|."""
+    from oracle import pyoracle
+    out = {}
+    for name, (rho, omega_gpu, mass, hsd) in kept.items():
+        o = pyoracle.Oracle(SHAPE, DX, "WhiteBearI", hsd=hsd, lj=True, kT=KT, fixed_mass=mass)
+        _, t, dF, _ = o.eval(rho)
+        out[name] = {"omega_oracle": t["Omega"], "omega_gpu": omega_gpu,
+                     "omega_rel_vs_oracle": abs(omega_gpu - t["Omega"]) / abs(t["Omega"]),
+                     "oracle_resid": float(np.abs(dF).max() / DX ** 3)}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -146,28 +181,64 @@ def ddft_initial_density(n=256, dx=0.1, seed=3, rho0=0.3, amp=0.1, ell=1.0):
     return np.maximum(rho0 * (1 + amp * g), 1e-6)
 
 
-def ddft_leg(cd, n=256, steps=2000):
-    """Integrating-factor DDFT of the LJ system at 256^3, dx = 0.1, dt = 1e-4 fixed,
-    FP32 bulk with the FP64 mass restore: the full 2000-step run, its wall time, ms per
-    step and the mass drift over the run."""
+def ddft_leg(cd, n=256, steps=2000, compare_at=101):
+    """Integrating-factor DDFT of the LJ system at 256^3, dx = 0.1, dt = 1e-4 fixed.
+    FP32 bulk with the FP64 mass restore: one warm-up step, then 2000 timed steps (wall
+    time, ms per step, and the largest mass deviation the restore corrected). The same
+    FP32 run without the restore gives the propagator's own FP32 mass drift over the
+    whole run. An FP64 run of the first `compare_at` steps (the reference's arithmetic)
+    gives the FP32 trajectory's error at that step, with and without the restore."""
     import torch
     rho = ddft_initial_density(n)
-    c = cd.Context((n, n, n), DX, cd.WHITEBEAR_I, hsd=cd.bh_diameter(1.0, 1.0, 3.0, KT), lj=True, kT=KT,
-                   precision=cd.FP32)
-    c.set_chem_potential(c.bulk(0.3)["mu"])
-    c.set_density(rho)
-    c.ddft_init(1e-4, 1e-4)
+    hsd = cd.bh_diameter(1.0, 1.0, 3.0, KT)
     m0 = float(np.sum(rho)) * DX ** 3
-    c.ddft_step(1)  # warm-up
+
+    def ctx(prec, restore=True):
+        c = cd.Context((n, n, n), DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT, precision=prec)
+        c.set_chem_potential(c.bulk(0.3)["mu"])
+        c.set_density(rho)
+        c.ddft_init(1e-4, 1e-4)
+        c.ddft_set_mass_restore(restore)
+        return c
+
+    c = ctx(cd.FP32)
+    c.ddft_step(1)  # warm-up: step 1 of the trajectory
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    r = c.ddft_step(steps)
+    c.ddft_step(compare_at - 1)
     torch.cuda.synchronize()
-    el = (time.perf_counter() - t0) / steps
+    el = time.perf_counter() - t0
+    d32 = c.get_density()  # outside the timing
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = c.ddft_step(steps - (compare_at - 1))
+    torch.cuda.synchronize()
+    el = (el + time.perf_counter() - t0) / steps
     out = {"grid": [n, n, n], "dt": 1e-4, "ms_per_step": 1e3 * el, "steps_timed": steps,
-           "run_s": steps * el, "mass_rel_drift": abs(r["mass"] - m0) / m0,
-           "precision": "fp32 bulk, fp64 mass restore"}
+           "run_s": steps * el, "precision": "fp32 bulk, fp64 mass restore",
+           "mass_rel_drift": abs(r["mass"] - m0) / m0,
+           "mass_note": "zero by construction: each propagated density is shifted back to the starting mass",
+           "restore_max_rel_correction": c.ddft_mass_deviation()}
     c.close()
+    c = ctx(cd.FP32, restore=False)
+    c.ddft_step(compare_at)
+    d32n = c.get_density()
+    r = c.ddft_step(steps + 1 - compare_at)
+    out["no_restore"] = {"steps": steps + 1, "mass_rel_drift": abs(r["mass"] - m0) / m0,
+                         "max_rel_mass_deviation": c.ddft_mass_deviation()}
+    c.close()
+    c = ctx(cd.FP64)
+    t0 = time.perf_counter()
+    r64 = c.ddft_step(compare_at)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    d64 = c.get_density()
+    c.close()
+    out["vs_fp64"] = {"step": compare_at, "fp64_ms_per_step": 1e3 * t64 / compare_at,
+                      "fp64_mass_rel_drift": abs(r64["mass"] - m0) / m0,
+                      "max_abs_rho_diff": float(np.abs(d32 - d64).max()),
+                      "max_abs_rho_diff_no_restore": float(np.abs(d32n - d64).max()),
+                      "max_rho": float(d64.max()), "min_rho": float(d64.min())}
     return out
 
 
@@ -227,7 +298,7 @@ def spectral_leg(cd, rho):
     return out
 
 
-def fire_legs(cd, rho, tol=1e-8, max_steps=20000, legs=("newton", "mixed_newton", "mixed_fire", "plain_fp64")):
+def fire_legs(cd, rho, tol=1e-8, max_steps=20000, legs=("newton", "mixed_newton", "mixed_fire", "plain_fp64"), keep=None):
     """Wall seconds to reach max|dOmega/drho| <= tol on the droplet at fixed mass,
     every leg device-resident and starting from the same tanh profile, FIRE2 with
     the reference defaults (dt = 1e-3, dt_max = 1e-2):
@@ -237,7 +308,8 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000, legs=("newton", "mixed_newton"
                     refinement (FP32 Hessian products, FP64 residuals);
       newton        Newton-Krylov from the start (FP32 Hessian products, FP64
                     residuals and line search).
-    Each end state is re-evaluated in FP64."""
+    Each end state is re-evaluated in FP64; with `keep` (a dict) each end density is
+    kept there for the oracle's check of the converged state."""
     import torch
     hsd = cd.bh_diameter(1.0, 1.0, 3.0, KT)
     mass = float(rho.sum()) * DX ** 3
@@ -261,6 +333,8 @@ def fire_legs(cd, rho, tol=1e-8, max_steps=20000, legs=("newton", "mixed_newton"
         res[name] = {"seconds": el, "fire_steps": r["total_steps"], "fp32_steps": r["steps_fp32"],
                      "newton": r["newton"], "cg_iters": r["cg_iters"], "resid": t["resid"],
                      "Omega": t["Omega"], "converged": bool(t["resid"] <= tol)}
+        if keep is not None:
+            keep[name] = (c.get_density(), t["Omega"], mass, hsd)
         c.close()
     out.update(res)
     if len(res) < 4:  # a subset of the legs (e.g. for a profile): no ratios
@@ -458,7 +532,7 @@ def main():
     import classicaldft_gb300 as cd
 
     rho = droplet()
-    c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=None, lj=True, kT=KT, precision=cd.FP32)
+    c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=None, lj=True, kT=KT, precision=cd.FP64)
     c.set_chem_potential(c.bulk(RHO_V)["mu"])
     c.set_density(rho)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -484,16 +558,13 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return t.item() / K  # ms per step, max over ranks
 
+    # the headline: FP64 evaluations, the reference's own precision
     with Clocks(local) as clk:
-        ms32 = timed(args.steps, max(3, args.warmup), lambda: c.eval(want_dF=False))
+        ms64 = timed(args.steps, max(3, args.warmup), lambda: c.eval(want_dF=False))
     clocks = clk.summary()
-    passes = c.time_passes(reps=5)
-    c.set_precision(cd.FP64)
-    ms64 = timed(max(3, args.steps // 10), 3, lambda: c.eval(want_dF=False))
     passes64 = c.time_passes(reps=3)
-    c.set_precision(cd.FP32)
-    # e2e through the public API: the density from pinned host memory in, dF to pinned host
-    # memory out, every step (cdft_set_density + cdft_eval with host pointers)
+    # e2e through the public API, FP64: the density from pinned host memory in, dF to pinned
+    # host memory out, every step (cdft_set_density + cdft_eval with host pointers)
     host_rho = torch.from_numpy(rho.copy()).pin_memory()
     host_dF = torch.empty(rho.shape, dtype=torch.float64).pin_memory()
     K2 = max(5, args.steps // 2)
@@ -506,28 +577,55 @@ def main():
         c.set_density(host_rho)
         c.eval(dF_out=host_dF)
     e2e_s = (time.perf_counter() - t0) / K2
+    # the FP32-bulk evaluation of the same system, and its error against FP64 on the same density
+    t64, dF64 = c.eval()
+    c.set_precision(cd.FP32)
+    ms32 = timed(args.steps, max(3, args.warmup), lambda: c.eval(want_dF=False))
+    passes32 = c.time_passes(reps=5)
+    t32, dF32 = c.eval()
+    c.set_precision(cd.FP64)
+    fp32_err = {"omega_rel": abs(t32["Omega"] - t64["Omega"]) / abs(t64["Omega"]),
+                "dF_max_abs_over_max_dF64": float(np.abs(dF32 - dF64).max() / np.abs(dF64).max()),
+                "dF_max_abs_over_dV": float(np.abs(dF32 - dF64).max() / DX ** 3)}
     n_per_eval = 11  # kernels per evaluation: 9 passes, one finish of the sums, one finish of the residual norms
     peak, peak_kind = measured_peaks()
-    top = max(passes, key=lambda p: p["ms"])
-    achieved = top["bytes"] / (top["ms"] * 1e-3) / 1e9
+    fp64_peak = fp64_fma_peak(cd)
     N = int(np.prod(SHAPE))
     Nc = SHAPE[0] * SHAPE[1] * (SHAPE[2] // 2 + 1)
-    B_dft = 4 * (N * (4 * 11 + 3) + Nc * (2 * 11 + 11))
-    line = {"metric": METRIC, "value": world * 1e3 / ms32, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload(),
+    M = 11
+    B64 = 8 * (N * (4 * M + 3) + Nc * (2 * M + 11))
+    B32 = 4 * (N * (4 * M + 3) + Nc * (2 * M + 11))
+    top64 = max(passes64, key=lambda p: p["ms"])
+    top32 = max(passes32, key=lambda p: p["ms"])
+    ops = NCU_FP64_FLOPS.get(top64["pass"])
+    hbm64 = top64["bytes"] / (top64["ms"] * 1e-3) / 1e9  # the pass's algorithmic bytes at FP64 width
+    line = {"metric": METRIC, "value": world * 1e3 / ms64, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload(),
             "gpu_launches": n_per_eval * args.steps,
             "e2e": {"value": world / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(N * 8),
                     "d2h_bytes_per_step": int(N * 8 + 8 * 8)},
-            "roofline": {"bound": "hbm", "kernel": top["pass"], "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": NCU_TRAFFIC.get((top["pass"], "fp32"))},
-            "eval_roofline": {"algorithmic_bytes_per_eval": B_dft, "achieved_gbs": B_dft / (ms32 * 1e-3) / 1e9,
-                              "frac": B_dft / (ms32 * 1e-3) / 1e9 / peak},
-            "fp64_evals_per_s": world * 1e3 / ms64, "fp64_ms_per_step": ms64,
-            "passes": [{"pass": p["pass"], "ms": round(p["ms"], 5), "GBs": round(p["bytes"] / max(p["ms"], 1e-9) / 1e6, 1)}
-                       for p in passes],
+            "roofline": {"bound": "fp64", "kernel": top64["pass"] + " (FP64)",
+                         "achieved": (ops / (top64["ms"] * 1e-3) / 1e12) if ops else None,
+                         "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": (ops / (top64["ms"] * 1e-3) / 1e12 / fp64_peak) if (ops and fp64_peak) else None,
+                         "flops_per_launch": ops, "flops_source": "executed FP64 add/mul/fma (fma = 2) per launch, ncu",
+                         "peak_source": "measured in this run: cdft_fp64_fma_rate (independent FMA chains on every SM)",
+                         "traffic": NCU_TRAFFIC.get((top64["pass"], "fp64")),
+                         "hbm": {"achieved_gbs": hbm64, "peak_gbs": peak, "frac": hbm64 / peak, "peak_source": peak_kind}},
+            "eval_roofline": {"algorithmic_bytes_per_eval": B64, "achieved_gbs": B64 / (ms64 * 1e-3) / 1e9,
+                              "frac": B64 / (ms64 * 1e-3) / 1e9 / peak},
             "passes_fp64": [{"pass": p["pass"], "ms": round(p["ms"], 4)} for p in passes64],
+            "fp32": {"evals_per_s": world * 1e3 / ms32, "ms_per_step": ms32, "dtype": "f32 transforms, f64 reductions",
+                     "error_vs_fp64_same_density": fp32_err,
+                     "roofline": {"bound": "hbm", "kernel": top32["pass"],
+                                  "achieved": top32["bytes"] / (top32["ms"] * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                                  "frac": top32["bytes"] / (top32["ms"] * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
+                                  "traffic": NCU_TRAFFIC.get((top32["pass"], "fp32"))},
+                     "eval_roofline": {"algorithmic_bytes_per_eval": B32, "achieved_gbs": B32 / (ms32 * 1e-3) / 1e9,
+                                       "frac": B32 / (ms32 * 1e-3) / 1e9 / peak},
+                     "passes": [{"pass": p["pass"], "ms": round(p["ms"], 5),
+                                 "GBs": round(p["bytes"] / max(p["ms"], 1e-9) / 1e6, 1)} for p in passes32]},
             "clocks": clocks}
     if not args.no_batch:  # sharded over the ranks when there are several
         sweep = batch_leg(cd, n=args.sweep_points, grids=tuple(int(g) for g in args.sweep_grids.split(",")),
@@ -535,8 +633,9 @@ def main():
         if rank == 0:
             line["statepoint_sweep"] = sweep
     # the single-GPU legs below are reported by rank 0 only (the other replicas skip them)
+    kept = {}
     if rank == 0 and not args.no_fire:
-        line["fire_to_resid_1e-8"] = fire_legs(cd, rho, legs=tuple(args.fire_legs.split(",")))
+        line["fire_to_resid_1e-8"] = fire_legs(cd, rho, legs=tuple(args.fire_legs.split(",")), keep=kept)
     if rank == 0 and not args.no_ddft:
         line["eval_256"] = eval_256_leg(cd)
         line["ddft_256"] = ddft_leg(cd)
@@ -549,6 +648,8 @@ def main():
         line["cpu_baseline"] = {"value": rate, "unit": "evals/s", "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
                                 "sample": "%d FP64 F+dF evaluations of the same 128^3 system by the oracle in %.1f s" % (n, el)}
         fr = line.get("fire_to_resid_1e-8")
+        if fr and kept:  # the converged droplets checked by the oracle (FP64, CPU)
+            fr["oracle_pins"] = oracle_pins(kept)
         if fr and "plain_fp64" in fr:  # the CPU time to resid 1e-8, extrapolated: one FP64 evaluation per FIRE2 step
             steps = fr["plain_fp64"]["fire_steps"]
             fr["cpu_oracle_plain_fp64_extrapolated_s"] = steps / rate

@@ -36,7 +36,8 @@ C_FUNCTIONS = [
     "cdft_fire_run_batch", "cdft_autotune", "cdft_get_radices", "cdft_radix_candidates", "cdft_hessian_dot_v",
     "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex", "cdft_ddft_matrix_dot_v",
     "cdft_density_write", "cdft_density_read", "cdft_density_write_vtk", "cdft_log_det", "cdft_eigenvalue",
-    "cdft_arnoldi_largest", "cdft_set_boundary",
+    "cdft_arnoldi_largest", "cdft_set_boundary", "cdft_ddft_set_mass_restore", "cdft_ddft_mass_deviation",
+    "cdft_fp64_fma_rate",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -128,6 +129,8 @@ def lib():
             "cdft_fire_step": ([vp, i, P(FireReport)], i), "cdft_fire_run": ([vp, ctypes.c_long, P(FireReport)], i),
             "cdft_fire_run_to_residual": ([vp, d, ctypes.c_long, P(FireReport)], i),
             "cdft_ddft_init": ([vp, d, d, d], i), "cdft_ddft_step": ([vp, i, P(DdftReport)], i),
+            "cdft_ddft_set_mass_restore": ([vp, i], i), "cdft_ddft_mass_deviation": ([vp, dp], i),
+            "cdft_fp64_fma_rate": ([dp, vp], i),
             "cdft_time_passes": ([vp, i, dp, dp, P(i)], i),
             "cdft_fmt_weights": ([i, i, i, d, d, dp], i),
             "cdft_number_of_atoms_noalloc": ([vp, ctypes.c_long, d, vp, dp], i),
@@ -464,6 +467,18 @@ class Context:
         r = DdftReport()
         self._check(lib().cdft_ddft_step(self._h, n, ctypes.byref(r)))
         return self._rep(r)
+
+    def ddft_set_mass_restore(self, on):
+        """FP32 mode: keep (True, the default) or drop the uniform FP64 shift back to the
+        starting mass after each propagation."""
+        self._check(lib().cdft_ddft_set_mass_restore(self._h, int(bool(on))))
+
+    def ddft_mass_deviation(self):
+        """FP32 mode: the largest relative mass deviation of a propagated density from the
+        run's start, before any restore, since ddft_init."""
+        v = ctypes.c_double()
+        self._check(lib().cdft_ddft_mass_deviation(self._h, ctypes.byref(v)))
+        return v.value
 
 
 def _radices(r):

@@ -1257,7 +1257,20 @@ int cdft_ddft_init(cdft_ctx* c, double dt, double dt_max, double tol) {
   c->ddft_time = 0;
   c->ddft_successes = 0;
   c->ddft_have_factors = false;
+  c->ddft_max_dev = 0;
   c->ddft_ready = true;
+  return CDFT_OK;
+}
+
+int cdft_ddft_set_mass_restore(cdft_ctx* c, int on) {
+  if (!c) return CDFT_ERR_ARG;
+  c->ddft_restore = on != 0;
+  return CDFT_OK;
+}
+
+int cdft_ddft_mass_deviation(cdft_ctx* c, double* max_rel) {
+  if (!c || !max_rel) return CDFT_ERR_ARG;
+  *max_rel = c->ddft_max_dev;
   return CDFT_OK;
 }
 
@@ -1346,10 +1359,12 @@ static int ddft_one_step(cdft_ctx* c, int* restarts, bool dF_current) {
       if (c->precision == CDFT_FP32) {
         // FP32 transforms keep the k = 0 mode only to FP32 rounding: restore
         // the run's mass with a uniform FP64 shift (compensated FP64 sum).
+        // The deviation found before the shift is recorded either way.
         double m;
         rc = map_reduce<1, 0>(c, N, FSumRho{c->ddn}, &m);
         if (rc) return rc;
-        k_add_const<<<grid_for(N), 256, 0, c->stream>>>(c->ddn, N, (m - c->ddft_mass0) / (double)N);
+        if (c->ddft_mass0 != 0) c->ddft_max_dev = std::max(c->ddft_max_dev, std::fabs(m - c->ddft_mass0) / std::fabs(c->ddft_mass0));
+        if (c->ddft_restore) k_add_const<<<grid_for(N), 256, 0, c->stream>>>(c->ddn, N, (m - c->ddft_mass0) / (double)N);
       }
       if (c->fixed_bg)  // the boundary keeps the iterate's densities (src/DDFT.cpp:280-281)
         k_boundary_copy<<<grid_for(N), 256, 0, c->stream>>>(c->ddn, c->dd1, N, c->p.ny, c->p.nz);

@@ -51,6 +51,8 @@ struct cdft_ctx {
   bool ddft_ready = false;
   double ddft_dt = 0, ddft_dt_max = 1, ddft_tol = 1e-4, ddft_time = 0, ddft_rhs = 1;
   double ddft_mass0 = 0;  // sum rho of the run's start (FP32 mode restores it after each propagation)
+  bool ddft_restore = true;   // FP32 mode: shift each propagated density back to ddft_mass0
+  double ddft_max_dev = 0;    // FP32 mode: largest |sum rho - mass0| / mass0 of a propagation, before any restore
   bool ddft_have_factors = false;
   int ddft_successes = 0;
   double *dd0 = nullptr, *dd1 = nullptr, *ddn = nullptr, *dR = nullptr, *dfac = nullptr;

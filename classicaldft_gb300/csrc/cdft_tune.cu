@@ -190,3 +190,56 @@ extern "C" int cdft_radix_candidates(int n, int* out, int max_plans, int* count)
       for (int i = 0; i < 8; ++i) out[k * 8 + i] = i < (int)cand[k].size() ? cand[k][i] : 0;
   return CDFT_OK;
 }
+
+// ------------------------------------------------- FP64 pipe rate probe ---
+// Sustained FP64 FMA rate of the current device: every thread runs kChains
+// independent dependent-FMA chains (enough in flight to cover the pipe's
+// latency), the grid fills every SM several times over. The result is what an
+// FP64-bound pass can reach at best, the denominator of its roofline.
+namespace {
+constexpr int kChains = 8, kIters = 2048;
+__global__ void __launch_bounds__(256) k_fp64_fma_chains(double b, double c, double* __restrict__ sink) {
+  double a[kChains];
+#pragma unroll
+  for (int j = 0; j < kChains; ++j) a[j] = (double)(threadIdx.x + j) * 1e-3;
+  for (int i = 0; i < kIters; ++i)
+#pragma unroll
+    for (int j = 0; j < kChains; ++j) a[j] = fma(a[j], b, c);
+  double s = 0;
+#pragma unroll
+  for (int j = 0; j < kChains; ++j) s += a[j];
+  if (s == 12345.678) sink[0] = s;  // never true for these inputs: keeps the chains live
+}
+}  // namespace
+
+int cdft_fp64_fma_rate(double* tflops, void* stream) {
+  if (!tflops) return CDFT_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return CDFT_ERR_CUDA;
+  double* sink = nullptr;
+  if (cudaMalloc(&sink, sizeof(double)) != cudaSuccess) return CDFT_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const unsigned grid = (unsigned)sms * 16;
+  k_fp64_fma_chains<<<grid, 256, 0, s>>>(0.999999, 1e-7, sink);  // warm-up
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    cudaEventRecord(e0, s);
+    k_fp64_fma_chains<<<grid, 256, 0, s>>>(0.999999, 1e-7, sink);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  const cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (err != cudaSuccess) return CDFT_ERR_CUDA;
+  const double flops = 2.0 * kChains * kIters * (double)grid * 256;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return CDFT_OK;
+}

@@ -305,6 +305,10 @@ int cdft_get_radices(const cdft_ctx* ctx, int* radices_out);
 /* The orderings the autotuner tries for a transform length n (host only, no
  * GPU): count receives the number of plans; out (max_plans x 8 ints) the first ones. */
 int cdft_radix_candidates(int n, int* out, int max_plans, int* count);
+/* Measurement aid, no reference counterpart: the current device's sustained FP64
+ * FMA rate in TFLOP/s (independent FMA chains on every SM, best of five timed
+ * launches on `stream`), the ceiling of an FP64-bound pass. Allocates 8 bytes. */
+int cdft_fp64_fma_rate(double* tflops, void* stream);
 
 /* Newton-Krylov refinement of a minimum (no counterpart in the reference):
  * Newton corrections H d = -dF solved by preconditioned conjugate gradients
@@ -363,19 +367,31 @@ int cdft_ddft_init(cdft_ctx* ctx, double dt, double dt_max, double tol_fixed_poi
  * with, which the FP32 transforms keep only to ~1e-7 per step; CDFT_FP64 mode is
  * the reference's arithmetic unchanged. */
 int cdft_ddft_step(cdft_ctx* ctx, int nsteps, cdft_ddft_report* rep);
+/* CDFT_FP32 mode only: on != 0 (the default) keeps the mass restore described
+ * above; 0 leaves each propagated density as the FP32 transforms return it, so
+ * the run shows the propagator's own FP32 mass drift. No reference counterpart
+ * (the reference has no FP32 mode). */
+int cdft_ddft_set_mass_restore(cdft_ctx* ctx, int on);
+/* CDFT_FP32 mode: the largest relative deviation |sum rho - sum rho_0| / sum rho_0
+ * of a propagated density from the run's starting mass, measured before any
+ * restore, over every propagation since cdft_ddft_init (0 in CDFT_FP64 mode). */
+int cdft_ddft_mass_deviation(cdft_ctx* ctx, double* max_rel);
 
 /* Number of atoms, sum(rho) * dV with FP64 compensated summation, of a density
  * that is already on the device (rho: n doubles, a device pointer), written to
- * *out (host). Allocates nothing: for callers that cannot call cudaMalloc (an
- * application passing only pointers from its own memory pool, or code that must
- * not allocate between launches it records into a CUDA graph). No counterpart in
- * the reference. Its scratch is a 64 KiB file-scope device array that every GPU
- * loading this library holds until exit; n above 2^25 (33,554,432) points is
- * rejected with CDFT_ERR_ARG. The first call on a device resolves the array's
- * address there (make it before any stream capture). Calls share the array:
- * calls that overlap on the GPU race and must be serialised by the caller. The
- * work runs on `stream` (NULL: the legacy default stream), which is synchronised
- * before returning. */
+ * *out (host). Allocates nothing: for callers that cannot call cudaMalloc, such
+ * as an application that hands this library only device memory from its own
+ * pool (a cudaMalloc would draw memory outside that pool's budget and can
+ * synchronise the whole device under the application's other streams). No
+ * counterpart in the reference. Its scratch is a 64 KiB file-scope device array
+ * that every GPU loading this library holds until exit; n above 2^25
+ * (33,554,432) points is rejected with CDFT_ERR_ARG. The first call on a device
+ * resolves the array's address there with cudaGetSymbolAddress (make that first
+ * call before any stream capture); it is resolved again if the device's context
+ * has been replaced (cudaDeviceReset). Calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. The work runs on
+ * `stream` (NULL: the legacy default stream), which is synchronised before
+ * returning; the call reads and clears the runtime's last-error state. */
 int cdft_number_of_atoms_noalloc(const double* rho, long n, double dV, void* stream, double* out);
 
 #ifdef __cplusplus

@@ -3,7 +3,7 @@
 // Header-only. Code written against jimlutsko/classicalDFT's DFT / Species /
 // FMT / Interaction / Minimizer classes for the free-energy-and-derivative
 // path compiles against this header with the same class names and method
-// signatures (see INTEGRATION.md), and runs on the GPU through include/cdft.h
+// signatures, and runs on the GPU through include/cdft.h
 // (link with classicaldft_gb300/libcdft.so and the CUDA runtime).
 //
 // Covered: Lattice/Density (include/Lattice.h, include/Density.h), FMT models

@@ -80,7 +80,8 @@ def main():
         i = args.index("--cases")
         cases = args[i + 1].split(",")
         del args[i:i + 2]
-    ref = args[0] if args else "/root/reference"
+    # the reference checkout: the first argument, else $CDFT_REFERENCE_DIR, else its usual mount point
+    ref = args[0] if args else os.environ.get("CDFT_REFERENCE_DIR", "/root/reference")
     subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + ref])
     drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
     with tempfile.TemporaryDirectory() as tmp:  # FIRE writes snapshot files into the cwd

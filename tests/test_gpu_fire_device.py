@@ -67,6 +67,14 @@ def test_mixed_precision_reaches_fp64_minimum():
         res[mixed] = (t["Omega"], c.get_density(), r["total_steps"])
     assert abs(res[True][0] - res[False][0]) <= 1e-10 * abs(res[False][0])
     np.testing.assert_allclose(res[True][1], res[False][1], rtol=0, atol=1e-6)
+    # both minima checked by the FP64 oracle (the reference's arithmetic): Omega within
+    # 1e-10 relative and the oracle's own max|dOmega/drho| at most 1e-8 (+ the 1e-10 dF bar)
+    from oracle import pyoracle
+    o = pyoracle.Oracle(shape, dx, "WhiteBearI", hsd=hsd, lj=True, kT=0.8, fixed_mass=mass)
+    for mixed in (False, True):
+        _, t, dFo, _ = o.eval(res[mixed][1])
+        assert abs(res[mixed][0] - t["Omega"]) <= 1e-10 * abs(t["Omega"]), (mixed, res[mixed][0], t["Omega"])
+        assert np.abs(dFo).max() / dx ** 3 <= 1e-8 + 1e-10, (mixed, np.abs(dFo).max() / dx ** 3)
 
 
 def test_ddft_fp32_conserves_mass_and_tracks_fp64():
@@ -88,3 +96,36 @@ def test_ddft_fp32_conserves_mass_and_tracks_fp64():
     assert max(abs(m - m0) for m in m32) <= 1e-12 * m0
     assert max(abs(m - m0) for m in m64) <= 1e-12 * m0
     assert np.abs(d32 - d64).max() <= 1e-5
+
+
+def test_ddft_fp32_64cubed_tracks_fp64_50_steps():
+    """50 DDFT steps at 64^3 (dt = 1e-4, the LJ droplet functional) in FP32 bulk against
+    the FP64 step (the reference's arithmetic, pinned to it at 16^3): with the mass
+    restore the FP32 trajectory stays within 2e-5 of FP64 and keeps the mass to 1e-12;
+    without it the FP32 propagator's own drift is reported and stays below 1e-5."""
+    import classicaldft_gb300 as cd
+    from oracle import pyoracle
+    shape, dx = (64, 64, 64), 0.1
+    rho = pyoracle.fill_noise(shape, 0.3, 0.1, 64)
+    hsd = cd.bh_diameter(1, 1, 3, 0.8)
+    m0 = np.sum(rho) * dx ** 3
+    out = {}
+    for name, prec, restore in (("fp64", cd.FP64, True), ("fp32", cd.FP32, True), ("fp32_raw", cd.FP32, False)):
+        c = cd.Context(shape, dx, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.8, precision=prec)
+        c.set_chem_potential(c.bulk(0.3)["mu"])
+        c.set_density(rho)
+        c.ddft_init(1e-4, 1e-4)
+        c.ddft_set_mass_restore(restore)
+        r = c.ddft_step(50)
+        out[name] = (c.get_density(), r["mass"], c.ddft_mass_deviation(), r["time"])
+        c.close()
+    d64, m64, dev64, t64 = out["fp64"]
+    d32, m32, dev32, t32 = out["fp32"]
+    dr, mr, devr, tr = out["fp32_raw"]
+    assert t64 == t32 == tr
+    assert abs(m64 - m0) <= 1e-12 * m0 and dev64 == 0.0
+    assert abs(m32 - m0) <= 1e-12 * m0
+    assert 0.0 < dev32 <= 1e-5 and 0.0 < devr <= 1e-5
+    assert abs(mr - m0) <= 1e-5 * m0
+    assert np.abs(d32 - d64).max() <= 2e-5, np.abs(d32 - d64).max()
+    assert np.abs(dr - d64).max() <= 2e-5, np.abs(dr - d64).max()

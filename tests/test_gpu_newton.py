@@ -41,6 +41,17 @@ def test_mixed_newton_reaches_fp64_minimum(cd):
     assert abs(tb["Omega"] - ta["Omega"]) <= 1e-10 * abs(ta["Omega"])
     assert abs(tb["N"] - ta["N"]) <= 1e-12 * ta["N"]  # fixed mass kept
     np.testing.assert_allclose(b.get_density(), a.get_density(), rtol=0, atol=1e-6)
+    # both minima checked by the FP64 oracle: Omega within 1e-10 relative, its own
+    # max|dOmega/drho| at most 1e-8 (+ the 1e-10 dF bar)
+    from oracle import pyoracle
+    from classicaldft_gb300 import statepoints as sp
+    hsd = cd.bh_diameter(1.0, 1.0, 3.0, 0.8)
+    mass = float(sp.droplet((48,) * 3, 0.1, 0.02, 0.65, 1.6).sum() * 1e-3)
+    o = pyoracle.Oracle((48,) * 3, 0.1, "WhiteBearI", hsd=hsd, lj=True, kT=0.8, fixed_mass=mass)
+    for ctx, t in ((a, ta), (b, tb)):
+        _, to, dFo, _ = o.eval(ctx.get_density())
+        assert abs(t["Omega"] - to["Omega"]) <= 1e-10 * abs(to["Omega"]), (t["Omega"], to["Omega"])
+        assert np.abs(dFo).max() / 1e-3 <= 1e-8 + 1e-10
     a.close()
     b.close()
 
