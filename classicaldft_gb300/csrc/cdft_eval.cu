@@ -418,11 +418,11 @@ bool Evaluator<T>::setup_phi_tma() {
   bool ok = false;
   with_nf(fz_, [&](auto nf_) {
     constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
-    const int NP = (M_ + 1) / 2, L = NP * RB;
+    const int L = phi_lines(M_, RB, PhiCross<T>::value);
     uint64_t dims[3] = {(uint64_t)pz_ * E, (uint64_t)rows_, (uint64_t)M_};
     uint64_t str[2] = {(uint64_t)pz_ * cb, (uint64_t)Nc_ * cb};
     uint32_t box[3] = {(uint32_t)(pz_ * E), (uint32_t)RB, (uint32_t)M_};
-    smem_tphi_ = PhiBufs<T>::value * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L + 1) * cb) + 1024;
+    smem_tphi_ = PhiBufs<T>::value * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L | 1) * cb) + 1024;
     if (smem_tphi_ > 220 * 1024 || !encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) return;
     auto set_phi = [&](auto kern) {
       raise_smem(kern, smem_tphi_);

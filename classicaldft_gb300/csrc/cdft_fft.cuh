@@ -66,7 +66,8 @@ __device__ __forceinline__ void dft8(C* a) {
 
 // One radix-P butterfly of a Stockham stage: loads x[k + s*(q + m*j)],
 // applies the P-point DFT and the stage twiddles, stores y[k + s*(P*q + t)].
-template <int DIR, class T, int P>
+// UNIT: every stage twiddle is 1 (the last stage, m = 1): no products with them.
+template <int DIR, class T, int P, bool UNIT = false>
 __device__ __forceinline__ void butterfly(const typename Cx<T>::type* __restrict__ xl, typename Cx<T>::type* __restrict__ yl,
                                           int q, int k, int m, int s, const typename Cx<T>::type* __restrict__ tw,
                                           const typename Cx<T>::type* __restrict__ roots) {
@@ -98,7 +99,10 @@ __device__ __forceinline__ void butterfly(const typename Cx<T>::type* __restrict
   const C* twq = tw + q * P;
   yl[k + s * (P * q)] = a[0];
 #pragma unroll
-  for (int t = 1; t < P; ++t) yl[k + s * (P * q + t)] = cmul_dir<DIR>(a[t], __ldg(reinterpret_cast<const C*>(twq + t)));
+  for (int t = 1; t < P; ++t) {
+    if constexpr (UNIT) yl[k + s * (P * q + t)] = a[t];
+    else yl[k + s * (P * q + t)] = cmul_dir<DIR>(a[t], __ldg(reinterpret_cast<const C*>(twq + t)));
+  }
 }
 
 // Any other prime radix (up to kMaxRadix): direct DFT through local memory.
@@ -220,7 +224,7 @@ __device__ __forceinline__ typename Cx<T>::type* block_fft_fixed(typename Cx<T>:
       const int q = u / s, k = u - q * s;
       const C* xl = src + line * LP;
       C* yl = dst + line * LP;
-      if constexpr (p == 2 || p == 3 || p == 4 || p == 5 || p == 7 || p == 8) butterfly<DIR, T, p>(xl, yl, q, k, m, s, tw, rt);
+      if constexpr (p == 2 || p == 3 || p == 4 || p == 5 || p == 7 || p == 8) butterfly<DIR, T, p, m == 1>(xl, yl, q, k, m, s, tw, rt);
       else butterfly_generic<DIR, T>(xl, yl, q, k, m, s, p, tw, rt);
     }
     return block_fft_fixed<DIR, T, NF, ST + 1>(dst, src, L, LP, table);

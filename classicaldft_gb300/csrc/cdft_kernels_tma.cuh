@@ -15,7 +15,9 @@ namespace cdft {
 
 // Radix-P butterfly on column c of a row-major tile with TC columns.
 // TC here is the tile's row pitch in complex elements (>= the column count).
-template <int DIR, class T, int P, int TC>
+// UNIT: every stage twiddle is 1 (the last stage of a plan, m = 1, where q = 0):
+// the products with them are skipped, which leaves every value's bits unchanged.
+template <int DIR, class T, int P, int TC, bool UNIT = false>
 __device__ __forceinline__ void tile_butterfly(const typename Cx<T>::type* __restrict__ x, typename Cx<T>::type* __restrict__ y, int c,
                                                int q, int k, int m, int s, const typename Cx<T>::type* __restrict__ tw,
                                                const typename Cx<T>::type* __restrict__ roots) {
@@ -46,7 +48,10 @@ __device__ __forceinline__ void tile_butterfly(const typename Cx<T>::type* __res
   const C* twq = tw + q * P;
   y[(k + s * (P * q)) * TC + c] = a[0];
 #pragma unroll
-  for (int t = 1; t < P; ++t) y[(k + s * (P * q + t)) * TC + c] = cmul_dir<DIR>(a[t], __ldg(reinterpret_cast<const C*>(twq + t)));
+  for (int t = 1; t < P; ++t) {
+    if constexpr (UNIT) y[(k + s * (P * q + t)) * TC + c] = a[t];
+    else y[(k + s * (P * q + t)) * TC + c] = cmul_dir<DIR>(a[t], __ldg(reinterpret_cast<const C*>(twq + t)));
+  }
 }
 
 // Odd radices out of line: keeps their register arrays out of the kernels'
@@ -172,7 +177,7 @@ __device__ __forceinline__ void fx_stage(const typename Cx<T>::type* __restrict_
   for (int w = threadIdx.x; w < items; w += NTH) {
     const int c = w % TC, u = w / TC;
     const int q = u / s, k = u % s;
-    if constexpr (p == 2 || p == 4 || p == 8) tile_butterfly<DIR, T, p, PITCH>(src, dst, c, q, k, m, s, tw, rt);
+    if constexpr (p == 2 || p == 4 || p == 8) tile_butterfly<DIR, T, p, PITCH, m == 1>(src, dst, c, q, k, m, s, tw, rt);
     else if constexpr (p == 3 || p == 5 || p == 7) tile_butterfly_odd<DIR, T, p, PITCH>(src, dst, c, q, k, m, s, tw, rt);
     else tile_butterfly_generic<DIR, T, PITCH>(src, dst, c, q, k, m, s, p, tw, rt);
   }
@@ -294,7 +299,7 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
 // C[a] = IFFT_x(FFT_x(A) . w_a) for a < M. The density spectrum lives in
 // registers; weight tiles are double-buffered; results leave by tensor store.
 template <class T, int NF = 0>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xconv_tma(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW,
+__global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW,
                                                    const __grid_constant__ CUtensorMap mapC, int M, FFTPlan px,
                                                    const typename Cx<T>::type* __restrict__ tw, unsigned* __restrict__ status) {
   typedef typename Cx<T>::type C;
@@ -373,7 +378,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xconv_tma(const
 // double-buffered (spectrum tile + weight tile per stage), the sum lives in
 // registers. With the mean field, the Parseval sum for its energy goes to part.
 template <class T, int NF = 0>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xbackconv_tma(const __grid_constant__ CUtensorMap mapD, const __grid_constant__ CUtensorMap mapW,
+__global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant__ CUtensorMap mapD, const __grid_constant__ CUtensorMap mapW,
                                                        const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapWatt,
                                                        const __grid_constant__ CUtensorMap mapE, int M, int with_mf, Dims d, FFTPlan px,
                                                        const typename Cx<T>::type* __restrict__ tw, double* __restrict__ part,
@@ -473,8 +478,8 @@ namespace cdft {
 // tensor copy brings the group's M field rows ({pz*E, rows, M}, box
 // {pz*E, RB, M}) while an earlier group is computed (PhiBufs input buffers:
 // the next group's copy is issued as soon as a buffer has been unpacked). The M rows of a (x, y)
-// are paired into NP = ceil(M/2) complex lines; a group is a [nz][L] tile,
-// L = NP*RB lines, transformed column-wise (line-fastest, conflict-free):
+// are paired into complex lines (PhiPack); a group is a [nz][L] tile of L lines,
+// transformed column-wise (line-fastest, conflict-free):
 // c2r (z), Phi and dPhi per point, r2c (z), then the M derivative rows are
 // stored over the inputs.
 // threads per block of the fused Phi pass (512 threads with two blocks per SM
@@ -486,7 +491,42 @@ template <class T> struct PhiThreads { static constexpr int value = 256; };
 // FP32 that frees the shared memory for a third resident block per SM.
 template <class T> struct PhiBufs { static constexpr int value = sizeof(T) == 4 ? 1 : 2; };
 // minimum resident blocks the register allocation must allow
-template <class T> struct PhiMinBlocks { static constexpr int value = sizeof(T) == 4 ? 3 : 1; };
+template <class T> struct PhiMinBlocks { static constexpr int value = sizeof(T) == 4 ? 3 : 2; };
+
+// How a row group's M field rows share complex lines for the z transforms: two fields
+// per line (real part the even field a, imaginary part a + 1). With CROSS, M odd and RB
+// even, the last field of rows 2j and 2j + 1 shares one line (real part row 2j), so no
+// line is half empty: M = 11 takes 5 RB + RB / 2 lines instead of 6 RB. It pays in FP64,
+// where the FP64 pipe bounds the pass (1/12 fewer transforms); the FP32 pass is bound by
+// instruction issue and measured slower with the extra index work, so it keeps 6 RB.
+template <int M, int RB, bool CROSS = true> struct PhiPack {
+  static constexpr bool cross = CROSS && (M % 2 == 1) && (RB % 2 == 0);
+  static constexpr int per_row = cross ? M / 2 : (M + 1) / 2;  // lines holding fields of one row only
+  static constexpr int L = per_row * RB + (cross ? RB / 2 : 0);
+  // the line and the component (0 real, 1 imaginary) of field a of row r
+  __host__ __device__ static constexpr int line(int r, int a) { return (cross && a == M - 1) ? per_row * RB + r / 2 : r * per_row + a / 2; }
+  __host__ __device__ static constexpr int comp(int r, int a) { return (cross && a == M - 1) ? (r & 1) : (a & 1); }
+  // the field a (-1: none) and row r of a line's real (h = 0) or imaginary (h = 1) part
+  __host__ __device__ static constexpr void source(int l, int h, int& a, int& r) {
+    if (l < per_row * RB) {
+      r = l / per_row;
+      a = 2 * (l - r * per_row) + h;
+      if (a >= M) a = -1;
+    } else {
+      r = 2 * (l - per_row * RB) + h;
+      a = M - 1;
+    }
+  }
+};
+// PhiPack<M, RB, cross>::L for a runtime M (host side)
+inline int phi_lines(int M, int RB, bool cross) { return (cross && M % 2 == 1 && RB % 2 == 0) ? (M / 2) * RB + RB / 2 : ((M + 1) / 2) * RB; }
+// the Phi pass pairs across rows in FP64 only
+template <class T> struct PhiCross { static constexpr bool value = sizeof(T) == 8; };
+template <class T> __device__ __forceinline__ T cpart(const typename Cx<T>::type& z, int h) { return h ? z.y : z.x; }
+template <class T> __device__ __forceinline__ void set_cpart(typename Cx<T>::type* z, int h, T v) {
+  if (h) z->y = v;
+  else z->x = v;
+}
 
 // MODE selects what the pass does per point after the z c2r:
 //   kPhiEval  Phi and dPhi (the evaluation; Phi summed into part);
@@ -508,10 +548,10 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
                                                       T* __restrict__ NA = nullptr, T* __restrict__ XA = nullptr, T iph = 0, T iph2 = 0) {
   typedef typename Cx<T>::type C;
   constexpr int M = ModelTraits<MODEL>::M;
-  constexpr int NP = (M + 1) / 2;
+  typedef PhiPack<M, RB, PhiCross<T>::value> PK;
   const T ih = (T)(1.0 / (double)hsd), ih2 = (T)(1.0 / ((double)hsd * (double)hsd));
-  constexpr int L = NP * RB;
-  constexpr int LPd = L + 1;  // odd row pitch: the per-point loops stride rows without bank conflicts
+  constexpr int L = PK::L;
+  constexpr int LPd = L | 1;  // odd row pitch: the per-point loops stride rows without bank conflicts
   constexpr int E = ElemsPerComplex<T>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* sm = aligned_smem(smem_raw);
@@ -551,12 +591,14 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
     if (!__syncthreads_and(ok)) break;
     const long row0 = g * RB;
     const C* in = In[b];
-    // packed Hermitian spectra: line = r*NP + pair, element k of [nz][L]
+    // packed Hermitian spectra (PhiPack's lines), element k of [nz][L]
     for (int e = threadIdx.x; e < nz * L; e += blockDim.x) {
       const int line = e % L, k = e / L;
-      const int r = line / NP, pr = line - r * NP;
-      const C* Arow = in + ((size_t)(2 * pr) * RB + r) * pz;
-      const C* Brow = (2 * pr + 1 < M) ? in + ((size_t)(2 * pr + 1) * RB + r) * pz : nullptr;
+      int aA, rA, aB, rB;
+      PK::source(line, 0, aA, rA);
+      PK::source(line, 1, aB, rB);
+      const C* Arow = in + ((size_t)aA * RB + rA) * pz;
+      const C* Brow = aB >= 0 ? in + ((size_t)aB * RB + rB) * pz : nullptr;
       Z0[k * LPd + line] = pair_spectrum<T>(Arow, Brow, k, nz);
     }
     __syncthreads();
@@ -570,10 +612,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
         const int k = e % nz, r = e / nz;
         if (row0 + r >= d.rows) continue;
 #pragma unroll
-        for (int a = 0; a < M; ++a) {
-          const C z = res[k * LPd + r * NP + a / 2];
-          NA[(long)a * d.N + (row0 + r) * nz + k] = (a & 1) ? z.y : z.x;
-        }
+        for (int a = 0; a < M; ++a) NA[(long)a * d.N + (row0 + r) * nz + k] = cpart<T>(res[k * LPd + PK::line(r, a)], PK::comp(r, a));
       }
       __syncthreads();
       continue;
@@ -581,13 +620,14 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
     C* oth = (res == Z0) ? Z1 : Z0;
     for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
       const int k = e % nz, r = e / nz;
-      if (row0 + r >= d.rows) continue;
+      if (row0 + r >= d.rows) {  // a row past the end: zeros into its slots (a line may pair it with a live row)
+#pragma unroll
+        for (int a = 0; a < M; ++a) set_cpart<T>(&oth[k * LPd + PK::line(r, a)], PK::comp(r, a), (T)0);
+        continue;
+      }
       T nv[11];
 #pragma unroll
-      for (int a = 0; a < M; ++a) {
-        const C z = res[k * LPd + r * NP + a / 2];
-        nv[a] = (a & 1) ? z.y : z.x;
-      }
+      for (int a = 0; a < M; ++a) nv[a] = cpart<T>(res[k * LPd + PK::line(r, a)], PK::comp(r, a));
       if constexpr (MODE == kPhiHess) {
         T nd[11];
 #pragma unroll
@@ -611,18 +651,19 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
         }
       }
 #pragma unroll
-      for (int p = 0; p < NP; ++p) oth[k * LPd + r * NP + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
+      for (int p = 0; p < PK::per_row; ++p) oth[k * LPd + r * PK::per_row + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
+      if constexpr (PK::cross) set_cpart<T>(&oth[k * LPd + PK::line(r, M - 1)], PK::comp(r, M - 1), nv[M - 1]);
     }
     C* res2 = tfft<-1, T, L, LPd, NF, PhiThreads<T>::value>(oth, res, pz_plan, tw);
     for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
       const int k = e % nzc, line = e / nzc;
-      const int r = line / NP, pr = line - r * NP;
-      const long row = row0 + r;
-      if (row >= d.rows) continue;
+      int aA, rA, aB, rB;
+      PK::source(line, 0, aA, rA);
+      PK::source(line, 1, aB, rB);
       const C Z = res2[k * LPd + line];
       const C W = res2[(k == 0 ? 0 : nz - k) * LPd + line];
-      Cf[(long)(2 * pr) * d.Nc + row * pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
-      if (2 * pr + 1 < M) Cf[(long)(2 * pr + 1) * d.Nc + row * pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+      if (row0 + rA < d.rows) Cf[(long)aA * d.Nc + (row0 + rA) * pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
+      if (aB >= 0 && row0 + rB < d.rows) Cf[(long)aB * d.Nc + (row0 + rB) * pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
     }
     __syncthreads();
   }

@@ -26,12 +26,42 @@ template <> __device__ __forceinline__ double exp_t<double>(double x) { return e
 template <> __device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
 
 // f1, f2, f3 and first derivatives. Divisions are replaced by products with
-// g = 1/(1 - eta) and ie = 1/eta (two reciprocals per point): GB300 runs FP64
-// division as a long FP64 instruction sequence.
+// g = 1/(1 - eta) and ie = 1/eta: GB300 runs FP64 division as a long FP64
+// instruction sequence, so WhiteBear I and RSLT take both from one division.
 template <class T, int MODEL>
 __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, T& f3p) {
   const T one = (T)1;
   const T L = log1m<T>(e);
+  if (MODEL == MODEL_RSLT || MODEL == MODEL_WHITEBEAR_I) {
+    // one division for both reciprocals away from eta = 0: q = 1/(eta (1 - eta)),
+    // 1/(1 - eta) = eta q, 1/eta = (1 - eta) q
+    const T om = one - e;
+    T g, ie = 0;
+    const bool small = e < (T)1e-12;
+    if (small) {
+      g = one / om;
+    } else {
+      const T q = one / (e * om);
+      g = e * q;
+      ie = om * q;
+    }
+    f1 = L;
+    f1p = -g;
+    f2 = g;
+    f2p = g * g;
+    if (small) {
+      f3 = (T)1.5 + (T)(8.0 / 3) * e + (T)3.75 * e * e + (T)4.8 * e * e * e;
+      f3p = (T)(8.0 / 3) + (T)7.5 * e + (T)14.4 * e * e;
+    } else {
+      const T g2 = g * g;
+      f3 = ie * g2 + L * ie * ie;
+      if (MODEL == MODEL_RSLT)
+        f3p = -ie * ie * g2 * g * (e * e - (T)5 * e + (T)2) - (T)2 * ie * ie * ie * L;
+      else
+        f3p = (-(T)2 + (T)5 * e - e * e) * ie * ie * g2 * g - (T)2 * ie * ie * ie * L;
+    }
+    return;
+  }
   const T g = one / (one - e);
   f1 = L;
   f1p = -g;
@@ -50,24 +80,11 @@ __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, 
     }
     return;
   }
+  // Rosenfeld and esFMT
   f2 = g;
   f2p = g * g;
-  if (MODEL == MODEL_RSLT || MODEL == MODEL_WHITEBEAR_I) {
-    if (e < (T)1e-12) {
-      f3 = (T)1.5 + (T)(8.0 / 3) * e + (T)3.75 * e * e + (T)4.8 * e * e * e;
-      f3p = (T)(8.0 / 3) + (T)7.5 * e + (T)14.4 * e * e;
-    } else {
-      const T ie = one / e, g2 = g * g;
-      f3 = ie * g2 + L * ie * ie;
-      if (MODEL == MODEL_RSLT)
-        f3p = -ie * ie * g2 * g * (e * e - (T)5 * e + (T)2) - (T)2 * ie * ie * ie * L;
-      else
-        f3p = (-(T)2 + (T)5 * e - e * e) * ie * ie * g2 * g - (T)2 * ie * ie * ie * L;
-    }
-  } else {  // Rosenfeld and esFMT
-    f3 = g * g;
-    f3p = (T)2 * g * g * g;
-  }
+  f3 = g * g;
+  f3p = (T)2 * g * g * g;
 }
 
 // n[] holds the weighted densities in the order eta, s, v0, v1, v2, T00, T01,
@@ -100,17 +117,16 @@ __device__ __forceinline__ T fmt_phi_point(T* n, T ih, T ih2, T A, T B, T* ao = 
     T vT[3], TT[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) vT[i] = v2[0] * Tm[0][i] + v2[1] * Tm[1][i] + v2[2] * Tm[2][i];
+    // T is symmetric, so is T.T: its six distinct entries, mirrored
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) TT[i][j] = Tm[i][0] * Tm[0][j] + Tm[i][1] * Tm[1][j] + Tm[i][2] * Tm[2][j];
+      for (int j = i; j < 3; ++j) TT[i][j] = TT[j][i] = Tm[i][0] * Tm[0][j] + Tm[i][1] * Tm[1][j] + Tm[i][2] * Tm[2][j];
     const T vTv = v2[0] * vT[0] + v2[1] * vT[1] + v2[2] * vT[2];
     const T T2 = TT[0][0] + TT[1][1] + TT[2][2];
-    T T3 = 0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) T3 += TT[i][j] * Tm[j][i];
+    // tr(T^3) = sum_ij (T.T)_ij T_ij, the off-diagonal pairs counted twice
+    const T T3 = TT[0][0] * Tm[0][0] + TT[1][1] * Tm[1][1] + TT[2][2] * Tm[2][2] +
+                 (T)2 * (TT[0][1] * Tm[0][1] + TT[0][2] * Tm[0][2] + TT[1][2] * Tm[1][2]);
     const T a = (MODEL == MODEL_ESFMT) ? A : (T)1, b = (MODEL == MODEL_ESFMT) ? B : (T)-1;
     const T a24 = a * i_24pi, b24 = b * i_24pi;
     Phi3 = a24 * (s2 * s2 * s2 - (T)3 * s2 * v2_v2 + (T)3 * vTv - T3) + b24 * (s2 * s2 * s2 - (T)3 * s2 * T2 + (T)2 * T3);
