@@ -37,7 +37,7 @@ C_FUNCTIONS = [
     "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex", "cdft_ddft_matrix_dot_v",
     "cdft_density_write", "cdft_density_read", "cdft_density_write_vtk", "cdft_log_det", "cdft_eigenvalue",
     "cdft_arnoldi_largest", "cdft_set_boundary", "cdft_ddft_set_mass_restore", "cdft_ddft_mass_deviation",
-    "cdft_fp64_fma_rate",
+    "cdft_fp64_fma_rate", "cdft_arnoldi_largest_matrix",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -152,6 +152,7 @@ def lib():
             "cdft_log_det": ([vp, i, i, d, d, ctypes.c_long, i, i, dp, dp], i),
             "cdft_eigenvalue": ([vp, d, d, i, vp, vp, ctypes.c_long, dp, vp, i, P(EigenReport)], i),
             "cdft_arnoldi_largest": ([vp, d, i, i, i, ctypes.c_long, d, vp, dp, vp, i, P(EigenReport)], i),
+            "cdft_arnoldi_largest_matrix": ([vp, i, d, i, i, i, ctypes.c_long, d, vp, dp, vp, i, P(EigenReport)], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -434,16 +435,17 @@ class Context:
                                           vec.ctypes.data_as(ctypes.c_void_p), 0, ctypes.byref(r)))
         return val.value, vec, self._eigen_rep(r)
 
-    def arnoldi(self, shift, k, p, all_k=True, max_steps=1000, tol=1e-8, guess=None):
-        """Arnoldi(dft).determine_largest_eigenpairs(shift, k, p, all_k, max_steps, tol):
-        the k eigenpairs of H + shift of largest magnitude; returns (eigenvalues without
-        the shift, eigenvectors (k, *shape), report)."""
+    def arnoldi(self, shift, k, p, all_k=True, max_steps=1000, tol=1e-8, guess=None, matrix=MATRIX_HESSIAN):
+        """Arnoldi(matrix).determine_largest_eigenpairs(shift, k, p, all_k, max_steps, tol):
+        the k eigenpairs of M + shift of largest magnitude, M the Hessian (MATRIX_HESSIAN,
+        Arnoldi(dft)) or the DDFT dynamical matrix g.H (MATRIX_DDFT, Arnoldi(ddft));
+        returns (eigenvalues without the shift, unit eigenvectors (k, *shape), report)."""
         gs, gsp = self._host_vec(guess)
         vals = np.empty(k)
         vecs = np.empty((k,) + tuple(self.shape))
         r = EigenReport()
-        self._check(lib().cdft_arnoldi_largest(self._h, shift, k, p, int(all_k), max_steps, tol, gsp, _dptr(vals),
-                                               vecs.ctypes.data_as(ctypes.c_void_p), 0, ctypes.byref(r)))
+        self._check(lib().cdft_arnoldi_largest_matrix(self._h, matrix, shift, k, p, int(all_k), max_steps, tol, gsp, _dptr(vals),
+                                                      vecs.ctypes.data_as(ctypes.c_void_p), 0, ctypes.byref(r)))
         return vals, vecs, self._eigen_rep(r)
 
     # FFT plans

@@ -114,6 +114,51 @@ __global__ void __launch_bounds__(256) k_seed_vector(double* __restrict__ x, lon
   }
 }
 
+// The DDFT mobility of DDFT::g_dot_x (src/DDFT.cpp:320-351, forward differences) is
+// g = -C^T C, with C the edge-weighted difference operator on the 3N lattice edges
+// (p, p + e_ax): (C x)_(ax, p) = c (x[p + e_ax] - x[p]), c = sqrt(D (rho[p] + rho[p + e_ax])),
+// D = 1/(2 dx^2). Edge fields are stored axis-major, w[ax * N + p].
+__device__ __forceinline__ long sp_nb(long p, int ax, int dir, int nx, int ny, int nz) {
+  const int k = (int)(p % nz);
+  const long t = p / nz;
+  int j = (int)(t % ny), i = (int)(t / ny);
+  int kk = k;
+  if (ax == 0) i = (i + dir + nx) % nx;
+  else if (ax == 1) j = (j + dir + ny) % ny;
+  else kk = (k + dir + nz) % nz;
+  return kk + (long)nz * (j + (long)ny * i);
+}
+// w = s C x
+__global__ void __launch_bounds__(256) k_mob_c(const double* __restrict__ rho, const double* __restrict__ x, double* __restrict__ w, int nx,
+                                               int ny, int nz, double D, double s) {
+  const long N = (long)nx * ny * nz;
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256)
+    for (int ax = 0; ax < 3; ++ax) {
+      const long q = sp_nb(p, ax, 1, nx, ny, nz);
+      w[ax * N + p] = s * sqrt(D * (rho[p] + rho[q])) * (x[q] - x[p]);
+    }
+}
+// y = C^T w: y[p] = sum_ax c(p - e_ax, p) w[ax, p - e_ax] - c(p, p + e_ax) w[ax, p]
+__global__ void __launch_bounds__(256) k_mob_ct(const double* __restrict__ rho, const double* __restrict__ w, double* __restrict__ y, int nx,
+                                                int ny, int nz, double D) {
+  const long N = (long)nx * ny * nz;
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) {
+    double acc = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+      const long q = sp_nb(p, ax, 1, nx, ny, nz), m = sp_nb(p, ax, -1, nx, ny, nz);
+      acc += sqrt(D * (rho[m] + rho[p])) * w[ax * N + m] - sqrt(D * (rho[p] + rho[q])) * w[ax * N + p];
+    }
+    y[p] = acc;
+  }
+}
+// y = a x + b y
+__global__ void __launch_bounds__(256) k_axpby(double a, const double* __restrict__ x, double b, double* __restrict__ y, long N) {
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) y[p] = a * x[p] + b * y[p];
+}
+__global__ void __launch_bounds__(256) k_fill(double* __restrict__ y, double v, long N) {
+  for (long p = blockIdx.x * 256L + threadIdx.x; p < N; p += (long)gridDim.x * 256) y[p] = v;
+}
+
 // Chebyshev steps of Log_Det::calculate_log_det (src/Log_Det.cpp:113-144). r = M x
 // from the matrix pass; the matrix the estimator expands is A x = sg r + z sum(x)
 // (sg = -1 for a dynamic matrix, z = lam_mid / N when it has a zero eigenvalue).
@@ -358,6 +403,7 @@ struct SymOp {
   double *part, *sdot;
   bool prepared;
   long matvecs;
+  long n;  // vector length: N
   int apply(const double* x, double* y) {
     const long N = c->info.N;
     int rc = cdft_internal_matvec(c, CDFT_MATRIX_HESSIAN, x, y, !prepared);
@@ -366,6 +412,34 @@ struct SymOp {
     ++matvecs;
     if (vshift) dots(vshift, 1, x, N, part, sdot, c->stream);
     k_op_finish<<<sp_grid(N), 256, 0, c->stream>>>(y, x, vshift, sdot, a, 0.5 * a, shift, N);
+    return CDFT_OK;
+  }
+};
+
+// The symmetric operator behind the DDFT dynamical matrix g.H = -C^T C H: on 3N-vectors,
+// A w = -C H C^T w. For w in the range of C (where every Krylov vector started from C x0
+// stays), A has exactly the non-zero eigenvalues of g.H; an eigenvector w of A gives the
+// eigenvector C^T w of g.H. The shift is not applied here (components outside the range
+// of C, left by rounding, are annihilated by A instead of kept at the shift).
+struct MobOp {
+  cdft_ctx* c;
+  double shift;  // 0: the drivers rank by |theta + shift| outside the operator
+  double *part, *sdot;
+  bool prepared;
+  long matvecs;
+  long n;           // 3N
+  double *tN, *uN;  // N-vector work arrays
+  double D;
+  int apply(const double* w, double* y) {
+    const long N = c->info.N;
+    const unsigned g = sp_grid(N);
+    k_mob_ct<<<g, 256, 0, c->stream>>>(c->rho, w, tN, c->p.nx, c->p.ny, c->p.nz, D);
+    if (c->fixed_bg) cdft_internal_boundary_set(c, tN, 0.0);
+    int rc = cdft_internal_matvec(c, CDFT_MATRIX_HESSIAN, tN, uN, !prepared);
+    if (rc) return rc;
+    prepared = true;
+    ++matvecs;
+    k_mob_c<<<g, 256, 0, c->stream>>>(c->rho, uN, y, c->p.nx, c->p.ny, c->p.nz, D, -1.0);
     return CDFT_OK;
   }
 };
@@ -385,9 +459,13 @@ struct LanczosResult {
 // |residual| <= tol |theta - shift|, or (degenerate_rule) lies within tol of the first
 // discarded Ritz value (the stopping rule of src/Arnoldi.cpp:247-263). vecs (nev * N, device) receives the
 // Ritz vectors, unit norm.
-int lanczos(cdft_ctx* c, SymOp& op, Want want, int nev, int ncv, double tol, bool all, bool degenerate_rule, long max_matvecs,
-            int max_restarts, const double* x0, double* vecs, LanczosResult* out) {
-  const long N = c->info.N;
+// The eigenvalues are ranked by theta (Smallest) or by |theta + sel_shift| (LargestMagnitude).
+// drop_zero ranks Ritz values with |theta| <= 1e-10 max|theta| last: for MobOp those are
+// rounding residue outside the range of C (exact zeros of -C H C^T), not eigenvalues of g.H.
+template <class Op>
+int lanczos(cdft_ctx* c, Op& op, Want want, int nev, int ncv, double tol, bool all, bool degenerate_rule, long max_matvecs,
+            int max_restarts, const double* x0, double* vecs, LanczosResult* out, double sel_shift = 0.0, bool drop_zero = false) {
+  const long N = op.n;
   cudaStream_t s = c->stream;
   const unsigned g = sp_grid(N);
   DevBuf buf;
@@ -441,8 +519,11 @@ int lanczos(cdft_ctx* c, SymOp& op, Want want, int nev, int ncv, double tol, boo
     jacobi_eigen(Hm, m, theta, Z);
     std::vector<int> idx(m);
     for (int i = 0; i < m; ++i) idx[i] = i;
+    double tmax = 0;
+    for (int i = 0; i < m; ++i) tmax = std::max(tmax, std::fabs(theta[i]));
+    auto key = [&](int x) { return (drop_zero && std::fabs(theta[x]) <= 1e-10 * tmax) ? -1.0 : std::fabs(theta[x] + sel_shift); };
     std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
-      return want == Want::Smallest ? theta[x] < theta[y] : std::fabs(theta[x]) > std::fabs(theta[y]);
+      return want == Want::Smallest ? theta[x] < theta[y] : key(x) > key(y);
     });
     const int nw = std::min(nev, m);
     out->theta.assign(nw, 0.0);
@@ -517,7 +598,7 @@ int cdft_eigenvalue(cdft_ctx* c, double scale, double tol, int change_sign, cons
   int rc = start_vector(c, guess, on_device, 20240601, x0);
   if (rc) return rc;
   const double a = (change_sign ? -1.0 : 1.0) * scale;
-  SymOp op{c, a, 0.0, vs, nullptr, nullptr, false, 0};
+  SymOp op{c, a, 0.0, vs, nullptr, nullptr, false, 0, N};
   const int ncv = (int)std::min<long>(24, N);
   LanczosResult r;
   rc = lanczos(c, op, Want::Smallest, 1, ncv, tol, true, false, max_matvecs, 1 << 30, x0, vec, &r);
@@ -549,7 +630,7 @@ int cdft_arnoldi_largest(cdft_ctx* c, double shift, int k, int p, int all_k, lon
   if (!x0 || !vecs) return cdft_internal_fail(c, CDFT_ERR_CUDA, "arnoldi: out of device memory");
   int rc = start_vector(c, guess, on_device, 20240601, x0);
   if (rc) return rc;
-  SymOp op{c, 1.0, shift, nullptr, nullptr, nullptr, false, 0};
+  SymOp op{c, 1.0, shift, nullptr, nullptr, nullptr, false, 0, N};
   LanczosResult r;
   rc = lanczos(c, op, Want::LargestMagnitude, k, k + p, tol, all_k != 0, true, 1L << 62, (int)std::min<long>(max_steps, 1 << 30), x0,
                vecs, &r);
@@ -565,6 +646,125 @@ int cdft_arnoldi_largest(cdft_ctx* c, double shift, int k, int p, int all_k, lon
     rep->restarts = r.restarts;
     rep->converged = r.converged ? 1 : 0;
     rep->residual = r.resid.empty() ? 0 : r.resid[0];
+  }
+  if (!r.converged) return cdft_internal_fail(c, CDFT_ERR_TIMEOUT, "IRArnoldi method: Exceeded max iterations");
+  return CDFT_OK;
+}
+
+namespace {
+// The eigenvector of the zero eigenvalue of g.H on a periodic lattice: g 1 = 0, so
+// g.H x = 0 for H x = 1. Conjugate gradients on H (Hessian products; H is positive
+// definite at a stable state), then x / |x|. Returns whether the residual reached
+// 1e-10 |1|.
+int zero_mode_vector(cdft_ctx* c, double* x, bool* converged) {
+  const long N = c->info.N;
+  const unsigned g = sp_grid(N);
+  cudaStream_t s = c->stream;
+  DevBuf buf;
+  double *r = buf.get(N), *pv = buf.get(N), *q = buf.get(N), *part = buf.get(kDotBlocks), *dh = buf.get(2);
+  if (!r || !pv || !q || !part || !dh) return cdft_internal_fail(c, CDFT_ERR_CUDA, "arnoldi: out of device memory");
+  k_fill<<<g, 256, 0, s>>>(x, 0.0, N);
+  k_fill<<<g, 256, 0, s>>>(r, 1.0, N);
+  k_fill<<<g, 256, 0, s>>>(pv, 1.0, N);
+  double rr = (double)N, h[2];
+  const double stop = 1e-10 * std::sqrt((double)N);
+  *converged = false;
+  for (int it = 0; it < 4000; ++it) {
+    int rc = cdft_internal_matvec(c, CDFT_MATRIX_HESSIAN, pv, q, false);
+    if (rc) return rc;
+    dots(pv, 1, q, N, part, dh, s);
+    SP_CK(c, cudaMemcpyAsync(h, dh, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SP_CK(c, cudaStreamSynchronize(s));
+    if (!(h[0] > 0)) break;  // H not positive definite along pv: leave the current iterate
+    const double alpha = rr / h[0];
+    k_axpby<<<g, 256, 0, s>>>(alpha, pv, 1.0, x, N);
+    k_axpby<<<g, 256, 0, s>>>(-alpha, q, 1.0, r, N);
+    dots(r, 1, r, N, part, dh + 1, s);
+    SP_CK(c, cudaMemcpyAsync(h + 1, dh + 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SP_CK(c, cudaStreamSynchronize(s));
+    const double rr_new = h[1];
+    if (std::sqrt(rr_new) <= stop) {
+      *converged = true;
+      break;
+    }
+    k_axpby<<<g, 256, 0, s>>>(1.0, r, rr_new / rr, pv, N);
+    rr = rr_new;
+  }
+  dots(x, 1, x, N, part, dh, s);
+  k_normalise<<<g, 256, 0, s>>>(x, x, dh, N);
+  return CDFT_OK;
+}
+}  // namespace
+
+// Arnoldi::determine_largest_eigenpairs (src/Arnoldi.cpp:72-283) on either matrix of the
+// path: the Hessian (as cdft_arnoldi_largest), or the DDFT dynamical matrix g.H (DDFT is a
+// Dynamical_Matrix, include/Minimizer.h:189). For g.H the k eigenvalues of largest
+// |lambda + shift| come from thick-restart Lanczos on -C H C^T over the range of C
+// (MobOp), each eigenvector C^T w normalised, plus, on a periodic lattice, the zero
+// eigenvalue of the conserved mass with eigenvector H^-1 1 (zero_mode_vector).
+int cdft_arnoldi_largest_matrix(cdft_ctx* c, int matrix, double shift, int k, int p, int all_k, long max_steps, double tol,
+                                const double* guess, double* eigvals, double* eigvecs, int on_device, cdft_eigen_report* rep) {
+  if (matrix == CDFT_MATRIX_HESSIAN) return cdft_arnoldi_largest(c, shift, k, p, all_k, max_steps, tol, guess, eigvals, eigvecs, on_device, rep);
+  if (!c || !eigvals) return CDFT_ERR_ARG;
+  if (matrix != CDFT_MATRIX_DDFT) return cdft_internal_fail(c, CDFT_ERR_ARG, "arnoldi: matrix must be CDFT_MATRIX_HESSIAN or CDFT_MATRIX_DDFT");
+  const long N = c->info.N, n3 = 3 * N;
+  if (k < 1 || p < 1 || (long)k + p > N || max_steps < 1 || !(tol > 0))
+    return cdft_internal_fail(c, CDFT_ERR_ARG, "arnoldi: needs k >= 1, p >= 1, k + p <= N, max_steps >= 1 and tol > 0");
+  if (c->homo_bd) return cdft_internal_fail(c, CDFT_ERR_ARG, "arnoldi on the DDFT matrix: the homogeneous boundary is not built");
+  DevBuf buf;
+  double *x0 = buf.get(N), *w0 = buf.get(n3), *tN = buf.get(N), *uN = buf.get(N), *vecs3 = buf.get((size_t)k * n3),
+         *out = buf.get((size_t)k * N), *part = buf.get(kDotBlocks), *dh = buf.get(1);
+  if (!x0 || !w0 || !tN || !uN || !vecs3 || !out || !part || !dh) return cdft_internal_fail(c, CDFT_ERR_CUDA, "arnoldi: out of device memory");
+  int rc = start_vector(c, guess, on_device, 20240601, x0);
+  if (rc) return rc;
+  const double D = 1.0 / (2.0 * c->p.dx * c->p.dx);
+  const unsigned g = sp_grid(N);
+  k_mob_c<<<g, 256, 0, c->stream>>>(c->rho, x0, w0, c->p.nx, c->p.ny, c->p.nz, D, 1.0);  // start in the range of C
+  MobOp op{c, 0.0, nullptr, nullptr, false, 0, n3, tN, uN, D};
+  LanczosResult r;
+  rc = lanczos(c, op, Want::LargestMagnitude, k, k + p, tol, all_k != 0, true, 1L << 62, (int)std::min<long>(max_steps, 1 << 30), w0, vecs3,
+               &r, shift, true);
+  if (rc) return rc;
+  struct Cand {
+    double lam, res;
+    int src;  // Ritz pair index, or -1 for the zero mode
+  };
+  std::vector<Cand> cand;
+  double tmax = 0;
+  for (double t : r.theta) tmax = std::max(tmax, std::fabs(t));
+  for (int i = 0; i < (int)r.theta.size(); ++i)
+    if (std::fabs(r.theta[i]) > 1e-10 * tmax) cand.push_back({r.theta[i], r.resid[i], i});  // not residue outside range(C)
+  if (!c->fixed_bg) cand.push_back({0.0, 0.0, -1});
+  std::stable_sort(cand.begin(), cand.end(), [&](const Cand& a, const Cand& b) { return std::fabs(a.lam + shift) > std::fabs(b.lam + shift); });
+  bool zero_ok = true;
+  for (int i = 0; i < k; ++i) {
+    double* v = out + (long)i * N;
+    if (i >= (int)cand.size()) {
+      eigvals[i] = NAN;
+      k_fill<<<g, 256, 0, c->stream>>>(v, 0.0, N);
+      continue;
+    }
+    eigvals[i] = cand[i].lam;
+    if (cand[i].src >= 0) {
+      k_mob_ct<<<g, 256, 0, c->stream>>>(c->rho, vecs3 + (long)cand[i].src * n3, v, c->p.nx, c->p.ny, c->p.nz, D);
+      if (c->fixed_bg) cdft_internal_boundary_set(c, v, 0.0);
+      dots(v, 1, v, N, part, dh, c->stream);
+      k_normalise<<<g, 256, 0, c->stream>>>(v, v, dh, N);
+    } else {
+      rc = zero_mode_vector(c, v, &zero_ok);
+      if (rc) return rc;
+    }
+  }
+  if (eigvecs)
+    SP_CK(c, cudaMemcpyAsync(eigvecs, out, (size_t)k * N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             c->stream));
+  SP_CK(c, cudaStreamSynchronize(c->stream));
+  SP_CK(c, cudaGetLastError());
+  if (rep) {
+    rep->matvecs = op.matvecs;
+    rep->restarts = r.restarts;
+    rep->converged = (r.converged && zero_ok) ? 1 : 0;
+    rep->residual = cand.empty() ? 0 : cand[0].res;
   }
   if (!r.converged) return cdft_internal_fail(c, CDFT_ERR_TIMEOUT, "IRArnoldi method: Exceeded max iterations");
   return CDFT_OK;

@@ -176,6 +176,17 @@ int cdft_eigenvalue(cdft_ctx* ctx, double scale, double tol, int change_sign, co
  * here eigvals[i] is the i-th pair's own value. Hessian only. */
 int cdft_arnoldi_largest(cdft_ctx* ctx, double shift, int k, int p, int all_k, long max_steps, double tol, const double* guess,
                          double* eigvals, double* eigvecs, int on_device, cdft_eigen_report* rep);
+/* The same driver on either matrix of the path (Arnoldi takes any Dynamical_Matrix,
+ * include/Arnoldi.h:21; DDFT is one, include/Minimizer.h:189): CDFT_MATRIX_HESSIAN is
+ * cdft_arnoldi_largest; CDFT_MATRIX_DDFT gives the k eigenpairs of the DDFT matrix g.H
+ * (cdft_ddft_matrix_dot_v) of largest |lambda + shift|, eigvals without the shift, each
+ * eigenvector of unit norm (g.H is not symmetric: they are not orthogonal). Its spectrum
+ * is real (g = -C^T C, so g.H shares its non-zero eigenvalues with -C H C^T), plus, on a
+ * periodic lattice, the zero eigenvalue of the conserved mass (eigenvector H^-1 1, by
+ * conjugate gradients). rep->matvecs counts Hessian products. The homogeneous boundary is
+ * rejected (CDFT_ERR_ARG) for the DDFT matrix. */
+int cdft_arnoldi_largest_matrix(cdft_ctx* ctx, int matrix, double shift, int k, int p, int all_k, long max_steps, double tol,
+                                const double* guess, double* eigvals, double* eigvecs, int on_device, cdft_eigen_report* rep);
 
 /* Times each pass of one evaluation in the current precision with CUDA events
  * on the context's stream (no reference counterpart; used by the benchmark's

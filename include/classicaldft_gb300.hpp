@@ -371,6 +371,7 @@ class DDFT {
   double get_time() const { return r_.time; }
   double getTimeStep() const { return r_.dt > 0 ? r_.dt : dt_; }
   double get_convergence_monitor() const { return r_.rhs_max; }
+  DFT* dft() const { return dft_; }  // the system whose dynamical matrix g.H the spectral drivers take
 
  private:
   void start() {
@@ -446,7 +447,9 @@ class Eigenvalues {
 // include/Arnoldi.h:19-84 (src/Arnoldi.cpp) on the DFT's Hessian.
 class Arnoldi {
  public:
-  explicit Arnoldi(DFT& dft, bool verbose = false) : dft_(&dft) { (void)verbose; }
+  // Arnoldi(const Dynamical_Matrix&): the DFT's Hessian, or a DDFT's dynamical matrix g.H
+  explicit Arnoldi(DFT& dft, bool verbose = false) : dft_(&dft), matrix_(CDFT_MATRIX_HESSIAN) { (void)verbose; }
+  explicit Arnoldi(DDFT& ddft, bool verbose = false) : dft_(ddft.dft()), matrix_(CDFT_MATRIX_DDFT) { (void)verbose; }
   void set_initial_guess(const std::vector<double>& v) { guess_ = v; }
   void determine_largest_eigenpairs(double shift, int k, int p, bool compute_all_k_largest = true, long maxSteps = 1000000,
                                     double tol = 1e-8) {
@@ -456,8 +459,8 @@ class Arnoldi {
     vals_.assign(k, 0.0);
     vecs_.assign((size_t)k * N, 0.0);
     executed_ = true;
-    const int rc = cdft_arnoldi_largest(c, shift, k, p, compute_all_k_largest ? 1 : 0, maxSteps, tol,
-                                        guess_.size() == (size_t)N ? guess_.data() : nullptr, vals_.data(), vecs_.data(), 0, &rep_);
+    const int rc = cdft_arnoldi_largest_matrix(c, matrix_, shift, k, p, compute_all_k_largest ? 1 : 0, maxSteps, tol,
+                                               guess_.size() == (size_t)N ? guess_.data() : nullptr, vals_.data(), vecs_.data(), 0, &rep_);
     success_ = rc == CDFT_OK;
     check(rc, c);
   }
@@ -479,6 +482,7 @@ class Arnoldi {
 
  private:
   DFT* dft_;
+  int matrix_;
   std::vector<double> guess_, vals_, vecs_;
   cdft_eigen_report rep_{};
   bool executed_ = false, success_ = false;

@@ -636,6 +636,9 @@ int main(int argc, char** argv) {
       double var = 0;
       const double val = lg.calculate_log_det(4321, 2, true, var);
       put("sp16.logdet.ddft", {val, var});
+      // the dense DDFT dynamical matrix g.H (every column a DDFT::matrix_dot_v1), whose
+      // spectrum pins the eigen drivers on it (make_golden.py keeps its eigenvalues)
+      put("sp16.G", dense_matrix(ddft, N));
       System T = make_system(0.1, 16, "WhiteBearI", true, 0.8);
       fill_noise(*T.d, 0.3, 0.1, 5);
       T.s->setChemPotential(T.dft->mu_times_beta(0.3));

@@ -51,6 +51,22 @@ def spectral_post(arrays):
     (Eigenvalues::calculate_gradients, src/Eigenvalues.cpp) for a seeded vshift."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
+    # the DDFT dynamical matrix g.H: not symmetric, but similar to a symmetric matrix on
+    # the range of the mobility, so its eigenvalues are real; every eigenvalue (sorted),
+    # the largest imaginary part LAPACK leaves, and the unit eigenvectors of the two
+    # eigenvalues of largest magnitude
+    G = arrays.pop("sp16.G")
+    n = int(round(np.sqrt(G.size)))
+    G = G.reshape(n, n).T
+    w, V = np.linalg.eig(G)
+    order = np.argsort(w.real)
+    arrays["sp16.G.eig"] = w.real[order]
+    arrays["sp16.G.eig_imag_max"] = np.array([np.abs(w.imag).max()])
+    top = np.argsort(-np.abs(w.real))[:2]
+    for j, i in enumerate(top):
+        v = V[:, i].real
+        v = v / np.linalg.norm(v)
+        arrays["sp16.G.evec_top%d" % j] = v * np.sign(v[np.argmax(np.abs(v))])
     for tag in ("sp16", "splj16"):
         H = arrays.pop(tag + ".H")
         n = int(round(np.sqrt(H.size)))

@@ -202,3 +202,60 @@ def test_spectral_drivers_reject_ao(cd):
     with pytest.raises(cd.CDFTError):
         c.eigenvalue()
     c.close()
+
+
+def _ddft_residual(c, lam, y):
+    gy = c.ddft_matrix_dot_v(y)
+    return float(np.linalg.norm(gy.ravel() - lam * y.ravel()))
+
+
+def test_arnoldi_ddft_matrix_largest_pairs(cd, oracle):
+    """Arnoldi(ddft).determine_largest_eigenpairs(0, 4, 16) on the DDFT dynamical matrix
+    g.H of the hard-sphere state: the four eigenvalues of largest magnitude (the fastest
+    relaxing modes) of the reference's dense g.H (every column a DDFT::matrix_dot_v1,
+    eigenvalues by LAPACK), and unit eigenvectors with g.H y = lambda y."""
+    g = golden("spectral")
+    c = hs_context(cd, oracle)
+    vals, vecs, rep = c.arnoldi(0.0, 4, 16, tol=1e-9, matrix=cd.MATRIX_DDFT)
+    ref = g["sp16.G.eig"]
+    ref = ref[np.argsort(-np.abs(ref))][:4]
+    assert rep["converged"], rep
+    np.testing.assert_allclose(vals, ref, rtol=1e-9, atol=0)
+    for lam, y in zip(vals, vecs):
+        assert abs(np.linalg.norm(y) - 1) <= 1e-12
+        assert _ddft_residual(c, lam, y) <= 1e-7 * abs(lam)
+    # the isolated fastest mode: the reference's eigenvector, up to sign
+    assert abs(np.dot(vecs[0].ravel(), g["sp16.G.evec_top0"])) >= 1 - 1e-8
+    c.close()
+
+
+def test_arnoldi_ddft_matrix_shift_selects_slow_modes_and_mass_mode(cd, oracle):
+    """With shift = 2.5 the largest |lambda + shift| are the conserved-mass mode (lambda = 0,
+    eigenvector H^-1 1) and then the slowest relaxing modes of g.H, as in the reference's
+    spectrum."""
+    g = golden("spectral")
+    c = hs_context(cd, oracle)
+    vals, vecs, rep = c.arnoldi(2.5, 3, 20, tol=1e-9, matrix=cd.MATRIX_DDFT)
+    ref = g["sp16.G.eig"]
+    ref = ref[np.argsort(-np.abs(ref + 2.5))][:3]
+    assert rep["converged"], rep
+    assert vals[0] == 0.0 and abs(ref[0]) <= 1e-12
+    np.testing.assert_allclose(vals[1:], ref[1:], rtol=1e-9, atol=0)
+    assert _ddft_residual(c, 0.0, vecs[0]) <= 1e-9
+    for lam, y in zip(vals[1:], vecs[1:]):
+        assert _ddft_residual(c, lam, y) <= 1e-7 * abs(lam)
+    c.close()
+
+
+def test_arnoldi_ddft_matrix_fixed_background(cd, oracle):
+    """With a fixed background the boundary is held (g and H act on interior points only),
+    so there is no mass mode: every returned pair satisfies g.H y = lambda y with y zero on
+    the boundary planes."""
+    c = hs_context(cd, oracle)
+    c.set_boundary(fixed_background=True)
+    vals, vecs, rep = c.arnoldi(2.5, 2, 20, tol=1e-9, matrix=cd.MATRIX_DDFT)
+    assert rep["converged"] and np.all(vals < 0)
+    for lam, y in zip(vals, vecs):
+        assert np.abs(y[0, :, :]).max() == 0 and np.abs(y[:, 0, :]).max() == 0 and np.abs(y[:, :, 0]).max() == 0
+        assert _ddft_residual(c, lam, y) <= 1e-7 * abs(lam)
+    c.close()
