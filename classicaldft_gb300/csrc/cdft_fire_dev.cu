@@ -270,6 +270,37 @@ __global__ void k_zero_boundary(S* dF, long n, int ny, int nz, const FireState* 
     if (cdft_on_boundary(i, ny, nz)) dF[i] = (S)0;
 }
 
+// Species::endForceCalculation with a homogeneous boundary (src/Species.cpp:84-95): dF on
+// the boundary planes replaced by its mean over them (k_boundary_dF_sum, then the finished
+// sum in red[7], k_boundary_dF_fill); with fixed mass the sum dF . rho is then taken again
+// over the averaged dF (k_dF_rho_sum, red[7], k_mu_from_sum), as the host path does.
+template <class S>
+__global__ void __launch_bounds__(kThreads) k_boundary_dF_sum(const S* dF, long n, int ny, int nz, const FireState* st, double* part) {
+  if (st->skip || st->failed) return;
+  double acc[1] = {0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    if (cdft_on_boundary(i, ny, nz)) acc[0] += (double)dF[i];
+  block_sums_to<S>(acc, 1, part);
+}
+template <class S>
+__global__ void k_boundary_dF_fill(S* dF, long n, int ny, int nz, const FireState* st, double inv_nb) {
+  if (st->skip || st->failed) return;
+  const S m = (S)(st->red[7] * inv_nb);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    if (cdft_on_boundary(i, ny, nz)) dF[i] = m;
+}
+template <class S>
+__global__ void __launch_bounds__(kThreads) k_dF_rho_sum(const S* dF, const S* rho, long n, const FireState* st, double* part) {
+  if (st->skip || st->failed) return;
+  double acc[1] = {0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) acc[0] += (double)dF[i] * (double)rho[i];
+  block_sums_to<S>(acc, 1, part);
+}
+__global__ void k_mu_from_sum(FireState* st, FireConsts k) {
+  if (st->skip || st->failed) return;
+  st->mu = st->red[7] / k.fixed_mass;
+}
+
 // Minimizer::getDF_DX after the evaluation (src/Minimizer.cpp:90-115): alias
 // derivative into g of the pending state; sums v.g; maxima |dF|, |g|.
 template <class S>
@@ -417,6 +448,16 @@ static void record_step(cdft_ctx* c, FireDevEngine* E, Evaluator<T>* ev, S* x[2]
   }
   ev->template launch<S>(rho, c->vext, dF, c->info.dV, mu_eval, 1, s, nullptr);
   k_eval_finish<<<1, 1, 0, s>>>(ev->dev_terms(), ev->dev_status(), E->st, k, mu_eval, ev->M() > 0 ? 1 : 0, ev->has_mf() ? 1 : 0);
+  if (c->homo_bd) {
+    k_boundary_dF_sum<S><<<gn, kThreads, 0, s>>>(dF, N, c->p.ny, c->p.nz, E->st, E->part);
+    k_fire_sum_finish<<<1, 256, 0, s>>>(E->part, (int)gn, 0, 1, E->st, 7);
+    k_boundary_dF_fill<S><<<gn, kThreads, 0, s>>>(dF, N, c->p.ny, c->p.nz, E->st, 1.0 / (double)cdft_n_boundary(c->p.nx, c->p.ny, c->p.nz));
+    if (c->fixed_mass > 0) {
+      k_dF_rho_sum<S><<<gn, kThreads, 0, s>>>(dF, rho, N, E->st, E->part);
+      k_fire_sum_finish<<<1, 256, 0, s>>>(E->part, (int)gn, 0, 1, E->st, 7);
+      k_mu_from_sum<<<1, 1, 0, s>>>(E->st, k);
+    }
+  }
   if (c->fixed_mass > 0) k_sub_mu<S><<<gn, kThreads, 0, s>>>(dF, N, E->st, k);
   if (c->fixed_bg) k_zero_boundary<S><<<gn, kThreads, 0, s>>>(dF, N, c->p.ny, c->p.nz, E->st);
   k_fire_post<S><<<gn, kThreads, 0, s>>>(dF, x[0], x[1], v[0], v[1], g[0], g[1], E->st, N, k, E->part);
@@ -630,8 +671,7 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
   if (!c->fire_ready) return cdft_internal_fail(c, CDFT_ERR_STATE, "cdft_fire_init has not been called");
   if (mixed < 0 || mixed > 3) return cdft_internal_fail(c, CDFT_ERR_ARG, "mixed must be 0, 1, 2 or 3");
   if (mixed >= 2 && c->p.ao_rp > 0) mixed = 1;  // no Hessian products for the AO model: the FIRE2 policy
-  if (c->homo_bd) return cdft_internal_fail(c, CDFT_ERR_ARG, "the homogeneous boundary is built for the host-stepped FIRE2 calls only");
-  if (mixed >= 2 && c->fixed_bg) mixed = 1;  // Newton-Krylov is not built for a fixed background
+  if (mixed >= 2 && c->homo_bd) mixed = 1;  // Newton-Krylov is not built for the homogeneous boundary: the FIRE2 policy
   int rc = ensure_engine(c);
   if (rc) return rc;
   long total = 0, taken = 0, steps32 = 0;
@@ -797,7 +837,8 @@ extern "C" int cdft_fire_run_batch(cdft_ctx* const* ctx, int n, double resid_tol
     for (int j = 0; j < i; ++j)
       if (ctx[j] == ctx[i]) return cdft_internal_fail(ctx[i], CDFT_ERR_ARG, "a context appears twice in the batch");
     if (!ctx[i]->fire_ready) return cdft_internal_fail(ctx[i], CDFT_ERR_STATE, "cdft_fire_init has not been called");
-    if (ctx[i]->fixed_bg || ctx[i]->homo_bd) return cdft_internal_fail(ctx[i], CDFT_ERR_ARG, "the batched driver is not built for boundary modes");
+    // Newton-Krylov is not built for the homogeneous boundary: such a batch takes the FIRE2 policy
+    if (mixed >= 2 && ctx[i]->homo_bd) mixed = 1;
   }
   if (mixed == 3) return batch_newton(ctx, n, resid_tol, switch_tol, max_steps, reps, rcs);
   // allocation first (nothing may allocate while a stream is captured), and

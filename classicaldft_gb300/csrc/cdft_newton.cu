@@ -117,6 +117,12 @@ __global__ void __launch_bounds__(kT) k_nk_loss(const double* rho, const float* 
     part[blockIdx.x] = (double)x;
   }
 }
+// a fixed background holds the boundary planes (Species::setFixedBackground): the
+// correction lives on the interior, so each Hessian product's boundary rows are zeroed
+__global__ void k_nk_zero_boundary(float* q, long n, int ny, int nz) {
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT)
+    if (cdft_on_boundary(i, ny, nz)) q[i] = 0.f;
+}
 __global__ void k_nk_step(double* rho, const double* rho0, const float* dl, long n, double s) {
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < n; i += (long)gridDim.x * kT) rho[i] = rho0[i] + s * (double)dl[i];
 }
@@ -247,6 +253,7 @@ struct NewtonWork {
   CgDev* hcg = nullptr;     // pinned copy
   cudaGraphExec_t cg_exec = nullptr;
   unsigned cg_plan_gen = ~0u;
+  int cg_fixed_bg = -1;  // the boundary mode the graph was built for
   cudaStream_t cg_stream = nullptr;  // capture stream of the CG graph
   bool cg_ok = true;                 // false: the graph could not be built; host-driven CG
   ~NewtonWork() {
@@ -292,7 +299,7 @@ int cdft_internal_newton_ensure(cdft_ctx* c) {
 // Builds (once per set of transform plans) the graph of the device-driven CG loop.
 static bool build_cg_graph(cdft_ctx* c) {
   NewtonWork* W = c->newton;
-  if (W->cg_exec && W->cg_plan_gen == c->plan_gen) return true;
+  if (W->cg_exec && W->cg_plan_gen == c->plan_gen && W->cg_fixed_bg == c->fixed_bg) return true;
   if (W->cg_exec) cudaGraphExecDestroy(W->cg_exec);
   W->cg_exec = nullptr;
   const long N = c->info.N;
@@ -317,6 +324,7 @@ static bool build_cg_graph(cdft_ctx* c) {
     ok = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if (ok) {
       bool launch_ok = c->e32->hess_apply<float>(W->p, c->rho, W->q, dV, s) == 0;
+      if (c->fixed_bg) k_nk_zero_boundary<<<g, kT, 0, s>>>(W->q, N, c->p.ny, c->p.nz);
       k_nk_pq<<<g, kT, 0, s>>>(W->p, W->q, N, W->part);
       k_cg_fin_pq<<<1, 256, 0, s>>>(W->part, (int)g, W->cg);
       k_cg_update<<<g, kT, 0, s>>>(W->dl, W->r, W->p, W->q, N, W->cg);
@@ -338,6 +346,7 @@ static bool build_cg_graph(cdft_ctx* c) {
     return false;
   }
   W->cg_plan_gen = c->plan_gen;
+  W->cg_fixed_bg = c->fixed_bg;
   return true;
 }
 
@@ -376,7 +385,7 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
 extern "C" int cdft_newton_refine_ex(cdft_ctx* c, double tol, const cdft_newton_params* prm, cdft_newton_report* rep) {
   if (!c || !prm) return CDFT_ERR_ARG;
   if (c->p.ao_rp > 0) return cdft_internal_fail(c, CDFT_ERR_ARG, "Newton-Krylov needs Hessian products, which are not built for the AO model");
-  if (c->fixed_bg || c->homo_bd) return cdft_internal_fail(c, CDFT_ERR_ARG, "Newton-Krylov is not built for boundary modes");
+  if (c->homo_bd) return cdft_internal_fail(c, CDFT_ERR_ARG, "Newton-Krylov is not built for the homogeneous boundary");
   const int max_newton = prm->max_newton, max_cg = prm->max_cg;
   const double cg_rtol = prm->cg_rtol, eta_max = prm->eta_max, fp32_above = prm->fp32_above;
   if (!(tol > 0) || max_newton <= 0 || max_cg <= 0 || !(cg_rtol > 0) || !(eta_max >= 0) || !(fp32_above >= 0)) return CDFT_ERR_ARG;
@@ -457,6 +466,7 @@ extern "C" int cdft_newton_refine_ex(cdft_ctx* c, double tol, const cdft_newton_
     }
     for (; !max_cg_done && it < max_cg; ++it) {
       if (c->e32->hess_apply<float>(W->p, c->rho, W->q, dV, s)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Hessian product failed");
+      if (c->fixed_bg) k_nk_zero_boundary<<<g, kT, 0, s>>>(W->q, N, c->p.ny, c->p.nz);
       k_nk_pq<<<g, kT, 0, s>>>(W->p, W->q, N, W->part);
       double pq[2];
       if (!sums<2>(c, g, pq)) return cdft_internal_fail(c, CDFT_ERR_CUDA, "Newton reduction");

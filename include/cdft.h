@@ -98,10 +98,11 @@ int cdft_get_chem_potential(const cdft_ctx* ctx, double* mu);
  * is zero there and the boundary densities stay as they are (src/DDFT.cpp:280-281).
  * homogeneous = 1: dF on the boundary is replaced by its mean over the boundary
  * (src/Species.cpp:84-95). A fixed background with a fixed mass makes the next
- * evaluation fail with CDFT_ERR_ARG (the reference throws). Not built with either mode:
- * the batched driver, Newton-Krylov (cdft_fire_run_device takes its FIRE2 policy), and
- * the homogeneous mode in cdft_fire_run_device (CDFT_ERR_ARG; the host-stepped FIRE2
- * calls take both modes). */
+ * evaluation fail with CDFT_ERR_ARG (the reference throws). Every FIRE2 call (host-stepped,
+ * device-resident, batched) and the DDFT step take both modes; Newton-Krylov takes the
+ * fixed background (its corrections live on the interior points) but not the homogeneous
+ * boundary (cdft_newton_refine returns CDFT_ERR_ARG; cdft_fire_run_device and
+ * cdft_fire_run_batch take the FIRE2 policy, mixed = 1, instead of 2 or 3). */
 int cdft_set_boundary(cdft_ctx* ctx, int fixed_background, int homogeneous);
 
 /* DFT::calculateFreeEnergyAndDerivatives(onlyFex) (include/DFT.h:77, src/DFT.cpp:360-425);

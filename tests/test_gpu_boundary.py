@@ -28,9 +28,9 @@ def boundary_mask():
     return ((i == 0) | (j == 0) | (k == 0)).ravel()
 
 
-def context(cd, oracle, fixed=False, homo=False, precision="FP64"):
+def context(cd, oracle, fixed=False, homo=False, precision="FP64", seed=11):
     c = cd.Context(SHAPE, 0.2, cd.WHITEBEAR_I, hsd=1.0, precision=getattr(cd, precision))
-    c.set_density(oracle.fill_noise(SHAPE, 0.6, 0.2, 11))
+    c.set_density(oracle.fill_noise(SHAPE, 0.6, 0.2, seed))
     c.set_chem_potential(c.bulk(0.6)["mu"])
     c.set_boundary(fixed_background=fixed, homogeneous=homo)
     return c
@@ -148,9 +148,77 @@ def test_ddft_with_boundary_mode(cd, oracle, tag, fixed):
     c.close()
 
 
+@pytest.mark.parametrize("fixed_mass", [False, True])
+def test_device_fire_with_homogeneous_boundary_matches_host_steps(cd, oracle, fixed_mass):
+    """The homogeneous boundary in the device-resident FIRE2 step (the boundary mean of dF,
+    then, at fixed mass, mu from sum dF . rho over the averaged dF) against the host-stepped
+    FIRE2, whose evaluation follows Species::endForceCalculation (pinned by the bhom and
+    bhomfm goldens): the same dt and alpha after 30 steps, F and the density to roundoff."""
+    g = golden("boundary")
+    runs = []
+    for device in (False, True):
+        c = context(cd, oracle, homo=True)
+        if fixed_mass:
+            c.set_fixed_mass(float(g["bhomfm.fixed_mass"][0]))
+        c.fire_init(force_limit=0.0)
+        r = c.fire_run_device(0.0, max_steps=30) if device else c.fire_step(30)
+        runs.append((r, c.get_density()))
+        c.close()
+    (rh, dh), (rd, dd) = runs
+    assert rh["dt"] == rd["dt"] and rh["alpha"] == rd["alpha"]
+    assert abs(rh["F"] - rd["F"]) <= 1e-12 * abs(rh["F"])
+    np.testing.assert_allclose(dd, dh, rtol=1e-11, atol=0)
+
+
+def test_newton_with_fixed_background(cd, oracle):
+    """Newton-Krylov (mixed = 3) with a fixed background: the correction lives on the
+    interior, the boundary densities stay, and it reaches the minimum plain FP64 FIRE2
+    finds (Omega within 1e-10, max|dOmega/drho| <= 1e-8)."""
+    res = {}
+    rho0 = oracle.fill_noise(SHAPE, 0.6, 0.2, 11).ravel()
+    for mixed in (0, 3):
+        c = context(cd, oracle, fixed=True)
+        c.fire_init(force_limit=0.0)
+        r = c.fire_run_device(1e-8, max_steps=40000, mixed=mixed)
+        t, _ = c.eval(want_dF=False)
+        assert t["resid"] <= 1e-8, (mixed, r, t["resid"])
+        rho = c.get_density().ravel()
+        np.testing.assert_allclose(rho[boundary_mask()], rho0[boundary_mask()], rtol=1e-13, atol=0)
+        res[mixed] = (t["Omega"], rho, r)
+        c.close()
+    assert res[3][2]["newton"] >= 1
+    assert abs(res[3][0] - res[0][0]) <= 1e-10 * abs(res[0][0])
+    np.testing.assert_allclose(res[3][1], res[0][1], rtol=0, atol=1e-6)
+
+
+def test_batch_with_boundary_modes(cd, oracle):
+    """The batched driver takes contexts with boundary modes: two fixed-background contexts
+    under Newton-Krylov (mixed = 3), and a homogeneous-boundary one, for which the batch
+    takes the FIRE2 policy (mixed = 1); each reaches the state it reaches alone with the
+    same settings (with a homogeneous boundary only the boundary mean of dF vanishes, so the
+    end state depends on the path, and the two runs must take the same one)."""
+    for modes, mixed_alone in (((dict(fixed=True, seed=11), dict(fixed=True, seed=12)), 3), ((dict(homo=True, seed=11),), 1)):
+        ctxs = [context(cd, oracle, **m) for m in modes]
+        for c in ctxs:
+            c.fire_init(force_limit=0.0)
+        reps, status = cd.fire_run_batch(ctxs, 1e-8, max_steps=40000, mixed=3, switch_tol=1e-4)
+        assert not any(status), (status, reps)
+        batched = [c.eval(want_dF=False)[0] for c in ctxs]
+        for c in ctxs:
+            c.close()
+        for m, b in zip(modes, batched):
+            c = context(cd, oracle, **m)
+            c.fire_init(force_limit=0.0)
+            c.fire_run_device(1e-8, max_steps=40000, mixed=mixed_alone, switch_tol=1e-4)
+            a = c.eval(want_dF=False)[0]
+            c.close()
+            assert b["resid"] <= 1e-8 and a["resid"] <= 1e-8, (m, b["resid"], a["resid"])
+            assert abs(b["Omega"] - a["Omega"]) <= 1e-10 * abs(a["Omega"])
+
+
 def test_boundary_modes_report_what_is_not_built(cd, oracle):
     c = context(cd, oracle, homo=True)
-    c.fire_init(force_limit=0.0)
-    with pytest.raises(cd.CDFTError):
-        c.fire_run_device(1e-8, max_steps=10)
+    with pytest.raises(cd.CDFTError) as e:
+        c.newton_refine(1e-8)
+    assert e.value.code == cd.ERR_ARG
     c.close()
