@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdint>
 #include <memory>
 #include <string>
 #include <vector>
@@ -1055,17 +1056,24 @@ extern "C++" int cdft_internal_fire_resync(cdft_ctx* c) {
   return fire_accept(c, k);
 }
 
-int cdft_fire_init(cdft_ctx* c, const cdft_fire_params* p) {
-  if (!c) return CDFT_ERR_ARG;
-  cdft_fire_params d;
-  cdft_fire_default_params(&d);
-  c->fp = p ? *p : d;
+static int fire_buffers(cdft_ctx* c) {
   const long N = c->info.N;
   for (int i = 0; i < 2; ++i) {
     if (!c->fx[i]) CUDA_OR_FAIL(c, cudaMalloc(&c->fx[i], N * sizeof(double)));
     if (!c->fv[i]) CUDA_OR_FAIL(c, cudaMalloc(&c->fv[i], N * sizeof(double)));
     if (!c->fg[i]) CUDA_OR_FAIL(c, cudaMalloc(&c->fg[i], N * sizeof(double)));
   }
+  return CDFT_OK;
+}
+
+int cdft_fire_init(cdft_ctx* c, const cdft_fire_params* p) {
+  if (!c) return CDFT_ERR_ARG;
+  cdft_fire_params d;
+  cdft_fire_default_params(&d);
+  c->fp = p ? *p : d;
+  const long N = c->info.N;
+  int rc0 = fire_buffers(c);
+  if (rc0) return rc0;
   c->cur = 0;
   const Alias a = c->alias();
   // Minimizer::Minimizer: x = alias(rho); fireMinimizer2: F = getDF_DX(), v = 0
@@ -1087,6 +1095,93 @@ int cdft_fire_init(cdft_ctx* c, const cdft_fire_params* p) {
   c->Npos = c->Nneg = c->backtracks = 0;
   c->it = 0;
   c->fire_steps = 0;
+  c->fire_ready = true;
+  return CDFT_OK;
+}
+
+// FIRE2 state on disk: the minimizer the reference serialises with Boost
+// (fireMinimizer2::serialize, include/Minimizer.h:145-180: the alias coordinates x of
+// Minimizer, v, the step parameters and counters), here as raw native doubles behind a
+// small header: "CDFTFIR1", int64 N, int32 nx ny nz 0, the parameters (8 doubles, 3 int32
+// and one pad), the state (10 doubles: F dt dt_max alpha vv dt_best fmax resid vdotf mu;
+// int32 Npos Nneg backtracks it; int64 steps calls), then rho, x, v (N doubles each).
+namespace {
+const char kFireMagic[8] = {'C', 'D', 'F', 'T', 'F', 'I', 'R', '1'};
+struct FireFileHead {
+  char magic[8];
+  int64_t N;
+  int32_t nx, ny, nz, pad0;
+  double prm_d[8];  // dt dt_max dt_min alpha_start f_alf f_dec f_inc force_limit
+  int32_t prm_i[4];  // n_delay n_p_negative_max initial_delay 0
+  double st_d[10];
+  int32_t st_i[4];
+  int64_t st_l[2];
+};
+}  // namespace
+
+int cdft_fire_save(cdft_ctx* c, const char* path) {
+  if (!c || !path) return CDFT_ERR_ARG;
+  if (!c->fire_ready) return fail(c, CDFT_ERR_STATE, "cdft_fire_init has not been called");
+  const long N = c->info.N;
+  FireFileHead h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, kFireMagic, 8);
+  h.N = N; h.nx = c->p.nx; h.ny = c->p.ny; h.nz = c->p.nz;
+  const cdft_fire_params& q = c->fp;
+  const double pd[8] = {q.dt, q.dt_max, q.dt_min, q.alpha_start, q.f_alf, q.f_dec, q.f_inc, q.force_limit};
+  std::memcpy(h.prm_d, pd, sizeof(pd));
+  h.prm_i[0] = q.n_delay; h.prm_i[1] = q.n_p_negative_max; h.prm_i[2] = q.initial_delay;
+  const double sd[10] = {c->F, c->dt, c->dt_max, c->alpha, c->vv, c->dt_best, c->fmax, c->resid, c->vdotf, c->mu};
+  std::memcpy(h.st_d, sd, sizeof(sd));
+  h.st_i[0] = c->Npos; h.st_i[1] = c->Nneg; h.st_i[2] = c->backtracks; h.st_i[3] = (int32_t)c->it;
+  h.st_l[0] = c->fire_steps; h.st_l[1] = c->calls;
+  std::vector<double> buf(3 * (size_t)N);
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(buf.data(), c->rho, N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(buf.data() + N, c->fx[c->cur], N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(buf.data() + 2 * N, c->fv[c->cur], N * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(c, CDFT_ERR_ARG, std::string("could not open ") + path);
+  const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(buf.data(), sizeof(double), buf.size(), f) == buf.size();
+  if (std::fclose(f) != 0 || !ok) return fail(c, CDFT_ERR_ARG, std::string("could not write ") + path);
+  return CDFT_OK;
+}
+
+static int fire_buffers(cdft_ctx* c);
+
+int cdft_fire_load(cdft_ctx* c, const char* path) {
+  if (!c || !path) return CDFT_ERR_ARG;
+  const long N = c->info.N;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(c, CDFT_ERR_ARG, std::string("could not open ") + path);
+  FireFileHead h;
+  std::vector<double> buf(3 * (size_t)N);
+  const bool rd = std::fread(&h, sizeof(h), 1, f) == 1;
+  const bool ok = rd && std::memcmp(h.magic, kFireMagic, 8) == 0 && h.N == N && h.nx == c->p.nx && h.ny == c->p.ny && h.nz == c->p.nz &&
+                  std::fread(buf.data(), sizeof(double), buf.size(), f) == buf.size();
+  std::fclose(f);
+  if (!ok) return fail(c, CDFT_ERR_ARG, std::string(path) + " is not a FIRE2 state of this lattice");
+  int rc = fire_buffers(c);
+  if (rc) return rc;
+  cdft_fire_params& q = c->fp;
+  q.dt = h.prm_d[0]; q.dt_max = h.prm_d[1]; q.dt_min = h.prm_d[2]; q.alpha_start = h.prm_d[3];
+  q.f_alf = h.prm_d[4]; q.f_dec = h.prm_d[5]; q.f_inc = h.prm_d[6]; q.force_limit = h.prm_d[7];
+  q.n_delay = h.prm_i[0]; q.n_p_negative_max = h.prm_i[1]; q.initial_delay = h.prm_i[2];
+  c->cur = 0;
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->rho, buf.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->fx[0], buf.data() + N, N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CUDA_OR_FAIL(c, cudaMemcpyAsync(c->fv[0], buf.data() + 2 * N, N * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (c->fixed_mass <= 0) c->mu = h.st_d[9];
+  // the derivative and alias gradient of the saved state, from one evaluation at its density
+  double t[8];
+  rc = eval_internal(c, t);
+  if (rc) return rc;
+  rc = fire_accept(c, 0);
+  if (rc) return rc;
+  c->F = h.st_d[0]; c->dt = h.st_d[1]; c->dt_max = h.st_d[2]; c->alpha = h.st_d[3]; c->vv = h.st_d[4]; c->dt_best = h.st_d[5];
+  c->fmax = h.st_d[6];
+  c->Npos = h.st_i[0]; c->Nneg = h.st_i[1]; c->backtracks = h.st_i[2]; c->it = (unsigned)h.st_i[3];
+  c->fire_steps = h.st_l[0]; c->calls = h.st_l[1];
   c->fire_ready = true;
   return CDFT_OK;
 }

@@ -238,14 +238,17 @@ def train(model, samples, shape, steps=300, lr=3e-3, device="cuda", log=None):
     """samples: list of (seed_coarse, kT, rho_converged). Loss: mean squared error of log rho."""
     model.to(device)
     opt = torch.optim.Adam(model.parameters(), lr=lr)
+    # per sample only the coarse seed and the FP32 target stay resident (N floats); the
+    # (N, K_IN) features are rebuilt for each step, so thousands of samples fit on the device
     data = []
     for seed, kT, rho in samples:
-        f, up = features(seed, kT, shape, device)
+        _, up = features(seed, kT, shape, device)
         target = torch.log(torch.as_tensor(rho, device=device, dtype=torch.float32).reshape(-1)) - torch.log(up.reshape(-1))
-        data.append((f, target))
+        data.append((seed, kT, target))
     g = torch.Generator().manual_seed(7)
     for it in range(steps):
-        f, target = data[int(torch.randint(len(data), (1,), generator=g))]
+        seed, kT, target = data[int(torch.randint(len(data), (1,), generator=g))]
+        f, _ = features(seed, kT, shape, device)
         out = model(f, shape)
         loss = torch.mean((out - target) ** 2)
         opt.zero_grad()

@@ -259,6 +259,15 @@ typedef struct cdft_fire_report {
   long newton, cg_iters; /* Newton-Krylov refinement of cdft_fire_run_device (mixed = 2): corrections, CG iterations */
 } cdft_fire_report;
 
+/* fireMinimizer2 serialisation (include/Minimizer.h:145-180, Boost archives there): the
+ * whole FIRE2 state (density, alias coordinates x, velocities v, parameters, dt, alpha,
+ * counters) to a file of raw native doubles behind a small header, and back. After
+ * cdft_fire_load (no cdft_fire_init needed; the file must come from the same lattice) the
+ * next steps continue the saved run, the state's dF recomputed by one evaluation.
+ * CDFT_ERR_ARG when the file cannot be opened or does not fit the context. */
+int cdft_fire_save(cdft_ctx* ctx, const char* path);
+int cdft_fire_load(cdft_ctx* ctx, const char* path);
+
 int cdft_fire_default_params(cdft_fire_params* p);
 /* fireMinimizer2::fireMinimizer2: x = alias(rho), one evaluation, v = 0. */
 int cdft_fire_init(cdft_ctx* ctx, const cdft_fire_params* p);

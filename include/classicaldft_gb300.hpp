@@ -16,8 +16,12 @@
 #ifndef CLASSICALDFT_GB300_HPP
 #define CLASSICALDFT_GB300_HPP
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <istream>
+#include <ostream>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -63,6 +67,85 @@ class Lattice {
  protected:
   double dx_;
   long n_[3];
+};
+
+// include/DFT_LinAlg.h:14-98: the reference's real vector, with the behaviour of its
+// Armadillo adapter (additionalCode/DFT_Armadillo.cpp), in host memory. getDF returns one.
+class DFT_Vec {
+ public:
+  DFT_Vec() : d_(1, 0.0) {}
+  explicit DFT_Vec(unsigned N) : d_(N, 0.0) {}
+  void set(unsigned pos, double val) { d_[pos] = val; }
+  double get(unsigned pos) const { return d_[pos]; }
+  void set(const DFT_Vec& x) { d_ = x.d_; }
+  void set(const DFT_Vec& v1, const DFT_Vec& v2, double scale) {  // v1 + v2 * scale
+    d_.resize(v1.size());
+    for (size_t i = 0; i < d_.size(); ++i) d_[i] = v1.d_[i] + v2.d_[i] * scale;
+  }
+  void set(const double* x, unsigned n) { d_.assign(x, x + n); }
+  void set(double v) { std::fill(d_.begin(), d_.end(), v); }
+  void set_random_normal() {
+    std::mt19937_64 g(std::random_device{}());
+    std::normal_distribution<double> nd(0.0, 1.0);
+    for (double& x : d_) x = nd(g);
+  }
+  void set_random() {  // uniform in (-1, 1)
+    std::mt19937_64 g(std::random_device{}());
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    for (double& x : d_) x = 2 * u(g) - 1;
+  }
+  void resize(long N) { d_.resize(N, 0.0); }
+  void zeros(long N) { d_.assign(N, 0.0); }
+  void zeros() { std::fill(d_.begin(), d_.end(), 0.0); }
+  double inf_norm() const {
+    double m = 0;
+    for (double x : d_) m = std::max(m, std::fabs(x));
+    return m;
+  }
+  double euclidean_norm() const { return std::sqrt(dotWith(*this)); }
+  void normalise() { MultBy(1.0 / euclidean_norm()); }
+  double min() const { return *std::min_element(d_.begin(), d_.end()); }
+  double max() const { return *std::max_element(d_.begin(), d_.end()); }
+  double* memptr() { return d_.data(); }
+  const void* get_raw_data() const { return d_.data(); }
+  unsigned size() const { return (unsigned)d_.size(); }
+  double dotWith(const DFT_Vec& v) const {
+    double s = 0;
+    for (size_t i = 0; i < d_.size(); ++i) s += v.d_[i] * d_[i];
+    return s;
+  }
+  double accu() const {
+    double s = 0;
+    for (double x : d_) s += x;
+    return s;
+  }
+  void MultBy(double val) { for (double& x : d_) x *= val; }
+  void IncrementBy(const DFT_Vec& v) { for (size_t i = 0; i < d_.size(); ++i) d_[i] += v.d_[i]; }
+  void DecrementBy(const DFT_Vec& v) { for (size_t i = 0; i < d_.size(); ++i) d_[i] -= v.d_[i]; }
+  void add(double shift) { for (double& x : d_) x += shift; }
+  void IncrementBy(unsigned pos, double val) { d_[pos] += val; }
+  void IncrementBy_Scaled_Vector(const DFT_Vec& v, double scale) { for (size_t i = 0; i < d_.size(); ++i) d_[i] += v.d_[i] * scale; }
+  void Schur(const DFT_Vec& v1, const DFT_Vec& v2) {
+    d_.resize(v1.size());
+    for (size_t i = 0; i < d_.size(); ++i) d_[i] = v1.d_[i] * v2.d_[i];
+  }
+  // the reference's stream format: unsigned N, then N doubles
+  friend std::ostream& operator<<(std::ostream& of, const DFT_Vec& v) {
+    const unsigned N = v.size();
+    of.write((const char*)&N, sizeof(unsigned));
+    of.write((const char*)v.d_.data(), N * sizeof(double));
+    return of;
+  }
+  friend std::istream& operator>>(std::istream& in, DFT_Vec& v) {
+    unsigned N = 0;
+    in.read((char*)&N, sizeof(unsigned));
+    v.resize(N);
+    in.read((char*)v.d_.data(), N * sizeof(double));
+    return in;
+  }
+
+ private:
+  std::vector<double> d_;
 };
 
 // include/Density.h:35-118 (the host copy of the field; the GPU holds the working copy)
@@ -168,12 +251,9 @@ class FMT_Species {
   double getHSD() const { return hsd_; }
   Density& getDensity() { return density_; }
   const Density& getLattice() const { return density_; }
-  std::vector<double>& getDF() { return dF_; }
-  double get_convergence_monitor() const {
-    double m = 0;
-    for (double x : dF_) m = std::max(m, std::fabs(x));
-    return m / density_.dV();
-  }
+  DFT_Vec& getDF() { return dF_; }
+  const DFT_Vec& getDF() const { return dF_; }
+  double get_convergence_monitor() const { return dF_.inf_norm() / density_.dV(); }
   double fixedMass() const { return fixedMass_; }
   void setMuInternal(double m) { mu_ = m; }
 
@@ -182,7 +262,7 @@ class FMT_Species {
   double hsd_, mu_;
   double fixedMass_ = -1;
   bool fixedBackground_ = false, homogeneousBoundary_ = false;
-  std::vector<double> dF_;
+  DFT_Vec dF_;
 };
 
 // include/Species.h:380-461, src/FMT_Species.cpp:645-738: hard-sphere colloids with ideal
@@ -228,9 +308,9 @@ class DFT {
   double calculateFreeEnergyAndDerivatives(bool onlyFex) {
     push();
     double t[8];
-    std::vector<double>& dF = s_->getDF();
+    DFT_Vec& dF = s_->getDF();
     dF.resize(s_->getDensity().Ntot());
-    int rc = cdft_eval(context(), onlyFex ? 1 : 0, t, dF.data(), 0);
+    int rc = cdft_eval(context(), onlyFex ? 1 : 0, t, dF.memptr(), 0);
     check(rc, ctx_);
     pull(t);
     return t[0];
@@ -242,12 +322,18 @@ class DFT {
   double get_f_hs() const { return F_[1]; }
   double get_f_mf() const { return F_[2]; }
   double get_f_ext() const { return F_[3]; }
-  std::vector<double>& getDF(int) { return s_->getDF(); }
+  DFT_Vec& getDF(int) { return s_->getDF(); }
   FMT_Species* getSpecies(int) const { return s_; }
   double get_convergence_monitor() const { return s_->get_convergence_monitor(); }
 
   // Dynamical_Matrix::matrix_dot_v1 (src/Dynamical_Matrix.cpp): the full Hessian of Omega
   // (DFT::matrix_dot_v_intern, src/DFT.cpp:435-488) times v, at the current density.
+  void matrix_dot_v1(const DFT_Vec& v, DFT_Vec& result, void* param = nullptr) {
+    (void)param;
+    push();
+    result.resize(v.size());
+    check(cdft_hessian_dot_v(context(), (const double*)v.get_raw_data(), result.memptr(), 0), ctx_);
+  }
   void matrix_dot_v1(const std::vector<double>& v, std::vector<double>& result) {
     push();
     result.resize(v.size());
@@ -298,7 +384,9 @@ class DFT {
   void pull(const double* t) {
     F_[0] = t[1]; F_[1] = t[2]; F_[2] = t[3]; F_[3] = t[4];
     s_->setMuInternal(t[5]);
-    pull_density();  // fixed mass rescales the density, as the reference's Density does
+    // a fixed mass rescales the density, as the reference's Density does; otherwise the
+    // evaluation leaves it as pushed and nothing comes back
+    if (s_->is_mass_fixed()) pull_density();
   }
   FMT_Species* s_;
   FMT* fmt_ = nullptr;
@@ -320,14 +408,48 @@ class fireMinimizer2 {
   double step() {
     start();
     check(cdft_fire_step(dft_->context(), 1, &r_), dft_->context());
+    snapshot_after(1);
     return r_.F;
   }
+  // Minimizer::run (src/Minimizer.cpp:36-87), steps on the GPU; with snapshots on, the run
+  // is cut where the reference's step() writes one, and the density comes back there
   void run(long maxSteps = -1) {
     start();
-    check(cdft_fire_run(dft_->context(), maxSteps, &r_), dft_->context());
+    if (!snapshots_) {
+      check(cdft_fire_run(dft_->context(), maxSteps, &r_), dft_->context());
+      dft_->pull_density();
+      return;
+    }
+    long done = 0;
+    for (;;) {
+      long chunk = (10 - counter() % 10) % 10 + 1;  // steps up to and including the next writing one
+      if (maxSteps >= 0) chunk = std::min(chunk, maxSteps - done);
+      if (chunk <= 0) break;
+      cdft_fire_report r;
+      check(cdft_fire_run(dft_->context(), chunk, &r), dft_->context());
+      r_ = r;
+      done += r.steps;
+      snapshot_after(r.steps);
+      if (r.steps < chunk || r.stop != 0) break;
+    }
     dft_->pull_density();
   }
   void resume(long maxSteps = -1) { run(maxSteps); }
+  // fireMinimizer2::step writes snapshot_s0.dat (Density::writeDensity) at every tenth call
+  // counted over the process (src/Minimizer.cpp:258-268); off: no files, no density reads
+  void setSnapshots(bool on) { snapshots_ = on; }
+  // the minimizer's state (Boost serialisation in the reference, include/Minimizer.h:145-180)
+  // to a file and back; a loaded minimizer continues the saved run
+  void save_state(const std::string& path) {
+    start();
+    check(cdft_fire_save(dft_->context(), path.c_str()), dft_->context());
+  }
+  void load_state(const std::string& path) {
+    dft_->push();
+    check(cdft_fire_load(dft_->context(), path.c_str()), dft_->context());
+    started_ = true;
+    dft_->pull_density();
+  }
   double getF() const { return r_.F; }
   double get_convergence_monitor() const { return std::fabs(r_.vv / dft_->getSpecies(0)->getDensity().getVolume()); }
   const cdft_fire_report& report() const { return r_; }
@@ -340,10 +462,25 @@ class fireMinimizer2 {
       started_ = true;
     }
   }
+  static long& counter() {  // the reference's static step counter, shared by every minimizer
+    static long ic = 0;
+    return ic;
+  }
+  // after n more step() calls: write snapshot_s0.dat for each that lands on a multiple of 10
+  void snapshot_after(long n) {
+    if (n <= 0) return;
+    const long first = counter(), last = counter() + n - 1;
+    counter() += n;
+    if (!snapshots_) return;
+    if ((last / 10) * 10 < first) return;  // no multiple of 10 in [first, last]
+    dft_->pull_density();
+    dft_->getSpecies(0)->getDensity().writeDensity("snapshot_s0.dat");
+  }
   DFT* dft_;
   cdft_fire_params p_;
   cdft_fire_report r_{};
   bool started_ = false;
+  bool snapshots_ = true;
 };
 
 // include/Minimizer.h:189-266 (periodic boundaries)

@@ -2,10 +2,12 @@
 // against include/classicaldft_gb300.hpp: config 1 (hard spheres, WhiteBearI,
 // 32^3 at dx = 0.2, rho = 0.7 (1 + noise)), one evaluation, then FIRE2 steps.
 // Prints "Omega F_hs mu steps F_final sum(Hv) sum|Hv| max|snapshot - density| Omega_AO log_det
-// lambda_max" for the test to compare.
+// lambda_max max|dF| sum(dF) F_resumed steps_resumed" for the test to compare.
 #include <algorithm>
 #include <cstdint>
+#include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "classicaldft_gb300.hpp"
@@ -33,13 +35,15 @@ int main(int argc, char** argv) {
   species.setChemPotential(dft.mu_times_beta(0.7));
   double F = dft.calculateFreeEnergyAndDerivatives(false);
   double Fhs = dft.get_f_hs();
+  // the derivative as the reference hands it out: a DFT_Vec with its BLAS-1 calls
+  const double dF_inf = dft.getDF(0).inf_norm(), dF_accu = dft.getDF(0).accu();
   // Hessian . v at this density (DFT::matrix_dot_v1), v_i = 0.3 (2u - 1) from splitmix64(77)
-  std::vector<double> v(density.Ntot()), Hv;
+  DFT_Vec v(density.Ntot()), Hv;
   uint64_t vs = 77;
-  for (auto& x : v) x = 0.3 * (2.0 * splitmix_uniform(vs) - 1.0);
-  dft.matrix_dot_v1(v, Hv);
-  double hsum = 0, habs = 0;
-  for (double x : Hv) { hsum += x; habs += x < 0 ? -x : x; }
+  for (unsigned i = 0; i < v.size(); ++i) v.set(i, 0.3 * (2.0 * splitmix_uniform(vs) - 1.0));
+  dft.matrix_dot_v1(v, Hv, nullptr);
+  double hsum = Hv.accu(), habs = 0;
+  for (unsigned i = 0; i < Hv.size(); ++i) habs += std::fabs(Hv.get(i));
   // the spectral drivers at this density: Log_Det (order 6, one probe, seed 1234, spectrum
   // bracket [0.005, 0.2]) and Eigenvalues with change_sign (the largest eigenvalue)
   Log_Det ld(dft, 6, 0.2, 0.005);
@@ -50,9 +54,19 @@ int main(int argc, char** argv) {
   eig.set_tolerence(1e-10);
   eig.calculate_eigenvector();
   const double lam_max = eig.get_eigenvalue();
+  // FIRE2 writes snapshot_s0.dat at its 1st, 11th, ... step, as the reference does; its
+  // state is saved after the run and a second minimizer resumes it for 10 more steps
   fireMinimizer2 fire(&dft);
   fire.setForceTerminationCriterion(0.0);
   fire.run(fire_steps);
+  fire.save_state("fire.state");
+  const double F_run = fire.getF();
+  const long steps_run = fire.report().total_steps;
+  fireMinimizer2 resumed(&dft);
+  resumed.setSnapshots(false);
+  resumed.load_state("fire.state");
+  resumed.run(10);
+  const double F_resumed = resumed.getF();
   // the density files (src/Density.cpp:197-244): snapshot round trip, and the VTK file
   density.writeDensity("snapshot.dat");
   Density back(0.2, L);
@@ -74,7 +88,8 @@ int main(int argc, char** argv) {
     sa.setChemPotential(dftA.mu_times_beta(0.4));
     FA = dftA.calculateFreeEnergyAndDerivatives(false);
   }
-  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", F, Fhs, species.getChemPotential(),
-              fire.report().total_steps, fire.getF(), hsum, habs, snap_diff, FA, logdet, lam_max);
+  std::printf("%.17g %.17g %.17g %ld %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %ld\n", F, Fhs,
+              species.getChemPotential(), steps_run, F_run, hsum, habs, snap_diff, FA, logdet, lam_max, dF_inf, dF_accu, F_resumed,
+              resumed.report().total_steps);
   return 0;
 }

@@ -68,3 +68,21 @@ def test_reference_style_app_runs_config1(tmp_path):
     lam, _, _ = c.eigenvalue(tol=1e-10, change_sign=True)
     c.close()
     assert abs(float(out[10]) - lam) <= 1e-9 * lam
+    # getDF(0) is a DFT_Vec: its inf_norm and accu against the reference's dF
+    dV = 0.2 ** 3
+    assert abs(float(out[11]) - g["hs32.dF.absmax"][0]) <= 1e-10 * dV
+    assert abs(float(out[12]) - g["hs32.dF.sum"][0]) <= 1e-10 * dV * 32 ** 3
+    # the state saved after 20 steps and resumed by a second minimizer: steps 21-30 of the
+    # reference's trajectory
+    assert int(out[14]) == 30
+    assert abs(float(out[13]) - fire["fire32.F"][29]) <= 1e-12 * abs(float(out[13]))
+    # snapshot_s0.dat: written by the 1st and 11th steps (the reference's every tenth call),
+    # so it holds the density after step 11
+    snap = cd.read_density(str(tmp_path / "snapshot_s0.dat"), shape)
+    c = cd.Context(32, 0.2, cd.WHITEBEAR_I, hsd=1.0)
+    c.set_chem_potential(c.bulk(0.7)["mu"])
+    c.set_density(rho)
+    c.fire_init(force_limit=0.0)
+    c.fire_step(11)
+    np.testing.assert_allclose(snap, c.get_density(), rtol=1e-12, atol=0)
+    c.close()

@@ -129,3 +129,40 @@ def test_ddft_fp32_64cubed_tracks_fp64_50_steps():
     assert abs(mr - m0) <= 1e-5 * m0
     assert np.abs(d32 - d64).max() <= 2e-5, np.abs(d32 - d64).max()
     assert np.abs(dr - d64).max() <= 2e-5, np.abs(dr - d64).max()
+
+
+def test_fire_state_saved_and_resumed_matches_reference(tmp_path):
+    """fireMinimizer2's serialised state: 30 fixed-mass FIRE2 steps of the LJ droplet, the
+    state saved, a fresh context resumes it for 30 more (host-stepped) and the device-resident
+    driver from a second copy; both land on the reference's 60-step trajectory (dt, alpha,
+    F, the final density)."""
+    import classicaldft_gb300 as cd
+    g = golden("fire_lj24")
+    rho = golden("eval_lj")["lj24.rho"].reshape(24, 24, 24)
+    hsd = golden("eval_lj")["lj24.hsd"][0]
+    mass = rho.sum() * 0.2 ** 3
+
+    def ctx():
+        return cd.Context(24, 0.2, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.8, fixed_mass=mass)
+    a = ctx()
+    a.set_density(rho)
+    a.fire_init(force_limit=0.0)
+    a.fire_step(30)
+    path = str(tmp_path / "fire.state")
+    a.fire_save(path)
+    a.close()
+    for device in (False, True):
+        b = ctx()
+        b.fire_load(path)
+        if device:
+            r = b.fire_run_device(0.0, max_steps=30)
+        else:
+            reps = [b.fire_step(1) for _ in range(30)]
+            np.testing.assert_allclose([q["F"] for q in reps], g["firelj.F"][30:], rtol=1e-12)
+            np.testing.assert_array_equal([q["dt"] for q in reps], g["firelj.dt"][30:])
+            r = reps[-1]
+        assert r["total_steps"] == 60
+        assert r["dt"] == g["firelj.dt"][59] and r["alpha"] == g["firelj.alpha"][59]
+        assert abs(r["F"] - g["firelj.F"][59]) <= 1e-12 * abs(g["firelj.F"][59])
+        np.testing.assert_allclose(b.get_density().ravel(), g["firelj.rho_final"], rtol=0, atol=1e-12)
+        b.close()
