@@ -53,10 +53,12 @@ def workload():
 
 # DRAM bytes per launch (read + write) from one ncu capture of the named kernel on
 # this workload; None where none was taken.
-NCU_TRAFFIC = {("phi_rows", "fp32"): 98.1e6 + 39.7e6}
+NCU_TRAFFIC = {("phi_rows", "fp32"): 98.1e6 + 40.0e6, ("phi_rows", "fp64"): 196.8e6 + 133.2e6}
 # FP64 work per launch of a pass (ncu: smsp__sass_thread_inst_executed_op_{dadd,dmul}_pred_on.sum
-# + 2 x ..._dfma_pred_on.sum) on this workload; None where none was taken.
-NCU_FP64_FLOPS = {}
+# + 2 x ..._dfma_pred_on.sum) on this workload, and how busy that launch kept the FP64 pipe
+# (sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active); None where none was taken.
+NCU_FP64_FLOPS = {"phi_rows": 424.27e6 + 266.25e6 + 2 * 306.44e6}
+NCU_FP64_PIPE_BUSY = {"phi_rows": 0.843}
 
 
 def fp64_fma_peak(cd):
@@ -630,6 +632,7 @@ def main():
                          "flops_per_launch": ops, "flops_source": "executed FP64 add/mul/fma (fma = 2) per launch, ncu",
                          "peak_source": "measured in this run: cdft_fp64_fma_rate (independent FMA chains on every SM)",
                          "traffic": NCU_TRAFFIC.get((top64["pass"], "fp64")),
+                         "fp64_pipe_busy": NCU_FP64_PIPE_BUSY.get(top64["pass"]),
                          "hbm": {"achieved_gbs": hbm64, "peak_gbs": peak, "frac": hbm64 / peak, "peak_source": peak_kind}},
             "eval_roofline": {"algorithmic_bytes_per_eval": B64, "achieved_gbs": B64 / (ms64 * 1e-3) / 1e9,
                               "frac": B64 / (ms64 * 1e-3) / 1e9 / peak},
