@@ -754,7 +754,6 @@ static int product_input(cdft_ctx* c, const double* v, int on_device, const doub
 
 int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
   if (!c || !v || !out) return CDFT_ERR_ARG;
-  if (c->p.ao_rp > 0) return fail(c, CDFT_ERR_ARG, "Hessian products are not built for the AO model");
   int rc = hessian_buffers(c);
   if (rc) return rc;
   const size_t nb = c->info.N * sizeof(double);
@@ -776,7 +775,6 @@ int cdft_hessian_dot_v(cdft_ctx* c, const double* v, double* out, int on_device)
 // (C++ linkage: an internal helper between the ABI's entry points.)
 }  // extern "C"
 int cdft_internal_matvec(cdft_ctx* c, int matrix, const double* x, double* y, bool prepare) {
-  if (c->p.ao_rp > 0) return fail(c, CDFT_ERR_ARG, "Hessian products are not built for the AO model");
   int rc = hessian_buffers(c);
   if (rc) return rc;
   if (prepare) {
@@ -803,7 +801,6 @@ extern "C" {
 // DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): g . (H v) at the current density.
 int cdft_ddft_matrix_dot_v(cdft_ctx* c, const double* v, double* out, int on_device) {
   if (!c || !v || !out) return CDFT_ERR_ARG;
-  if (c->p.ao_rp > 0) return fail(c, CDFT_ERR_ARG, "Hessian products are not built for the AO model");
   int rc = hessian_buffers(c);
   if (rc) return rc;
   const size_t nb = c->info.N * sizeof(double);

@@ -670,7 +670,7 @@ extern "C" int cdft_fire_run_device(cdft_ctx* c, double resid_tol, double switch
   if (!c) return CDFT_ERR_ARG;
   if (!c->fire_ready) return cdft_internal_fail(c, CDFT_ERR_STATE, "cdft_fire_init has not been called");
   if (mixed < 0 || mixed > 3) return cdft_internal_fail(c, CDFT_ERR_ARG, "mixed must be 0, 1, 2 or 3");
-  if (mixed >= 2 && c->p.ao_rp > 0) mixed = 1;  // no Hessian products for the AO model: the FIRE2 policy
+  if (mixed >= 2 && c->p.ao_rp > 0) mixed = 1;  // no Newton-Krylov for the AO model: the FIRE2 policy
   if (mixed >= 2 && c->homo_bd) mixed = 1;  // Newton-Krylov is not built for the homogeneous boundary: the FIRE2 policy
   int rc = ensure_engine(c);
   if (rc) return rc;

@@ -384,7 +384,9 @@ extern "C" int cdft_newton_refine(cdft_ctx* c, double tol, int max_newton, int m
 
 extern "C" int cdft_newton_refine_ex(cdft_ctx* c, double tol, const cdft_newton_params* prm, cdft_newton_report* rep) {
   if (!c || !prm) return CDFT_ERR_ARG;
-  if (c->p.ao_rp > 0) return cdft_internal_fail(c, CDFT_ERR_ARG, "Newton-Krylov needs Hessian products, which are not built for the AO model");
+  // the reference's Hessian of an FMT_AO_Species system (src/FMT.cpp:437-567) leaves out the
+  // AO free energy, so it is not the Jacobian of the AO force that Newton-Krylov would need
+  if (c->p.ao_rp > 0) return cdft_internal_fail(c, CDFT_ERR_ARG, "Newton-Krylov is not built for the AO model (its Hessian omits the AO term)");
   if (c->homo_bd) return cdft_internal_fail(c, CDFT_ERR_ARG, "Newton-Krylov is not built for the homogeneous boundary");
   const int max_newton = prm->max_newton, max_cg = prm->max_cg;
   const double cg_rtol = prm->cg_rtol, eta_max = prm->eta_max, fp32_above = prm->fp32_above;

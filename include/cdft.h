@@ -122,7 +122,11 @@ int cdft_eval(cdft_ctx* ctx, int only_fex, double* terms, double* dF, int on_dev
  * FMT::add_second_derivative src/FMT.cpp:437-567, the mean-field convolution
  * src/Interaction.cpp:119-147), taken at the context's current density (the
  * reference uses the fundamental measures of the last evaluation: call
- * cdft_eval first for the same state). v and out hold N values. */
+ * cdft_eval first for the same state). v and out hold N values. For an
+ * FMT_AO_Species system this is the reference's product too: its
+ * add_second_derivative takes the AO species through the hard-sphere branch, so the
+ * AO free energy has no term in it (Newton-Krylov, which needs the Jacobian of the
+ * AO force, is therefore not offered for the AO model). */
 int cdft_hessian_dot_v(cdft_ctx* ctx, const double* v, double* out, int on_device);
 /* DDFT::matrix_dot_v_intern (src/DDFT.cpp:353-361): the DDFT dynamical matrix
  * times v, g . (H v), with DDFT::g_dot_x's forward-difference mobility operator

@@ -526,6 +526,17 @@ int main(int argc, char** argv) {
         for (double r : {0.05, 0.2, 0.4, 0.6}) { mu.push_back(dft->mu_times_beta(r)); om.push_back(dft->omega_times_beta_over_volume(r)); }
         put(tag + ".bulk_mu", mu);
         put(tag + ".bulk_omega", om);
+        // Dynamical_Matrix::matrix_dot_v1 of the AO system at this density: the reference's
+        // FMT::add_second_derivative (src/FMT.cpp:437-567) takes the AO species through the
+        // plain FMT_Species branch, so this is the hard-sphere FMT Hessian plus the ideal gas
+        {
+          const long N = d->Ntot();
+          DFT_Vec v(N), r(N);
+          SplitMix64 g(77);
+          for (long i = 0; i < N; ++i) v.set(i, 0.3 * (2.0 * g.uniform() - 1.0));
+          dft->matrix_dot_v1(v, r, nullptr);
+          put(tag + ".Hv", vec_of(r));
+        }
       }
     } else if (c == "files") {
       case_files(argv[2]);

@@ -194,14 +194,25 @@ def test_eigen_drivers_at_128_uniform_state(cd):
     c.close()
 
 
-def test_spectral_drivers_reject_ao(cd):
-    c = cd.Context(16, 0.2, cd.WHITEBEAR_I, hsd=1.0, ao_rp=0.35, ao_reservoir=0.4)
-    c.set_density(np.full(SHAPE, 0.3))
-    with pytest.raises(cd.CDFTError):
-        c.log_det(4, 1.0, 0.01, 1, 1)
-    with pytest.raises(cd.CDFTError):
-        c.eigenvalue()
-    c.close()
+def test_spectral_drivers_on_ao_system(cd, oracle):
+    """The reference's Hessian of an FMT_AO_Species system is its hard-sphere FMT Hessian plus
+    the ideal gas (FMT::add_second_derivative takes the AO species through the plain branch),
+    so the spectral drivers on an AO system give what they give on the same density without
+    polymers: Log_Det with the same probes, and the smallest eigenvalue."""
+    rho = oracle.fill_noise(SHAPE, 0.6, 0.2, 11)
+    out = []
+    for ao in (True, False):
+        kw = dict(ao_rp=0.35, ao_reservoir=0.4) if ao else {}
+        c = cd.Context(SHAPE, 0.2, cd.WHITEBEAR_I, hsd=1.0, **kw)
+        c.set_density(rho)
+        c.eval()
+        ld, _ = c.log_det(10, 0.16, 0.008, 1234, 2)
+        lam, _, rep = c.eigenvalue(tol=1e-9, max_matvecs=40000)
+        assert rep["converged"]
+        out.append((ld, lam))
+        c.close()
+    assert abs(out[0][0] - out[1][0]) <= 1e-12 * abs(out[1][0])
+    assert abs(out[0][1] - out[1][1]) <= 1e-9 * abs(out[1][1])
 
 
 def _ddft_residual(c, lam, y):
