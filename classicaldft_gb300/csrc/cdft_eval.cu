@@ -91,17 +91,23 @@ std::shared_ptr<FFTTable> make_fft_table(int n, std::string* err, const std::vec
     len = sub;
   }
   const size_t cnt = re.size();
-  std::vector<double2> h64(cnt);
+  // the FP64 table, then the same twiddles as df64 pairs (hi, lo of the real part, hi, lo
+  // of the imaginary part), which the FP64 transforms of the compile-time plans read
+  std::vector<double2> h64(2 * cnt);
   std::vector<float2> h32(cnt);
   for (size_t i = 0; i < cnt; ++i) {
     h64[i] = make_double2((double)re[i], (double)im[i]);
     h32[i] = make_float2((float)re[i], (float)im[i]);
+    const float rh = (float)re[i], ih = (float)im[i];
+    const float rl = (float)(re[i] - (long double)rh), il = (float)(im[i] - (long double)ih);
+    float4 q = make_float4(rh, rl, ih, il);
+    std::memcpy(&h64[cnt + i], &q, sizeof(q));
   }
-  if (cudaMalloc(&t->d64, cnt * sizeof(double2)) != cudaSuccess || cudaMalloc(&t->d32, cnt * sizeof(float2)) != cudaSuccess) {
+  if (cudaMalloc(&t->d64, 2 * cnt * sizeof(double2)) != cudaSuccess || cudaMalloc(&t->d32, cnt * sizeof(float2)) != cudaSuccess) {
     if (err) *err = "cudaMalloc of FFT tables failed";
     return nullptr;
   }
-  cudaMemcpy(t->d64, h64.data(), cnt * sizeof(double2), cudaMemcpyHostToDevice);
+  cudaMemcpy(t->d64, h64.data(), 2 * cnt * sizeof(double2), cudaMemcpyHostToDevice);
   cudaMemcpy(t->d32, h32.data(), cnt * sizeof(float2), cudaMemcpyHostToDevice);
   return t;
 }
