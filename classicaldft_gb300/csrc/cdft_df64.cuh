@@ -28,6 +28,7 @@ struct dfs {
   float h, l;
   __host__ __device__ dfs() {}
   __host__ __device__ constexpr dfs(float a, float b) : h(a), l(b) {}
+  __host__ __device__ constexpr dfs(int z) : h((float)z), l(0.f) {}  // small integer constants, exact
   // a constant (folded at compile time for literals): hi the nearest float, lo the rest
   __host__ __device__ constexpr explicit dfs(double d) : h((float)d), l((float)(d - (double)(float)d)) {}
 };

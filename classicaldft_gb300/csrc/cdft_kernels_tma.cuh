@@ -242,11 +242,11 @@ __device__ __forceinline__ void tile_butterfly_df(const void* __restrict__ xv, v
 
 // (no unrolling of the item loop: a df64 butterfly is ~12x the instructions of an FP64
 // one, and unrolled copies of every stage overflowed the instruction cache)
-template <int DIR, int TC, int PITCH, int NF, int ST, int NTH>
+template <int DIR, int TC, int PITCH, int NF, int ST, int NTH, bool IN_D, bool OUT_D>
 __device__ __forceinline__ void fx_stage_df(const void* __restrict__ src, void* __restrict__ dst, const float4* __restrict__ tws) {
   constexpr int p = fx_radix(NF, ST), len = fx_len(NF, ST), m = len / p, s = NF / len;
   constexpr int items = TC * (NF / p);
-  constexpr bool first = ST == 0, last = fx_radix(NF, ST + 1) == 0;
+  constexpr bool first = IN_D && ST == 0, last = OUT_D && fx_radix(NF, ST + 1) == 0;
   static_assert(p == 2 || p == 4 || p == 8, "df64 stages take radices 2, 4 and 8");
   const float4* tw = tws + fx_twoff(NF, ST);
 #pragma unroll 1
@@ -257,26 +257,27 @@ __device__ __forceinline__ void fx_stage_df(const void* __restrict__ src, void* 
   }
 }
 
-template <int DIR, int TC, int PITCH, int NF, int NTH, int ST = 0>
+template <int DIR, int TC, int PITCH, int NF, int NTH, bool IN_D, bool OUT_D, int ST = 0>
 __device__ __forceinline__ double2* tile_fft_fixed_df_stages(double2* b0, double2* b1, const float4* __restrict__ tws) {
   __syncthreads();
   if constexpr (fx_radix(NF, ST) == 0) {
     return b0;
   } else {
-    fx_stage_df<DIR, TC, PITCH, NF, ST, NTH>(b0, b1, tws);
-    return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, ST + 1>(b1, b0, tws);
+    fx_stage_df<DIR, TC, PITCH, NF, ST, NTH, IN_D, OUT_D>(b0, b1, tws);
+    return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D, ST + 1>(b1, b0, tws);
   }
 }
 // Each call stages the plan's df64 twiddles (fx_table_len(NF) entries, 2.6 KB for 128
 // points) in shared memory first: read by every butterfly, they made the texture path
 // the bottleneck when fetched from global memory. The previous call ended on a barrier,
-// so the copy cannot overwrite twiddles still in use.
-template <int DIR, int TC, int PITCH, int NF, int NTH>
+// so the copy cannot overwrite twiddles still in use. IN_D / OUT_D: the tile holds
+// doubles on entry / exit (else df64 values, for a caller that keeps them).
+template <int DIR, int TC, int PITCH, int NF, int NTH, bool IN_D = true, bool OUT_D = true>
 __device__ __forceinline__ double2* tile_fft_fixed_df(double2* b0, double2* b1, const dfc* __restrict__ twdf) {
   constexpr int NT = fx_table_len(NF);
   __shared__ float4 tws[NT];
   for (int i = threadIdx.x; i < NT; i += NTH) tws[i] = __ldg(reinterpret_cast<const float4*>(twdf) + i);
-  return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH>(b0, b1, tws);
+  return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D>(b0, b1, tws);
 }
 
 // FP64 tiles of the compile-time plans transform in df64 (see above)
@@ -639,6 +640,28 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   constexpr int M = ModelTraits<MODEL>::M;
   typedef PhiPack<M, RB, PhiCross<T>::value> PK;
   const T ih = (T)(1.0 / (double)hsd), ih2 = (T)(1.0 / ((double)hsd * (double)hsd));
+  // FP64 with a compile-time plan: the tile holds df64 values from the unpacking to the
+  // Hermitian split (both transforms on the FP32 pipe), and the evaluation's functional
+  // runs in df64 too, its f-functions of eta in FP64 (fmt_f_df); the other modes and RSLT
+  // take FP64 values per point (getv / setv convert).
+  constexpr bool DF = kDf64Transforms && std::is_same<T, double>::value && NF > 0;
+  constexpr bool DF_FUNC = DF && MODE == kPhiEval && MODEL != MODEL_RSLT;
+  auto getv = [&](const C* buf, int i, int h) -> T {
+    if constexpr (DF) {
+      const dfc z = reinterpret_cast<const dfc*>(buf)[i];
+      return (T)dfs_join(h ? z.y : z.x);
+    } else {
+      return cpart<T>(buf[i], h);
+    }
+  };
+  auto setv = [&](C* buf, int i, int h, T v) {
+    if constexpr (DF) {
+      dfc* z = reinterpret_cast<dfc*>(buf) + i;
+      (h ? z->y : z->x) = dfs_split((double)v);
+    } else {
+      set_cpart<T>(&buf[i], h, v);
+    }
+  };
   constexpr int L = PK::L;
   constexpr int LPd = L | 1;  // odd row pitch: the per-point loops stride rows without bank conflicts
   constexpr int E = ElemsPerComplex<T>::value;
@@ -688,20 +711,23 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
       PK::source(line, 1, aB, rB);
       const C* Arow = in + ((size_t)aA * RB + rA) * pz;
       const C* Brow = aB >= 0 ? in + ((size_t)aB * RB + rB) * pz : nullptr;
-      Z0[k * LPd + line] = pair_spectrum<T>(Arow, Brow, k, nz);
+      if constexpr (DF) reinterpret_cast<dfc*>(Z0)[k * LPd + line] = dfc_split(pair_spectrum<T>(Arow, Brow, k, nz));
+      else Z0[k * LPd + line] = pair_spectrum<T>(Arow, Brow, k, nz);
     }
     __syncthreads();
     if (threadIdx.x == 0) {  // In[b] consumed: bring the group NB steps ahead
       const long gn = g + (long)NB * gridDim.x;
       if (gn < ngroup) issue(gn, b);
     }
-    C* res = tfft<+1, T, L, LPd, NF, PhiThreads<T>::value>(Z0, Z1, pz_plan, tw);
+    C* res;
+    if constexpr (DF) res = tile_fft_fixed_df<+1, L, LPd, NF, PhiThreads<T>::value, false, false>(Z0, Z1, reinterpret_cast<const dfc*>(tw + fx_table_len(NF)));
+    else res = tfft<+1, T, L, LPd, NF, PhiThreads<T>::value>(Z0, Z1, pz_plan, tw);
     if constexpr (MODE == kPhiStoreN) {
       for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
         const int k = e % nz, r = e / nz;
         if (row0 + r >= d.rows) continue;
 #pragma unroll
-        for (int a = 0; a < M; ++a) NA[(long)a * d.N + (row0 + r) * nz + k] = cpart<T>(res[k * LPd + PK::line(r, a)], PK::comp(r, a));
+        for (int a = 0; a < M; ++a) NA[(long)a * d.N + (row0 + r) * nz + k] = getv(res, k * LPd + PK::line(r, a), PK::comp(r, a));
       }
       __syncthreads();
       continue;
@@ -711,12 +737,40 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
       const int k = e % nz, r = e / nz;
       if (row0 + r >= d.rows) {  // a row past the end: zeros into its slots (a line may pair it with a live row)
 #pragma unroll
-        for (int a = 0; a < M; ++a) set_cpart<T>(&oth[k * LPd + PK::line(r, a)], PK::comp(r, a), (T)0);
+        for (int a = 0; a < M; ++a) setv(oth, k * LPd + PK::line(r, a), PK::comp(r, a), (T)0);
+        continue;
+      }
+      if constexpr (DF_FUNC) {  // the functional in df64, values kept in df64 both ways
+        const dfc* rd = reinterpret_cast<const dfc*>(res);
+        dfc* od = reinterpret_cast<dfc*>(oth);
+        dfs nw[11];
+#pragma unroll
+        for (int a = 0; a < M; ++a) {
+          const dfc z = rd[k * LPd + PK::line(r, a)];
+          nw[a] = PK::comp(r, a) ? z.y : z.x;
+        }
+        const double eta = dfs_join(nw[0]);
+        const double phi = dfs_join(fmt_phi_point<dfs, MODEL>(nw, dfs_split((double)ih), dfs_split((double)ih2), dfs_split((double)esA),
+                                                               dfs_split((double)esB)));
+        if (eta > 0.5 && 1.0 - eta < 0.0) st |= 1u;
+        if (!isfinite(phi)) st |= 2u;
+        psum.add((T)phi);
+#pragma unroll
+        for (int p = 0; p < PK::per_row; ++p) {
+          dfc z;
+          z.x = nw[2 * p];
+          z.y = (2 * p + 1 < M) ? nw[2 * p + 1] : dfs(0);
+          od[k * LPd + r * PK::per_row + p] = z;
+        }
+        if constexpr (PK::cross) {
+          dfc* z = od + k * LPd + PK::line(r, M - 1);
+          (PK::comp(r, M - 1) ? z->y : z->x) = nw[M - 1];
+        }
         continue;
       }
       T nv[11];
 #pragma unroll
-      for (int a = 0; a < M; ++a) nv[a] = cpart<T>(res[k * LPd + PK::line(r, a)], PK::comp(r, a));
+      for (int a = 0; a < M; ++a) nv[a] = getv(res, k * LPd + PK::line(r, a), PK::comp(r, a));
       if constexpr (MODE == kPhiHess) {
         T nd[11];
 #pragma unroll
@@ -740,19 +794,34 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
         }
       }
 #pragma unroll
-      for (int p = 0; p < PK::per_row; ++p) oth[k * LPd + r * PK::per_row + p] = mk<T>(nv[2 * p], (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
-      if constexpr (PK::cross) set_cpart<T>(&oth[k * LPd + PK::line(r, M - 1)], PK::comp(r, M - 1), nv[M - 1]);
+      for (int p = 0; p < PK::per_row; ++p) {
+        setv(oth, k * LPd + r * PK::per_row + p, 0, nv[2 * p]);
+        setv(oth, k * LPd + r * PK::per_row + p, 1, (2 * p + 1 < M) ? nv[2 * p + 1] : (T)0);
+      }
+      if constexpr (PK::cross) setv(oth, k * LPd + PK::line(r, M - 1), PK::comp(r, M - 1), nv[M - 1]);
     }
-    C* res2 = tfft<-1, T, L, LPd, NF, PhiThreads<T>::value>(oth, res, pz_plan, tw);
+    C* res2;
+    if constexpr (DF) res2 = tile_fft_fixed_df<-1, L, LPd, NF, PhiThreads<T>::value, false, false>(oth, res, reinterpret_cast<const dfc*>(tw + fx_table_len(NF)));
+    else res2 = tfft<-1, T, L, LPd, NF, PhiThreads<T>::value>(oth, res, pz_plan, tw);
     for (int e = threadIdx.x; e < L * nzc; e += blockDim.x) {
       const int k = e % nzc, line = e / nzc;
       int aA, rA, aB, rB;
       PK::source(line, 0, aA, rA);
       PK::source(line, 1, aB, rB);
-      const C Z = res2[k * LPd + line];
-      const C W = res2[(k == 0 ? 0 : nz - k) * LPd + line];
-      if (row0 + rA < d.rows) Cf[(long)aA * d.Nc + (row0 + rA) * pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
-      if (aB >= 0 && row0 + rB < d.rows) Cf[(long)aB * d.Nc + (row0 + rB) * pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+      if constexpr (DF) {  // the split in df64, each output joined once
+        const dfc* rd = reinterpret_cast<const dfc*>(res2);
+        const dfc Z = rd[k * LPd + line], W = rd[(k == 0 ? 0 : nz - k) * LPd + line];
+        auto half = [](dfs a) { return dfs(__fmul_rn(0.5f, a.h), __fmul_rn(0.5f, a.l)); };  // exact
+        if (row0 + rA < d.rows)
+          Cf[(long)aA * d.Nc + (row0 + rA) * pz + k] = make_double2(dfs_join(half(Z.x + W.x)), dfs_join(half(Z.y - W.y)));
+        if (aB >= 0 && row0 + rB < d.rows)
+          Cf[(long)aB * d.Nc + (row0 + rB) * pz + k] = make_double2(dfs_join(half(Z.y + W.y)), dfs_join(half(W.x - Z.x)));
+      } else {
+        const C Z = res2[k * LPd + line];
+        const C W = res2[(k == 0 ? 0 : nz - k) * LPd + line];
+        if (row0 + rA < d.rows) Cf[(long)aA * d.Nc + (row0 + rA) * pz + k] = mk<T>((T)0.5 * (Z.x + W.x), (T)0.5 * (Z.y - W.y));
+        if (aB >= 0 && row0 + rB < d.rows) Cf[(long)aB * d.Nc + (row0 + rB) * pz + k] = mk<T>((T)0.5 * (Z.y + W.y), (T)0.5 * (W.x - Z.x));
+      }
     }
     __syncthreads();
   }

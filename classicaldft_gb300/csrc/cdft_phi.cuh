@@ -7,6 +7,8 @@
 // vector derivative carries the parity sign, off-diagonal tensor terms x2.
 #pragma once
 #include <cuda_runtime.h>
+#include <type_traits>
+#include "cdft_df64.cuh"
 #include "cdft_types.h"
 
 namespace cdft {
@@ -87,6 +89,16 @@ __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, 
   f3p = (T)2 * g * g * g;
 }
 
+// The same f-functions for a df64 eta (the FP64 Phi pass keeps its values in df64):
+// computed in FP64 from the joined eta (the logarithm and the division), then split.
+template <int MODEL>
+__device__ __forceinline__ void fmt_f_df(dfs e, dfs& f1, dfs& f2, dfs& f3, dfs& f1p, dfs& f2p, dfs& f3p) {
+  double a1, a2, a3, b1, b2, b3;
+  fmt_f<double, MODEL>(dfs_join(e), a1, a2, a3, b1, b2, b3);
+  f1 = dfs_split(a1); f2 = dfs_split(a2); f3 = dfs_split(a3);
+  f1p = dfs_split(b1); f2p = dfs_split(b2); f3p = dfs_split(b3);
+}
+
 // n[] holds the weighted densities in the order eta, s, v0, v1, v2, T00, T01,
 // T02, T11, T12, T22 (M = 11) or the first five (M = 5). On return n[] holds
 // dPhi/dn_a folded as described above. Returns Phi. ih = 1/hsd, ih2 = 1/hsd^2.
@@ -107,11 +119,12 @@ __device__ __forceinline__ T fmt_phi_point(T* n, T ih, T ih2, T A, T B, T* ao = 
   const T v1_v2 = v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2];
   const T v2_v2 = v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2];
   T f1, f2, f3, f1p, f2p, f3p;
-  fmt_f<T, MODEL>(eta, f1, f2, f3, f1p, f2p, f3p);
+  if constexpr (std::is_same<T, dfs>::value) fmt_f_df<MODEL>(eta, f1, f2, f3, f1p, f2p, f3p);
+  else fmt_f<T, MODEL>(eta, f1, f2, f3, f1p, f2p, f3p);
 
   T Phi3, dP3_dS2, dP3_dV2[3], dP3_dT[3][3];
   T Tm[3][3];
-  if (ModelTraits<MODEL>::tensor) {
+  if constexpr (ModelTraits<MODEL>::tensor) {
     Tm[0][0] = n[5]; Tm[0][1] = Tm[1][0] = n[6]; Tm[0][2] = Tm[2][0] = n[7];
     Tm[1][1] = n[8]; Tm[1][2] = Tm[2][1] = n[9]; Tm[2][2] = n[10];
     T vT[3], TT[3][3];
@@ -138,7 +151,7 @@ __device__ __forceinline__ T fmt_phi_point(T* n, T ih, T ih2, T A, T B, T* ao = 
     for (int j = 0; j < 3; ++j)
 #pragma unroll
       for (int k = 0; k < 3; ++k) dP3_dT[j][k] = a8 * (v2[j] * v2[k] - TT[k][j]) + b4 * (-s2 * Tm[k][j] + TT[k][j]);
-  } else if (MODEL == MODEL_RSLT) {
+  } else if constexpr (MODEL == MODEL_RSLT) {
     if (s2 < (T)1e-20) {
       Phi3 = 0; dP3_dS2 = 0; dP3_dV2[0] = dP3_dV2[1] = dP3_dV2[2] = 0;
     } else {

@@ -8,7 +8,8 @@ parameter must agree to the precision of BF16 operands (2^-9 relative rounding o
 GEMM operand, FP32 accumulation). Forward, that is 1e-2 on the loss; backward, the
 rounding of activations and gradients compounds through the six GEMM layers of the chain
 (the lift weights, deepest in it, come out ~4% off in norm), so each gradient must lie
-within 6e-2 of the FP64 gradient's norm and point the same way (cosine >= 0.998)."""
+within 6e-2 of the FP64 gradient's norm and point the same way (cosine >= 0.998); the
+output bias's one live entry, a sum of terms of both signs, within 2e-2 of their size."""
 import math
 
 import numpy as np
@@ -81,6 +82,12 @@ def test_fno_gradients_match_fp64_cpu_network():
     for gpu, cpu in pairs:
         a = gpu.grad.double().cpu()
         b = cpu.grad
+        if gpu is model.p2_b:
+            # one live entry, 2 mean(out - target): a sum of terms of both signs, so its
+            # error is judged against the size of the terms, 2 mean|out - target|
+            scale = 2 * float(torch.mean(torch.abs(out64 - target.double().cpu())))
+            assert abs(float(a[0] - b[0])) <= 2e-2 * scale and float(torch.abs(a[1:]).max()) == 0.0
+            continue
         rel = float(torch.linalg.norm(a - b) / max(float(torch.linalg.norm(b)), 1e-300))
         cos = float(torch.sum(a * b) / max(float(torch.linalg.norm(a) * torch.linalg.norm(b)), 1e-300))
         assert rel <= 6e-2 and cos >= 0.998, (tuple(gpu.shape), rel, cos)
