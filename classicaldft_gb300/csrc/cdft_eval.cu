@@ -91,23 +91,46 @@ std::shared_ptr<FFTTable> make_fft_table(int n, std::string* err, const std::vec
     len = sub;
   }
   const size_t cnt = re.size();
-  // the FP64 table, then the same twiddles as df64 pairs (hi, lo of the real part, hi, lo
-  // of the imaginary part), which the FP64 transforms of the compile-time plans read
-  std::vector<double2> h64(2 * cnt);
+  // the FP64 table, then, for the compile-time lengths, the twiddles of the df64
+  // transforms' radix order (fxd_radix) as df64 pairs (hi, lo of the real part, hi, lo of
+  // the imaginary part), in the same entry layout
+  std::vector<long double> dre, dim;
+  if (n == 128 || n == 256) {
+    int dlen = n;
+    for (int st = 0; fxd_radix(n, st) != 0; ++st) {
+      const int p = fxd_radix(n, st), sub = dlen / p;
+      for (int q = 0; q < sub; ++q)
+        for (int tt = 0; tt < p; ++tt) {
+          const long double a = 6.283185307179586476925286766559005768L * (long double)(((long)q * tt) % dlen) / (long double)dlen;
+          dre.push_back(cosl(a));
+          dim.push_back(-sinl(a));
+        }
+      for (int tt = 0; tt < p; ++tt) {
+        const long double a = 6.283185307179586476925286766559005768L * (long double)tt / (long double)p;
+        dre.push_back(cosl(a));
+        dim.push_back(-sinl(a));
+      }
+      dlen = sub;
+    }
+  }
+  const size_t dcnt = dre.size();
+  std::vector<double2> h64(cnt + dcnt);
   std::vector<float2> h32(cnt);
   for (size_t i = 0; i < cnt; ++i) {
     h64[i] = make_double2((double)re[i], (double)im[i]);
     h32[i] = make_float2((float)re[i], (float)im[i]);
-    const float rh = (float)re[i], ih = (float)im[i];
-    const float rl = (float)(re[i] - (long double)rh), il = (float)(im[i] - (long double)ih);
+  }
+  for (size_t i = 0; i < dcnt; ++i) {
+    const float rh = (float)dre[i], ih = (float)dim[i];
+    const float rl = (float)(dre[i] - (long double)rh), il = (float)(dim[i] - (long double)ih);
     float4 q = make_float4(rh, rl, ih, il);
     std::memcpy(&h64[cnt + i], &q, sizeof(q));
   }
-  if (cudaMalloc(&t->d64, 2 * cnt * sizeof(double2)) != cudaSuccess || cudaMalloc(&t->d32, cnt * sizeof(float2)) != cudaSuccess) {
+  if (cudaMalloc(&t->d64, (cnt + dcnt) * sizeof(double2)) != cudaSuccess || cudaMalloc(&t->d32, cnt * sizeof(float2)) != cudaSuccess) {
     if (err) *err = "cudaMalloc of FFT tables failed";
     return nullptr;
   }
-  cudaMemcpy(t->d64, h64.data(), 2 * cnt * sizeof(double2), cudaMemcpyHostToDevice);
+  cudaMemcpy(t->d64, h64.data(), (cnt + dcnt) * sizeof(double2), cudaMemcpyHostToDevice);
   cudaMemcpy(t->d32, h32.data(), cnt * sizeof(float2), cudaMemcpyHostToDevice);
   return t;
 }

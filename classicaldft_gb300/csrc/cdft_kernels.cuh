@@ -117,6 +117,16 @@ struct KahanT {
   }
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
+// FP64 per-thread partials are plain sums: a thread adds only a few dozen terms (its
+// rounding error stays near 1e-15 of them), the merges across threads and blocks are the
+// compensated ones, and each Kahan step costs three more instructions of GB300's small
+// FP64 pipe.
+template <>
+struct KahanT<double> {
+  double s = 0, c = 0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double value() const { return s; }
+};
 
 // Block-wide merge of NV per-thread Kahan partials, stored like block_sum_store.
 // FP32 partials merge across the warp in FP32 with error-free sums (Knuth's
