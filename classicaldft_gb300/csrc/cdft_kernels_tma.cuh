@@ -346,6 +346,42 @@ template <class T> struct ElemsPerComplex;
 template <> struct ElemsPerComplex<float> { static constexpr int value = 1; };
 template <> struct ElemsPerComplex<double> { static constexpr int value = 2; };
 
+// The x passes' transforms. In FP64 with a compile-time plan they run in df64 and may
+// leave (OUT_D = false) or take (IN_D = false) df64 values, so that the products with
+// the weights happen in df64 too and no join / split pair surrounds them; XReg is the
+// type a thread holds such values in.
+template <int DIR, class T, int TC, int NF, bool IN_D, bool OUT_D>
+__device__ __forceinline__ typename Cx<T>::type* xfft(typename Cx<T>::type* b0, typename Cx<T>::type* b1, const FFTPlan& P,
+                                                      const typename Cx<T>::type* __restrict__ tw) {
+  if constexpr (kDf64Transforms && std::is_same<T, double>::value && NF > 0)
+    return tile_fft_fixed_df<DIR, TC, TC, NF, 256, IN_D, OUT_D>(b0, b1, reinterpret_cast<const dfc*>(tw + fx_table_len(NF)));
+  else
+    return tfft<DIR, T, TC, TC, NF>(b0, b1, P, tw);
+}
+template <class T, int NF> struct XReg {
+  static constexpr bool df = kDf64Transforms && std::is_same<T, double>::value && NF > 0;
+  typedef typename std::conditional<df, dfc, typename Cx<T>::type>::type C;  // a complex value
+  typedef typename std::conditional<df, dfs, T>::type W;                      // a weight
+  __device__ static W weight(T w) {
+    if constexpr (df) return dfs_split((double)w);
+    else return w;
+  }
+  __device__ static C zero() {
+    C z;
+    if constexpr (df) z.x = z.y = dfs(0);
+    else z.x = z.y = (T)0;
+    return z;
+  }
+  __device__ static T re(const C& z) {
+    if constexpr (df) return (T)dfs_join(z.x);
+    else return z.x;
+  }
+  __device__ static T im(const C& z) {
+    if constexpr (df) return (T)dfs_join(z.y);
+    else return z.y;
+  }
+};
+
 // ---------------------------------------------------------------- y pass ---
 // Work item = (field f, plane x, column tile t): the tile [ny][TC] at kz0 = t*TC.
 // Tensor map (4D, 8-byte elements): {pz*E, ny, nx, nfield}.
@@ -459,12 +495,14 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
     if (threadIdx.x == 0) bulk_wait_all();
     return;
   }
-  C* res = tfft<-1, T, TC, TC, NF>(X, Y, px, tw);
-  C R[PER];
+  typedef XReg<T, NF> XR;
+  typedef typename XR::C RC;
+  C* res = xfft<-1, T, TC, NF, true, false>(X, Y, px, tw);
+  RC R[PER];
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int e = threadIdx.x + j * 256;
-    if (e < nel) R[j] = res[e];
+    if (e < nel) R[j] = reinterpret_cast<const RC*>(res)[e];
   }
   C* prev = nullptr;  // the buffer the last tensor store reads
   for (int a = 0; a < M; ++a) {
@@ -479,7 +517,7 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
       const int e = threadIdx.x + j * 256;
-      if (e < nel) in[e] = mul_weight(R[j], Wst[b][e], odd);
+      if (e < nel) reinterpret_cast<RC*>(in)[e] = mul_weight(R[j], XR::weight(Wst[b][e]), odd);
     }
     if (threadIdx.x == 0) bulk_wait_read();
     __syncthreads();
@@ -487,7 +525,7 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
       mbar_arrive_expect_tx(&bar[b], (unsigned)wbytes);
       tma_load_3d(Wst[b], &mapW, col0, 0, a + 2, &bar[b]);
     }
-    C* r2 = tfft<+1, T, TC, TC, NF>(in, other, px, tw);
+    C* r2 = xfft<+1, T, TC, NF, false, true>(in, other, px, tw);
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -541,31 +579,34 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
   };
   if (threadIdx.x == 0)
     for (int b = 0; b < 2 && b < nsrc; ++b) issue(b, b);
-  C S[PER];
+  typedef XReg<T, NF> XR;
+  typedef typename XR::C RC;
+  RC S[PER];
 #pragma unroll
-  for (int j = 0; j < PER; ++j) S[j] = mk<T>(0, 0);
+  for (int j = 0; j < PER; ++j) S[j] = XR::zero();
   KahanT<T> pars;  // the mean-field energy by Parseval: compensated in the bulk precision, merged in FP64
   bool ok = true;
   for (int a = 0; a < nsrc; ++a) {
     const int b = a & 1;
     ok = mbar_wait(&bar[b], (unsigned)((a >> 1) & 1), status);
     if (!__syncthreads_and(ok)) break;
-    C* res = tfft<-1, T, TC, TC, NF>(Dst[b], Y, px, tw);
+    C* res = xfft<-1, T, TC, NF, true, false>(Dst[b], Y, px, tw);
     const bool is_mf = (a == M);
     const bool odd = !is_mf && weight_is_odd(a);
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
       const int e = threadIdx.x + j * 256;
       if (e < nel) {
-        const C z = res[e];
+        const RC z = reinterpret_cast<const RC*>(res)[e];
         const T wv = Wst[b][e];
-        S[j] = cadd(S[j], mul_weight(z, wv, odd));
+        S[j] = cadd(S[j], mul_weight(z, XR::weight(wv), odd));
         if (is_mf) {
           const int col = col0 + (e % TC);
           const int kz = col % d.pz;
           if (kz < d.nzc && col < d.ny * d.pz) {
             const T mult = (kz == 0 || 2 * kz == d.nz) ? (T)1 : (T)2;
-            pars.add(mult * (z.x * z.x + z.y * z.y) * wv);
+            const T zx = XR::re(z), zy = XR::im(z);
+            pars.add(mult * (zx * zx + zy * zy) * wv);
           }
         }
       }
@@ -582,9 +623,9 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int e = threadIdx.x + j * 256;
-    if (e < nel) X[e] = S[j];
+    if (e < nel) reinterpret_cast<RC*>(X)[e] = S[j];
   }
-  C* r2 = tfft<+1, T, TC, TC, NF>(X, Y, px, tw);
+  C* r2 = xfft<+1, T, TC, NF, false, true>(X, Y, px, tw);
   fence_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
