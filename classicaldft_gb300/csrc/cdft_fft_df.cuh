@@ -1,0 +1,174 @@
+// FP64 transforms in double-float (df64) arithmetic on the FP32 pipe (cdft_df64.cuh),
+// for the compile-time plans (128- and 256-point axes): the first stage of a transform
+// reads doubles and splits them, the stages between keep df64 values in the tile (16
+// bytes, as a double2), the last stage joins them back into doubles; IN_D / OUT_D = false
+// leave the values in df64 for a caller that keeps computing in df64. Used by the tile
+// passes (cdft_kernels_tma.cuh) and the row passes (cdft_kernels.cuh) in FP64.
+#pragma once
+#include <cuda_runtime.h>
+#include "cdft_df64.cuh"
+#include "cdft_fft.cuh"
+
+namespace cdft {
+
+// FP64 transforms of the compile-time plans run in df64 (tile and row passes)
+constexpr bool kDf64Transforms = true;
+
+// The df64 transforms take their own radix order for power-of-two lengths: radix-4
+// stages, with a final radix-8 when the exponent is odd (128 = 4 4 8, 256 = 4 4 4 4).
+// A tile of 8 FP64 columns gives a radix-8 stage only half as many butterflies as
+// threads; last, its twiddles are all 1, so the idle half waits for the cheapest stage.
+// Its twiddle table (same entry layout) follows the FP64 table of the default order.
+__host__ __device__ constexpr int fxd_radix(int n, int i) {
+  int m = n;
+  for (int st = 0; m > 1; ++st) {
+    int a = 0;
+    while ((1 << (a + 1)) <= m) ++a;
+    const int f = a == 3 ? 8 : (a >= 2 ? 4 : 2);
+    if (st == i) return f;
+    m /= f;
+  }
+  return 0;
+}
+__host__ __device__ constexpr int fxd_len(int n, int i) {
+  int len = n;
+  for (int st = 0; st < i; ++st) len /= fxd_radix(n, st);
+  return len;
+}
+__host__ __device__ constexpr int fxd_twoff(int n, int i) {
+  int off = 0, len = n;
+  for (int st = 0; st < i; ++st) {
+    const int p = fxd_radix(n, st);
+    off += len + p;
+    len /= p;
+  }
+  return off;
+}
+__host__ __device__ constexpr int fxd_table_len(int n) {
+  int st = 0;
+  while (fxd_radix(n, st) != 0) ++st;
+  return fxd_twoff(n, st);
+}
+
+// a df64 twiddle from the plan's table staged in shared memory
+__device__ __forceinline__ dfc ld_twiddle(const float4* p) {
+  const float4 v = *p;
+  dfc r;
+  r.x = dfs(v.x, v.y);
+  r.y = dfs(v.z, v.w);
+  return r;
+}
+
+template <int DIR, int P, int TC, bool UNIT, bool IN_D, bool OUT_D>
+__device__ __forceinline__ void tile_butterfly_df(const void* __restrict__ xv, void* __restrict__ yv, int c, int q, int k, int m, int s,
+                                                  const float4* __restrict__ tw) {
+  dfc a[P];
+#pragma unroll
+  for (int j = 0; j < P; ++j) {
+    const int idx = (k + s * (q + m * j)) * TC + c;
+    if constexpr (IN_D) a[j] = dfc_split(reinterpret_cast<const double2*>(xv)[idx]);
+    else a[j] = reinterpret_cast<const dfc*>(xv)[idx];
+  }
+  if constexpr (P == 8) dft8<DIR, dfs>(a);
+  else if constexpr (P == 4) dft4<DIR>(a);
+  else dft2<DIR>(a);
+  const float4* twq = tw + q * P;
+#pragma unroll
+  for (int t = 0; t < P; ++t) {
+    const dfc v = (UNIT || t == 0) ? a[t] : cmul_dir<DIR>(a[t], ld_twiddle(twq + t));
+    const int idx = (k + s * (P * q + t)) * TC + c;
+    if constexpr (OUT_D) reinterpret_cast<double2*>(yv)[idx] = dfc_join(v);
+    else reinterpret_cast<dfc*>(yv)[idx] = v;
+  }
+}
+
+// (no unrolling of the item loop: a df64 butterfly is ~12x the instructions of an FP64
+// one, and unrolled copies of every stage overflowed the instruction cache)
+template <int DIR, int TC, int PITCH, int NF, int ST, int NTH, bool IN_D, bool OUT_D>
+__device__ __forceinline__ void fx_stage_df(const void* __restrict__ src, void* __restrict__ dst, const float4* __restrict__ tws) {
+  constexpr int p = fxd_radix(NF, ST), len = fxd_len(NF, ST), m = len / p, s = NF / len;
+  constexpr int items = TC * (NF / p);
+  constexpr bool first = IN_D && ST == 0, last = OUT_D && fxd_radix(NF, ST + 1) == 0;
+  static_assert(p == 2 || p == 4 || p == 8, "df64 stages take radices 2, 4 and 8");
+  const float4* tw = tws + fxd_twoff(NF, ST);
+#pragma unroll 1
+  for (int w = threadIdx.x; w < items; w += NTH) {
+    const int c = w % TC, u = w / TC;
+    const int q = u / s, k = u % s;
+    tile_butterfly_df<DIR, p, PITCH, m == 1, first, last>(src, dst, c, q, k, m, s, tw);
+  }
+}
+
+template <int DIR, int TC, int PITCH, int NF, int NTH, bool IN_D, bool OUT_D, int ST = 0>
+__device__ __forceinline__ double2* tile_fft_fixed_df_stages(double2* b0, double2* b1, const float4* __restrict__ tws) {
+  __syncthreads();
+  if constexpr (fxd_radix(NF, ST) == 0) {
+    return b0;
+  } else {
+    fx_stage_df<DIR, TC, PITCH, NF, ST, NTH, IN_D, OUT_D>(b0, b1, tws);
+    return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D, ST + 1>(b1, b0, tws);
+  }
+}
+// Each call stages the plan's df64 twiddles (fxd_table_len(NF) entries, 2.7 KB for 128
+// points) in shared memory first: read by every butterfly, they made the texture path
+// the bottleneck when fetched from global memory. The previous call ended on a barrier,
+// so the copy cannot overwrite twiddles still in use. IN_D / OUT_D: the tile holds
+// doubles on entry / exit (else df64 values, for a caller that keeps them).
+template <int DIR, int TC, int PITCH, int NF, int NTH, bool IN_D = true, bool OUT_D = true>
+__device__ __forceinline__ double2* tile_fft_fixed_df(double2* b0, double2* b1, const dfc* __restrict__ twdf) {
+  constexpr int NT = fxd_table_len(NF);
+  __shared__ float4 tws[NT];
+  for (int i = threadIdx.x; i < NT; i += NTH) tws[i] = __ldg(reinterpret_cast<const float4*>(twdf) + i);
+  return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D>(b0, b1, tws);
+}
+
+
+// The same transform on RB rows of length NF held line-contiguously (row r at r * LP),
+// the layout of the row passes.
+template <int DIR, int NF, int NTH, bool IN_D, bool OUT_D, int ST = 0>
+__device__ __forceinline__ double2* rows_fft_df_stages(double2* b0, double2* b1, int L, int LP, const float4* __restrict__ tws) {
+  __syncthreads();
+  if constexpr (fxd_radix(NF, ST) == 0) {
+    return b0;
+  } else {
+    constexpr int p = fxd_radix(NF, ST), len = fxd_len(NF, ST), m = len / p, s = NF / len, per_line = NF / p;
+    constexpr bool first = IN_D && ST == 0, last = OUT_D && fxd_radix(NF, ST + 1) == 0;
+    const float4* tw = tws + fxd_twoff(NF, ST);
+#pragma unroll 1
+    for (int w = threadIdx.x; w < L * per_line; w += NTH) {
+      const int line = w / per_line, u = w - line * per_line;
+      const int q = u / s, k = u % s;
+      tile_butterfly_df<DIR, p, 1, m == 1, first, last>(b0 + (long)line * LP, b1 + (long)line * LP, 0, q, k, m, s, tw);
+    }
+    return rows_fft_df_stages<DIR, NF, NTH, IN_D, OUT_D, ST + 1>(b1, b0, L, LP, tws);
+  }
+}
+template <int DIR, int NF, int NTH, bool IN_D = true, bool OUT_D = true>
+__device__ __forceinline__ double2* rows_fft_df(double2* b0, double2* b1, int L, int LP, const dfc* __restrict__ twdf) {
+  constexpr int NT = fxd_table_len(NF);
+  __shared__ float4 tws[NT];
+  for (int i = threadIdx.x; i < NT; i += NTH) tws[i] = __ldg(reinterpret_cast<const float4*>(twdf) + i);
+  return rows_fft_df_stages<DIR, NF, NTH, IN_D, OUT_D>(b0, b1, L, LP, tws);
+}
+
+// offset of the df64 twiddles after the FP64 table of the default plan of length n
+__host__ __device__ constexpr int df_table_offset(int n) {
+  int st = 0;
+  while (radix_at(n, st) != 0) ++st;
+  return twoff_at(n, st);
+}
+
+// The row passes' transform: in df64 for FP64 with a compile-time plan, else block_fft_nf.
+template <int DIR, class T, int NF>
+__device__ __forceinline__ typename Cx<T>::type* rows_fft(typename Cx<T>::type* b0, typename Cx<T>::type* b1, int L, int LP, const FFTPlan& P,
+                                                          const typename Cx<T>::type* __restrict__ table) {
+  if constexpr (kDf64Transforms && NF > 0 && sizeof(T) == 8) {
+    double2* r = rows_fft_df<DIR, NF, 256>(b0, b1, L, LP, reinterpret_cast<const dfc*>(table + df_table_offset(NF)));
+    __syncthreads();
+    return r;
+  } else {
+    return block_fft_nf<DIR, T, NF>(b0, b1, L, LP, P, table);
+  }
+}
+
+}  // namespace cdft

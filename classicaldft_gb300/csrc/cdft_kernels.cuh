@@ -20,6 +20,7 @@
 //   final_rows   E, rho -> dF (f64)         z-axis c2r + ideal/external terms
 #pragma once
 #include "cdft_fft.cuh"
+#include "cdft_fft_df.cuh"
 #include "cdft_phi.cuh"
 #include "cdft_convert.cuh"
 
@@ -240,7 +241,7 @@ __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, ty
     if (rb < d.rows) vb = conv<T>(in[rb * nz + k]);
     b0[r * LP + k] = mk<T>(va, vb);
   }
-  C* res = block_fft_nf<-1, T, NF>(b0, b1, RB, LP, pz, tw);
+  C* res = rows_fft<-1, T, NF>(b0, b1, RB, LP, pz, tw);
   const int nzc = NF > 0 ? NF / 2 + 1 : d.nzc;
   for (int e = threadIdx.x; e < RB * nzc; e += blockDim.x) {
     const int r = e / nzc, k = e - r * nzc;
@@ -291,7 +292,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r(const typename Cx<T>::type* __
     const C* B = rb < d.rows ? in + rb * d.pz : nullptr;
     b0[r * LP + k] = pair_spectrum<T>(A, B, k, nz);
   }
-  C* res = block_fft_nf<+1, T, NF>(b0, b1, RB, LP, pz, tw);
+  C* res = rows_fft<+1, T, NF>(b0, b1, RB, LP, pz, tw);
   for (int e = threadIdx.x; e < RB * nz; e += blockDim.x) {
     const int r = e / nz, k = e - r * nz;
     const long ra = 2 * (pair0 + r), rb = ra + 1;
@@ -604,7 +605,7 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
       const C* Br = rb < d.rows ? E + rb * d.pz : nullptr;
       b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
-    res = block_fft_nf<+1, T, NF>(b0, b1, RB, LP, pz, tw);
+    res = rows_fft<+1, T, NF>(b0, b1, RB, LP, pz, tw);
   }
   const T dVt = (T)dV;
   for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
@@ -651,7 +652,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
       const C* Br = rb < d.rows ? E + rb * d.pz : nullptr;
       b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
-    res = block_fft_nf<+1, T, NF>(b0, b1, RB, LP, pz, tw);
+    res = rows_fft<+1, T, NF>(b0, b1, RB, LP, pz, tw);
   }
   // Pointwise terms in the bulk precision T (FP64 in FP64 mode); each thread
   // keeps Kahan partials in T over its few points, merged in FP64 across the

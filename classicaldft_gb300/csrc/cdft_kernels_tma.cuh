@@ -9,7 +9,7 @@
 // leave through tensor stores from shared memory.
 #pragma once
 #include <type_traits>
-#include "cdft_df64.cuh"
+#include "cdft_fft_df.cuh"
 #include "cdft_kernels.cuh"
 #include "cdft_tma.cuh"
 
@@ -197,126 +197,13 @@ __device__ __forceinline__ typename Cx<T>::type* tile_fft_fixed(typename Cx<T>::
   }
 }
 
-// ---- FP64 transforms in df64 arithmetic (cdft_df64.cuh), compile-time plans: the
-// first stage reads doubles and splits them, the stages between keep df64 values in
-// the tile (16 bytes, as a double2), the last stage joins them back into doubles.
-// The df64 twiddles follow the plan's FP64 table (fx_table_len entries further on).
+// ---- FP64 transforms in df64 arithmetic: cdft_fft_df.cuh.
 __host__ __device__ constexpr int fx_nstages(int n) {
   int st = 0;
   while (fx_radix(n, st) != 0) ++st;
   return st;
 }
 __host__ __device__ constexpr int fx_table_len(int n) { return fx_twoff(n, fx_nstages(n)); }
-// The df64 transforms take their own radix order for power-of-two lengths: radix-4
-// stages, with a final radix-8 when the exponent is odd (128 = 4 4 8, 256 = 4 4 4 4).
-// A tile of 8 FP64 columns gives a radix-8 stage only half as many butterflies as
-// threads; last, its twiddles are all 1, so the idle half waits for the cheapest stage.
-// Its twiddle table (same entry layout) follows the FP64 table of the default order.
-__host__ __device__ constexpr int fxd_radix(int n, int i) {
-  int m = n;
-  for (int st = 0; m > 1; ++st) {
-    int a = 0;
-    while ((1 << (a + 1)) <= m) ++a;
-    const int f = a == 3 ? 8 : (a >= 2 ? 4 : 2);
-    if (st == i) return f;
-    m /= f;
-  }
-  return 0;
-}
-__host__ __device__ constexpr int fxd_len(int n, int i) {
-  int len = n;
-  for (int st = 0; st < i; ++st) len /= fxd_radix(n, st);
-  return len;
-}
-__host__ __device__ constexpr int fxd_twoff(int n, int i) {
-  int off = 0, len = n;
-  for (int st = 0; st < i; ++st) {
-    const int p = fxd_radix(n, st);
-    off += len + p;
-    len /= p;
-  }
-  return off;
-}
-__host__ __device__ constexpr int fxd_table_len(int n) {
-  int st = 0;
-  while (fxd_radix(n, st) != 0) ++st;
-  return fxd_twoff(n, st);
-}
-
-// a df64 twiddle from the plan's table staged in shared memory
-__device__ __forceinline__ dfc ld_twiddle(const float4* p) {
-  const float4 v = *p;
-  dfc r;
-  r.x = dfs(v.x, v.y);
-  r.y = dfs(v.z, v.w);
-  return r;
-}
-
-template <int DIR, int P, int TC, bool UNIT, bool IN_D, bool OUT_D>
-__device__ __forceinline__ void tile_butterfly_df(const void* __restrict__ xv, void* __restrict__ yv, int c, int q, int k, int m, int s,
-                                                  const float4* __restrict__ tw) {
-  dfc a[P];
-#pragma unroll
-  for (int j = 0; j < P; ++j) {
-    const int idx = (k + s * (q + m * j)) * TC + c;
-    if constexpr (IN_D) a[j] = dfc_split(reinterpret_cast<const double2*>(xv)[idx]);
-    else a[j] = reinterpret_cast<const dfc*>(xv)[idx];
-  }
-  if constexpr (P == 8) dft8<DIR, dfs>(a);
-  else if constexpr (P == 4) dft4<DIR>(a);
-  else dft2<DIR>(a);
-  const float4* twq = tw + q * P;
-#pragma unroll
-  for (int t = 0; t < P; ++t) {
-    const dfc v = (UNIT || t == 0) ? a[t] : cmul_dir<DIR>(a[t], ld_twiddle(twq + t));
-    const int idx = (k + s * (P * q + t)) * TC + c;
-    if constexpr (OUT_D) reinterpret_cast<double2*>(yv)[idx] = dfc_join(v);
-    else reinterpret_cast<dfc*>(yv)[idx] = v;
-  }
-}
-
-// (no unrolling of the item loop: a df64 butterfly is ~12x the instructions of an FP64
-// one, and unrolled copies of every stage overflowed the instruction cache)
-template <int DIR, int TC, int PITCH, int NF, int ST, int NTH, bool IN_D, bool OUT_D>
-__device__ __forceinline__ void fx_stage_df(const void* __restrict__ src, void* __restrict__ dst, const float4* __restrict__ tws) {
-  constexpr int p = fxd_radix(NF, ST), len = fxd_len(NF, ST), m = len / p, s = NF / len;
-  constexpr int items = TC * (NF / p);
-  constexpr bool first = IN_D && ST == 0, last = OUT_D && fxd_radix(NF, ST + 1) == 0;
-  static_assert(p == 2 || p == 4 || p == 8, "df64 stages take radices 2, 4 and 8");
-  const float4* tw = tws + fxd_twoff(NF, ST);
-#pragma unroll 1
-  for (int w = threadIdx.x; w < items; w += NTH) {
-    const int c = w % TC, u = w / TC;
-    const int q = u / s, k = u % s;
-    tile_butterfly_df<DIR, p, PITCH, m == 1, first, last>(src, dst, c, q, k, m, s, tw);
-  }
-}
-
-template <int DIR, int TC, int PITCH, int NF, int NTH, bool IN_D, bool OUT_D, int ST = 0>
-__device__ __forceinline__ double2* tile_fft_fixed_df_stages(double2* b0, double2* b1, const float4* __restrict__ tws) {
-  __syncthreads();
-  if constexpr (fxd_radix(NF, ST) == 0) {
-    return b0;
-  } else {
-    fx_stage_df<DIR, TC, PITCH, NF, ST, NTH, IN_D, OUT_D>(b0, b1, tws);
-    return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D, ST + 1>(b1, b0, tws);
-  }
-}
-// Each call stages the plan's df64 twiddles (fxd_table_len(NF) entries, 2.7 KB for 128
-// points) in shared memory first: read by every butterfly, they made the texture path
-// the bottleneck when fetched from global memory. The previous call ended on a barrier,
-// so the copy cannot overwrite twiddles still in use. IN_D / OUT_D: the tile holds
-// doubles on entry / exit (else df64 values, for a caller that keeps them).
-template <int DIR, int TC, int PITCH, int NF, int NTH, bool IN_D = true, bool OUT_D = true>
-__device__ __forceinline__ double2* tile_fft_fixed_df(double2* b0, double2* b1, const dfc* __restrict__ twdf) {
-  constexpr int NT = fxd_table_len(NF);
-  __shared__ float4 tws[NT];
-  for (int i = threadIdx.x; i < NT; i += NTH) tws[i] = __ldg(reinterpret_cast<const float4*>(twdf) + i);
-  return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D>(b0, b1, tws);
-}
-
-// FP64 tiles of the compile-time plans transform in df64 (see above)
-constexpr bool kDf64Transforms = true;
 
 // The transform of a tile: the compile-time plan when NF > 0 (launched only
 // when the runtime plan is that default plan of length NF), else the runtime plan.

@@ -8,8 +8,9 @@ parameter must agree to the precision of BF16 operands (2^-9 relative rounding o
 GEMM operand, FP32 accumulation). Forward, that is 1e-2 on the loss; backward, the
 rounding of activations and gradients compounds through the six GEMM layers of the chain
 (the lift weights, deepest in it, come out ~4% off in norm), so each gradient must lie
-within 6e-2 of the FP64 gradient's norm and point the same way (cosine >= 0.998); the
-output bias's one live entry, a sum of terms of both signs, within 2e-2 of their size."""
+within 6e-2 of the FP64 gradient's norm (0.15 for the bias vectors, sums over all points
+of terms of both signs) and point the same way (cosine >= 0.998); the output bias's one
+live entry within 2e-2 of the size of its terms."""
 import math
 
 import numpy as np
@@ -90,4 +91,7 @@ def test_fno_gradients_match_fp64_cpu_network():
             continue
         rel = float(torch.linalg.norm(a - b) / max(float(torch.linalg.norm(b)), 1e-300))
         cos = float(torch.sum(a * b) / max(float(torch.linalg.norm(a) * torch.linalg.norm(b)), 1e-300))
-        assert rel <= 6e-2 and cos >= 0.998, (tuple(gpu.shape), rel, cos)
+        # a bias gradient is a sum over all points of terms of both signs, so its norm
+        # carries the cancellation of those sums: its direction is the sharper check
+        bar = 0.15 if gpu.dim() == 1 else 6e-2
+        assert rel <= bar and cos >= 0.998, (tuple(gpu.shape), rel, cos)
