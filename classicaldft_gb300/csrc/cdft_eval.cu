@@ -389,10 +389,11 @@ bool Evaluator<T>::setup_tma(std::string* err) {
       ok = ok && encode_map(&mapWatt_, (int)sizeof(T), watt_, 3, wd, ws, wb);
     }
   }
+  constexpr int TCY = TileColsY<T>::value;
   {  // y-pass maps: {pz*E, ny, nx, fields}
     uint64_t dims[4] = {(uint64_t)pz_ * E, (uint64_t)ny_, (uint64_t)nx_, 1};
     uint64_t str[3] = {(uint64_t)pz_ * cb, (uint64_t)ny_ * pz_ * cb, (uint64_t)Nc_ * cb};
-    uint32_t box[4] = {(uint32_t)(TC * E), (uint32_t)ny_, 1, 1};
+    uint32_t box[4] = {(uint32_t)(TCY * E), (uint32_t)ny_, 1, 1};
     ok = ok && encode_map(&mapYA_, 8, A_, 4, dims, str, box);
     ok = ok && encode_map(&mapYE_, 8, E_, 4, dims, str, box);
     if (M_ > 0) {
@@ -401,7 +402,7 @@ bool Evaluator<T>::setup_tma(std::string* err) {
     }
   }
   if (!ok) return false;
-  const size_t tile_x = r128((size_t)nx_ * TC * sizeof(C)), tile_y = r128((size_t)ny_ * TC * sizeof(C)),
+  const size_t tile_x = r128((size_t)nx_ * TC * sizeof(C)), tile_y = r128((size_t)ny_ * TCY * sizeof(C)),
                wt = r128((size_t)nx_ * TC * sizeof(T));
   smem_ty_ = 3 * tile_y + 1024;
   smem_tconv_ = 2 * tile_x + 2 * wt + 1024;
@@ -424,7 +425,7 @@ bool Evaluator<T>::setup_tma(std::string* err) {
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cols_y_tma<T, -1, 0>, 256, smem_ty_);
   bps = std::max(bps, 1);
-  const long ntile = (nzc_ + TC - 1) / TC;
+  const long ntile = (nzc_ + TCY - 1) / TCY;
   grid_ty1_ = (int)std::min<long>((long)nx_ * ntile, (long)nsm * bps);
   grid_tyM_ = (int)std::min<long>((long)std::max(M_, 1) * nx_ * ntile, (long)nsm * bps);
   tma_ = true;

@@ -220,6 +220,9 @@ __device__ __forceinline__ typename Cx<T>::type* tfft(typename Cx<T>::type* b0, 
 template <class T> struct TileCols;
 template <> struct TileCols<float> { static constexpr int value = 16; };
 template <> struct TileCols<double> { static constexpr int value = 8; };
+// the y pass's tiles: 16 columns in both precisions (256-byte FP64 rows), so that every
+// stage of a df64 transform has a butterfly for each of the 256 threads
+template <class T> struct TileColsY { static constexpr int value = 16; };
 // rows per group of the fused Phi kernel
 template <class T> struct PhiRows;
 template <> struct PhiRows<float> { static constexpr int value = 4; };
@@ -276,7 +279,7 @@ template <class T, int DIR, int NF = 0>
 __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUtensorMap map, Dims d, FFTPlan P,
                                                     const typename Cx<T>::type* __restrict__ tw, int nfield, unsigned* __restrict__ status) {
   typedef typename Cx<T>::type C;
-  constexpr int TC = TileCols<T>::value, E = ElemsPerComplex<T>::value;
+  constexpr int TC = TileColsY<T>::value, E = ElemsPerComplex<T>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned char* sm = aligned_smem(smem_raw);
   const int n = P.n;
