@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # formulas cancel heavily near the sphere surface, and contracting a*b+c (the
 # default of GCC on aarch64) moves the weights by up to ~1e-5 relative.
 CUFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-O3"]
-SOURCES = ["cdft_eval.cu", "cdft_api.cu", "cdft_setup.cpp", "cdft_noalloc.cu", "cdft_fire_dev.cu", "cdft_tune.cu", "cdft_newton.cu", "cdft_tc_gemm.cu", "cdft_files.cpp", "cdft_spectral.cu"]
+SOURCES = ["cdft_eval.cu", "cdft_phi_rosenfeld.cu", "cdft_phi_rslt.cu", "cdft_phi_esfmt.cu", "cdft_phi_wbi.cu", "cdft_phi_wbii.cu", "cdft_api.cu", "cdft_setup.cpp", "cdft_noalloc.cu", "cdft_fire_dev.cu", "cdft_tune.cu", "cdft_newton.cu", "cdft_tc_gemm.cu", "cdft_files.cpp", "cdft_spectral.cu"]
 
 
 def _compile(src):

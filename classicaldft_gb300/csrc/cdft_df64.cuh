@@ -64,6 +64,9 @@ __device__ __forceinline__ dfs& operator+=(dfs& a, dfs b) { return a = a + b; }
 __device__ __forceinline__ dfs& operator-=(dfs& a, dfs b) { return a = a - b; }
 __device__ __forceinline__ dfs& operator*=(dfs& a, dfs b) { return a = a * b; }
 
+// a / 2, exact (both parts scaled by a power of two)
+__device__ __forceinline__ dfs df_half(dfs a) { return dfs(__fmul_rn(0.5f, a.h), __fmul_rn(0.5f, a.l)); }
+
 // double -> df64: hi = RN(d), lo = RN(d - hi); d - hi is exact in FP64
 __device__ __forceinline__ dfs dfs_split(double d) {
   const float h = cvt_f32(d);

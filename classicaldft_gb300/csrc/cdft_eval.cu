@@ -7,6 +7,7 @@
 #include "cdft_internal.h"
 #include "cdft_kernels.cuh"
 #include "cdft_kernels_tma.cuh"
+#include "cdft_phi_launch.h"
 
 namespace cdft {
 
@@ -33,6 +34,21 @@ inline void with_nf(int nf, F&& f) {
   if (nf == 128) f(std::integral_constant<int, 128>());
   else if (nf == 256) f(std::integral_constant<int, 256>());
   else f(std::integral_constant<int, 0>());
+}
+
+// with_nf, and whether the launch's spectra are double-float (f's second argument,
+// std::true_type only for FP64 with a compile-time plan and io set)
+template <class T, class F>
+inline void with_nf_io(int nf, bool io, F&& f) {
+  with_nf(nf, [&](auto nf_) {
+    constexpr int NF = decltype(nf_)::value;
+    if constexpr (kDf64Transforms && std::is_same<T, double>::value && NF > 0) {
+      if (io) f(nf_, std::true_type());
+      else f(nf_, std::false_type());
+    } else {
+      f(nf_, std::false_type());
+    }
+  });
 }
 
 std::vector<int> default_radices(int n) {
@@ -420,6 +436,16 @@ bool Evaluator<T>::setup_tma(std::string* err) {
   raise_smem(k_xconv_tma<T, 256>, smem_tconv_);
   raise_smem(k_xbackconv_tma<T, 128>, smem_tback_);
   raise_smem(k_xbackconv_tma<T, 256>, smem_tback_);
+  if constexpr (std::is_same<T, double>::value) {  // the double-float-spectra instances
+    raise_smem(k_cols_y_tma<T, -1, 128, true>, smem_ty_);
+    raise_smem(k_cols_y_tma<T, -1, 256, true>, smem_ty_);
+    raise_smem(k_cols_y_tma<T, +1, 128, true>, smem_ty_);
+    raise_smem(k_cols_y_tma<T, +1, 256, true>, smem_ty_);
+    raise_smem(k_xconv_tma<T, 128, true>, smem_tconv_);
+    raise_smem(k_xconv_tma<T, 256, true>, smem_tconv_);
+    raise_smem(k_xbackconv_tma<T, 128, true>, smem_tback_);
+    raise_smem(k_xbackconv_tma<T, 256, true>, smem_tback_);
+  }
   int nsm = 0, dev = 0, bps = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -445,43 +471,23 @@ bool Evaluator<T>::setup_phi_tma() {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const uint64_t cb = sizeof(C);
-  bool ok = false;
-  with_nf(fz_, [&](auto nf_) {
-    constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
-    const int L = phi_lines(M_, RB, PhiCross<T>::value);
-    uint64_t dims[3] = {(uint64_t)pz_ * E, (uint64_t)rows_, (uint64_t)M_};
-    uint64_t str[2] = {(uint64_t)pz_ * cb, (uint64_t)Nc_ * cb};
-    uint32_t box[3] = {(uint32_t)(pz_ * E), (uint32_t)RB, (uint32_t)M_};
-    smem_tphi_ = PhiBufs<T>::value * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L | 1) * cb) + 1024;
-    if (smem_tphi_ > 220 * 1024 || !encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) return;
-    auto set_phi = [&](auto kern) {
-      raise_smem(kern, smem_tphi_);
-      int b2 = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, kern, PhiThreads<T>::value, smem_tphi_);
-      return std::max(b2, 1);
-    };
-    int bp, bh;  // resident blocks per SM of the Phi and of the Hessian instances
-    switch (model_) {
-      case MODEL_ROSENFELD: bp = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiHess>); break;
-      case MODEL_RSLT: bp = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiHess>); break;
-      case MODEL_ESFMT: bp = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiHess>); break;
-      case MODEL_WHITEBEAR_I: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiHess>); break;
-      default: bp = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF>); bh = set_phi(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiHess>); break;
-    }
-    switch (model_) {  // the weighted-density store of the Hessian set-up runs on the Phi grid
-      case MODEL_ROSENFELD: raise_smem(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiStoreN>, smem_tphi_); break;
-      case MODEL_RSLT: raise_smem(k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiStoreN>, smem_tphi_); break;
-      case MODEL_ESFMT: raise_smem(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiStoreN>, smem_tphi_); break;
-      case MODEL_WHITEBEAR_I: raise_smem(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiStoreN>, smem_tphi_); break;
-      default: raise_smem(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiStoreN>, smem_tphi_); break;
-    }
-    const long ngroup = (rows_ + RB - 1) / RB;
-    grid_tphi_ = (int)std::min<long>(ngroup, (long)nsm * bp);
-    grid_thess_ = (int)std::min<long>(ngroup, (long)nsm * bh);
-    ok = true;
-  });
-  tma_phi_ = ok;
-  return ok;
+  const int nf = phi_nf();
+  const int RB = nf == 256 ? PhiRowsFor<T, 256>::value : PhiRowsFor<T, 128>::value;
+  static_assert(PhiRowsFor<T, 128>::value == PhiRowsFor<T, 0>::value, "the runtime-plan instance groups rows as the 128-point one");
+  const int L = phi_lines(M_, RB, PhiCross<T>::value);
+  uint64_t dims[3] = {(uint64_t)pz_ * E, (uint64_t)rows_, (uint64_t)M_};
+  uint64_t str[2] = {(uint64_t)pz_ * cb, (uint64_t)Nc_ * cb};
+  uint32_t box[3] = {(uint32_t)(pz_ * E), (uint32_t)RB, (uint32_t)M_};
+  smem_tphi_ = PhiBufs<T>::value * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L | 1) * cb) + 1024;
+  if (smem_tphi_ > 220 * 1024 || !encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) return false;
+  int blocks[4];  // resident blocks per SM of the Phi instances, by mode
+  with_model(model_, [&](auto m) { PhiLauncher<T, decltype(m)::value>::prepare_tma(nf, ao_, smem_tphi_, blocks); });
+  const long ngroup = (rows_ + RB - 1) / RB;
+  grid_tphi_ = (int)std::min<long>(ngroup, (long)nsm * blocks[kPhiEval]);
+  grid_thess_ = (int)std::min<long>(ngroup, (long)nsm * blocks[kPhiHess]);
+  grid_tao_ = (int)std::min<long>(ngroup, (long)nsm * blocks[kPhiAO]);
+  tma_phi_ = true;
+  return true;
 }
 
 template <class T>
@@ -527,32 +533,19 @@ int Evaluator<T>::enable_ao(double hsdp, double reservoir, const std::vector<dou
   CK(cudaMalloc(&psir_, N_ * sizeof(T)));
   gao_ = (int)std::min<long>((N_ + 255) / 256, 152 * 8);
   CK(cudaMalloc(&part_ao_, 2 * (size_t)gao_ * sizeof(double)));
-  int nsm = 0, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  with_nf(fz_, [&](auto nf_) {
-    constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
-    auto set_ao = [&](auto kern) {
-      raise_smem(kern, smem_tphi_);
-      int b = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, PhiThreads<T>::value, smem_tphi_);
-      return std::max(b, 1);
-    };
-    int b;
-    switch (model_) {
-      case MODEL_ROSENFELD: b = set_ao(k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiAO>); break;
-      case MODEL_RSLT: b = set_ao(k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiAO>); break;
-      case MODEL_ESFMT: b = set_ao(k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiAO>); break;
-      case MODEL_WHITEBEAR_I: b = set_ao(k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiAO>); break;
-      default: b = set_ao(k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiAO>); break;
-    }
-    grid_tao_ = (int)std::min<long>((rows_ + RB - 1) / RB, (long)nsm * b);
-  });
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
   ao_hp_ = hsdp;
   ao_res_ = reservoir;
   ao_ = true;
+  // the Phi pass again, now with its AO instance (and, in FP64, on FP64 spectra: the AO
+  // passes run the runtime-plan kernels, which do not take double-float spectra)
+  if (!setup_phi_tma()) {
+    ao_ = false;
+    setup_phi_tma();  // back to the pass without the AO model
+    if (err) *err = "the Phi pass with the AO model does not fit this grid";
+    return 4;
+  }
   return 0;
 }
 
@@ -665,16 +658,7 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_cols_fft<T, +1>, std::max(smem_colx_, smem_coly_));
   set_smem<T>(k_xconv<T>, smem_xconv_);
   set_smem<T>(k_xbackconv<T>, smem_xback_);
-  set_smem<T>(k_phi_rows<T, MODEL_ROSENFELD>, smem_phi_);
-  set_smem<T>(k_phi_rows<T, MODEL_RSLT>, smem_phi_);
-  set_smem<T>(k_phi_rows<T, MODEL_ESFMT>, smem_phi_);
-  set_smem<T>(k_phi_rows<T, MODEL_WHITEBEAR_I>, smem_phi_);
-  set_smem<T>(k_phi_rows<T, MODEL_WHITEBEAR_II>, smem_phi_);
-  set_smem<T>(k_hess_rows<T, MODEL_ROSENFELD>, smem_phi_);
-  set_smem<T>(k_hess_rows<T, MODEL_RSLT>, smem_phi_);
-  set_smem<T>(k_hess_rows<T, MODEL_ESFMT>, smem_phi_);
-  set_smem<T>(k_hess_rows<T, MODEL_WHITEBEAR_I>, smem_phi_);
-  set_smem<T>(k_hess_rows<T, MODEL_WHITEBEAR_II>, smem_phi_);
+  if (M_ > 0) with_model(model_, [&](auto m) { PhiLauncher<T, decltype(m)::value>::prepare_rows(smem_phi_); });
   set_smem<T>(k_rows_c2r<T, T>, smem_rows_);
   set_smem<T>(k_hess_final_rows<T, double>, smem_rows_);
   set_smem<T>(k_hess_final_rows<T, T>, smem_rows_);
@@ -682,6 +666,14 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_hess_final_rows<T, T, 128>, smem_rows_);
   set_smem<T>(k_hess_final_rows<T, double, 256>, smem_rows_);
   set_smem<T>(k_hess_final_rows<T, T, 256>, smem_rows_);
+  if constexpr (std::is_same<T, double>::value) {  // the double-float-spectra instances
+    set_smem<T>(k_rows_r2c<T, double, 128, true>, smem_rows_);
+    set_smem<T>(k_rows_r2c<T, double, 256, true>, smem_rows_);
+    set_smem<T>(k_final_rows<T, double, 128, true>, smem_rows_);
+    set_smem<T>(k_final_rows<T, double, 256, true>, smem_rows_);
+    set_smem<T>(k_hess_final_rows<T, double, 128, true>, smem_rows_);
+    set_smem<T>(k_hess_final_rows<T, double, 256, true>, smem_rows_);
+  }
   // partial-sum storage: phi blocks (1 value), x columns (1 value), final rows (4 values)
   const long ncolx = ((long)ny * pz_ + 7) / 8 + 16;  // x-pass blocks of the widest grid (8 columns per tile)
   // phi partials: at most one per row (both the row-group and the persistent grids stay below it)
@@ -772,19 +764,22 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   double* part_mf = part_ + 2 * rows_;
   double* part_fin = part_mf + 2 * (long)std::max(gcx, gtx);
   const bool any = M_ > 0 || mf_;
+  const bool io = df_spectra();
   auto yfwd = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, -1, decltype(nf_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
+    if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, -1, decltype(nf_)::value, decltype(io_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
     else k_cols_fft<T, -1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   auto yinv = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, +1, decltype(nf_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
+    if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, +1, decltype(nf_)::value, decltype(io_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
     else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   cudaMemsetAsync(status_, 0, sizeof(unsigned), s);
   mark(0);
   if (any) {
-    with_nf(fz_, [&](auto nf_) { k_rows_r2c<T, RT, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan,
-                                                                                                       twp<T>(tz_), rb_rows_); });
+    with_nf_io<T>(fz_, io, [&](auto nf_, auto io_) {
+      k_rows_r2c<T, RT, decltype(nf_)::value, decltype(io_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho, A_, d, tz_->plan,
+                                                                                                                        twp<T>(tz_), rb_rows_);
+    });
     mark(1);
     yfwd(A_, mapYA_, 1, grid_ty1_);
     mark(2);
@@ -793,45 +788,37 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     mark(2);
   }
   if (M_ > 0) {
-    if (tma_) with_nf(fx_, [&](auto nf_) { k_xconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
+    if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     mark(3);
     yinv(Cf_, mapYC_, M_, grid_tyM_);
     mark(4);
-    const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
-    const unsigned gphi = (unsigned)nphi;
-    phi_blocks_last_ = nphi;
-    if (tma_phi_) {
-      phi_blocks_last_ = grid_tphi_;
-      if (ao_) {  // FMT_AO_Species: the Phi pass also leaves NA and the polymer-folded fields
-        const T iph = (T)(1.0 / ao_hp_), iph2 = (T)(1.0 / (ao_hp_ * ao_hp_));
-        phi_blocks_last_ = grid_tao_;
-        with_nf(fz_, [&](auto nf_) {
-          constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
-          switch (model_) {
-            case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
-            case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
-            case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
-            case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
-            default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiAO><<<grid_tao_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_, NA_, XA_, iph, iph2); break;
-          }
-        });
-        ao_block(s);
-      } else
-      switch (model_) {
-        case MODEL_ROSENFELD: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_ROSENFELD, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
-        case MODEL_RSLT: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_RSLT, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
-        case MODEL_ESFMT: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_ESFMT, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
-        case MODEL_WHITEBEAR_I: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_WHITEBEAR_I, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
-        default: with_nf(fz_, [&](auto nf_) { k_phi_rows_tma<T, MODEL_WHITEBEAR_II, PhiRowsFor<T, decltype(nf_)::value>::value, decltype(nf_)::value><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, part_phi, status_); }); break;
-      }
-    } else
-    switch (model_) {
-      case MODEL_ROSENFELD: k_phi_rows<T, MODEL_ROSENFELD><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
-      case MODEL_RSLT: k_phi_rows<T, MODEL_RSLT><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
-      case MODEL_ESFMT: k_phi_rows<T, MODEL_ESFMT><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
-      case MODEL_WHITEBEAR_I: k_phi_rows<T, MODEL_WHITEBEAR_I><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
-      default: k_phi_rows<T, MODEL_WHITEBEAR_II><<<gphi, 256, smem_phi_, s>>>(Cf_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b, part_phi, status_); break;
+    PhiArgs pa;
+    pa.map = &mapR_;
+    pa.Cf = Cf_;
+    pa.d = d;
+    pa.plan = tz_->plan;
+    pa.tw = twp<T>(tz_);
+    pa.hsd = hsd_;
+    pa.esA = esA_;
+    pa.esB = esB_;
+    pa.part = part_phi;
+    pa.status = status_;
+    pa.NA = NA_;
+    pa.XA = XA_;
+    if (ao_) {
+      pa.iph = 1.0 / ao_hp_;
+      pa.iph2 = 1.0 / (ao_hp_ * ao_hp_);
+    }
+    if (tma_phi_) {  // FMT_AO_Species: the Phi pass also leaves NA and the polymer-folded fields
+      phi_blocks_last_ = ao_ ? grid_tao_ : grid_tphi_;
+      with_model(model_, [&](auto m) {
+        PhiLauncher<T, decltype(m)::value>::launch_tma(phi_nf(), ao_ ? kPhiAO : kPhiEval, pa, (int)phi_blocks_last_, smem_tphi_, s);
+      });
+      if (ao_) ao_block(s);
+    } else {
+      phi_blocks_last_ = nphi;
+      with_model(model_, [&](auto m) { PhiLauncher<T, decltype(m)::value>::launch_rows(false, pa, rb_phi_, (unsigned)nphi, smem_phi_, s); });
     }
     mark(5);
     yfwd(Cf_, mapYC_, M_, grid_tyM_);
@@ -841,8 +828,10 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   }
   if (any) {
     if (tma_)
-      with_nf(fx_, [&](auto nf_) { k_xbackconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan,
-                                                        twp<T>(tx_), mf_ ? part_mf : nullptr, status_); });
+      with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) {
+        k_xbackconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tback_, s>>>(
+            mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
+      });
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
                                                    mf_ ? part_mf : nullptr);
@@ -854,8 +843,10 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     mark(8);
   }
   const unsigned gfin = (unsigned)grid_blocks_rows();
-  with_nf(fz_, [&](auto nf_) { k_final_rows<T, RT, decltype(nf_)::value><<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_),
-                                                                                         rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin, nrm); });
+  with_nf_io<T>(fz_, io, [&](auto nf_, auto io_) {
+    k_final_rows<T, RT, decltype(nf_)::value, decltype(io_)::value><<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_),
+                                                                                                 rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin, nrm);
+  });
   {
     const FinishSeg sphi{part_phi, phi_blocks_last_, M_ > 0 ? 1 : 0, terms_ + 0};
     const FinishSeg smf{part_mf, (long)gxb, mf_ ? 1 : 0, terms_ + 1};
@@ -877,28 +868,30 @@ int Evaluator<T>::hess_prepare(const double* rho0, cudaStream_t s) {
   const unsigned gcx = (unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_);
   constexpr int TCt = TileCols<T>::value;
   const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
-  with_nf(fz_, [&](auto nf_) {
-    k_rows_r2c<T, double, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(rho0, A_, d, tz_->plan, twp<T>(tz_),
-                                                                                                    rb_rows_);
+  const bool io = df_spectra();
+  with_nf_io<T>(fz_, io, [&](auto nf_, auto io_) {
+    k_rows_r2c<T, double, decltype(nf_)::value, decltype(io_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(
+        rho0, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
   });
-  if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, -1, decltype(nf_)::value><<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_); });
+  if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, -1, decltype(nf_)::value, decltype(io_)::value><<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_); });
   else k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
-  if (tma_) with_nf(fx_, [&](auto nf_) { k_xconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
+  if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
   else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
-  if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, +1, decltype(nf_)::value><<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_); });
+  if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, +1, decltype(nf_)::value, decltype(io_)::value><<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_); });
   else k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  PhiArgs pa;
+  pa.map = &mapR_;
+  pa.Cf = Cf_;
+  pa.d = d;
+  pa.plan = tz_->plan;
+  pa.tw = twp<T>(tz_);
+  pa.hsd = hsd_;
+  pa.esA = esA_;
+  pa.esB = esB_;
+  pa.status = status_;
+  pa.NA = NA_;
   if (tma_phi_) {  // one tensor-copied pass: z c2r of all M fields, stored as the weighted densities
-    with_nf(fz_, [&](auto nf_) {
-      constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
-      const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
-      switch (model_) {
-        case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-        case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-        case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-        case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-        default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiStoreN><<<grid_tphi_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-      }
-    });
+    with_model(model_, [&](auto m) { PhiLauncher<T, decltype(m)::value>::launch_tma(phi_nf(), kPhiStoreN, pa, grid_tphi_, smem_tphi_, s); });
   } else {
     for (int a = 0; a < M_; ++a)
       k_rows_c2r<T, T><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(Cf_ + (long)a * Nc_, NA_ + (long)a * N_, d, tz_->plan,
@@ -917,60 +910,58 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
   constexpr int TCt = TileCols<T>::value;
   const unsigned gtx = (unsigned)(((long)ny_ * pz_ + TCt - 1) / TCt);
   const bool any = M_ > 0 || mf_;
+  const bool io = df_spectra();
   auto yfwd = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, -1, decltype(nf_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
+    if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, -1, decltype(nf_)::value, decltype(io_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
     else k_cols_fft<T, -1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   auto yinv = [&](C* buf, const CUtensorMap& map, int nf, int grid) {
-    if (tma_) with_nf(fy_, [&](auto nf_) { k_cols_y_tma<T, +1, decltype(nf_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
+    if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, +1, decltype(nf_)::value, decltype(io_)::value><<<grid, 256, smem_ty_, s>>>(map, d, ty_->plan, twp<T>(ty_), nf, status_); });
     else k_cols_fft<T, +1><<<dim3(gcy, nf), 256, smem_coly_, s>>>(buf, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   };
   if (any) {
-    with_nf(fz_, [&](auto nf_) {
-      k_rows_r2c<T, RT, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(v, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
+    with_nf_io<T>(fz_, io, [&](auto nf_, auto io_) {
+      k_rows_r2c<T, RT, decltype(nf_)::value, decltype(io_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(v, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
     });
     yfwd(A_, mapYA_, 1, grid_ty1_);
   }
   if (M_ > 0) {
-    if (tma_) with_nf(fx_, [&](auto nf_) { k_xconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
+    if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     yinv(Cf_, mapYC_, M_, grid_tyM_);
-    const T h = (T)hsd_, a = (T)esA_, b = (T)esB_;
     const unsigned g = (unsigned)((rows_ + rb_phi_ - 1) / rb_phi_);
-    if (tma_phi_) {
-      with_nf(fz_, [&](auto nf_) {
-        constexpr int NF = decltype(nf_)::value, RB = PhiRowsFor<T, NF>::value;
-        switch (model_) {
-          case MODEL_ROSENFELD: k_phi_rows_tma<T, MODEL_ROSENFELD, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-          case MODEL_RSLT: k_phi_rows_tma<T, MODEL_RSLT, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-          case MODEL_ESFMT: k_phi_rows_tma<T, MODEL_ESFMT, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-          case MODEL_WHITEBEAR_I: k_phi_rows_tma<T, MODEL_WHITEBEAR_I, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-          default: k_phi_rows_tma<T, MODEL_WHITEBEAR_II, RB, NF, kPhiHess><<<grid_thess_, PhiThreads<T>::value, smem_tphi_, s>>>(mapR_, Cf_, d, tz_->plan, twp<T>(tz_), h, a, b, nullptr, status_, NA_); break;
-        }
-      });
-    } else
-    switch (model_) {
-      case MODEL_ROSENFELD: k_hess_rows<T, MODEL_ROSENFELD><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
-      case MODEL_RSLT: k_hess_rows<T, MODEL_RSLT><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
-      case MODEL_ESFMT: k_hess_rows<T, MODEL_ESFMT><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
-      case MODEL_WHITEBEAR_I: k_hess_rows<T, MODEL_WHITEBEAR_I><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
-      default: k_hess_rows<T, MODEL_WHITEBEAR_II><<<g, 256, smem_phi_, s>>>(Cf_, NA_, d, tz_->plan, twp<T>(tz_), rb_phi_, h, a, b); break;
-    }
+    PhiArgs pa;
+    pa.map = &mapR_;
+    pa.Cf = Cf_;
+    pa.d = d;
+    pa.plan = tz_->plan;
+    pa.tw = twp<T>(tz_);
+    pa.hsd = hsd_;
+    pa.esA = esA_;
+    pa.esB = esB_;
+    pa.status = status_;
+    pa.NA = NA_;
+    with_model(model_, [&](auto m) {
+      if (tma_phi_) PhiLauncher<T, decltype(m)::value>::launch_tma(phi_nf(), kPhiHess, pa, grid_thess_, smem_tphi_, s);
+      else PhiLauncher<T, decltype(m)::value>::launch_rows(true, pa, rb_phi_, g, smem_phi_, s);
+    });
     yfwd(Cf_, mapYC_, M_, grid_tyM_);
   }
   double* part_mf = part_ + 2 * rows_;
   if (any) {
     if (tma_)
-      with_nf(fx_, [&](auto nf_) { k_xbackconv_tma<T, decltype(nf_)::value><<<gtx, 256, smem_tback_, s>>>(mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_),
-                                                        mf_ ? part_mf : nullptr, status_); });
+      with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) {
+        k_xbackconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tback_, s>>>(
+            mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
+      });
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
                                                    mf_ ? part_mf : nullptr);
     yinv(E_, mapYE_, 1, grid_ty1_);
   }
-  with_nf(fz_, [&](auto nf_) {
-    k_hess_final_rows<T, RT, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(E_, rho0, v, out, d, tz_->plan,
-                                                                                                      twp<T>(tz_), rb_rows_, dV, any ? 1 : 0);
+  with_nf_io<T>(fz_, io, [&](auto nf_, auto io_) {
+    k_hess_final_rows<T, RT, decltype(nf_)::value, decltype(io_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(
+        E_, rho0, v, out, d, tz_->plan, twp<T>(tz_), rb_rows_, dV, any ? 1 : 0);
   });
   return cudaGetLastError() == cudaSuccess ? 0 : 5;
 }
@@ -989,6 +980,16 @@ void Evaluator<T>::fixed_plans() {
   fx_ = fixed_len(tx_);
   fy_ = fixed_len(ty_);
   fz_ = fixed_len(tz_);
+}
+
+template <class T>
+bool Evaluator<T>::df_candidate() const {
+  return kDf64Transforms && std::is_same<T, double>::value && fx_ > 0 && fy_ > 0 && fz_ > 0 && tma_ && !ao_ && M_ > 0;
+}
+
+template <class T>
+int Evaluator<T>::phi_nf() const {
+  return (kDf64Transforms && std::is_same<T, double>::value && !df_candidate()) ? 0 : fz_;
 }
 
 template <class T>

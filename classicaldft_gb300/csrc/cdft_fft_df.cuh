@@ -159,11 +159,12 @@ __host__ __device__ constexpr int df_table_offset(int n) {
 }
 
 // The row passes' transform: in df64 for FP64 with a compile-time plan, else block_fft_nf.
-template <int DIR, class T, int NF>
+// IN_D / OUT_D as for tile_fft_fixed_df (df64 only).
+template <int DIR, class T, int NF, bool IN_D = true, bool OUT_D = true>
 __device__ __forceinline__ typename Cx<T>::type* rows_fft(typename Cx<T>::type* b0, typename Cx<T>::type* b1, int L, int LP, const FFTPlan& P,
                                                           const typename Cx<T>::type* __restrict__ table) {
   if constexpr (kDf64Transforms && NF > 0 && sizeof(T) == 8) {
-    double2* r = rows_fft_df<DIR, NF, 256>(b0, b1, L, LP, reinterpret_cast<const dfc*>(table + df_table_offset(NF)));
+    double2* r = rows_fft_df<DIR, NF, 256, IN_D, OUT_D>(b0, b1, L, LP, reinterpret_cast<const dfc*>(table + df_table_offset(NF)));
     __syncthreads();
     return r;
   } else {

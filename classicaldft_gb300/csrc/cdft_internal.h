@@ -159,6 +159,16 @@ class Evaluator {
   // the tensor-copy kernels' compile-time plans (length 128, default radix order) apply to x / y / z
   int fx_ = 0, fy_ = 0, fz_ = 0;  // compile-time plan length per axis (128, 256) or 0
   void fixed_plans();
+  // FP64 spectra kept in double-float between passes: every pass of an evaluation and of a
+  // Hessian product on the tensor-copy path with compile-time plans on all three axes (not
+  // with the AO passes, whose spectra go through the runtime-plan kernels). Each complex
+  // value is then a dfc (two float pairs, 16 bytes like a double2) in A_, Cf_ and E_, and no
+  // pass splits or joins at its edges.
+  bool df_candidate() const;
+  bool df_spectra() const { return df_candidate() && tma_phi_; }
+  // the plan length of the Phi pass's instance: in FP64 its compile-time instance reads and
+  // writes double-float spectra, so it runs only when every pass does
+  int phi_nf() const;
   bool setup_phi_tma();
   CUtensorMap mapR_;
   size_t smem_tphi_ = 0;

@@ -220,12 +220,19 @@ __device__ __forceinline__ void block_norms_store(const KahanT<T>& q, T mx, doub
 __global__ void k_finish_reduce(const double* __restrict__ part, long nblk, int nv, double* __restrict__ out);
 
 // ------------------------------------------------------------ row passes ---
+// FP64 spectra kept in double-float between passes: an instance with DFS (FP64, compile-time
+// plan) reads and writes each complex value as a dfc where the others use a double2.
+template <class T, int NF, bool DFS> struct DfSpectra {
+  static constexpr bool value = DFS && kDf64Transforms && sizeof(T) == 8 && NF > 0;
+};
+
 // z-axis r2c: rows of a real field (SRC = double or T) to half spectra.
 // Each block owns RB row pairs; pair r packs rows (2r, 2r+1) as re/im.
-template <class T, class SRC, int NF = 0>
+template <class T, class SRC, int NF = 0, bool DFS = false>
 __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, typename Cx<T>::type* __restrict__ out, Dims d,
                                                   FFTPlan pz, const typename Cx<T>::type* __restrict__ tw, int RB) {
   typedef typename Cx<T>::type C;
+  constexpr bool DS = DfSpectra<T, NF, DFS>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
   const int nz = NF > 0 ? NF : d.nz, LP = nz + 1;
@@ -241,11 +248,19 @@ __global__ void __launch_bounds__(256) k_rows_r2c(const SRC* __restrict__ in, ty
     if (rb < d.rows) vb = conv<T>(in[rb * nz + k]);
     b0[r * LP + k] = mk<T>(va, vb);
   }
-  C* res = rows_fft<-1, T, NF>(b0, b1, RB, LP, pz, tw);
+  C* res = rows_fft<-1, T, NF, true, !DS>(b0, b1, RB, LP, pz, tw);
   const int nzc = NF > 0 ? NF / 2 + 1 : d.nzc;
   for (int e = threadIdx.x; e < RB * nzc; e += blockDim.x) {
     const int r = e / nzc, k = e - r * nzc;
     const long ra = 2 * (pair0 + r), rb = ra + 1;
+    if constexpr (DS) {  // the same split in df64
+      const dfc* rd = reinterpret_cast<const dfc*>(res);
+      const dfc Z = rd[r * LP + k], W = rd[r * LP + (k == 0 ? 0 : nz - k)];
+      dfc* o = reinterpret_cast<dfc*>(out);
+      if (ra < d.rows) o[ra * d.pz + k] = dfc{df_half(Z.x + W.x), df_half(Z.y - W.y)};
+      if (rb < d.rows) o[rb * d.pz + k] = dfc{df_half(Z.y + W.y), df_half(W.x - Z.x)};
+      continue;
+    }
     const C Z = res[r * LP + k];
     const C W = res[r * LP + (k == 0 ? 0 : nz - k)];  // Z_{N-k}
     // X = (Z + conj(W))/2, Y = (Z - conj(W))/(2i)
@@ -273,6 +288,27 @@ __device__ __forceinline__ typename Cx<T>::type pair_spectrum(const typename Cx<
     b.y = -b.y;
   }
   return mk<T>(a.x - b.y, a.y + b.x);
+}
+
+// pair_spectrum on double-float spectra
+__device__ __forceinline__ dfc pair_spectrum_df(const dfc* __restrict__ A, const dfc* __restrict__ B, int k, int nz) {
+  const int nzc = nz / 2 + 1;
+  const dfc zero{dfs(0), dfs(0)};
+  dfc a, b;
+  if (k < nzc) {
+    a = A ? A[k] : zero;
+    b = B ? B[k] : zero;
+    if (k == 0 || 2 * k == nz) {
+      a.y = dfs(0);
+      b.y = dfs(0);
+    }
+  } else {
+    a = A ? A[nz - k] : zero;
+    b = B ? B[nz - k] : zero;
+    a.y = -a.y;
+    b.y = -b.y;
+  }
+  return dfc{a.x - b.y, a.y + b.x};
 }
 
 // z-axis c2r: half spectra rows to real rows (DST = double or T), times scale.
@@ -585,11 +621,12 @@ __global__ void __launch_bounds__(256) k_hess_rows(typename Cx<T>::type* __restr
 // Last step of the Hessian-vector product: c2r of E (FMT + mean-field
 // back-convolution of the Lambda fields) and the ideal-gas term,
 //   Hv = (v / rho + c2r(E)) dV   (DFT::matrix_dot_v_intern, src/DFT.cpp:455-462).
-template <class T, class RT, int NF = 0>
+template <class T, class RT, int NF = 0, bool DFS = false>
 __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::type* __restrict__ E, const double* __restrict__ rho,
                                                          const RT* __restrict__ v, RT* __restrict__ out, Dims d, FFTPlan pz,
                                                          const typename Cx<T>::type* __restrict__ tw, int RB, double dV, int have_fmt_or_mf) {
   typedef typename Cx<T>::type C;
+  constexpr bool DS = DfSpectra<T, NF, DFS>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
   const int nz = NF > 0 ? NF : d.nz, LP = nz + 1;
@@ -603,9 +640,12 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
       const long ra = 2 * (pair0 + r), rb = ra + 1;
       const C* Ar = ra < d.rows ? E + ra * d.pz : nullptr;
       const C* Br = rb < d.rows ? E + rb * d.pz : nullptr;
-      b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
+      if constexpr (DS)
+        reinterpret_cast<dfc*>(b0)[r * LP + k] = pair_spectrum_df(reinterpret_cast<const dfc*>(Ar), reinterpret_cast<const dfc*>(Br), k, nz);
+      else
+        b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
-    res = rows_fft<+1, T, NF>(b0, b1, RB, LP, pz, tw);
+    res = rows_fft<+1, T, NF, !DS, true>(b0, b1, RB, LP, pz, tw);
   }
   const T dVt = (T)dV;
   for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
@@ -630,13 +670,14 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
 //   dF = ln(rho) dV + c2r(E) dV + V_ext dV - mu dV
 // with FP64 partial sums: F_id = sum (rho ln rho - rho) dV, sum rho,
 // sum V_ext rho, sum dF rho (for the fixed-mass projection).
-template <class T, class RT = double, int NF = 0>
+template <class T, class RT = double, int NF = 0, bool DFS = false>
 __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* __restrict__ E, const RT* __restrict__ rho,
                                                     const double* __restrict__ vext, RT* __restrict__ dF, Dims d, FFTPlan pz,
                                                     const typename Cx<T>::type* __restrict__ tw, int RB, double dV, double mu,
                                                     int have_fmt_or_mf, int ideal, double* __restrict__ part,
                                                     double* __restrict__ nrm) {
   typedef typename Cx<T>::type C;
+  constexpr bool DS = DfSpectra<T, NF, DFS>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
   const int nz = NF > 0 ? NF : d.nz, LP = nz + 1;
@@ -650,9 +691,12 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
       const long ra = 2 * (pair0 + r), rb = ra + 1;
       const C* Ar = ra < d.rows ? E + ra * d.pz : nullptr;
       const C* Br = rb < d.rows ? E + rb * d.pz : nullptr;
-      b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
+      if constexpr (DS)
+        reinterpret_cast<dfc*>(b0)[r * LP + k] = pair_spectrum_df(reinterpret_cast<const dfc*>(Ar), reinterpret_cast<const dfc*>(Br), k, nz);
+      else
+        b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
-    res = rows_fft<+1, T, NF>(b0, b1, RB, LP, pz, tw);
+    res = rows_fft<+1, T, NF, !DS, true>(b0, b1, RB, LP, pz, tw);
   }
   // Pointwise terms in the bulk precision T (FP64 in FP64 mode); each thread
   // keeps Kahan partials in T over its few points, merged in FP64 across the

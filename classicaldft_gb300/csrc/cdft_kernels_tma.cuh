@@ -275,7 +275,7 @@ template <class T, int NF> struct XReg {
 // ---------------------------------------------------------------- y pass ---
 // Work item = (field f, plane x, column tile t): the tile [ny][TC] at kz0 = t*TC.
 // Tensor map (4D, 8-byte elements): {pz*E, ny, nx, nfield}.
-template <class T, int DIR, int NF = 0>
+template <class T, int DIR, int NF = 0, bool DFS = false>
 __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUtensorMap map, Dims d, FFTPlan P,
                                                     const typename Cx<T>::type* __restrict__ tw, int nfield, unsigned* __restrict__ status) {
   typedef typename Cx<T>::type C;
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
     // buffer) before this tile's transform writes work
     if (threadIdx.x == 0) bulk_wait_read();
     if (!__syncthreads_and(ok)) break;
-    C* res = tfft<DIR, T, TC, TC, NF>(stage[b], work, P, tw);
+    C* res = xfft<DIR, T, TC, NF, !DFS, !DFS>(stage[b], work, P, tw);
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
 
 // C[a] = IFFT_x(FFT_x(A) . w_a) for a < M. The density spectrum lives in
 // registers; weight tiles are double-buffered; results leave by tensor store.
-template <class T, int NF = 0>
+template <class T, int NF = 0, bool DFS = false>
 __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapW,
                                                    const __grid_constant__ CUtensorMap mapC, int M, FFTPlan px,
                                                    const typename Cx<T>::type* __restrict__ tw, unsigned* __restrict__ status) {
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
   }
   typedef XReg<T, NF> XR;
   typedef typename XR::C RC;
-  C* res = xfft<-1, T, TC, NF, true, false>(X, Y, px, tw);
+  C* res = xfft<-1, T, TC, NF, !DFS, false>(X, Y, px, tw);
   RC R[PER];
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
       mbar_arrive_expect_tx(&bar[b], (unsigned)wbytes);
       tma_load_3d(Wst[b], &mapW, col0, 0, a + 2, &bar[b]);
     }
-    C* r2 = xfft<+1, T, TC, NF, false, true>(in, other, px, tw);
+    C* r2 = xfft<+1, T, TC, NF, false, !DFS>(in, other, px, tw);
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
 // E = IFFT_x(sum_a FFT_x(D[a]) . w_a + FFT_x(A) . w_att); sources are
 // double-buffered (spectrum tile + weight tile per stage), the sum lives in
 // registers. With the mean field, the Parseval sum for its energy goes to part.
-template <class T, int NF = 0>
+template <class T, int NF = 0, bool DFS = false>
 __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant__ CUtensorMap mapD, const __grid_constant__ CUtensorMap mapW,
                                                        const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapWatt,
                                                        const __grid_constant__ CUtensorMap mapE, int M, int with_mf, Dims d, FFTPlan px,
@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
     const int b = a & 1;
     ok = mbar_wait(&bar[b], (unsigned)((a >> 1) & 1), status);
     if (!__syncthreads_and(ok)) break;
-    C* res = xfft<-1, T, TC, NF, true, false>(Dst[b], Y, px, tw);
+    C* res = xfft<-1, T, TC, NF, !DFS, false>(Dst[b], Y, px, tw);
     const bool is_mf = (a == M);
     const bool odd = !is_mf && weight_is_odd(a);
 #pragma unroll
@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
     const int e = threadIdx.x + j * 256;
     if (e < nel) reinterpret_cast<RC*>(X)[e] = S[j];
   }
-  C* r2 = xfft<+1, T, TC, NF, false, true>(X, Y, px, tw);
+  C* r2 = xfft<+1, T, TC, NF, false, !DFS>(X, Y, px, tw);
   fence_async_smem();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -606,10 +606,11 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   constexpr int M = ModelTraits<MODEL>::M;
   typedef PhiPack<M, RB, PhiCross<T>::value> PK;
   const T ih = (T)(1.0 / (double)hsd), ih2 = (T)(1.0 / ((double)hsd * (double)hsd));
-  // FP64 with a compile-time plan: the tile holds df64 values from the unpacking to the
-  // Hermitian split (both transforms on the FP32 pipe), and the evaluation's functional
-  // runs in df64 too, its f-functions of eta in FP64 (fmt_f_df); the other modes and RSLT
-  // take FP64 values per point (getv / setv convert).
+  // FP64 with a compile-time plan: the spectra in HBM are double-float (the evaluator runs
+  // this instance only when every pass keeps them so), the tile holds df64 values from the
+  // unpacking to the Hermitian split (both transforms on the FP32 pipe), and the
+  // evaluation's functional runs in df64 too, its f-functions of eta in FP64 (fmt_f_df);
+  // the other modes and RSLT take FP64 values per point (getv / setv convert).
   constexpr bool DF = kDf64Transforms && std::is_same<T, double>::value && NF > 0;
   constexpr bool DF_FUNC = DF && MODE == kPhiEval && MODEL != MODEL_RSLT;
   auto getv = [&](const C* buf, int i, int h) -> T {
@@ -677,7 +678,8 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
       PK::source(line, 1, aB, rB);
       const C* Arow = in + ((size_t)aA * RB + rA) * pz;
       const C* Brow = aB >= 0 ? in + ((size_t)aB * RB + rB) * pz : nullptr;
-      if constexpr (DF) reinterpret_cast<dfc*>(Z0)[k * LPd + line] = dfc_split(pair_spectrum<T>(Arow, Brow, k, nz));
+      if constexpr (DF)
+        reinterpret_cast<dfc*>(Z0)[k * LPd + line] = pair_spectrum_df(reinterpret_cast<const dfc*>(Arow), reinterpret_cast<const dfc*>(Brow), k, nz);
       else Z0[k * LPd + line] = pair_spectrum<T>(Arow, Brow, k, nz);
     }
     __syncthreads();
@@ -774,14 +776,12 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
       int aA, rA, aB, rB;
       PK::source(line, 0, aA, rA);
       PK::source(line, 1, aB, rB);
-      if constexpr (DF) {  // the split in df64, each output joined once
+      if constexpr (DF) {  // the split in df64, the spectra stored as df64
         const dfc* rd = reinterpret_cast<const dfc*>(res2);
         const dfc Z = rd[k * LPd + line], W = rd[(k == 0 ? 0 : nz - k) * LPd + line];
-        auto half = [](dfs a) { return dfs(__fmul_rn(0.5f, a.h), __fmul_rn(0.5f, a.l)); };  // exact
-        if (row0 + rA < d.rows)
-          Cf[(long)aA * d.Nc + (row0 + rA) * pz + k] = make_double2(dfs_join(half(Z.x + W.x)), dfs_join(half(Z.y - W.y)));
-        if (aB >= 0 && row0 + rB < d.rows)
-          Cf[(long)aB * d.Nc + (row0 + rB) * pz + k] = make_double2(dfs_join(half(Z.y + W.y)), dfs_join(half(W.x - Z.x)));
+        dfc* o = reinterpret_cast<dfc*>(Cf);
+        if (row0 + rA < d.rows) o[(long)aA * d.Nc + (row0 + rA) * pz + k] = dfc{df_half(Z.x + W.x), df_half(Z.y - W.y)};
+        if (aB >= 0 && row0 + rB < d.rows) o[(long)aB * d.Nc + (row0 + rB) * pz + k] = dfc{df_half(Z.y + W.y), df_half(W.x - Z.x)};
       } else {
         const C Z = res2[k * LPd + line];
         const C W = res2[(k == 0 ? 0 : nz - k) * LPd + line];

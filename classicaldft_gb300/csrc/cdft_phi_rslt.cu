@@ -1,0 +1,4 @@
+// The Phi-pass instances of the RSLT functional, both precisions.
+#include "cdft_phi_launch.cuh"
+
+CDFT_PHI_INSTANTIATE(MODEL_RSLT)
