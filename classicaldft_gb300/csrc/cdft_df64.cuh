@@ -74,6 +74,88 @@ __device__ __forceinline__ dfs dfs_split(double d) {
 }
 // df64 -> double: hi + lo, rounded once
 __device__ __forceinline__ double dfs_join(dfs a) { return cvt_f64(a.h) + cvt_f64(a.l); }
+__device__ __forceinline__ bool operator<(dfs a, dfs b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+__device__ __forceinline__ dfs df_abs(dfs a) { return a.h < 0.f ? -a : a; }
+
+// 1 / b: the FP32 reciprocal refined by two residual corrections in df64 (each residual
+// 1 - b q is formed with exact products), relative error ~5e-15
+__device__ __forceinline__ dfs df_rcp(dfs b) {
+  const float y = __frcp_rn(b.h);
+  dfs r = dfs(1) - b * dfs(y, 0.f);
+  const float q2 = __fmul_rn(r.h, y);
+  r = r - b * dfs(q2, 0.f);
+  const float q3 = __fmul_rn(r.h, y);
+  return df_fast_two_sum(y, q2) + dfs(q3, 0.f);
+}
+__device__ __forceinline__ dfs operator/(dfs a, dfs b) { return a * df_rcp(b); }
+
+// ---- logarithms in df64, table-driven (P. T. P. Tang, "Table-driven implementation of the
+// logarithm function in IEEE floating-point arithmetic", ACM TOMS 16, 1990): 1 + x = 2^k F (1 + r)
+// with F = 1 + j/128 (j = -32..64, so that F and 2^-k (1 + x) lie within 1/256 of each
+// other), u = 2^-k (1 + x) - F formed exactly (Sterbenz), r = u / F, and
+// log(1 + x) = k ln2 + log F + log1p(r), |r| <= 2^-8, where log1p(r) = r - r^2/2 + r^3/3
+// + r^4 q(r) takes its first three terms in df64 and q (a cubic) in FP32. Near x = 0 the
+// reduction is skipped (k = 0, F = 1), so the result keeps its relative accuracy there.
+// Relative error ~1e-14 (against ~1e-16 in FP64), far inside the evaluation's 1e-12.
+// The table (log F and 1/F as df64) lives in shared memory: a kernel calls
+// df_log_table_init once and synchronises before the first logarithm.
+constexpr int kDfLogLo = -32, kDfLogN = 97;
+__device__ __forceinline__ float4* df_log_table() {
+  __shared__ float4 t[kDfLogN];
+  return t;
+}
+__device__ __forceinline__ void df_log_table_init(int tid, int nthreads) {
+  float4* t = df_log_table();
+  for (int i = tid; i < kDfLogN; i += nthreads) {
+    const int j = i + kDfLogLo;
+    const dfs l = dfs_split(log1p((double)j / 128.0)), v = dfs_split(1.0 / (1.0 + (double)j / 128.0));
+    t[i] = make_float4(l.h, l.l, v.h, v.l);
+  }
+}
+__device__ __forceinline__ dfs df_ln2() { return dfs(0.6931471805599453094); }
+__device__ __forceinline__ dfs df_third() { return dfs(0.3333333333333333333); }
+__device__ __forceinline__ dfs df_log1p_reduced(dfs r) {  // |r| <= 2^-8
+  const dfs r2 = r * r, r3 = r2 * r;
+  const float rh = r.h;
+  const float q = __fmaf_rn(rh, __fmaf_rn(rh, __fmaf_rn(rh, 0.142857142857f, -0.166666666667f), 0.2f), -0.25f);
+  const float r4q = __fmul_rn(__fmul_rn(r2.h, r2.h), q);
+  return (r + (r3 * df_third() + (-df_half(r2)))) + dfs(r4q, 0.f);
+}
+__device__ __forceinline__ dfs df_log1p(dfs x) {
+  if (fabsf(x.h) < 0.00390625f) return df_log1p_reduced(x);
+  const float y = __fadd_rn(1.0f, x.h);
+  if (!(y >= 1.17549435e-38f && y <= 1.0e30f)) return dfs_split(log1p(dfs_join(x)));  // 1 + x <= 0, huge, NaN: FP64
+  const int bits = __float_as_int(y);
+  int k = ((bits >> 23) & 0xff) - 127;
+  float m = __int_as_float((bits & 0x007fffff) | 0x3f800000);  // y = 2^k m, m in [1, 2)
+  if (m >= 1.5f) {
+    m = __fmul_rn(m, 0.5f);
+    ++k;
+  }
+  int j = __float2int_rn(__fmul_rn(__fadd_rn(m, -1.0f), 128.0f));
+  j = j < kDfLogLo ? kDfLogLo : (j > kDfLogLo + kDfLogN - 1 ? kDfLogLo + kDfLogN - 1 : j);
+  const float F = __fmaf_rn((float)j, 0.0078125f, 1.0f);
+  const float p = __int_as_float((127 - k) << 23);  // 2^-k (k in [-126, 100] here)
+  const dfs u = dfs(__fadd_rn(p, -F), 0.f) + dfs(__fmul_rn(x.h, p), __fmul_rn(x.l, p));
+  const float4 t = df_log_table()[j - kDfLogLo];
+  const dfs lf = dfs(t.x, t.y) + dfs((float)k, 0.f) * df_ln2();
+  return lf + df_log1p_reduced(u * dfs(t.z, t.w));
+}
+// log x for x > 0: x = 2^k m, m in [0.75, 1.5), log x = k ln2 + log1p(m - 1 + lo 2^-k)
+__device__ __forceinline__ dfs df_log(dfs x) {
+  if (!(x.h >= 1.17549435e-38f && x.h <= 1.0e30f)) return dfs_split(log(dfs_join(x)));  // zero, subnormal, huge, NaN: FP64
+  const int bits = __float_as_int(x.h);
+  int k = ((bits >> 23) & 0xff) - 127;
+  float m = __int_as_float((bits & 0x007fffff) | 0x3f800000);
+  if (m >= 1.5f) {
+    m = __fmul_rn(m, 0.5f);
+    ++k;
+  }
+  const float p = __int_as_float((127 - k) << 23);
+  const dfs u = df_two_sum(__fadd_rn(m, -1.0f), __fmul_rn(x.l, p));
+  return dfs((float)k, 0.f) * df_ln2() + df_log1p(u);
+}
+
 __device__ __forceinline__ dfc dfc_split(double2 z) {
   dfc r;
   r.x = dfs_split(z.x);

@@ -645,7 +645,25 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
       else
         b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
-    res = rows_fft<+1, T, NF, !DS, true>(b0, b1, RB, LP, pz, tw);
+    res = rows_fft<+1, T, NF, !DS, !DS>(b0, b1, RB, LP, pz, tw);
+  }
+  if constexpr (DS) {  // double-float spectra: (v / rho + h) dV in df64, one join per point
+    const dfc* rd = reinterpret_cast<const dfc*>(res);
+    const dfs dVd = dfs_split(dV);
+    for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
+      const int rr = e / nz, k = e - rr * nz;
+      const long row = 2 * pair0 + rr;
+      if (row >= d.rows) continue;
+      const long p = row * nz + k;
+      dfs h = dfs(0);
+      if (have_fmt_or_mf) {
+        const dfc z = rd[(rr >> 1) * LP + k];
+        h = (rr & 1) ? z.y : z.x;
+      }
+      const dfs f = (dfs_split((double)v[p]) / dfs_split(rho[p])) * dVd + h * dVd;
+      out[p] = (RT)dfs_join(f);
+    }
+    return;
   }
   const T dVt = (T)dV;
   for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
@@ -664,6 +682,60 @@ __global__ void __launch_bounds__(256) k_hess_final_rows(const typename Cx<T>::t
 }
 
 // ------------------------------------------------------ final z rows ---
+// The final row pass's pointwise terms on double-float spectra (FP64 evaluation with
+// compile-time plans): ln rho by the table-driven df64 logarithm, every product and sum in
+// df64 on the FP32 pipe; rho is split and dF joined once per point, and each thread's sums
+// are joined once before the FP64 block merges. Same terms and order as the FP64 loop.
+template <class RT>
+__device__ __forceinline__ void final_points_df(const double2* __restrict__ res, const RT* __restrict__ rho,
+                                                const double* __restrict__ vext, RT* __restrict__ dF, const Dims& d, int RB,
+                                                int LP, int nz, long pair0, double dV, double mu, int have_fmt_or_mf, int ideal,
+                                                double* __restrict__ part, double* __restrict__ nrm) {
+  const dfc* rd = reinterpret_cast<const dfc*>(res);
+  const dfs dVd = dfs_split(dV), mud = dfs_split(mu);
+  dfs a0 = dfs(0), a1 = dfs(0), a2 = dfs(0), a3 = dfs(0), aq = dfs(0), mx = dfs(0);
+  for (int e = threadIdx.x; e < 2 * RB * nz; e += blockDim.x) {
+    const int rr = e / nz, k = e - rr * nz;
+    const long row = 2 * pair0 + rr;
+    if (row >= d.rows) continue;
+    const long p = row * nz + k;
+    const dfs r0 = dfs_split((double)rho[p]);
+    const dfs lr = df_log(r0);
+    dfs f = ideal ? lr * dVd : dfs(0);
+    if (have_fmt_or_mf) {
+      const dfc z = rd[(rr >> 1) * LP + k];
+      f += ((rr & 1) ? z.y : z.x) * dVd;
+    }
+    dfs ve = dfs(0);
+    if (vext) {
+      ve = dfs_split(vext[p]);
+      f += ve * dVd;
+    }
+    f += -mud * dVd;
+    dF[p] = (RT)dfs_join(f);
+    if (ideal) a0 += (r0 * lr - r0) * dVd;
+    a1 += r0;
+    if (vext) a2 += ve * r0;
+    a3 += f * r0;
+    if (nrm) {
+      aq += f * f;
+      const dfs af = df_abs(f);
+      if (mx < af) mx = af;
+    }
+  }
+  KahanT<double> ks[4];
+  ks[0].add(dfs_join(a0));
+  ks[1].add(dfs_join(a1));
+  ks[2].add(dfs_join(a2));
+  ks[3].add(dfs_join(a3));
+  block_kahan_store<4>(ks, part, blockIdx.x);
+  if (nrm) {
+    KahanT<double> kq;
+    kq.add(dfs_join(aq));
+    block_norms_store<double>(kq, dfs_join(mx), nrm, blockIdx.x);
+  }
+}
+
 // c2r of E (the summed hard-sphere + mean-field back-convolution) and the
 // pointwise terms of DFT::calculateFreeEnergyAndDerivatives_internal_
 // (src/DFT.cpp:377-425) and Species::externalField (src/Species.cpp:51-61):
@@ -678,6 +750,10 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
                                                     double* __restrict__ nrm) {
   typedef typename Cx<T>::type C;
   constexpr bool DS = DfSpectra<T, NF, DFS>::value;
+  if constexpr (DS) {
+    df_log_table_init(threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* b0 = reinterpret_cast<C*>(smem_raw);
   const int nz = NF > 0 ? NF : d.nz, LP = nz + 1;
@@ -696,7 +772,11 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
       else
         b0[r * LP + k] = pair_spectrum<T>(Ar, Br, k, nz);
     }
-    res = rows_fft<+1, T, NF, !DS, true>(b0, b1, RB, LP, pz, tw);
+    res = rows_fft<+1, T, NF, !DS, !DS>(b0, b1, RB, LP, pz, tw);
+  }
+  if constexpr (DS) {  // double-float spectra: the pointwise terms in df64 too
+    final_points_df(res, rho, vext, dF, d, RB, LP, nz, pair0, dV, mu, have_fmt_or_mf, ideal, part, nrm);
+    return;
   }
   // Pointwise terms in the bulk precision T (FP64 in FP64 mode); each thread
   // keeps Kahan partials in T over its few points, merged in FP64 across the

@@ -644,6 +644,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   C* Z1 = reinterpret_cast<C*>(sm + NB * ib + zb);
   __shared__ __align__(8) uint64_t bar[NB];
   const long ngroup = (d.rows + RB - 1) / RB;
+  if constexpr (DF_FUNC) df_log_table_init(threadIdx.x, blockDim.x);  // read after the barrier below
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) mbar_init(&bar[b], 1);

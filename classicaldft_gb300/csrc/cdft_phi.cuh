@@ -18,6 +18,8 @@ template <int MODEL> struct ModelTraits { static constexpr bool tensor = MODEL >
 template <class T> __device__ __forceinline__ T log1m(T e);
 template <> __device__ __forceinline__ double log1m<double>(double e) { return log(1.0 - e); }
 template <> __device__ __forceinline__ float log1m<float>(float e) { return log1pf(-e); }
+// df64: table-driven log1p on the FP32 pipe (the kernel initialises df_log_table first)
+template <> __device__ __forceinline__ dfs log1m<dfs>(dfs e) { return df_log1p(-e); }
 // natural logarithm in the argument's own precision (logf for FP32, never a promotion to FP64)
 template <class T> __device__ __forceinline__ T ln_t(T x);
 template <> __device__ __forceinline__ double ln_t<double>(double x) { return log(x); }
@@ -89,14 +91,12 @@ __device__ __forceinline__ void fmt_f(T e, T& f1, T& f2, T& f3, T& f1p, T& f2p, 
   f3p = (T)2 * g * g * g;
 }
 
-// The same f-functions for a df64 eta (the FP64 Phi pass keeps its values in df64):
-// computed in FP64 from the joined eta (the logarithm and the division), then split.
+// The same f-functions for a df64 eta (the FP64 Phi pass keeps its values in df64): the
+// same formulas in df64, the logarithm and the reciprocals too (cdft_df64.cuh), so the
+// pass runs no FP64 arithmetic per point. The kernel initialises df_log_table first.
 template <int MODEL>
 __device__ __forceinline__ void fmt_f_df(dfs e, dfs& f1, dfs& f2, dfs& f3, dfs& f1p, dfs& f2p, dfs& f3p) {
-  double a1, a2, a3, b1, b2, b3;
-  fmt_f<double, MODEL>(dfs_join(e), a1, a2, a3, b1, b2, b3);
-  f1 = dfs_split(a1); f2 = dfs_split(a2); f3 = dfs_split(a3);
-  f1p = dfs_split(b1); f2p = dfs_split(b2); f3p = dfs_split(b3);
+  fmt_f<dfs, MODEL>(e, f1, f2, f3, f1p, f2p, f3p);
 }
 
 // n[] holds the weighted densities in the order eta, s, v0, v1, v2, T00, T01,
