@@ -218,6 +218,13 @@ __global__ void k_compact(const double2* __restrict__ full, T* __restrict__ out,
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     out[i] = (T)((odd ? full[i].y : full[i].x) * scale);
 }
+// FP64 values to df64 pairs (hi = RN(d), lo = RN(d - hi))
+__global__ void k_split_df(const double* __restrict__ in, float2* __restrict__ out, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const dfs v = dfs_split(in[i]);
+    out[i] = make_float2(v.h, v.l);
+  }
+}
 template <class T>
 __global__ void k_round_spectra(const double* __restrict__ in, T* __restrict__ out, long n) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) out[i] = (T)in[i];
@@ -299,6 +306,7 @@ Evaluator<T>::~Evaluator() {
   cudaFree(A_); cudaFree(Cf_); cudaFree(E_); cudaFree(w_); cudaFree(watt_); cudaFree(part_); cudaFree(terms_); cudaFree(status_);
   cudaFree(NA_);
   cudaFree(wao_); cudaFree(XA_); cudaFree(S_); cudaFree(psi_); cudaFree(psir_); cudaFree(part_ao_);
+  cudaFree(wdf_); cudaFree(wattdf_);
 }
 
 template <class T>
@@ -403,6 +411,28 @@ bool Evaluator<T>::setup_tma(std::string* err) {
       uint64_t ws[2] = {ncol * sizeof(T), (uint64_t)Nc_ * sizeof(T)};
       uint32_t wb[3] = {(uint32_t)TC, (uint32_t)nx_, 1};
       ok = ok && encode_map(&mapWatt_, (int)sizeof(T), watt_, 3, wd, ws, wb);
+    }
+    // FP64 with compile-time plans on every axis: df64 copies of the weights for the
+    // double-float-spectra x passes (same geometry, 8-byte elements)
+    if (std::is_same<T, double>::value && fx_ > 0 && fy_ > 0 && fz_ > 0) {
+      const unsigned cg = (unsigned)std::min<long>(((long)std::max(M_, 1) * Nc_ + 255) / 256, 4096);
+      if (M_ > 0) {
+        if (!wdf_ && cudaMalloc(&wdf_, (size_t)M_ * Nc_ * sizeof(float2)) != cudaSuccess) return false;
+        k_split_df<<<cg, 256>>>(reinterpret_cast<const double*>(w_), static_cast<float2*>(wdf_), (long)M_ * Nc_);
+        uint64_t wd[3] = {ncol, (uint64_t)nx_, (uint64_t)M_};
+        uint64_t ws[2] = {ncol * 8, (uint64_t)Nc_ * 8};
+        uint32_t wb[3] = {(uint32_t)TC, (uint32_t)nx_, 1};
+        ok = ok && encode_map(&mapWdf_, 8, wdf_, 3, wd, ws, wb);
+      }
+      if (mf_) {
+        if (!wattdf_ && cudaMalloc(&wattdf_, (size_t)Nc_ * sizeof(float2)) != cudaSuccess) return false;
+        k_split_df<<<cg, 256>>>(reinterpret_cast<const double*>(watt_), static_cast<float2*>(wattdf_), Nc_);
+        uint64_t wd[3] = {ncol, (uint64_t)nx_, 1};
+        uint64_t ws[2] = {ncol * 8, (uint64_t)Nc_ * 8};
+        uint32_t wb[3] = {(uint32_t)TC, (uint32_t)nx_, 1};
+        ok = ok && encode_map(&mapWattdf_, 8, wattdf_, 3, wd, ws, wb);
+      }
+      if (cudaDeviceSynchronize() != cudaSuccess) return false;
     }
   }
   constexpr int TCY = TileColsY<T>::value;
@@ -788,7 +818,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     mark(2);
   }
   if (M_ > 0) {
-    if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
+    if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, decltype(io_)::value ? mapWdf_ : mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     mark(3);
     yinv(Cf_, mapYC_, M_, grid_tyM_);
@@ -830,7 +860,8 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     if (tma_)
       with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) {
         k_xbackconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tback_, s>>>(
-            mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
+            mapCf_, decltype(io_)::value ? mapWdf_ : mapW_, mapA_, decltype(io_)::value ? mapWattdf_ : mapWatt_, mapE_, M_, mf_ ? 1 : 0, d,
+            tx_->plan, twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
       });
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
@@ -875,7 +906,7 @@ int Evaluator<T>::hess_prepare(const double* rho0, cudaStream_t s) {
   });
   if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, -1, decltype(nf_)::value, decltype(io_)::value><<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_); });
   else k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
-  if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
+  if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, decltype(io_)::value ? mapWdf_ : mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
   else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
   if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, +1, decltype(nf_)::value, decltype(io_)::value><<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_); });
   else k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
@@ -926,7 +957,7 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
     yfwd(A_, mapYA_, 1, grid_ty1_);
   }
   if (M_ > 0) {
-    if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
+    if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, decltype(io_)::value ? mapWdf_ : mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     yinv(Cf_, mapYC_, M_, grid_tyM_);
     const unsigned g = (unsigned)((rows_ + rb_phi_ - 1) / rb_phi_);
@@ -952,7 +983,8 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
     if (tma_)
       with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) {
         k_xbackconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tback_, s>>>(
-            mapCf_, mapW_, mapA_, mapWatt_, mapE_, M_, mf_ ? 1 : 0, d, tx_->plan, twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
+            mapCf_, decltype(io_)::value ? mapWdf_ : mapW_, mapA_, decltype(io_)::value ? mapWattdf_ : mapWatt_, mapE_, M_, mf_ ? 1 : 0, d,
+            tx_->plan, twp<T>(tx_), mf_ ? part_mf : nullptr, status_);
       });
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
@@ -984,7 +1016,8 @@ void Evaluator<T>::fixed_plans() {
 
 template <class T>
 bool Evaluator<T>::df_candidate() const {
-  return kDf64Transforms && std::is_same<T, double>::value && fx_ > 0 && fy_ > 0 && fz_ > 0 && tma_ && !ao_ && M_ > 0;
+  return kDf64Transforms && std::is_same<T, double>::value && fx_ > 0 && fy_ > 0 && fz_ > 0 && tma_ && !ao_ && M_ > 0 && wdf_ &&
+         (!mf_ || wattdf_);
 }
 
 template <class T>

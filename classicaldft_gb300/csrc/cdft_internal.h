@@ -153,6 +153,11 @@ class Evaluator {
   // tensor-copy path (cdft_kernels_tma.cuh)
   bool tma_ = false;
   CUtensorMap mapA_, mapCf_, mapE_, mapW_, mapWatt_, mapYA_, mapYC_, mapYE_;
+  // FP64: the weight spectra again as df64 (hi, lo float pairs, 8 bytes like a double) for
+  // the x passes on double-float spectra, which then split no weight per tile
+  void* wdf_ = nullptr;
+  void* wattdf_ = nullptr;
+  CUtensorMap mapWdf_, mapWattdf_;
   size_t smem_ty_ = 0, smem_tconv_ = 0, smem_tback_ = 0;
   int grid_ty1_ = 0, grid_tyM_ = 0;
   bool tma_phi_ = false;

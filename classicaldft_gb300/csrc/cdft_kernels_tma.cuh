@@ -256,6 +256,12 @@ template <class T, int NF> struct XReg {
     if constexpr (df) return dfs_split((double)w);
     else return w;
   }
+  // weight e of a staged tile: FP64 weights split here, or (DFS) weights stored as df64
+  template <bool DFS>
+  __device__ static W load_weight(const T* tile, int e) {
+    if constexpr (df && DFS) return reinterpret_cast<const dfs*>(tile)[e];
+    else return weight(tile[e]);
+  }
   __device__ static C zero() {
     C z;
     if constexpr (df) z.x = z.y = dfs(0);
@@ -407,7 +413,7 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
       const int e = threadIdx.x + j * 256;
-      if (e < nel) reinterpret_cast<RC*>(in)[e] = mul_weight(R[j], XR::weight(Wst[b][e]), odd);
+      if (e < nel) reinterpret_cast<RC*>(in)[e] = mul_weight(R[j], XR::template load_weight<DFS>(Wst[b], e), odd);
     }
     if (threadIdx.x == 0) bulk_wait_read();
     __syncthreads();
@@ -475,6 +481,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
 #pragma unroll
   for (int j = 0; j < PER; ++j) S[j] = XR::zero();
   KahanT<T> pars;  // the mean-field energy by Parseval: compensated in the bulk precision, merged in FP64
+  dfs parsd = dfs(0);  // the same in df64 (DFS)
   bool ok = true;
   for (int a = 0; a < nsrc; ++a) {
     const int b = a & 1;
@@ -488,15 +495,21 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
       const int e = threadIdx.x + j * 256;
       if (e < nel) {
         const RC z = reinterpret_cast<const RC*>(res)[e];
-        const T wv = Wst[b][e];
-        S[j] = cadd(S[j], mul_weight(z, XR::weight(wv), odd));
+        const typename XR::W wv = XR::template load_weight<DFS>(Wst[b], e);
+        S[j] = cadd(S[j], mul_weight(z, wv, odd));
         if (is_mf) {
           const int col = col0 + (e % TC);
           const int kz = col % d.pz;
           if (kz < d.nzc && col < d.ny * d.pz) {
-            const T mult = (kz == 0 || 2 * kz == d.nz) ? (T)1 : (T)2;
-            const T zx = XR::re(z), zy = XR::im(z);
-            pars.add(mult * (zx * zx + zy * zy) * wv);
+            const bool one = (kz == 0 || 2 * kz == d.nz);
+            if constexpr (XR::df && DFS) {
+              const dfs q = (z.x * z.x + z.y * z.y) * wv;
+              parsd += one ? q : q + q;
+            } else {
+              const T mult = one ? (T)1 : (T)2;
+              const T zx = XR::re(z), zy = XR::im(z);
+              pars.add(mult * (zx * zx + zy * zy) * Wst[b][e]);
+            }
           }
         }
       }
@@ -504,6 +517,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
     __syncthreads();
     if (threadIdx.x == 0 && a + 2 < nsrc) issue(a + 2, b);
   }
+  if constexpr (XR::df && DFS) pars.add((T)dfs_join(parsd));
   if (part) block_kahan_store<1>(&pars, part, blockIdx.x);
   if (!__syncthreads_and(ok)) {
     if (threadIdx.x == 0) bulk_wait_all();
@@ -661,6 +675,9 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
       if (g < ngroup) issue(g, b);
     }
   KahanT<T> psum;
+  dfs psd = dfs(0);  // the df64 functional's sum (a thread's points), joined once
+  struct DfParams { dfs x, y, z, w; } dfi;  // 1/hsd, 1/hsd^2, esA, esB in df64
+  if constexpr (DF_FUNC) dfi = {dfs_split((double)ih), dfs_split((double)ih2), dfs_split((double)esA), dfs_split((double)esB)};
   unsigned st = 0;
   bool ok = true;
   for (long it = 0;; ++it) {
@@ -718,12 +735,10 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
           const dfc z = rd[k * LPd + PK::line(r, a)];
           nw[a] = PK::comp(r, a) ? z.y : z.x;
         }
-        const double eta = dfs_join(nw[0]);
-        const double phi = dfs_join(fmt_phi_point<dfs, MODEL>(nw, dfs_split((double)ih), dfs_split((double)ih2), dfs_split((double)esA),
-                                                               dfs_split((double)esB)));
-        if (eta > 0.5 && 1.0 - eta < 0.0) st |= 1u;
-        if (!isfinite(phi)) st |= 2u;
-        psum.add((T)phi);
+        if ((dfs(1) - nw[0]).h < 0.f) st |= 1u;  // eta > 1 (nw[0] is eta until the functional overwrites it)
+        const dfs phi = fmt_phi_point<dfs, MODEL>(nw, dfi.x, dfi.y, dfi.z, dfi.w);
+        if (!isfinite(phi.h)) st |= 2u;
+        psd += phi;
 #pragma unroll
         for (int p = 0; p < PK::per_row; ++p) {
           dfc z;
@@ -794,6 +809,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   }
   if constexpr (MODE == kPhiEval || MODE == kPhiAO) {
     if (st) atomicOr(status, st);
+    if constexpr (DF_FUNC) psum.add((T)dfs_join(psd));
     block_kahan_store<1>(&psum, part, blockIdx.x);
   }
   (void)E;

@@ -8,9 +8,10 @@ parameter must agree to the precision of BF16 operands (2^-9 relative rounding o
 GEMM operand, FP32 accumulation). Forward, that is 1e-2 on the loss; backward, the
 rounding of activations and gradients compounds through the six GEMM layers of the chain
 (the lift weights, deepest in it, come out ~4% off in norm), so each gradient must lie
-within 6e-2 of the FP64 gradient's norm (0.15 for the bias vectors, sums over all points
-of terms of both signs) and point the same way (cosine >= 0.998); the output bias's one
-live entry within 2e-2 of the size of its terms."""
+within 6e-2 of the FP64 gradient's norm and point the same way (cosine >= 0.998). A bias
+gradient is a sum over all points of terms of both signs, whose cancellation makes its norm
+a poor yardstick: each entry must lie within 3e-2 of the size of its terms (the sum of their
+magnitudes, from the FP64 network)."""
 import math
 
 import numpy as np
@@ -36,12 +37,19 @@ def _spectral64(v, W, shape, m):
     return torch.fft.irfftn(out, s=shape, dim=(1, 2, 3)).reshape(C, -1).t()
 
 
-def _forward64(p, feats, shape, m):
-    v = feats @ p["lift_w"] + p["lift_b"]
+def _forward64(p, feats, shape, m, pre=None):
+    """The network in FP64; pre (a dict) receives each bias's layer output (points x
+    channels, gradients retained), whose column sums are the bias gradients."""
+    def keep(name, z):
+        if pre is not None:
+            z.retain_grad()
+            pre[name] = z
+        return z
+    v = keep("lift_b", feats @ p["lift_w"] + p["lift_b"])
     for k in range(len(p["ws"])):
         W = torch.view_as_complex(p["spec"][k])
-        v = _gelu64(v @ p["ws"][k] + p["bs"][k] + _spectral64(v, W, shape, m))
-    h = _gelu64(v @ p["p1_w"] + p["p1_b"])
+        v = _gelu64(keep("bs%d" % k, v @ p["ws"][k] + p["bs"][k] + _spectral64(v, W, shape, m)))
+    h = _gelu64(keep("p1_b", v @ p["p1_w"] + p["p1_b"]))
     return (h @ p["p2_w"] + p["p2_b"])[:, 0]
 
 
@@ -73,9 +81,15 @@ def test_fno_gradients_match_fp64_cpu_network():
     p["ws"] = [w.detach().double().cpu().requires_grad_(True) for w in model.ws]
     p["bs"] = [b.detach().double().cpu().requires_grad_(True) for b in model.bs]
     p["spec"] = [s.w.detach().double().cpu().requires_grad_(True) for s in model.spec]
-    out64 = _forward64(p, feats.double().cpu(), shape, m)
+    pre = {}
+    out64 = _forward64(p, feats.double().cpu(), shape, m, pre)
     loss64 = torch.mean((out64 - target.double().cpu()) ** 2)
     loss64.backward()
+    # a bias gradient is a sum over all points of terms of both signs; its error is judged
+    # per channel against the size of those terms (the sum of their magnitudes)
+    terms = {name: torch.sum(torch.abs(z.grad), dim=0) for name, z in pre.items()}
+    bias_name = {id(model.lift_b): "lift_b", id(model.p1_b): "p1_b"}
+    bias_name.update({id(b): "bs%d" % k for k, b in enumerate(model.bs)})
     assert abs(float(loss.detach()) - float(loss64.detach())) <= 1e-2 * float(loss64.detach())
     pairs = [(model.lift_w, p["lift_w"]), (model.lift_b, p["lift_b"]), (model.p1_w, p["p1_w"]), (model.p1_b, p["p1_b"]),
              (model.p2_w, p["p2_w"]), (model.p2_b, p["p2_b"])]
@@ -89,9 +103,13 @@ def test_fno_gradients_match_fp64_cpu_network():
             scale = 2 * float(torch.mean(torch.abs(out64 - target.double().cpu())))
             assert abs(float(a[0] - b[0])) <= 2e-2 * scale and float(torch.abs(a[1:]).max()) == 0.0
             continue
+        if id(gpu) in bias_name:
+            name = bias_name[id(gpu)]
+            t = terms[name]
+            assert torch.allclose(pre[name].grad.sum(dim=0), b)  # the terms are this bias's
+            worst = float(torch.max(torch.abs(a - b) / torch.clamp(t, min=1e-300)))
+            assert worst <= 3e-2, (name, worst)
+            continue
         rel = float(torch.linalg.norm(a - b) / max(float(torch.linalg.norm(b)), 1e-300))
         cos = float(torch.sum(a * b) / max(float(torch.linalg.norm(a) * torch.linalg.norm(b)), 1e-300))
-        # a bias gradient is a sum over all points of terms of both signs, so its norm
-        # carries the cancellation of those sums: its direction is the sharper check
-        bar = 0.15 if gpu.dim() == 1 else 6e-2
-        assert rel <= bar and cos >= 0.998, (tuple(gpu.shape), rel, cos)
+        assert rel <= 6e-2 and cos >= 0.998, (tuple(gpu.shape), rel, cos)
