@@ -6,11 +6,11 @@ one JSON line on stdout.
          in HBM, timed with CUDA events per step; L2 flushed between steps.
 `e2e`    the same FP64 evaluation through the public C ABI from host buffers
          (host density in, host dF out, copies inside the timed region).
-`roofline`  the dominant FP64 pass against the device's FP64 FMA rate, measured in
-         the same run (GB300's FP64 unit, not HBM, bounds an all-FP64 pass), with its
-         HBM fraction beside it. The work counted is the pass's FP64-equivalent work
-         (what its all-FP64 form executes); the shipped pass does its transforms in
-         double-float on the FP32 pipe, so frac above 1 is its margin over that bound.
+`roofline`  the dominant pass of the FP64 evaluation (the Phi pass), which does its
+         arithmetic in double-float on the FP32 pipe: its executed FP32 work (ncu count
+         per launch) over its event-timed duration against the FP32 FMA rate measured in
+         the same run, with its HBM fraction and its FP64-equivalent rate (the all-FP64
+         form's work over this time, against the measured FP64 unit rate) beside it.
 `fp32`   the FP32-bulk evaluation of the same system (FP64 reductions): its rate,
          its error against FP64 on the same density, its HBM roofline.
 Extra keys: per-pass breakdowns, the time-to-residual legs (their converged
@@ -59,20 +59,24 @@ NCU_TRAFFIC = {("phi_rows", "fp32"): 98.1e6 + 40.0e6, ("phi_rows", "fp64"): 196.
 # FP64-equivalent work per launch of a pass: the FP64 add/mul/fma instructions (fma = 2)
 # the pass executes when all its arithmetic is FP64 (ncu on that build:
 # smsp__sass_thread_inst_executed_op_{dadd,dmul}_pred_on.sum + 2 x ..._dfma_pred_on.sum).
-# The shipped pass runs its transforms in double-float on the FP32 pipe, so the same
-# work over its time can exceed the FP64 unit's peak.
 NCU_FP64_FLOPS = {"phi_rows": 424.27e6 + 266.25e6 + 2 * 306.44e6}
-# what the shipped pass still executes on the FP64 pipe (same counters), and how busy
-# it keeps that pipe (sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active)
-NCU_FP64_EXECUTED = {"phi_rows": 129.55e6 + 33.63e6 + 2 * 53.21e6}
-NCU_FP64_PIPE_BUSY = {"phi_rows": 0.435}
+# What the shipped FP64 pass executes instead: its arithmetic runs in double-float on the
+# FP32 pipe. FP32 work per launch (ncu: smsp__sass_thread_inst_executed_op_{fadd,fmul}_pred_on.sum
+# + 2 x ..._ffma_pred_on.sum), how busy it keeps the FMA pipe
+# (sm__inst_executed_pipe_fma.avg.pct_of_peak_sustained_active) and the issue slots
+# (smsp__issue_active.avg.pct_of_peak_sustained_active); None where none was taken.
+NCU_FP32_FLOPS = {"phi_rows": None}
+NCU_FMA_PIPE_BUSY = {"phi_rows": 0.559}
+NCU_ISSUE_ACTIVE = {"phi_rows": 0.663}
+# FP64 instructions the shipped pass still executes (same counters)
+NCU_FP64_EXECUTED = {"phi_rows": 0.880e6 + 0.226e6 + 2 * 1.370e6}
 
 
-def fp64_fma_peak(cd):
-    """The device's sustained FP64 FMA rate in TFLOP/s, measured now (cdft_fp64_fma_rate)."""
+def fma_peak(cd, fn):
+    """The device's sustained FMA rate in TFLOP/s for one precision, measured now."""
     import ctypes
     v = ctypes.c_double()
-    if cd.lib().cdft_fp64_fma_rate(ctypes.byref(v), None) != 0:
+    if getattr(cd.lib(), fn)(ctypes.byref(v), None) != 0:
         return None
     return v.value
 
@@ -616,7 +620,8 @@ def main():
                 "dF_max_abs_over_dV": float(np.abs(dF32 - dF64).max() / DX ** 3)}
     n_per_eval = 11  # kernels per evaluation: 9 passes, one finish of the sums, one finish of the residual norms
     peak, peak_kind = measured_peaks()
-    fp64_peak = fp64_fma_peak(cd)
+    fp64_peak = fma_peak(cd, "cdft_fp64_fma_rate")
+    fp32_peak = fma_peak(cd, "cdft_fp32_fma_rate")
     N = int(np.prod(SHAPE))
     Nc = SHAPE[0] * SHAPE[1] * (SHAPE[2] // 2 + 1)
     M = 11
@@ -625,6 +630,8 @@ def main():
     top64 = max(passes64, key=lambda p: p["ms"])
     top32 = max(passes32, key=lambda p: p["ms"])
     ops = NCU_FP64_FLOPS.get(top64["pass"])
+    f32ops = NCU_FP32_FLOPS.get(top64["pass"])
+    t64s = top64["ms"] * 1e-3
     hbm64 = top64["bytes"] / (top64["ms"] * 1e-3) / 1e9  # the pass's algorithmic bytes at FP64 width
     line = {"metric": METRIC, "value": world * 1e3 / ms64, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
@@ -632,19 +639,22 @@ def main():
             "gpu_launches": n_per_eval * args.steps,
             "e2e": {"value": world / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(N * 8),
                     "d2h_bytes_per_step": int(N * 8 + 8 * 8)},
-            "roofline": {"bound": "fp64", "kernel": top64["pass"] + " (FP64)",
-                         "achieved": (ops / (top64["ms"] * 1e-3) / 1e12) if ops else None,
-                         "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": (ops / (top64["ms"] * 1e-3) / 1e12 / fp64_peak) if (ops and fp64_peak) else None,
-                         "flops_per_launch": ops,
-                         "flops_source": "FP64-equivalent work: FP64 add/mul/fma (fma = 2) per launch of the all-FP64 "
-                                         "build of the pass (ncu); the shipped pass runs its transforms in double-float "
-                                         "on the FP32 pipe, so frac > 1 is the margin over an FP64-unit-bound pass",
-                         "fp64_executed_per_launch": NCU_FP64_EXECUTED.get(top64["pass"]),
-                         "peak_source": "measured in this run: cdft_fp64_fma_rate (independent FMA chains on every SM)",
+            "roofline": {"bound": "fp32", "kernel": top64["pass"] + " (FP64 evaluation, double-float arithmetic on the FP32 pipe)",
+                         "achieved": (f32ops / t64s / 1e12) if f32ops else None, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": (f32ops / t64s / 1e12 / fp32_peak) if (f32ops and fp32_peak) else None,
+                         "flops_per_launch": f32ops,
+                         "flops_source": "executed FP32 add/mul/fma (fma = 2) per launch, ncu",
+                         "peak_source": "measured in this run: cdft_fp32_fma_rate (independent FMA chains on every SM)",
+                         "fma_pipe_busy": NCU_FMA_PIPE_BUSY.get(top64["pass"]),
+                         "issue_active": NCU_ISSUE_ACTIVE.get(top64["pass"]),
                          "traffic": NCU_TRAFFIC.get((top64["pass"], "fp64")),
-                         "fp64_pipe_busy": NCU_FP64_PIPE_BUSY.get(top64["pass"]),
-                         "hbm": {"achieved_gbs": hbm64, "peak_gbs": peak, "frac": hbm64 / peak, "peak_source": peak_kind}},
+                         "hbm": {"achieved_gbs": hbm64, "peak_gbs": peak, "frac": hbm64 / peak, "peak_source": peak_kind},
+                         "fp64_equivalent": {"flops_per_launch": ops, "achieved_tflops": (ops / t64s / 1e12) if ops else None,
+                                             "fp64_fma_peak_tflops": fp64_peak,
+                                             "ratio": (ops / t64s / 1e12 / fp64_peak) if (ops and fp64_peak) else None,
+                                             "fp64_executed_per_launch": NCU_FP64_EXECUTED.get(top64["pass"]),
+                                             "note": "the work of the all-FP64 form of the pass over this pass's time, against the "
+                                                     "FP64 unit's measured rate: the margin the double-float arithmetic buys"}},
             "eval_roofline": {"algorithmic_bytes_per_eval": B64, "achieved_gbs": B64 / (ms64 * 1e-3) / 1e9,
                               "frac": B64 / (ms64 * 1e-3) / 1e9 / peak},
             "passes_fp64": [{"pass": p["pass"], "ms": round(p["ms"], 4)} for p in passes64],

@@ -37,7 +37,7 @@ C_FUNCTIONS = [
     "cdft_newton_refine", "cdft_tc_gemm_bf16", "cdft_newton_refine_ex", "cdft_ddft_matrix_dot_v",
     "cdft_density_write", "cdft_density_read", "cdft_density_write_vtk", "cdft_log_det", "cdft_eigenvalue",
     "cdft_arnoldi_largest", "cdft_set_boundary", "cdft_ddft_set_mass_restore", "cdft_ddft_mass_deviation",
-    "cdft_fp64_fma_rate", "cdft_arnoldi_largest_matrix", "cdft_fire_save", "cdft_fire_load",
+    "cdft_fp64_fma_rate", "cdft_fp32_fma_rate", "cdft_arnoldi_largest_matrix", "cdft_fire_save", "cdft_fire_load",
 ]
 PASS_NAMES = ("rows_r2c", "cols_y_fwd(rho)", "xconv", "cols_y_inv(n_a)", "phi_rows", "cols_y_fwd(dPhi_a)", "xbackconv",
               "cols_y_inv(E)", "final_rows")
@@ -131,6 +131,7 @@ def lib():
             "cdft_ddft_init": ([vp, d, d, d], i), "cdft_ddft_step": ([vp, i, P(DdftReport)], i),
             "cdft_ddft_set_mass_restore": ([vp, i], i), "cdft_ddft_mass_deviation": ([vp, dp], i),
             "cdft_fp64_fma_rate": ([dp, vp], i),
+            "cdft_fp32_fma_rate": ([dp, vp], i),
             "cdft_fire_save": ([vp, ctypes.c_char_p], i), "cdft_fire_load": ([vp, ctypes.c_char_p], i),
             "cdft_time_passes": ([vp, i, dp, dp, P(i)], i),
             "cdft_fmt_weights": ([i, i, i, d, d, dp], i),

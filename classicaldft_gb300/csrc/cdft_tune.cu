@@ -191,43 +191,45 @@ extern "C" int cdft_radix_candidates(int n, int* out, int max_plans, int* count)
   return CDFT_OK;
 }
 
-// ------------------------------------------------- FP64 pipe rate probe ---
-// Sustained FP64 FMA rate of the current device: every thread runs kChains
-// independent dependent-FMA chains (enough in flight to cover the pipe's
-// latency), the grid fills every SM several times over. The result is what an
-// FP64-bound pass can reach at best, the denominator of its roofline.
+// ------------------------------------------- FP64 / FP32 pipe rate probes ---
+// Sustained FMA rate of the current device in one precision: every thread runs
+// kChains independent dependent-FMA chains (enough in flight to cover the pipe's
+// latency), the grid fills every SM several times over. The result is what a pass
+// bound by that pipe can reach at best, the denominator of its roofline.
 namespace {
 constexpr int kChains = 8, kIters = 2048;
-__global__ void __launch_bounds__(256) k_fp64_fma_chains(double b, double c, double* __restrict__ sink) {
-  double a[kChains];
+template <class T>
+__global__ void __launch_bounds__(256) k_fma_chains(T b, T c, T* __restrict__ sink) {
+  T a[kChains];
 #pragma unroll
-  for (int j = 0; j < kChains; ++j) a[j] = (double)(threadIdx.x + j) * 1e-3;
+  for (int j = 0; j < kChains; ++j) a[j] = (T)(threadIdx.x + j) * (T)1e-3;
   for (int i = 0; i < kIters; ++i)
 #pragma unroll
     for (int j = 0; j < kChains; ++j) a[j] = fma(a[j], b, c);
-  double s = 0;
+  T s = 0;
 #pragma unroll
   for (int j = 0; j < kChains; ++j) s += a[j];
-  if (s == 12345.678) sink[0] = s;  // never true for these inputs: keeps the chains live
+  if (s == (T)12345.678) sink[0] = s;  // never true for these inputs: keeps the chains live
 }
-}  // namespace
 
-int cdft_fp64_fma_rate(double* tflops, void* stream) {
+template <class T>
+int fma_rate(double* tflops, void* stream) {
   if (!tflops) return CDFT_ERR_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return CDFT_ERR_CUDA;
-  double* sink = nullptr;
-  if (cudaMalloc(&sink, sizeof(double)) != cudaSuccess) return CDFT_ERR_CUDA;
+  T* sink = nullptr;
+  if (cudaMalloc(&sink, sizeof(T)) != cudaSuccess) return CDFT_ERR_CUDA;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const unsigned grid = (unsigned)sms * 16;
-  k_fp64_fma_chains<<<grid, 256, 0, s>>>(0.999999, 1e-7, sink);  // warm-up
+  // FP32 runs 64x faster than FP64 here: a longer grid keeps its launches well above the timer's resolution
+  const unsigned grid = (unsigned)sms * (sizeof(T) == 8 ? 16 : 256);
+  k_fma_chains<T><<<grid, 256, 0, s>>>((T)0.999999, (T)1e-7, sink);  // warm-up
   float best = 1e30f;
   for (int r = 0; r < 5; ++r) {
     cudaEventRecord(e0, s);
-    k_fp64_fma_chains<<<grid, 256, 0, s>>>(0.999999, 1e-7, sink);
+    k_fma_chains<T><<<grid, 256, 0, s>>>((T)0.999999, (T)1e-7, sink);
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     float ms = 0;
@@ -243,3 +245,7 @@ int cdft_fp64_fma_rate(double* tflops, void* stream) {
   *tflops = flops / (best * 1e-3) / 1e12;
   return CDFT_OK;
 }
+}  // namespace
+
+int cdft_fp64_fma_rate(double* tflops, void* stream) { return fma_rate<double>(tflops, stream); }
+int cdft_fp32_fma_rate(double* tflops, void* stream) { return fma_rate<float>(tflops, stream); }

@@ -334,6 +334,9 @@ int cdft_radix_candidates(int n, int* out, int max_plans, int* count);
  * FMA rate in TFLOP/s (independent FMA chains on every SM, best of five timed
  * launches on `stream`), the ceiling of an FP64-bound pass. Allocates 8 bytes. */
 int cdft_fp64_fma_rate(double* tflops, void* stream);
+/* The same for FP32 FMAs: the ceiling of a pass bound by the FP32 pipe (the FP64
+ * passes' double-float arithmetic runs there). Allocates 4 bytes. */
+int cdft_fp32_fma_rate(double* tflops, void* stream);
 
 /* Newton-Krylov refinement of a minimum (no counterpart in the reference):
  * Newton corrections H d = -dF solved by preconditioned conjugate gradients
