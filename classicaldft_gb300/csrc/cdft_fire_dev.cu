@@ -15,6 +15,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 #include <thread>
 #include <vector>
 #include "cdft_ctx.h"
@@ -782,6 +783,13 @@ static void batch_start_fp64(BatchItem& b, double tol, long max_steps, cdft_fire
   if (phase_launch(b.c, &b.ph, kStepsPerRead) == 0) batch_finish(b, rep, 0);
 }
 
+// Host threads of a Newton-Krylov batch: CDFT_BATCH_THREADS (1-64) when set, else 8.
+static int batch_threads() {
+  const char* e = std::getenv("CDFT_BATCH_THREADS");
+  const int v = e ? std::atoi(e) : 0;
+  return v >= 1 && v <= 64 ? v : 8;
+}
+
 // mixed = 3: Newton-Krylov per context is host-driven (a synchronisation per CG
 // iteration), so contexts are spread over host threads, each context on its own
 // stream, and the GPU interleaves their kernels.
@@ -814,7 +822,7 @@ static int batch_newton(cdft_ctx* const* ctx, int n, double resid_tol, double sw
       if (reps) reps[i] = r;
     }
   };
-  const int nt = std::min(n, 8);
+  const int nt = std::min(n, batch_threads());
   std::vector<std::thread> pool;
   for (int t = 0; t < nt; ++t) pool.emplace_back(work);
   for (auto& t : pool) t.join();

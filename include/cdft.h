@@ -308,8 +308,9 @@ int cdft_fire_run_device(cdft_ctx* ctx, double resid_tol, double switch_tol, lon
  * previous ones have finished, so systems too small to fill the GPU overlap.
  * mixed is cdft_fire_run_device's (0 to 3; with 2 a context's Newton-Krylov
  * refinement runs on its own stream while the others' steps continue; with 3
- * the contexts are spread over up to 8 host threads, each driving its
- * contexts' Newton iterations on their own streams).
+ * the contexts are spread over host threads, 8 unless the environment variable
+ * CDFT_BATCH_THREADS sets 1 to 64, each driving its contexts' Newton iterations on
+ * their own streams).
  * Every context must have had cdft_fire_init and must appear once. reps[i] and
  * rcs[i] (either array may be NULL) receive each context's report and status;
  * the return value is the first non-zero status, or CDFT_OK. */
