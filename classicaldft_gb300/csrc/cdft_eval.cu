@@ -496,19 +496,22 @@ template <class T>
 bool Evaluator<T>::setup_phi_tma() {
   tma_phi_ = false;
   constexpr int E = ElemsPerComplex<T>::value;
-  if (!tma_ || M_ == 0 || (long)pz_ * E > 256) return false;
+  const int nf = phi_nf();
+  // the FP64 256-point instance copies each row group in two boxes of half a row
+  const bool split = sizeof(T) == 8 && nf == 256;
+  if (!tma_ || M_ == 0 || (long)pz_ * E > (split ? 512 : 256)) return false;
   int nsm = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const uint64_t cb = sizeof(C);
-  const int nf = phi_nf();
   const int RB = nf == 256 ? PhiRowsFor<T, 256>::value : PhiRowsFor<T, 128>::value;
   static_assert(PhiRowsFor<T, 128>::value == PhiRowsFor<T, 0>::value, "the runtime-plan instance groups rows as the 128-point one");
   const int L = phi_lines(M_, RB, PhiCross<T>::value);
   uint64_t dims[3] = {(uint64_t)pz_ * E, (uint64_t)rows_, (uint64_t)M_};
   uint64_t str[2] = {(uint64_t)pz_ * cb, (uint64_t)Nc_ * cb};
-  uint32_t box[3] = {(uint32_t)(pz_ * E), (uint32_t)RB, (uint32_t)M_};
-  smem_tphi_ = PhiBufs<T>::value * r128((size_t)M_ * RB * pz_ * cb) + 2 * r128((size_t)nz_ * (L | 1) * cb) + 1024;
+  uint32_t box[3] = {(uint32_t)(split ? pz_ * E / 2 : pz_ * E), (uint32_t)RB, (uint32_t)M_};
+  const size_t ib = split ? 2 * r128((size_t)M_ * RB * (pz_ / 2) * cb) : r128((size_t)M_ * RB * pz_ * cb);
+  smem_tphi_ = PhiBufs<T>::value * ib + 2 * r128((size_t)nz_ * (L | 1) * cb) + 1024;
   if (smem_tphi_ > 220 * 1024 || !encode_map(&mapR_, 8, Cf_, 3, dims, str, box)) return false;
   int blocks[4];  // resident blocks per SM of the Phi instances, by mode
   with_model(model_, [&](auto m) { PhiLauncher<T, decltype(m)::value>::prepare_tma(nf, ao_, smem_tphi_, blocks); });

@@ -290,8 +290,9 @@ __device__ __forceinline__ typename Cx<T>::type pair_spectrum(const typename Cx<
   return mk<T>(a.x - b.y, a.y + b.x);
 }
 
-// pair_spectrum on double-float spectra
-__device__ __forceinline__ dfc pair_spectrum_df(const dfc* __restrict__ A, const dfc* __restrict__ B, int k, int nz) {
+// pair_spectrum on double-float spectra (R: a pointer, or a row accessor with [] and bool)
+template <class R>
+__device__ __forceinline__ dfc pair_spectrum_df(const R& A, const R& B, int k, int nz) {
   const int nzc = nz / 2 + 1;
   const dfc zero{dfs(0), dfs(0)};
   dfc a, b;

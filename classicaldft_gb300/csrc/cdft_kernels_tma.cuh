@@ -588,6 +588,18 @@ template <int M, int RB, bool CROSS = true> struct PhiPack {
     }
   }
 };
+// the FP64 256-point instance reads its row groups in two tensor copies (a row of 264
+// doubles exceeds the 256-element box)
+template <class T, int NF> struct PhiSplit { static constexpr bool value = sizeof(T) == 8 && NF == 256; };
+// one row of df64 spectra in the Phi pass's input buffer: element k is p0[k] below `half`,
+// else p1[k - half] (the second box of a split row group)
+struct DfRow {
+  const dfc* p0 = nullptr;
+  const dfc* p1 = nullptr;
+  int half = 0;
+  __device__ __forceinline__ dfc operator[](int k) const { return k < half ? p0[k] : p1[k - half]; }
+  __device__ __forceinline__ explicit operator bool() const { return p0 != nullptr; }
+};
 // PhiPack<M, RB, cross>::L for a runtime M (host side)
 inline int phi_lines(int M, int RB, bool cross) { return (cross && M % 2 == 1 && RB % 2 == 0) ? (M / 2) * RB + RB / 2 : ((M + 1) / 2) * RB; }
 // the Phi pass pairs across rows in FP64 only
@@ -650,7 +662,13 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   unsigned char* sm = aligned_smem(smem_raw);
   // with a compile-time plan the row length is a constant too (the divisions below fold)
   const int nz = NF > 0 ? NF : d.nz, nzc = NF > 0 ? NF / 2 + 1 : d.nzc, pz = d.pz;
-  const size_t in_bytes = (size_t)M * RB * pz * sizeof(C), ib = r128(in_bytes);
+  // A 256-point FP64 row (132 complex, 264 doubles) is wider than a tensor copy's 256-element
+  // box: the group then arrives in two boxes, the first and second half of every row, each
+  // box a [M][RB][pz / 2] block (the second 128-byte aligned).
+  constexpr bool SPLIT = PhiSplit<T, NF>::value;
+  const int rowc = SPLIT ? pz / 2 : pz;  // complex values per row in one block
+  const size_t in_bytes = (size_t)M * RB * pz * sizeof(C), hb = r128((size_t)M * RB * rowc * sizeof(C));
+  const size_t ib = SPLIT ? 2 * hb : r128(in_bytes);
   const size_t zb = r128((size_t)nz * LPd * sizeof(C));
   constexpr int NB = PhiBufs<T>::value;
   C* In[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + (NB - 1) * ib)};
@@ -668,6 +686,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   auto issue = [&](long g, int b) {
     mbar_arrive_expect_tx(&bar[b], (unsigned)in_bytes);
     tma_load_3d(In[b], &mapR, 0, (int)(g * RB), 0, &bar[b]);
+    if constexpr (SPLIT) tma_load_3d(reinterpret_cast<unsigned char*>(In[b]) + hb, &mapR, rowc * E, (int)(g * RB), 0, &bar[b]);
   };
   if (threadIdx.x == 0)
     for (int b = 0; b < NB; ++b) {
@@ -694,11 +713,17 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
       int aA, rA, aB, rB;
       PK::source(line, 0, aA, rA);
       PK::source(line, 1, aB, rB);
-      const C* Arow = in + ((size_t)aA * RB + rA) * pz;
-      const C* Brow = aB >= 0 ? in + ((size_t)aB * RB + rB) * pz : nullptr;
-      if constexpr (DF)
-        reinterpret_cast<dfc*>(Z0)[k * LPd + line] = pair_spectrum_df(reinterpret_cast<const dfc*>(Arow), reinterpret_cast<const dfc*>(Brow), k, nz);
-      else Z0[k * LPd + line] = pair_spectrum<T>(Arow, Brow, k, nz);
+      if constexpr (DF) {
+        const dfc* h0 = reinterpret_cast<const dfc*>(in);
+        const dfc* h1 = reinterpret_cast<const dfc*>(reinterpret_cast<const unsigned char*>(in) + hb);
+        const DfRow Ar{h0 + ((size_t)aA * RB + rA) * rowc, h1 + ((size_t)aA * RB + rA) * rowc, rowc};
+        const DfRow Br = aB >= 0 ? DfRow{h0 + ((size_t)aB * RB + rB) * rowc, h1 + ((size_t)aB * RB + rB) * rowc, rowc} : DfRow{};
+        reinterpret_cast<dfc*>(Z0)[k * LPd + line] = pair_spectrum_df(Ar, Br, k, nz);
+      } else {
+        const C* Arow = in + ((size_t)aA * RB + rA) * pz;
+        const C* Brow = aB >= 0 ? in + ((size_t)aB * RB + rB) * pz : nullptr;
+        Z0[k * LPd + line] = pair_spectrum<T>(Arow, Brow, k, nz);
+      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {  // In[b] consumed: bring the group NB steps ahead

@@ -20,9 +20,8 @@ inline int resident(F f, int threads, size_t bytes) {
 }
 template <class T, class F>
 inline void with_phi_nf(int nf, F&& f) {
-  constexpr int n256 = phi_nf_instance<T>(256);
   if (nf == 128) f(std::integral_constant<int, 128>());
-  else if (nf == 256 && n256 == 256) f(std::integral_constant<int, n256>());
+  else if (nf == 256) f(std::integral_constant<int, 256>());
   else f(std::integral_constant<int, 0>());
 }
 }  // namespace phi_detail

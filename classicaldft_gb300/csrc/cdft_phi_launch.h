@@ -22,11 +22,6 @@ struct PhiArgs {
   double iph = 0, iph2 = 0;          // inverse polymer diameter and its square (AO)
 };
 
-// The plan length a tensor-copy instance is compiled for: 128 or 256 with the default radix
-// order, else 0 (the runtime plan). In FP64 only 128 has an instance: a 256-point z row does
-// not fit the tensor copy's 256-element box in FP64, so the pass never runs there.
-template <class T> constexpr int phi_nf_instance(int nf) { return nf == 128 ? 128 : (nf == 256 && sizeof(T) == 4 ? 256 : 0); }
-
 template <class T, int MODEL>
 struct PhiLauncher {
   // Raises the shared-memory limit of the tensor-copy instances for plan length nf to smem

@@ -55,8 +55,11 @@ def test_hessian_lj_vs_reference(cd, oracle):
 
 @pytest.mark.parametrize("shape,prec,tol", [((48, 48, 48), "FP64", 1e-12), ((40, 36, 30), "FP64", 1e-12),
                                             ((48, 48, 48), "FP32", 2e-5), ((128, 32, 128), "FP32", 2e-5),
-                                            ((128, 32, 128), "FP64", 1e-12), ((32, 16, 256), "FP32", 2e-5)])
+                                            ((128, 32, 128), "FP64", 1e-12), ((32, 16, 256), "FP32", 2e-5),
+                                            ((128, 128, 128), "FP64", 1e-12), ((128, 128, 256), "FP64", 1e-12)])
 def test_hessian_vs_oracle(cd, oracle, shape, prec, tol):
+    """The last two shapes take the double-float-spectra path of FP64 (compile-time plans on
+    every axis), the second with 256-point z rows copied in two boxes."""
     hsd = cd.bh_diameter(1.0, 1.0, 3.0, 0.8)
     c = cd.Context(shape, 0.1, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.8, precision=getattr(cd, prec))
     rho = oracle.fill_noise(shape, 0.4, 0.3, 9)

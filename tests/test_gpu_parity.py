@@ -150,10 +150,12 @@ def test_config2_128_fp64_and_fp32_vs_oracle(cd, oracle):
     assert np.abs(dF32 - dFo).max() <= 2e-6 * np.abs(dFo).max()
 
 
-@pytest.mark.parametrize("shape", [(256, 16, 256), (16, 256, 24)])
+@pytest.mark.parametrize("shape", [(256, 16, 256), (16, 256, 24), (128, 128, 256)])
 def test_256_point_axes_vs_oracle(cd, oracle, shape):
     """Axes of 256 points run the compile-time 256-point plans (x and z in the first shape,
-    y in the second): FP64 at the reference bars. In FP32 the error of dF is relative to the
+    y in the second; every axis in the third, whose FP64 spectra stay in double-float between
+    passes and whose 256-point z rows reach the Phi pass in two tensor copies): FP64 at the
+    reference bars. In FP32 the error of dF is relative to the
     terms that cancel in it near equilibrium (ln rho + c1 against mu, each of order |mu| dV),
     so the FP32 bar on dF is 2e-6 of the larger of max|dF| and |mu| dV."""
     dx = 0.1
