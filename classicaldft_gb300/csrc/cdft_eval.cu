@@ -689,6 +689,12 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
   set_smem<T>(k_rows_r2c<T, double, 256>, smem_rows_);
   set_smem<T>(k_cols_fft<T, -1>, std::max(smem_colx_, smem_coly_));
   set_smem<T>(k_cols_fft<T, +1>, std::max(smem_colx_, smem_coly_));
+  set_smem<T>(k_cols_fft<T, -1, 128>, std::max(smem_colx_, smem_coly_));
+  set_smem<T>(k_cols_fft<T, +1, 128>, std::max(smem_colx_, smem_coly_));
+  set_smem<T>(k_cols_fft<T, -1, 256>, std::max(smem_colx_, smem_coly_));
+  set_smem<T>(k_cols_fft<T, +1, 256>, std::max(smem_colx_, smem_coly_));
+  set_smem<T>(k_rows_c2r<T, double, 128>, smem_rows_);
+  set_smem<T>(k_rows_c2r<T, double, 256>, smem_rows_);
   set_smem<T>(k_xconv<T>, smem_xconv_);
   set_smem<T>(k_xbackconv<T>, smem_xback_);
   if (M_ > 0) with_model(model_, [&](auto m) { PhiLauncher<T, decltype(m)::value>::prepare_rows(smem_phi_); });
@@ -764,19 +770,35 @@ int Evaluator<T>::init(int nx, int ny, int nz, int model, double hsd, double esA
 template <class T>
 void Evaluator<T>::r2c(const double* in, C* out, cudaStream_t s) {
   Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
-  k_rows_r2c<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(in, out, d, tz_->plan, twp<T>(tz_), rb_rows_);
-  k_cols_fft<T, -1><<<dim3((unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_coly_, s>>>(out, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
-  k_cols_fft<T, -1><<<dim3((unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_), 1), 256, smem_colx_, s>>>(out, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  const unsigned gy = (unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_), gx = (unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_);
+  with_nf(fz_, [&](auto nf_) {
+    k_rows_r2c<T, double, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(in, out, d, tz_->plan, twp<T>(tz_),
+                                                                                                    rb_rows_);
+  });
+  with_nf(fy_, [&](auto nf_) {
+    k_cols_fft<T, -1, decltype(nf_)::value><<<dim3(gy, 1), 256, smem_coly_, s>>>(out, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  });
+  with_nf(fx_, [&](auto nf_) {
+    k_cols_fft<T, -1, decltype(nf_)::value><<<dim3(gx, 1), 256, smem_colx_, s>>>(out, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  });
 }
 
 template <class T>
 void Evaluator<T>::c2r(const C* in, double* out, T scale, cudaStream_t s) {
   Dims d{nx_, ny_, nz_, nzc_, N_, Nc_, rows_, pz_};
-  C* work = E_;
+  const unsigned gy = (unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_), gx = (unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_);
+  C* work = E_;  // scratch between evaluations (the next evaluation rewrites it)
   cudaMemcpyAsync(work, in, Nc_ * sizeof(C), cudaMemcpyDeviceToDevice, s);
-  k_cols_fft<T, +1><<<dim3((unsigned)(((long)ny_ * pz_ + tc_ - 1) / tc_), 1), 256, smem_colx_, s>>>(work, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
-  k_cols_fft<T, +1><<<dim3((unsigned)(((long)nx_ * nzc_ + tc_ - 1) / tc_), 1), 256, smem_coly_, s>>>(work, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
-  k_rows_c2r<T, double><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(work, out, d, tz_->plan, twp<T>(tz_), rb_rows_, scale);
+  with_nf(fx_, [&](auto nf_) {
+    k_cols_fft<T, +1, decltype(nf_)::value><<<dim3(gx, 1), 256, smem_colx_, s>>>(work, 0, 0, d, tx_->plan, twp<T>(tx_), tc_);
+  });
+  with_nf(fy_, [&](auto nf_) {
+    k_cols_fft<T, +1, decltype(nf_)::value><<<dim3(gy, 1), 256, smem_coly_, s>>>(work, 0, 1, d, ty_->plan, twp<T>(ty_), tc_);
+  });
+  with_nf(fz_, [&](auto nf_) {
+    k_rows_c2r<T, double, decltype(nf_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(work, out, d, tz_->plan, twp<T>(tz_),
+                                                                                                    rb_rows_, scale);
+  });
 }
 
 template <class T>

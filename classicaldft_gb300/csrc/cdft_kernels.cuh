@@ -366,7 +366,7 @@ __device__ __forceinline__ void store_cols(const typename Cx<T>::type* __restric
   }
 }
 
-template <class T, int DIR>
+template <class T, int DIR, int NF = 0>
 __global__ void __launch_bounds__(256) k_cols_fft(typename Cx<T>::type* __restrict__ data, long field_stride, int axis, Dims d,
                                                   FFTPlan P, const typename Cx<T>::type* __restrict__ tw, int TC) {
   typedef typename Cx<T>::type C;
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(256) k_cols_fft(typename Cx<T>::type* __restri
   const long stride = axis == 0 ? (long)d.ny * d.pz : (long)d.pz;
   const long c0 = (long)blockIdx.x * TC;
   load_cols<T>(b0, g, axis, c0, ncol, n, stride, TC, LP, d);
-  C* res = block_fft<DIR, T>(b0, b1, TC, LP, P, tw);
+  C* res = rows_fft<DIR, T, NF>(b0, b1, TC, LP, P, tw);  // the compile-time plan when NF > 0 (df64 in FP64)
   store_cols<T>(res, g, axis, c0, ncol, n, stride, TC, LP, d);
 }
 
