@@ -290,7 +290,9 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
   unsigned char* sm = aligned_smem(smem_raw);
   const int n = P.n;
   const size_t tile_bytes = (size_t)n * TC * sizeof(C), tb = r128(tile_bytes);
-  C* stage[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + tb)};
+  // buffers by address arithmetic (an array of pointers indexed by the stage would live in
+  // local memory)
+  auto stage = [&](int b) { return reinterpret_cast<C*>(sm + (size_t)b * tb); };
   C* work = reinterpret_cast<C*>(sm + 2 * tb);
   __shared__ __align__(8) uint64_t bar[2];
   const int ntile = (d.nzc + TC - 1) / TC;
@@ -312,7 +314,7 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
     int kz0, x, f;
     coords(item, kz0, x, f);
     mbar_arrive_expect_tx(&bar[b], (unsigned)tile_bytes);
-    tma_load_4d(stage[b], &map, kz0 * E, 0, x, f, &bar[b]);
+    tma_load_4d(stage(b), &map, kz0 * E, 0, x, f, &bar[b]);
   };
   if (threadIdx.x == 0) {
     for (int b = 0; b < 2; ++b) {
@@ -330,7 +332,7 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
     // buffer) before this tile's transform writes work
     if (threadIdx.x == 0) bulk_wait_read();
     if (!__syncthreads_and(ok)) break;
-    C* res = xfft<DIR, T, TC, NF, !DFS, !DFS>(stage[b], work, P, tw);
+    C* res = xfft<DIR, T, TC, NF, !DFS, !DFS>(stage(b), work, P, tw);
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -340,7 +342,7 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
       bulk_commit();
       const long next = item + 2L * gridDim.x;
       if (next < total) {
-        if (res == stage[b]) bulk_wait_read();  // the store reads the buffer about to be refilled
+        if (res == stage(b)) bulk_wait_read();  // the store reads the buffer about to be refilled
         issue(next, b);
       }
     }
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
   const size_t tb = r128(tile_bytes), wb = r128(wbytes);
   C* X = reinterpret_cast<C*>(sm);
   C* Y = reinterpret_cast<C*>(sm + tb);
-  T* Wst[2] = {reinterpret_cast<T*>(sm + 2 * tb), reinterpret_cast<T*>(sm + 2 * tb + wb)};
+  auto Wst = [&](int b) { return reinterpret_cast<T*>(sm + 2 * tb + (size_t)b * wb); };  // not a pointer array (local memory)
   __shared__ __align__(8) uint64_t bar[3];  // 0, 1: weights; 2: density tile
   const int col0 = blockIdx.x * TC;
   const int nel = n * TC;
@@ -383,7 +385,7 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
     tma_load_3d(X, &mapA, col0 * E, 0, 0, &bar[2]);
     for (int b = 0; b < 2 && b < M; ++b) {
       mbar_arrive_expect_tx(&bar[b], (unsigned)wbytes);
-      tma_load_3d(Wst[b], &mapW, col0, 0, b, &bar[b]);
+      tma_load_3d(Wst(b), &mapW, col0, 0, b, &bar[b]);
     }
   }
   bool ok = mbar_wait(&bar[2], 0, status);
@@ -413,13 +415,13 @@ __global__ void __launch_bounds__(256, 2) k_xconv_tma(const __grid_constant__ CU
 #pragma unroll
     for (int j = 0; j < PER; ++j) {
       const int e = threadIdx.x + j * 256;
-      if (e < nel) reinterpret_cast<RC*>(in)[e] = mul_weight(R[j], XR::template load_weight<DFS>(Wst[b], e), odd);
+      if (e < nel) reinterpret_cast<RC*>(in)[e] = mul_weight(R[j], XR::template load_weight<DFS>(Wst(b), e), odd);
     }
     if (threadIdx.x == 0) bulk_wait_read();
     __syncthreads();
     if (threadIdx.x == 0 && a + 2 < M) {
       mbar_arrive_expect_tx(&bar[b], (unsigned)wbytes);
-      tma_load_3d(Wst[b], &mapW, col0, 0, a + 2, &bar[b]);
+      tma_load_3d(Wst(b), &mapW, col0, 0, a + 2, &bar[b]);
     }
     C* r2 = xfft<+1, T, TC, NF, false, !DFS>(in, other, px, tw);
     fence_async_smem();
@@ -450,9 +452,9 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
   const int n = px.n;
   const size_t tile_bytes = (size_t)n * TC * sizeof(C), wbytes = (size_t)n * TC * sizeof(T);
   const size_t tb = r128(tile_bytes), wb = r128(wbytes);
-  C* Dst[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + tb)};
+  auto Dst = [&](int b) { return reinterpret_cast<C*>(sm + (size_t)b * tb); };  // not pointer arrays (local memory)
   C* Y = reinterpret_cast<C*>(sm + 2 * tb);
-  T* Wst[2] = {reinterpret_cast<T*>(sm + 3 * tb), reinterpret_cast<T*>(sm + 3 * tb + wb)};
+  auto Wst = [&](int b) { return reinterpret_cast<T*>(sm + 3 * tb + (size_t)b * wb); };
   __shared__ __align__(8) uint64_t bar[2];
   const int col0 = blockIdx.x * TC;
   const int nel = n * TC;
@@ -466,11 +468,11 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
   auto issue = [&](int a, int b) {
     mbar_arrive_expect_tx(&bar[b], (unsigned)(tile_bytes + wbytes));
     if (a < M) {
-      tma_load_3d(Dst[b], &mapD, col0 * E, 0, a, &bar[b]);
-      tma_load_3d(Wst[b], &mapW, col0, 0, a, &bar[b]);
+      tma_load_3d(Dst(b), &mapD, col0 * E, 0, a, &bar[b]);
+      tma_load_3d(Wst(b), &mapW, col0, 0, a, &bar[b]);
     } else {
-      tma_load_3d(Dst[b], &mapA, col0 * E, 0, 0, &bar[b]);
-      tma_load_3d(Wst[b], &mapWatt, col0, 0, 0, &bar[b]);
+      tma_load_3d(Dst(b), &mapA, col0 * E, 0, 0, &bar[b]);
+      tma_load_3d(Wst(b), &mapWatt, col0, 0, 0, &bar[b]);
     }
   };
   if (threadIdx.x == 0)
@@ -487,7 +489,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
     const int b = a & 1;
     ok = mbar_wait(&bar[b], (unsigned)((a >> 1) & 1), status);
     if (!__syncthreads_and(ok)) break;
-    C* res = xfft<-1, T, TC, NF, !DFS, false>(Dst[b], Y, px, tw);
+    C* res = xfft<-1, T, TC, NF, !DFS, false>(Dst(b), Y, px, tw);
     const bool is_mf = (a == M);
     const bool odd = !is_mf && weight_is_odd(a);
 #pragma unroll
@@ -495,7 +497,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
       const int e = threadIdx.x + j * 256;
       if (e < nel) {
         const RC z = reinterpret_cast<const RC*>(res)[e];
-        const typename XR::W wv = XR::template load_weight<DFS>(Wst[b], e);
+        const typename XR::W wv = XR::template load_weight<DFS>(Wst(b), e);
         S[j] = cadd(S[j], mul_weight(z, wv, odd));
         if (is_mf) {
           const int col = col0 + (e % TC);
@@ -508,7 +510,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
             } else {
               const T mult = one ? (T)1 : (T)2;
               const T zx = XR::re(z), zy = XR::im(z);
-              pars.add(mult * (zx * zx + zy * zy) * Wst[b][e]);
+              pars.add(mult * (zx * zx + zy * zy) * Wst(b)[e]);
             }
           }
         }
@@ -523,7 +525,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
     if (threadIdx.x == 0) bulk_wait_all();
     return;
   }
-  C* X = Dst[0];
+  C* X = Dst(0);
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int e = threadIdx.x + j * 256;
@@ -671,7 +673,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   const size_t ib = SPLIT ? 2 * hb : r128(in_bytes);
   const size_t zb = r128((size_t)nz * LPd * sizeof(C));
   constexpr int NB = PhiBufs<T>::value;
-  C* In[2] = {reinterpret_cast<C*>(sm), reinterpret_cast<C*>(sm + (NB - 1) * ib)};
+  auto In = [&](int b) { return reinterpret_cast<C*>(sm + (size_t)(b % NB) * ib); };  // not a pointer array (local memory)
   C* Z0 = reinterpret_cast<C*>(sm + NB * ib);
   C* Z1 = reinterpret_cast<C*>(sm + NB * ib + zb);
   __shared__ __align__(8) uint64_t bar[NB];
@@ -685,8 +687,8 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   __syncthreads();
   auto issue = [&](long g, int b) {
     mbar_arrive_expect_tx(&bar[b], (unsigned)in_bytes);
-    tma_load_3d(In[b], &mapR, 0, (int)(g * RB), 0, &bar[b]);
-    if constexpr (SPLIT) tma_load_3d(reinterpret_cast<unsigned char*>(In[b]) + hb, &mapR, rowc * E, (int)(g * RB), 0, &bar[b]);
+    tma_load_3d(In(b), &mapR, 0, (int)(g * RB), 0, &bar[b]);
+    if constexpr (SPLIT) tma_load_3d(reinterpret_cast<unsigned char*>(In(b)) + hb, &mapR, rowc * E, (int)(g * RB), 0, &bar[b]);
   };
   if (threadIdx.x == 0)
     for (int b = 0; b < NB; ++b) {
@@ -706,7 +708,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
     ok = mbar_wait(&bar[b], (unsigned)((it / NB) & 1), status);
     if (!__syncthreads_and(ok)) break;
     const long row0 = g * RB;
-    const C* in = In[b];
+    const C* in = In(b);
     // packed Hermitian spectra (PhiPack's lines), element k of [nz][L]
     for (int e = threadIdx.x; e < nz * L; e += blockDim.x) {
       const int line = e % L, k = e / L;
@@ -726,7 +728,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {  // In[b] consumed: bring the group NB steps ahead
+    if (threadIdx.x == 0) {  // In(b) consumed: bring the group NB steps ahead
       const long gn = g + (long)NB * gridDim.x;
       if (gn < ngroup) issue(gn, b);
     }
