@@ -760,6 +760,13 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
   const int nz = NF > 0 ? NF : d.nz, LP = nz + 1;
   C* b1 = b0 + RB * LP;
   const long pair0 = (long)blockIdx.x * RB;
+  {  // the block's densities (its rows are consecutive) into L2 now: they are read after the
+     // transform, and by then the evaluation's earlier passes have long evicted them
+    const char* r0 = reinterpret_cast<const char*>(rho + 2 * pair0 * nz);
+    const long nbytes = (long)(min(2L * RB, d.rows - 2 * pair0) * nz) * (long)sizeof(RT);
+    for (long o = (long)threadIdx.x * 128; o < nbytes; o += (long)blockDim.x * 128)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(r0 + o));
+  }
   C* res = b0;
   if (have_fmt_or_mf) {
 #pragma unroll 4
