@@ -396,13 +396,13 @@ static int map_reduce(cdft_ctx* c, long n, F f, double* host_out) {
 // DFT::calculateFreeEnergyAndDerivatives_internal_, Species::endForceCalculation.
 // Grand-canonical evaluation as one graph launch and one synchronisation:
 // the pass sequence, max|dF| and the copies of every sum to pinned memory.
-static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
+static int eval_graph(cdft_ctx* c, double* terms8, int only_fex, double* mirror = nullptr) {
   const long N = c->info.N;
   const double dV = c->info.dV;
   const int gi = c->precision == CDFT_FP64 ? 1 : 0;
   cudaGraphExec_t& exec = c->eval_exec[gi];
   if (!exec || c->eg_only_fex[gi] != only_fex || c->eg_vext[gi] != c->vext || c->eg_mu[gi] != c->mu ||
-      c->eg_plan_gen[gi] != c->plan_gen) {
+      c->eg_plan_gen[gi] != c->plan_gen || c->eg_mirror[gi] != mirror) {
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
     if (!c->cap_stream) CUDA_OR_FAIL(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
@@ -414,8 +414,8 @@ static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
     // the final row pass stores the dF-norm partials itself when they fit red_part
     const long fb = c->precision == CDFT_FP64 ? c->e64->final_blocks() : c->e32->final_blocks();
     double* nrm = 2 * fb <= kRedPartLen ? c->red_part : nullptr;
-    if (c->precision == CDFT_FP64) rc = c->e64->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s, nullptr, nrm);
-    else rc = c->e32->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s, nullptr, nrm);
+    if (c->precision == CDFT_FP64) rc = c->e64->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s, nullptr, nrm, mirror);
+    else rc = c->e32->launch(c->rho, c->vext, c->dF, dV, c->mu, only_fex ? 0 : 1, s, nullptr, nrm, mirror);
     if (nrm) {
       k_dF_norms_finish<<<1, 256, 0, s>>>(c->red_part, (int)fb, c->red_out);
     } else {
@@ -440,6 +440,7 @@ static int eval_graph(cdft_ctx* c, double* terms8, int only_fex) {
     c->eg_vext[gi] = c->vext;
     c->eg_mu[gi] = c->mu;
     c->eg_plan_gen[gi] = c->plan_gen;
+    c->eg_mirror[gi] = mirror;
   }
   CUDA_OR_FAIL(c, cudaGraphLaunch(exec, c->stream));
   CUDA_OR_FAIL(c, cudaStreamSynchronize(c->stream));
@@ -475,12 +476,18 @@ void cdft_internal_boundary_set(cdft_ctx* c, double* a, double value) {
   k_boundary_set<<<grid_for(c->info.N), 256, 0, c->stream>>>(a, c->info.N, c->p.ny, c->p.nz, value);
 }
 
-static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0) {
+// mirror (optional, device-visible): the graph path's final pass also stores dF there;
+// *mirrored tells whether it did.
+static int eval_internal(cdft_ctx* c, double* terms8, int only_fex = 0, double* mirror = nullptr, bool* mirrored = nullptr) {
   const long N = c->info.N;
   const double dV = c->info.dV;
   int rc = ensure_evaluator(c, c->precision);
   if (rc) return rc;
-  if (c->fixed_mass <= 0 && !c->fixed_bg && !c->homo_bd) return eval_graph(c, terms8, only_fex);
+  if (mirrored) *mirrored = false;
+  if (c->fixed_mass <= 0 && !c->fixed_bg && !c->homo_bd) {
+    if (mirrored) *mirrored = mirror != nullptr;
+    return eval_graph(c, terms8, only_fex, mirror);
+  }
   if (c->fixed_bg && c->fixed_mass > 0)  // src/Species.cpp:75-76
     return fail(c, CDFT_ERR_ARG, "Cannot have both fixed background and fixed mass .... aborting");
   if (c->fixed_mass > 0) {  // src/Species.cpp:64-71
@@ -821,8 +828,20 @@ int cdft_ddft_matrix_dot_v(cdft_ctx* c, const double* v, double* out, int on_dev
 
 int cdft_eval(cdft_ctx* c, int only_fex, double* terms, double* dF, int on_device) {
   if (!c) return CDFT_ERR_ARG;
-  int rc = eval_internal(c, terms, only_fex);
-  if (dF && (rc == CDFT_OK || rc == CDFT_ERR_ETA)) {
+  // a page-locked host dF: the final row pass writes it directly (over the host link while
+  // the pass runs) instead of a copy after the evaluation
+  double* mirror = nullptr;
+  if (dF && !on_device) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, dF) == cudaSuccess) {
+      if (a.type == cudaMemoryTypeHost && a.devicePointer) mirror = static_cast<double*>(a.devicePointer);
+    } else {
+      cudaGetLastError();  // not a CUDA-known pointer: the copy path below
+    }
+  }
+  bool mirrored = false;
+  int rc = eval_internal(c, terms, only_fex, mirror, &mirrored);
+  if (dF && !mirrored && (rc == CDFT_OK || rc == CDFT_ERR_ETA)) {
     if (cudaMemcpyAsync(dF, c->dF, c->info.N * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream) !=
             cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess)

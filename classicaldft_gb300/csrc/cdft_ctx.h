@@ -70,6 +70,7 @@ struct cdft_ctx {
   const double* eg_vext[2] = {nullptr, nullptr};
   double eg_mu[2] = {0, 0};
   unsigned plan_gen = 0, eg_plan_gen[2] = {~0u, ~0u};
+  double* eg_mirror[2] = {nullptr, nullptr};  // the host dF the graph's final pass also writes
   unsigned* host_status = nullptr;  // pinned
   double last_dF_l2 = 0;            // ||dF||_2 / dV of the last evaluation
   // Hessian-vector product buffers (device, N doubles each; allocated on first use)

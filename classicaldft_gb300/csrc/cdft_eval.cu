@@ -804,7 +804,7 @@ void Evaluator<T>::c2r(const C* in, double* out, T scale, cudaStream_t s) {
 template <class T>
 template <class RT>
 int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, double mu, int ideal, cudaStream_t s, cudaEvent_t* ev,
-                         double* nrm) {
+                         double* nrm, RT* dF_mirror) {
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
   };
@@ -901,7 +901,8 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
   const unsigned gfin = (unsigned)grid_blocks_rows();
   with_nf_io<T>(fz_, io, [&](auto nf_, auto io_) {
     k_final_rows<T, RT, decltype(nf_)::value, decltype(io_)::value><<<gfin, 256, smem_rows_, s>>>(E_, rho, vext, dF, d, tz_->plan, twp<T>(tz_),
-                                                                                                 rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin, nrm);
+                                                                                                 rb_rows_, dV, mu, any ? 1 : 0, ideal, part_fin, nrm,
+                                                                                                 dF_mirror);
   });
   {
     const FinishSeg sphi{part_phi, phi_blocks_last_, M_ > 0 ? 1 : 0, terms_ + 0};
@@ -1103,7 +1104,7 @@ int Evaluator<T>::eval(const double* rho, const double* vext, double* dF, double
 template class Evaluator<float>;
 template class Evaluator<double>;
 template int Evaluator<float>::launch<float>(const float*, const double*, float*, double, double, int, cudaStream_t, cudaEvent_t*,
-                                             double*);
+                                             double*, float*);
 template int Evaluator<float>::hess_apply<float>(const float*, const double*, float*, double, cudaStream_t);
 template int Evaluator<float>::hess_apply<double>(const double*, const double*, double*, double, cudaStream_t);
 template int Evaluator<double>::hess_apply<double>(const double*, const double*, double*, double, cudaStream_t);

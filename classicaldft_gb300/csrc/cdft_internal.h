@@ -67,12 +67,14 @@ class Evaluator {
   // RT: storage type of rho and dF (double, or T for an all-T pipeline).
   // nrm (optional, 2 * final_blocks() doubles): the final row pass also stores
   // per block (sum dF^2, max |dF|) there, the partials k_dF_norms would make.
+  // dF_mirror (optional, N values, device-visible, e.g. pinned host memory): the final row
+  // pass stores dF there too, so that a caller's host copy needs no separate transfer.
   template <class RT>
   int launch(const RT* rho, const double* vext, RT* dF, double dV, double mu, int ideal, cudaStream_t s, cudaEvent_t* ev = nullptr,
-             double* nrm = nullptr);
+             double* nrm = nullptr, RT* dF_mirror = nullptr);
   int launch(const double* rho, const double* vext, double* dF, double dV, double mu, int ideal, cudaStream_t s,
-             cudaEvent_t* ev = nullptr, double* nrm = nullptr) {
-    return launch<double>(rho, vext, dF, dV, mu, ideal, s, ev, nrm);
+             cudaEvent_t* ev = nullptr, double* nrm = nullptr, double* dF_mirror = nullptr) {
+    return launch<double>(rho, vext, dF, dV, mu, ideal, s, ev, nrm, dF_mirror);
   }
   long final_blocks() const { return grid_blocks_rows(); }
   bool has_mf() const { return mf_; }

@@ -691,7 +691,7 @@ template <class RT>
 __device__ __forceinline__ void final_points_df(const double2* __restrict__ res, const RT* __restrict__ rho,
                                                 const double* __restrict__ vext, RT* __restrict__ dF, const Dims& d, int RB,
                                                 int LP, int nz, long pair0, double dV, double mu, int have_fmt_or_mf, int ideal,
-                                                double* __restrict__ part, double* __restrict__ nrm) {
+                                                double* __restrict__ part, double* __restrict__ nrm, RT* __restrict__ dF2) {
   const dfc* rd = reinterpret_cast<const dfc*>(res);
   const dfs dVd = dfs_split(dV), mud = dfs_split(mu);
   dfs a0 = dfs(0), a1 = dfs(0), a2 = dfs(0), a3 = dfs(0), aq = dfs(0), mx = dfs(0);
@@ -713,7 +713,9 @@ __device__ __forceinline__ void final_points_df(const double2* __restrict__ res,
       f += ve * dVd;
     }
     f += -mud * dVd;
-    dF[p] = (RT)dfs_join(f);
+    const RT fv = (RT)dfs_join(f);
+    dF[p] = fv;
+    if (dF2) dF2[p] = fv;
     if (ideal) a0 += (r0 * lr - r0) * dVd;
     a1 += r0;
     if (vext) a2 += ve * r0;
@@ -748,7 +750,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
                                                     const double* __restrict__ vext, RT* __restrict__ dF, Dims d, FFTPlan pz,
                                                     const typename Cx<T>::type* __restrict__ tw, int RB, double dV, double mu,
                                                     int have_fmt_or_mf, int ideal, double* __restrict__ part,
-                                                    double* __restrict__ nrm) {
+                                                    double* __restrict__ nrm, RT* __restrict__ dF2 = nullptr) {
   typedef typename Cx<T>::type C;
   constexpr bool DS = DfSpectra<T, NF, DFS>::value;
   if constexpr (DS) {
@@ -783,7 +785,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     res = rows_fft<+1, T, NF, !DS, !DS>(b0, b1, RB, LP, pz, tw);
   }
   if constexpr (DS) {  // double-float spectra: the pointwise terms in df64 too
-    final_points_df(res, rho, vext, dF, d, RB, LP, nz, pair0, dV, mu, have_fmt_or_mf, ideal, part, nrm);
+    final_points_df(res, rho, vext, dF, d, RB, LP, nz, pair0, dV, mu, have_fmt_or_mf, ideal, part, nrm, dF2);
     return;
   }
   // Pointwise terms in the bulk precision T (FP64 in FP64 mode); each thread
@@ -811,6 +813,7 @@ __global__ void __launch_bounds__(256) k_final_rows(const typename Cx<T>::type* 
     f += ve * dVt;
     f += -mut * dVt;
     dF[p] = conv<RT>(f);
+    if (dF2) dF2[p] = conv<RT>(f);
     if (ideal) ks[0].add((r0 * lr - r0) * dVt);
     ks[1].add(r0);
     ks[2].add(ve * r0);

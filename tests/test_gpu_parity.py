@@ -219,6 +219,33 @@ def test_determinism_and_only_fex(cd, oracle):
     np.testing.assert_allclose(d1 - d3, np.log(rho) * c.info.dV, rtol=0, atol=1e-15)
 
 
+def test_pinned_host_dF_matches_copied_dF(cd, oracle):
+    """cdft_eval with a page-locked host dF (the final row pass writes it directly) gives the
+    same bits as the copy into pageable memory, for grand-canonical and fixed-mass systems
+    (the latter takes the copy path), in both precisions."""
+    import torch
+    shape = (128, 128, 128)
+    rho = oracle.fill_noise(shape, 0.4, 0.3, 5)
+    hsd = cd.bh_diameter(1.0, 1.0, 3.0, 0.8)
+    for kw in ({"mu": 0.3}, {"fixed_mass": float(rho.sum()) * 1e-3}):
+        for prec in (cd.FP64, cd.FP32):
+            c = cd.Context(shape, 0.1, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.8, precision=prec, **kw)
+            c.set_density(rho)
+            t0, d0 = c.eval()
+            pinned = torch.full(shape, float("nan"), dtype=torch.float64).pin_memory()
+            # at fixed mass every evaluation rescales rho to the mass again (a factor within
+            # rounding of 1), so there the bar is rounding, not bits
+            same = (lambda a, b: np.array_equal(a, b)) if "mu" in kw else \
+                (lambda a, b: np.allclose(a, b, rtol=1e-13, atol=1e-13 * np.abs(b).max()))
+            for _ in range(2):  # the second reuses the graph captured with this buffer
+                t1, _ = c.eval(dF_out=pinned)
+                assert same(pinned.numpy(), d0), (kw, prec)
+                assert same(np.array(t1["Omega"]), np.array(t0["Omega"]))
+            t2, d2 = c.eval()  # and the device dF stays the same for the next copy
+            assert same(d2, d0)
+            c.close()
+
+
 def test_external_field(cd, oracle):
     c = cd.Context(24, 0.2, cd.WHITEBEAR_I, hsd=1.0, mu=0.3)
     rho = oracle.fill_noise((24, 24, 24), 0.5, 0.1, 8)
