@@ -641,6 +641,9 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   // the other modes and RSLT take FP64 values per point (getv / setv convert).
   constexpr bool DF = kDf64Transforms && std::is_same<T, double>::value && NF > 0;
   constexpr bool DF_FUNC = DF && MODE == kPhiEval && MODEL != MODEL_RSLT;
+  // the Hessian's per-point step in df64 too: the set-up pass (kPhiStoreN) then stores the
+  // weighted densities NA as df64 pairs (8 bytes, like the doubles they replace)
+  constexpr bool DF_HESS = DF && (MODE == kPhiHess || MODE == kPhiStoreN) && MODEL != MODEL_RSLT;
   auto getv = [&](const C* buf, int i, int h) -> T {
     if constexpr (DF) {
       const dfc z = reinterpret_cast<const dfc*>(buf)[i];
@@ -678,7 +681,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   C* Z1 = reinterpret_cast<C*>(sm + NB * ib + zb);
   __shared__ __align__(8) uint64_t bar[NB];
   const long ngroup = (d.rows + RB - 1) / RB;
-  if constexpr (DF_FUNC) df_log_table_init(threadIdx.x, blockDim.x);  // read after the barrier below
+  if constexpr (DF_FUNC || (DF_HESS && MODE == kPhiHess)) df_log_table_init(threadIdx.x, blockDim.x);  // read after the barrier below
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int b = 0; b < NB; ++b) mbar_init(&bar[b], 1);
@@ -698,7 +701,7 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
   KahanT<T> psum;
   dfs psd = dfs(0);  // the df64 functional's sum (a thread's points), joined once
   struct DfParams { dfs x, y, z, w; } dfi;  // 1/hsd, 1/hsd^2, esA, esB in df64
-  if constexpr (DF_FUNC) dfi = {dfs_split((double)ih), dfs_split((double)ih2), dfs_split((double)esA), dfs_split((double)esB)};
+  if constexpr (DF_FUNC || DF_HESS) dfi = {dfs_split((double)ih), dfs_split((double)ih2), dfs_split((double)esA), dfs_split((double)esB)};
   unsigned st = 0;
   bool ok = true;
   for (long it = 0;; ++it) {
@@ -740,7 +743,14 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
         const int k = e % nz, r = e / nz;
         if (row0 + r >= d.rows) continue;
 #pragma unroll
-        for (int a = 0; a < M; ++a) NA[(long)a * d.N + (row0 + r) * nz + k] = getv(res, k * LPd + PK::line(r, a), PK::comp(r, a));
+        for (int a = 0; a < M; ++a) {
+          if constexpr (DF_HESS) {  // df64 pairs, read back by the Hessian's df64 step
+            const dfc z = reinterpret_cast<const dfc*>(res)[k * LPd + PK::line(r, a)];
+            reinterpret_cast<dfs*>(NA)[(long)a * d.N + (row0 + r) * nz + k] = PK::comp(r, a) ? z.y : z.x;
+          } else {
+            NA[(long)a * d.N + (row0 + r) * nz + k] = getv(res, k * LPd + PK::line(r, a), PK::comp(r, a));
+          }
+        }
       }
       __syncthreads();
       continue;
@@ -766,6 +776,31 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
         const dfs phi = fmt_phi_point<dfs, MODEL>(nw, dfi.x, dfi.y, dfi.z, dfi.w);
         if (!isfinite(phi.h)) st |= 2u;
         psd += phi;
+#pragma unroll
+        for (int p = 0; p < PK::per_row; ++p) {
+          dfc z;
+          z.x = nw[2 * p];
+          z.y = (2 * p + 1 < M) ? nw[2 * p + 1] : dfs(0);
+          od[k * LPd + r * PK::per_row + p] = z;
+        }
+        if constexpr (PK::cross) {
+          dfc* z = od + k * LPd + PK::line(r, M - 1);
+          (PK::comp(r, M - 1) ? z->y : z->x) = nw[M - 1];
+        }
+        continue;
+      }
+      if constexpr (DF_HESS && MODE == kPhiHess) {  // (d2Phi).Psi per point in df64, NA stored as df64 pairs
+        const dfc* rd = reinterpret_cast<const dfc*>(res);
+        dfc* od = reinterpret_cast<dfc*>(oth);
+        const dfs* nad = reinterpret_cast<const dfs*>(NA);
+        dfs nw[11], nd[11];
+#pragma unroll
+        for (int a = 0; a < M; ++a) {
+          const dfc z = rd[k * LPd + PK::line(r, a)];
+          nw[a] = PK::comp(r, a) ? z.y : z.x;
+          nd[a] = nad[(long)a * d.N + (row0 + r) * nz + k];
+        }
+        fmt_d2phi_dot_point<dfs, MODEL>(nd, nw, dfi.x, dfi.y, dfi.z, dfi.w, dfi.x, dfi.y);
 #pragma unroll
         for (int p = 0; p < PK::per_row; ++p) {
           dfc z;
