@@ -111,7 +111,10 @@ int cdft_set_boundary(cdft_ctx* ctx, int fixed_background, int homogeneous);
  * reference's get_f_* of include/DFT.h:121-124), mu after the call, the
  * convergence monitor max|dF|/dV (Species::get_convergence_monitor,
  * include/Species.h:55) and the number of atoms. dF (may be NULL) receives N
- * values. Under fixed mass the context's density is rescaled first, as
+ * values (on_device = 1: a device pointer); a page-locked host dF (cudaHostAlloc,
+ * cudaHostRegister) is written by the evaluation's last pass itself, with no copy
+ * after it (the first call with a new such buffer re-captures the evaluation).
+ * Under fixed mass the context's density is rescaled first, as
  * Species::beginForceCalculation does (src/Species.cpp:64-71).
  * Returns CDFT_ERR_ETA where the reference throws Eta_Too_Large_Exception. */
 int cdft_eval(cdft_ctx* ctx, int only_fex, double* terms, double* dF, int on_device);
