@@ -311,6 +311,30 @@ def test_ddft_matches_reference(cd, oracle, case, tag, nsteps, dt, dtmax):
     np.testing.assert_allclose(c.get_density().ravel(), g[tag + ".rho_final"], rtol=0, atol=1e-12)
 
 
+def test_ddft_128_fp64_vs_oracle(cd, oracle):
+    """Two DDFT steps at 128^3 in FP64: the evaluations run on double-float spectra and the
+    propagator's own transforms on the compile-time 128-point plans, against the oracle's
+    restatement of DDFT::step on the same density (time steps exactly, F and mass to 1e-12,
+    the densities to 1e-12 absolute)."""
+    shape = (128, 128, 128)
+    hsd = oracle.bh_diameter(3.0, 0.8)
+    rho = oracle.fill_noise(shape, 0.3, 0.1, 17)
+    dt, dtmax = 1e-4, 1e-3
+    o = oracle.Oracle(shape, 0.1, "WhiteBearI", hsd=hsd, lj=True, kT=0.8)
+    n, rec, rfin = o.ddft(rho, 2, dt, dtmax)
+    assert n == 2
+    c = cd.Context(shape, 0.1, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=0.8)
+    c.set_density(rho)
+    c.ddft_init(dt, dtmax)
+    for i in range(2):
+        r = c.ddft_step(1)
+        assert r["dt"] == rec["dt"][i]
+        assert abs(r["F"] - rec["F"][i]) <= 1e-12 * abs(rec["F"][i])
+        assert abs(r["mass"] - rec["mass"][i]) <= 1e-12 * abs(rec["mass"][i])
+    assert np.max(np.abs(c.get_density() - rfin)) <= 1e-12
+    c.close()
+
+
 def test_reference_shaped_api(cd, oracle):
     # The reference's own call sequence, on the GPU (config 1 evaluation).
     d = cd.Density(0.2, [6.4, 6.4, 6.4])
