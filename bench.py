@@ -477,7 +477,7 @@ def warm_start_leg(cd, n_train=120, n_test=8, steps=600, tol=1e-8, plain_fp64_s=
         res[name] = {"seconds": el, "newton": r["newton"], "cg_iters": r["cg_iters"], "fire_steps": r["total_steps"],
                      "resid": t["resid"], "Omega": t["Omega"]}
         c.close()
-    # warm start + mixed FIRE2 (FP32 bulk phase, then FP64 FIRE2), the policy the benchmark spec names
+    # warm start + mixed FIRE2 (FP32 bulk phase, then FP64 FIRE2): the warm-started mixed-precision FIRE2 policy
     c = cd.Context(SHAPE, DX, cd.WHITEBEAR_I, hsd=hsd, lj=True, kT=KT, fixed_mass=mass)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
