@@ -81,10 +81,13 @@ __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z
 
 // K multiple of 16 (<= 64), N multiple of 32 (<= 128), M any (rows past M are zero-filled, not written).
 // Dynamic shared memory: the X tile, W^T, and a 32 x 33 FP32 staging block per warp through which the
-// accumulator rows are turned into coalesced row-major stores.
+// accumulator rows are turned into coalesced row-major stores; with N = 32 also the tile's rows of
+// the residual input `add`, copied in with the X tile so that the epilogue does not wait on them.
+template <int N> struct StageAdd { static constexpr bool value = N == 32; };
 template <int N, int K>
 __host__ __device__ constexpr size_t smem_bytes() {
-  return (size_t)2 * kRows * K * 2 + (size_t)N * K * 2 + (size_t)4 * 32 * 33 * 4;  // two X tiles (double buffer)
+  return (size_t)2 * kRows * K * 2 + (size_t)N * K * 2 + (size_t)4 * 32 * 33 * 4  // two X tiles (double buffer)
+         + (StageAdd<N>::value ? (size_t)2 * kRows * N * 4 : 0);                   // two add tiles
 }
 
 // 16-byte asynchronous copy global -> shared; zero-fills when `valid` is false
@@ -101,9 +104,13 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restri
   static_assert(K % 16 == 0 && K <= 64 && N % 32 == 0 && N <= 128, "tile shape");
   constexpr int TCOLS = N <= 32 ? 32 : (N <= 64 ? 64 : 128);  // power of two >= 32
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  unsigned char* sxb[2] = {smem_raw, smem_raw + (size_t)kRows * K * 2};
+  // the two X tiles by address arithmetic (a pointer array indexed by the buffer would live in local memory)
+  auto sxb = [&](int b) { return smem_raw + (size_t)b * kRows * K * 2; };
   unsigned char* sw = smem_raw + (size_t)2 * kRows * K * 2;
   float* ep = reinterpret_cast<float*>(sw + (size_t)N * K * 2);
+  constexpr bool SA = StageAdd<N>::value;
+  float* sadd0 = ep + 4 * 32 * 33;  // add tiles (SA only): [kRows][N], two buffers
+  const bool stage_add = SA && add != nullptr && (reinterpret_cast<uintptr_t>(add) & 15u) == 0;  // 16-byte copies
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_base;
   __shared__ int stop;
@@ -130,28 +137,38 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restri
   const long ntile = (M + kRows - 1) / kRows;
   constexpr uint32_t idesc = instr_desc(N);
   unsigned phase = 0;
-  // X tile t into buffer b: 16-byte chunks (8 BF16 along K), asynchronous, rows past M zero-filled
-  auto load_tile = [&](long t, unsigned char* buf) {
+  // X tile t into buffer b: 16-byte chunks (8 BF16 along K), asynchronous, rows past M zero-filled;
+  // with stage_add the tile's add rows too (4 floats per chunk)
+  auto load_tile = [&](long t, int b) {
+    unsigned char* buf = sxb(b);
     const long r0 = t * kRows;
     for (int e = tid; e < kRows * (K / 8); e += blockDim.x) {
       const int r = e / (K / 8), k8 = (e - r * (K / 8)) * 8;
       const bool valid = r0 + r < M;
       cp_async16(buf + kmajor_off(r, k8, kRows), X + (valid ? (r0 + r) * K + k8 : 0), valid);
     }
+    if (stage_add) {
+      float* sa = sadd0 + (size_t)b * kRows * N;
+      for (int e = tid; e < kRows * (N / 4); e += blockDim.x) {
+        const int r = e / (N / 4), c4 = (e - r * (N / 4)) * 4;
+        const bool valid = r0 + r < M;
+        cp_async16(sa + r * N + c4, add + (valid ? (r0 + r) * N + c4 : 0), valid);
+      }
+    }
     cp_async_commit();
   };
-  if (blockIdx.x < ntile) load_tile(blockIdx.x, sxb[0]);
+  if (blockIdx.x < ntile) load_tile(blockIdx.x, 0);
   int b = 0;
   for (long t = blockIdx.x; t < ntile; t += gridDim.x, b ^= 1) {
     const long row0 = t * kRows;
-    unsigned char* sx = sxb[b];
+    unsigned char* sx = sxb(b);
     cp_async_wait_all();  // this tile's copies (the only group in flight)
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
     // the next tile streams into the other buffer while this one is multiplied and stored
-    if (t + gridDim.x < ntile) load_tile(t + gridDim.x, sxb[b ^ 1]);
+    if (t + gridDim.x < ntile) load_tile(t + gridDim.x, b ^ 1);
     if (tid == 0) {
       const uint32_t ax = smem_u32(sx), aw = smem_u32(sw);
 #pragma unroll
@@ -176,11 +193,13 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restri
       __syncwarp();
       const int col = c0 + lane;
       const float bc = bias ? bias[col] : 0.f;
+      const float* sa = sadd0 + (size_t)b * kRows * N;
       for (int r = 0; r < 32; ++r) {
         const long row = row0 + warp * 32 + r;
         if (row >= M) break;
         float z = my[r * 33 + lane] + bc;
-        if (add) z += add[row * N + col];
+        if (stage_add) z += sa[(warp * 32 + r) * N + col];
+        else if (add) z += add[row * N + col];
         if (Z) Z[row * N + col] = z;
         Y[row * N + col] = act ? gelu(z) : z;
       }
@@ -213,13 +232,14 @@ static int launch_gemm(const void* X, const void* W, const float* bias, const fl
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const long ntile = (M + kRows - 1) / kRows;
-  const unsigned grid = (unsigned)std::min<long>(ntile, (long)nsm * 4);
   constexpr size_t sm = smem_bytes<N, K>();
-  static bool attr = false;
-  if (!attr) {
+  static int per_sm = 0;  // resident CTAs per SM: the persistent grid is that many per SM
+  if (!per_sm) {
     cudaFuncSetAttribute(k_gemm_bf16<N, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    attr = true;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_bf16<N, K>, 128, sm);
+    per_sm = std::max(1, std::min(per_sm, 4));
   }
+  const unsigned grid = (unsigned)std::min<long>(ntile, (long)nsm * per_sm);
   k_gemm_bf16<N, K><<<grid, 128, sm, s>>>(reinterpret_cast<const __nv_bfloat16*>(X), reinterpret_cast<const __nv_bfloat16*>(W), bias, add,
                                           Y, Z, M, act, status);
   return cudaGetLastError() == cudaSuccess ? CDFT_OK : CDFT_ERR_CUDA;
