@@ -122,6 +122,54 @@ def test_eval_vs_oracle_fp64(cd, oracle, shape, dx, model, lj):
     np.testing.assert_allclose(dF, dFo, rtol=0, atol=dF_tol(dx))
 
 
+@pytest.mark.parametrize("model", MODELS)
+@pytest.mark.parametrize("lj", [False, True])
+def test_double_float_path_models_vs_oracle(cd, oracle, model, lj):
+    """At 128^3 FP64 takes the double-float-spectra path (compile-time plans on every axis;
+    RSLT with its per-point FP64 branch): every model, with and without the mean field, at the
+    reference bars, and its Hessian product against the oracle's to 1e-12 of its maximum."""
+    shape, dx = (128, 128, 128), 0.1
+    hsd = oracle.bh_diameter(3.0, 0.9) if lj else 1.0
+    o = oracle.Oracle(shape, dx, model, hsd=hsd, lj=lj, kT=0.9)
+    c = cd.Context(shape, dx, model_id(cd, model), hsd=hsd, lj=lj, kT=0.9)
+    rho = oracle.fill_noise(shape, 0.4, 0.3, 4321)
+    mu = c.bulk(0.4)["mu"]
+    o.set_mu(mu)
+    c.set_chem_potential(mu)
+    c.set_density(rho)
+    terms, dF = c.eval()
+    st, t, dFo, _ = o.eval(rho)
+    for k in ("Omega", "F_id", "F_hs", "F_mf", "F_ext"):
+        assert abs(terms[k] - t[k]) <= 1e-12 * max(1.0, abs(t[k])), (k, terms[k], t[k])
+    np.testing.assert_allclose(dF, dFo, rtol=0, atol=dF_tol(dx))
+    if lj:
+        v = (oracle.fill_noise(shape, 1.0, 1.0, 99) - 1.0) * rho  # signed, of the size of rho
+        hv = c.hessian_dot_v(v)
+        ref = o.hessian_dot_v(rho, v)
+        assert np.max(np.abs(hv - ref)) <= 1e-12 * np.max(np.abs(ref))
+    c.close()
+
+
+def test_double_float_path_only_fex_and_external_field(cd, oracle):
+    """The double-float final pass (ln rho, dF and the sums in df64) without the ideal gas and
+    with an external field, at 128^3 FP64: the differences are ln(rho) dV and V dV."""
+    shape = (128, 128, 128)
+    c = cd.Context(shape, 0.1, cd.WHITEBEAR_I, hsd=cd.bh_diameter(1.0, 1.0, 3.0, 0.9), lj=True, kT=0.9, mu=0.2)
+    rho = oracle.fill_noise(shape, 0.4, 0.3, 7)
+    c.set_density(rho)
+    dV = c.info.dV
+    t0, d0 = c.eval()
+    t3, d3 = c.eval(only_fex=True)
+    assert t3["F_id"] == 0.0
+    np.testing.assert_allclose(d0 - d3, np.log(rho) * dV, rtol=0, atol=1e-15)
+    V = np.sin(np.arange(np.prod(shape)).reshape(shape) * 1e-3)
+    c.set_external_field(V)
+    t1, d1 = c.eval()
+    np.testing.assert_allclose(d1 - d0, V * dV, rtol=0, atol=1e-15)
+    assert abs((t1["F_ext"] - t0["F_ext"]) - np.sum(V * rho) * dV) <= 1e-10 * max(1.0, abs(t1["F_ext"]))
+    c.close()
+
+
 def droplet(shape, dx, rho_v=0.01, rho_l=0.75, R=4.0, w=0.5):
     n = np.array(shape)
     ax = [dx * (np.arange(m) - m / 2.0) for m in shape]
