@@ -59,6 +59,69 @@ __device__ __forceinline__ dfc ld_twiddle(const float4* p) {
   return r;
 }
 
+// The P-point DFTs of a df64 butterfly, with the sums that skip renormalisation
+// (dfl_add, dfl_mul, dfl_dot2 in cdft_df64.cuh): inputs normalised pairs, outputs not.
+__device__ __forceinline__ dfc dfcl_add(dfc a, dfc b) {
+  dfc r;
+  r.x = dfl_add(a.x, b.x);
+  r.y = dfl_add(a.y, b.y);
+  return r;
+}
+__device__ __forceinline__ dfc dfcl_sub(dfc a, dfc b) {
+  dfc r;
+  r.x = dfl_add(a.x, -b.x);
+  r.y = dfl_add(a.y, -b.y);
+  return r;
+}
+// a w (DIR < 0, forward) or a conj(w) (DIR > 0, backward)
+template <int DIR>
+__device__ __forceinline__ dfc dfcl_mul_dir(dfc a, dfc w) {
+  dfc r;
+  if constexpr (DIR < 0) {
+    r.x = dfl_dot2(a.x, w.x, -a.y, w.y);
+    r.y = dfl_dot2(a.x, w.y, a.y, w.x);
+  } else {
+    r.x = dfl_dot2(a.x, w.x, a.y, w.y);
+    r.y = dfl_dot2(a.y, w.x, -a.x, w.y);
+  }
+  return r;
+}
+template <int DIR>
+__device__ __forceinline__ void dft4_dfl(dfc* a) {
+  const dfc t0 = dfcl_add(a[0], a[2]), t1 = dfcl_sub(a[0], a[2]), t2 = dfcl_add(a[1], a[3]),
+            t3 = cmul_mi<DIR>(dfcl_sub(a[1], a[3]));
+  a[0] = dfcl_add(t0, t2);
+  a[2] = dfcl_sub(t0, t2);
+  a[1] = dfcl_add(t1, t3);
+  a[3] = dfcl_sub(t1, t3);
+}
+template <int DIR>
+__device__ __forceinline__ void dft8_dfl(dfc* a) {
+  constexpr dfs r(0.70710678118654752440084436210484903928);
+  dfc e[4] = {a[0], a[2], a[4], a[6]}, o[4] = {a[1], a[3], a[5], a[7]};
+  dft4_dfl<DIR>(e);
+  dft4_dfl<DIR>(o);
+  // w8^k for k = 1, 2, 3 on the odd half
+  const dfc o1 = o[1], o3 = o[3];
+  if constexpr (DIR < 0) {
+    o[1].x = dfl_mul(r, dfl_add(o1.x, o1.y));
+    o[1].y = dfl_mul(r, dfl_add(o1.y, -o1.x));
+    o[3].x = dfl_mul(r, dfl_add(o3.y, -o3.x));
+    o[3].y = -dfl_mul(r, dfl_add(o3.x, o3.y));
+  } else {
+    o[1].x = dfl_mul(r, dfl_add(o1.x, -o1.y));
+    o[1].y = dfl_mul(r, dfl_add(o1.x, o1.y));
+    o[3].x = -dfl_mul(r, dfl_add(o3.x, o3.y));
+    o[3].y = dfl_mul(r, dfl_add(o3.x, -o3.y));
+  }
+  o[2] = cmul_mi<DIR>(o[2]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    a[k] = dfcl_add(e[k], o[k]);
+    a[k + 4] = dfcl_sub(e[k], o[k]);
+  }
+}
+
 template <int DIR, int P, int TC, bool UNIT, bool IN_D, bool OUT_D>
 __device__ __forceinline__ void tile_butterfly_df(const void* __restrict__ xv, void* __restrict__ yv, int c, int q, int k, int m, int s,
                                                   const float4* __restrict__ tw) {
@@ -69,16 +132,25 @@ __device__ __forceinline__ void tile_butterfly_df(const void* __restrict__ xv, v
     if constexpr (IN_D) a[j] = dfc_split(reinterpret_cast<const double2*>(xv)[idx]);
     else a[j] = reinterpret_cast<const dfc*>(xv)[idx];
   }
-  if constexpr (P == 8) dft8<DIR, dfs>(a);
-  else if constexpr (P == 4) dft4<DIR>(a);
-  else dft2<DIR>(a);
+  if constexpr (P == 8) dft8_dfl<DIR>(a);
+  else if constexpr (P == 4) dft4_dfl<DIR>(a);
+  else {
+    const dfc t = a[0];
+    a[0] = dfcl_add(t, a[1]);
+    a[1] = dfcl_sub(t, a[1]);
+  }
   const float4* twq = tw + q * P;
 #pragma unroll
   for (int t = 0; t < P; ++t) {
-    const dfc v = (UNIT || t == 0) ? a[t] : cmul_dir<DIR>(a[t], ld_twiddle(twq + t));
+    dfc v = (UNIT || t == 0) ? a[t] : dfcl_mul_dir<DIR>(a[t], ld_twiddle(twq + t));
     const int idx = (k + s * (P * q + t)) * TC + c;
-    if constexpr (OUT_D) reinterpret_cast<double2*>(yv)[idx] = dfc_join(v);
-    else reinterpret_cast<dfc*>(yv)[idx] = v;
+    if constexpr (OUT_D) {
+      reinterpret_cast<double2*>(yv)[idx] = dfc_join(v);  // hi + lo rounded once, normalised or not
+    } else {
+      v.x = df_renorm(v.x);
+      v.y = df_renorm(v.y);
+      reinterpret_cast<dfc*>(yv)[idx] = v;
+    }
   }
 }
 
