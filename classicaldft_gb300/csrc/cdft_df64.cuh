@@ -191,6 +191,29 @@ __device__ __forceinline__ dfs df_log(dfs x) {
   return dfs((float)k, 0.f) * df_ln2() + df_log1p(u);
 }
 
+// df64 with the butterflies' sums and products (dfl_add, dfl_mul) as its operators, for the
+// per-point functional of the Phi pass: its outputs feed the forward transforms and its value
+// the Phi sum, both with normwise bounds. The logarithm, reciprocals and comparisons
+// renormalise their arguments first (norm()).
+struct dfl {
+  float h, l;
+  __device__ dfl() {}
+  __device__ constexpr dfl(int z) : h((float)z), l(0.f) {}  // small integer constants, exact
+  __device__ constexpr explicit dfl(double d) : h((float)d), l((float)(d - (double)(float)d)) {}
+  __device__ explicit dfl(dfs a) : h(a.h), l(a.l) {}
+  __device__ dfs norm() const { return df_fast_two_sum(h, l); }
+  __device__ dfs raw() const { return dfs(h, l); }
+};
+__device__ __forceinline__ dfl mk_dfl(dfs a) { return dfl(a); }
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) { return mk_dfl(dfl_add(a.raw(), b.raw())); }
+__device__ __forceinline__ dfl operator-(dfl a) { return mk_dfl(dfs(-a.h, -a.l)); }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) { return mk_dfl(dfl_mul(a.raw(), b.raw())); }
+__device__ __forceinline__ dfl operator/(dfl a, dfl b) { return a * mk_dfl(df_rcp(b.norm())); }
+__device__ __forceinline__ dfl& operator+=(dfl& a, dfl b) { return a = a + b; }
+__device__ __forceinline__ dfl& operator-=(dfl& a, dfl b) { return a = a - b; }
+__device__ __forceinline__ bool operator<(dfl a, dfl b) { return a.norm() < b.norm(); }
+
 __device__ __forceinline__ dfc dfc_split(double2 z) {
   dfc r;
   r.x = dfs_split(z.x);

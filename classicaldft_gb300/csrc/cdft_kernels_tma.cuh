@@ -498,7 +498,8 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
       if (e < nel) {
         const RC z = reinterpret_cast<const RC*>(res)[e];
         const typename XR::W wv = XR::template load_weight<DFS>(Wst(b), e);
-        S[j] = cadd(S[j], mul_weight(z, wv, odd));
+        if constexpr (XR::df) S[j] = dfcl_add(S[j], mul_weight(z, wv, odd));  // summed unnormalised, read by the transform
+        else S[j] = cadd(S[j], mul_weight(z, wv, odd));
         if (is_mf) {
           const int col = col0 + (e % TC);
           const int kz = col % d.pz;
@@ -773,9 +774,16 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
           nw[a] = PK::comp(r, a) ? z.y : z.x;
         }
         if ((dfs(1) - nw[0]).h < 0.f) st |= 1u;  // eta > 1 (nw[0] is eta until the functional overwrites it)
-        const dfs phi = fmt_phi_point<dfs, MODEL>(nw, dfi.x, dfi.y, dfi.z, dfi.w);
+        // the functional in the lazy df64 arithmetic (dfl): its derivatives go straight into
+        // the forward transform's first stage, which takes unnormalised pairs
+        dfl nl[11];
+#pragma unroll
+        for (int a = 0; a < M; ++a) nl[a] = dfl(nw[a]);
+        const dfs phi = fmt_phi_point<dfl, MODEL>(nl, dfl(dfi.x), dfl(dfi.y), dfl(dfi.z), dfl(dfi.w)).norm();
         if (!isfinite(phi.h)) st |= 2u;
         psd += phi;
+#pragma unroll
+        for (int a = 0; a < M; ++a) nw[a] = nl[a].raw();
 #pragma unroll
         for (int p = 0; p < PK::per_row; ++p) {
           dfc z;

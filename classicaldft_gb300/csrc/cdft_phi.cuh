@@ -20,6 +20,7 @@ template <> __device__ __forceinline__ double log1m<double>(double e) { return l
 template <> __device__ __forceinline__ float log1m<float>(float e) { return log1pf(-e); }
 // df64: table-driven log1p on the FP32 pipe (the kernel initialises df_log_table first)
 template <> __device__ __forceinline__ dfs log1m<dfs>(dfs e) { return df_log1p(-e); }
+template <> __device__ __forceinline__ dfl log1m<dfl>(dfl e) { return dfl(df_log1p(-e.norm())); }
 // natural logarithm in the argument's own precision (logf for FP32, never a promotion to FP64)
 template <class T> __device__ __forceinline__ T ln_t(T x);
 template <> __device__ __forceinline__ double ln_t<double>(double x) { return log(x); }
