@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
       if (e < nel) {
         const RC z = reinterpret_cast<const RC*>(res)[e];
         const typename XR::W wv = XR::template load_weight<DFS>(Wst(b), e);
-        if constexpr (XR::df) S[j] = dfcl_add(S[j], mul_weight(z, wv, odd));  // summed unnormalised, read by the transform
+        if constexpr (XR::df) S[j] = dfcl_add(S[j], mul_weight(z, wv, odd));  // summed unnormalised, renormalised once below
         else S[j] = cadd(S[j], mul_weight(z, wv, odd));
         if (is_mf) {
           const int col = col0 + (e % TC);
@@ -530,7 +530,13 @@ __global__ void __launch_bounds__(256, 2) k_xbackconv_tma(const __grid_constant_
 #pragma unroll
   for (int j = 0; j < PER; ++j) {
     const int e = threadIdx.x + j * 256;
-    if (e < nel) reinterpret_cast<RC*>(X)[e] = S[j];
+    if (e < nel) {
+      if constexpr (XR::df) {  // renormalised once: a transform's first stage keeps its error small on normalised pairs
+        S[j].x = df_renorm(S[j].x);
+        S[j].y = df_renorm(S[j].y);
+      }
+      reinterpret_cast<RC*>(X)[e] = S[j];
+    }
   }
   C* r2 = xfft<+1, T, TC, NF, false, !DFS>(X, Y, px, tw);
   fence_async_smem();
@@ -808,7 +814,18 @@ __global__ void __launch_bounds__(PhiThreads<T>::value, (MODE == kPhiHess || MOD
           nw[a] = PK::comp(r, a) ? z.y : z.x;
           nd[a] = nad[(long)a * d.N + (row0 + r) * nz + k];
         }
-        fmt_d2phi_dot_point<dfs, MODEL>(nd, nw, dfi.x, dfi.y, dfi.z, dfi.w, dfi.x, dfi.y);
+        {  // in the lazy df64 arithmetic, as the functional above
+          dfl ndl[11], nwl[11];
+#pragma unroll
+          for (int a = 0; a < M; ++a) {
+            ndl[a] = dfl(nd[a]);
+            nwl[a] = dfl(nw[a]);
+          }
+          const dfl ih(dfi.x), ih2(dfi.y);
+          fmt_d2phi_dot_point<dfl, MODEL>(ndl, nwl, ih, ih2, dfl(dfi.z), dfl(dfi.w), ih, ih2);
+#pragma unroll
+          for (int a = 0; a < M; ++a) nw[a] = nwl[a].raw();
+        }
 #pragma unroll
         for (int p = 0; p < PK::per_row; ++p) {
           dfc z;
