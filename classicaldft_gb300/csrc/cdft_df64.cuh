@@ -20,6 +20,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "cdft_convert.cuh"
+#include "cdft_df_log_table.h"
 #include "cdft_types.h"
 
 namespace cdft {
@@ -132,20 +133,18 @@ __device__ __forceinline__ dfs operator/(dfs a, dfs b) { return a * df_rcp(b); }
 // + r^4 q(r) takes its first three terms in df64 and q (a cubic) in FP32. Near x = 0 the
 // reduction is skipped (k = 0, F = 1), so the result keeps its relative accuracy there.
 // Relative error ~1e-14 (against ~1e-16 in FP64), far inside the evaluation's 1e-12.
-// The table (log F and 1/F as df64) lives in shared memory: a kernel calls
-// df_log_table_init once and synchronises before the first logarithm.
+// The table (log F and 1/F as df64, from 50-digit decimal arithmetic: cdft_df_log_table.h)
+// is read from shared memory: a kernel calls df_log_table_init once, which copies it there
+// from global memory, and synchronises before the first logarithm.
 constexpr int kDfLogLo = -32, kDfLogN = 97;
+static __device__ const float4 kDfLogTable[kDfLogN] = {CDFT_DF_LOG_TABLE};
 __device__ __forceinline__ float4* df_log_table() {
   __shared__ float4 t[kDfLogN];
   return t;
 }
 __device__ __forceinline__ void df_log_table_init(int tid, int nthreads) {
   float4* t = df_log_table();
-  for (int i = tid; i < kDfLogN; i += nthreads) {
-    const int j = i + kDfLogLo;
-    const dfs l = dfs_split(log1p((double)j / 128.0)), v = dfs_split(1.0 / (1.0 + (double)j / 128.0));
-    t[i] = make_float4(l.h, l.l, v.h, v.l);
-  }
+  for (int i = tid; i < kDfLogN; i += nthreads) t[i] = __ldg(&kDfLogTable[i]);
 }
 __device__ __forceinline__ dfs df_ln2() { return dfs(0.6931471805599453094); }
 __device__ __forceinline__ dfs df_third() { return dfs(0.3333333333333333333); }

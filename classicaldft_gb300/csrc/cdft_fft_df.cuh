@@ -156,29 +156,42 @@ __device__ __forceinline__ void tile_butterfly_df(const void* __restrict__ xv, v
 
 // (no unrolling of the item loop: a df64 butterfly is ~12x the instructions of an FP64
 // one, and unrolled copies of every stage overflowed the instruction cache)
+// ncols < TC: a partial tile (the last column tile of a half spectrum), whose first ncols
+// columns alone are transformed, their butterflies packed onto the first threads so that
+// the other warps skip the stage; the last stage writes zeros into the other columns.
 template <int DIR, int TC, int PITCH, int NF, int ST, int NTH, bool IN_D, bool OUT_D>
-__device__ __forceinline__ void fx_stage_df(const void* __restrict__ src, void* __restrict__ dst, const float4* __restrict__ tws) {
+__device__ __forceinline__ void fx_stage_df(const void* __restrict__ src, void* __restrict__ dst, const float4* __restrict__ tws,
+                                            int ncols) {
   constexpr int p = fxd_radix(NF, ST), len = fxd_len(NF, ST), m = len / p, s = NF / len;
-  constexpr int items = TC * (NF / p);
-  constexpr bool first = IN_D && ST == 0, last = OUT_D && fxd_radix(NF, ST + 1) == 0;
+  constexpr bool first = IN_D && ST == 0, final_stage = fxd_radix(NF, ST + 1) == 0, last = OUT_D && final_stage;
   static_assert(p == 2 || p == 4 || p == 8, "df64 stages take radices 2, 4 and 8");
   const float4* tw = tws + fxd_twoff(NF, ST);
+  const bool full = ncols >= TC;
+  const int items = (full ? TC : ncols) * (NF / p);
 #pragma unroll 1
   for (int w = threadIdx.x; w < items; w += NTH) {
-    const int c = w % TC, u = w / TC;
+    const int c = full ? w % TC : w % ncols, u = full ? w / TC : w / ncols;
     const int q = u / s, k = u % s;
     tile_butterfly_df<DIR, p, PITCH, m == 1, first, last>(src, dst, c, q, k, m, s, tw);
+  }
+  if (final_stage && !full) {
+    const int dead = TC - ncols;
+    for (int w = threadIdx.x; w < dead * NF; w += NTH) {
+      const int idx = (w / dead) * PITCH + ncols + w % dead;
+      if constexpr (OUT_D) reinterpret_cast<double2*>(dst)[idx] = make_double2(0.0, 0.0);
+      else reinterpret_cast<dfc*>(dst)[idx] = dfc{dfs(0), dfs(0)};
+    }
   }
 }
 
 template <int DIR, int TC, int PITCH, int NF, int NTH, bool IN_D, bool OUT_D, int ST = 0>
-__device__ __forceinline__ double2* tile_fft_fixed_df_stages(double2* b0, double2* b1, const float4* __restrict__ tws) {
+__device__ __forceinline__ double2* tile_fft_fixed_df_stages(double2* b0, double2* b1, const float4* __restrict__ tws, int ncols) {
   __syncthreads();
   if constexpr (fxd_radix(NF, ST) == 0) {
     return b0;
   } else {
-    fx_stage_df<DIR, TC, PITCH, NF, ST, NTH, IN_D, OUT_D>(b0, b1, tws);
-    return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D, ST + 1>(b1, b0, tws);
+    fx_stage_df<DIR, TC, PITCH, NF, ST, NTH, IN_D, OUT_D>(b0, b1, tws, ncols);
+    return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D, ST + 1>(b1, b0, tws, ncols);
   }
 }
 // Each call stages the plan's df64 twiddles (fxd_table_len(NF) entries, 2.7 KB for 128
@@ -187,11 +200,11 @@ __device__ __forceinline__ double2* tile_fft_fixed_df_stages(double2* b0, double
 // so the copy cannot overwrite twiddles still in use. IN_D / OUT_D: the tile holds
 // doubles on entry / exit (else df64 values, for a caller that keeps them).
 template <int DIR, int TC, int PITCH, int NF, int NTH, bool IN_D = true, bool OUT_D = true>
-__device__ __forceinline__ double2* tile_fft_fixed_df(double2* b0, double2* b1, const dfc* __restrict__ twdf) {
+__device__ __forceinline__ double2* tile_fft_fixed_df(double2* b0, double2* b1, const dfc* __restrict__ twdf, int ncols = TC) {
   constexpr int NT = fxd_table_len(NF);
   __shared__ float4 tws[NT];
   for (int i = threadIdx.x; i < NT; i += NTH) tws[i] = __ldg(reinterpret_cast<const float4*>(twdf) + i);
-  return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D>(b0, b1, tws);
+  return tile_fft_fixed_df_stages<DIR, TC, PITCH, NF, NTH, IN_D, OUT_D>(b0, b1, tws, ncols);
 }
 
 

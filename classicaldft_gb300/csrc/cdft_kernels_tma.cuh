@@ -240,11 +240,12 @@ template <> struct ElemsPerComplex<double> { static constexpr int value = 2; };
 // leave (OUT_D = false) or take (IN_D = false) df64 values, so that the products with
 // the weights happen in df64 too and no join / split pair surrounds them; XReg is the
 // type a thread holds such values in.
+// ncols (df64 only): the tile's live columns, as for tile_fft_fixed_df.
 template <int DIR, class T, int TC, int NF, bool IN_D, bool OUT_D>
 __device__ __forceinline__ typename Cx<T>::type* xfft(typename Cx<T>::type* b0, typename Cx<T>::type* b1, const FFTPlan& P,
-                                                      const typename Cx<T>::type* __restrict__ tw) {
+                                                      const typename Cx<T>::type* __restrict__ tw, int ncols = TC) {
   if constexpr (kDf64Transforms && std::is_same<T, double>::value && NF > 0)
-    return tile_fft_fixed_df<DIR, TC, TC, NF, 256, IN_D, OUT_D>(b0, b1, reinterpret_cast<const dfc*>(tw + fx_table_len(NF)));
+    return tile_fft_fixed_df<DIR, TC, TC, NF, 256, IN_D, OUT_D>(b0, b1, reinterpret_cast<const dfc*>(tw + fx_table_len(NF)), ncols);
   else
     return tfft<DIR, T, TC, TC, NF>(b0, b1, P, tw);
 }
@@ -332,12 +333,13 @@ __global__ void __launch_bounds__(256) k_cols_y_tma(const __grid_constant__ CUte
     // buffer) before this tile's transform writes work
     if (threadIdx.x == 0) bulk_wait_read();
     if (!__syncthreads_and(ok)) break;
-    C* res = xfft<DIR, T, TC, NF, !DFS, !DFS>(stage(b), work, P, tw);
+    int kz0, x, f;
+    coords(item, kz0, x, f);
+    // the last column tile holds nzc - kz0 live columns (one of 16 at 128 points)
+    C* res = xfft<DIR, T, TC, NF, !DFS, !DFS>(stage(b), work, P, tw, min(TC, d.nzc - kz0));
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
-      int kz0, x, f;
-      coords(item, kz0, x, f);
       tma_store_4d(&map, kz0 * E, 0, x, f, res);
       bulk_commit();
       const long next = item + 2L * gridDim.x;
