@@ -476,14 +476,19 @@ bool Evaluator<T>::setup_tma(std::string* err) {
     raise_smem(k_xbackconv_tma<T, 128, true>, smem_tback_);
     raise_smem(k_xbackconv_tma<T, 256, true>, smem_tback_);
   }
-  int nsm = 0, dev = 0, bps = 0;
+  int nsm = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cols_y_tma<T, -1, 0>, 256, smem_ty_);
-  bps = std::max(bps, 1);
   const long ntile = (nzc_ + TCY - 1) / TCY;
-  grid_ty1_ = (int)std::min<long>((long)nx_ * ntile, (long)nsm * bps);
-  grid_tyM_ = (int)std::min<long>((long)std::max(M_, 1) * nx_ * ntile, (long)nsm * bps);
+  for (int io = 0; io < 2; ++io) {  // persistent grids from the residency of the instance launched (io: df64 spectra)
+    int bps = 0;
+    with_nf_io<T>(fy_, io != 0, [&](auto nf_, auto io_) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_cols_y_tma<T, -1, decltype(nf_)::value, decltype(io_)::value>, 256, smem_ty_);
+    });
+    bps = std::max(bps, 1);
+    grid_ty1_[io] = (int)std::min<long>((long)nx_ * ntile, (long)nsm * bps);
+    grid_tyM_[io] = (int)std::min<long>((long)std::max(M_, 1) * nx_ * ntile, (long)nsm * bps);
+  }
   tma_ = true;
   setup_phi_tma();
   return true;
@@ -836,7 +841,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
                                                                                                                         twp<T>(tz_), rb_rows_);
     });
     mark(1);
-    yfwd(A_, mapYA_, 1, grid_ty1_);
+    yfwd(A_, mapYA_, 1, grid_ty1_[io]);
     mark(2);
   } else {
     mark(1);
@@ -846,7 +851,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
     if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, decltype(io_)::value ? mapWdf_ : mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
     mark(3);
-    yinv(Cf_, mapYC_, M_, grid_tyM_);
+    yinv(Cf_, mapYC_, M_, grid_tyM_[io]);
     mark(4);
     PhiArgs pa;
     pa.map = &mapR_;
@@ -876,7 +881,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
       with_model(model_, [&](auto m) { PhiLauncher<T, decltype(m)::value>::launch_rows(false, pa, rb_phi_, (unsigned)nphi, smem_phi_, s); });
     }
     mark(5);
-    yfwd(Cf_, mapYC_, M_, grid_tyM_);
+    yfwd(Cf_, mapYC_, M_, grid_tyM_[io]);
     mark(6);
   } else {
     for (int i = 3; i <= 6; ++i) mark(i);
@@ -892,7 +897,7 @@ int Evaluator<T>::launch(const RT* rho, const double* vext, RT* dF, double dV, d
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
                                                    mf_ ? part_mf : nullptr);
     mark(7);
-    yinv(E_, mapYE_, 1, grid_ty1_);
+    yinv(E_, mapYE_, 1, grid_ty1_[io]);
     mark(8);
   } else {
     mark(7);
@@ -930,11 +935,11 @@ int Evaluator<T>::hess_prepare(const double* rho0, cudaStream_t s) {
     k_rows_r2c<T, double, decltype(nf_)::value, decltype(io_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(
         rho0, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
   });
-  if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, -1, decltype(nf_)::value, decltype(io_)::value><<<grid_ty1_, 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_); });
+  if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, -1, decltype(nf_)::value, decltype(io_)::value><<<grid_ty1_[io], 256, smem_ty_, s>>>(mapYA_, d, ty_->plan, twp<T>(ty_), 1, status_); });
   else k_cols_fft<T, -1><<<dim3(gcy, 1), 256, smem_coly_, s>>>(A_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, decltype(io_)::value ? mapWdf_ : mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
   else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
-  if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, +1, decltype(nf_)::value, decltype(io_)::value><<<grid_tyM_, 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_); });
+  if (tma_) with_nf_io<T>(fy_, io, [&](auto nf_, auto io_) { k_cols_y_tma<T, +1, decltype(nf_)::value, decltype(io_)::value><<<grid_tyM_[io], 256, smem_ty_, s>>>(mapYC_, d, ty_->plan, twp<T>(ty_), M_, status_); });
   else k_cols_fft<T, +1><<<dim3(gcy, M_), 256, smem_coly_, s>>>(Cf_, Nc_, 1, d, ty_->plan, twp<T>(ty_), tc_);
   PhiArgs pa;
   pa.map = &mapR_;
@@ -980,12 +985,12 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
     with_nf_io<T>(fz_, io, [&](auto nf_, auto io_) {
       k_rows_r2c<T, RT, decltype(nf_)::value, decltype(io_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(v, A_, d, tz_->plan, twp<T>(tz_), rb_rows_);
     });
-    yfwd(A_, mapYA_, 1, grid_ty1_);
+    yfwd(A_, mapYA_, 1, grid_ty1_[io]);
   }
   if (M_ > 0) {
     if (tma_) with_nf_io<T>(fx_, io, [&](auto nf_, auto io_) { k_xconv_tma<T, decltype(nf_)::value, decltype(io_)::value><<<gtx, 256, smem_tconv_, s>>>(mapA_, decltype(io_)::value ? mapWdf_ : mapW_, mapCf_, M_, tx_->plan, twp<T>(tx_), status_); });
     else k_xconv<T><<<gcx, 256, smem_xconv_, s>>>(A_, Cf_, w_, M_, d, tx_->plan, twp<T>(tx_), tc_);
-    yinv(Cf_, mapYC_, M_, grid_tyM_);
+    yinv(Cf_, mapYC_, M_, grid_tyM_[io]);
     const unsigned g = (unsigned)((rows_ + rb_phi_ - 1) / rb_phi_);
     PhiArgs pa;
     pa.map = &mapR_;
@@ -1002,7 +1007,7 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
       if (tma_phi_) PhiLauncher<T, decltype(m)::value>::launch_tma(phi_nf(), kPhiHess, pa, grid_thess_, smem_tphi_, s);
       else PhiLauncher<T, decltype(m)::value>::launch_rows(true, pa, rb_phi_, g, smem_phi_, s);
     });
-    yfwd(Cf_, mapYC_, M_, grid_tyM_);
+    yfwd(Cf_, mapYC_, M_, grid_tyM_[io]);
   }
   double* part_mf = part_ + 2 * rows_;
   if (any) {
@@ -1015,7 +1020,7 @@ int Evaluator<T>::hess_apply(const RT* v, const double* rho0, RT* out, double dV
     else
       k_xbackconv<T><<<gcx, 256, smem_xback_, s>>>(Cf_, A_, E_, w_, mf_ ? watt_ : nullptr, M_, d, tx_->plan, twp<T>(tx_), tc_,
                                                    mf_ ? part_mf : nullptr);
-    yinv(E_, mapYE_, 1, grid_ty1_);
+    yinv(E_, mapYE_, 1, grid_ty1_[io]);
   }
   with_nf_io<T>(fz_, io, [&](auto nf_, auto io_) {
     k_hess_final_rows<T, RT, decltype(nf_)::value, decltype(io_)::value><<<(unsigned)grid_blocks_rows(), 256, smem_rows_, s>>>(

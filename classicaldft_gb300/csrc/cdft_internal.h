@@ -161,7 +161,7 @@ class Evaluator {
   void* wattdf_ = nullptr;
   CUtensorMap mapWdf_, mapWattdf_;
   size_t smem_ty_ = 0, smem_tconv_ = 0, smem_tback_ = 0;
-  int grid_ty1_ = 0, grid_tyM_ = 0;
+  int grid_ty1_[2] = {0, 0}, grid_tyM_[2] = {0, 0};  // y-pass persistent grids, by df64 spectra or not
   bool tma_phi_ = false;
   // the tensor-copy kernels' compile-time plans (length 128, default radix order) apply to x / y / z
   int fx_ = 0, fy_ = 0, fz_ = 0;  // compile-time plan length per axis (128, 256) or 0

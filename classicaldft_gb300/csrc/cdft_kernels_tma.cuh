@@ -221,7 +221,8 @@ template <class T> struct TileCols;
 template <> struct TileCols<float> { static constexpr int value = 16; };
 template <> struct TileCols<double> { static constexpr int value = 8; };
 // the y pass's tiles: 16 columns in both precisions (256-byte FP64 rows), so that every
-// stage of a df64 transform has a butterfly for each of the 256 threads
+// stage of a df64 transform has a butterfly for each of the 256 threads (12-column FP64
+// tiles, three blocks per SM instead of two, measured 9% slower)
 template <class T> struct TileColsY { static constexpr int value = 16; };
 // rows per group of the fused Phi kernel
 template <class T> struct PhiRows;
