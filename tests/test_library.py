@@ -83,3 +83,24 @@ def test_create_rejects_bad_systems_before_touching_the_gpu():
         h = ctypes.c_void_p()
         assert L.cdft_create(ctypes.byref(p), ctypes.byref(h)) == 4
         assert not h.value
+
+
+def test_double_float_log_table_is_the_generated_one():
+    """cdft_df_log_table.h (the df64 logarithm's table of log F and 1/F, F = 1 + j/128) is
+    what its generator writes, and every entry's float pair carries its value to 2^-48."""
+    import subprocess
+    import sys
+    from decimal import Decimal, getcontext
+    csrc = os.path.join(ROOT, "classicaldft_gb300", "csrc")
+    out = subprocess.run([sys.executable, os.path.join(csrc, "gen_df_log_table.py")], capture_output=True, text=True, check=True).stdout
+    with open(os.path.join(csrc, "cdft_df_log_table.h")) as f:
+        assert f.read() == out
+    rows = re.findall(r"^\s*\{([^}]*)\}", out, re.M)
+    assert len(rows) == 97
+    getcontext().prec = 50
+    for i, r in enumerate(rows):
+        v = [np.float32(x.strip().rstrip("f")) for x in r.split(",")]
+        F = 1 + Decimal(i - 32) / 128
+        for (h, l), exact in (((v[0], v[1]), F.ln()), ((v[2], v[3]), 1 / F)):
+            assert abs(Decimal(float(h)) + Decimal(float(l)) - exact) <= abs(exact) * Decimal(2) ** -48
+            assert abs(float(l)) <= abs(float(h)) * 2.0 ** -23 or h == 0
