@@ -150,7 +150,9 @@ class Evaluator {
   T* psir_ = nullptr;
   double* part_ao_ = nullptr;
   int gao_ = 0, grid_tao_ = 0;
-  int rb_rows_ = 16, rb_phi_ = 4, tc_ = 16;
+  // row pairs per block of the z-row passes: 8 in FP64 (1024 blocks at 128^3, fewer idle SMs in
+  // the last wave than 512 blocks of 16 pairs: r2c + final 0.126 -> 0.108 ms), 16 in FP32
+  int rb_rows_ = sizeof(T) == 8 ? 8 : 16, rb_phi_ = 4, tc_ = 16;
   size_t smem_rows_ = 0, smem_phi_ = 0, smem_colx_ = 0, smem_coly_ = 0, smem_xconv_ = 0, smem_xback_ = 0;
   // tensor-copy path (cdft_kernels_tma.cuh)
   bool tma_ = false;
