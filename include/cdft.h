@@ -418,9 +418,8 @@ int cdft_ddft_mass_deviation(cdft_ctx* ctx, double* max_rel);
  * counterpart in the reference. Its scratch is a 64 KiB file-scope device array
  * that every GPU loading this library holds until exit; n above 2^25
  * (33,554,432) points is rejected with CDFT_ERR_ARG. The first call on a device
- * resolves the array's address there with cudaGetSymbolAddress (make that first
- * call before any stream capture); it is resolved again if the device's context
- * has been replaced (cudaDeviceReset). Calls share the array: calls that overlap
+ * resolves the array's address there with cudaGetSymbolAddress; it is resolved
+ * again if the device's context has been replaced (cudaDeviceReset). Calls share the array: calls that overlap
  * on the GPU race and must be serialised by the caller. The work runs on
  * `stream` (NULL: the legacy default stream), which is synchronised before
  * returning; the call reads and clears the runtime's last-error state. */
