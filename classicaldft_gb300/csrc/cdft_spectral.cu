@@ -8,7 +8,8 @@
 // Log_Det keeps the reference's estimator exactly: the Chebyshev coefficients of log,
 // the three-term recurrence and Hutchinson's trace with the +-1 vectors that
 // std::mt19937(seed) and uniform_int_distribution<>(0, 1) give, drawn in point order
-// (the host draws sample i + 1 while the device runs sample i's queued products).
+// (on the device, k_mt_probe; with another standard library than libstdc++ 13, the host
+// draws sample i + 1 while the device runs sample i's queued products).
 // Eigenvalues and Arnoldi compute what the reference computes (the smallest eigenvalue of the signed, scaled and
 // rank-one shifted Hessian; the k eigenpairs of H + shift of largest magnitude) with a
 // thick-restart Lanczos iteration, fully re-orthogonalised, instead of nlopt's L-BFGS on
@@ -213,6 +214,63 @@ namespace {
 unsigned sp_grid(long n) { return (unsigned)std::max<long>(1, std::min<long>((n + 255) / 256, 152 * 8)); }
 
 // Device work arrays of one driver call (freed on return).
+// Log_Det's +-1 probes drawn on the device, bit for bit those of the host loop
+//   std::mt19937 rng(seed); std::uniform_int_distribution<> d(0, 1); d(rng) > 0 ? 1 : -1
+// One block keeps the generator's 624-word state in shared memory. A twist updates word i
+// from words i, i + 1 and i + 397 (mod 624) in increasing i, so it runs as three parallel
+// phases (i < 227 reads only old words; 227 <= i < 454 reads the words the first phase made;
+// the rest reads the second phase's, word 623 also the new word 0) into a second copy of the
+// state, and each new word is tempered into one draw. libstdc++ (release 13 here) maps a
+// 32-bit draw to {0, 1} by Lemire's method with range 2, which is its top bit. The state
+// and the position of the next unused word live in gst (625 words) between calls, as in
+// the engine object.
+__device__ __forceinline__ unsigned mt_next_word(unsigned xi, unsigned xi1, unsigned xm) {
+  const unsigned y = (xi & 0x80000000u) | (xi1 & 0x7fffffffu);
+  return xm ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+}
+__device__ __forceinline__ double mt_sign(unsigned y) {
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return (y >> 31) ? 1.0 : -1.0;
+}
+__global__ void __launch_bounds__(256) k_mt_probe(unsigned* __restrict__ gst, double* __restrict__ out, long N) {
+  __shared__ unsigned xs[2][624];
+  const int t = threadIdx.x;
+  for (int i = t; i < 624; i += 256) xs[0][i] = gst[i];
+  int pos = (int)gst[624];
+  __syncthreads();
+  int cur = 0;
+  long p = min((long)(624 - pos), N);  // the words left from the previous call
+  for (int i = t; i < p; i += 256) out[i] = mt_sign(xs[0][pos + i]);
+  pos += (int)p;
+  while (p < N) {
+    const unsigned* o = xs[cur];
+    unsigned* n = xs[cur ^ 1];
+    if (t < 227) n[t] = mt_next_word(o[t], o[t + 1], o[t + 397]);
+    __syncthreads();
+    if (t < 227) n[t + 227] = mt_next_word(o[t + 227], o[t + 228], n[t]);
+    __syncthreads();
+    if (t < 169) n[t + 454] = mt_next_word(o[t + 454], o[t + 455], n[t + 227]);
+    else if (t == 169) n[623] = mt_next_word(o[623], n[0], n[396]);
+    __syncthreads();  // n complete; o is read no more, so the next twist may overwrite it
+    cur ^= 1;
+    const long cnt = min(624L, N - p);
+    for (int i = t; i < cnt; i += 256) out[p + i] = mt_sign(n[i]);
+    p += cnt;
+    pos = (int)cnt;
+  }
+  __syncthreads();
+  for (int i = t; i < 624; i += 256) gst[i] = xs[cur][i];
+  if (t == 0) gst[624] = (unsigned)pos;
+}
+#if defined(_GLIBCXX_RELEASE) && _GLIBCXX_RELEASE >= 13
+constexpr bool kDeviceProbes = true;
+#else
+constexpr bool kDeviceProbes = false;  // another standard library's distribution: draw on the host
+#endif
+
 struct DevBuf {
   std::vector<void*> ptrs;
   ~DevBuf() {
@@ -336,7 +394,19 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
       for (long p = 0; p < N; ++p)
         if (cdft_on_boundary(p, ny, nz)) h[p] = 0.0;
   };
-  draw(hv[0]);
+  unsigned* mt = nullptr;  // the device generator's state (kDeviceProbes)
+  if (kDeviceProbes) {
+    mt = reinterpret_cast<unsigned*>(buf.get(313));  // 625 words
+    if (!mt) return cdft_internal_fail(c, CDFT_ERR_CUDA, "log_det: out of device memory");
+    std::vector<unsigned> x(625);  // std::mt19937's seeding; its first draw twists
+    x[0] = (unsigned)(unsigned long)seed;
+    for (int i = 1; i < 624; ++i) x[i] = 1812433253u * (x[i - 1] ^ (x[i - 1] >> 30)) + (unsigned)i;
+    x[624] = 624;
+    SP_CK(c, cudaMemcpyAsync(mt, x.data(), 625 * sizeof(unsigned), cudaMemcpyHostToDevice, s));
+    SP_CK(c, cudaStreamSynchronize(s));
+  } else {
+    draw(hv[0]);
+  }
   const unsigned g = sp_grid(N);
   bool prepared = false;
   auto matvec = [&](const double* x, double* y) -> int {
@@ -350,7 +420,12 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
   };
   for (int i = 0; i < num_samples; ++i) {
     const int cur = i & 1;
-    SP_CK(c, cudaMemcpyAsync(v, hv[cur], N * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (kDeviceProbes) {
+      k_mt_probe<<<1, 256, 0, s>>>(mt, v, N);
+      if (c->fixed_bg) cdft_internal_boundary_set(c, v, 0.0);  // Log_Det::set_boundary_points_to_zero
+    } else {
+      SP_CK(c, cudaMemcpyAsync(v, hv[cur], N * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
     SP_CK(c, cudaEventRecord(copied[cur], s));
     int rc = matvec(v, r);
     if (rc) return rc;
@@ -367,7 +442,7 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
     }
     dots(v, 1, u, N, part, scal + 2 + i, s);
     SP_CK(c, cudaGetLastError());
-    if (i + 1 < num_samples) {  // with this sample's products queued, draw the next probe into the other pinned buffer
+    if (!kDeviceProbes && i + 1 < num_samples) {  // with this sample's products queued, draw the next probe into the other pinned buffer
       SP_CK(c, cudaEventSynchronize(copied[cur ^ 1]));  // (once the copy that last read it is done)
       draw(hv[cur ^ 1]);
     }
