@@ -76,6 +76,28 @@ def test_ao_bulk_limit(cd, shape, prec):
     c.close()
 
 
+def test_ao_fp64_128_point_y_axis_matches_the_transposed_lattice(cd, oracle):
+    """FP64 with AO keeps FP64 spectra between passes, so a 128-point y axis runs the
+    double-float y transform that joins to doubles, including its partial last column
+    tile; the lattice with x and y exchanged (32-point y axis, runtime plan) gives the same
+    Omega and the transposed dF. The reference's lattice weights themselves depend on the
+    axis order at ~3e-9 of max|dF| (the oracle shows the same difference between these two
+    lattices without AO), hence the dF bar."""
+    dx = 0.1
+    rho = oracle.fill_noise((32, 128, 128), 0.3, 0.1, 11)
+    out = []
+    for shape, r in (((32, 128, 128), rho), ((128, 32, 128), np.ascontiguousarray(rho.transpose(1, 0, 2)))):
+        c = cd.Context(shape, dx, cd.WHITEBEAR_I, hsd=1.0, ao_rp=RP, ao_reservoir=RES, precision=cd.FP64)
+        c.set_chem_potential(c.bulk(0.25)["mu"])
+        c.set_density(r)
+        out.append(c.eval())
+        c.close()
+    (t0, d0), (t1, d1) = out
+    for k in ("Omega", "F_id", "F_hs"):
+        assert abs(t0[k] - t1[k]) <= 1e-12 * max(1.0, abs(t1[k])), (k, t0[k], t1[k])
+    np.testing.assert_allclose(d0, d1.transpose(1, 0, 2), rtol=0, atol=2e-8 * np.abs(d1).max())
+
+
 @pytest.mark.parametrize("model", ["Rosenfeld", "WhiteBearI"])
 @pytest.mark.parametrize("prec", ["FP64", "FP32"])
 def test_ao_hessian_product_matches_reference(cd, model, prec):
