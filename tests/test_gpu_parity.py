@@ -150,6 +150,26 @@ def test_double_float_path_models_vs_oracle(cd, oracle, model, lj):
     c.close()
 
 
+@pytest.mark.parametrize("shape", [(32, 128, 128), (128, 48, 128), (128, 128, 32)])
+def test_mixed_plan_lattices_vs_oracle(cd, oracle, shape):
+    """Lattices mixing a runtime-plan axis with 128-point axes (double-float transforms on
+    those, FP64 spectra between passes): FP64 at the reference bars against the oracle."""
+    dx = 0.1
+    rho = oracle.fill_noise(shape, 0.3, 0.1, 11)
+    o = oracle.Oracle(shape, dx, "WhiteBearI", hsd=1.0)
+    c = cd.Context(shape, dx, cd.WHITEBEAR_I, hsd=1.0)
+    mu = c.bulk(0.25)["mu"]
+    c.set_chem_potential(mu)
+    o.set_mu(mu)
+    c.set_density(rho)
+    terms, dF = c.eval()
+    st, t, dFo, _ = o.eval(rho)
+    for k in ("Omega", "F_id", "F_hs"):
+        assert abs(terms[k] - t[k]) <= 1e-12 * max(1.0, abs(t[k])), (k, terms[k], t[k])
+    np.testing.assert_allclose(dF, dFo, rtol=0, atol=dF_tol(dx))
+    c.close()
+
+
 def test_double_float_path_only_fex_and_external_field(cd, oracle):
     """The double-float final pass (ln rho, dF and the sums in df64) without the ideal gas and
     with an external field, at 128^3 FP64: the differences are ln(rho) dV and V dV."""
