@@ -147,8 +147,10 @@ __device__ __forceinline__ void tile_butterfly_df(const void* __restrict__ xv, v
     if constexpr (OUT_D) {
       reinterpret_cast<double2*>(yv)[idx] = dfc_join(v);  // hi + lo rounded once, normalised or not
     } else {
-      v.x = df_renorm(v.x);
-      v.y = df_renorm(v.y);
+      if constexpr (UNIT) {  // the last stage: what leaves the transform is renormalised
+        v.x = df_renorm(v.x);
+        v.y = df_renorm(v.y);
+      }
       reinterpret_cast<dfc*>(yv)[idx] = v;
     }
   }
