@@ -73,10 +73,10 @@ __device__ __forceinline__ dfs& operator*=(dfs& a, dfs b) { return a = a * b; }
 // twiddle product forms each component as one two-term dot product (16 instead of 25),
 // and the values a transform leaves are renormalised once (df_renorm), while its inner
 // stages pass unnormalised pairs on. In a float32 emulation of the 128- and 256-point
-// transforms (random, near-constant and DC-dominated inputs) the normwise error stays
-// within 3.6x of that of the renormalising operations above (worst 5.8e-14 against
-// 1.6e-14); a transform's first stage is given normalised pairs (unnormalised weight
-// products there raised the evaluation's Omega error tenfold).
+// transforms (tests/cpp/df64_fft_emulation.cpp: random, near-constant and DC-dominated
+// inputs) the normwise error stays within 3x of that of the renormalising operations above
+// (worst 4.7e-14 against 1.6e-14); a transform's first stage is given normalised pairs
+// (unnormalised weight products there raised the evaluation's Omega error tenfold).
 __device__ __forceinline__ dfs dfl_add(dfs a, dfs b) {
   const dfs s = df_two_sum(a.h, b.h);
   return dfs(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
