@@ -134,7 +134,8 @@ __device__ __forceinline__ dfs operator/(dfs a, dfs b) { return a * df_rcp(b); }
 // log(1 + x) = k ln2 + log F + log1p(r), |r| <= 2^-8, where log1p(r) = r - r^2/2 + r^3/3
 // + r^4 q(r) takes its first three terms in df64 and q (a cubic) in FP32. Near x = 0 the
 // reduction is skipped (k = 0, F = 1), so the result keeps its relative accuracy there.
-// Relative error ~1e-14 (against ~1e-16 in FP64), far inside the evaluation's 1e-12.
+// Relative error ~1.3e-14 (against ~1e-16 in FP64; a float32 emulation of these operations,
+// tests/cpp/df64_log_emulation.cpp), far inside the evaluation's 1e-12.
 // The table (log F and 1/F as df64, from 50-digit decimal arithmetic: cdft_df_log_table.h)
 // is read from shared memory: a kernel calls df_log_table_init once, which copies it there
 // from global memory, and synchronises before the first logarithm.

@@ -1,4 +1,4 @@
-"""The double-float transforms' error bound, on the CPU: tests/cpp/df64_fft_emulation.cpp
+"""The double-float arithmetic's error bounds, on the CPU: tests/cpp/df64_fft_emulation.cpp
 restates in float32 the 128- and 256-point transforms of the FP64 evaluation, once with the
 renormalising double-word operations and once as the device computes them (sums without the
 closing FastTwoSum, fused two-term twiddle products, renormalisation only where values leave
@@ -28,3 +28,20 @@ def test_lazy_double_float_transforms_stay_normwise(tmp_path):
         assert err_r < 3e-14, (n, kind, direction, err_r)
         assert err_l < 1e-13, (n, kind, direction, err_l)
         assert err_l < 4 * err_r, (n, kind, direction, err_r, err_l)
+
+
+def test_double_float_logarithm_and_reciprocal(tmp_path):
+    """tests/cpp/df64_log_emulation.cpp restates df_log1p, df_log and df_rcp operation for
+    operation, with the generated table, over 200,000 arguments of each (eta-like, tiny,
+    around the reduction threshold; densities from 1e-30 to 1e25; reciprocals of both
+    signs from 1e-20 to 1e20): relative errors at the 2^-48 level."""
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    exe = str(tmp_path / "df64_log_emulation")
+    src = os.path.join(ROOT, "tests", "cpp", "df64_log_emulation.cpp")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I",
+                           os.path.join(ROOT, "classicaldft_gb300", "csrc"), src, "-o", exe])
+    e_log1p, e_log, e_rcp = (float(v) for v in subprocess.check_output([exe], text=True).split())
+    assert e_log1p < 2e-14, e_log1p
+    assert e_log < 1.5e-14, e_log
+    assert e_rcp < 1e-14, e_rcp
