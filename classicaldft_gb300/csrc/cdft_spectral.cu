@@ -8,8 +8,9 @@
 // Log_Det keeps the reference's estimator exactly: the Chebyshev coefficients of log,
 // the three-term recurrence and Hutchinson's trace with the +-1 vectors that
 // std::mt19937(seed) and uniform_int_distribution<>(0, 1) give, drawn in point order
-// (on the device, k_mt_probe; with another standard library than libstdc++ 13, the host
-// draws sample i + 1 while the device runs sample i's queued products).
+// (on the device, k_mt_probe, sample i + 1's on a side stream while sample i's products
+// run; with another standard library than libstdc++ 13, the host draws sample i + 1 while
+// the device runs sample i's queued products).
 // Eigenvalues and Arnoldi compute what the reference computes (the smallest eigenvalue of the signed, scaled and
 // rank-one shifted Hessian; the k eigenpairs of H + shift of largest magnitude) with a
 // thick-restart Lanczos iteration, fully re-orthogonalised, instead of nlopt's L-BFGS on
@@ -395,6 +396,19 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
         if (cdft_on_boundary(p, ny, nz)) h[p] = 0.0;
   };
   unsigned* mt = nullptr;  // the device generator's state (kDeviceProbes)
+  // Device probes: sample i's probe is in pb[i & 1]; probe i + 1 is drawn on a side stream
+  // (one block) while sample i's products run, after probe i (the generator's state is
+  // sequential) and after sample i - 1 has stopped reading the buffer it overwrites.
+  double* pb[2] = {v, nullptr};
+  struct Side {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ready = nullptr, freed = nullptr;
+    ~Side() {
+      if (ready) cudaEventDestroy(ready);
+      if (freed) cudaEventDestroy(freed);
+      if (st) cudaStreamDestroy(st);
+    }
+  } side;
   if (kDeviceProbes) {
     mt = reinterpret_cast<unsigned*>(buf.get(313));  // 625 words
     if (!mt) return cdft_internal_fail(c, CDFT_ERR_CUDA, "log_det: out of device memory");
@@ -404,6 +418,15 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
     x[624] = 624;
     SP_CK(c, cudaMemcpyAsync(mt, x.data(), 625 * sizeof(unsigned), cudaMemcpyHostToDevice, s));
     SP_CK(c, cudaStreamSynchronize(s));
+    if (num_samples > 1) {
+      pb[1] = buf.get(N);
+      if (!pb[1]) return cdft_internal_fail(c, CDFT_ERR_CUDA, "log_det: out of device memory");
+      SP_CK(c, cudaStreamCreateWithFlags(&side.st, cudaStreamNonBlocking));
+      SP_CK(c, cudaEventCreateWithFlags(&side.ready, cudaEventDisableTiming));
+      SP_CK(c, cudaEventCreateWithFlags(&side.freed, cudaEventDisableTiming));
+    }
+    k_mt_probe<<<1, 256, 0, s>>>(mt, pb[0], N);
+    if (num_samples > 1) SP_CK(c, cudaEventRecord(side.freed, s));  // the side stream's first draw follows probe 0
   } else {
     draw(hv[0]);
   }
@@ -420,8 +443,14 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
   };
   for (int i = 0; i < num_samples; ++i) {
     const int cur = i & 1;
+    double* const v = kDeviceProbes ? pb[cur] : pb[0];  // this sample's probe
     if (kDeviceProbes) {
-      k_mt_probe<<<1, 256, 0, s>>>(mt, v, N);
+      if (i > 0) SP_CK(c, cudaStreamWaitEvent(s, side.ready, 0));  // probe i drawn
+      if (i + 1 < num_samples) {
+        SP_CK(c, cudaStreamWaitEvent(side.st, side.freed, 0));
+        k_mt_probe<<<1, 256, 0, side.st>>>(mt, pb[cur ^ 1], N);
+        SP_CK(c, cudaEventRecord(side.ready, side.st));
+      }
       if (c->fixed_bg) cdft_internal_boundary_set(c, v, 0.0);  // Log_Det::set_boundary_points_to_zero
     } else {
       SP_CK(c, cudaMemcpyAsync(v, hv[cur], N * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -442,6 +471,7 @@ int cdft_log_det(cdft_ctx* c, int matrix, int order, double lam_max, double lam_
     }
     dots(v, 1, u, N, part, scal + 2 + i, s);
     SP_CK(c, cudaGetLastError());
+    if (kDeviceProbes && i + 2 < num_samples) SP_CK(c, cudaEventRecord(side.freed, s));  // probe i + 2 may now overwrite v
     if (!kDeviceProbes && i + 1 < num_samples) {  // with this sample's products queued, draw the next probe into the other pinned buffer
       SP_CK(c, cudaEventSynchronize(copied[cur ^ 1]));  // (once the copy that last read it is done)
       draw(hv[cur ^ 1]);
