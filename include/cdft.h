@@ -38,11 +38,12 @@ extern "C" {
 #define CDFT_WHITEBEAR_II 4
 
 /* Arithmetic of the bulk FFT / pointwise passes. Reductions are FP64 always.
- * CDFT_FP64 is the reference's precision: on 128- and 256-point axes its transforms and
- * per-point terms run in double-float (float pairs, 48 significant bits) on the FP32
- * pipe, which keeps Omega within ~1e-14 relative and dF within ~2e-16 absolute of an
- * all-FP64 evaluation at 128^3 (the parity bars are 1e-12 and 1e-10 dV); other axis
- * lengths run FP64 throughout. CDFT_FP32 runs the transforms and the pointwise terms in
+ * CDFT_FP64 is the reference's precision: its transforms along 128- and 256-point axes
+ * run in double-float (float pairs, 48 significant bits) on the FP32 pipe, and when all
+ * three axes have those lengths so do the per-point terms and the spectra between passes;
+ * at 128^3 Omega stays within ~1e-14 relative and dF within ~2e-16 absolute of an
+ * all-FP64 evaluation (the parity bars are 1e-12 and 1e-10 dV). Transforms along other
+ * axis lengths run in FP64. CDFT_FP32 runs the transforms and the pointwise terms in
  * FP32 (Omega ~2.5e-7 relative, dF ~5e-7 of max|dF| from FP64). */
 #define CDFT_FP64 0
 #define CDFT_FP32 1
